@@ -1,0 +1,358 @@
+"""bemuse_gb300 -- GB300-native frequency-domain panel-method solver.
+
+Python mirror of the reference's hydrodynamic solver interface (ZeppSav/BEMUse,
+src/Solver/Hydrodynamic_Solver.h:35-160 behind src/Solver/Solver_Base.h:39-153)
+over the C ABI in include/bemgpu.h.  All computation happens in
+bemuse_gb300/_lib/libbemgpu.so (hand-written sm_103a kernels); this module only
+marshals arguments.  There is no CPU fallback: importing works without the
+library, but every call that needs it raises if it is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "BEMError", "lib", "Parameter", "Mesh", "Half_Cylinder", "Barge", "unify",
+    "Hydrodynamic_Radiation_Solver", "havelock_gf", "dense_solve", "PLAIN_FP64", "MIXED",
+]
+
+PLAIN_FP64 = 0
+MIXED = 1
+
+_STATUS = {0: "BEM_OK", 1: "BEM_ERR_ARG", 2: "BEM_ERR_CUDA", 3: "BEM_ERR_STATE", 4: "BEM_ERR_NUMERIC",
+           5: "BEM_ERR_NOMEM", 6: "BEM_ERR_UNSUPPORTED"}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class BEMError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_STATUS.get(status, str(status)), msg))
+        self.status = status
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_int), ("nodes", _dp), ("n_elems", ctypes.c_int), ("elems", _ip),
+                ("n_comp", ctypes.c_int), ("comp_first", _ip), ("comp_origin", _dp)]
+
+
+class _Props(ctypes.Structure):
+    _fields_ = [("mass", ctypes.c_double), ("cog", ctypes.c_double * 3), ("gyration", ctypes.c_double * 9),
+                ("mass_matrix", _dp), ("stiffness", _dp), ("aux", ctypes.POINTER(_Mesh))]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("A", _dp), ("B", _dp), ("FK", _dp), ("SC", _dp), ("F", _dp), ("RAO", _dp),
+                ("refine_iters", _ip), ("residual", _dp), ("phi_rad", _dp), ("phi_scat", _dp)]
+
+
+_LIB = None
+
+
+def lib():
+    """Load libbemgpu.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise BEMError(6, "native library %s is missing; run bemuse_gb300.build.build()" % path)
+    L = ctypes.CDLL(path)
+    c_int, c_double, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    sig = {
+        "bem_version": ([], ctypes.c_char_p),
+        "bem_last_error": ([vp], ctypes.c_char_p),
+        "bem_mesh_cylinder_sizes": ([c_int] * 4 + [_ip] * 4, c_int),
+        "bem_mesh_cylinder": ([c_double, c_double, c_int, c_int, c_int, c_int, c_int, _dp, _ip, _dp, _ip], c_int),
+        "bem_mesh_barge_sizes": ([c_int] * 3 + [_ip] * 4, c_int),
+        "bem_mesh_barge": ([c_double] * 3 + [c_int] * 4 + [_dp, _ip, _dp, _ip], c_int),
+        "bem_create": ([ctypes.POINTER(vp), c_int], c_int),
+        "bem_destroy": ([vp], None),
+        "bem_set_params": ([vp, c_double, c_double, c_int, _dp], c_int),
+        "bem_setup": ([vp, ctypes.POINTER(_Mesh), ctypes.POINTER(_Props)], c_int),
+        "bem_solve": ([vp, c_int, _dp, c_int, c_double, ctypes.POINTER(_Result)], c_int),
+        "bem_get_sizes": ([vp, _ip, _ip], c_int),
+        "bem_get_body_matrices": ([vp, _dp, _dp, _dp], c_int),
+        "bem_get_rankine": ([vp, _dp, _dp, _dp, _dp], c_int),
+        "bem_wave_matrices": ([vp, c_double, c_int, _dp, _dp], c_int),
+        "bem_havelock": ([c_int, c_int, _dp, _dp, _dp, c_int, _dp], c_int),
+        "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
+        "bem_stage_times": ([vp, _dp, c_int], c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _LIB = L
+    return L
+
+
+def _p(a, t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _check(st, ctx=None):
+    if st != 0:
+        msg = lib().bem_last_error(ctx)
+        raise BEMError(st, msg.decode() if msg else "")
+
+
+class Parameter(tuple):
+    """(name, value) pair as in Boundary_Base.h:47-55."""
+
+    def __new__(cls, name, value):
+        return super().__new__(cls, (name, value))
+
+
+class Mesh:
+    """Panel mesh: component-local nodes (n x 3), elements (m x 4, -1 = triangle),
+    components (element ranges + translation origins) and an optional interior
+    waterplane ('aux') mesh for hydrostatics."""
+
+    def __init__(self, nodes, elems, comp_first=None, comp_origin=None, aux=None):
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        self.elems = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1, 4)
+        if comp_first is None:
+            comp_first, comp_origin = [0, self.elems.shape[0]], [[0.0, 0.0, 0.0]]
+        self.comp_first = np.ascontiguousarray(comp_first, dtype=np.int32)
+        self.comp_origin = np.ascontiguousarray(comp_origin, dtype=np.float64).reshape(-1, 3)
+        self.aux = aux
+
+    @property
+    def n(self):
+        return self.elems.shape[0]
+
+    def _struct(self):
+        return _Mesh(self.nodes.shape[0], _p(self.nodes), self.elems.shape[0], _p(self.elems, _ip),
+                     self.comp_first.shape[0] - 1, _p(self.comp_first, _ip), _p(self.comp_origin))
+
+
+def _cylinder_arrays(R, draft, NA, NR, NV, NRFS, cosine):
+    L = lib()
+    nn, ne, nna, nea = (ctypes.c_int() for _ in range(4))
+    _check(L.bem_mesh_cylinder_sizes(NA, NR, NV, NRFS, nn, ne, nna, nea))
+    nodes = np.zeros((nn.value, 3))
+    elems = np.zeros((ne.value, 4), np.int32)
+    an = np.zeros((max(nna.value, 1), 3))
+    ae = np.zeros((max(nea.value, 1), 4), np.int32)
+    _check(L.bem_mesh_cylinder(R, draft, NA, NR, NV, NRFS, int(cosine), _p(nodes), _p(elems, _ip), _p(an),
+                               _p(ae, _ip)))
+    aux = Mesh(an[:nna.value], ae[:nea.value]) if NRFS > 0 else None
+    return nodes, elems, aux
+
+
+def Half_Cylinder(Radius, Draft, NPanels_Azimuthal, NPanels_Radial, NPanels_Vertical,
+                  NPanels_FreeSurface_Int_Radial=0, Cosine_Disc=True):
+    """Half_Cylinder (Volume_of_Revolution.cpp:167-199); parameter names as the
+    reference's Set_Parameters keys."""
+    nodes, elems, aux = _cylinder_arrays(Radius, Draft, NPanels_Azimuthal, NPanels_Radial, NPanels_Vertical,
+                                         NPanels_FreeSurface_Int_Radial, Cosine_Disc)
+    return Mesh(nodes, elems, aux=aux)
+
+
+def Barge(Tank_Length, Tank_Width, Tank_Depth, NPanels_Tank_Length, NPanels_Tank_Width, NPanels_Tank_Depth,
+          Cosine_Disc=True):
+    """Barge (Barge.cpp:12-204)."""
+    L = lib()
+    nn, ne, nna, nea = (ctypes.c_int() for _ in range(4))
+    _check(L.bem_mesh_barge_sizes(NPanels_Tank_Length, NPanels_Tank_Width, NPanels_Tank_Depth, nn, ne, nna, nea))
+    nodes = np.zeros((nn.value, 3))
+    elems = np.zeros((ne.value, 4), np.int32)
+    an = np.zeros((nna.value, 3))
+    ae = np.zeros((nea.value, 4), np.int32)
+    _check(L.bem_mesh_barge(Tank_Length, Tank_Width, Tank_Depth, NPanels_Tank_Length, NPanels_Tank_Width,
+                            NPanels_Tank_Depth, int(Cosine_Disc), _p(nodes), _p(elems, _ip), _p(an), _p(ae, _ip)))
+    return Mesh(nodes, elems, aux=Mesh(an, ae))
+
+
+def unify(meshes, origins):
+    """Several component meshes in translated frames as one system
+    (Triple_Spar::Unify_Geometries, Triple_Spar.cpp:120-166)."""
+    nodes, elems, first, org, an, ae, afirst = [], [], [0], [], [], [], [0]
+    off = aoff = 0
+    for m, o in zip(meshes, origins):
+        nodes.append(m.nodes)
+        e = m.elems.copy()
+        e[e >= 0] += off
+        elems.append(e)
+        off += m.nodes.shape[0]
+        first.append(first[-1] + m.n)
+        org.append(o)
+        if m.aux is not None:
+            an.append(m.aux.nodes)
+            a = m.aux.elems.copy()
+            a[a >= 0] += aoff
+            ae.append(a)
+            aoff += m.aux.nodes.shape[0]
+            afirst.append(afirst[-1] + m.aux.n)
+    aux = None
+    if an and len(an) == len(meshes):
+        aux = Mesh(np.concatenate(an), np.concatenate(ae), afirst, org)
+    return Mesh(np.concatenate(nodes), np.concatenate(elems), first, org, aux=aux)
+
+
+class Hydrodynamic_Radiation_Solver:
+    """Drop-in for BEMUse::Hydrodynamic_Radiation_Solver (Hydrodynamic_Solver.h:35-160).
+
+    Set_Parameters([...Parameter...]) -> Setup(mesh) -> Set_Real(Frequency) -> Solve().
+    As in the reference, Solve() uses Omega = Frequency / (2 pi)
+    (Hydrodynamic_Solver.cpp:405).  Results: A_ij, B_ij, FK_i, SC_i, F_i, RAO_i
+    (Hydrodynamic_Solver.h:55-62) and RadSolArray / DiffSolArray
+    (Solver_Base.h:148-151).  solve_omegas() runs a whole frequency list in one
+    call.  precision: PLAIN_FP64 (the reference's arithmetic) or MIXED.
+    """
+
+    def __init__(self, device=0, precision=PLAIN_FP64, refine_tol=1e-12):
+        L = lib()
+        h = ctypes.c_void_p()
+        _check(L.bem_create(ctypes.byref(h), int(device)))
+        self._h = h
+        self.precision = precision
+        self.refine_tol = refine_tol
+        self.Rho = 1025.0
+        self.Grav = 9.81
+        self.BetaArray = []
+        self.Frequency = 0.0
+        self.mass = 0.0
+        self.cog = np.zeros(3)
+        self.gyration = np.zeros((3, 3))
+        self.Mass_Mat = None
+        self.Stiffness_Mat = None
+        self.RadSolArray, self.DiffSolArray = [], []
+        self.N = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().bem_destroy(h)
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    # Set_Parameters (Hydrodynamic_Solver.cpp:11-27)
+    def Set_Parameters(self, params):
+        for name, val in params:
+            if name == "WaveAngle":
+                self.BetaArray.append(float(val))
+            elif name == "Density":
+                self.Rho = float(val)
+            elif name == "Gravity":
+                self.Grav = float(val)
+            elif name == "IFR" and val:
+                raise BEMError(6, "irregular-frequency removal is not implemented")
+        b = np.asarray(self.BetaArray, dtype=np.float64)
+        _check(lib().bem_set_params(self._h, self.Rho, self.Grav, b.size, _p(b) if b.size else None), self._h)
+
+    def Set_Mass_Properties(self, mass=0.0, cog=(0, 0, 0), gyration=None, Mass_Mat=None, Stiffness_Mat=None):
+        self.mass = float(mass)
+        self.cog = np.asarray(cog, dtype=np.float64)
+        self.gyration = np.zeros((3, 3)) if gyration is None else np.asarray(gyration, dtype=np.float64)
+        self.Mass_Mat = None if Mass_Mat is None else np.ascontiguousarray(Mass_Mat, dtype=np.float64)
+        self.Stiffness_Mat = None if Stiffness_Mat is None else np.ascontiguousarray(Stiffness_Mat, dtype=np.float64)
+
+    def Setup(self, mesh):
+        self.mesh = mesh
+        ms = mesh._struct()
+        props = _Props()
+        props.mass = self.mass
+        props.cog[:] = list(self.cog)
+        props.gyration[:] = list(self.gyration.ravel())
+        props.mass_matrix = _p(self.Mass_Mat)
+        props.stiffness = _p(self.Stiffness_Mat)
+        aux_s = mesh.aux._struct() if mesh.aux is not None else None
+        props.aux = ctypes.pointer(aux_s) if aux_s is not None else None
+        _check(lib().bem_setup(self._h, ctypes.byref(ms), ctypes.byref(props)), self._h)
+        n, nb = ctypes.c_int(), ctypes.c_int()
+        _check(lib().bem_get_sizes(self._h, n, nb), self._h)
+        self.N, self.NBeta = n.value, nb.value
+        M = np.zeros((6, 6))
+        C = np.zeros((6, 6))
+        vc = np.zeros(4)
+        _check(lib().bem_get_body_matrices(self._h, _p(M), _p(C), _p(vc)), self._h)
+        self.M_ij, self.C_ij = M, C
+        self.Volume, self.Centre_Buoyancy = vc[0], vc[1:]
+
+    def Set_Real(self, D):
+        self.Frequency = float(D)
+
+    def Solve(self):
+        r = self.solve_omegas([self.Frequency * (0.5 / np.pi)], want_phi=True)
+        self.A_ij, self.B_ij = r["A"][0], r["B"][0]
+        self.FK_i, self.SC_i, self.F_i, self.RAO_i = r["FK"][0], r["SC"][0], r["F"][0], r["RAO"][0]
+        self.RadSolArray.append(r["phiJ"])
+        self.DiffSolArray.append(r["phiS"])
+        return r
+
+    def solve_omegas(self, omegas, want_phi=False, precision=None):
+        om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
+        nf, nb, N = om.size, self.NBeta, self.N
+        out = dict(A=np.zeros((nf, 6, 6)), B=np.zeros((nf, 6, 6)), FK=np.zeros((nf, 6, nb), np.complex128),
+                   SC=np.zeros((nf, 6, nb), np.complex128), F=np.zeros((nf, 6, nb), np.complex128),
+                   RAO=np.zeros((nf, 6, nb), np.complex128), iters=np.zeros(nf, np.int32),
+                   residual=np.zeros(nf))
+        res = _Result()
+        res.A, res.B = _p(out["A"]), _p(out["B"])
+        for k in ("FK", "SC", "F", "RAO"):
+            setattr(res, k, _p(out[k].view(np.float64)))
+        res.refine_iters = _p(out["iters"], _ip)
+        res.residual = _p(out["residual"])
+        if want_phi:
+            out["phiJ"] = np.zeros((N, 6), np.complex128)
+            out["phiS"] = np.zeros((N, nb), np.complex128)
+            res.phi_rad = _p(out["phiJ"].view(np.float64))
+            res.phi_scat = _p(out["phiS"].view(np.float64)) if nb else None
+        prec = self.precision if precision is None else precision
+        _check(lib().bem_solve(self._h, nf, _p(om), int(prec), float(self.refine_tol), ctypes.byref(res)), self._h)
+        return out
+
+    # Influence matrices
+    def rankine(self):
+        N = self.N
+        s, sr, d, dr = (np.zeros((N, N)) for _ in range(4))
+        _check(lib().bem_get_rankine(self._h, _p(s), _p(sr), _p(d), _p(dr)), self._h)
+        return s, sr, d, dr
+
+    def wave_matrices(self, K, precision=PLAIN_FP64):
+        N = self.N
+        ws = np.zeros((N, N), np.complex128)
+        wd = np.zeros((N, N), np.complex128)
+        _check(lib().bem_wave_matrices(self._h, float(K), int(precision), _p(ws.view(np.float64)),
+                                       _p(wd.view(np.float64))), self._h)
+        return ws, wd
+
+    def stage_times(self, reset=False):
+        t = np.zeros(6)
+        _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
+        return t
+
+
+def havelock_gf(x, y, v, precision=PLAIN_FP64, device=0):
+    """HavelockGF (Kernels.cpp:342-412) on the GPU; returns n x 4 complex: G, dGx, dGy, dGz."""
+    x, y, v = (np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (x, y, v))
+    out = np.zeros((x.size, 8))
+    _check(lib().bem_havelock(int(device), x.size, _p(x), _p(y), _p(v), int(precision), _p(out)))
+    return out[:, 0::2] + 1j * out[:, 1::2]
+
+
+def dense_solve(A, B, precision=PLAIN_FP64, refine_tol=1e-12, device=0):
+    """Solve A X = B (complex) with the GPU LU; returns (X, refine_iters, residual)."""
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    B = np.array(B, dtype=np.complex128, order="C")
+    squeeze = B.ndim == 1
+    if squeeze:
+        B = B[:, None].copy()
+    L = lib()
+    h = ctypes.c_void_p()
+    _check(L.bem_create(ctypes.byref(h), int(device)))
+    try:
+        it, res = ctypes.c_int(), ctypes.c_double()
+        _check(L.bem_dense_solve(h, A.shape[0], _p(A.view(np.float64)), B.shape[1], _p(B.view(np.float64)),
+                                 int(precision), float(refine_tol), it, res), h)
+    finally:
+        L.bem_destroy(h)
+    return (B[:, 0] if squeeze else B), it.value, res.value

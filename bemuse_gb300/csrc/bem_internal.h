@@ -1,0 +1,81 @@
+// bem_internal.h -- declarations shared by the host runtime and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace bem {
+
+constexpr int RK_STRIDE = 32;   // doubles per Rankine panel record
+constexpr int MAX_RHS = 16;     // 6 radiation + up to 10 headings
+constexpr int MAX_BETA = MAX_RHS - 6;
+constexpr int LD_ALIGN = 128;   // matrix leading dimension / padded order
+
+// Sticky device status bits (one int per context, read back after a solve).
+enum DevFlag : int {
+    FLAG_PIVOT = 1,      // a multiplier |l_ik| > 1: partial pivoting would exchange rows
+    FLAG_ZERO_PIVOT = 2, // a zero (or non-finite) pivot
+    FLAG_NONFINITE = 4,  // non-finite residual
+};
+
+struct WaveArgs {
+    int N, ld, R, mode;   // mode 0: assemble D and S*B; 1: raw ws/wd (N x N interleaved)
+    double K;
+    const double* xr;     // collocation points [3][N]
+    const double* gq;     // mirrored-panel Gauss data [7][4][N]: x, y, z, w, nx, ny, nz
+    const int* nq;        // Gauss points per panel (3 or 4)
+    const double* RD;     // d + dr           [N][ld]
+    const double* RSR;    // -sr * 2 n_z(S)   [N][ld]
+    const double* Bm;     // RHS block B      [N][R] complex interleaved
+    double* Y;            // S * B accumulator [N][R] complex interleaved (+=)
+    double* D64r; double* D64i;   // [ld][ld]
+    float* D32r; float* D32i;     // [ld][ld] or null
+    double* ws_out; double* wd_out;
+};
+
+cudaError_t upload_poly_constants(int device);
+void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
+                    double* o0, double* o1, double* o2, double* o3);
+void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
+void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i);
+void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
+                     const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
+                     double* Bm);
+void launch_rhs_static(cudaStream_t st, int N, int ld, int R, int j0, int j1, const double* RS, const double* Bm,
+                       double* Y);
+void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
+                 const double* phiI, const double* dphiI, double* part, double* out);
+void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,
+                     bool fp32);
+
+// ---- dense LU / solves (k_lu.cu, k_tc_gemm.cu) ------------------------------
+// A planar complex matrix view.
+template <typename T> struct CMat {
+    T* re;
+    T* im;
+    int ld;
+};
+
+struct LUWork;  // opaque workspace (host_api.cpp)
+
+// Blocked LU without row exchanges of the n x n (n % nb == 0) planar matrix;
+// diagonal-block inverses go to inv (re/im, [n/nb][2][nb][nb]: L^-1 then U^-1).
+// tc = true uses the tcgen05 TF32 trailing update (float only).
+void lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
+                   int* flags);
+void lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
+                   float* wut, int* flags, bool tc);
+// Forward/back substitution with the factors: X (n x R, interleaved complex) in place.
+void lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X);
+void lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X);
+// Rres = Y - D X (FP64), and per-column max |Rres| and max |Y| into nrm[2R]
+// (as ordered int bit patterns; zero them first).
+void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
+                     const double* Y, double* Rres, unsigned long long* nrm);
+void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
+void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
+void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
+
+int tc_gemm_supported(int device);
+
+}  // namespace bem

@@ -1,0 +1,207 @@
+// green.cuh -- device forms of the infinite-depth wave Green function.
+//
+// HavelockGF of the reference (src/Kernels.cpp:342-412): the Liang/Wu/Noblesse
+// global approximation of the free-surface term,
+//   G    = L0(d, v, alpha, beta, rho) + 2 pi e^v (H0(h) - i J0(h))
+//   dG/dh = Ls(...)                  + 2 pi e^v ((2/pi - H1(h)) + i J1(h))
+//   dG/dx = dG/dh x/h, dG/dy = dG/dh y/h (0 for h <= 1e-6), dG/dz = G
+// with h = sqrt(x^2+y^2), d = sqrt(h^2+v^2), alpha = -v/d, beta = h/d,
+// rho = d/(1+d).  L0 and Ls use the polynomial fits of Liang, Wu & Noblesse,
+// Appl. Ocean Res. 74 (2018), eq. 14a-c / 16a-c; H0/H1 the Struve fits of
+// Kernels.cpp:35-116.  J0/J1/Y0/Y1 are CUDA's j0/j1/y0/y1 (FP64) and
+// j0f/j1f/y0f/y1f (FP32).
+//
+// gf64: FP64, same operation order as the reference (a common subexpression
+//       e^v is computed once; the reference recomputes the same value).
+// gf32: FP32.  The polynomials have coefficients up to 2e5 with alternating
+//       signs, which cancel badly in FP32 around rho ~ 0.5; gf32 evaluates
+//       each one re-expanded about rho = 1/2 (coefficients from host-side FP64
+//       expansion, held in constant memory), which is the same polynomial.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace bem {
+
+struct cd { double re, im; };
+struct cf { float re, im; };
+
+// Monomial coefficients, ascending powers of rho (Kernels.cpp:120-256).
+#define BEM_POLY_TABLE(X)                                                                                     \
+    X(A, 10, 1.21, -13.328, 215.896, -1763.96, 8418.94, -24314.21, 42002.57, -41592.9, 21859.0, -4838.6)      \
+    X(B, 10, 0.938, 5.737, -67.92, 796.534, -4780.77, 17137.74, -36618.81, 44894.06, -29030.24, 7671.22)      \
+    X(C, 8, 1.268, -9.747, 209.653, -1397.89, 5155.67, -9844.35, 9136.4, -3272.62)                           \
+    X(D, 10, 0.632, -40.97, 667.16, -6072.07, 31127.39, -96293.05, 181856.75, -205690.43, 128170.2, -33744.6) \
+    X(dA, 10, 2.948, -24.53, 249.69, -754.85, -1187.71, 16370.75, -48811.41, 68220.87, -46688.0, 12622.25)    \
+    X(dB, 10, 1.11, 2.894, -76.765, 1565.35, -11336.19, 44270.15, -97014.11, 118879.26, -76209.82, 19923.28)  \
+    X(dC, 6, 14.19, -148.24, 847.8, -2318.58, 3168.35, -1590.27)
+
+// Incremental-power evaluation exactly as the reference writes it:
+// S = c0; t = x; S += c_i t; t *= x.
+__device__ __forceinline__ double poly_inc64(const double* c, int n, double x) {
+    double S = c[0], t = x;
+#pragma unroll
+    for (int i = 1; i < 10; ++i) {
+        if (i < n) { S += c[i] * t; t *= x; }
+    }
+    return S;
+}
+
+struct PolyCoef64 {
+    double A[10], B[10], C[10], D[10], dA[10], dB[10], dC[10];
+};
+
+// Shifted-basis coefficients for FP32: p(rho) = sum_k s_k (rho - 1/2)^k.
+struct PolyCoef32 {
+    float A[10], B[10], C[10], D[10], dA[10], dB[10], dC[10];
+};
+
+__device__ __forceinline__ float horner32(const float* s, int n, float u) {
+    float r = s[n - 1];
+#pragma unroll
+    for (int k = 8; k >= 0; --k)
+        if (k < n - 1) r = fmaf(r, u, s[k]);
+    return r;
+}
+
+// ---- FP64 -----------------------------------------------------------------
+__device__ __forceinline__ double struve_h0_64(double x, double y0x) {
+    if (x <= 3.0) {
+        double yy = (x / 3.0) * (x / 3.0);
+        double s = 1.909859164 + (-1.909855001 + (0.687514637 + (-0.126164557 + (0.013828813 + -0.000876918 * yy) * yy) * yy) * yy) * yy;
+        return s * (x / 3.0);
+    }
+    double yy = (3.0 / x) * (3.0 / x);
+    double c1 = 2.0 * (0.99999906 + (4.77228920 + (3.85542044 + 0.32303607 * yy) * yy) * yy);
+    double c2 = 3.14159265358979323846 * x * (1.0 + (4.88331068 + (4.28957333 + 0.52120508 * yy) * yy) * yy);
+    return c1 / c2 + y0x;
+}
+__device__ __forceinline__ double struve_h1_64(double x, double y1x) {
+    if (x <= 3.0) {
+        double yy = (x / 3.0) * (x / 3.0);
+        return (1.909859286 + (-1.145914713 + (0.294656958 + (-0.042070508 + (0.003785727 + -0.000207183 * yy) * yy) * yy) * yy) * yy) * yy;
+    }
+    double yy = (3.0 / x) * (3.0 / x);
+    double c1 = 2.0 * (1.00000004 + (3.92205313 + (2.64893033 + 0.27450895 * yy) * yy) * yy);
+    double c2 = 3.14159265358979323846 * (1.0 + (3.81095112 + (2.26216956 + 0.10885141 * yy) * yy) * yy);
+    return c1 / c2 + y1x;
+}
+
+// Returns G and dG/dh (complex).  dx, dy only enter through h here.
+__device__ __forceinline__ void gf64(const PolyCoef64& P, double hh, double vv, cd& G, cd& Gh) {
+    const double PI = 3.14159265358979323846;
+    const double EUL = 0.5772156649;
+    double dd = sqrt(hh * hh + vv * vv);
+    double alpha = -vv / dd;
+    double beta = hh / dd;
+    double rho = dd / (1.0 + dd);
+    double ev = exp(vv);
+    double d2 = dd * dd;
+    double d3 = d2 * dd;
+    // GF_Func_L0 (Kernels.cpp:258-282)
+    double PP = log(0.5 * (dd - vv)) + EUL - 2.0 * d2;
+    PP *= ev;
+    PP += d2 - vv;
+    double A = poly_inc64(P.A, 10, rho), B = poly_inc64(P.B, 10, rho);
+    double C = poly_inc64(P.C, 8, rho), D = poly_inc64(P.D, 10, rho);
+    double omr = 1.0 - rho;
+    double RR = (1.0 - beta) * A;
+    RR -= beta * B;
+    RR -= alpha * C / (1.0 + 6.0 * alpha * rho * omr);
+    RR += beta * (1.0 - beta) * D;
+    double r3 = rho * (omr * omr * omr);
+    double L0 = 2.0 * PP / (1.0 + d3) + 2.0 * (r3 * RR);
+    // GF_Func_W (:284-295), GF_Func_Wh (:327-338)
+    bool far = hh > 3.0;
+    double j0v = j0(hh), j1v = j1(hh);
+    double y0v = far ? y0(hh) : 0.0, y1v = far ? y1(hh) : 0.0;
+    double H0 = struve_h0_64(hh, y0v), H1 = struve_h1_64(hh, y1v);
+    double E = 2.0 * PI * ev;
+    G.re = L0 + E * H0;
+    G.im = -E * j0v;
+    // GF_Func_Ls (:297-325)
+    double PS = (beta + hh) / (dd - vv);
+    PS -= 2.0 * beta;
+    PS += 2.0 * dd * ev;
+    PS -= hh;
+    double QS = exp(-dd) * (1.0 - beta);
+    QS *= 1.0 + dd / (1.0 + d3);
+    double a2 = poly_inc64(P.dA, 10, rho), b2 = poly_inc64(P.dB, 10, rho), c2 = poly_inc64(P.dC, 6, rho);
+    double RS = beta * a2;
+    RS -= (1.0 - alpha) * b2;
+    RS += beta * (1.0 - beta) * rho * (1.0 - 2.0 * rho) * c2;
+    double Ls = 2.0 * PS / (1.0 + d3) - 4.0 * QS + 2.0 * (r3 * RS);
+    Gh.re = Ls + E * (2.0 / PI - H1);
+    Gh.im = E * j1v;
+}
+
+// ---- FP32 -----------------------------------------------------------------
+__device__ __forceinline__ float struve_h0_32(float x, float y0x) {
+    if (x <= 3.0f) {
+        float yy = (x * (1.0f / 3.0f)) * (x * (1.0f / 3.0f));
+        float s = fmaf(fmaf(fmaf(fmaf(fmaf(-0.000876918f, yy, 0.013828813f), yy, -0.126164557f), yy, 0.687514637f), yy, -1.909855001f), yy, 1.909859164f);
+        return s * (x * (1.0f / 3.0f));
+    }
+    float r = 3.0f / x;
+    float yy = r * r;
+    float c1 = 2.0f * fmaf(fmaf(fmaf(0.32303607f, yy, 3.85542044f), yy, 4.77228920f), yy, 0.99999906f);
+    float c2 = 3.14159265f * x * fmaf(fmaf(fmaf(0.52120508f, yy, 4.28957333f), yy, 4.88331068f), yy, 1.0f);
+    return __fdividef(c1, c2) + y0x;
+}
+__device__ __forceinline__ float struve_h1_32(float x, float y1x) {
+    if (x <= 3.0f) {
+        float yy = (x * (1.0f / 3.0f)) * (x * (1.0f / 3.0f));
+        return fmaf(fmaf(fmaf(fmaf(fmaf(-0.000207183f, yy, 0.003785727f), yy, -0.042070508f), yy, 0.294656958f), yy, -1.145914713f), yy, 1.909859286f) * yy;
+    }
+    float r = 3.0f / x;
+    float yy = r * r;
+    float c1 = 2.0f * fmaf(fmaf(fmaf(0.27450895f, yy, 2.64893033f), yy, 3.92205313f), yy, 1.00000004f);
+    float c2 = 3.14159265f * fmaf(fmaf(fmaf(0.10885141f, yy, 2.26216956f), yy, 3.81095112f), yy, 1.0f);
+    return __fdividef(c1, c2) + y1x;
+}
+
+__device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf& G, cf& Gh) {
+    const float PI = 3.14159265358979f;
+    const float EUL = 0.5772156649f;
+    float dd = sqrtf(fmaf(hh, hh, vv * vv));
+    float inv_d = 1.0f / dd;
+    float alpha = -vv * inv_d;
+    float beta = hh * inv_d;
+    float rho = dd / (1.0f + dd);
+    float u = rho - 0.5f;
+    float ev = expf(vv);
+    float d2 = dd * dd;
+    float d3 = d2 * dd;
+    float inv_1d3 = 1.0f / (1.0f + d3);
+    float dmv = dd - vv;
+    float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
+    PP = fmaf(PP, ev, d2 - vv);
+    float A = horner32(P.A, 10, u), B = horner32(P.B, 10, u);
+    float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
+    float omr = 1.0f - rho;
+    float RR = (1.0f - beta) * A - beta * B;
+    RR -= alpha * C / fmaf(6.0f * alpha * rho, omr, 1.0f);
+    RR = fmaf(beta * (1.0f - beta), D, RR);
+    float r3 = rho * (omr * omr * omr);
+    float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
+    bool far = hh > 3.0f;
+    float j0v = j0f(hh), j1v = j1f(hh);
+    float y0v = far ? y0f(hh) : 0.0f, y1v = far ? y1f(hh) : 0.0f;
+    float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
+    float E = 2.0f * PI * ev;
+    G.re = fmaf(E, H0, L0);
+    G.im = -E * j0v;
+    float PS = (beta + hh) / dmv;
+    PS -= 2.0f * beta;
+    PS = fmaf(2.0f * dd, ev, PS);
+    PS -= hh;
+    float QS = expf(-dd) * (1.0f - beta);
+    QS *= 1.0f + dd * inv_1d3;
+    float a2 = horner32(P.dA, 10, u), b2 = horner32(P.dB, 10, u), c2 = horner32(P.dC, 6, u);
+    float RS = beta * a2 - (1.0f - alpha) * b2;
+    RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
+    float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);
+    Gh.re = fmaf(E, 0.636619772f - H1, Ls);
+    Gh.im = E * j1v;
+}
+
+}  // namespace bem

@@ -1,0 +1,695 @@
+// host_api.cpp -- the C ABI (include/bemgpu.h): context, setup, per-frequency
+// pipeline, refinement loop and the 6x6 post algebra.
+//
+// Pipeline of one frequency-solve (Hydrodynamic_Radiation_Solver::Solve,
+// Hydrodynamic_Solver.cpp:400-487), all on the context's stream:
+//   k_incident      phi_I, dphi_I/dn, diffraction RHS columns      (:444, :575-596)
+//   k_rhs_static    (Ssrc + Srefl) * B_diff                        (:437, :445)
+//   k_wave          D = Drankine + Dwave and Y += (-ws) * B        (:413-429)
+//   LU              FP64 (plain) or TF32 tensor-core (mixed)       (:430)
+//   solve / refine  FP64 residual against the FP64 operator        (:438, :446)
+//   k_post          hull integrals                                (:462-476)
+//   host            A, B, FK, SC, F, RAO                           (:463-487)
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bemgpu.h"
+#include "bem_internal.h"
+#include "host_geom.h"
+
+using bem::CMat;
+using cplx = std::complex<double>;
+
+struct bem_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+    double rho = 1025.0, grav = 9.81;
+    std::vector<double> betas;
+    bool ready = false;
+    int N = 0, Np = 0, NB = 0, R = 6;
+    std::vector<double> cen, nrm, area, Nk;  // host copies
+    double M[36], C[36], volcob[4];
+    // device buffers
+    double *d_rec = nullptr, *d_xr = nullptr, *d_gq = nullptr, *d_rn = nullptr;
+    int* d_nq = nullptr;
+    double *d_cen = nullptr, *d_nrm = nullptr, *d_area = nullptr, *d_Nk = nullptr, *d_betas = nullptr;
+    double *d_RS = nullptr, *d_RD = nullptr, *d_RSR = nullptr;
+    double *d_D64r = nullptr, *d_D64i = nullptr;
+    float *d_D32r = nullptr, *d_D32i = nullptr;
+    double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
+    float* d_X32 = nullptr;
+    double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr;
+    double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
+    float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
+    int* d_flags = nullptr;
+    unsigned long long* d_norms = nullptr;
+    std::vector<void*> allocs;
+    // stage timing (ms) and launch counts
+    cudaEvent_t ev[8] = {};
+    double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+    long long launches = 0;
+};
+
+namespace {
+
+static char g_static_err[512] = "";
+
+bem_status fail(bem_ctx* c, bem_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    else snprintf(g_static_err, sizeof(g_static_err), "%s", msg.c_str());
+    return s;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? BEM_ERR_NOMEM : BEM_ERR_CUDA,      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+template <typename T> bem_status dalloc(bem_ctx* ctx, T** p, size_t count) {
+    if (*p) return BEM_OK;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, BEM_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
+                                            " bytes failed: " + cudaGetErrorString(e));
+    }
+    *p = static_cast<T*>(q);
+    ctx->allocs.push_back(q);
+    return BEM_OK;
+}
+#define DA(ptr, count)                                         \
+    do {                                                       \
+        bem_status s_ = dalloc(ctx, &(ptr), (size_t)(count));  \
+        if (s_ != BEM_OK) return s_;                           \
+    } while (0)
+
+void free_all(bem_ctx* ctx) {
+    for (void* p : ctx->allocs) cudaFree(p);
+    ctx->allocs.clear();
+    double** dp[] = {&ctx->d_rec, &ctx->d_xr, &ctx->d_gq, &ctx->d_rn, &ctx->d_cen, &ctx->d_nrm, &ctx->d_area,
+                     &ctx->d_Nk, &ctx->d_betas, &ctx->d_RS, &ctx->d_RD, &ctx->d_RSR, &ctx->d_D64r, &ctx->d_D64i,
+                     &ctx->d_Bm, &ctx->d_Y, &ctx->d_Ys6, &ctx->d_X, &ctx->d_Rr, &ctx->d_phiI, &ctx->d_dphiI,
+                     &ctx->d_part, &ctx->d_post, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
+    for (auto p : dp) *p = nullptr;
+    float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
+                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32};
+    for (auto p : fp) *p = nullptr;
+    ctx->d_nq = nullptr;
+    ctx->d_flags = nullptr;
+    ctx->d_norms = nullptr;
+    ctx->ready = false;
+}
+
+int round_up(int n, int a) { return (n + a - 1) / a * a; }
+
+bool inv6(const cplx* M, cplx* out) {
+    cplx a[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 12; ++j) a[i][j] = j < 6 ? M[i * 6 + j] : cplx(i == j - 6 ? 1.0 : 0.0, 0.0);
+    for (int k = 0; k < 6; ++k) {
+        int p = k;
+        for (int i = k + 1; i < 6; ++i)
+            if (std::abs(a[i][k]) > std::abs(a[p][k])) p = i;
+        if (std::abs(a[p][k]) == 0.0) return false;
+        if (p != k)
+            for (int j = 0; j < 12; ++j) std::swap(a[k][j], a[p][j]);
+        cplx inv = 1.0 / a[k][k];
+        for (int j = 0; j < 12; ++j) a[k][j] *= inv;
+        for (int i = 0; i < 6; ++i) {
+            if (i == k) continue;
+            cplx f = a[i][k];
+            for (int j = 0; j < 12; ++j) a[i][j] -= f * a[k][j];
+        }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) out[i * 6 + j] = a[i][j + 6];
+    return true;
+}
+
+bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
+    const int nb64 = 64, nb32 = 128;
+    if (!mixed) {
+        DA(ctx->d_inv64r, (size_t)(Np / nb64) * 2 * nb64 * nb64);
+        DA(ctx->d_inv64i, (size_t)(Np / nb64) * 2 * nb64 * nb64);
+        DA(ctx->d_wl64, (size_t)2 * Np * nb64);
+        DA(ctx->d_wu64, (size_t)2 * Np * nb64);
+    } else {
+        DA(ctx->d_D32r, (size_t)Np * Np);
+        DA(ctx->d_D32i, (size_t)Np * Np);
+        DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
+        DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
+        DA(ctx->d_wl32, (size_t)2 * Np * nb32);
+        DA(ctx->d_wu32, (size_t)2 * Np * nb32);
+        DA(ctx->d_wut32, (size_t)2 * Np * nb32);
+        DA(ctx->d_X32, (size_t)4 * Np * R);
+        DA(ctx->d_Rr, (size_t)2 * Np * R);
+    }
+    DA(ctx->d_X, (size_t)4 * Np * R);
+    DA(ctx->d_flags, 1);
+    DA(ctx->d_norms, 2 * bem::MAX_RHS);
+    return BEM_OK;
+}
+
+// Factor + solve.  D64 (planar, ld = Np) holds the operator; Y (N x R, interleaved)
+// the right-hand sides; the solution lands in d_X.  mixed: TF32 LU of the FP32
+// copy + FP64 refinement against D64; plain: FP64 LU of D64 (destroyed).
+bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
+                            double* resid_out, double* t_lu, double* t_solve) {
+    cudaStream_t st = ctx->st;
+    bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
+    if (s != BEM_OK) return s;
+    CK(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), st));
+    const size_t nr2 = (size_t)2 * Np * R;
+    CK(cudaEventRecord(ctx->ev[2], st));
+    int iters = 0;
+    double resid = 0.0;
+    if (!mixed) {
+        CMat<double> A{ctx->d_D64r, ctx->d_D64i, Np};
+        bem::lu_factor_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, ctx->d_wl64, ctx->d_wu64, ctx->d_flags);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[3], st));
+        CK(cudaMemcpyAsync(ctx->d_X, ctx->d_Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
+        bem::launch_pad_rhs(st, N, Np, R, ctx->d_X);
+        bem::lu_solve_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, R, ctx->d_X);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[4], st));
+    } else {
+        CMat<float> A{ctx->d_D32r, ctx->d_D32i, Np};
+        bool tc = bem::tc_gemm_supported(ctx->device) != 0;
+        bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32, ctx->d_wut32,
+                           ctx->d_flags, tc);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[3], st));
+        // x0 = LU^-1 y
+        CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * nr2, st));
+        CK(cudaMemcpyAsync(ctx->d_Rr, ctx->d_Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
+        bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+        std::vector<unsigned long long> hn(2 * R);
+        for (;;) {
+            bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
+            bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32);
+            bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
+            CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+            bem::launch_residual(st, N, Np, ctx->d_D64r, ctx->d_D64i, R, ctx->d_X, ctx->d_Y, ctx->d_Rr, ctx->d_norms);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            ++iters;
+            resid = 0.0;
+            for (int j = 0; j < R; ++j) {
+                double rn, yn;
+                memcpy(&rn, &hn[j], 8);
+                memcpy(&yn, &hn[R + j], 8);
+                double rel = yn > 0 ? rn / yn : rn;
+                resid = std::max(resid, rel);
+            }
+            if (resid <= tol) break;
+            if (iters >= max_iter || !(resid < 1e300)) {
+                if (iters_out) *iters_out = iters;
+                if (resid_out) *resid_out = resid;
+                return fail(ctx, BEM_ERR_NUMERIC, "iterative refinement did not reach the tolerance (residual " +
+                                                      std::to_string(resid) + " after " + std::to_string(iters) +
+                                                      " sweeps)");
+            }
+            bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+        }
+        CK(cudaEventRecord(ctx->ev[4], st));
+    }
+    int hflags = 0;
+    CK(cudaMemcpyAsync(&hflags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+    *t_lu += ms;
+    cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+    *t_solve += ms;
+    if (iters_out) *iters_out = iters;
+    if (resid_out) *resid_out = resid;
+    if (hflags & bem::FLAG_ZERO_PIVOT) return fail(ctx, BEM_ERR_NUMERIC, "zero or non-finite pivot in the LU");
+    if (hflags & bem::FLAG_PIVOT)
+        return fail(ctx, BEM_ERR_NUMERIC,
+                    "a multiplier |l_ik| > 1 occurred: partial pivoting would exchange rows for this matrix");
+    return BEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bem_version(void) { return "bemgpu 0.1 (sm_103a)"; }
+
+const char* bem_last_error(const bem_ctx* ctx) { return ctx ? ctx->err.c_str() : g_static_err; }
+
+int bem_mesh_cylinder_sizes(int na, int nr, int nv, int nrfs, int* nn, int* ne, int* nna, int* nea) {
+    if (na < 3 || nr < 1 || nv < 1 || nrfs < 0 || !nn || !ne || !nna || !nea) return BEM_ERR_ARG;
+    bem::cylinder_sizes(na, nr, nv, nrfs, nn, ne, nna, nea);
+    return BEM_OK;
+}
+int bem_mesh_cylinder(double R, double draft, int na, int nr, int nv, int nrfs, int cosine, double* nodes,
+                      int* elems, double* aux_nodes, int* aux_elems) {
+    if (na < 3 || nr < 1 || nv < 1 || nrfs < 0 || !nodes || !elems || !(R > 0) || !(draft > 0)) return BEM_ERR_ARG;
+    bem::cylinder_mesh(R, draft, na, nr, nv, nrfs, cosine != 0, nodes, elems, aux_nodes, aux_elems);
+    return BEM_OK;
+}
+int bem_mesh_barge_sizes(int nx, int ny, int nz, int* nn, int* ne, int* nna, int* nea) {
+    if (nx < 1 || ny < 1 || nz < 1 || !nn || !ne || !nna || !nea) return BEM_ERR_ARG;
+    bem::barge_sizes(nx, ny, nz, nn, ne, nna, nea);
+    return BEM_OK;
+}
+int bem_mesh_barge(double L, double W, double D, int nx, int ny, int nz, int cosine, double* nodes, int* elems,
+                   double* aux_nodes, int* aux_elems) {
+    if (nx < 1 || ny < 1 || nz < 1 || !nodes || !elems || !(L > 0) || !(W > 0) || !(D > 0)) return BEM_ERR_ARG;
+    bem::barge_mesh(L, W, D, nx, ny, nz, cosine != 0, nodes, elems, aux_nodes, aux_elems);
+    return BEM_OK;
+}
+
+bem_status bem_create(bem_ctx** out, int device) {
+    bem_ctx* ctx = nullptr;
+    if (!out) return fail(nullptr, BEM_ERR_ARG, "bem_create: null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, BEM_ERR_UNSUPPORTED, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= ndev) return fail(nullptr, BEM_ERR_ARG, "bem_create: device index out of range");
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, device);
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(nullptr, BEM_ERR_UNSUPPORTED,
+                    "this build targets sm_103a (GB300); device is sm_" + std::to_string(prop.major) +
+                        std::to_string(prop.minor));
+    ctx = new bem_ctx();
+    ctx->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+    for (auto& ev : ctx->ev) CK(cudaEventCreate(&ev));
+    CK(bem::upload_poly_constants(device));
+    *out = ctx;
+    return BEM_OK;
+}
+
+void bem_destroy(bem_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    free_all(ctx);
+    for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+bem_status bem_set_params(bem_ctx* ctx, double density, double gravity, int n_beta, const double* betas) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (n_beta < 0 || n_beta > bem::MAX_BETA || (n_beta > 0 && !betas))
+        return fail(ctx, BEM_ERR_ARG, "n_beta must be in [0, " + std::to_string(bem::MAX_BETA) + "]");
+    if (!(density > 0) || !(gravity > 0)) return fail(ctx, BEM_ERR_ARG, "density and gravity must be positive");
+    if (ctx->ready && n_beta != ctx->NB)
+        return fail(ctx, BEM_ERR_STATE, "headings must be set before bem_setup (Set_Parameters precedes Setup)");
+    ctx->rho = density;
+    ctx->grav = gravity;
+    ctx->betas.assign(betas, betas + n_beta);
+    return BEM_OK;
+}
+
+bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* props) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!mesh) return fail(ctx, BEM_ERR_ARG, "null mesh");
+    CK(cudaSetDevice(ctx->device));
+    if (mesh->n_comp > 0 && (!mesh->comp_first || !mesh->comp_origin))
+        return fail(ctx, BEM_ERR_ARG, "n_comp > 0 needs comp_first and comp_origin");
+    if (mesh->n_comp > 0 && (mesh->comp_first[0] != 0 || mesh->comp_first[mesh->n_comp] != mesh->n_elems))
+        return fail(ctx, BEM_ERR_ARG, "components must cover the element list");
+    free_all(ctx);
+    bem::MeshView mv{mesh->n_nodes, mesh->nodes, mesh->n_elems, mesh->elems, mesh->n_comp, mesh->comp_first,
+                     mesh->comp_origin};
+    std::vector<bem::PanelGeom> body, mirror;
+    std::string gerr;
+    if (!bem::build_geometry(mv, body, mirror, gerr)) return fail(ctx, BEM_ERR_ARG, "mesh: " + gerr);
+    const int N = mesh->n_elems;
+    const int Np = round_up(N, bem::LD_ALIGN);
+    const int NB = (int)ctx->betas.size();
+    const int R = 6 + NB;
+    ctx->N = N; ctx->Np = Np; ctx->NB = NB; ctx->R = R;
+    // host-side arrays
+    std::vector<double> rec((size_t)2 * N * bem::RK_STRIDE), gq((size_t)7 * 4 * N, 0.0), rn(N), xr;
+    std::vector<int> nq(N);
+    ctx->cen.assign(3 * (size_t)N, 0);
+    ctx->nrm.assign(3 * (size_t)N, 0);
+    ctx->area.assign(N, 0);
+    ctx->Nk.assign(6 * (size_t)N, 0);
+    for (int i = 0; i < N; ++i) {
+        bem::rankine_record(body[i], &rec[(size_t)i * bem::RK_STRIDE]);
+        bem::rankine_record(mirror[i], &rec[((size_t)N + i) * bem::RK_STRIDE]);
+        rn[i] = body[i].e[8] * 2.0;  // ReflNormMat(S) = 2 n_z (Hydrodynamic_Solver.cpp:96-97)
+        nq[i] = mirror[i].nq;
+        for (int q = 0; q < 4; ++q) {
+            const bem::PanelGeom& p = mirror[i];
+            double f[7] = {p.qp[3 * q], p.qp[3 * q + 1], p.qp[3 * q + 2], p.qw[q], p.qn[3 * q], p.qn[3 * q + 1],
+                           p.qn[3 * q + 2]};
+            for (int k = 0; k < 7; ++k) gq[((size_t)k * 4 + q) * N + i] = f[k];
+        }
+        const double* c = body[i].c;
+        const double* n = body[i].e + 6;
+        for (int d = 0; d < 3; ++d) { ctx->cen[(size_t)d * N + i] = c[d]; ctx->nrm[(size_t)d * N + i] = n[d]; }
+        ctx->area[i] = body[i].area;
+        // N_k = [n, c x n] at the centroid (Set_RHS_Mat, :117-138)
+        double* nk = &ctx->Nk[(size_t)i * 6];
+        nk[0] = n[0]; nk[1] = n[1]; nk[2] = n[2];
+        nk[3] = c[1] * n[2] - c[2] * n[1];
+        nk[4] = c[2] * n[0] - c[0] * n[2];
+        nk[5] = c[0] * n[1] - c[1] * n[0];
+    }
+    bem::collocation_points(body, xr);
+    // mass properties
+    double cog[3] = {0, 0, 0}, gyr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, mass = 0;
+    std::vector<bem::PanelGeom> auxb, auxm;
+    const std::vector<bem::PanelGeom>* auxp = nullptr;
+    if (props) {
+        mass = props->mass;
+        memcpy(cog, props->cog, sizeof(cog));
+        memcpy(gyr, props->gyration, sizeof(gyr));
+        if (props->aux && props->aux->n_elems > 0) {
+            bem::MeshView av{props->aux->n_nodes, props->aux->nodes, props->aux->n_elems, props->aux->elems,
+                             props->aux->n_comp, props->aux->comp_first, props->aux->comp_origin};
+            if (!bem::build_geometry(av, auxb, auxm, gerr)) return fail(ctx, BEM_ERR_ARG, "aux mesh: " + gerr);
+            auxp = &auxb;
+        }
+    }
+    bem::mass_and_stiffness(body, auxp, ctx->rho, ctx->grav, mass, cog, gyr, ctx->M, ctx->C, ctx->volcob);
+    if (props && props->mass_matrix) memcpy(ctx->M, props->mass_matrix, sizeof(ctx->M));
+    if (props && props->stiffness) memcpy(ctx->C, props->stiffness, sizeof(ctx->C));
+    // device upload
+    DA(ctx->d_rec, rec.size());
+    DA(ctx->d_gq, gq.size());
+    DA(ctx->d_xr, xr.size());
+    DA(ctx->d_rn, N);
+    DA(ctx->d_nq, N);
+    DA(ctx->d_cen, 3 * (size_t)N);
+    DA(ctx->d_nrm, 3 * (size_t)N);
+    DA(ctx->d_area, N);
+    DA(ctx->d_Nk, 6 * (size_t)N);
+    DA(ctx->d_betas, std::max(NB, 1));
+    DA(ctx->d_RS, (size_t)N * Np);
+    DA(ctx->d_RD, (size_t)N * Np);
+    DA(ctx->d_RSR, (size_t)N * Np);
+    DA(ctx->d_D64r, (size_t)Np * Np);
+    DA(ctx->d_D64i, (size_t)Np * Np);
+    DA(ctx->d_Bm, 2 * (size_t)N * R);
+    DA(ctx->d_Y, 2 * (size_t)N * R);
+    DA(ctx->d_Ys6, 2 * (size_t)N * R);
+    DA(ctx->d_phiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(ctx->d_dphiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(ctx->d_part, 2 * (size_t)((N + 255) / 256) * (36 + 12 * NB));
+    DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
+    cudaStream_t st = ctx->st;
+    CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_gq, gq.data(), gq.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_rn, rn.data(), rn.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_nq, nq.data(), nq.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_cen, ctx->cen.data(), ctx->cen.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_nrm, ctx->nrm.data(), ctx->nrm.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_area, ctx->area.data(), ctx->area.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_Nk, ctx->Nk.data(), ctx->Nk.size() * 8, cudaMemcpyHostToDevice, st));
+    if (NB) CK(cudaMemcpyAsync(ctx->d_betas, ctx->betas.data(), NB * 8, cudaMemcpyHostToDevice, st));
+    // B columns 0..5 = N_k (real), frequency independent
+    std::vector<double> B((size_t)2 * N * R, 0.0);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < 6; ++j) B[2 * ((size_t)i * R + j)] = ctx->Nk[(size_t)i * 6 + j];
+    CK(cudaMemcpyAsync(ctx->d_Bm, B.data(), B.size() * 8, cudaMemcpyHostToDevice, st));
+    // K1: Rankine influence (once per body), then Ys6 = RS * N_k
+    bem::launch_rankine(st, N, Np, ctx->d_rec, ctx->d_xr, ctx->d_rn, 0, ctx->d_RS, ctx->d_RD, ctx->d_RSR, nullptr);
+    CK(cudaGetLastError());
+    bem::launch_rhs_static(st, N, Np, R, 0, 6, ctx->d_RS, ctx->d_Bm, ctx->d_Ys6);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    ctx->ready = true;
+    return BEM_OK;
+}
+
+bem_status bem_get_sizes(const bem_ctx* cctx, int* n, int* nb) {
+    bem_ctx* ctx = const_cast<bem_ctx*>(cctx);
+    if (!ctx || !n || !nb) return fail(ctx, BEM_ERR_ARG, "null argument");
+    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_setup has not run");
+    *n = ctx->N;
+    *nb = ctx->NB;
+    return BEM_OK;
+}
+
+bem_status bem_get_body_matrices(const bem_ctx* cctx, double* M, double* C, double* vc) {
+    bem_ctx* ctx = const_cast<bem_ctx*>(cctx);
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_setup has not run");
+    if (M) memcpy(M, ctx->M, sizeof(ctx->M));
+    if (C) memcpy(C, ctx->C, sizeof(ctx->C));
+    if (vc) memcpy(vc, ctx->volcob, sizeof(ctx->volcob));
+    return BEM_OK;
+}
+
+bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double tol, bem_result* out) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_solve before bem_setup");
+    if (n_freq < 0 || (n_freq > 0 && !omega)) return fail(ctx, BEM_ERR_ARG, "bad frequency list");
+    if (precision != BEM_PLAIN_FP64 && precision != BEM_MIXED) return fail(ctx, BEM_ERR_ARG, "unknown precision mode");
+    for (int f = 0; f < n_freq; ++f)
+        if (!std::isfinite(omega[f])) return fail(ctx, BEM_ERR_ARG, "non-finite frequency");
+    CK(cudaSetDevice(ctx->device));
+    const bool mixed = precision == BEM_MIXED;
+    if (!(tol > 0)) tol = 1e-12;
+    const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R;
+    cudaStream_t st = ctx->st;
+    bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
+    if (s != BEM_OK) return s;
+    const int nout = 36 + 12 * NB;
+    std::vector<double> post(2 * (size_t)nout);
+    for (int f = 0; f < n_freq; ++f) {
+        const double Om = omega[f];
+        const double K = Om * Om / 9.81;  // Kappa uses the global Gravity (Hydrodynamic_Solver.cpp:409)
+        CK(cudaEventRecord(ctx->ev[0], st));
+        bem::launch_incident(st, N, NB, R, ctx->d_betas, K, Om, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_phiI,
+                             ctx->d_dphiI, ctx->d_Bm);
+        // Y[:, 0:6] = RS N_k (precomputed); Y[:, 6:] = RS B_diff
+        CK(cudaMemcpy2DAsync(ctx->d_Y, sizeof(double) * 2 * R, ctx->d_Ys6, sizeof(double) * 2 * R,
+                             sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToDevice, st));
+        if (NB > 0) bem::launch_rhs_static(st, N, Np, R, 6, R, ctx->d_RS, ctx->d_Bm, ctx->d_Y);
+        CK(cudaEventRecord(ctx->ev[1], st));
+        bem::WaveArgs a;
+        memset(&a, 0, sizeof(a));
+        a.N = N; a.ld = Np; a.R = R; a.mode = 0; a.K = K;
+        a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.RD = ctx->d_RD; a.RSR = ctx->d_RSR;
+        a.Bm = ctx->d_Bm; a.Y = ctx->d_Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
+        a.D32r = mixed ? ctx->d_D32r : nullptr; a.D32i = mixed ? ctx->d_D32i : nullptr;
+        bem::launch_wave(st, a, mixed);
+        bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, mixed ? ctx->d_D32r : nullptr,
+                                 mixed ? ctx->d_D32i : nullptr);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[5], st));
+        int iters = 0;
+        double resid = 0;
+        double t_lu = 0, t_sv = 0;
+        s = factor_and_solve(ctx, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
+        if (s != BEM_OK) return s;
+        CK(cudaEventRecord(ctx->ev[6], st));
+        bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, ctx->d_phiI, ctx->d_dphiI, ctx->d_part,
+                         ctx->d_post);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaEventRecord(ctx->ev[7], st));
+        CK(cudaStreamSynchronize(st));
+        float ms;
+        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); ctx->stage_ms[0] += ms;
+        cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[5]); ctx->stage_ms[1] += ms;
+        ctx->stage_ms[2] += t_lu;
+        ctx->stage_ms[3] += t_sv;
+        cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); ctx->stage_ms[4] += ms;
+        ctx->stage_ms[5] += 1;
+        // 6x6 algebra (Hydrodynamic_Solver.cpp:463-487)
+        if (!out) continue;
+        const cplx I(0.0, 1.0);
+        cplx AM[36];
+        for (int i = 0; i < 36; ++i) AM[i] = cplx(post[2 * i], post[2 * i + 1]);
+        if (out->A) for (int i = 0; i < 36; ++i) out->A[36 * (size_t)f + i] = AM[i].real();
+        if (out->B) for (int i = 0; i < 36; ++i) out->B[36 * (size_t)f + i] = AM[i].imag();
+        std::vector<cplx> F(6 * (size_t)NB);
+        for (int i = 0; i < 6; ++i)
+            for (int b = 0; b < NB; ++b) {
+                int u = i * NB + b;
+                cplx F1(post[2 * (36 + u)], post[2 * (36 + u) + 1]);
+                cplx F2(post[2 * (36 + 6 * NB + u)], post[2 * (36 + 6 * NB + u) + 1]);
+                cplx FK = -I * Om * F1, SC = I * Om * F2;
+                cplx Fv = std::conj(FK + SC);
+                if (Om == 0.0) { FK = 0; SC = 0; Fv = 0; }
+                size_t o = 2 * ((size_t)f * 6 * NB + u);
+                if (out->FK) { out->FK[o] = FK.real(); out->FK[o + 1] = FK.imag(); }
+                if (out->SC) { out->SC[o] = SC.real(); out->SC[o + 1] = SC.imag(); }
+                if (out->F) { out->F[o] = Fv.real(); out->F[o + 1] = Fv.imag(); }
+                F[u] = Fv;
+            }
+        if (out->RAO) {
+            // B_ijOm := Omega * B_ij (Hydrodynamic_Solver.h:57 declares it but never sets it)
+            cplx L[36], Li[36];
+            for (int i = 0; i < 36; ++i)
+                L[i] = -Om * Om * (AM[i].real() + ctx->M[i] / 1025.0) + Om * I * (Om * AM[i].imag()) +
+                       ctx->C[i] / 1025.0;
+            bool ok = inv6(L, Li);
+            for (int i = 0; i < 6; ++i)
+                for (int b = 0; b < NB; ++b) {
+                    cplx acc(0, 0);
+                    if (ok) for (int k = 0; k < 6; ++k) acc += Li[i * 6 + k] * F[k * NB + b];
+                    else acc = cplx(NAN, NAN);
+                    size_t o = 2 * ((size_t)f * 6 * NB + i * NB + b);
+                    out->RAO[o] = acc.real();
+                    out->RAO[o + 1] = acc.imag();
+                }
+        }
+        if (out->refine_iters) out->refine_iters[f] = mixed ? iters : 0;
+        if (out->residual) out->residual[f] = resid;
+        if (f == n_freq - 1) {
+            if (out->phi_rad)
+                CK(cudaMemcpy2D(out->phi_rad, sizeof(double) * 2 * 6, ctx->d_X, sizeof(double) * 2 * R,
+                                sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToHost));
+            if (out->phi_scat && NB > 0)
+                CK(cudaMemcpy2D(out->phi_scat, sizeof(double) * 2 * NB, ctx->d_X + 2 * 6, sizeof(double) * 2 * R,
+                                sizeof(double) * 2 * NB, N, cudaMemcpyDeviceToHost));
+        }
+    }
+    return BEM_OK;
+}
+
+bem_status bem_get_rankine(bem_ctx* ctx, double* s, double* sr, double* d, double* dr) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_setup has not run");
+    CK(cudaSetDevice(ctx->device));
+    const int N = ctx->N;
+    double* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(double) * 4 * (size_t)N * N));
+    bem::launch_rankine(ctx->st, N, N, ctx->d_rec, ctx->d_xr, ctx->d_rn, 1, buf, buf + (size_t)N * N,
+                        buf + 2 * (size_t)N * N, buf + 3 * (size_t)N * N);
+    cudaError_t e = cudaGetLastError();
+    double* dst[4] = {s, sr, d, dr};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (dst[k]) e = cudaMemcpyAsync(dst[k], buf + k * (size_t)N * N, sizeof(double) * N * N,
+                                        cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_get_rankine: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, double* wd) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_setup has not run");
+    if (!ws || !wd || !std::isfinite(K) || K < 0) return fail(ctx, BEM_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int N = ctx->N;
+    double* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(double) * 4 * (size_t)N * N));
+    bem::WaveArgs a;
+    memset(&a, 0, sizeof(a));
+    a.N = N; a.ld = N; a.R = ctx->R; a.mode = 1; a.K = K;
+    a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.Bm = ctx->d_Bm;
+    a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
+    bem::launch_wave(ctx->st, a, precision == BEM_MIXED);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws, buf, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(wd, buf + 2 * (size_t)N * N, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_wave_matrices: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+bem_status bem_havelock(int device, int n, const double* x, const double* y, const double* v, int precision,
+                        double* out) {
+    bem_ctx* ctx = nullptr;
+    if (n < 0 || (n > 0 && (!x || !y || !v || !out))) return fail(nullptr, BEM_ERR_ARG, "bem_havelock: bad arguments");
+    if (n == 0) return BEM_OK;
+    CK(cudaSetDevice(device));
+    CK(bem::upload_poly_constants(device));
+    double* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(double) * 11 * (size_t)n));
+    cudaError_t e = cudaMemcpy(buf, x, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(buf + n, y, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(buf + 2 * (size_t)n, v, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        bem::launch_havelock(0, n, buf, buf + n, buf + 2 * (size_t)n, buf + 3 * (size_t)n, precision == BEM_MIXED);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, buf + 3 * (size_t)n, 64 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(nullptr, BEM_ERR_CUDA, std::string("bem_havelock: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, double* B, int precision, double tol,
+                           int* iters, double* resid) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (n <= 0 || nrhs <= 0 || nrhs > bem::MAX_RHS || !A || !B)
+        return fail(ctx, BEM_ERR_ARG, "bem_dense_solve: bad sizes (1 <= nrhs <= 16)");
+    if (precision != BEM_PLAIN_FP64 && precision != BEM_MIXED) return fail(ctx, BEM_ERR_ARG, "unknown precision");
+    CK(cudaSetDevice(ctx->device));
+    if (!(tol > 0)) tol = 1e-12;
+    // This call owns the context's solver buffers for its duration.
+    free_all(ctx);
+    const int Np = round_up(n, bem::LD_ALIGN);
+    const bool mixed = precision == BEM_MIXED;
+    DA(ctx->d_D64r, (size_t)Np * Np);
+    DA(ctx->d_D64i, (size_t)Np * Np);
+    DA(ctx->d_Y, 2 * (size_t)Np * nrhs);
+    std::vector<double> re((size_t)Np * Np, 0.0), im((size_t)Np * Np, 0.0);
+    for (int i = 0; i < Np; ++i)
+        for (int j = 0; j < Np; ++j) {
+            if (i < n && j < n) {
+                re[(size_t)i * Np + j] = A[2 * ((size_t)i * n + j)];
+                im[(size_t)i * Np + j] = A[2 * ((size_t)i * n + j) + 1];
+            } else if (i == j) {
+                re[(size_t)i * Np + j] = 1.0;
+            }
+        }
+    cudaStream_t st = ctx->st;
+    CK(cudaMemcpyAsync(ctx->d_D64r, re.data(), re.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_D64i, im.data(), im.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_Y, B, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyHostToDevice, st));
+    bem_status s = ensure_lu_buffers(ctx, Np, nrhs, mixed);
+    if (s != BEM_OK) return s;
+    if (mixed) {
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->d_D32r);
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64i, ctx->d_D32i);
+    }
+    double t0 = 0, t1 = 0;
+    s = factor_and_solve(ctx, n, Np, nrhs, mixed, tol, 60, iters, resid, &t0, &t1);
+    if (s != BEM_OK) { free_all(ctx); return s; }
+    cudaError_t e = cudaMemcpyAsync(B, ctx->d_X, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    free_all(ctx);
+    if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_dense_solve: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+// Stage times (ms, accumulated since the last reset) of bem_solve:
+// [0] incident + static RHS, [1] wave assembly, [2] LU, [3] solve/refine,
+// [4] post, [5] number of frequency-solves.
+bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (out6) memcpy(out6, ctx->stage_ms, sizeof(ctx->stage_ms));
+    if (reset) memset(ctx->stage_ms, 0, sizeof(ctx->stage_ms));
+    return BEM_OK;
+}
+
+}  // extern "C"

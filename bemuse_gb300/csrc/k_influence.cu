@@ -1,0 +1,446 @@
+// k_influence.cu -- influence-matrix assembly and hull integrations on sm_103a.
+//
+//   k_rankine      Prepare_Linear_System (Hydrodynamic_Solver.cpp:83-115) with
+//                  FlatQuad/TriPanel::Inf_SourceKernel (Panel.cpp:17-156), FP64.
+//   k_wave<T>      Prepare_Linear_System_Wave_Terms (Hydrodynamic_Solver.cpp:177-203),
+//                  FlatWave*Panel::CInf_SingleDoubleLayerQuad (Panel.cpp:676-694,
+//                  776-794), FreeSurface_Wave_Kernel (:601-636), composed with the
+//                  Rankine part (Solve :415-429) and with the source matrix applied
+//                  to the right-hand sides (Solve :437, :445) so that S is never stored.
+//   k_incident     Calc_Phi_Incident / Set_Incident_Potential_Mats (:544-596).
+//   k_rhs_static   (Ssrc + Srefl) * B, the frequency-independent half of S * B.
+//   k_post_*       AddedMassMat * Phi_J, AddedMassMat * Phi_I, Phi_J^T (dPhi_I .* A)
+//                  (:462-476).
+//
+// Matrix layout: row-major, row = receiver (collocation point), column = source
+// panel, leading dimension ld (a multiple of 128).  Complex matrices are planar
+// (separate re and im arrays).
+#include "bem_internal.h"
+#include "green.cuh"
+
+namespace bem {
+
+__constant__ PolyCoef64 c_poly64;
+__constant__ PolyCoef32 c_poly32;
+
+static const double kFourPIinv = 0.25 / 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// K1: analytic constant-strength source and dipole of a flat panel.
+// Panel record (RK_STRIDE doubles): nv, c[3], ex[3], ey[3], ez[3], lx[4], ly[4],
+// m[4], d[4]; lx/ly are the vertices in the panel frame, m the edge slopes and d
+// the edge lengths, precomputed on the host exactly as Inf_SourceKernel does.
+__device__ __forceinline__ void source_kernel(const double* __restrict__ p, double Px, double Py, double Pz,
+                                              double& S, double& D) {
+    const int n = (int)p[0];
+    double dx = Px - p[1], dy = Py - p[2], dz = Pz - p[3];
+    double PLx = p[4] * dx + p[5] * dy + p[6] * dz;
+    double PLy = p[7] * dx + p[8] * dy + p[9] * dz;
+    double PLz = p[10] * dx + p[11] * dy + p[12] * dz;
+    double Z2 = PLz * PLz;
+    double DX[4], DY[4], e[4], h[4], r[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (k < n) {
+            DX[k] = PLx - p[13 + k];
+            DY[k] = PLy - p[17 + k];
+            e[k] = DX[k] * DX[k] + Z2;
+            h[k] = DX[k] * DY[k];
+            r[k] = sqrt(DX[k] * DX[k] + DY[k] * DY[k] + Z2);
+        }
+    }
+    double Phi = 0.0, sumBL = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (k < n) {
+            int k1 = (k + 1 < n) ? k + 1 : 0;
+            double m = p[21 + k];
+            Phi += atan((m * e[k] - h[k]) / (PLz * r[k])) - atan((m * e[k1] - h[k1]) / (PLz * r[k1]));
+            double ddx = p[13 + k1] - p[13 + k], ddy = p[17 + k1] - p[17 + k];
+            double d = p[25 + k];
+            double B = (DX[k] * ddy - DY[k] * ddx) / d;
+            double L = log((r[k] + r[k1] + d) / (r[k] + r[k1] - d));
+            sumBL += B * L;
+        }
+    }
+    D = Phi * kFourPIinv;
+    S = (PLz * Phi - sumBL) * kFourPIinv;
+}
+
+// mode 0: RS = -(s + sr), RD = d + dr, RSR = -sr * 2 n_z(S)  (composed, ld stride)
+// mode 1: o0 = s, o1 = sr, o2 = d, o3 = dr                    (raw, ld stride)
+__global__ void __launch_bounds__(256) k_rankine(int N, int ld, const double* __restrict__ rec,
+                                                 const double* __restrict__ xr, const double* __restrict__ rn,
+                                                 int mode, double* __restrict__ o0, double* __restrict__ o1,
+                                                 double* __restrict__ o2, double* __restrict__ o3) {
+    int s = blockIdx.x * 32 + threadIdx.x;
+    int r = blockIdx.y * 8 + threadIdx.y;
+    if (s >= N || r >= N) return;
+    double Px = xr[r], Py = xr[N + r], Pz = xr[2 * N + r];
+    double sd, dd, sm, dm;
+    source_kernel(rec + (size_t)s * RK_STRIDE, Px, Py, Pz, sd, dd);
+    source_kernel(rec + ((size_t)N + s) * RK_STRIDE, Px, Py, Pz, sm, dm);
+    size_t o = (size_t)r * ld + s;
+    if (mode == 0) {
+        o0[o] = (-sd) + (-sm);
+        o1[o] = dd + dm;
+        o2[o] = (-sm) * rn[s];
+    } else {
+        o0[o] = sd; o1[o] = sm; o2[o] = dd; o3[o] = dm;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K2: wave term.  One warp per receiver row, lanes over source panels; the
+// eight warps of a CTA sweep the same source tiles so those come from L1.
+template <typename T> struct WaveMath;
+template <> struct WaveMath<double> {
+    typedef cd C;
+    static __device__ __forceinline__ void gf(double h, double v, cd& G, cd& Gh) { gf64(c_poly64, h, v, G, Gh); }
+};
+template <> struct WaveMath<float> {
+    typedef cf C;
+    static __device__ __forceinline__ void gf(float h, float v, cf& G, cf& Gh) { gf32(c_poly32, h, v, G, Gh); }
+};
+
+// Influence (ws, wd) of mirrored wave panel s at receiver point (xr, yr, zr).
+template <typename T>
+__device__ __forceinline__ void wave_pair(const WaveArgs& a, int s, double X, double Y, double Z, T& wsr, T& wsi,
+                                          T& wdr, T& wdi) {
+    const int N = a.N;
+    const int nq = a.nq[s];
+    const T K = (T)a.K;
+    const T c1 = (T)(a.K * kFourPIinv);
+    const T c2 = (T)(a.K * a.K * kFourPIinv);
+    wsr = wsi = wdr = wdi = (T)0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (q < nq) {
+            const double* g = a.gq + (size_t)q * N + s;  // field stride 4N
+            double qx = g[0], qy = g[(size_t)4 * N], qz = g[(size_t)8 * N];
+            T w = (T)g[(size_t)12 * N];
+            T nx = (T)g[(size_t)16 * N], ny = (T)g[(size_t)20 * N], nz = (T)g[(size_t)24 * N];
+            T XX = (T)(X - qx) * K, YY = (T)(Y - qy) * K, VV = (T)(Z - qz) * K;
+            T hh = sqrt(XX * XX + YY * YY);
+            typename WaveMath<T>::C G, Gh;
+            WaveMath<T>::gf(hh, VV, G, Gh);
+            T gxr = 0, gxi = 0, gyr = 0, gyi = 0;
+            if (hh > (T)1.0e-6) {
+                gxr = Gh.re * XX / hh; gxi = Gh.im * XX / hh;
+                gyr = Gh.re * YY / hh; gyi = Gh.im * YY / hh;
+            }
+            // FreeSurface_Wave_Kernel scaling: G *= K/(4 pi), dG *= K^2/(4 pi)
+            T Gr = G.re * c1, Gi = G.im * c1;
+            T dxr = gxr * c2, dxi = gxi * c2, dyr = gyr * c2, dyi = gyi * c2;
+            T dzr = G.re * c2, dzi = G.im * c2;
+            wsr += w * Gr;
+            wsi += w * Gi;
+            wdr += w * (dxr * nx + dyr * ny + dzr * nz);
+            wdi += w * (dxi * nx + dyi * ny + dzi * nz);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= a.N) return;
+    const int N = a.N, R = a.R;
+    const double X = a.xr[r], Y = a.xr[N + r], Z = a.xr[2 * N + r];
+    T acc_re[MAX_RHS], acc_im[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0; acc_im[j] = 0; }
+    const size_t row = (size_t)r * a.ld;
+    for (int s = lane; s < N; s += 32) {
+        T wsr, wsi, wdr, wdi;
+        wave_pair<T>(a, s, X, Y, Z, wsr, wsi, wdr, wdi);
+        if (a.mode == 1) {
+            size_t o = 2 * ((size_t)r * N + s);
+            a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = (double)wsi;
+            a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
+            continue;
+        }
+        // D = (d + dr) + (wd + (-sr) 2 n_z K): Solve (:428) with DWave (:200)
+        double dre = a.RD[row + s] + ((double)wdr + a.RSR[row + s] * a.K);
+        double dim = (double)wdi;
+        a.D64r[row + s] = dre;
+        a.D64i[row + s] = dim;
+        if (a.D32r) { a.D32r[row + s] = (float)dre; a.D32i[row + s] = (float)dim; }
+        // S = Ssrc + Srefl - ws; the (-ws) part times the RHS block B (N x R).
+        const double* b = a.Bm + (size_t)s * 2 * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                T br = (T)b[2 * j], bi = (T)b[2 * j + 1];
+                acc_re[j] -= wsr * br - wsi * bi;
+                acc_im[j] -= wsr * bi + wsi * br;
+            }
+        }
+    }
+    if (a.mode == 1) return;
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            T vr = acc_re[j], vi = acc_im[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {
+                a.Y[2 * ((size_t)r * R + j)] += (double)vr;
+                a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
+            }
+        }
+    }
+}
+
+// Padding rows/columns of the working matrices: identity (so the padded LU
+// factors the block diagonal [D, 0; 0, I]).
+__global__ void k_pad_identity(int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int total = ld - N;
+    if (total <= 0) return;
+    // rows N..ld-1 (full) and columns N..ld-1 of rows 0..N-1
+    for (size_t idx = i; idx < (size_t)ld * ld; idx += (size_t)gridDim.x * blockDim.x) {
+        int r = (int)(idx / ld), c = (int)(idx % ld);
+        if (r < N && c < N) continue;
+        double v = (r == c) ? 1.0 : 0.0;
+        if (D64r) { D64r[idx] = v; D64i[idx] = 0.0; }
+        if (D32r) { D32r[idx] = (float)v; D32i[idx] = 0.0f; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Incident wave (infinite depth, Calc_Phi_Incident :544-561) at the panel
+// centroids and the diffraction right-hand sides -dPhi_I/dn .* area (:445).
+__global__ void k_incident(int N, int NB, int R, const double* __restrict__ betas, double K, double Omega,
+                           const double* __restrict__ cen, const double* __restrict__ nrm,
+                           const double* __restrict__ area, double* __restrict__ phiI, double* __restrict__ dphiI,
+                           double* __restrict__ Bm) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const double g = 9.81;
+    double x = cen[p], y = cen[N + p], z = cen[2 * N + p];
+    double nx = nrm[p], ny = nrm[N + p], nz = nrm[2 * N + p];
+    for (int b = 0; b < NB; ++b) {
+        double pr = 0, pi = 0, dr = 0, di = 0;
+        if (Omega != 0.0) {
+            double CB = cos(betas[b]), SB = sin(betas[b]);
+            // Phi_I = (i g / Omega) exp(i K (x cos b + y sin b)); Phi_i = e^{K z} Phi_I
+            double arg = K * (x * CB + y * SB);
+            double sa, ca;
+            sincos(arg, &sa, &ca);
+            double a = g / Omega;          // Im*Gravity/Omega = (0, g/Omega)
+            double Pr = -a * sa, Pi = a * ca;  // (0 + i a)(ca + i sa)
+            double Zf = exp(K * z);
+            pr = Zf * Pr; pi = Zf * Pi;
+            // dPhi/dx = i K CB Phi, dPhi/dy = i K SB Phi, dPhi/dz = K Phi
+            double kx = K * CB, ky = K * SB;
+            double dxr = -kx * pi, dxi = kx * pr;
+            double dyr = -ky * pi, dyi = ky * pr;
+            double dzr = K * pr, dzi = K * pi;
+            dr = nx * dxr + ny * dyr + nz * dzr;
+            di = nx * dxi + ny * dyi + nz * dzi;
+        }
+        size_t o = 2 * ((size_t)p * NB + b);
+        phiI[o] = pr; phiI[o + 1] = pi;
+        dphiI[o] = dr; dphiI[o + 1] = di;
+        size_t ob = 2 * ((size_t)p * R + 6 + b);
+        Bm[ob] = -(dr * area[p]);
+        Bm[ob + 1] = -(di * area[p]);
+    }
+}
+
+// Y[:, j0:j1] = RS * B[:, j0:j1] (RS real N x N, B complex N x R). One warp per row.
+__global__ void __launch_bounds__(256) k_rhs_static(int N, int ld, int R, int j0, int j1,
+                                                    const double* __restrict__ RS, const double* __restrict__ Bm,
+                                                    double* __restrict__ Y) {
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= N) return;
+    double ar[MAX_RHS], ai[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+    const double* row = RS + (size_t)r * ld;
+    for (int s = lane; s < N; s += 32) {
+        double v = row[s];
+        const double* b = Bm + (size_t)s * 2 * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j)
+            if (j >= j0 && j < j1) { ar[j] += v * b[2 * j]; ai[j] += v * b[2 * j + 1]; }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j >= j0 && j < j1) {
+            double vr = ar[j], vi = ai[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) { Y[2 * ((size_t)r * R + j)] = vr; Y[2 * ((size_t)r * R + j) + 1] = vi; }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Hull integrations (Hydrodynamic_Solver.cpp:462-476).  X = solution (N x R,
+// interleaved complex; columns 0..5 = Phi_J).  Outputs per CTA partial sums of
+//   AM[i][j]  = sum_p Nk[p][i] A_p X[p][j]          (36 complex)
+//   F1[i][b]  = sum_p Nk[p][i] A_p PhiI[p][b]       (6 NB complex)
+//   F2[i][b]  = sum_p X[p][i] dPhiI[p][b] A_p       (6 NB complex)
+__global__ void __launch_bounds__(256) k_post_partial(int N, int NB, int R, const double* __restrict__ X,
+                                                      const double* __restrict__ Nk, const double* __restrict__ area,
+                                                      const double* __restrict__ phiI,
+                                                      const double* __restrict__ dphiI, double* __restrict__ part) {
+    const int nout = 36 + 12 * NB;
+    const int p0 = blockIdx.x * 256;
+    const int pend = min(N, p0 + 256);
+    for (int t = threadIdx.x; t < nout; t += blockDim.x) {
+        double sr = 0, si = 0;
+        if (t < 36) {
+            int i = t / 6, j = t % 6;
+            for (int p = p0; p < pend; ++p) {
+                double w = Nk[(size_t)p * 6 + i] * area[p];
+                sr += w * X[2 * ((size_t)p * R + j)];
+                si += w * X[2 * ((size_t)p * R + j) + 1];
+            }
+        } else if (t < 36 + 6 * NB) {
+            int u = t - 36, i = u / NB, b = u % NB;
+            for (int p = p0; p < pend; ++p) {
+                double w = Nk[(size_t)p * 6 + i] * area[p];
+                sr += w * phiI[2 * ((size_t)p * NB + b)];
+                si += w * phiI[2 * ((size_t)p * NB + b) + 1];
+            }
+        } else {
+            int u = t - 36 - 6 * NB, i = u / NB, b = u % NB;
+            for (int p = p0; p < pend; ++p) {
+                double xr = X[2 * ((size_t)p * R + i)], xi = X[2 * ((size_t)p * R + i) + 1];
+                double gr = dphiI[2 * ((size_t)p * NB + b)] * area[p], gi = dphiI[2 * ((size_t)p * NB + b) + 1] * area[p];
+                sr += xr * gr - xi * gi;
+                si += xr * gi + xi * gr;
+            }
+        }
+        part[2 * ((size_t)blockIdx.x * nout + t)] = sr;
+        part[2 * ((size_t)blockIdx.x * nout + t) + 1] = si;
+    }
+}
+
+__global__ void k_post_reduce(int nblk, int nout, const double* __restrict__ part, double* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nout) return;
+    double sr = 0, si = 0;
+    for (int b = 0; b < nblk; ++b) {
+        sr += part[2 * ((size_t)b * nout + t)];
+        si += part[2 * ((size_t)b * nout + t) + 1];
+    }
+    out[2 * t] = sr;
+    out[2 * t + 1] = si;
+}
+
+// Batch HavelockGF (Kernels.cpp:342-412) for the C ABI and tests.
+template <typename T>
+__global__ void k_havelock(int n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ v, double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T dx = (T)x[i], dy = (T)y[i], vv = (T)v[i];
+    T hh = sqrt(dx * dx + dy * dy);
+    typename WaveMath<T>::C G, Gh;
+    WaveMath<T>::gf(hh, vv, G, Gh);
+    double* o = out + 8 * (size_t)i;
+    o[0] = G.re; o[1] = G.im;
+    if (hh > (T)1.0e-6) {
+        o[2] = (double)(Gh.re * dx / hh); o[3] = (double)(Gh.im * dx / hh);
+        o[4] = (double)(Gh.re * dy / hh); o[5] = (double)(Gh.im * dy / hh);
+    } else {
+        o[2] = o[3] = o[4] = o[5] = 0.0;
+    }
+    o[6] = G.re; o[7] = G.im;
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+static bool g_poly_ready[64] = {false};
+
+cudaError_t upload_poly_constants(int device) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (g_poly_ready[device]) return cudaSuccess;
+    PolyCoef64 p64;
+    PolyCoef32 p32;
+    memset(&p64, 0, sizeof(p64));
+    memset(&p32, 0, sizeof(p32));
+    double* dst64[7] = {p64.A, p64.B, p64.C, p64.D, p64.dA, p64.dB, p64.dC};
+    float* dst32[7] = {p32.A, p32.B, p32.C, p32.D, p32.dA, p32.dB, p32.dC};
+    int k = 0;
+#define BEM_FILL(name, n, ...)                                            \
+    {                                                                      \
+        const double c[] = {__VA_ARGS__};                                  \
+        for (int i = 0; i < n; ++i) dst64[k][i] = c[i];                    \
+        /* re-expand about rho = 1/2: s_j = sum_i c_i C(i,j) 2^-(i-j) */   \
+        for (int j = 0; j < n; ++j) {                                      \
+            long double s = 0;                                             \
+            for (int i = j; i < n; ++i) {                                  \
+                long double bin = 1;                                       \
+                for (int t = 0; t < j; ++t) bin = bin * (i - t) / (t + 1); \
+                s += (long double)c[i] * bin * powl(0.5L, i - j);          \
+            }                                                              \
+            dst32[k][j] = (float)s;                                        \
+        }                                                                  \
+        ++k;                                                               \
+    }
+    BEM_POLY_TABLE(BEM_FILL)
+#undef BEM_FILL
+    cudaError_t e = cudaMemcpyToSymbol(c_poly64, &p64, sizeof(p64));
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyToSymbol(c_poly32, &p32, sizeof(p32));
+    if (e == cudaSuccess) g_poly_ready[device] = true;
+    return e;
+}
+
+void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
+                    double* o0, double* o1, double* o2, double* o3) {
+    dim3 blk(32, 8), grd((N + 31) / 32, (N + 7) / 8);
+    k_rankine<<<grd, blk, 0, st>>>(N, ld, rec, xr, rn, mode, o0, o1, o2, o3);
+}
+
+void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
+    dim3 grd((a.N + 7) / 8);
+    if (fp32) k_wave<float><<<grd, 256, 0, st>>>(a);
+    else k_wave<double><<<grd, 256, 0, st>>>(a);
+}
+
+void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i) {
+    if (ld <= N) return;
+    k_pad_identity<<<1024, 256, 0, st>>>(N, ld, D64r, D64i, D32r, D32i);
+}
+
+void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
+                     const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
+                     double* Bm) {
+    k_incident<<<(N + 127) / 128, 128, 0, st>>>(N, NB, R, betas, K, Omega, cen, nrm, area, phiI, dphiI, Bm);
+}
+
+void launch_rhs_static(cudaStream_t st, int N, int ld, int R, int j0, int j1, const double* RS, const double* Bm,
+                       double* Y) {
+    k_rhs_static<<<(N + 7) / 8, 256, 0, st>>>(N, ld, R, j0, j1, RS, Bm, Y);
+}
+
+void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
+                 const double* phiI, const double* dphiI, double* part, double* out) {
+    int nblk = (N + 255) / 256;
+    int nout = 36 + 12 * NB;
+    k_post_partial<<<nblk, 256, 0, st>>>(N, NB, R, X, Nk, area, phiI, dphiI, part);
+    k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out);
+}
+
+void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,
+                     bool fp32) {
+    int g = (n + 127) / 128;
+    if (fp32) k_havelock<float><<<g, 128, 0, st>>>(n, x, y, v, out);
+    else k_havelock<double><<<g, 128, 0, st>>>(n, x, y, v, out);
+}
+
+}  // namespace bem

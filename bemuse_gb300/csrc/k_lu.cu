@@ -1,0 +1,449 @@
+// k_lu.cu -- blocked complex LU, triangular solves and the FP64 residual.
+//
+// Replaces Eigen::PartialPivLU<CMatrix> (Hydrodynamic_Solver.cpp:430, 438, 446).
+// The BIE matrix D = (1/2) I + K has |D_kk| >= |D_ik| at every elimination step
+// on the meshes this solver targets, so partial pivoting never exchanges rows;
+// the factorization here performs no exchanges and flags FLAG_PIVOT whenever a
+// multiplier has |l_ik| > 1 (+1e-6), i.e. whenever partial pivoting *would*
+// have exchanged rows.  With no flag raised, L and U are those of partial
+// pivoting with the identity permutation.
+//
+// Step k0 (block width nb):
+//   k_lu_diag      one CTA factors D11 in shared memory and forms L11^-1, U11^-1
+//   k_cgemm        L21 = A21 U11^-1 and U12 = L11^-1 A12 (into workspaces)
+//   k_copy_back    writes L21 / U12 into the matrix, checks |l_ik| <= 1
+//   k_cgemm / tc   A22 -= L21 U12 (SIMT complex GEMM; tcgen05 TF32 in k_tc_gemm.cu)
+// Solves use the stored off-diagonal blocks and the diagonal-block inverses.
+#include "bem_internal.h"
+#include <cstdio>
+
+namespace bem {
+
+void tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut);
+
+template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
+
+// ---------------------------------------------------------------------------
+template <typename T, int NB>
+__global__ void __launch_bounds__(1024) k_lu_diag(int k0, CMat<T> A, T* invr, T* invi, int* flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int P = NB + 1;
+    T* ar = reinterpret_cast<T*>(smem_raw);
+    T* ai = ar + NB * P;
+    T* tr = ai + NB * P;  // column scratch
+    T* ti = tr + NB;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const size_t ld = A.ld;
+    for (int idx = tid; idx < NB * NB; idx += nt) {
+        int i = idx / NB, j = idx % NB;
+        size_t g = (size_t)(k0 + i) * ld + k0 + j;
+        ar[i * P + j] = A.re[g];
+        ai[i * P + j] = A.im[g];
+    }
+    __syncthreads();
+    int local_flags = 0;
+    for (int k = 0; k < NB; ++k) {
+        T pr = ar[k * P + k], pi = ai[k * P + k];
+        T den = pr * pr + pi * pi;
+        if (!(den > (T)0) || !finite_(den)) local_flags |= FLAG_ZERO_PIVOT;
+        T ir = pr / den, ii = -pi / den;
+        for (int i = k + 1 + tid; i < NB; i += nt) {
+            T xr = ar[i * P + k], xi = ai[i * P + k];
+            T lr = xr * ir - xi * ii, li = xr * ii + xi * ir;
+            ar[i * P + k] = lr;
+            ai[i * P + k] = li;
+            if (lr * lr + li * li > (T)(1.000002)) local_flags |= FLAG_PIVOT;
+        }
+        __syncthreads();
+        const int m = NB - k - 1;
+        for (int idx = tid; idx < m * m; idx += nt) {
+            int i = k + 1 + idx / m, j = k + 1 + idx % m;
+            T lr = ar[i * P + k], li = ai[i * P + k];
+            T ur = ar[k * P + j], ui = ai[k * P + j];
+            ar[i * P + j] -= lr * ur - li * ui;
+            ai[i * P + j] -= lr * ui + li * ur;
+        }
+        __syncthreads();
+    }
+    // Factors back to the matrix.
+    for (int idx = tid; idx < NB * NB; idx += nt) {
+        int i = idx / NB, j = idx % NB;
+        size_t g = (size_t)(k0 + i) * ld + k0 + j;
+        A.re[g] = ar[i * P + j];
+        A.im[g] = ai[i * P + j];
+    }
+    __syncthreads();
+    // L^-1 in place on the strict lower part (unit diagonal): for j descending,
+    // X[i][j] = -sum_{m=j+1..i} X[i][m] L[m][j]  with X[i][i] = 1.
+    for (int j = NB - 2; j >= 0; --j) {
+        for (int m = j + 1 + tid; m < NB; m += nt) { tr[m] = ar[m * P + j]; ti[m] = ai[m * P + j]; }
+        __syncthreads();
+        for (int i = j + 1 + tid; i < NB; i += nt) {
+            T sr = tr[i], si = ti[i];  // X[i][i] = 1
+            for (int m = j + 1; m < i; ++m) {
+                T xr = ar[i * P + m], xi = ai[i * P + m];
+                sr += xr * tr[m] - xi * ti[m];
+                si += xr * ti[m] + xi * tr[m];
+            }
+            ar[i * P + j] = -sr;
+            ai[i * P + j] = -si;
+        }
+        __syncthreads();
+    }
+    // U^-1 in place on the upper part: for j ascending,
+    // X[j][j] = 1/U[j][j];  X[i][j] = -(sum_{m=i..j-1} X[i][m] U[m][j]) X[j][j], i < j.
+    for (int j = 0; j < NB; ++j) {
+        for (int m = tid; m <= j; m += nt) { tr[m] = ar[m * P + j]; ti[m] = ai[m * P + j]; }
+        __syncthreads();
+        T pr = tr[j], pi = ti[j];
+        T den = pr * pr + pi * pi;
+        T dr = pr / den, di = -pi / den;
+        for (int i = tid; i < j; i += nt) {
+            T sr = 0, si = 0;
+            for (int m = i; m < j; ++m) {
+                T xr = ar[i * P + m], xi = ai[i * P + m];
+                sr += xr * tr[m] - xi * ti[m];
+                si += xr * ti[m] + xi * tr[m];
+            }
+            ar[i * P + j] = -(sr * dr - si * di);
+            ai[i * P + j] = -(sr * di + si * dr);
+        }
+        if (tid == 0) { ar[j * P + j] = dr; ai[j * P + j] = di; }
+        __syncthreads();
+    }
+    // inv layout: [blk][0] = L^-1 (unit lower, diagonal stored as 1), [blk][1] = U^-1.
+    const int blk = k0 / NB;
+    T* Lr = invr + (size_t)blk * 2 * NB * NB;
+    T* Li = invi + (size_t)blk * 2 * NB * NB;
+    T* Ur = Lr + NB * NB;
+    T* Ui = Li + NB * NB;
+    for (int idx = tid; idx < NB * NB; idx += nt) {
+        int i = idx / NB, j = idx % NB;
+        T lr = (i > j) ? ar[i * P + j] : (i == j ? (T)1 : (T)0);
+        T li = (i > j) ? ai[i * P + j] : (T)0;
+        Lr[idx] = lr; Li[idx] = li;
+        Ur[idx] = (i <= j) ? ar[i * P + j] : (T)0;
+        Ui[idx] = (i <= j) ? ai[i * P + j] : (T)0;
+    }
+    if (local_flags) atomicOr(flags, local_flags);
+}
+
+// ---------------------------------------------------------------------------
+// C = beta C + sgn * A B, planar complex, row-major.  M, N multiples of 64,
+// K multiple of 16.  256 threads, 64x64 tile, 4x4 outputs per thread.
+template <typename T>
+__global__ void __launch_bounds__(256) k_cgemm(int M, int N, int K, CMat<T> A, CMat<T> B, CMat<T> C, T sgn,
+                                               int beta) {
+    __shared__ T Asr[16][64], Asi[16][64], Bsr[16][64], Bsi[16][64];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    T cr[4][4], ci[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { cr[i][j] = 0; ci[i][j] = 0; }
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        // A tile: 64 rows x 16 k  (stored transposed As[k][m])
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            int idx = tid + t * 256;
+            int m = idx >> 4, k = idx & 15;
+            size_t g = (size_t)(m0 + m) * A.ld + k0 + k;
+            Asr[k][m] = A.re[g];
+            Asi[k][m] = A.im[g];
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            int idx = tid + t * 256;
+            int k = idx >> 6, n = idx & 63;
+            size_t g = (size_t)(k0 + k) * B.ld + n0 + n;
+            Bsr[k][n] = B.re[g];
+            Bsi[k][n] = B.im[g];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            T ar_[4], ai_[4], br_[4], bi_[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) { ar_[i] = Asr[k][ty * 4 + i]; ai_[i] = Asi[k][ty * 4 + i]; }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { br_[j] = Bsr[k][tx * 4 + j]; bi_[j] = Bsi[k][tx * 4 + j]; }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    cr[i][j] = fma(ar_[i], br_[j], cr[i][j]);
+                    cr[i][j] = fma(-ai_[i], bi_[j], cr[i][j]);
+                    ci[i][j] = fma(ar_[i], bi_[j], ci[i][j]);
+                    ci[i][j] = fma(ai_[i], br_[j], ci[i][j]);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            size_t g = (size_t)(m0 + ty * 4 + i) * C.ld + n0 + tx * 4 + j;
+            T vr = sgn * cr[i][j], vi = sgn * ci[i][j];
+            if (beta) { vr += C.re[g]; vi += C.im[g]; }
+            C.re[g] = vr;
+            C.im[g] = vi;
+        }
+}
+
+// Copy a panel workspace (rows x cols, ld = wld) into the matrix block at
+// (r0, c0); optionally check |x| <= 1 (L21 multipliers) and write a transposed
+// copy (for the tensor-core B operand).
+template <typename T>
+__global__ void k_copy_back(int rows, int cols, const T* wr, const T* wi, int wld, CMat<T> A, int r0, int c0,
+                            int check, T* tr, T* ti, int tld, int* flags) {
+    size_t total = (size_t)rows * cols;
+    int bad = 0;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        int i = (int)(idx / cols), j = (int)(idx % cols);
+        T vr = wr[(size_t)i * wld + j], vi = wi[(size_t)i * wld + j];
+        size_t g = (size_t)(r0 + i) * A.ld + c0 + j;
+        A.re[g] = vr;
+        A.im[g] = vi;
+        if (check && vr * vr + vi * vi > (T)(1.000002)) bad = 1;
+        if (tr) { tr[(size_t)j * tld + i] = vr; ti[(size_t)j * tld + i] = vi; }
+    }
+    if (bad) atomicOr(flags, FLAG_PIVOT);
+}
+
+template <typename T, int NB>
+static void lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
+                        bool tc) {
+    const size_t smem = (size_t)(2 * NB * (NB + 1) + 2 * NB) * sizeof(T);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_lu_diag<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    // workspaces: wl [2][n][NB] (L21), wu [2][NB][n] (U12), wut [2][n][NB] (U12^T)
+    T* wlr = wl; T* wli = wl + (size_t)n * NB;
+    T* wur = wu; T* wui = wu + (size_t)n * NB;
+    T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        k_lu_diag<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags);
+        const int rem = n - k0 - NB;
+        if (rem <= 0) break;
+        const int blk = k0 / NB;
+        CMat<T> Linv{invr + (size_t)blk * 2 * NB * NB, invi + (size_t)blk * 2 * NB * NB, NB};
+        CMat<T> Uinv{Linv.re + NB * NB, Linv.im + NB * NB, NB};
+        CMat<T> A21{A.re + (size_t)(k0 + NB) * A.ld + k0, A.im + (size_t)(k0 + NB) * A.ld + k0, A.ld};
+        CMat<T> A12{A.re + (size_t)k0 * A.ld + k0 + NB, A.im + (size_t)k0 * A.ld + k0 + NB, A.ld};
+        CMat<T> WL{wlr, wli, NB};
+        CMat<T> WU{wur, wui, rem};
+        // L21 = A21 U^-1  (rem x NB),  U12 = L^-1 A12  (NB x rem)
+        k_cgemm<T><<<dim3(NB / 64, rem / 64), 256, 0, st>>>(rem, NB, NB, A21, Uinv, WL, (T)1, 0);
+        k_cgemm<T><<<dim3(rem / 64, NB / 64), 256, 0, st>>>(NB, rem, NB, Linv, A12, WU, (T)1, 0);
+        int nblk = (int)(((size_t)rem * NB + 255) / 256);
+        if (nblk > 4096) nblk = 4096;
+        k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 1, (T*)nullptr, (T*)nullptr, 0,
+                                             flags);
+        k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, wur, wui, rem, A, k0, k0 + NB, 0, wtr, wti, NB, flags);
+        CMat<T> A22{A.re + (size_t)(k0 + NB) * A.ld + k0 + NB, A.im + (size_t)(k0 + NB) * A.ld + k0 + NB, A.ld};
+        if (tc) {
+            tc_trailing_update(st, n, k0, NB, *reinterpret_cast<CMat<float>*>(&A), reinterpret_cast<const float*>(wl),
+                               reinterpret_cast<const float*>(wut));
+        } else {
+            k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, WU, A22, (T)-1, 1);
+        }
+    }
+}
+
+void lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
+                   int* flags) {
+    lu_factor_t<double, 64>(st, n, A, invr, invi, wl, wu, nullptr, flags, false);
+}
+void lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu, float* wut,
+                   int* flags, bool tc) {
+    lu_factor_t<float, 128>(st, n, A, invr, invi, wl, wu, wut, flags, tc);
+}
+
+// ---------------------------------------------------------------------------
+// Block triangular solves.  X is n x R complex interleaved (T2 = {re, im}).
+// diag: Z[blk] = Inv[blk] * Yin[blk]  (one CTA; Yin, Z may alias only if equal)
+template <typename T, int NB>
+__global__ void k_trsv_diag(int blk, int R, const T* __restrict__ invr, const T* __restrict__ invi, int which,
+                            const T* __restrict__ Yin, T* __restrict__ Z) {
+    __shared__ T yr[NB * MAX_RHS], yi[NB * MAX_RHS];
+    const T* Mr = invr + ((size_t)blk * 2 + which) * NB * NB;
+    const T* Mi = invi + ((size_t)blk * 2 + which) * NB * NB;
+    const size_t base = (size_t)blk * NB;
+    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
+        int k = idx / R, j = idx % R;
+        yr[idx] = Yin[2 * ((base + k) * R + j)];
+        yi[idx] = Yin[2 * ((base + k) * R + j) + 1];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
+        int i = idx / R, j = idx % R;
+        T sr = 0, si = 0;
+        for (int k = 0; k < NB; ++k) {
+            T mr = Mr[i * NB + k], mi = Mi[i * NB + k];
+            T vr = yr[k * R + j], vi = yi[k * R + j];
+            sr += mr * vr - mi * vi;
+            si += mr * vi + mi * vr;
+        }
+        Z[2 * ((base + i) * R + j)] = sr;
+        Z[2 * ((base + i) * R + j) + 1] = si;
+    }
+}
+
+// update: Y[r] -= A[r][blk*NB : +NB] * Z[blk] for r in [r0, r1). One warp per row.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) k_trsv_update(int blk, int r0, int r1, int R, CMat<T> A,
+                                                     const T* __restrict__ Z, T* __restrict__ Y) {
+    __shared__ T zr[NB * MAX_RHS], zi[NB * MAX_RHS];
+    const size_t base = (size_t)blk * NB;
+    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
+        zr[idx] = Z[2 * (base * R + idx)];
+        zi[idx] = Z[2 * (base * R + idx) + 1];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int r = r0 + blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= r1) return;
+    T ar_[MAX_RHS], ai_[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar_[j] = 0; ai_[j] = 0; }
+    const T* rr = A.re + (size_t)r * A.ld + base;
+    const T* ri = A.im + (size_t)r * A.ld + base;
+    for (int k = lane; k < NB; k += 32) {
+        T mr = rr[k], mi = ri[k];
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                T vr = zr[k * R + j], vi = zi[k * R + j];
+                ar_[j] += mr * vr - mi * vi;
+                ai_[j] += mr * vi + mi * vr;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            T vr = ar_[j], vi = ai_[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {
+                Y[2 * ((size_t)r * R + j)] -= vr;
+                Y[2 * ((size_t)r * R + j) + 1] -= vi;
+            }
+        }
+    }
+}
+
+template <typename T, int NB>
+static void lu_solve_t(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* invi, int R, T* X, T* tmp) {
+    const int nblk = n / NB;
+    // forward: tmp = L^-1 X  (X updated in place below the current block)
+    for (int b = 0; b < nblk; ++b) {
+        k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 0, X, tmp);
+        int r0 = (b + 1) * NB;
+        if (r0 < n) k_trsv_update<T, NB><<<(n - r0 + 7) / 8, 256, 0, st>>>(b, r0, n, R, A, tmp, X);
+    }
+    // backward: X = U^-1 tmp  (tmp updated in place above the current block)
+    for (int b = nblk - 1; b >= 0; --b) {
+        k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 1, tmp, X);
+        int r1 = b * NB;
+        if (r1 > 0) k_trsv_update<T, NB><<<(r1 + 7) / 8, 256, 0, st>>>(b, 0, r1, R, A, X, tmp);
+    }
+}
+
+// The solve needs an n x R scratch; it lives right after X (caller allocates 2 n R).
+void lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X) {
+    lu_solve_t<double, 64>(st, n, A, invr, invi, R, X, X + (size_t)2 * n * R);
+}
+void lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X) {
+    lu_solve_t<float, 128>(st, n, A, invr, invi, R, X, X + (size_t)2 * n * R);
+}
+
+// ---------------------------------------------------------------------------
+// Rres = Y - D X in FP64; one warp per row.  nrm[j] = max_r |Rres[r][j]|,
+// nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (non-negative doubles).
+__global__ void __launch_bounds__(256) k_residual(int N, int ld, const double* __restrict__ Dr,
+                                                  const double* __restrict__ Di, int R, const double* __restrict__ X,
+                                                  const double* __restrict__ Y, double* __restrict__ Rres,
+                                                  unsigned long long* nrm) {
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= N) return;
+    double ar_[MAX_RHS], ai_[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar_[j] = 0; ai_[j] = 0; }
+    const double* rr = Dr + (size_t)r * ld;
+    const double* ri = Di + (size_t)r * ld;
+    for (int s = lane; s < N; s += 32) {
+        double mr = rr[s], mi = ri[s];
+        const double* x = X + 2 * (size_t)s * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double vr = x[2 * j], vi = x[2 * j + 1];
+                ar_[j] = fma(mr, vr, ar_[j]);
+                ar_[j] = fma(-mi, vi, ar_[j]);
+                ai_[j] = fma(mr, vi, ai_[j]);
+                ai_[j] = fma(mi, vr, ai_[j]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            double vr = ar_[j], vi = ai_[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {
+                double yr = Y[2 * ((size_t)r * R + j)], yi = Y[2 * ((size_t)r * R + j) + 1];
+                double er = yr - vr, ei = yi - vi;
+                Rres[2 * ((size_t)r * R + j)] = er;
+                Rres[2 * ((size_t)r * R + j) + 1] = ei;
+                double en = sqrt(er * er + ei * ei), yn = sqrt(yr * yr + yi * yi);
+                if (!isfinite(en)) en = 1.0e300;
+                atomicMax(nrm + j, (unsigned long long)__double_as_longlong(en));
+                atomicMax(nrm + R + j, (unsigned long long)__double_as_longlong(yn));
+            }
+        }
+    }
+}
+
+__global__ void k_to_f32(size_t n, const double* __restrict__ s, float* __restrict__ d) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        d[i] = (float)s[i];
+}
+__global__ void k_add_f32(size_t n, const float* __restrict__ s, double* __restrict__ d) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        d[i] += (double)s[i];
+}
+__global__ void k_pad_rhs(int N, int Np, int R, double* X) {
+    size_t total = (size_t)(Np - N) * R * 2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+        X[(size_t)N * R * 2 + i] = 0.0;
+}
+
+void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
+                     const double* Y, double* Rres, unsigned long long* nrm) {
+    k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres, nrm);
+}
+void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst) {
+    k_to_f32<<<1024, 256, 0, st>>>(n, src, dst);
+}
+void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst) {
+    k_add_f32<<<1024, 256, 0, st>>>(n, src, dst);
+}
+void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X) {
+    if (Np > N) k_pad_rhs<<<256, 256, 0, st>>>(N, Np, R, X);
+}
+
+}  // namespace bem

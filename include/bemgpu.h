@@ -1,0 +1,187 @@
+/*
+ * bemgpu.h -- C ABI of the GB300-native frequency-domain panel-method solver.
+ *
+ * This is the drop-in boundary for the reference's hydrodynamic path
+ * (ZeppSav/BEMUse):
+ *   - the Boundary mesh generators           (src/Boundary/*.cpp),
+ *   - Hydrodynamic_Radiation_Solver           (src/Solver/Hydrodynamic_Solver.{h,cpp}),
+ *     behind the virtual BEMUse::Solver API   (src/Solver/Solver_Base.h:39-153),
+ *   - the Green-function kernels              (src/Kernels.cpp).
+ * Plain pointers and sizes only; all arrays are caller-owned host memory
+ * unless stated.  Every call returns a bem_status; bem_last_error() gives the
+ * message.  Nothing here aborts the process.
+ *
+ * Frequency convention: bem_solve takes the internal angular frequency Omega
+ * (rad/s).  The reference's Set_Real(Frequency) stores Frequency and computes
+ * Omega = Frequency / (2 pi) (Hydrodynamic_Solver.cpp:405); a caller porting
+ * Set_Real code passes Frequency / (2 pi).
+ */
+#ifndef BEMGPU_H
+#define BEMGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BEM_OK = 0,
+    BEM_ERR_ARG = 1,         /* invalid argument (null pointer, bad size, bad mesh) */
+    BEM_ERR_CUDA = 2,        /* CUDA runtime error (message holds the CUDA error string) */
+    BEM_ERR_STATE = 3,       /* call out of order (e.g. bem_solve before bem_setup) */
+    BEM_ERR_NUMERIC = 4,     /* non-finite values, a multiplier |l_ik| > 1 (row exchange needed),
+                                or refinement that did not reach its tolerance */
+    BEM_ERR_NOMEM = 5,       /* device allocation failed */
+    BEM_ERR_UNSUPPORTED = 6  /* feature or device not supported (e.g. no sm_103 GPU) */
+} bem_status;
+
+/* Precision modes of bem_solve. */
+typedef enum {
+    BEM_PLAIN_FP64 = 0, /* FP64 wave assembly, FP64 LU, FP64 solves (the reference's arithmetic) */
+    BEM_MIXED = 1       /* FP32 wave assembly into an FP64 operator, TF32 tensor-core LU,
+                           FP64 iterative refinement to rel. residual <= refine_tol */
+} bem_precision;
+
+typedef struct bem_ctx bem_ctx;
+
+/* A panel mesh.  Nodes are given in the frame of their component; element e of
+ * component c has global vertex positions nodes[...] + comp_origin[3c..3c+2]
+ * (the translation-only CoordSys of Triple_Spar.cpp:60-67).  elems holds four
+ * node indices per element; elems[4e+3] = -1 marks a triangle.  Element order
+ * is the panel order of the linear system.  The optional aux mesh is the
+ * interior waterplane used for hydrostatics (Hydrodynamic_Solver.cpp:353-367). */
+typedef struct {
+    int n_nodes;
+    const double* nodes;        /* n_nodes x 3 */
+    int n_elems;
+    const int* elems;           /* n_elems x 4 */
+    int n_comp;                 /* >= 1; 0 means one component at the origin */
+    const int* comp_first;      /* n_comp + 1 element offsets (may be NULL if n_comp == 0) */
+    const double* comp_origin;  /* n_comp x 3 (may be NULL if n_comp == 0) */
+} bem_mesh;
+
+/* Mass properties (Boundary_Base.h:149-156).  If mass_matrix / stiffness are
+ * non-NULL they are used as given (Hydrodynamic_Solver.cpp:305-309, 346-350);
+ * otherwise M and C follow Calculate_Mass_Matrix / Calculate_Hydrostatic_
+ * Stiffness_Matrix (:300-397) from mass (0 -> Volume * 1025), cog, gyration
+ * radii and the aux waterplane mesh. */
+typedef struct {
+    double mass;
+    double cog[3];
+    double gyration[9];          /* row-major 3x3 radii of gyration */
+    const double* mass_matrix;   /* optional 6x6 row-major */
+    const double* stiffness;     /* optional 6x6 row-major */
+    const bem_mesh* aux;         /* optional interior waterplane mesh */
+} bem_body_props;
+
+/* Per-frequency outputs; every pointer may be NULL to skip that output.
+ * Layouts (f = frequency index, nb = number of headings):
+ *   A, B            [f][6][6] row-major (A = Re(AM*Phi_J), B = Im(AM*Phi_J),
+ *                   per unit density; Hydrodynamic_Solver.cpp:463-465)
+ *   FK, SC, F, RAO  [f][6][nb] complex, interleaved re,im
+ *   refine_iters    [f] refinement sweeps used (0 for BEM_PLAIN_FP64)
+ *   residual        [f] final max relative residual ||b - D x|| / ||b|| over RHS
+ *   phi_rad         N x 6 complex (radiation potentials Phi_J), last frequency
+ *   phi_scat        N x nb complex (scattering potentials Phi_S), last frequency */
+typedef struct {
+    double* A;
+    double* B;
+    double* FK;
+    double* SC;
+    double* F;
+    double* RAO;
+    int* refine_iters;
+    double* residual;
+    double* phi_rad;
+    double* phi_scat;
+} bem_result;
+
+/* ---- mesh generators (host only; no device needed) ------------------------ */
+
+/* Half_Cylinder (Volume_of_Revolution.cpp:167-199, 12-41, 92-130): radius R,
+ * draft, na azimuthal, nr radial (bottom), nv vertical panels, nrfs interior
+ * waterplane rings (0 = none), cosine spacing flag (PiCosFac, Boundary_Base.h:39). */
+int bem_mesh_cylinder_sizes(int na, int nr, int nv, int nrfs, int* n_nodes, int* n_elems, int* n_aux_nodes,
+                            int* n_aux_elems);
+int bem_mesh_cylinder(double radius, double draft, int na, int nr, int nv, int nrfs, int cosine, double* nodes,
+                      int* elems, double* aux_nodes, int* aux_elems);
+
+/* Barge (Barge.cpp:12-204): length, width, draft; nx, ny, nz panels; five faces. */
+int bem_mesh_barge_sizes(int nx, int ny, int nz, int* n_nodes, int* n_elems, int* n_aux_nodes, int* n_aux_elems);
+int bem_mesh_barge(double length, double width, double draft, int nx, int ny, int nz, int cosine, double* nodes,
+                   int* elems, double* aux_nodes, int* aux_elems);
+
+/* ---- solver context (Hydrodynamic_Radiation_Solver) ------------------------ */
+
+/* Creates a context on CUDA device `device` (replaces `new Hydrodynamic_Radiation_Solver`). */
+bem_status bem_create(bem_ctx** ctx, int device);
+/* Frees every device buffer of the context (replaces `delete Solver`). */
+void bem_destroy(bem_ctx* ctx);
+/* Message of the last failing call on this context (static storage if ctx is NULL). */
+const char* bem_last_error(const bem_ctx* ctx);
+
+/* Set_Parameters (Hydrodynamic_Solver.cpp:11-27): density `Density`, gravity
+ * `Gravity` (used by the hydrostatics only, as in the reference; the wave
+ * number uses g = 9.81, :409) and the headings `WaveAngle` in radians. */
+bem_status bem_set_params(bem_ctx* ctx, double density, double gravity, int n_beta, const double* betas);
+
+/* Setup(Boundary*) (Hydrodynamic_Solver.cpp:269-298): panel geometry, mirror
+ * panels, collocation points and the frequency-independent Rankine influence
+ * matrices (computed on the GPU in FP64).  props may be NULL. */
+bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* props);
+
+/* Set_Real + Solve (Hydrodynamic_Solver.cpp:400-487) for n_freq angular
+ * frequencies in one call.  refine_tol <= 0 selects the default 1e-12. */
+bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double refine_tol,
+                     bem_result* out);
+
+/* Panel count N and heading count of the current setup. */
+bem_status bem_get_sizes(const bem_ctx* ctx, int* n_panels, int* n_beta);
+
+/* Mass and stiffness matrices used for the RAO (6x6 row-major each), and
+ * {volume, xb, yb, zb} (Boundary_Base.cpp:177-224). */
+bem_status bem_get_body_matrices(const bem_ctx* ctx, double* mass_matrix, double* stiffness, double* vol_cob);
+
+/* ---- influence matrices (Prepare_Linear_System / _Wave_Terms) -------------- */
+
+/* Copies the Rankine kernel values of the current setup to host, N x N
+ * row-major (row = receiver, column = source): s, d for the body panels and
+ * sr, dr for the mirrored panels (Hydrodynamic_Solver.cpp:103-109 stores
+ * SSrc = -s, SSrcRefl = -sr, DSrc = d, DSrcRefl = dr).  Any pointer may be NULL. */
+bem_status bem_get_rankine(bem_ctx* ctx, double* s, double* sr, double* d, double* dr);
+
+/* Wave-term influence matrices at wave number K (Hydrodynamic_Solver.cpp:193-202
+ * without the Rankine K-term): ws, wd as N x N complex interleaved, computed in
+ * FP64 (precision = BEM_PLAIN_FP64) or FP32 (BEM_MIXED). */
+bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, double* wd);
+
+/* ---- Green function (Kernels.cpp) ------------------------------------------ */
+
+/* HavelockGF (Kernels.cpp:342-412) at n nondimensional points (x, y, v) on
+ * device `device`; out = n x 8 doubles: Re/Im of G, dG/dx, dG/dy, dG/dz.
+ * precision: BEM_PLAIN_FP64 or BEM_MIXED (FP32 arithmetic). */
+bem_status bem_havelock(int device, int n, const double* x, const double* y, const double* v, int precision,
+                        double* out);
+
+/* ---- dense complex solve ----------------------------------------------------- */
+
+/* Solves A X = B for complex A (n x n) and B (n x nrhs), both row-major
+ * interleaved, with the GPU LU of `precision` (refined to refine_tol in
+ * BEM_MIXED).  X overwrites B.  Replaces Eigen::PartialPivLU<CMatrix>
+ * compute/solve (Hydrodynamic_Solver.cpp:430, 438, 446).  The call uses the
+ * context's solver buffers and discards any previous bem_setup. */
+bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, double* B, int precision,
+                           double refine_tol, int* refine_iters, double* residual);
+
+/* Accumulated device time (ms) of bem_solve stages since the last reset:
+ * [0] incident wave + static RHS, [1] wave assembly, [2] LU factorization,
+ * [3] solves and refinement, [4] hull integrals, [5] frequency-solves counted.
+ * reset != 0 zeroes the counters after reading. */
+bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
+
+/* Library version string. */
+const char* bem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEMGPU_H */

@@ -1,0 +1,69 @@
+"""The C ABI: header declarations vs exported symbols (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "bemgpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(bem_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("bem_create", "bem_destroy", "bem_setup", "bem_solve", "bem_havelock", "bem_dense_solve"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    from bemuse_gb300 import build
+    if not os.path.exists(build.LIB):
+        try:
+            build.build()
+        except Exception as e:  # no nvcc on this machine
+            pytest.skip("library not buildable here: %s" % e)
+    lib = ctypes.CDLL(build.LIB)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_mesh_generators_match_oracle(orc):
+    import numpy as np
+    import bemuse_gb300 as bg
+    from bemuse_gb300 import build
+    if not os.path.exists(build.LIB):
+        pytest.skip("library not built")
+    m = bg.Half_Cylinder(10.0, 20.0, 16, 3, 6, 3, False)
+    o, oa = orc.cylinder(10.0, 20.0, 16, 3, 6, NRFS=3, cosine=False)
+    assert np.array_equal(m.elems, o.elems)
+    assert np.max(np.abs(m.nodes - o.nodes)) == 0.0
+    assert np.array_equal(m.aux.elems, oa.elems)
+    b = bg.Barge(30.0, 12.0, 8.0, 8, 4, 3, True)
+    ob, oba = orc.barge(30.0, 12.0, 8.0, 8, 4, 3, cosine=True)
+    assert np.array_equal(b.elems, ob.elems)
+    assert np.max(np.abs(b.nodes - ob.nodes)) == 0.0
+    assert np.max(np.abs(b.aux.nodes - oba.nodes)) == 0.0
+
+
+def test_errors_without_gpu_are_reported():
+    """bem_create on a machine without a GB300 returns an error, never aborts."""
+    import bemuse_gb300 as bg
+    from bemuse_gb300 import build
+    if not os.path.exists(build.LIB):
+        pytest.skip("library not built")
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("GPU present")
+    except ImportError:
+        pass
+    with pytest.raises(bg.BEMError) as ei:
+        bg.Hydrodynamic_Radiation_Solver()
+    assert ei.value.status in (2, 6)

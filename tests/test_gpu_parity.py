@@ -1,0 +1,168 @@
+"""GPU parity: every stage of the CUDA path against the FP64 CPU oracle.
+
+Tolerances (normwise = max|gpu - oracle| / max|oracle|):
+  HavelockGF FP64        1e-9  relative per point (CUDA j0/y0 vs libstdc++)
+  HavelockGF FP32        2e-4  relative to max(|G|, 1) per point
+  Rankine influence      1e-11 absolute (values are O(1))
+  wave influence FP64    1e-9  normwise
+  plain FP64 solve       1e-8  normwise per frequency on A, B, F, FK, SC, RAO
+  mixed solve            1e-6  normwise per frequency on A, B, F
+"""
+import numpy as np
+import pytest
+
+import cases
+from conftest import normwise
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bg():
+    import bemuse_gb300
+    bemuse_gb300.build.build()
+    return bemuse_gb300
+
+
+def _grid(n=4000, seed=0):
+    rng = np.random.default_rng(seed)
+    kr = 10 ** rng.uniform(-3, np.log10(200), n)
+    th = rng.uniform(0, 2 * np.pi, n)
+    v = -10 ** rng.uniform(-3, 2, n)
+    return kr * np.cos(th), kr * np.sin(th), v
+
+
+def test_havelock_fp64_matches_oracle(bg, orc):
+    x, y, v = _grid()
+    g = bg.havelock_gf(x, y, v, bg.PLAIN_FP64)
+    o = orc.havelock(x, y, v)
+    rel = np.abs(g - o) / np.maximum(np.abs(o), 1e-300)
+    assert np.max(rel) < 1e-9, np.max(rel)
+
+
+def test_havelock_fp32_accuracy(bg, orc):
+    x, y, v = _grid(seed=1)
+    g = bg.havelock_gf(x, y, v, bg.MIXED)
+    o = orc.havelock(x, y, v)
+    err = np.abs(g - o) / np.maximum(np.abs(o), 1.0)
+    print("fp32 HavelockGF max err", err.max(axis=0))
+    assert np.max(err) < 2e-4
+
+
+def test_havelock_branches_and_small_h(bg, orc):
+    # both Struve branches (h <= 3, h > 3) and the h <= 1e-6 guard
+    h = np.array([1e-8, 1e-7, 5e-7, 0.5, 2.999, 3.0, 3.001, 10.0, 150.0])
+    v = np.full_like(h, -0.7)
+    g = bg.havelock_gf(h, 0 * h, v, bg.PLAIN_FP64)
+    o = orc.havelock(h, 0 * h, v)
+    assert np.allclose(g, o, rtol=1e-9, atol=1e-12)
+    assert np.all(g[:3, 1] == 0) and np.all(g[:3, 2] == 0)
+
+
+def _solver(bg, mesh, betas=cases.BETAS, precision=0, gyr=cases.GYR_UNIT):
+    s = bg.Hydrodynamic_Radiation_Solver(precision=precision)
+    s.Set_Parameters([bg.Parameter("WaveAngle", b) for b in betas])
+    s.Set_Mass_Properties(mass=0.0, cog=(0, 0, 0), gyration=gyr)
+    s.Setup(mesh)
+    return s
+
+
+def test_rankine_matches_oracle(bg, orc):
+    m, _ = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL))
+    got = s.rankine()
+    ref = orc.rankine(m)[:4]
+    for a, b in zip(got, ref):
+        assert np.max(np.abs(a - b)) < 1e-11
+
+
+@pytest.mark.parametrize("K", [0.01, 0.2, 1.0])
+def test_wave_matrices_match_oracle(bg, orc, K):
+    m, _ = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL))
+    ws, wd = s.wave_matrices(K, bg.PLAIN_FP64)
+    ows, owd = orc.wave(m, K)
+    assert normwise(ws, ows) < 1e-9
+    assert normwise(wd, owd) < 1e-9
+    ws32, wd32 = s.wave_matrices(K, bg.MIXED)
+    e32 = max(normwise(ws32, ows), normwise(wd32, owd))
+    print("fp32 wave matrices normwise err", e32)
+    assert e32 < 1e-4
+
+
+def _oracle_solve(orc, mesh, aux, omegas, betas, s):
+    return orc.solve(mesh, omegas, betas, M=s.M_ij, C=s.C_ij)
+
+
+def _compare(got, ref, tol, keys=("A", "B", "F", "FK", "SC")):
+    worst = {}
+    for k in keys:
+        e = max(normwise(got[k][f], ref[k][f]) for f in range(got[k].shape[0]))
+        worst[k] = e
+    print(worst)
+    for k, e in worst.items():
+        assert e < tol, (k, e)
+
+
+def test_plain_fp64_solve_matches_oracle_cylinder(bg, orc):
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL))
+    got = s.solve_omegas(cases.OMEGAS)
+    ref = _oracle_solve(orc, m, aux, cases.OMEGAS, cases.BETAS, s)
+    _compare(got, ref, 1e-8, keys=("A", "B", "F", "FK", "SC", "RAO"))
+
+
+def test_mixed_solve_matches_oracle_cylinder(bg, orc):
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL), precision=bg.MIXED)
+    got = s.solve_omegas(cases.OMEGAS)
+    ref = _oracle_solve(orc, m, aux, cases.OMEGAS, cases.BETAS, s)
+    print("refine sweeps", got["iters"], "residual", got["residual"])
+    assert np.all(got["residual"] <= 1e-12)
+    _compare(got, ref, 1e-6)
+
+
+def test_plain_fp64_solve_matches_oracle_array(bg, orc):
+    c = cases.ARRAY_SMALL
+    om, _ = orc.cylinder(c["R"], c["draft"], c["NA"], c["NR"], c["NV"], cosine=False)
+    from oracle.oracle import Mesh as OMesh
+    omesh = OMesh.concat([om] * 4, cases.ARRAY_ORIGINS)
+    lm = bg.Half_Cylinder(c["R"], c["draft"], c["NA"], c["NR"], c["NV"], 0, False)
+    lmesh = bg.unify([lm] * 4, cases.ARRAY_ORIGINS)
+    s = _solver(bg, lmesh)
+    got = s.solve_omegas(cases.OMEGAS[:3])
+    ref = orc.solve(omesh, cases.OMEGAS[:3], cases.BETAS, M=s.M_ij, C=s.C_ij)
+    _compare(got, ref, 1e-8)
+
+
+def test_plain_fp64_solve_matches_oracle_barge(bg, orc):
+    c = cases.BARGE_SMALL
+    om, oa = orc.barge(c["L"], c["W"], c["D"], c["NX"], c["NY"], c["NZ"], cosine=c["cosine"])
+    s = _solver(bg, bg.Barge(c["L"], c["W"], c["D"], c["NX"], c["NY"], c["NZ"], c["cosine"]), betas=[0.0])
+    got = s.solve_omegas(cases.OMEGAS[1:4])
+    ref = orc.solve(om, cases.OMEGAS[1:4], [0.0], M=s.M_ij, C=s.C_ij)
+    _compare(got, ref, 1e-8)
+
+
+def test_set_real_uses_frequency_over_two_pi(bg, orc):
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL))
+    s.Set_Real(2 * np.pi * 0.8)
+    s.Solve()
+    ref = orc.solve(m, [0.8], cases.BETAS, M=s.M_ij, C=s.C_ij, want_phi=True)
+    assert normwise(s.A_ij, ref["A"][0]) < 1e-8
+    assert normwise(s.RadSolArray[-1], ref["phiJ"]) < 1e-8
+    assert normwise(s.DiffSolArray[-1], ref["phiS"]) < 1e-8
+
+
+def test_dense_solve_plain_and_mixed(bg):
+    rng = np.random.default_rng(3)
+    for n in (100, 300):
+        A = 0.5 * np.eye(n) + 0.3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+        A += np.diag(np.sign(rng.standard_normal(n)) * 0.0)
+        B = rng.standard_normal((n, 5)) + 1j * rng.standard_normal((n, 5))
+        ref = np.linalg.solve(A, B)
+        x, _, _ = bg.dense_solve(A, B, bg.PLAIN_FP64)
+        assert normwise(x, ref) < 1e-11
+        x, it, res = bg.dense_solve(A, B, bg.MIXED)
+        assert res <= 1e-12 and normwise(x, ref) < 1e-10
