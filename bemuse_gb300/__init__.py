@@ -82,6 +82,8 @@ def lib():
         "bem_havelock": ([c_int, c_int, _dp, _dp, _dp, c_int, _dp], c_int),
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
+        "bem_launch_count": ([], ctypes.c_ulonglong),
+        "bem_selftest_tc": ([c_int, c_int], c_double),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -337,6 +339,16 @@ def havelock_gf(x, y, v, precision=PLAIN_FP64, device=0):
     out = np.zeros((x.size, 8))
     _check(lib().bem_havelock(int(device), x.size, _p(x), _p(y), _p(v), int(precision), _p(out)))
     return out[:, 0::2] + 1j * out[:, 1::2]
+
+
+def launch_count():
+    """Kernel launches issued by libbemgpu.so in this process."""
+    return int(lib().bem_launch_count())
+
+
+def selftest_tc(n=1024, device=0):
+    """Tensor-core trailing update vs the FP32 CUDA-core update (relative max diff)."""
+    return float(lib().bem_selftest_tc(int(device), int(n)))
 
 
 def dense_solve(A, B, precision=PLAIN_FP64, refine_tol=1e-12, device=0):

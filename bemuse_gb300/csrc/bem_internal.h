@@ -6,6 +6,10 @@
 
 namespace bem {
 
+// Count of kernel launches issued by this library (all contexts).
+extern unsigned long long g_launches;
+#define BEM_LAUNCH(...) (++::bem::g_launches, __VA_ARGS__)
+
 constexpr int RK_STRIDE = 32;   // doubles per Rankine panel record
 constexpr int MAX_RHS = 16;     // 6 radiation + up to 10 headings
 constexpr int MAX_BETA = MAX_RHS - 6;
@@ -16,6 +20,7 @@ enum DevFlag : int {
     FLAG_PIVOT = 1,      // a multiplier |l_ik| > 1: partial pivoting would exchange rows
     FLAG_ZERO_PIVOT = 2, // a zero (or non-finite) pivot
     FLAG_NONFINITE = 4,  // non-finite residual
+    FLAG_TIMEOUT = 8,    // a bounded device-side wait expired (kernel abandoned its tile)
 };
 
 struct WaveArgs {
@@ -31,6 +36,11 @@ struct WaveArgs {
     double* D64r; double* D64i;   // [ld][ld]
     float* D32r; float* D32i;     // [ld][ld] or null
     double* ws_out; double* wd_out;
+    // mixed mode only
+    const float* xr32;    // collocation points, hi/lo split: [6][N] (xh, yh, zh, xl, yl, zl)
+    const float* gq32;    // Gauss data [10][4][N]: xh, yh, zh, w, nx, ny, nz, xl, yl, zl
+    const double* cst;    // per-source FP64 leading imaginary parts [6][N]: alpha, beta, gamma, dx, dy, dz
+    double P[6], Q[6];    // sum_s alpha_s N_k(s, j), sum_s beta_s N_k(s, j)
 };
 
 cudaError_t upload_poly_constants(int device);
@@ -61,10 +71,11 @@ struct LUWork;  // opaque workspace (host_api.cpp)
 // Blocked LU without row exchanges of the n x n (n % nb == 0) planar matrix;
 // diagonal-block inverses go to inv (re/im, [n/nb][2][nb][nb]: L^-1 then U^-1).
 // tc = true uses the tcgen05 TF32 trailing update (float only).
-void lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
-                   int* flags);
-void lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
-                   float* wut, int* flags, bool tc);
+// Returns 0 on success, nonzero if the tensor-core path could not be set up.
+int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
+                  int* flags);
+int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
+                  float* wut, int* flags, bool tc);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place.
 void lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X);
 void lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X);
@@ -77,5 +88,8 @@ void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
 
 int tc_gemm_supported(int device);
+// C -= L U^T-trailing update on random data with the tensor-core and SIMT kernels;
+// returns max |tc - simt| / max |simt| (negative on setup failure).
+double tc_selftest(int device, int n);
 
 }  // namespace bem

@@ -204,4 +204,96 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     Gh.im = E * j1v;
 }
 
+// ---- FP32 real parts + imaginary-part remainders ----------------------------
+// Real parts of G and dG/dh (as gf32 computes them).
+__device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float& Gr, float& Ghr) {
+    const float PI = 3.14159265358979f;
+    const float EUL = 0.5772156649f;
+    float dd = sqrtf(fmaf(hh, hh, vv * vv));
+    float inv_d = 1.0f / dd;
+    float alpha = -vv * inv_d;
+    float beta = hh * inv_d;
+    float rho = dd / (1.0f + dd);
+    float u = rho - 0.5f;
+    float d2 = dd * dd;
+    float d3 = d2 * dd;
+    float inv_1d3 = 1.0f / (1.0f + d3);
+    float dmv = dd - vv;
+    float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
+    PP = fmaf(PP, ev, d2 - vv);
+    float A = horner32(P.A, 10, u), B = horner32(P.B, 10, u);
+    float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
+    float omr = 1.0f - rho;
+    float RR = (1.0f - beta) * A - beta * B;
+    RR -= alpha * C / fmaf(6.0f * alpha * rho, omr, 1.0f);
+    RR = fmaf(beta * (1.0f - beta), D, RR);
+    float r3 = rho * (omr * omr * omr);
+    float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
+    bool far = hh > 3.0f;
+    float y0v = far ? y0f(hh) : 0.0f, y1v = far ? y1f(hh) : 0.0f;
+    float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
+    float E = 2.0f * PI * ev;
+    Gr = fmaf(E, H0, L0);
+    float PS = (beta + hh) / dmv;
+    PS -= 2.0f * beta;
+    PS = fmaf(2.0f * dd, ev, PS);
+    PS -= hh;
+    float QS = expf(-dd) * (1.0f - beta);
+    QS *= 1.0f + dd * inv_1d3;
+    float a2 = horner32(P.dA, 10, u), b2 = horner32(P.dB, 10, u), c2 = horner32(P.dC, 6, u);
+    float RS = beta * a2 - (1.0f - alpha) * b2;
+    RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
+    float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);
+    Ghr = fmaf(E, 0.636619772f - H1, Ls);
+}
+
+// Imaginary parts: Im G = -2 pi e^v J0(h), Im dG/dh = 2 pi e^v J1(h).  With
+// a0 = e^v J0(h) and a1 = e^v J1(h)/h, return the remainders
+//   r0 = a0 - (1 + v),   r1 = a1 - 1/2,
+// which are O((|v| + h)^2); the separable leading parts 1 + v and 1/2 are
+// summed exactly in FP64 by the caller.  Small arguments use the power series
+// of expm1, J0 - 1 and J1(h)/h - 1/2 so the remainders keep FP32 relative
+// accuracy (the leading parts would otherwise cancel them).
+__device__ __forceinline__ void im_remainders(float hh, float vv, float& r0, float& r1) {
+    float em1 = expm1f(vv);
+    float em2;  // e^v - 1 - v
+    if (vv > -0.5f) {
+        em2 = vv * vv * fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, 2.7557319e-6f, 2.4801587e-5f),
+              1.9841270e-4f), 1.3888889e-3f), 8.3333333e-3f), 4.1666667e-2f), 0.16666667f), 0.5f);
+    } else {
+        em2 = em1 - vv;
+    }
+    float j0m1, j1h, j1hm;
+    if (hh < 2.0f) {
+        float q = 0.25f * hh * hh;
+        // J0 - 1 = sum_{k>=1} (-q)^k/(k!)^2 ;  J1/h - 1/2 = (1/2) sum_{k>=1} (-q)^k/(k!(k+1)!)
+        float t0 = fmaf(-q * (1.0f / 81.0f), 1.0f, 1.0f);
+        t0 = fmaf(-q * (1.0f / 64.0f), t0, 1.0f);
+        t0 = fmaf(-q * (1.0f / 49.0f), t0, 1.0f);
+        t0 = fmaf(-q * (1.0f / 36.0f), t0, 1.0f);
+        t0 = fmaf(-q * (1.0f / 25.0f), t0, 1.0f);
+        t0 = fmaf(-q * (1.0f / 16.0f), t0, 1.0f);
+        t0 = fmaf(-q * (1.0f / 9.0f), t0, 1.0f);
+        t0 = fmaf(-q * 0.25f, t0, 1.0f);
+        j0m1 = -q * t0;
+        float t1 = fmaf(-q * (1.0f / 90.0f), 1.0f, 1.0f);
+        t1 = fmaf(-q * (1.0f / 72.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 56.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 42.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 30.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 20.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 12.0f), t1, 1.0f);
+        t1 = fmaf(-q * (1.0f / 6.0f), t1, 1.0f);
+        j1hm = -0.25f * q * t1;
+        j1h = 0.5f + j1hm;
+    } else {
+        float j0v = j0f(hh), j1v = j1f(hh);
+        j0m1 = j0v - 1.0f;
+        j1h = j1v / hh;
+        j1hm = j1h - 0.5f;
+    }
+    r0 = em2 + fmaf(em1, j0m1, j0m1);
+    r1 = fmaf(em1, j1h, j1hm);
+}
+
 }  // namespace bem

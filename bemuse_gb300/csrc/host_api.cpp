@@ -25,6 +25,8 @@
 #include "host_geom.h"
 
 using bem::CMat;
+
+unsigned long long bem::g_launches = 0;
 using cplx = std::complex<double>;
 
 struct bem_ctx {
@@ -51,6 +53,12 @@ struct bem_ctx {
     float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
     int* d_flags = nullptr;
     unsigned long long* d_norms = nullptr;
+    // mixed-precision wave assembly
+    float *d_xr32 = nullptr, *d_gq32 = nullptr;
+    double* d_cst = nullptr;
+    double* h_cst = nullptr;          // pinned, 6 N
+    std::vector<double> csum;         // per-source Gauss sums [8][N]
+    double cst_P[6], cst_Q[6];
     std::vector<void*> allocs;
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
@@ -109,7 +117,50 @@ void free_all(bem_ctx* ctx) {
     ctx->d_nq = nullptr;
     ctx->d_flags = nullptr;
     ctx->d_norms = nullptr;
+    ctx->d_xr32 = nullptr;
+    ctx->d_gq32 = nullptr;
+    ctx->d_cst = nullptr;
+    if (ctx->h_cst) cudaFreeHost(ctx->h_cst);
+    ctx->h_cst = nullptr;
     ctx->ready = false;
+}
+
+// Leading (separable) imaginary parts of the wave influence at wave number K for
+// the mixed kernel, from the frequency-independent per-source Gauss sums
+//   Cs = sum w, Cz = sum w z, Cnx = sum w nx, Cxnx = sum w x nx, Cny = sum w ny,
+//   Cyny = sum w y ny, Cnz = sum w nz, Cznz = sum w z nz   (mirrored panel s).
+// Im ws(r,s) = alpha_s + beta_s z_r + ...,  Im wd(r,s) = gamma_s + dx_s x_r + dy_s y_r + dz_s z_r + ...
+bem_status upload_wave_constants(bem_ctx* ctx, double K) {
+    const int N = ctx->N;
+    const double pi = 3.14159265358979323846;
+    const double c1 = K * 0.25 / pi, c2 = K * K * 0.25 / pi;
+    const double t1 = 2.0 * pi * c1, t2 = 2.0 * pi * c2;
+    const double* C = ctx->csum.data();
+    double* h = ctx->h_cst;
+    for (int j = 0; j < 6; ++j) { ctx->cst_P[j] = 0.0; ctx->cst_Q[j] = 0.0; }
+    for (int s = 0; s < N; ++s) {
+        double Cs = C[s], Cz = C[N + s], Cnx = C[2 * N + s], Cxnx = C[3 * N + s];
+        double Cny = C[4 * N + s], Cyny = C[5 * N + s], Cnz = C[6 * N + s], Cznz = C[7 * N + s];
+        double al = -t1 * (Cs - K * Cz), be = -t1 * K * Cs;
+        h[s] = al;
+        h[N + s] = be;
+        h[2 * N + s] = t2 * (-0.5 * K * (Cxnx + Cyny) - Cnz + K * Cznz);
+        h[3 * N + s] = t2 * 0.5 * K * Cnx;
+        h[4 * N + s] = t2 * 0.5 * K * Cny;
+        h[5 * N + s] = -t2 * K * Cnz;
+        const double* nk = &ctx->Nk[(size_t)s * 6];
+        for (int j = 0; j < 6; ++j) { ctx->cst_P[j] += al * nk[j]; ctx->cst_Q[j] += be * nk[j]; }
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->d_cst, h, sizeof(double) * 6 * (size_t)N, cudaMemcpyHostToDevice, ctx->st);
+    if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("constants upload: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+void fill_mixed_args(bem_ctx* ctx, bem::WaveArgs& a) {
+    a.xr32 = ctx->d_xr32;
+    a.gq32 = ctx->d_gq32;
+    a.cst = ctx->d_cst;
+    for (int j = 0; j < 6; ++j) { a.P[j] = ctx->cst_P[j]; a.Q[j] = ctx->cst_Q[j]; }
 }
 
 int round_up(int n, int a) { return (n + a - 1) / a * a; }
@@ -188,8 +239,9 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
     } else {
         CMat<float> A{ctx->d_D32r, ctx->d_D32i, Np};
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
-        bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32, ctx->d_wut32,
-                           ctx->d_flags, tc);
+        if (bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32, ctx->d_wut32,
+                               ctx->d_flags, tc) != 0)
+            return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[3], st));
         // x0 = LU^-1 y
@@ -237,6 +289,8 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
     *t_solve += ms;
     if (iters_out) *iters_out = iters;
     if (resid_out) *resid_out = resid;
+    if (hflags & bem::FLAG_TIMEOUT)
+        return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the tensor-core LU update expired");
     if (hflags & bem::FLAG_ZERO_PIVOT) return fail(ctx, BEM_ERR_NUMERIC, "zero or non-finite pivot in the LU");
     if (hflags & bem::FLAG_PIVOT)
         return fail(ctx, BEM_ERR_NUMERIC,
@@ -249,6 +303,10 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
 extern "C" {
 
 const char* bem_version(void) { return "bemgpu 0.1 (sm_103a)"; }
+
+unsigned long long bem_launch_count(void) { return bem::g_launches; }
+
+double bem_selftest_tc(int device, int n) { return bem::tc_selftest(device, n); }
 
 const char* bem_last_error(const bem_ctx* ctx) { return ctx ? ctx->err.c_str() : g_static_err; }
 
@@ -375,6 +433,33 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
         nk[5] = c[0] * n[1] - c[1] * n[0];
     }
     bem::collocation_points(body, xr);
+    // FP32 hi/lo copies for the mixed wave kernel and the per-source Gauss sums
+    std::vector<float> xr32((size_t)6 * N), gq32((size_t)10 * 4 * N, 0.0f);
+    for (int i = 0; i < N; ++i)
+        for (int d = 0; d < 3; ++d) {
+            double v = xr[(size_t)d * N + i];
+            float hi = (float)v;
+            xr32[(size_t)d * N + i] = hi;
+            xr32[(size_t)(3 + d) * N + i] = (float)(v - (double)hi);
+        }
+    ctx->csum.assign((size_t)8 * N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        const bem::PanelGeom& p = mirror[i];
+        for (int q = 0; q < p.nq; ++q) {
+            double x = p.qp[3 * q], y = p.qp[3 * q + 1], z = p.qp[3 * q + 2], w = p.qw[q];
+            double nx = p.qn[3 * q], ny = p.qn[3 * q + 1], nz = p.qn[3 * q + 2];
+            double f[7] = {x, y, z, w, nx, ny, nz};
+            for (int k = 0; k < 3; ++k) {
+                float hi = (float)f[k];
+                gq32[((size_t)k * 4 + q) * N + i] = hi;
+                gq32[((size_t)(7 + k) * 4 + q) * N + i] = (float)(f[k] - (double)hi);
+            }
+            for (int k = 3; k < 7; ++k) gq32[((size_t)k * 4 + q) * N + i] = (float)f[k];
+            double* C = ctx->csum.data();
+            C[i] += w; C[N + i] += w * z; C[2 * N + i] += w * nx; C[3 * N + i] += w * x * nx;
+            C[4 * N + i] += w * ny; C[5 * N + i] += w * y * ny; C[6 * N + i] += w * nz; C[7 * N + i] += w * z * nz;
+        }
+    }
     // mass properties
     double cog[3] = {0, 0, 0}, gyr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, mass = 0;
     std::vector<bem::PanelGeom> auxb, auxm;
@@ -416,7 +501,13 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_dphiI, 2 * (size_t)N * std::max(NB, 1));
     DA(ctx->d_part, 2 * (size_t)((N + 255) / 256) * (36 + 12 * NB));
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
+    DA(ctx->d_xr32, xr32.size());
+    DA(ctx->d_gq32, gq32.size());
+    DA(ctx->d_cst, 6 * (size_t)N);
+    CK(cudaMallocHost(&ctx->h_cst, sizeof(double) * 6 * (size_t)N));
     cudaStream_t st = ctx->st;
+    CK(cudaMemcpyAsync(ctx->d_xr32, xr32.data(), xr32.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_gq32, gq32.data(), gq32.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_gq, gq.data(), gq.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
@@ -494,6 +585,11 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.RD = ctx->d_RD; a.RSR = ctx->d_RSR;
         a.Bm = ctx->d_Bm; a.Y = ctx->d_Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
         a.D32r = mixed ? ctx->d_D32r : nullptr; a.D32i = mixed ? ctx->d_D32i : nullptr;
+        if (mixed) {
+            s = upload_wave_constants(ctx, K);
+            if (s != BEM_OK) return s;
+            fill_mixed_args(ctx, a);
+        }
         bem::launch_wave(st, a, mixed);
         bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, mixed ? ctx->d_D32r : nullptr,
                                  mixed ? ctx->d_D32i : nullptr);
@@ -604,6 +700,11 @@ bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, 
     a.N = N; a.ld = N; a.R = ctx->R; a.mode = 1; a.K = K;
     a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.Bm = ctx->d_Bm;
     a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
+    if (precision == BEM_MIXED) {
+        bem_status s = upload_wave_constants(ctx, K);
+        if (s != BEM_OK) { cudaFree(buf); return s; }
+        fill_mixed_args(ctx, a);
+    }
     bem::launch_wave(ctx->st, a, precision == BEM_MIXED);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(ws, buf, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, ctx->st);

@@ -113,6 +113,7 @@ __device__ __forceinline__ void wave_pair(const WaveArgs& a, int s, double X, do
     const T c1 = (T)(a.K * kFourPIinv);
     const T c2 = (T)(a.K * a.K * kFourPIinv);
     wsr = wsi = wdr = wdi = (T)0;
+    if (a.K == 0.0) return;  // FreeSurface_Wave_Kernel returns zero for K == 0 (Panel.cpp:607-614)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         if (q < nq) {
@@ -191,6 +192,112 @@ __global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
             if (lane == 0) {
                 a.Y[2 * ((size_t)r * R + j)] += (double)vr;
                 a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K2, mixed precision.  Real parts of G and dG in FP32.  Imaginary parts
+// split as  a0 = e^v J0(h) = 1 + v + r0  and  a1 = e^v J1(h)/h = 1/2 + r1:
+// the leading parts are separable in (receiver, source) and enter through the
+// per-source FP64 constants cst (alpha..dz) and P, Q; only the O((Kr)^2)
+// remainders r0, r1 are evaluated and summed in FP32.  This keeps the
+// imaginary parts accurate to FP64-level relative error at low K, where the
+// radiation damping is a small difference of O(K) imaginary terms.
+__global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= a.N) return;
+    const int N = a.N, R = a.R;
+    const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
+    const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
+    const double Xr = a.xr[r], Yr = a.xr[N + r], Zr = a.xr[2 * N + r];
+    const float K = (float)a.K;
+    const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
+    const double tpc1 = 2.0 * 3.14159265358979323846 * a.K * kFourPIinv;
+    const double tpc2 = tpc1 * a.K;
+    float acc_re[MAX_RHS], acc_im[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
+    const size_t row = (size_t)r * a.ld;
+    const bool live = a.K != 0.0;
+    for (int s = lane; s < N; s += 32) {
+        float wsr = 0.f, wdr = 0.f, S0 = 0.f, S1 = 0.f;
+        const int nq = live ? a.nq[s] : 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (q < nq) {
+                const float* g = a.gq32 + (size_t)q * N + s;  // field stride 4N
+                const size_t fs = (size_t)4 * N;
+                float dx = (xh - g[0]) + (xl - g[7 * fs]);
+                float dy = (yh - g[fs]) + (yl - g[8 * fs]);
+                float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
+                float w = g[3 * fs], nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
+                float XX = dx * K, YY = dy * K, VV = dz * K;
+                float hh = sqrtf(fmaf(XX, XX, YY * YY));
+                float ev = expf(VV);
+                float Gr, Ghr, r0, r1;
+                gf32_re(c_poly32, hh, VV, ev, Gr, Ghr);
+                im_remainders(hh, VV, r0, r1);
+                float proj = fmaf(XX, nx, YY * ny);
+                float dgr = 0.f;
+                if (hh > 1.0e-6f) dgr = Ghr * proj / hh;
+                else r1 = -0.5f;  // the reference sets dG/dx = dG/dy = 0 there
+                wsr = fmaf(w * c1, Gr, wsr);
+                wdr = fmaf(w * c2, fmaf(Gr, nz, dgr), wdr);
+                S0 = fmaf(w, r0, S0);
+                S1 = fmaf(w, fmaf(r1, proj, -r0 * nz), S1);
+            }
+        }
+        const double* cs = a.cst + s;
+        double wsi = live ? fma(cs[N], Zr, cs[0]) - tpc1 * (double)S0 : 0.0;
+        double wdi = live ? fma(cs[5 * N], Zr, fma(cs[4 * N], Yr, fma(cs[3 * N], Xr, cs[2 * (size_t)N]))) +
+                                tpc2 * (double)S1
+                          : 0.0;
+        if (a.mode == 1) {
+            size_t o = 2 * ((size_t)r * N + s);
+            a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = wsi;
+            a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = wdi;
+            continue;
+        }
+        double dre = a.RD[row + s] + fma(a.RSR[row + s], a.K, (double)wdr);
+        a.D64r[row + s] = dre;
+        a.D64i[row + s] = wdi;
+        a.D32r[row + s] = (float)dre;
+        a.D32i[row + s] = (float)wdi;
+        const double* b = a.Bm + (size_t)s * 2 * R;
+        const float wsi32 = (float)wsi;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            float br = (float)b[2 * j];
+            acc_re[j] = fmaf(-wsr, br, acc_re[j]);
+            acc_im[j] = fmaf(S0, br, acc_im[j]);
+        }
+#pragma unroll
+        for (int j = 6; j < MAX_RHS; ++j) {
+            if (j < R) {
+                float br = (float)b[2 * j], bi = (float)b[2 * j + 1];
+                acc_re[j] -= wsr * br - wsi32 * bi;
+                acc_im[j] -= wsr * bi + wsi32 * br;
+            }
+        }
+    }
+    if (a.mode == 1) return;
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            float vr = acc_re[j], vi = acc_im[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {
+                double add_im = j < 6 ? tpc1 * (double)vi - fma(Zr, a.Q[j], a.P[j]) : (double)vi;
+                if (!live) add_im = 0.0;
+                a.Y[2 * ((size_t)r * R + j)] += (double)vr;
+                a.Y[2 * ((size_t)r * R + j) + 1] += add_im;
             }
         }
     }
@@ -403,44 +510,44 @@ cudaError_t upload_poly_constants(int device) {
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
                     double* o0, double* o1, double* o2, double* o3) {
     dim3 blk(32, 8), grd((N + 31) / 32, (N + 7) / 8);
-    k_rankine<<<grd, blk, 0, st>>>(N, ld, rec, xr, rn, mode, o0, o1, o2, o3);
+    BEM_LAUNCH(k_rankine<<<grd, blk, 0, st>>>(N, ld, rec, xr, rn, mode, o0, o1, o2, o3));
 }
 
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
     dim3 grd((a.N + 7) / 8);
-    if (fp32) k_wave<float><<<grd, 256, 0, st>>>(a);
-    else k_wave<double><<<grd, 256, 0, st>>>(a);
+    if (fp32) BEM_LAUNCH(k_wave_mixed<<<grd, 256, 0, st>>>(a));
+    else BEM_LAUNCH(k_wave<double><<<grd, 256, 0, st>>>(a));
 }
 
 void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i) {
     if (ld <= N) return;
-    k_pad_identity<<<1024, 256, 0, st>>>(N, ld, D64r, D64i, D32r, D32i);
+    BEM_LAUNCH(k_pad_identity<<<1024, 256, 0, st>>>(N, ld, D64r, D64i, D32r, D32i));
 }
 
 void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
                      double* Bm) {
-    k_incident<<<(N + 127) / 128, 128, 0, st>>>(N, NB, R, betas, K, Omega, cen, nrm, area, phiI, dphiI, Bm);
+    BEM_LAUNCH(k_incident<<<(N + 127) / 128, 128, 0, st>>>(N, NB, R, betas, K, Omega, cen, nrm, area, phiI, dphiI, Bm));
 }
 
 void launch_rhs_static(cudaStream_t st, int N, int ld, int R, int j0, int j1, const double* RS, const double* Bm,
                        double* Y) {
-    k_rhs_static<<<(N + 7) / 8, 256, 0, st>>>(N, ld, R, j0, j1, RS, Bm, Y);
+    BEM_LAUNCH(k_rhs_static<<<(N + 7) / 8, 256, 0, st>>>(N, ld, R, j0, j1, RS, Bm, Y));
 }
 
 void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
                  const double* phiI, const double* dphiI, double* part, double* out) {
     int nblk = (N + 255) / 256;
     int nout = 36 + 12 * NB;
-    k_post_partial<<<nblk, 256, 0, st>>>(N, NB, R, X, Nk, area, phiI, dphiI, part);
-    k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out);
+    BEM_LAUNCH(k_post_partial<<<nblk, 256, 0, st>>>(N, NB, R, X, Nk, area, phiI, dphiI, part));
+    BEM_LAUNCH(k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out));
 }
 
 void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,
                      bool fp32) {
     int g = (n + 127) / 128;
-    if (fp32) k_havelock<float><<<g, 128, 0, st>>>(n, x, y, v, out);
-    else k_havelock<double><<<g, 128, 0, st>>>(n, x, y, v, out);
+    if (fp32) BEM_LAUNCH(k_havelock<float><<<g, 128, 0, st>>>(n, x, y, v, out));
+    else BEM_LAUNCH(k_havelock<double><<<g, 128, 0, st>>>(n, x, y, v, out));
 }
 
 }  // namespace bem

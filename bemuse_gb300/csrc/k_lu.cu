@@ -16,10 +16,12 @@
 // Solves use the stored off-diagonal blocks and the diagonal-block inverses.
 #include "bem_internal.h"
 #include <cstdio>
+#include <cstring>
 
 namespace bem {
 
-void tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut);
+bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
+                        int* flags);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -214,20 +216,16 @@ __global__ void k_copy_back(int rows, int cols, const T* wr, const T* wi, int wl
 }
 
 template <typename T, int NB>
-static void lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
-                        bool tc) {
+static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
+                       bool tc) {
     const size_t smem = (size_t)(2 * NB * (NB + 1) + 2 * NB) * sizeof(T);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_lu_diag<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    cudaFuncSetAttribute(k_lu_diag<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // workspaces: wl [2][n][NB] (L21), wu [2][NB][n] (U12), wut [2][n][NB] (U12^T)
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
     T* wur = wu; T* wui = wu + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
     for (int k0 = 0; k0 < n; k0 += NB) {
-        k_lu_diag<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags);
+        BEM_LAUNCH(k_lu_diag<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
         if (rem <= 0) break;
         const int blk = k0 / NB;
@@ -238,30 +236,98 @@ static void lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* 
         CMat<T> WL{wlr, wli, NB};
         CMat<T> WU{wur, wui, rem};
         // L21 = A21 U^-1  (rem x NB),  U12 = L^-1 A12  (NB x rem)
-        k_cgemm<T><<<dim3(NB / 64, rem / 64), 256, 0, st>>>(rem, NB, NB, A21, Uinv, WL, (T)1, 0);
-        k_cgemm<T><<<dim3(rem / 64, NB / 64), 256, 0, st>>>(NB, rem, NB, Linv, A12, WU, (T)1, 0);
+        BEM_LAUNCH(k_cgemm<T><<<dim3(NB / 64, rem / 64), 256, 0, st>>>(rem, NB, NB, A21, Uinv, WL, (T)1, 0));
+        BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, NB / 64), 256, 0, st>>>(NB, rem, NB, Linv, A12, WU, (T)1, 0));
         int nblk = (int)(((size_t)rem * NB + 255) / 256);
         if (nblk > 4096) nblk = 4096;
-        k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 1, (T*)nullptr, (T*)nullptr, 0,
-                                             flags);
-        k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, wur, wui, rem, A, k0, k0 + NB, 0, wtr, wti, NB, flags);
+        BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 1, (T*)nullptr,
+                                                        (T*)nullptr, 0, flags));
+        BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, wur, wui, rem, A, k0, k0 + NB, 0, wtr, wti, NB, flags));
         CMat<T> A22{A.re + (size_t)(k0 + NB) * A.ld + k0 + NB, A.im + (size_t)(k0 + NB) * A.ld + k0 + NB, A.ld};
         if (tc) {
-            tc_trailing_update(st, n, k0, NB, *reinterpret_cast<CMat<float>*>(&A), reinterpret_cast<const float*>(wl),
-                               reinterpret_cast<const float*>(wut));
+            if (!tc_trailing_update(st, n, k0, NB, *reinterpret_cast<CMat<float>*>(&A),
+                                    reinterpret_cast<const float*>(wl), reinterpret_cast<const float*>(wut), flags))
+                return 1;
         } else {
-            k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, WU, A22, (T)-1, 1);
+            BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, WU, A22, (T)-1, 1));
         }
     }
+    return 0;
 }
 
-void lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
-                   int* flags) {
-    lu_factor_t<double, 64>(st, n, A, invr, invi, wl, wu, nullptr, flags, false);
+int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
+                  int* flags) {
+    return lu_factor_t<double, 64>(st, n, A, invr, invi, wl, wu, nullptr, flags, false);
 }
-void lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu, float* wut,
-                   int* flags, bool tc) {
-    lu_factor_t<float, 128>(st, n, A, invr, invi, wl, wu, wut, flags, tc);
+int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu, float* wut,
+                  int* flags, bool tc) {
+    return lu_factor_t<float, 128>(st, n, A, invr, invi, wl, wu, wut, flags, tc);
+}
+
+// Self-test of the tensor-core trailing update: A22 -= L21 U12 on random data
+// (n x n, nb = 128, one step k0 = 0) with the tcgen05 kernel and with the SIMT
+// kernel; returns max |tc - simt| / max |simt|.
+__global__ void k_fill_random(size_t n, float* x, unsigned seed) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        unsigned h = (unsigned)(i * 2654435761u) ^ seed;
+        h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+        x[i] = ((float)(h & 0xffffff) / 16777216.0f) - 0.5f;
+    }
+}
+__global__ void k_maxdiff(size_t n, const float* a, const float* b, unsigned long long* out) {
+    float m = 0.f, r = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        m = fmaxf(m, fabsf(a[i] - b[i]));
+        r = fmaxf(r, fabsf(b[i]));
+    }
+    atomicMax(out, (unsigned long long)__float_as_uint(m));
+    atomicMax(out + 1, (unsigned long long)__float_as_uint(r));
+}
+
+double tc_selftest(int device, int n) {
+    if (cudaSetDevice(device) != cudaSuccess || n % 128 != 0 || n < 256) return -1.0;
+    const int NB = 128, rem = n - NB;
+    size_t nn = (size_t)n * n;
+    float *A1 = nullptr, *A2 = nullptr, *wl = nullptr, *wu = nullptr, *wut = nullptr;
+    unsigned long long* d = nullptr;
+    int* flags = nullptr;
+    double result = -1.0;
+    if (cudaMalloc(&A1, 2 * nn * 4) || cudaMalloc(&A2, 2 * nn * 4) || cudaMalloc(&wl, 2 * (size_t)n * NB * 4) ||
+        cudaMalloc(&wu, 2 * (size_t)n * NB * 4) || cudaMalloc(&wut, 2 * (size_t)n * NB * 4) ||
+        cudaMalloc(&d, 16) || cudaMalloc(&flags, 4)) {
+        cudaGetLastError();
+    } else {
+        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * nn, A1, 12345u));
+        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * (size_t)n * NB, wl, 777u));
+        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * (size_t)n * NB, wu, 999u));
+        cudaMemcpy(A2, A1, 2 * nn * 4, cudaMemcpyDeviceToDevice);
+        cudaMemset(d, 0, 16);
+        cudaMemset(flags, 0, 4);
+        // U12^T for the tensor-core operand
+        CMat<float> A{A1, A1 + nn, n};
+        BEM_LAUNCH(k_copy_back<float><<<1024, 256>>>(NB, rem, wu, wu + (size_t)n * NB, rem, A, 0, NB, 0, wut,
+                                                     wut + (size_t)n * NB, NB, flags));
+        cudaMemcpy(A2, A1, 2 * nn * 4, cudaMemcpyDeviceToDevice);
+        CMat<float> WL{wl, wl + (size_t)n * NB, NB}, WU{wu, wu + (size_t)n * NB, rem};
+        CMat<float> C1{A1 + (size_t)NB * n + NB, A1 + nn + (size_t)NB * n + NB, n};
+        BEM_LAUNCH(k_cgemm<float><<<dim3(rem / 64, rem / 64), 256>>>(rem, rem, NB, WL, WU, C1, -1.0f, 1));
+        CMat<float> B2{A2, A2 + nn, n};
+        bool ok = tc_trailing_update(0, n, 0, NB, B2, wl, wut, flags);
+        BEM_LAUNCH(k_maxdiff<<<1024, 256>>>(2 * nn, A2, A1, d));
+        unsigned long long h[2] = {0, 0};
+        int hf = 0;
+        cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&hf, flags, 4, cudaMemcpyDeviceToHost);
+        if (ok && cudaGetLastError() == cudaSuccess && !(hf & FLAG_TIMEOUT)) {
+            unsigned a = (unsigned)h[0], b = (unsigned)h[1];
+            float fa, fb;
+            memcpy(&fa, &a, 4);
+            memcpy(&fb, &b, 4);
+            result = fb > 0 ? (double)fa / fb : (double)fa;
+        }
+    }
+    cudaFree(A1); cudaFree(A2); cudaFree(wl); cudaFree(wu); cudaFree(wut); cudaFree(d); cudaFree(flags);
+    return result;
 }
 
 // ---------------------------------------------------------------------------
@@ -346,15 +412,15 @@ static void lu_solve_t(cudaStream_t st, int n, CMat<T> A, const T* invr, const T
     const int nblk = n / NB;
     // forward: tmp = L^-1 X  (X updated in place below the current block)
     for (int b = 0; b < nblk; ++b) {
-        k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 0, X, tmp);
+        BEM_LAUNCH(k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 0, X, tmp));
         int r0 = (b + 1) * NB;
-        if (r0 < n) k_trsv_update<T, NB><<<(n - r0 + 7) / 8, 256, 0, st>>>(b, r0, n, R, A, tmp, X);
+        if (r0 < n) BEM_LAUNCH(k_trsv_update<T, NB><<<(n - r0 + 7) / 8, 256, 0, st>>>(b, r0, n, R, A, tmp, X));
     }
     // backward: X = U^-1 tmp  (tmp updated in place above the current block)
     for (int b = nblk - 1; b >= 0; --b) {
-        k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 1, tmp, X);
+        BEM_LAUNCH(k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 1, tmp, X));
         int r1 = b * NB;
-        if (r1 > 0) k_trsv_update<T, NB><<<(r1 + 7) / 8, 256, 0, st>>>(b, 0, r1, R, A, X, tmp);
+        if (r1 > 0) BEM_LAUNCH(k_trsv_update<T, NB><<<(r1 + 7) / 8, 256, 0, st>>>(b, 0, r1, R, A, X, tmp));
     }
 }
 
@@ -434,16 +500,16 @@ __global__ void k_pad_rhs(int N, int Np, int R, double* X) {
 
 void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
                      const double* Y, double* Rres, unsigned long long* nrm) {
-    k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres, nrm);
+    BEM_LAUNCH(k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres, nrm));
 }
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst) {
-    k_to_f32<<<1024, 256, 0, st>>>(n, src, dst);
+    BEM_LAUNCH(k_to_f32<<<1024, 256, 0, st>>>(n, src, dst));
 }
 void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst) {
-    k_add_f32<<<1024, 256, 0, st>>>(n, src, dst);
+    BEM_LAUNCH(k_add_f32<<<1024, 256, 0, st>>>(n, src, dst));
 }
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X) {
-    if (Np > N) k_pad_rhs<<<256, 256, 0, st>>>(N, Np, R, X);
+    if (Np > N) BEM_LAUNCH(k_pad_rhs<<<256, 256, 0, st>>>(N, Np, R, X));
 }
 
 }  // namespace bem

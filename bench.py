@@ -1,0 +1,320 @@
+"""Benchmark: frequency-solves/s of the panel-method hot path on GB300.
+
+Workload (default): the four-column array -- four truncated cylinders, radius
+6 m, draft 20 m, 64 azimuthal x (8 bottom + 24 side) panels each (2048 panels,
+8192 in total), centred at (+-25, +-25, 0) m; infinite depth; 100 frequencies
+uniform on 0.05-3.0 rad/s; headings 0/45/90 deg (6 radiation + 3 diffraction
+right-hand sides).  Synthetic by construction (generated mesh, no dataset).
+
+One step = one frequency-solve in the mixed-precision mode: wave assembly
+(FP32 real parts, FP64-accurate imaginary parts), TF32 tensor-core LU, FP64
+iterative refinement to 1e-12 relative residual, hull integrals.  The plain
+FP64 GPU path is timed on `--plain-steps` of the same frequencies and the
+mixed results are compared with it (A, B normwise).
+
+  value  = freq-solves/s from device time (CUDA events on the library stream)
+  e2e    = freq-solves/s of wall time around bem_solve (host in, host out)
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "freq-solves/s at 8k panels: mixed+surrogate vs FP64 GPU, A/B err <=1e-6"
+OMEGAS = np.linspace(0.05, 3.0, 100)
+BETAS = np.deg2rad([0.0, 45.0, 90.0])
+ORIGINS = [[25.0, 25.0, 0.0], [-25.0, 25.0, 0.0], [-25.0, -25.0, 0.0], [25.0, -25.0, 0.0]]
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--plain-steps", type=int, default=2)
+    p.add_argument("--na", type=int, default=64, help="azimuthal panels per cylinder (64 -> 8192 panels)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_mesh(bg, na):
+    cyl = bg.Half_Cylinder(6.0, 20.0, na, 8, 24, 0, False)
+    return bg.unify([cyl] * 4, ORIGINS)
+
+
+def cpu_baseline(na, budget_s):
+    """The FP64 oracle (CPU restatement of the reference path) on the host cores,
+    on a bounded sample of one frequency-solve: wave assembly of a block of
+    rows and a dense complex LU + solve of a smaller order, each scaled to the
+    full workload by its operation count (rows x N x Q, and n^3)."""
+    from oracle.oracle import Oracle, Mesh as OMesh
+    orc = Oracle()
+    cyl, _ = orc.cylinder(6.0, 20.0, na, 8, 24, cosine=False)
+    mesh = OMesh.concat([cyl] * 4, ORIGINS)
+    N = mesh.n
+    K = OMEGAS[50] ** 2 / 9.81
+    rows = 16
+    t0 = time.perf_counter()
+    orc.wave_rows(mesh, K, 0, rows)
+    t_rows = time.perf_counter() - t0
+    while t_rows < 0.25 * budget_s and rows < N // 4:
+        rows *= 2
+        t0 = time.perf_counter()
+        orc.wave_rows(mesh, K, 0, rows)
+        t_rows = time.perf_counter() - t0
+    t_asm = t_rows * N / rows
+    n = 512
+    rng = np.random.default_rng(0)
+    t_lu = 0.0
+    while True:
+        A = 0.5 * np.eye(n) + (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * (0.2 / np.sqrt(n))
+        B = rng.standard_normal((n, 9)) + 0j
+        t0 = time.perf_counter()
+        orc.lu_solve(A, B)
+        t_lu = time.perf_counter() - t0
+        if t_lu > 0.25 * budget_s or n >= 4096:
+            break
+        n *= 2
+    t_lu_full = t_lu * (N / n) ** 3
+    per_solve = t_asm + t_lu_full
+    return {"value": 1.0 / per_solve, "unit": "freq-solves/s", "cores": orc.num_threads(), "kind": "port",
+            "sample": "oracle wave assembly of %d of %d rows (scaled x%.0f) + oracle complex LU/solve at n=%d "
+                      "(scaled x%.0f by n^3); %.2f s + %.2f s per freq-solve" % (rows, N, N / rows, n, (N / n) ** 3,
+                                                                                 t_asm, t_lu_full),
+            "seconds_per_solve": per_solve}
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    steps = []
+    for _ in range(args.warmup):
+        pass
+    info = None
+    for _ in range(max(1, args.steps)):
+        info = cpu_baseline(args.na, args.cpu_seconds / max(1, args.steps))
+        steps.append(info["seconds_per_solve"])
+    v = 1.0 / float(np.mean(steps))
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "freq-solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "four-cylinder array, %d panels, 100 freqs 0.05-3.0 rad/s, 3 headings"
+                                   % (4 * args.na * 32)},
+            "cpu_baseline": {"value": v, "unit": "freq-solves/s", "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": "freq-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def normwise(a, b):
+    d = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (d if d > 0 else 1.0))
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        return
+    import bemuse_gb300 as bg
+    bg.build.build()
+    mesh = build_mesh(bg, args.na)
+    N = mesh.n
+    s = bg.Hydrodynamic_Radiation_Solver(device=local, precision=bg.MIXED)
+    s.Set_Parameters([bg.Parameter("WaveAngle", b) for b in BETAS])
+    t0 = time.perf_counter()
+    s.Setup(mesh)
+    setup_s = time.perf_counter() - t0
+    my = OMEGAS[rank::world]
+    seq = [my[i % len(my)] for i in range(args.warmup + args.steps)]
+    for om in seq[:args.warmup]:
+        s.solve_omegas([om])
+    s.stage_times(reset=True)
+    launches0 = bg.launch_count()
+    barrier(dist)
+    results = []
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for om in seq[args.warmup:]:
+            results.append(s.solve_omegas([om]))
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    launches = bg.launch_count() - launches0
+    st = s.stage_times(reset=True)
+    dev_ms = float(np.sum(st[:5]))
+    dev_ms_max = allmax(dist, dev_ms)
+    wall_max = allmax(dist, wall)
+    total = args.steps * world
+    value = total / (dev_ms_max / 1000.0)
+    e2e = total / wall_max
+    iters = [int(r["iters"][0]) for r in results]
+    # plain FP64 GPU path on the first frequencies of this rank, and accuracy of mixed vs plain
+    plain_om = seq[args.warmup:args.warmup + args.plain_steps]
+    sp = bg.Hydrodynamic_Radiation_Solver(device=local, precision=bg.PLAIN_FP64)
+    sp.Set_Parameters([bg.Parameter("WaveAngle", b) for b in BETAS])
+    sp.Setup(mesh)
+    sp.stage_times(reset=True)
+    errA, errB, errF = 0.0, 0.0, 0.0
+    t0 = time.perf_counter()
+    for i, om in enumerate(plain_om):
+        rp = sp.solve_omegas([om])
+        rm = results[i]
+        errA = max(errA, normwise(rm["A"][0], rp["A"][0]))
+        errB = max(errB, normwise(rm["B"][0], rp["B"][0]))
+        errF = max(errF, normwise(rm["F"][0], rp["F"][0]))
+    plain_wall = time.perf_counter() - t0
+    stp = sp.stage_times(reset=True)
+    plain_ms = float(np.sum(stp[:5])) / max(1, len(plain_om))
+    plain_value = 1000.0 / plain_ms
+    # roofline: the stage with the largest device time
+    names = ["incident+static rhs", "wave assembly", "lu factor", "solve+refine", "post"]
+    per = st[:5] / args.steps
+    dom = int(np.argmax(per))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    tf32_peak = peaks.get("bf16_tflops", 1900.0) / 2.0
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    Q_pairs = 4.0 * N - 3.0 * 4 * 0  # quads 4 pts, bottom-centre tris 3 pts
+    ntri = 4 * args.na
+    evals = float(N) * (4.0 * (N - ntri) + 3.0 * ntri)
+    Np = (N + 127) // 128 * 128
+    lu_flops = 8.0 / 3.0 * Np ** 3
+    if dom == 2:
+        roof = {"kernel": "lu factor (tcgen05 TF32 trailing update)", "bound": "tensor",
+                "achieved": lu_flops / (per[2] / 1000.0) / 1e12, "peak": tf32_peak, "unit": "TFLOP/s",
+                "traffic": None, "peak_source": "measured bf16 / 2 (TF32 rate), MEASURED_PEAKS.json"}
+    elif dom == 1:
+        # algorithmic bytes of the assembly: D written in FP64 (16 B) + FP32 (8 B), Rankine read (16 B) per pair
+        byts = 40.0 * N * N
+        roof = {"kernel": "wave assembly (k_wave_mixed)", "bound": "hbm",
+                "achieved": byts / (per[1] / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s", "traffic": None,
+                "green_evals_per_s": evals / (per[1] / 1000.0), "peak_source": "measured, MEASURED_PEAKS.json"}
+    else:
+        byts = 16.0 * N * N
+        roof = {"kernel": names[dom], "bound": "hbm", "achieved": byts / (per[dom] / 1000.0) / 1e9,
+                "peak": hbm_peak, "unit": "GB/s", "traffic": None, "peak_source": "measured, MEASURED_PEAKS.json"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    if rank != 0:
+        return
+    cpu = cpu_baseline(args.na, args.cpu_seconds)
+    cpu.pop("seconds_per_solve", None)
+    h2d = 8 + 6 * N * 8
+    d2h = (36 + 12 * len(BETAS)) * 16 + int(np.mean(iters)) * (2 * 9 * 8) + 4
+    line = {"metric": METRIC, "value": value, "unit": "freq-solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+tf32+f64", "data": "synthetic",
+            "config": {"workload": "four-cylinder array, %d panels, 100 freqs 0.05-3.0 rad/s, 3 headings, mixed "
+                                   "precision (FP32 assembly, TF32 LU, FP64 refinement to 1e-12)" % N,
+                       "panels": N, "rhs": 9, "l2": "inputs larger than L2 (Rankine matrices 3 x %.0f MB)"
+                       % (8.0 * N * Np / 1e6), "parallelism": "frequencies sharded over ranks"},
+            "e2e": {"value": e2e, "unit": "freq-solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "plain_fp64": {"value": plain_value, "unit": "freq-solves/s", "steps": len(plain_om),
+                           "ms_per_step": plain_ms, "wall_s": plain_wall,
+                           "stage_ms": [float(x) / max(1, len(plain_om)) for x in stp[:5]]},
+            "speedup_vs_plain_fp64": value / plain_value,
+            "accuracy_vs_plain_fp64": {"A": errA, "B": errB, "F": errF, "metric": "max|x-ref|/max|ref| per 6x6"},
+            "refine_sweeps": iters,
+            "stage_ms": dict(zip(names, [float(x) for x in per])),
+            "setup_s": setup_s}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -178,6 +178,15 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
  * reset != 0 zeroes the counters after reading. */
 bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
 
+/* Number of kernel launches this library has issued since it was loaded. */
+unsigned long long bem_launch_count(void);
+
+/* Diagnostic: one tensor-core (tcgen05, TF32) trailing update of an n x n
+ * complex block (n a multiple of 128, >= 256) on random data, compared with
+ * the FP32 CUDA-core update on the same data.  Returns max|tc - fp32| /
+ * max|fp32| (about 1e-3 for TF32 inputs), or a negative value on failure. */
+double bem_selftest_tc(int device, int n);
+
 /* Library version string. */
 const char* bem_version(void);
 

@@ -166,3 +166,10 @@ def test_dense_solve_plain_and_mixed(bg):
         assert normwise(x, ref) < 1e-11
         x, it, res = bg.dense_solve(A, B, bg.MIXED)
         assert res <= 1e-12 and normwise(x, ref) < 1e-10
+
+
+def test_tensor_core_update_matches_fp32(bg):
+    for n in (256, 1024):
+        err = bg.selftest_tc(n)
+        print("tcgen05 vs fp32 update, n=%d: %.3e" % (n, err))
+        assert 0 <= err < 2e-2
