@@ -39,14 +39,18 @@ struct WaveArgs {
     // mixed mode only
     const float* xr32;    // collocation points, hi/lo split: [6][N] (xh, yh, zh, xl, yl, zl)
     const float* gq32;    // Gauss data [10][4][N]: xh, yh, zh, w, nx, ny, nz, xl, yl, zl
-    const double* cst;    // per-source FP64 leading imaginary parts [6][N]: alpha, beta, gamma, dx, dy, dz
-    double P[6], Q[6];    // sum_s alpha_s N_k(s, j), sum_s beta_s N_k(s, j)
 };
 
 cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
                     double* o0, double* o1, double* o2, double* o3);
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
+// Plane-wave factors of the imaginary wave influence (M angles) and the exact
+// FP64 product out += i * scale * Re-part operator applied to Z (k_influence.cu).
+void launch_pw_build(cudaStream_t st, int N, int M, double K, const double* xr, const double* gq, const int* nq,
+                     double2* E, double2* V, double2* W);
+void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const double2* P, const double2* E,
+                       const double* Z, double2* T, double* out);
 void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i);
 void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
@@ -76,13 +80,19 @@ int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* 
                   int* flags);
 int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
                   float* wut, int* flags, bool tc);
-// Forward/back substitution with the factors: X (n x R, interleaved complex) in place.
-void lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X);
-void lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X);
-// Rres = Y - D X (FP64), and per-column max |Rres| and max |Y| into nrm[2R]
-// (as ordered int bit patterns; zero them first).
+// Forward/back substitution with the factors: X (n x R, interleaved complex) in place,
+// with an n x R scratch right after X.  ready: n/nb ints zeroed at allocation; epoch
+// strictly increasing across calls on the same ready array (each call uses epoch and
+// epoch + 1).  Returns nonzero if the cooperative launch failed.
+int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
+                 int* ready, int epoch, int* flags);
+int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
+                 int* ready, int epoch, int* flags);
+// Rres = Y - D X in FP64 (Di may be null: real operator part only).
 void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
-                     const double* Y, double* Rres, unsigned long long* nrm);
+                     const double* Y, double* Rres);
+// nrm[j] = max_r |Rres[r][j]|, nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (zero them first).
+void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm);
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
 void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);

@@ -247,53 +247,4 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     Ghr = fmaf(E, 0.636619772f - H1, Ls);
 }
 
-// Imaginary parts: Im G = -2 pi e^v J0(h), Im dG/dh = 2 pi e^v J1(h).  With
-// a0 = e^v J0(h) and a1 = e^v J1(h)/h, return the remainders
-//   r0 = a0 - (1 + v),   r1 = a1 - 1/2,
-// which are O((|v| + h)^2); the separable leading parts 1 + v and 1/2 are
-// summed exactly in FP64 by the caller.  Small arguments use the power series
-// of expm1, J0 - 1 and J1(h)/h - 1/2 so the remainders keep FP32 relative
-// accuracy (the leading parts would otherwise cancel them).
-__device__ __forceinline__ void im_remainders(float hh, float vv, float& r0, float& r1) {
-    float em1 = expm1f(vv);
-    float em2;  // e^v - 1 - v
-    if (vv > -0.5f) {
-        em2 = vv * vv * fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, fmaf(vv, 2.7557319e-6f, 2.4801587e-5f),
-              1.9841270e-4f), 1.3888889e-3f), 8.3333333e-3f), 4.1666667e-2f), 0.16666667f), 0.5f);
-    } else {
-        em2 = em1 - vv;
-    }
-    float j0m1, j1h, j1hm;
-    if (hh < 2.0f) {
-        float q = 0.25f * hh * hh;
-        // J0 - 1 = sum_{k>=1} (-q)^k/(k!)^2 ;  J1/h - 1/2 = (1/2) sum_{k>=1} (-q)^k/(k!(k+1)!)
-        float t0 = fmaf(-q * (1.0f / 81.0f), 1.0f, 1.0f);
-        t0 = fmaf(-q * (1.0f / 64.0f), t0, 1.0f);
-        t0 = fmaf(-q * (1.0f / 49.0f), t0, 1.0f);
-        t0 = fmaf(-q * (1.0f / 36.0f), t0, 1.0f);
-        t0 = fmaf(-q * (1.0f / 25.0f), t0, 1.0f);
-        t0 = fmaf(-q * (1.0f / 16.0f), t0, 1.0f);
-        t0 = fmaf(-q * (1.0f / 9.0f), t0, 1.0f);
-        t0 = fmaf(-q * 0.25f, t0, 1.0f);
-        j0m1 = -q * t0;
-        float t1 = fmaf(-q * (1.0f / 90.0f), 1.0f, 1.0f);
-        t1 = fmaf(-q * (1.0f / 72.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 56.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 42.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 30.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 20.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 12.0f), t1, 1.0f);
-        t1 = fmaf(-q * (1.0f / 6.0f), t1, 1.0f);
-        j1hm = -0.25f * q * t1;
-        j1h = 0.5f + j1hm;
-    } else {
-        float j0v = j0f(hh), j1v = j1f(hh);
-        j0m1 = j0v - 1.0f;
-        j1h = j1v / hh;
-        j1hm = j1h - 0.5f;
-    }
-    r0 = em2 + fmaf(em1, j0m1, j0m1);
-    r1 = fmaf(em1, j1h, j1hm);
-}
-
 }  // namespace bem

@@ -52,13 +52,19 @@ struct bem_ctx {
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
     float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
     int* d_flags = nullptr;
+    int* d_ready = nullptr;           // block-ready flags of the cooperative triangular solves
+    int solve_epoch = 0;
     unsigned long long* d_norms = nullptr;
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
-    double* d_cst = nullptr;
-    double* h_cst = nullptr;          // pinned, 6 N
-    std::vector<double> csum;         // per-source Gauss sums [8][N]
-    double cst_P[6], cst_Q[6];
+    // plane-wave factors of the exact imaginary parts: E, V, W [Mmax][N], T [Mmax][R][2]
+    double2 *d_pwE = nullptr, *d_pwV = nullptr, *d_pwW = nullptr, *d_pwT = nullptr;
+    int pw_Mmax = 0, pw_M = 0;
+    double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
+    double pw_K = -1.0;               // wave number the factors were built for
+    // operator used by the refinement residual: 0 = stored D64 (re, im); 1 = stored
+    // Re(D) only (real operator, K = 0); 2 = stored Re(D) + plane-wave Im(D)
+    int resid_mode = 0;
     std::vector<void*> allocs;
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
@@ -116,51 +122,53 @@ void free_all(bem_ctx* ctx) {
     for (auto p : fp) *p = nullptr;
     ctx->d_nq = nullptr;
     ctx->d_flags = nullptr;
+    ctx->d_ready = nullptr;
+    ctx->solve_epoch = 0;
     ctx->d_norms = nullptr;
     ctx->d_xr32 = nullptr;
     ctx->d_gq32 = nullptr;
-    ctx->d_cst = nullptr;
-    if (ctx->h_cst) cudaFreeHost(ctx->h_cst);
-    ctx->h_cst = nullptr;
+    ctx->d_pwE = ctx->d_pwV = ctx->d_pwW = ctx->d_pwT = nullptr;
+    ctx->pw_Mmax = ctx->pw_M = 0;
+    ctx->pw_K = -1.0;
     ctx->ready = false;
 }
 
-// Leading (separable) imaginary parts of the wave influence at wave number K for
-// the mixed kernel, from the frequency-independent per-source Gauss sums
-//   Cs = sum w, Cz = sum w z, Cnx = sum w nx, Cxnx = sum w x nx, Cny = sum w ny,
-//   Cyny = sum w y ny, Cnz = sum w nz, Cznz = sum w z nz   (mirrored panel s).
-// Im ws(r,s) = alpha_s + beta_s z_r + ...,  Im wd(r,s) = gamma_s + dx_s x_r + dy_s y_r + dz_s z_r + ...
-bem_status upload_wave_constants(bem_ctx* ctx, double K) {
-    const int N = ctx->N;
-    const double pi = 3.14159265358979323846;
-    const double c1 = K * 0.25 / pi, c2 = K * K * 0.25 / pi;
-    const double t1 = 2.0 * pi * c1, t2 = 2.0 * pi * c2;
-    const double* C = ctx->csum.data();
-    double* h = ctx->h_cst;
-    for (int j = 0; j < 6; ++j) { ctx->cst_P[j] = 0.0; ctx->cst_Q[j] = 0.0; }
-    for (int s = 0; s < N; ++s) {
-        double Cs = C[s], Cz = C[N + s], Cnx = C[2 * N + s], Cxnx = C[3 * N + s];
-        double Cny = C[4 * N + s], Cyny = C[5 * N + s], Cnz = C[6 * N + s], Cznz = C[7 * N + s];
-        double al = -t1 * (Cs - K * Cz), be = -t1 * K * Cs;
-        h[s] = al;
-        h[N + s] = be;
-        h[2 * N + s] = t2 * (-0.5 * K * (Cxnx + Cyny) - Cnz + K * Cznz);
-        h[3 * N + s] = t2 * 0.5 * K * Cnx;
-        h[4 * N + s] = t2 * 0.5 * K * Cny;
-        h[5 * N + s] = -t2 * K * Cnz;
-        const double* nk = &ctx->Nk[(size_t)s * 6];
-        for (int j = 0; j < 6; ++j) { ctx->cst_P[j] += al * nk[j]; ctx->cst_Q[j] += be * nk[j]; }
-    }
-    cudaError_t e = cudaMemcpyAsync(ctx->d_cst, h, sizeof(double) * 6 * (size_t)N, cudaMemcpyHostToDevice, ctx->st);
-    if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("constants upload: ") + cudaGetErrorString(e));
-    return BEM_OK;
+// Angles for the plane-wave form of the imaginary wave influence at wave number
+// K: the trapezoid error is ~|J_M(K D)|, below 1e-17 for M >= 1.3 K D + 30.
+int pw_angles(double K, double D) {
+    int M = (int)std::ceil(1.3 * K * D + 30.0);
+    return (M + 3) / 4 * 4;
 }
 
-void fill_mixed_args(bem_ctx* ctx, bem::WaveArgs& a) {
-    a.xr32 = ctx->d_xr32;
-    a.gq32 = ctx->d_gq32;
-    a.cst = ctx->d_cst;
-    for (int j = 0; j < 6; ++j) { a.P[j] = ctx->cst_P[j]; a.Q[j] = ctx->cst_Q[j]; }
+// Builds (once per wave number) the plane-wave factors E, V, W on the device.
+bem_status pw_prepare(bem_ctx* ctx, double K) {
+    if (ctx->pw_K == K) return BEM_OK;
+    const int M = pw_angles(K, ctx->pw_D);
+    if ((size_t)M * bem::MAX_RHS * 2 * sizeof(double2) > 220 * 1024)
+        return fail(ctx, BEM_ERR_UNSUPPORTED, "K * D too large for the plane-wave imaginary part (M = " +
+                                                  std::to_string(M) + " angles)");
+    if (M > ctx->pw_Mmax) {
+        if (ctx->d_pwE) {
+            // grow: release the old factor buffers
+            for (double2** p : {&ctx->d_pwE, &ctx->d_pwV, &ctx->d_pwW, &ctx->d_pwT}) {
+                auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void*)*p);
+                if (it != ctx->allocs.end()) ctx->allocs.erase(it);
+                cudaFree(*p);
+                *p = nullptr;
+            }
+        }
+        int Mmax = std::max(M, 128);
+        DA(ctx->d_pwE, (size_t)Mmax * ctx->N);
+        DA(ctx->d_pwV, (size_t)Mmax * ctx->N);
+        DA(ctx->d_pwW, (size_t)Mmax * ctx->N);
+        DA(ctx->d_pwT, (size_t)Mmax * bem::MAX_RHS * 2);
+        ctx->pw_Mmax = Mmax;
+    }
+    bem::launch_pw_build(ctx->st, ctx->N, M, K, ctx->d_xr, ctx->d_gq, ctx->d_nq, ctx->d_pwE, ctx->d_pwV, ctx->d_pwW);
+    CK(cudaGetLastError());
+    ctx->pw_M = M;
+    ctx->pw_K = K;
+    return BEM_OK;
 }
 
 int round_up(int n, int a) { return (n + a - 1) / a * a; }
@@ -209,6 +217,11 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     }
     DA(ctx->d_X, (size_t)4 * Np * R);
     DA(ctx->d_flags, 1);
+    if (!ctx->d_ready) {
+        DA(ctx->d_ready, Np / 64);
+        CK(cudaMemsetAsync(ctx->d_ready, 0, sizeof(int) * (Np / 64), ctx->st));
+        ctx->solve_epoch = 0;
+    }
     DA(ctx->d_norms, 2 * bem::MAX_RHS);
     return BEM_OK;
 }
@@ -233,7 +246,10 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
         CK(cudaEventRecord(ctx->ev[3], st));
         CK(cudaMemcpyAsync(ctx->d_X, ctx->d_Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
         bem::launch_pad_rhs(st, N, Np, R, ctx->d_X);
-        bem::lu_solve_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, R, ctx->d_X);
+        ctx->solve_epoch += 2;
+        if (bem::lu_solve_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, R, ctx->d_X, ctx->d_ready, ctx->solve_epoch - 1,
+                              ctx->d_flags))
+            return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[4], st));
     } else {
@@ -251,10 +267,23 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
         std::vector<unsigned long long> hn(2 * R);
         for (;;) {
             bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
-            bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32);
+            ctx->solve_epoch += 2;
+            if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
+                                  ctx->solve_epoch - 1, ctx->d_flags))
+                return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
             bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
             CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
-            bem::launch_residual(st, N, Np, ctx->d_D64r, ctx->d_D64i, R, ctx->d_X, ctx->d_Y, ctx->d_Rr, ctx->d_norms);
+            if (ctx->resid_mode == 2) {
+                // r = y - Re(D) x  (stored FP64) - i Im(D) x  (plane waves, FP64)
+                bem::launch_residual(st, N, Np, ctx->d_D64r, nullptr, R, ctx->d_X, ctx->d_Y, ctx->d_Rr);
+                const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
+                bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M, ctx->d_pwW,
+                                       ctx->d_pwE, ctx->d_X, ctx->d_pwT, ctx->d_Rr);
+            } else {
+                bem::launch_residual(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R,
+                                     ctx->d_X, ctx->d_Y, ctx->d_Rr);
+            }
+            bem::launch_norms(st, N, R, ctx->d_Rr, ctx->d_Y, ctx->d_norms);
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
@@ -442,23 +471,34 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
             xr32[(size_t)d * N + i] = hi;
             xr32[(size_t)(3 + d) * N + i] = (float)(v - (double)hi);
         }
-    ctx->csum.assign((size_t)8 * N, 0.0);
     for (int i = 0; i < N; ++i) {
         const bem::PanelGeom& p = mirror[i];
         for (int q = 0; q < p.nq; ++q) {
-            double x = p.qp[3 * q], y = p.qp[3 * q + 1], z = p.qp[3 * q + 2], w = p.qw[q];
-            double nx = p.qn[3 * q], ny = p.qn[3 * q + 1], nz = p.qn[3 * q + 2];
-            double f[7] = {x, y, z, w, nx, ny, nz};
+            double f[7] = {p.qp[3 * q], p.qp[3 * q + 1], p.qp[3 * q + 2], p.qw[q], p.qn[3 * q], p.qn[3 * q + 1],
+                           p.qn[3 * q + 2]};
             for (int k = 0; k < 3; ++k) {
                 float hi = (float)f[k];
                 gq32[((size_t)k * 4 + q) * N + i] = hi;
                 gq32[((size_t)(7 + k) * 4 + q) * N + i] = (float)(f[k] - (double)hi);
             }
             for (int k = 3; k < 7; ++k) gq32[((size_t)k * 4 + q) * N + i] = (float)f[k];
-            double* C = ctx->csum.data();
-            C[i] += w; C[N + i] += w * z; C[2 * N + i] += w * nx; C[3 * N + i] += w * x * nx;
-            C[4 * N + i] += w * ny; C[5 * N + i] += w * y * ny; C[6 * N + i] += w * nz; C[7 * N + i] += w * z * nz;
         }
+    }
+    {
+        // largest horizontal distance between a collocation point and a Gauss point (bounding boxes)
+        double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
+        for (int i = 0; i < N; ++i) {
+            for (int d = 0; d < 2; ++d) {
+                lo[d] = std::min(lo[d], xr[(size_t)d * N + i]);
+                hi[d] = std::max(hi[d], xr[(size_t)d * N + i]);
+            }
+            for (int q = 0; q < mirror[i].nq; ++q)
+                for (int d = 0; d < 2; ++d) {
+                    lo[d] = std::min(lo[d], mirror[i].qp[3 * q + d]);
+                    hi[d] = std::max(hi[d], mirror[i].qp[3 * q + d]);
+                }
+        }
+        ctx->pw_D = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]));
     }
     // mass properties
     double cog[3] = {0, 0, 0}, gyr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, mass = 0;
@@ -503,8 +543,6 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
     DA(ctx->d_xr32, xr32.size());
     DA(ctx->d_gq32, gq32.size());
-    DA(ctx->d_cst, 6 * (size_t)N);
-    CK(cudaMallocHost(&ctx->h_cst, sizeof(double) * 6 * (size_t)N));
     cudaStream_t st = ctx->st;
     CK(cudaMemcpyAsync(ctx->d_xr32, xr32.data(), xr32.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_gq32, gq32.data(), gq32.size() * 4, cudaMemcpyHostToDevice, st));
@@ -586,11 +624,18 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         a.Bm = ctx->d_Bm; a.Y = ctx->d_Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
         a.D32r = mixed ? ctx->d_D32r : nullptr; a.D32i = mixed ? ctx->d_D32i : nullptr;
         if (mixed) {
-            s = upload_wave_constants(ctx, K);
-            if (s != BEM_OK) return s;
-            fill_mixed_args(ctx, a);
+            a.xr32 = ctx->d_xr32;
+            a.gq32 = ctx->d_gq32;
         }
         bem::launch_wave(st, a, mixed);
+        if (mixed && K != 0.0) {
+            // exact FP64 imaginary part of S applied to B:  Y += -i Im(ws) B
+            s = pw_prepare(ctx, K);
+            if (s != BEM_OK) return s;
+            const double c1 = K * 0.25 / 3.14159265358979323846;
+            bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c1 / ctx->pw_M, ctx->d_pwV,
+                                   ctx->d_pwE, ctx->d_Bm, ctx->d_pwT, ctx->d_Y);
+        }
         bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, mixed ? ctx->d_D32r : nullptr,
                                  mixed ? ctx->d_D32i : nullptr);
         CK(cudaGetLastError());
@@ -598,7 +643,9 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         int iters = 0;
         double resid = 0;
         double t_lu = 0, t_sv = 0;
+        ctx->resid_mode = mixed ? (K != 0.0 ? 2 : 1) : 0;
         s = factor_and_solve(ctx, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
+        ctx->resid_mode = 0;
         if (s != BEM_OK) return s;
         CK(cudaEventRecord(ctx->ev[6], st));
         bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, ctx->d_phiI, ctx->d_dphiI, ctx->d_part,
@@ -700,11 +747,8 @@ bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, 
     a.N = N; a.ld = N; a.R = ctx->R; a.mode = 1; a.K = K;
     a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.Bm = ctx->d_Bm;
     a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
-    if (precision == BEM_MIXED) {
-        bem_status s = upload_wave_constants(ctx, K);
-        if (s != BEM_OK) { cudaFree(buf); return s; }
-        fill_mixed_args(ctx, a);
-    }
+    a.xr32 = ctx->d_xr32;
+    a.gq32 = ctx->d_gq32;
     bem::launch_wave(ctx->st, a, precision == BEM_MIXED);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(ws, buf, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, ctx->st);

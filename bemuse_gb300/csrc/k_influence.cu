@@ -198,13 +198,12 @@ __global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// K2, mixed precision.  Real parts of G and dG in FP32.  Imaginary parts
-// split as  a0 = e^v J0(h) = 1 + v + r0  and  a1 = e^v J1(h)/h = 1/2 + r1:
-// the leading parts are separable in (receiver, source) and enter through the
-// per-source FP64 constants cst (alpha..dz) and P, Q; only the O((Kr)^2)
-// remainders r0, r1 are evaluated and summed in FP32.  This keeps the
-// imaginary parts accurate to FP64-level relative error at low K, where the
-// radiation damping is a small difference of O(K) imaginary terms.
+// K2, mixed precision.  Every term of G and dG in FP32; the FP64 operator
+// gets the real part (Rankine FP64 + wave FP32) and the LU copy gets both parts
+// in FP32.  The imaginary part of the operator and of S*B is not taken from
+// here: it is applied exactly, in FP64, by the plane-wave kernels below
+// (k_pw_*), because the radiation damping at low K is a small difference of
+// O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
 __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
     const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -212,24 +211,22 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
     const int N = a.N, R = a.R;
     const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
     const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
-    const double Xr = a.xr[r], Yr = a.xr[N + r], Zr = a.xr[2 * N + r];
     const float K = (float)a.K;
     const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
-    const double tpc1 = 2.0 * 3.14159265358979323846 * a.K * kFourPIinv;
-    const double tpc2 = tpc1 * a.K;
+    const float twopi = 6.28318530717959f;
     float acc_re[MAX_RHS], acc_im[MAX_RHS];
 #pragma unroll
     for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
     const size_t row = (size_t)r * a.ld;
     const bool live = a.K != 0.0;
+    const size_t fs = (size_t)4 * N;
     for (int s = lane; s < N; s += 32) {
-        float wsr = 0.f, wdr = 0.f, S0 = 0.f, S1 = 0.f;
+        float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
         const int nq = live ? a.nq[s] : 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             if (q < nq) {
-                const float* g = a.gq32 + (size_t)q * N + s;  // field stride 4N
-                const size_t fs = (size_t)4 * N;
+                const float* g = a.gq32 + (size_t)q * N + s;
                 float dx = (xh - g[0]) + (xl - g[7 * fs]);
                 float dy = (yh - g[fs]) + (yl - g[8 * fs]);
                 float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
@@ -237,49 +234,40 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
                 float XX = dx * K, YY = dy * K, VV = dz * K;
                 float hh = sqrtf(fmaf(XX, XX, YY * YY));
                 float ev = expf(VV);
-                float Gr, Ghr, r0, r1;
+                float Gr, Ghr;
                 gf32_re(c_poly32, hh, VV, ev, Gr, Ghr);
-                im_remainders(hh, VV, r0, r1);
+                float j0v = j0f(hh), j1v = j1f(hh);
                 float proj = fmaf(XX, nx, YY * ny);
-                float dgr = 0.f;
-                if (hh > 1.0e-6f) dgr = Ghr * proj / hh;
-                else r1 = -0.5f;  // the reference sets dG/dx = dG/dy = 0 there
+                float dgr = 0.f, dgi = 0.f;
+                if (hh > 1.0e-6f) {
+                    float inv_h = 1.0f / hh;
+                    dgr = Ghr * proj * inv_h;
+                    dgi = twopi * ev * j1v * proj * inv_h;
+                }
+                float Gi = -twopi * ev * j0v;
                 wsr = fmaf(w * c1, Gr, wsr);
+                wsi = fmaf(w * c1, Gi, wsi);
                 wdr = fmaf(w * c2, fmaf(Gr, nz, dgr), wdr);
-                S0 = fmaf(w, r0, S0);
-                S1 = fmaf(w, fmaf(r1, proj, -r0 * nz), S1);
+                wdi = fmaf(w * c2, fmaf(Gi, nz, dgi), wdi);
             }
         }
-        const double* cs = a.cst + s;
-        double wsi = live ? fma(cs[N], Zr, cs[0]) - tpc1 * (double)S0 : 0.0;
-        double wdi = live ? fma(cs[5 * N], Zr, fma(cs[4 * N], Yr, fma(cs[3 * N], Xr, cs[2 * (size_t)N]))) +
-                                tpc2 * (double)S1
-                          : 0.0;
         if (a.mode == 1) {
             size_t o = 2 * ((size_t)r * N + s);
-            a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = wsi;
-            a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = wdi;
+            a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = (double)wsi;
+            a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
             continue;
         }
         double dre = a.RD[row + s] + fma(a.RSR[row + s], a.K, (double)wdr);
         a.D64r[row + s] = dre;
-        a.D64i[row + s] = wdi;
         a.D32r[row + s] = (float)dre;
-        a.D32i[row + s] = (float)wdi;
+        a.D32i[row + s] = wdi;
+        // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
         const double* b = a.Bm + (size_t)s * 2 * R;
-        const float wsi32 = (float)wsi;
 #pragma unroll
-        for (int j = 0; j < 6; ++j) {
-            float br = (float)b[2 * j];
-            acc_re[j] = fmaf(-wsr, br, acc_re[j]);
-            acc_im[j] = fmaf(S0, br, acc_im[j]);
-        }
-#pragma unroll
-        for (int j = 6; j < MAX_RHS; ++j) {
+        for (int j = 0; j < MAX_RHS; ++j) {
             if (j < R) {
-                float br = (float)b[2 * j], bi = (float)b[2 * j + 1];
-                acc_re[j] -= wsr * br - wsi32 * bi;
-                acc_im[j] -= wsr * bi + wsi32 * br;
+                acc_re[j] = fmaf(-wsr, (float)b[2 * j], acc_re[j]);
+                acc_im[j] = fmaf(-wsr, (float)b[2 * j + 1], acc_im[j]);
             }
         }
     }
@@ -294,11 +282,134 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
                 vi += __shfl_xor_sync(0xffffffffu, vi, off);
             }
             if (lane == 0) {
-                double add_im = j < 6 ? tpc1 * (double)vi - fma(Zr, a.Q[j], a.P[j]) : (double)vi;
-                if (!live) add_im = 0.0;
                 a.Y[2 * ((size_t)r * R + j)] += (double)vr;
-                a.Y[2 * ((size_t)r * R + j) + 1] += add_im;
+                a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
             }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exact FP64 imaginary parts by plane waves.  With Bessel's integral
+// J0(h) = (1/2pi) int exp(i h cos(t - phi)) dt, the imaginary parts of the wave
+// influence separate over M equispaced angles t_m (trapezoid rule; exact to
+// rounding once M > 1.3 K D + 30, D the largest horizontal distance):
+//   e^v J0(h)              = (1/M) sum_m E_r(m) F_q(m)
+//   e^v J1(h)/h (X nx + Y ny) = -(1/M) sum_m i (cos t nx + sin t ny) E_r F_q
+// with E_r(m) = exp(K z_r + i K (x_r cos t_m + y_r sin t_m)) at the receiver and
+// F_q(m) = exp(-K z_q - i K (x_q cos t_m + y_q sin t_m)) at the Gauss point, so
+//   Im ws(r,s) = -(2 pi c1 / M) Re sum_m E_r(m) Vs_s(m),  Vs_s = sum_q w_q F_q
+//   Im wd(r,s) = -(2 pi c2 / M) Re sum_m E_r(m) Wd_s(m),  Wd_s = sum_q w_q (nz + i(cos t nx + sin t ny)) F_q
+// (c1 = K/4pi, c2 = K^2/4pi; Panel.cpp:632-634).  The operator products then
+// cost O(N M R) instead of O(N^2).
+__global__ void k_pw_build(int N, int M, double K, const double* __restrict__ xr, const double* __restrict__ gq,
+                           const int* __restrict__ nq, double2* __restrict__ E, double2* __restrict__ V,
+                           double2* __restrict__ W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y;
+    if (i >= N) return;
+    double st, ct;
+    sincospi(2.0 * m / M, &st, &ct);
+    // receiver factor
+    {
+        double ph = K * (xr[i] * ct + xr[N + i] * st);
+        double amp = exp(K * xr[2 * N + i]);
+        double sp, cp;
+        sincos(ph, &sp, &cp);
+        E[(size_t)m * N + i] = make_double2(amp * cp, amp * sp);
+    }
+    // source panel i: sums over its Gauss points
+    double vr = 0, vi = 0, wr = 0, wi = 0;
+    const int n = nq[i];
+    for (int q = 0; q < 4; ++q) {
+        if (q < n) {
+            const double* g = gq + (size_t)q * N + i;
+            const size_t fs = (size_t)4 * N;
+            double x = g[0], y = g[fs], z = g[2 * fs], w = g[3 * fs];
+            double nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
+            double amp = w * exp(-K * z);
+            double sp, cp;
+            sincos(-K * (x * ct + y * st), &sp, &cp);
+            double fr = amp * cp, fi = amp * sp;
+            vr += fr; vi += fi;
+            double tr = nz, ti = ct * nx + st * ny;  // nz + i (cos t nx + sin t ny)
+            wr += tr * fr - ti * fi;
+            wi += tr * fi + ti * fr;
+        }
+    }
+    V[(size_t)m * N + i] = make_double2(vr, vi);
+    W[(size_t)m * N + i] = make_double2(wr, wi);
+}
+
+// T1[m][j] = sum_s P_s(m) Z[s][j],  T2[m][j] = sum_s conj(P_s(m)) Z[s][j]   (Z: N x R complex)
+__global__ void __launch_bounds__(256) k_pw_project(int N, int R, const double2* __restrict__ P,
+                                                    const double* __restrict__ Z, double2* __restrict__ T) {
+    const int m = blockIdx.x;
+    __shared__ double red[8][4 * MAX_RHS];
+    double a[4 * MAX_RHS];
+#pragma unroll
+    for (int k = 0; k < 4 * MAX_RHS; ++k) a[k] = 0.0;
+    const double2* pm = P + (size_t)m * N;
+    for (int s = threadIdx.x; s < N; s += blockDim.x) {
+        double2 p = pm[s];
+        const double* z = Z + 2 * (size_t)s * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double zr = z[2 * j], zi = z[2 * j + 1];
+                a[4 * j] += p.x * zr - p.y * zi;      // P Z
+                a[4 * j + 1] += p.x * zi + p.y * zr;
+                a[4 * j + 2] += p.x * zr + p.y * zi;  // conj(P) Z
+                a[4 * j + 3] += p.x * zi - p.y * zr;
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4 * MAX_RHS; ++k) {
+        double v = a[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 4 * R; k += blockDim.x) {
+        double v = 0;
+        for (int w = 0; w < 8; ++w) v += red[w][k];
+        int j = k / 4, c = k % 4;
+        double* t = reinterpret_cast<double*>(T + ((size_t)m * R + j) * 2);
+        t[c] = v;  // T[m][j] = {T1.re, T1.im, T2.re, T2.im}
+    }
+}
+
+// out[r][j] += i * scale * sum_m (E_r(m) T1[m][j] + conj(E_r(m)) T2[m][j])
+__global__ void __launch_bounds__(256) k_pw_apply(int N, int M, int R, double scale, const double2* __restrict__ E,
+                                                  const double2* __restrict__ T, double* __restrict__ out) {
+    extern __shared__ double2 Ts[];  // M * R * 2
+    for (int k = threadIdx.x; k < M * R * 2; k += blockDim.x) Ts[k] = T[k];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    double ar[MAX_RHS], ai[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+    for (int m = 0; m < M; ++m) {
+        double2 e = E[(size_t)m * N + r];
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double2 t1 = Ts[(m * R + j) * 2], t2 = Ts[(m * R + j) * 2 + 1];
+                ar[j] += e.x * t1.x - e.y * t1.y + e.x * t2.x + e.y * t2.y;
+                ai[j] += e.x * t1.y + e.y * t1.x + e.x * t2.y - e.y * t2.x;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            // i * scale * (ar + i ai) = -scale ai + i scale ar
+            out[2 * ((size_t)r * R + j)] += -scale * ai[j];
+            out[2 * ((size_t)r * R + j) + 1] += scale * ar[j];
         }
     }
 }
@@ -517,6 +628,20 @@ void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
     dim3 grd((a.N + 7) / 8);
     if (fp32) BEM_LAUNCH(k_wave_mixed<<<grd, 256, 0, st>>>(a));
     else BEM_LAUNCH(k_wave<double><<<grd, 256, 0, st>>>(a));
+}
+
+void launch_pw_build(cudaStream_t st, int N, int M, double K, const double* xr, const double* gq, const int* nq,
+                     double2* E, double2* V, double2* W) {
+    dim3 grd((N + 127) / 128, M);
+    BEM_LAUNCH(k_pw_build<<<grd, 128, 0, st>>>(N, M, K, xr, gq, nq, E, V, W));
+}
+
+void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const double2* P, const double2* E,
+                       const double* Z, double2* T, double* out) {
+    BEM_LAUNCH(k_pw_project<<<M, 256, 0, st>>>(N, R, P, Z, T));
+    size_t smem = sizeof(double2) * (size_t)M * R * 2;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_pw_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_pw_apply<<<(N + 255) / 256, 256, smem, st>>>(N, M, R, scale, E, T, out));
 }
 
 void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i) {

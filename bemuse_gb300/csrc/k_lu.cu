@@ -13,10 +13,11 @@
 //   k_cgemm        L21 = A21 U11^-1 and U12 = L11^-1 A12 (into workspaces)
 //   k_copy_back    writes L21 / U12 into the matrix, checks |l_ik| <= 1
 //   k_cgemm / tc   A22 -= L21 U12 (SIMT complex GEMM; tcgen05 TF32 in k_tc_gemm.cu)
-// Solves use the stored off-diagonal blocks and the diagonal-block inverses.
+// Solves (k_trsv_coop) use the stored off-diagonal blocks and the diagonal-block inverses.
 #include "bem_internal.h"
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 
 namespace bem {
 
@@ -75,42 +76,44 @@ __global__ void __launch_bounds__(1024) k_lu_diag(int k0, CMat<T> A, T* invr, T*
         A.im[g] = ai[i * P + j];
     }
     __syncthreads();
-    // L^-1 in place on the strict lower part (unit diagonal): for j descending,
-    // X[i][j] = -sum_{m=j+1..i} X[i][m] L[m][j]  with X[i][i] = 1.
-    for (int j = NB - 2; j >= 0; --j) {
-        for (int m = j + 1 + tid; m < NB; m += nt) { tr[m] = ar[m * P + j]; ti[m] = ai[m * P + j]; }
+    // L^-1 in place (unit lower), column sweep:  X = I;  for k: X[i][j] -= L[i][k] X[k][j]
+    // for i > k, j <= k.  Column k of L is copied out first because X[i][k] reuses its slot.
+    for (int k = 0; k < NB - 1; ++k) {
+        for (int i = k + 1 + tid; i < NB; i += nt) { tr[i] = ar[i * P + k]; ti[i] = ai[i * P + k]; }
         __syncthreads();
-        for (int i = j + 1 + tid; i < NB; i += nt) {
-            T sr = tr[i], si = ti[i];  // X[i][i] = 1
-            for (int m = j + 1; m < i; ++m) {
-                T xr = ar[i * P + m], xi = ai[i * P + m];
-                sr += xr * tr[m] - xi * ti[m];
-                si += xr * ti[m] + xi * tr[m];
-            }
-            ar[i * P + j] = -sr;
-            ai[i * P + j] = -si;
+        const int rows = NB - 1 - k, cols = k + 1;
+        for (int idx = tid; idx < rows * cols; idx += nt) {
+            int i = k + 1 + idx / cols, j = idx % cols;
+            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
+            T cur_r = (j == k) ? (T)0 : ar[i * P + j], cur_i = (j == k) ? (T)0 : ai[i * P + j];
+            ar[i * P + j] = cur_r - (tr[i] * xr - ti[i] * xi);
+            ai[i * P + j] = cur_i - (tr[i] * xi + ti[i] * xr);
         }
         __syncthreads();
     }
-    // U^-1 in place on the upper part: for j ascending,
-    // X[j][j] = 1/U[j][j];  X[i][j] = -(sum_{m=i..j-1} X[i][m] U[m][j]) X[j][j], i < j.
-    for (int j = 0; j < NB; ++j) {
-        for (int m = tid; m <= j; m += nt) { tr[m] = ar[m * P + j]; ti[m] = ai[m * P + j]; }
+    // U^-1 in place, backward sweep:  for k descending: X[k][j] /= U[k][k] (j >= k),
+    // then X[i][j] -= U[i][k] X[k][j] for i < k, j >= k.
+    for (int k = NB - 1; k >= 0; --k) {
+        for (int i = tid; i <= k; i += nt) { tr[i] = ar[i * P + k]; ti[i] = ai[i * P + k]; }
         __syncthreads();
-        T pr = tr[j], pi = ti[j];
+        T pr = tr[k], pi = ti[k];
         T den = pr * pr + pi * pi;
         T dr = pr / den, di = -pi / den;
-        for (int i = tid; i < j; i += nt) {
-            T sr = 0, si = 0;
-            for (int m = i; m < j; ++m) {
-                T xr = ar[i * P + m], xi = ai[i * P + m];
-                sr += xr * tr[m] - xi * ti[m];
-                si += xr * ti[m] + xi * tr[m];
-            }
-            ar[i * P + j] = -(sr * dr - si * di);
-            ai[i * P + j] = -(sr * di + si * dr);
+        // row k of X: X[k][k] = 1/U[k][k]; X[k][j] (j > k) already holds sum terms -> scale
+        for (int j = k + tid; j < NB; j += nt) {
+            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
+            ar[k * P + j] = xr * dr - xi * di;
+            ai[k * P + j] = xr * di + xi * dr;
         }
-        if (tid == 0) { ar[j * P + j] = dr; ai[j * P + j] = di; }
+        __syncthreads();
+        const int cols = NB - k;
+        for (int idx = tid; idx < k * cols; idx += nt) {
+            int i = idx / cols, j = k + idx % cols;
+            T xr = ar[k * P + j], xi = ai[k * P + j];
+            T cur_r = (j == k) ? (T)0 : ar[i * P + j], cur_i = (j == k) ? (T)0 : ai[i * P + j];
+            ar[i * P + j] = cur_r - (tr[i] * xr - ti[i] * xi);
+            ai[i * P + j] = cur_i - (tr[i] * xi + ti[i] * xr);
+        }
         __syncthreads();
     }
     // inv layout: [blk][0] = L^-1 (unit lower, diagonal stored as 1), [blk][1] = U^-1.
@@ -331,114 +334,149 @@ double tc_selftest(int device, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// Block triangular solves.  X is n x R complex interleaved (T2 = {re, im}).
-// diag: Z[blk] = Inv[blk] * Yin[blk]  (one CTA; Yin, Z may alias only if equal)
-template <typename T, int NB>
-__global__ void k_trsv_diag(int blk, int R, const T* __restrict__ invr, const T* __restrict__ invi, int which,
-                            const T* __restrict__ Yin, T* __restrict__ Z) {
-    __shared__ T yr[NB * MAX_RHS], yi[NB * MAX_RHS];
-    const T* Mr = invr + ((size_t)blk * 2 + which) * NB * NB;
-    const T* Mi = invi + ((size_t)blk * 2 + which) * NB * NB;
-    const size_t base = (size_t)blk * NB;
-    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
-        int k = idx / R, j = idx % R;
-        yr[idx] = Yin[2 * ((base + k) * R + j)];
-        yi[idx] = Yin[2 * ((base + k) * R + j) + 1];
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
-        int i = idx / R, j = idx % R;
-        T sr = 0, si = 0;
-        for (int k = 0; k < NB; ++k) {
-            T mr = Mr[i * NB + k], mi = Mi[i * NB + k];
-            T vr = yr[k * R + j], vi = yi[k * R + j];
-            sr += mr * vr - mi * vi;
-            si += mr * vi + mi * vr;
-        }
-        Z[2 * ((base + i) * R + j)] = sr;
-        Z[2 * ((base + i) * R + j) + 1] = si;
-    }
-}
-
-// update: Y[r] -= A[r][blk*NB : +NB] * Z[blk] for r in [r0, r1). One warp per row.
-template <typename T, int NB>
-__global__ void __launch_bounds__(256) k_trsv_update(int blk, int r0, int r1, int R, CMat<T> A,
-                                                     const T* __restrict__ Z, T* __restrict__ Y) {
+// Cooperative block triangular solve: one CTA per diagonal block (rounds if the
+// grid is smaller than the block count).  CTA b accumulates
+//     z_b = y_b - sum_{c before b} A_bc x_c
+// taking the x_c as soon as their CTAs publish them (epoch flags with release /
+// acquire ordering), then x_b = Inv_b z_b.  Forward (which = 0): unit-lower L,
+// c < b, Inv = L_bb^-1.  Backward (which = 1): U, c > b, Inv = U_bb^-1.  The
+// launch is cooperative, so every CTA is resident and every wait is on a CTA
+// that is running or finished; the waits are bounded all the same and record
+// FLAG_TIMEOUT if they expire.
+template <typename T, int NB, int TPR>
+__global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T> A, const T* __restrict__ invr,
+                                                        const T* __restrict__ invi, int which,
+                                                        const T* __restrict__ Yin, T* __restrict__ Xout,
+                                                        int* __restrict__ ready, int epoch, int* __restrict__ gflags) {
+    constexpr int NT = NB * TPR;
+    constexpr int JPT = (MAX_RHS + TPR - 1) / TPR;  // RHS columns per thread
     __shared__ T zr[NB * MAX_RHS], zi[NB * MAX_RHS];
-    const size_t base = (size_t)blk * NB;
-    for (int idx = threadIdx.x; idx < NB * R; idx += blockDim.x) {
-        zr[idx] = Z[2 * (base * R + idx)];
-        zi[idx] = Z[2 * (base * R + idx) + 1];
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int r = r0 + blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (r >= r1) return;
-    T ar_[MAX_RHS], ai_[MAX_RHS];
+    __shared__ int timed_out;
+    const int tid = threadIdx.x;
+    const int i = tid / TPR, jq = tid % TPR;  // row within the block, RHS phase
+    if (tid == 0) timed_out = 0;
+    for (int round = blockIdx.x; round < nblk; round += gridDim.x) {
+        const int b = which == 0 ? round : nblk - 1 - round;
+        const size_t row = (size_t)b * NB + i;
+        T ar_[JPT], ai_[JPT];
 #pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) { ar_[j] = 0; ai_[j] = 0; }
-    const T* rr = A.re + (size_t)r * A.ld + base;
-    const T* ri = A.im + (size_t)r * A.ld + base;
-    for (int k = lane; k < NB; k += 32) {
-        T mr = rr[k], mi = ri[k];
+        for (int u = 0; u < JPT; ++u) {
+            int j = jq + u * TPR;
+            ar_[u] = j < R ? Yin[2 * (row * R + j)] : (T)0;
+            ai_[u] = j < R ? Yin[2 * (row * R + j) + 1] : (T)0;
+        }
+        const int cnt = which == 0 ? b : nblk - 1 - b;
+        for (int t = 0; t < cnt; ++t) {
+            const int c = which == 0 ? t : nblk - 1 - t;
+            if (tid == 0) {
+                int v = 0;
+                long it = 0;
+                for (;;) {
+                    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(ready + c) : "memory");
+                    if (v >= epoch || timed_out) break;
+                    if (++it > (1L << 26)) { timed_out = 1; atomicOr(gflags, FLAG_TIMEOUT); break; }
+                }
+                __threadfence();
+            }
+            __syncthreads();
+            for (int idx = tid; idx < NB * R; idx += NT) {
+                size_t o = 2 * (((size_t)c * NB) * R + idx);
+                zr[idx] = __ldcg(Xout + o);
+                zi[idx] = __ldcg(Xout + o + 1);
+            }
+            __syncthreads();
+            const T* lr = A.re + row * A.ld + (size_t)c * NB;
+            const T* li = A.im + row * A.ld + (size_t)c * NB;
+            for (int k = 0; k < NB; ++k) {
+                T mr = lr[k], mi = li[k];
 #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) {
+                for (int u = 0; u < JPT; ++u) {
+                    int j = jq + u * TPR;
+                    if (j < R) {
+                        T vr = zr[k * R + j], vi = zi[k * R + j];
+                        ar_[u] -= mr * vr - mi * vi;
+                        ai_[u] -= mr * vi + mi * vr;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // x_b = Inv_b z_b
+#pragma unroll
+        for (int u = 0; u < JPT; ++u) {
+            int j = jq + u * TPR;
+            if (j < R) { zr[i * R + j] = ar_[u]; zi[i * R + j] = ai_[u]; }
+        }
+        __syncthreads();
+        const T* Mr = invr + ((size_t)b * 2 + which) * NB * NB + (size_t)i * NB;
+        const T* Mi = invi + ((size_t)b * 2 + which) * NB * NB + (size_t)i * NB;
+#pragma unroll
+        for (int u = 0; u < JPT; ++u) { ar_[u] = 0; ai_[u] = 0; }
+        for (int k = 0; k < NB; ++k) {
+            T mr = Mr[k], mi = Mi[k];
+#pragma unroll
+            for (int u = 0; u < JPT; ++u) {
+                int j = jq + u * TPR;
+                if (j < R) {
+                    T vr = zr[k * R + j], vi = zi[k * R + j];
+                    ar_[u] += mr * vr - mi * vi;
+                    ai_[u] += mr * vi + mi * vr;
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < JPT; ++u) {
+            int j = jq + u * TPR;
             if (j < R) {
-                T vr = zr[k * R + j], vi = zi[k * R + j];
-                ar_[j] += mr * vr - mi * vi;
-                ai_[j] += mr * vi + mi * vr;
+                Xout[2 * (row * R + j)] = ar_[u];
+                Xout[2 * (row * R + j) + 1] = ai_[u];
             }
         }
-    }
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) {
-        if (j < R) {
-            T vr = ar_[j], vi = ai_[j];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                vr += __shfl_xor_sync(0xffffffffu, vr, off);
-                vi += __shfl_xor_sync(0xffffffffu, vi, off);
-            }
-            if (lane == 0) {
-                Y[2 * ((size_t)r * R + j)] -= vr;
-                Y[2 * ((size_t)r * R + j) + 1] -= vi;
-            }
-        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0)
+            asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(ready + b), "r"(epoch) : "memory");
     }
 }
 
-template <typename T, int NB>
-static void lu_solve_t(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* invi, int R, T* X, T* tmp) {
+template <typename T, int NB, int TPR>
+static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* invi, int which, int R,
+                     const T* Y, T* X, int* ready, int epoch, int* flags) {
     const int nblk = n / NB;
-    // forward: tmp = L^-1 X  (X updated in place below the current block)
-    for (int b = 0; b < nblk; ++b) {
-        BEM_LAUNCH(k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 0, X, tmp));
-        int r0 = (b + 1) * NB;
-        if (r0 < n) BEM_LAUNCH(k_trsv_update<T, NB><<<(n - r0 + 7) / 8, 256, 0, st>>>(b, r0, n, R, A, tmp, X));
-    }
-    // backward: X = U^-1 tmp  (tmp updated in place above the current block)
-    for (int b = nblk - 1; b >= 0; --b) {
-        BEM_LAUNCH(k_trsv_diag<T, NB><<<1, 256, 0, st>>>(b, R, invr, invi, 1, tmp, X));
-        int r1 = b * NB;
-        if (r1 > 0) BEM_LAUNCH(k_trsv_update<T, NB><<<(r1 + 7) / 8, 256, 0, st>>>(b, 0, r1, R, A, X, tmp));
-    }
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_coop<T, NB, TPR>, NB * TPR, 0);
+    int grid = std::min(nblk, std::max(1, per_sm) * nsm);
+    void* args[] = {(void*)&nblk, (void*)&R, (void*)&A, (void*)&invr, (void*)&invi, (void*)&which, (void*)&Y,
+                    (void*)&X, (void*)&ready, (void*)&epoch, (void*)&flags};
+    ++g_launches;
+    return cudaLaunchCooperativeKernel((void*)k_trsv_coop<T, NB, TPR>, dim3(grid), dim3(NB * TPR), args, 0, st) ==
+                   cudaSuccess
+               ? 0
+               : 1;
 }
 
 // The solve needs an n x R scratch; it lives right after X (caller allocates 2 n R).
-void lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X) {
-    lu_solve_t<double, 64>(st, n, A, invr, invi, R, X, X + (size_t)2 * n * R);
+// ready: n/nb ints, zero at allocation; epoch: strictly increasing per call (2 used per call).
+int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
+                 int* ready, int epoch, int* flags) {
+    double* tmp = X + (size_t)2 * n * R;
+    if (trsv_coop<double, 64, 4>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
+    return trsv_coop<double, 64, 4>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
 }
-void lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X) {
-    lu_solve_t<float, 128>(st, n, A, invr, invi, R, X, X + (size_t)2 * n * R);
+int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
+                 int* ready, int epoch, int* flags) {
+    float* tmp = X + (size_t)2 * n * R;
+    if (trsv_coop<float, 128, 2>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
+    return trsv_coop<float, 128, 2>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
 }
 
 // ---------------------------------------------------------------------------
-// Rres = Y - D X in FP64; one warp per row.  nrm[j] = max_r |Rres[r][j]|,
-// nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (non-negative doubles).
+// Rres = Y - D X in FP64; one warp per row (Di null: real part of D only).
 __global__ void __launch_bounds__(256) k_residual(int N, int ld, const double* __restrict__ Dr,
                                                   const double* __restrict__ Di, int R, const double* __restrict__ X,
-                                                  const double* __restrict__ Y, double* __restrict__ Rres,
-                                                  unsigned long long* nrm) {
+                                                  const double* __restrict__ Y, double* __restrict__ Rres) {
     const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (r >= N) return;
@@ -446,9 +484,9 @@ __global__ void __launch_bounds__(256) k_residual(int N, int ld, const double* _
 #pragma unroll
     for (int j = 0; j < MAX_RHS; ++j) { ar_[j] = 0; ai_[j] = 0; }
     const double* rr = Dr + (size_t)r * ld;
-    const double* ri = Di + (size_t)r * ld;
+    const double* ri = Di ? Di + (size_t)r * ld : nullptr;
     for (int s = lane; s < N; s += 32) {
-        double mr = rr[s], mi = ri[s];
+        double mr = rr[s], mi = ri ? ri[s] : 0.0;
         const double* x = X + 2 * (size_t)s * R;
 #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) {
@@ -471,14 +509,43 @@ __global__ void __launch_bounds__(256) k_residual(int N, int ld, const double* _
                 vi += __shfl_xor_sync(0xffffffffu, vi, off);
             }
             if (lane == 0) {
-                double yr = Y[2 * ((size_t)r * R + j)], yi = Y[2 * ((size_t)r * R + j) + 1];
-                double er = yr - vr, ei = yi - vi;
-                Rres[2 * ((size_t)r * R + j)] = er;
-                Rres[2 * ((size_t)r * R + j) + 1] = ei;
-                double en = sqrt(er * er + ei * ei), yn = sqrt(yr * yr + yi * yi);
-                if (!isfinite(en)) en = 1.0e300;
-                atomicMax(nrm + j, (unsigned long long)__double_as_longlong(en));
-                atomicMax(nrm + R + j, (unsigned long long)__double_as_longlong(yn));
+                Rres[2 * ((size_t)r * R + j)] = Y[2 * ((size_t)r * R + j)] - vr;
+                Rres[2 * ((size_t)r * R + j) + 1] = Y[2 * ((size_t)r * R + j) + 1] - vi;
+            }
+        }
+    }
+}
+
+// Per-column max |Rres| and max |Y| (non-negative doubles compare as integers).
+__global__ void k_norms(int N, int R, const double* __restrict__ Rres, const double* __restrict__ Y,
+                        unsigned long long* nrm) {
+    double rn[MAX_RHS], yn[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { rn[j] = 0; yn[j] = 0; }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                size_t o = 2 * ((size_t)r * R + j);
+                double e = sqrt(Rres[o] * Rres[o] + Rres[o + 1] * Rres[o + 1]);
+                if (!isfinite(e)) e = 1.0e300;
+                rn[j] = fmax(rn[j], e);
+                yn[j] = fmax(yn[j], sqrt(Y[o] * Y[o] + Y[o + 1] * Y[o + 1]));
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            double a = rn[j], b = yn[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                a = fmax(a, __shfl_xor_sync(0xffffffffu, a, off));
+                b = fmax(b, __shfl_xor_sync(0xffffffffu, b, off));
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicMax(nrm + j, (unsigned long long)__double_as_longlong(a));
+                atomicMax(nrm + R + j, (unsigned long long)__double_as_longlong(b));
             }
         }
     }
@@ -499,8 +566,11 @@ __global__ void k_pad_rhs(int N, int Np, int R, double* X) {
 }
 
 void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
-                     const double* Y, double* Rres, unsigned long long* nrm) {
-    BEM_LAUNCH(k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres, nrm));
+                     const double* Y, double* Rres) {
+    BEM_LAUNCH(k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres));
+}
+void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm) {
+    BEM_LAUNCH(k_norms<<<152, 256, 0, st>>>(N, R, Rres, Y, nrm));
 }
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst) {
     BEM_LAUNCH(k_to_f32<<<1024, 256, 0, st>>>(n, src, dst));
