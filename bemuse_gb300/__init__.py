@@ -16,7 +16,8 @@ from . import build as _build
 
 __all__ = [
     "BEMError", "lib", "Parameter", "Mesh", "Half_Cylinder", "Barge", "unify",
-    "Hydrodynamic_Radiation_Solver", "havelock_gf", "dense_solve", "PLAIN_FP64", "MIXED",
+    "Hydrodynamic_Radiation_Solver", "Aerodynamic_Solver", "NACA_Wing", "havelock_gf", "dense_solve",
+    "PLAIN_FP64", "MIXED",
 ]
 
 PLAIN_FP64 = 0
@@ -83,6 +84,10 @@ def lib():
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
+        "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
+        "bem_mesh_wing": ([c_double, c_double, c_double, c_int, c_int, c_int, _dp, _ip], c_int),
+        "bem_aero_setup": ([vp, ctypes.POINTER(_Mesh)], c_int),
+        "bem_aero_solve": ([vp, c_int, _dp, c_int, c_double, _dp, _dp], c_int),
         "bem_selftest_tc": ([c_int, c_int], c_double),
     }
     for name, (args, res) in sig.items():
@@ -169,6 +174,18 @@ def Barge(Tank_Length, Tank_Width, Tank_Depth, NPanels_Tank_Length, NPanels_Tank
     _check(L.bem_mesh_barge(Tank_Length, Tank_Width, Tank_Depth, NPanels_Tank_Length, NPanels_Tank_Width,
                             NPanels_Tank_Depth, int(Cosine_Disc), _p(nodes), _p(elems, _ip), _p(an), _p(ae, _ip)))
     return Mesh(nodes, elems, aux=Mesh(an, ae))
+
+
+def NACA_Wing(chord=1.0, span=8.0, thickness=0.12, n_chord=120, n_span=60, cosine=True):
+    """Rectangular wing of a symmetric NACA 00xx section (n_chord panels around
+    the section, n_span strips; normals into the wing)."""
+    L = lib()
+    nn, ne = ctypes.c_int(), ctypes.c_int()
+    _check(L.bem_mesh_wing_sizes(n_chord, n_span, nn, ne))
+    nodes = np.zeros((nn.value, 3))
+    elems = np.zeros((ne.value, 4), np.int32)
+    _check(L.bem_mesh_wing(chord, span, thickness, n_chord, n_span, int(cosine), _p(nodes), _p(elems, _ip)))
+    return Mesh(nodes, elems)
 
 
 def unify(meshes, origins):
@@ -331,6 +348,49 @@ class Hydrodynamic_Radiation_Solver:
         t = np.zeros(6)
         _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
         return t
+
+
+class Aerodynamic_Solver:
+    """Drop-in for BEMUse::Aerodynamic_Solver with constant panels
+    (Aerodynamic_Solver.cpp:12-180): Setup(mesh) -> Set_External_BC(vels) ->
+    Solve_Steady(); the perturbation potential is X (one value per panel)."""
+
+    def __init__(self, device=0, precision=PLAIN_FP64, refine_tol=1e-12):
+        L = lib()
+        h = ctypes.c_void_p()
+        _check(L.bem_create(ctypes.byref(h), int(device)))
+        self._h = h
+        self.precision = precision
+        self.refine_tol = refine_tol
+        self.vels = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().bem_destroy(h)
+            self._h = None
+
+    def Set_Parameters(self, params):
+        for name, _ in params:
+            if name == "BilinearPanels":
+                raise BEMError(6, "bilinear panels are not implemented (constant panels only)")
+
+    def Setup(self, mesh):
+        self.mesh = mesh
+        ms = mesh._struct()
+        _check(lib().bem_aero_setup(self._h, ctypes.byref(ms)), self._h)
+        self.N = mesh.n
+
+    def Set_External_BC(self, vels):
+        self.vels = np.ascontiguousarray(vels, dtype=np.float64).reshape(-1, 3)
+
+    def Solve_Steady(self):
+        X = np.zeros(self.N)
+        BC = np.zeros(self.N)
+        _check(lib().bem_aero_solve(self._h, self.vels.shape[0], _p(self.vels), int(self.precision),
+                                    float(self.refine_tol), _p(X), _p(BC)), self._h)
+        self.X, self.BC = X, BC
+        return X
 
 
 def havelock_gf(x, y, v, precision=PLAIN_FP64, device=0):

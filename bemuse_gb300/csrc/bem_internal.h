@@ -55,8 +55,6 @@ void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D
 void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
                      double* Bm);
-void launch_rhs_static(cudaStream_t st, int N, int ld, int R, int j0, int j1, const double* RS, const double* Bm,
-                       double* Y);
 void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
                  const double* phiI, const double* dphiI, double* part, double* out);
 void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,
@@ -88,9 +86,13 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
                  int* ready, int epoch, int* flags);
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags);
-// Rres = Y - D X in FP64 (Di may be null: real operator part only).
-void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
-                     const double* Y, double* Rres);
+// out[:, j0:j0+R] = beta * base[:, j0:j0+R] + alpha * M X[:, j0:j0+R] for an N x N
+// row-major matrix M (real if Mi is null, else planar complex), X, base, out
+// N x stride complex interleaved.  part: scratch of matx_part_doubles(N, R) doubles.
+size_t matx_part_doubles(int N, int R);
+void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double* Mi, int R, int j0, const double* X,
+                 int xstride, double* part, double alpha, double beta, const double* base, double* out,
+                 int ostride);
 // nrm[j] = max_r |Rres[r][j]|, nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (zero them first).
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm);
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
@@ -98,6 +100,8 @@ void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
 
 int tc_gemm_supported(int device);
+// Sets the message returned by bem_last_error(NULL).
+void set_static_error(const char* msg);
 // C -= L U^T-trailing update on random data with the tensor-core and SIMT kernels;
 // returns max |tc - simt| / max |simt| (negative on setup failure).
 double tc_selftest(int device, int n);

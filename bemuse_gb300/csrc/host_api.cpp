@@ -4,7 +4,7 @@
 // Pipeline of one frequency-solve (Hydrodynamic_Radiation_Solver::Solve,
 // Hydrodynamic_Solver.cpp:400-487), all on the context's stream:
 //   k_incident      phi_I, dphi_I/dn, diffraction RHS columns      (:444, :575-596)
-//   k_rhs_static    (Ssrc + Srefl) * B_diff                        (:437, :445)
+//   launch_matx     (Ssrc + Srefl) * B_diff                        (:437, :445)
 //   k_wave          D = Drankine + Dwave and Y += (-ws) * B        (:413-429)
 //   LU              FP64 (plain) or TF32 tensor-core (mixed)       (:430)
 //   solve / refine  FP64 residual against the FP64 operator        (:438, :446)
@@ -36,6 +36,7 @@ struct bem_ctx {
     double rho = 1025.0, grav = 9.81;
     std::vector<double> betas;
     bool ready = false;
+    bool aero = false;                // set up by bem_aero_setup (G in d_RS, H in d_RD)
     int N = 0, Np = 0, NB = 0, R = 6;
     std::vector<double> cen, nrm, area, Nk;  // host copies
     double M[36], C[36], volcob[4];
@@ -48,7 +49,7 @@ struct bem_ctx {
     float *d_D32r = nullptr, *d_D32i = nullptr;
     double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
     float* d_X32 = nullptr;
-    double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr;
+    double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr, *d_mx = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
     float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
     int* d_flags = nullptr;
@@ -115,7 +116,7 @@ void free_all(bem_ctx* ctx) {
     double** dp[] = {&ctx->d_rec, &ctx->d_xr, &ctx->d_gq, &ctx->d_rn, &ctx->d_cen, &ctx->d_nrm, &ctx->d_area,
                      &ctx->d_Nk, &ctx->d_betas, &ctx->d_RS, &ctx->d_RD, &ctx->d_RSR, &ctx->d_D64r, &ctx->d_D64i,
                      &ctx->d_Bm, &ctx->d_Y, &ctx->d_Ys6, &ctx->d_X, &ctx->d_Rr, &ctx->d_phiI, &ctx->d_dphiI,
-                     &ctx->d_part, &ctx->d_post, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
+                     &ctx->d_part, &ctx->d_post, &ctx->d_mx, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
     for (auto p : dp) *p = nullptr;
     float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
                     &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32};
@@ -216,6 +217,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_Rr, (size_t)2 * Np * R);
     }
     DA(ctx->d_X, (size_t)4 * Np * R);
+    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
     DA(ctx->d_flags, 1);
     if (!ctx->d_ready) {
         DA(ctx->d_ready, Np / 64);
@@ -275,13 +277,14 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
             CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
             if (ctx->resid_mode == 2) {
                 // r = y - Re(D) x  (stored FP64) - i Im(D) x  (plane waves, FP64)
-                bem::launch_residual(st, N, Np, ctx->d_D64r, nullptr, R, ctx->d_X, ctx->d_Y, ctx->d_Rr);
+                bem::launch_matx(st, N, Np, ctx->d_D64r, nullptr, R, 0, ctx->d_X, R, ctx->d_mx, -1.0, 1.0, ctx->d_Y,
+                                 ctx->d_Rr, R);
                 const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
                 bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M, ctx->d_pwW,
                                        ctx->d_pwE, ctx->d_X, ctx->d_pwT, ctx->d_Rr);
             } else {
-                bem::launch_residual(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R,
-                                     ctx->d_X, ctx->d_Y, ctx->d_Rr);
+                bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0,
+                                 ctx->d_X, R, ctx->d_mx, -1.0, 1.0, ctx->d_Y, ctx->d_Rr, R);
             }
             bem::launch_norms(st, N, R, ctx->d_Rr, ctx->d_Y, ctx->d_norms);
             CK(cudaGetLastError());
@@ -328,6 +331,8 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
 }
 
 }  // namespace
+
+void bem::set_static_error(const char* msg) { snprintf(g_static_err, sizeof(g_static_err), "%s", msg); }
 
 extern "C" {
 
@@ -422,6 +427,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     if (mesh->n_comp > 0 && (mesh->comp_first[0] != 0 || mesh->comp_first[mesh->n_comp] != mesh->n_elems))
         return fail(ctx, BEM_ERR_ARG, "components must cover the element list");
     free_all(ctx);
+    ctx->aero = false;
     bem::MeshView mv{mesh->n_nodes, mesh->nodes, mesh->n_elems, mesh->elems, mesh->n_comp, mesh->comp_first,
                      mesh->comp_origin};
     std::vector<bem::PanelGeom> body, mirror;
@@ -564,7 +570,8 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     // K1: Rankine influence (once per body), then Ys6 = RS * N_k
     bem::launch_rankine(st, N, Np, ctx->d_rec, ctx->d_xr, ctx->d_rn, 0, ctx->d_RS, ctx->d_RD, ctx->d_RSR, nullptr);
     CK(cudaGetLastError());
-    bem::launch_rhs_static(st, N, Np, R, 0, 6, ctx->d_RS, ctx->d_Bm, ctx->d_Ys6);
+    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 6, 0, ctx->d_Bm, R, ctx->d_mx, 1.0, 0.0, nullptr, ctx->d_Ys6, R);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->ready = true;
@@ -592,7 +599,7 @@ bem_status bem_get_body_matrices(const bem_ctx* cctx, double* M, double* C, doub
 
 bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double tol, bem_result* out) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
-    if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_solve before bem_setup");
+    if (!ctx->ready || ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_solve before bem_setup");
     if (n_freq < 0 || (n_freq > 0 && !omega)) return fail(ctx, BEM_ERR_ARG, "bad frequency list");
     if (precision != BEM_PLAIN_FP64 && precision != BEM_MIXED) return fail(ctx, BEM_ERR_ARG, "unknown precision mode");
     for (int f = 0; f < n_freq; ++f)
@@ -615,7 +622,9 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         // Y[:, 0:6] = RS N_k (precomputed); Y[:, 6:] = RS B_diff
         CK(cudaMemcpy2DAsync(ctx->d_Y, sizeof(double) * 2 * R, ctx->d_Ys6, sizeof(double) * 2 * R,
                              sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToDevice, st));
-        if (NB > 0) bem::launch_rhs_static(st, N, Np, R, 6, R, ctx->d_RS, ctx->d_Bm, ctx->d_Y);
+        if (NB > 0)
+            bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, NB, 6, ctx->d_Bm, R, ctx->d_mx, 1.0, 0.0, nullptr,
+                             ctx->d_Y, R);
         CK(cudaEventRecord(ctx->ev[1], st));
         bem::WaveArgs a;
         memset(&a, 0, sizeof(a));
@@ -824,6 +833,103 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     free_all(ctx);
     if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_dense_solve: ") + cudaGetErrorString(e));
+    return BEM_OK;
+}
+
+int bem_mesh_wing_sizes(int nc, int ns, int* nn, int* ne) {
+    if (nc < 4 || nc % 2 || ns < 1 || !nn || !ne) return BEM_ERR_ARG;
+    bem::wing_sizes(nc, ns, nn, ne);
+    return BEM_OK;
+}
+
+int bem_mesh_wing(double chord, double span, double thickness, int nc, int ns, int cosine, double* nodes,
+                  int* elems) {
+    if (nc < 4 || nc % 2 || ns < 1 || !nodes || !elems || !(chord > 0) || !(span > 0) || !(thickness > 0))
+        return BEM_ERR_ARG;
+    bem::wing_mesh(chord, span, thickness, nc, ns, cosine != 0, nodes, elems);
+    return BEM_OK;
+}
+
+bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!mesh) return fail(ctx, BEM_ERR_ARG, "null mesh");
+    CK(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    bem::MeshView mv{mesh->n_nodes, mesh->nodes, mesh->n_elems, mesh->elems, mesh->n_comp, mesh->comp_first,
+                     mesh->comp_origin};
+    std::vector<bem::PanelGeom> body, mirror;
+    std::string gerr;
+    if (!bem::build_geometry(mv, body, mirror, gerr)) return fail(ctx, BEM_ERR_ARG, "mesh: " + gerr);
+    const int N = mesh->n_elems, Np = round_up(N, bem::LD_ALIGN);
+    ctx->N = N; ctx->Np = Np; ctx->NB = 0; ctx->R = 1;
+    std::vector<double> rec((size_t)2 * N * bem::RK_STRIDE, 0.0), xr;
+    ctx->nrm.assign(3 * (size_t)N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        bem::rankine_record(body[i], &rec[(size_t)i * bem::RK_STRIDE]);
+        for (int d = 0; d < 3; ++d) ctx->nrm[(size_t)d * N + i] = body[i].e[6 + d];
+    }
+    bem::collocation_points(body, xr);
+    DA(ctx->d_rec, rec.size());
+    DA(ctx->d_xr, xr.size());
+    DA(ctx->d_RS, (size_t)N * Np);
+    DA(ctx->d_RD, (size_t)N * Np);
+    DA(ctx->d_D64r, (size_t)Np * Np);
+    DA(ctx->d_D64i, (size_t)Np * Np);
+    DA(ctx->d_Bm, 2 * (size_t)N);
+    DA(ctx->d_Y, 2 * (size_t)N);
+    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    cudaStream_t st = ctx->st;
+    CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
+    bem::launch_rankine(st, N, Np, ctx->d_rec, ctx->d_xr, nullptr, 2, ctx->d_RS, ctx->d_RD, nullptr, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    ctx->aero = true;
+    ctx->ready = true;
+    return BEM_OK;
+}
+
+bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precision, double tol, double* X,
+                          double* BC) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready || !ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_aero_solve before bem_aero_setup");
+    const int N = ctx->N, Np = ctx->Np;
+    if (!vel || (n_vel != 1 && n_vel != N)) return fail(ctx, BEM_ERR_ARG, "velocity count must be 1 or N");
+    if (precision != BEM_PLAIN_FP64 && precision != BEM_MIXED) return fail(ctx, BEM_ERR_ARG, "unknown precision");
+    if (!(tol > 0)) tol = 1e-12;
+    CK(cudaSetDevice(ctx->device));
+    const bool mixed = precision == BEM_MIXED;
+    // Set_External_BC (Aerodynamic_Solver.cpp:150-166): BC_i = V_i . n_i
+    std::vector<double> bc(N), bcz(2 * (size_t)N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        const double* v = n_vel == 1 ? vel : vel + 3 * (size_t)i;
+        bc[i] = v[0] * ctx->nrm[i] + v[1] * ctx->nrm[(size_t)N + i] + v[2] * ctx->nrm[2 * (size_t)N + i];
+        bcz[2 * (size_t)i] = bc[i];
+    }
+    cudaStream_t st = ctx->st;
+    bem_status s = ensure_lu_buffers(ctx, Np, 1, mixed);
+    if (s != BEM_OK) return s;
+    CK(cudaMemcpyAsync(ctx->d_Bm, bcz.data(), bcz.size() * 8, cudaMemcpyHostToDevice, st));
+    // Solve_Steady (:169-180): S = G BC, X = H^-1 S
+    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 1, 0, ctx->d_Bm, 1, ctx->d_mx, 1.0, 0.0, nullptr, ctx->d_Y, 1);
+    CK(cudaMemcpyAsync(ctx->d_D64r, ctx->d_RD, sizeof(double) * (size_t)N * Np, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemsetAsync(ctx->d_D64i, 0, sizeof(double) * (size_t)Np * Np, st));
+    bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, nullptr, nullptr);
+    if (mixed) {
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->d_D32r);
+        CK(cudaMemsetAsync(ctx->d_D32i, 0, sizeof(float) * (size_t)Np * Np, st));
+    }
+    CK(cudaGetLastError());
+    int iters = 0;
+    double resid = 0, t0 = 0, t1 = 0;
+    ctx->resid_mode = mixed ? 1 : 0;
+    s = factor_and_solve(ctx, N, Np, 1, mixed, tol, 60, &iters, &resid, &t0, &t1);
+    ctx->resid_mode = 0;
+    if (s != BEM_OK) return s;
+    std::vector<double> x(2 * (size_t)N);
+    CK(cudaMemcpy(x.data(), ctx->d_X, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost));
+    if (X) for (int i = 0; i < N; ++i) X[i] = x[2 * (size_t)i];
+    if (BC) memcpy(BC, bc.data(), sizeof(double) * N);
     return BEM_OK;
 }
 

@@ -40,6 +40,8 @@ void cylinder_mesh(double R, double draft, int NA, int NR, int NV, int NRFS, boo
 void barge_sizes(int NX, int NY, int NZ, int* nn, int* ne, int* nna, int* nea);
 void barge_mesh(double L, double W, double D, int NX, int NY, int NZ, bool cosine, double* nodes, int* elems,
                 double* aux_nodes, int* aux_elems);
+void wing_sizes(int nc, int ns, int* nn, int* ne);
+void wing_mesh(double chord, double span, double t, int nc, int ns, bool cosine, double* nodes, int* elems);
 void mass_and_stiffness(const std::vector<PanelGeom>& body, const std::vector<PanelGeom>* aux, double rho, double g,
                         double mass, const double* cog, const double* gyr, double* M, double* C, double* vc);
 

@@ -337,6 +337,51 @@ void barge_mesh(double L, double W, double D, int NX, int NY, int NZ, bool cosin
     }
 }
 
+// Rectangular wing of a symmetric NACA 00xx section (chord c, span b, thickness
+// ratio t): half-cosine chordwise spacing on both surfaces, uniform spanwise
+// strips, open tips.  Section nodes run from the trailing edge along the lower
+// surface to the leading edge and back along the upper surface; the trailing
+// edge is closed (thickness coefficient -0.1036, Airfoil_Profiles.h:93).
+// x chordwise (0 = leading edge), y spanwise (centred), z thickness; panel
+// normals point into the wing, as the reference's body panels do.
+void wing_sizes(int nc, int ns, int* nn, int* ne) {
+    *nn = nc * (ns + 1);
+    *ne = nc * ns;
+}
+
+void wing_mesh(double chord, double span, double t, int nc, int ns, bool cosine, double* nodes, int* elems) {
+    const int half = nc / 2;
+    std::vector<double> xs(nc), zs(nc);
+    for (int k = 0; k < nc; ++k) {
+        // k = 0: trailing edge; k = half: leading edge
+        int i = k <= half ? half - k : k - half;                 // chordwise station 0..half
+        double f = cosine ? 0.5 * (1.0 - std::cos(kPi * i / half)) : 1.0 * i / half;
+        double x = f;
+        double yt = 5.0 * t * (0.2969 * std::sqrt(x) - 0.1260 * x - 0.3516 * x * x + 0.2843 * x * x * x -
+                               0.1036 * x * x * x * x);
+        xs[k] = chord * x;
+        zs[k] = chord * (k <= half ? -yt : yt);
+    }
+    for (int j = 0; j <= ns; ++j) {
+        double y = -0.5 * span + span * j / ns;
+        for (int k = 0; k < nc; ++k) {
+            size_t id = (size_t)j * nc + k;
+            nodes[3 * id] = xs[k];
+            nodes[3 * id + 1] = y;
+            nodes[3 * id + 2] = zs[k];
+        }
+    }
+    size_t e = 0;
+    for (int j = 0; j < ns; ++j)
+        for (int k = 0; k < nc; ++k, ++e) {
+            int k1 = (k + 1) % nc;
+            elems[4 * e] = j * nc + k;
+            elems[4 * e + 1] = j * nc + k1;
+            elems[4 * e + 2] = (j + 1) * nc + k1;
+            elems[4 * e + 3] = (j + 1) * nc + k;
+        }
+}
+
 // Calculate_Volume / Calculate_COB (Boundary_Base.cpp:177-224, with
 // Calculate_GridParams :125-150 for the zero clean-up), Calculate_Mass_Matrix
 // and Calculate_Hydrostatic_Stiffness_Matrix (Hydrodynamic_Solver.cpp:300-397).

@@ -8,7 +8,7 @@
 //                  Rankine part (Solve :415-429) and with the source matrix applied
 //                  to the right-hand sides (Solve :437, :445) so that S is never stored.
 //   k_incident     Calc_Phi_Incident / Set_Incident_Potential_Mats (:544-596).
-//   k_rhs_static   (Ssrc + Srefl) * B, the frequency-independent half of S * B.
+//   (Ssrc + Srefl) * B, the Rankine half of S * B, is launch_matx (k_lu.cu).
 //   k_post_*       AddedMassMat * Phi_J, AddedMassMat * Phi_I, Phi_J^T (dPhi_I .* A)
 //                  (:462-476).
 //
@@ -69,6 +69,7 @@ __device__ __forceinline__ void source_kernel(const double* __restrict__ p, doub
 
 // mode 0: RS = -(s + sr), RD = d + dr, RSR = -sr * 2 n_z(S)  (composed, ld stride)
 // mode 1: o0 = s, o1 = sr, o2 = d, o3 = dr                    (raw, ld stride)
+// mode 2: o0 = s, o1 = d of the body panels only               (aero G and H)
 __global__ void __launch_bounds__(256) k_rankine(int N, int ld, const double* __restrict__ rec,
                                                  const double* __restrict__ xr, const double* __restrict__ rn,
                                                  int mode, double* __restrict__ o0, double* __restrict__ o1,
@@ -79,8 +80,13 @@ __global__ void __launch_bounds__(256) k_rankine(int N, int ld, const double* __
     double Px = xr[r], Py = xr[N + r], Pz = xr[2 * N + r];
     double sd, dd, sm, dm;
     source_kernel(rec + (size_t)s * RK_STRIDE, Px, Py, Pz, sd, dd);
-    source_kernel(rec + ((size_t)N + s) * RK_STRIDE, Px, Py, Pz, sm, dm);
     size_t o = (size_t)r * ld + s;
+    if (mode == 2) {  // aero: G = s, H = d of the body panels only (Aerodynamic_Solver.cpp:49-54)
+        o0[o] = sd;
+        o1[o] = dd;
+        return;
+    }
+    source_kernel(rec + ((size_t)N + s) * RK_STRIDE, Px, Py, Pz, sm, dm);
     if (mode == 0) {
         o0[o] = (-sd) + (-sm);
         o1[o] = dd + dm;
@@ -471,38 +477,6 @@ __global__ void k_incident(int N, int NB, int R, const double* __restrict__ beta
     }
 }
 
-// Y[:, j0:j1] = RS * B[:, j0:j1] (RS real N x N, B complex N x R). One warp per row.
-__global__ void __launch_bounds__(256) k_rhs_static(int N, int ld, int R, int j0, int j1,
-                                                    const double* __restrict__ RS, const double* __restrict__ Bm,
-                                                    double* __restrict__ Y) {
-    const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (r >= N) return;
-    double ar[MAX_RHS], ai[MAX_RHS];
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
-    const double* row = RS + (size_t)r * ld;
-    for (int s = lane; s < N; s += 32) {
-        double v = row[s];
-        const double* b = Bm + (size_t)s * 2 * R;
-#pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j)
-            if (j >= j0 && j < j1) { ar[j] += v * b[2 * j]; ai[j] += v * b[2 * j + 1]; }
-    }
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) {
-        if (j >= j0 && j < j1) {
-            double vr = ar[j], vi = ai[j];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                vr += __shfl_xor_sync(0xffffffffu, vr, off);
-                vi += __shfl_xor_sync(0xffffffffu, vi, off);
-            }
-            if (lane == 0) { Y[2 * ((size_t)r * R + j)] = vr; Y[2 * ((size_t)r * R + j) + 1] = vi; }
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Hull integrations (Hydrodynamic_Solver.cpp:462-476).  X = solution (N x R,
 // interleaved complex; columns 0..5 = Phi_J).  Outputs per CTA partial sums of
@@ -653,11 +627,6 @@ void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
                      double* Bm) {
     BEM_LAUNCH(k_incident<<<(N + 127) / 128, 128, 0, st>>>(N, NB, R, betas, K, Omega, cen, nrm, area, phiI, dphiI, Bm));
-}
-
-void launch_rhs_static(cudaStream_t st, int N, int ld, int R, int j0, int j1, const double* RS, const double* Bm,
-                       double* Y) {
-    BEM_LAUNCH(k_rhs_static<<<(N + 7) / 8, 256, 0, st>>>(N, ld, R, j0, j1, RS, Bm, Y));
 }
 
 void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,

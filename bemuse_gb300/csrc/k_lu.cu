@@ -8,11 +8,10 @@
 // have exchanged rows.  With no flag raised, L and U are those of partial
 // pivoting with the identity permutation.
 //
-// Step k0 (block width nb):
-//   k_lu_diag      one CTA factors D11 in shared memory and forms L11^-1, U11^-1
-//   k_cgemm        L21 = A21 U11^-1 and U12 = L11^-1 A12 (into workspaces)
-//   k_copy_back    writes L21 / U12 into the matrix, checks |l_ik| <= 1
-//   k_cgemm / tc   A22 -= L21 U12 (SIMT complex GEMM; tcgen05 TF32 in k_tc_gemm.cu)
+// Step k0 (block width nb), block LU:
+//   k_gj_inv       one CTA inverts the diagonal block D11 (Gauss-Jordan, shared memory)
+//   k_cgemm        W21 = A21 D11^-1 (into a workspace), k_copy_back stores it in place
+//   k_cgemm / tc   A22 -= W21 A12 (SIMT complex GEMM; tcgen05 TF32 in k_tc_gemm.cu)
 // Solves (k_trsv_coop) use the stored off-diagonal blocks and the diagonal-block inverses.
 #include "bem_internal.h"
 #include <cstdio>
@@ -27,14 +26,20 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
 // ---------------------------------------------------------------------------
+// In-place Gauss-Jordan inverse of the nb x nb diagonal block (the current Schur
+// complement block), no row exchanges, in shared memory; written to inv[blk].
+// Multipliers |a_ik / a_kk| > 1 below the pivot raise FLAG_PIVOT (partial
+// pivoting would have exchanged rows inside the block); a zero or non-finite
+// pivot raises FLAG_ZERO_PIVOT.
 template <typename T, int NB>
-__global__ void __launch_bounds__(1024) k_lu_diag(int k0, CMat<T> A, T* invr, T* invi, int* flags) {
+__global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* invi, int* flags) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int P = NB + 1;
     T* ar = reinterpret_cast<T*>(smem_raw);
     T* ai = ar + NB * P;
-    T* tr = ai + NB * P;  // column scratch
-    T* ti = tr + NB;
+    T* cr = ai + NB * P;  // pivot column copy
+    T* ci = cr + NB;
+    __shared__ T pinv[2];
     const int tid = threadIdx.x, nt = blockDim.x;
     const size_t ld = A.ld;
     for (int idx = tid; idx < NB * NB; idx += nt) {
@@ -46,89 +51,51 @@ __global__ void __launch_bounds__(1024) k_lu_diag(int k0, CMat<T> A, T* invr, T*
     __syncthreads();
     int local_flags = 0;
     for (int k = 0; k < NB; ++k) {
-        T pr = ar[k * P + k], pi = ai[k * P + k];
-        T den = pr * pr + pi * pi;
-        if (!(den > (T)0) || !finite_(den)) local_flags |= FLAG_ZERO_PIVOT;
-        T ir = pr / den, ii = -pi / den;
-        for (int i = k + 1 + tid; i < NB; i += nt) {
-            T xr = ar[i * P + k], xi = ai[i * P + k];
-            T lr = xr * ir - xi * ii, li = xr * ii + xi * ir;
-            ar[i * P + k] = lr;
-            ai[i * P + k] = li;
+        // pivot column (before it is overwritten) and 1 / pivot
+        for (int i = tid; i < NB; i += nt) { cr[i] = ar[i * P + k]; ci[i] = ai[i * P + k]; }
+        if (tid == 0) {
+            T pr = ar[k * P + k], pi = ai[k * P + k];
+            T den = pr * pr + pi * pi;
+            if (!(den > (T)0) || !isfinite(den)) local_flags |= FLAG_ZERO_PIVOT;
+            pinv[0] = pr / den;
+            pinv[1] = -pi / den;
+        }
+        __syncthreads();
+        const T qr = pinv[0], qi = pinv[1];
+        // row k: a_kj /= p (j != k), a_kk = 1/p
+        for (int j = tid; j < NB; j += nt) {
+            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
+            ar[k * P + j] = xr * qr - xi * qi;
+            ai[k * P + j] = xr * qi + xi * qr;
+        }
+        if (tid > k && tid < NB) {
+            T lr = cr[tid] * qr - ci[tid] * qi, li = cr[tid] * qi + ci[tid] * qr;
             if (lr * lr + li * li > (T)(1.000002)) local_flags |= FLAG_PIVOT;
         }
         __syncthreads();
-        const int m = NB - k - 1;
-        for (int idx = tid; idx < m * m; idx += nt) {
-            int i = k + 1 + idx / m, j = k + 1 + idx % m;
-            T lr = ar[i * P + k], li = ai[i * P + k];
+        // rows i != k: a_ij -= c_i a_kj (j != k); a_ik = -c_i / p
+        for (int idx = tid; idx < NB * NB; idx += nt) {
+            int i = idx / NB, j = idx % NB;
+            if (i == k) continue;
+            T fr = cr[i], fi = ci[i];
             T ur = ar[k * P + j], ui = ai[k * P + j];
-            ar[i * P + j] -= lr * ur - li * ui;
-            ai[i * P + j] -= lr * ui + li * ur;
+            if (j == k) {
+                ar[i * P + j] = -(fr * ur - fi * ui);
+                ai[i * P + j] = -(fr * ui + fi * ur);
+            } else {
+                ar[i * P + j] -= fr * ur - fi * ui;
+                ai[i * P + j] -= fr * ui + fi * ur;
+            }
         }
         __syncthreads();
     }
-    // Factors back to the matrix.
-    for (int idx = tid; idx < NB * NB; idx += nt) {
-        int i = idx / NB, j = idx % NB;
-        size_t g = (size_t)(k0 + i) * ld + k0 + j;
-        A.re[g] = ar[i * P + j];
-        A.im[g] = ai[i * P + j];
-    }
-    __syncthreads();
-    // L^-1 in place (unit lower), column sweep:  X = I;  for k: X[i][j] -= L[i][k] X[k][j]
-    // for i > k, j <= k.  Column k of L is copied out first because X[i][k] reuses its slot.
-    for (int k = 0; k < NB - 1; ++k) {
-        for (int i = k + 1 + tid; i < NB; i += nt) { tr[i] = ar[i * P + k]; ti[i] = ai[i * P + k]; }
-        __syncthreads();
-        const int rows = NB - 1 - k, cols = k + 1;
-        for (int idx = tid; idx < rows * cols; idx += nt) {
-            int i = k + 1 + idx / cols, j = idx % cols;
-            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
-            T cur_r = (j == k) ? (T)0 : ar[i * P + j], cur_i = (j == k) ? (T)0 : ai[i * P + j];
-            ar[i * P + j] = cur_r - (tr[i] * xr - ti[i] * xi);
-            ai[i * P + j] = cur_i - (tr[i] * xi + ti[i] * xr);
-        }
-        __syncthreads();
-    }
-    // U^-1 in place, backward sweep:  for k descending: X[k][j] /= U[k][k] (j >= k),
-    // then X[i][j] -= U[i][k] X[k][j] for i < k, j >= k.
-    for (int k = NB - 1; k >= 0; --k) {
-        for (int i = tid; i <= k; i += nt) { tr[i] = ar[i * P + k]; ti[i] = ai[i * P + k]; }
-        __syncthreads();
-        T pr = tr[k], pi = ti[k];
-        T den = pr * pr + pi * pi;
-        T dr = pr / den, di = -pi / den;
-        // row k of X: X[k][k] = 1/U[k][k]; X[k][j] (j > k) already holds sum terms -> scale
-        for (int j = k + tid; j < NB; j += nt) {
-            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
-            ar[k * P + j] = xr * dr - xi * di;
-            ai[k * P + j] = xr * di + xi * dr;
-        }
-        __syncthreads();
-        const int cols = NB - k;
-        for (int idx = tid; idx < k * cols; idx += nt) {
-            int i = idx / cols, j = k + idx % cols;
-            T xr = ar[k * P + j], xi = ai[k * P + j];
-            T cur_r = (j == k) ? (T)0 : ar[i * P + j], cur_i = (j == k) ? (T)0 : ai[i * P + j];
-            ar[i * P + j] = cur_r - (tr[i] * xr - ti[i] * xi);
-            ai[i * P + j] = cur_i - (tr[i] * xi + ti[i] * xr);
-        }
-        __syncthreads();
-    }
-    // inv layout: [blk][0] = L^-1 (unit lower, diagonal stored as 1), [blk][1] = U^-1.
     const int blk = k0 / NB;
-    T* Lr = invr + (size_t)blk * 2 * NB * NB;
-    T* Li = invi + (size_t)blk * 2 * NB * NB;
-    T* Ur = Lr + NB * NB;
-    T* Ui = Li + NB * NB;
+    T* Mr = invr + (size_t)blk * NB * NB;
+    T* Mi = invi + (size_t)blk * NB * NB;
     for (int idx = tid; idx < NB * NB; idx += nt) {
         int i = idx / NB, j = idx % NB;
-        T lr = (i > j) ? ar[i * P + j] : (i == j ? (T)1 : (T)0);
-        T li = (i > j) ? ai[i * P + j] : (T)0;
-        Lr[idx] = lr; Li[idx] = li;
-        Ur[idx] = (i <= j) ? ar[i * P + j] : (T)0;
-        Ui[idx] = (i <= j) ? ai[i * P + j] : (T)0;
+        Mr[idx] = ar[i * P + j];
+        Mi[idx] = ai[i * P + j];
     }
     if (local_flags) atomicOr(flags, local_flags);
 }
@@ -218,41 +185,44 @@ __global__ void k_copy_back(int rows, int cols, const T* wr, const T* wi, int wl
     if (bad) atomicOr(flags, FLAG_PIVOT);
 }
 
+// Block LU without row exchanges: for each diagonal block (order nb),
+//   D11^-1 (Gauss-Jordan),  W21 = A21 D11^-1  (stored in place of A21),
+//   A22 -= W21 A12          (A12 is the block-upper factor, kept in place).
+// Then D = L U with L = I + (strictly lower blocks W), U = block upper with the
+// diagonal blocks D_bb, whose inverses are kept in inv[blk].
 template <typename T, int NB>
 static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
                        bool tc) {
+    (void)wu;
     const size_t smem = (size_t)(2 * NB * (NB + 1) + 2 * NB) * sizeof(T);
-    cudaFuncSetAttribute(k_lu_diag<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    // workspaces: wl [2][n][NB] (L21), wu [2][NB][n] (U12), wut [2][n][NB] (U12^T)
+    cudaFuncSetAttribute(k_gj_inv<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
-    T* wur = wu; T* wui = wu + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
     for (int k0 = 0; k0 < n; k0 += NB) {
-        BEM_LAUNCH(k_lu_diag<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags));
+        BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
         if (rem <= 0) break;
         const int blk = k0 / NB;
-        CMat<T> Linv{invr + (size_t)blk * 2 * NB * NB, invi + (size_t)blk * 2 * NB * NB, NB};
-        CMat<T> Uinv{Linv.re + NB * NB, Linv.im + NB * NB, NB};
+        CMat<T> Dinv{invr + (size_t)blk * NB * NB, invi + (size_t)blk * NB * NB, NB};
         CMat<T> A21{A.re + (size_t)(k0 + NB) * A.ld + k0, A.im + (size_t)(k0 + NB) * A.ld + k0, A.ld};
         CMat<T> A12{A.re + (size_t)k0 * A.ld + k0 + NB, A.im + (size_t)k0 * A.ld + k0 + NB, A.ld};
         CMat<T> WL{wlr, wli, NB};
-        CMat<T> WU{wur, wui, rem};
-        // L21 = A21 U^-1  (rem x NB),  U12 = L^-1 A12  (NB x rem)
-        BEM_LAUNCH(k_cgemm<T><<<dim3(NB / 64, rem / 64), 256, 0, st>>>(rem, NB, NB, A21, Uinv, WL, (T)1, 0));
-        BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, NB / 64), 256, 0, st>>>(NB, rem, NB, Linv, A12, WU, (T)1, 0));
+        // W21 = A21 D11^-1  (rem x NB)
+        BEM_LAUNCH(k_cgemm<T><<<dim3(NB / 64, rem / 64), 256, 0, st>>>(rem, NB, NB, A21, Dinv, WL, (T)1, 0));
         int nblk = (int)(((size_t)rem * NB + 255) / 256);
         if (nblk > 4096) nblk = 4096;
-        BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 1, (T*)nullptr,
+        BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 0, (T*)nullptr,
                                                         (T*)nullptr, 0, flags));
-        BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, wur, wui, rem, A, k0, k0 + NB, 0, wtr, wti, NB, flags));
         CMat<T> A22{A.re + (size_t)(k0 + NB) * A.ld + k0 + NB, A.im + (size_t)(k0 + NB) * A.ld + k0 + NB, A.ld};
         if (tc) {
+            // the tensor-core update wants A12^T (K-major): copy A12 onto itself and transpose into wut
+            BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, A12.re, A12.im, A.ld, A, k0, k0 + NB, 0, wtr,
+                                                            wti, NB, flags));
             if (!tc_trailing_update(st, n, k0, NB, *reinterpret_cast<CMat<float>*>(&A),
                                     reinterpret_cast<const float*>(wl), reinterpret_cast<const float*>(wut), flags))
                 return 1;
         } else {
-            BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, WU, A22, (T)-1, 1));
+            BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, A12, A22, (T)-1, 1));
         }
     }
     return 0;
@@ -338,8 +308,8 @@ double tc_selftest(int device, int n) {
 // grid is smaller than the block count).  CTA b accumulates
 //     z_b = y_b - sum_{c before b} A_bc x_c
 // taking the x_c as soon as their CTAs publish them (epoch flags with release /
-// acquire ordering), then x_b = Inv_b z_b.  Forward (which = 0): unit-lower L,
-// c < b, Inv = L_bb^-1.  Backward (which = 1): U, c > b, Inv = U_bb^-1.  The
+// acquire ordering).  Forward (which = 0): block-unit-lower L (blocks W), c < b,
+// x_b = z_b.  Backward (which = 1): block-upper U, c > b, x_b = D_bb^-1 z_b.  The
 // launch is cooperative, so every CTA is resident and every wait is on a CTA
 // that is running or finished; the waits are bounded all the same and record
 // FLAG_TIMEOUT if they expire.
@@ -401,15 +371,16 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
             }
             __syncthreads();
         }
-        // x_b = Inv_b z_b
+        // forward: x_b = z_b (unit block diagonal); backward: x_b = D_bb^-1 z_b
+        if (which == 1) {
 #pragma unroll
         for (int u = 0; u < JPT; ++u) {
             int j = jq + u * TPR;
             if (j < R) { zr[i * R + j] = ar_[u]; zi[i * R + j] = ai_[u]; }
         }
         __syncthreads();
-        const T* Mr = invr + ((size_t)b * 2 + which) * NB * NB + (size_t)i * NB;
-        const T* Mi = invi + ((size_t)b * 2 + which) * NB * NB + (size_t)i * NB;
+        const T* Mr = invr + (size_t)b * NB * NB + (size_t)i * NB;
+        const T* Mi = invi + (size_t)b * NB * NB + (size_t)i * NB;
 #pragma unroll
         for (int u = 0; u < JPT; ++u) { ar_[u] = 0; ai_[u] = 0; }
         for (int k = 0; k < NB; ++k) {
@@ -423,6 +394,7 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
                     ai_[u] += mr * vi + mi * vr;
                 }
             }
+        }
         }
 #pragma unroll
         for (int u = 0; u < JPT; ++u) {
@@ -473,47 +445,92 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
 }
 
 // ---------------------------------------------------------------------------
-// Rres = Y - D X in FP64; one warp per row (Di null: real part of D only).
-__global__ void __launch_bounds__(256) k_residual(int N, int ld, const double* __restrict__ Dr,
-                                                  const double* __restrict__ Di, int R, const double* __restrict__ X,
-                                                  const double* __restrict__ Y, double* __restrict__ Rres) {
-    const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (r >= N) return;
-    double ar_[MAX_RHS], ai_[MAX_RHS];
+// ---------------------------------------------------------------------------
+// P = M X for an N x N row-major matrix M (real, or complex planar when Mi is
+// given) and an N x R complex block X: a skinny, HBM-bound product.  Phase 1:
+// CTA (row tile of 64, column chunk of 512) stages its X chunk in shared
+// memory (planar per column, so lanes read consecutive words) and writes
+// partial sums for its 64 rows; each element of M is read once.  Phase 2 sums
+// the chunks: out = beta * base + alpha * P  (base may alias out).
+constexpr int MX_ROWS = 64, MX_COLS = 512;
+
+__global__ void __launch_bounds__(256) k_matx_partial(int N, int ld, const double* __restrict__ Mr,
+                                                      const double* __restrict__ Mi, int R, int j0,
+                                                      const double* __restrict__ X, int xstride,
+                                                      double* __restrict__ part) {
+    extern __shared__ double xs[];  // [2][R][MX_COLS]
+    const int rt = blockIdx.x, ct = blockIdx.y;
+    const int s0 = ct * MX_COLS;
+    const int ns = min(MX_COLS, N - s0);
+    for (int idx = threadIdx.x; idx < R * MX_COLS; idx += blockDim.x) {
+        int j = idx / MX_COLS, k = idx % MX_COLS;
+        double vr = 0, vi = 0;
+        if (k < ns) {
+            const double* x = X + 2 * ((size_t)(s0 + k) * xstride + j0 + j);
+            vr = x[0]; vi = x[1];
+        }
+        xs[(size_t)j * MX_COLS + k] = vr;
+        xs[(size_t)(R + j) * MX_COLS + k] = vi;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int rr = warp; rr < MX_ROWS; rr += 8) {
+        const int r = rt * MX_ROWS + rr;
+        if (r >= N) break;
+        double ar[MAX_RHS], ai[MAX_RHS];
 #pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) { ar_[j] = 0; ai_[j] = 0; }
-    const double* rr = Dr + (size_t)r * ld;
-    const double* ri = Di ? Di + (size_t)r * ld : nullptr;
-    for (int s = lane; s < N; s += 32) {
-        double mr = rr[s], mi = ri ? ri[s] : 0.0;
-        const double* x = X + 2 * (size_t)s * R;
+        for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+        const double* mr = Mr + (size_t)r * ld + s0;
+        const double* mi = Mi ? Mi + (size_t)r * ld + s0 : nullptr;
+        for (int k = lane; k < ns; k += 32) {
+            double a = mr[k], b = mi ? mi[k] : 0.0;
+#pragma unroll
+            for (int j = 0; j < MAX_RHS; ++j) {
+                if (j < R) {
+                    double xr = xs[(size_t)j * MX_COLS + k], xi = xs[(size_t)(R + j) * MX_COLS + k];
+                    ar[j] = fma(a, xr, ar[j]);
+                    ar[j] = fma(-b, xi, ar[j]);
+                    ai[j] = fma(a, xi, ai[j]);
+                    ai[j] = fma(b, xr, ai[j]);
+                }
+            }
+        }
 #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) {
             if (j < R) {
-                double vr = x[2 * j], vi = x[2 * j + 1];
-                ar_[j] = fma(mr, vr, ar_[j]);
-                ar_[j] = fma(-mi, vi, ar_[j]);
-                ai_[j] = fma(mr, vi, ai_[j]);
-                ai_[j] = fma(mi, vr, ai_[j]);
+                double vr = ar[j], vi = ai[j];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                    vi += __shfl_xor_sync(0xffffffffu, vi, off);
+                }
+                if (lane == 0) {
+                    double* p = part + 2 * (((size_t)ct * N + r) * R + j);
+                    p[0] = vr;
+                    p[1] = vi;
+                }
             }
         }
     }
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) {
-        if (j < R) {
-            double vr = ar_[j], vi = ai_[j];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                vr += __shfl_xor_sync(0xffffffffu, vr, off);
-                vi += __shfl_xor_sync(0xffffffffu, vi, off);
-            }
-            if (lane == 0) {
-                Rres[2 * ((size_t)r * R + j)] = Y[2 * ((size_t)r * R + j)] - vr;
-                Rres[2 * ((size_t)r * R + j) + 1] = Y[2 * ((size_t)r * R + j) + 1] - vi;
-            }
-        }
+}
+
+// out[r][j0 + j] = beta * base[r][j0 + j] + alpha * sum_c part[c][r][j]   (stride ostride)
+__global__ void k_matx_reduce(int N, int R, int nchunk, const double* __restrict__ part, double alpha, double beta,
+                              const double* base, double* out, int j0, int ostride) {
+    size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (idx >= (size_t)N * R) return;
+    int r = (int)(idx / R), j = (int)(idx % R);
+    double sr = 0, si = 0;
+    for (int c = 0; c < nchunk; ++c) {
+        const double* p = part + 2 * (((size_t)c * N + r) * R + j);
+        sr += p[0];
+        si += p[1];
     }
+    size_t o = 2 * ((size_t)r * ostride + j0 + j);
+    double br = 0, bi = 0;
+    if (beta != 0.0) { br = base[o]; bi = base[o + 1]; }
+    out[o] = beta * br + alpha * sr;
+    out[o + 1] = beta * bi + alpha * si;
 }
 
 // Per-column max |Rres| and max |Y| (non-negative doubles compare as integers).
@@ -565,10 +582,21 @@ __global__ void k_pad_rhs(int N, int Np, int R, double* X) {
         X[(size_t)N * R * 2 + i] = 0.0;
 }
 
-void launch_residual(cudaStream_t st, int N, int ld, const double* Dr, const double* Di, int R, const double* X,
-                     const double* Y, double* Rres) {
-    BEM_LAUNCH(k_residual<<<(N + 7) / 8, 256, 0, st>>>(N, ld, Dr, Di, R, X, Y, Rres));
+size_t matx_part_doubles(int N, int R) { return (size_t)2 * ((N + MX_COLS - 1) / MX_COLS) * N * R; }
+
+void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double* Mi, int R, int j0, const double* X,
+                 int xstride, double* part, double alpha, double beta, const double* base, double* out,
+                 int ostride) {
+    dim3 grd((N + MX_ROWS - 1) / MX_ROWS, (N + MX_COLS - 1) / MX_COLS);
+    size_t smem = sizeof(double) * 2 * R * MX_COLS;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_matx_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_matx_partial<<<grd, 256, smem, st>>>(N, ld, Mr, Mi, R, j0, X, xstride, part));
+    size_t tot = (size_t)N * R;
+    BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, R, (int)grd.y, part, alpha, beta,
+                                                                             base, out, j0, ostride));
 }
+
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm) {
     BEM_LAUNCH(k_norms<<<152, 256, 0, st>>>(N, R, Rres, Y, nrm));
 }

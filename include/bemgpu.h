@@ -110,6 +110,15 @@ int bem_mesh_barge_sizes(int nx, int ny, int nz, int* n_nodes, int* n_elems, int
 int bem_mesh_barge(double length, double width, double draft, int nx, int ny, int nz, int cosine, double* nodes,
                    int* elems, double* aux_nodes, int* aux_elems);
 
+/* Rectangular wing of a symmetric NACA 00xx section (chord, span, thickness
+ * ratio), nc panels around the section (even; half-cosine spacing on both
+ * surfaces when cosine != 0), ns spanwise strips, open tips, normals into the
+ * wing.  The steady-flow workload's geometry; the reference's Wing class
+ * (Wing.cpp:28-109) builds a different (elliptic, Karman-Trefftz) wing. */
+int bem_mesh_wing_sizes(int nc, int ns, int* n_nodes, int* n_elems);
+int bem_mesh_wing(double chord, double span, double thickness, int nc, int ns, int cosine, double* nodes,
+                  int* elems);
+
 /* ---- solver context (Hydrodynamic_Radiation_Solver) ------------------------ */
 
 /* Creates a context on CUDA device `device` (replaces `new Hydrodynamic_Radiation_Solver`). */
@@ -140,6 +149,20 @@ bem_status bem_get_sizes(const bem_ctx* ctx, int* n_panels, int* n_beta);
 /* Mass and stiffness matrices used for the RAO (6x6 row-major each), and
  * {volume, xb, yb, zb} (Boundary_Base.cpp:177-224). */
 bem_status bem_get_body_matrices(const bem_ctx* ctx, double* mass_matrix, double* stiffness, double* vol_cob);
+
+/* ---- steady potential flow (Aerodynamic_Solver, constant panels) ---------- */
+
+/* Aerodynamic_Solver::Setup (Aerodynamic_Solver.cpp:126-146) with constant
+ * panels: collocation points c + 1e-5 n and the Rankine influence matrices
+ * G (source) and H (dipole) of the body panels (:42-58), on the GPU in FP64.
+ * Replaces any hydrodynamic setup of the context. */
+bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh);
+
+/* Set_External_BC + Solve_Steady (:150-180): BC_i = V_i . n_i, X = H^-1 (G BC).
+ * vel: 3 doubles (uniform onset flow) if n_vel == 1, else 3 per panel (n_vel = N).
+ * X (N): perturbation potential at the panels; BC (N) may be NULL. */
+bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precision, double refine_tol, double* X,
+                          double* BC);
 
 /* ---- influence matrices (Prepare_Linear_System / _Wave_Terms) -------------- */
 

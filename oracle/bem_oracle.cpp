@@ -812,6 +812,40 @@ void orc_wave_rows(int nn, const double* nodes, int ne, const int* elems, int nc
         }
 }
 
+// Aerodynamic_Solver constant-panel steady solve (Aerodynamic_Solver.cpp:42-58,
+// 126-180): G(R,S), H(R,S) = Inf_SingleDoubleLayer of the body panel S at the
+// collocation point R (c + 1e-5 n, BCF = +1e-5 for constant panels, :134-137);
+// BC(i) = V_i . n_i (Set_External_BC :150-166, sgnBCF = +1); X = H^-1 (G BC).
+// vel: 3 doubles (uniform) if nvel == 1, else 3 N.  Outputs X (N) and BC (N).
+void orc_aero(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+              const double* comp_origin, int nvel, const double* vel, double* X, double* BC) {
+    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
+    std::vector<Panel> body, mir;
+    build_panels(m, body, mir);
+    std::vector<V3> x = collocation(body);
+    const int N = ne;
+    std::vector<double> G((size_t)N * N), H((size_t)N * N);
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int S = 0; S < N; ++S)
+        for (int R = 0; R < N; ++R) inf_source_kernel(body[S], x[R], G[(size_t)R * N + S], H[(size_t)R * N + S]);
+    for (int i = 0; i < N; ++i) {
+        const double* v = nvel == 1 ? vel : vel + 3 * (size_t)i;
+        BC[i] = v[0] * body[i].ez.x + v[1] * body[i].ez.y + v[2] * body[i].ez.z;
+    }
+    std::vector<cplx> A((size_t)N * N), b(N);
+    for (size_t k = 0; k < (size_t)N * N; ++k) A[k] = cplx(H[k], 0.0);
+    #pragma omp parallel for schedule(static)
+    for (int R = 0; R < N; ++R) {
+        double acc = 0;
+        for (int S = 0; S < N; ++S) acc += G[(size_t)R * N + S] * BC[S];
+        b[R] = cplx(acc, 0.0);
+    }
+    std::vector<int> piv(N);
+    lu_factor(N, A.data(), piv.data());
+    lu_solve(N, A.data(), piv.data(), 1, b.data());
+    for (int i = 0; i < N; ++i) X[i] = b[i].real();
+}
+
 // Complex LU + solve (interleaved re/im, row-major), exposed for baselines/tests.
 void orc_lu_solve(int n, double* a, int nr, double* b) {
     std::vector<int> piv(n);

@@ -94,6 +94,7 @@ class Oracle:
         L.orc_wave.argtypes = mesh_args + [_d, _dp, _dp]
         L.orc_wave_rows.argtypes = mesh_args + [_d, _i, _i, _dp, _dp]
         L.orc_lu_solve.argtypes = [_i, _dp, _i, _dp]
+        L.orc_aero.argtypes = mesh_args + [_i, _dp, _dp, _dp]
         L.orc_mass_hydrostatics.argtypes = mesh_args + mesh_args + [_d, _d, _d, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve.argtypes = mesh_args + [_i, _dp, _i, _dp, _d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                             _dp, _dp]
@@ -212,6 +213,14 @@ class Oracle:
             out["phiJ"] = pj
             out["phiS"] = ps
         return out
+
+    def aero(self, mesh, vel):
+        """Aerodynamic_Solver steady constant-panel solve: returns (X, BC)."""
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        X = np.zeros(mesh.n)
+        BC = np.zeros(mesh.n)
+        self.L.orc_aero(*mesh.args(), vel.shape[0], _p(vel), _p(X), _p(BC))
+        return X, BC
 
     def set_threads(self, n):
         self.L.orc_set_threads(int(n))

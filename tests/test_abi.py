@@ -67,3 +67,20 @@ def test_errors_without_gpu_are_reported():
     with pytest.raises(bg.BEMError) as ei:
         bg.Hydrodynamic_Radiation_Solver()
     assert ei.value.status in (2, 6)
+
+
+def test_wing_mesh_normals_point_inward():
+    import numpy as np
+    import bemuse_gb300 as bg
+    from bemuse_gb300 import build
+    from oracle.oracle import Oracle, Mesh
+    if not os.path.exists(build.LIB):
+        pytest.skip("library not built")
+    w = bg.NACA_Wing(1.0, 8.0, 0.12, 120, 60)
+    assert w.n == 7200
+    P = Oracle().panels(Mesh(w.nodes, w.elems))
+    c, n = P[:, 13:16], P[:, 22:25]
+    up = c[:, 2] > 1e-12
+    assert np.all(n[up, 2] < 0) and np.all(n[~up, 2] > 0)
+    # wetted area of a 12 % section is ~2.04 chords per unit span
+    assert abs(P[:, 25].sum() / 8.0 - 2.04) < 0.02

@@ -173,3 +173,19 @@ def test_tensor_core_update_matches_fp32(bg):
         err = bg.selftest_tc(n)
         print("tcgen05 vs fp32 update, n=%d: %.3e" % (n, err))
         assert 0 <= err < 2e-2
+
+
+def test_aero_steady_solve_matches_oracle(bg, orc):
+    """Aerodynamic_Solver constant-panel steady solve (Aerodynamic_Solver.cpp:42-58,
+    150-180) on a 240-panel NACA 0012 wing at 5 deg: X = H^-1 (G (U . n))."""
+    from oracle.oracle import Mesh as OMesh
+    w = bg.NACA_Wing(1.0, 8.0, 0.12, 24, 10)
+    U = [np.cos(np.radians(5.0)), 0.0, np.sin(np.radians(5.0))]
+    Xo, BCo = orc.aero(OMesh(w.nodes, w.elems), U)
+    for prec, tol in ((bg.PLAIN_FP64, 1e-10), (bg.MIXED, 1e-10)):
+        a = bg.Aerodynamic_Solver(precision=prec)
+        a.Setup(w)
+        a.Set_External_BC([U])
+        X = a.Solve_Steady()
+        assert np.max(np.abs(a.BC - BCo)) < 1e-14
+        assert normwise(X, Xo) < tol, (prec, normwise(X, Xo))
