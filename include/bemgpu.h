@@ -201,6 +201,27 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
  * reset != 0 zeroes the counters after reading. */
 bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
 
+/* ---- dense complex solve that allocates nothing --------------------------------
+ * This entry point has no counterpart in the reference.  It is the FP64 solve of
+ * bem_dense_solve (same kernels, same results) for callers that cannot call
+ * cudaMalloc: code inside an application that hands all device memory to its own
+ * pool allocator, or a loop where cudaMalloc's implicit device-wide
+ * synchronization and latency are not acceptable.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine; every buffer it needs lives in one
+ * fixed file-scope device array (10.9 MB, for n <= BEM_NOALLOC_MAX_N), which
+ * every GPU that loads the library holds until the process exits.
+ *   - Orders n > BEM_NOALLOC_MAX_N or nrhs outside [1, 16] are rejected with
+ *     BEM_ERR_ARG and a message.
+ *   - The first call on a device looks up the array's device address (with that
+ *     device current); make that first call before any stream capture.
+ *   - All calls share the one array: calls that overlap on the GPU (other host
+ *     threads, other streams) race and corrupt each other's results.
+ *   - Work runs on the legacy default stream; the call returns when X is on the host.
+ * A is n x n and B is n x nrhs, row-major interleaved complex host arrays; X
+ * overwrites B.  Errors: bem_last_error(NULL). */
+#define BEM_NOALLOC_MAX_N 512
+bem_status bem_dense_solve_noalloc(int device, int n, const double* A, int nrhs, double* B);
+
 /* Number of kernel launches this library has issued since it was loaded. */
 unsigned long long bem_launch_count(void);
 
