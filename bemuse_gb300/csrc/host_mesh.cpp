@@ -22,7 +22,6 @@ inline V mk(double a, double b, double c) { return V{a, b, c}; }
 inline V operator+(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
 inline V operator-(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
 inline V operator*(V a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
-inline double dotv(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline V crossv(V a, V b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 inline double len(V a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 inline V unit(V a) { double n = len(a); return n > 0 ? mk(a.x / n, a.y / n, a.z / n) : a; }

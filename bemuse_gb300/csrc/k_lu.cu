@@ -27,76 +27,101 @@ template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfi
 
 // ---------------------------------------------------------------------------
 // In-place Gauss-Jordan inverse of the nb x nb diagonal block (the current Schur
-// complement block), no row exchanges, in shared memory; written to inv[blk].
-// Multipliers |a_ik / a_kk| > 1 below the pivot raise FLAG_PIVOT (partial
-// pivoting would have exchanged rows inside the block); a zero or non-finite
-// pivot raises FLAG_ZERO_PIVOT.
+// complement block), no row exchanges; written to inv[blk].  1024 threads hold
+// the block in registers, thread (ty, tx) owning rows ty + 32 a and columns
+// tx + 32 b; per pivot, the owners publish row k and column k through shared
+// memory (double-buffered, one barrier per pivot) and every thread updates its
+// own elements.  Multipliers |a_ik / a_kk| > 1 below the pivot raise FLAG_PIVOT
+// (partial pivoting would have exchanged rows inside the block); a zero or
+// non-finite pivot raises FLAG_ZERO_PIVOT.
 template <typename T, int NB>
 __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* invi, int* flags) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int P = NB + 1;
-    T* ar = reinterpret_cast<T*>(smem_raw);
-    T* ai = ar + NB * P;
-    T* cr = ai + NB * P;  // pivot column copy
-    T* ci = cr + NB;
-    __shared__ T pinv[2];
-    const int tid = threadIdx.x, nt = blockDim.x;
+    constexpr int G = NB / 32;  // row / column groups per thread
+    __shared__ T rowr[2][NB], rowi[2][NB], colr[2][NB], coli[2][NB];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const size_t ld = A.ld;
-    for (int idx = tid; idx < NB * NB; idx += nt) {
-        int i = idx / NB, j = idx % NB;
-        size_t g = (size_t)(k0 + i) * ld + k0 + j;
-        ar[i * P + j] = A.re[g];
-        ai[i * P + j] = A.im[g];
-    }
-    __syncthreads();
+    T vr[G][G], vi[G][G];
+#pragma unroll
+    for (int a = 0; a < G; ++a)
+#pragma unroll
+        for (int b = 0; b < G; ++b) {
+            size_t g = (size_t)(k0 + ty + 32 * a) * ld + k0 + tx + 32 * b;
+            vr[a][b] = A.re[g];
+            vi[a][b] = A.im[g];
+        }
     int local_flags = 0;
     for (int k = 0; k < NB; ++k) {
-        // pivot column (before it is overwritten) and 1 / pivot
-        for (int i = tid; i < NB; i += nt) { cr[i] = ar[i * P + k]; ci[i] = ai[i * P + k]; }
-        if (tid == 0) {
-            T pr = ar[k * P + k], pi = ai[k * P + k];
-            T den = pr * pr + pi * pi;
-            if (!(den > (T)0) || !isfinite(den)) local_flags |= FLAG_ZERO_PIVOT;
-            pinv[0] = pr / den;
-            pinv[1] = -pi / den;
+        const int buf = k & 1;
+        const int ka = k >> 5, kt = k & 31;
+        // publish row k (owners: ty == kt) and column k (owners: tx == kt)
+        if (ty == kt) {
+#pragma unroll
+            for (int a = 0; a < G; ++a)
+                if (a == ka) {
+#pragma unroll
+                    for (int b = 0; b < G; ++b) { rowr[buf][tx + 32 * b] = vr[a][b]; rowi[buf][tx + 32 * b] = vi[a][b]; }
+                }
+        }
+        if (tx == kt) {
+#pragma unroll
+            for (int b = 0; b < G; ++b)
+                if (b == ka) {
+#pragma unroll
+                    for (int a = 0; a < G; ++a) { colr[buf][ty + 32 * a] = vr[a][b]; coli[buf][ty + 32 * a] = vi[a][b]; }
+                }
         }
         __syncthreads();
-        const T qr = pinv[0], qi = pinv[1];
-        // row k: a_kj /= p (j != k), a_kk = 1/p
-        for (int j = tid; j < NB; j += nt) {
-            T xr = (j == k) ? (T)1 : ar[k * P + j], xi = (j == k) ? (T)0 : ai[k * P + j];
-            ar[k * P + j] = xr * qr - xi * qi;
-            ai[k * P + j] = xr * qi + xi * qr;
+        const T pr = colr[buf][k], pi = coli[buf][k];
+        const T den = pr * pr + pi * pi;
+        if (threadIdx.x == 0 && (!(den > (T)0) || !isfinite(den))) local_flags |= FLAG_ZERO_PIVOT;
+        const T qr = pr / den, qi = -pi / den;  // 1 / pivot
+        // new row k: a_kj / p for j != k, 1/p at j == k
+        T nr[G], ni[G];
+#pragma unroll
+        for (int b = 0; b < G; ++b) {
+            const int j = tx + 32 * b;
+            T xr = (j == k) ? (T)1 : rowr[buf][j], xi = (j == k) ? (T)0 : rowi[buf][j];
+            nr[b] = xr * qr - xi * qi;
+            ni[b] = xr * qi + xi * qr;
         }
-        if (tid > k && tid < NB) {
-            T lr = cr[tid] * qr - ci[tid] * qi, li = cr[tid] * qi + ci[tid] * qr;
-            if (lr * lr + li * li > (T)(1.000002)) local_flags |= FLAG_PIVOT;
-        }
-        __syncthreads();
-        // rows i != k: a_ij -= c_i a_kj (j != k); a_ik = -c_i / p
-        for (int idx = tid; idx < NB * NB; idx += nt) {
-            int i = idx / NB, j = idx % NB;
-            if (i == k) continue;
-            T fr = cr[i], fi = ci[i];
-            T ur = ar[k * P + j], ui = ai[k * P + j];
-            if (j == k) {
-                ar[i * P + j] = -(fr * ur - fi * ui);
-                ai[i * P + j] = -(fr * ui + fi * ur);
+#pragma unroll
+        for (int a = 0; a < G; ++a) {
+            const int i = ty + 32 * a;
+            if (i == k) {
+#pragma unroll
+                for (int b = 0; b < G; ++b) { vr[a][b] = nr[b]; vi[a][b] = ni[b]; }
             } else {
-                ar[i * P + j] -= fr * ur - fi * ui;
-                ai[i * P + j] -= fr * ui + fi * ur;
+                const T cr = colr[buf][i], ci = coli[buf][i];
+                if (tx == kt && i > k) {
+                    T lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
+                    if (lr * lr + li * li > (T)(1.000002)) local_flags |= FLAG_PIVOT;
+                }
+#pragma unroll
+                for (int b = 0; b < G; ++b) {
+                    const int j = tx + 32 * b;
+                    T ur = nr[b], ui = ni[b];
+                    if (j == k) {
+                        vr[a][b] = -(cr * ur - ci * ui);
+                        vi[a][b] = -(cr * ui + ci * ur);
+                    } else {
+                        vr[a][b] -= cr * ur - ci * ui;
+                        vi[a][b] -= cr * ui + ci * ur;
+                    }
+                }
             }
         }
-        __syncthreads();
     }
     const int blk = k0 / NB;
     T* Mr = invr + (size_t)blk * NB * NB;
     T* Mi = invi + (size_t)blk * NB * NB;
-    for (int idx = tid; idx < NB * NB; idx += nt) {
-        int i = idx / NB, j = idx % NB;
-        Mr[idx] = ar[i * P + j];
-        Mi[idx] = ai[i * P + j];
-    }
+#pragma unroll
+    for (int a = 0; a < G; ++a)
+#pragma unroll
+        for (int b = 0; b < G; ++b) {
+            size_t o = (size_t)(ty + 32 * a) * NB + tx + 32 * b;
+            Mr[o] = vr[a][b];
+            Mi[o] = vi[a][b];
+        }
     if (local_flags) atomicOr(flags, local_flags);
 }
 
@@ -194,12 +219,10 @@ template <typename T, int NB>
 static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
                        bool tc) {
     (void)wu;
-    const size_t smem = (size_t)(2 * NB * (NB + 1) + 2 * NB) * sizeof(T);
-    cudaFuncSetAttribute(k_gj_inv<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
     for (int k0 = 0; k0 < n; k0 += NB) {
-        BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, smem, st>>>(k0, A, invr, invi, flags));
+        BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
         if (rem <= 0) break;
         const int blk = k0 / NB;
@@ -320,11 +343,28 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
                                                         int* __restrict__ ready, int epoch, int* __restrict__ gflags) {
     constexpr int NT = NB * TPR;
     constexpr int JPT = (MAX_RHS + TPR - 1) / TPR;  // RHS columns per thread
-    __shared__ T zr[NB * MAX_RHS], zi[NB * MAX_RHS];
+    constexpr int LP = NB + 16 / (int)sizeof(T);    // padded tile row (16-byte aligned)
+    constexpr int CH = 16 / (int)sizeof(T);         // elements per 16-byte chunk
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* Lr = reinterpret_cast<T*>(smem_raw);         // [NB][LP]
+    T* Li = Lr + NB * LP;
+    T* zr = Li + NB * LP;                           // [NB][MAX_RHS]
+    T* zi = zr + NB * MAX_RHS;
     __shared__ int timed_out;
     const int tid = threadIdx.x;
     const int i = tid / TPR, jq = tid % TPR;  // row within the block, RHS phase
     if (tid == 0) timed_out = 0;
+    // cp.async of an NB x NB tile (row-major, stride ld) into Lr/Li
+    auto issue_tile = [&](const T* gr, const T* gi, size_t ldg) {
+        for (int idx = tid; idx < NB * (NB / CH); idx += NT) {
+            int rr = idx / (NB / CH), cc = (idx % (NB / CH)) * CH;
+            unsigned dr = (unsigned)__cvta_generic_to_shared(Lr + rr * LP + cc);
+            unsigned di = (unsigned)__cvta_generic_to_shared(Li + rr * LP + cc);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dr), "l"(gr + rr * ldg + cc) : "memory");
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(di), "l"(gi + rr * ldg + cc) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     for (int round = blockIdx.x; round < nblk; round += gridDim.x) {
         const int b = which == 0 ? round : nblk - 1 - round;
         const size_t row = (size_t)b * NB + i;
@@ -338,6 +378,8 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
         const int cnt = which == 0 ? b : nblk - 1 - b;
         for (int t = 0; t < cnt; ++t) {
             const int c = which == 0 ? t : nblk - 1 - t;
+            const size_t goff = (size_t)b * NB * A.ld + (size_t)c * NB;
+            issue_tile(A.re + goff, A.im + goff, A.ld);   // overlaps with the wait below
             if (tid == 0) {
                 int v = 0;
                 long it = 0;
@@ -351,19 +393,22 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
             __syncthreads();
             for (int idx = tid; idx < NB * R; idx += NT) {
                 size_t o = 2 * (((size_t)c * NB) * R + idx);
-                zr[idx] = __ldcg(Xout + o);
-                zi[idx] = __ldcg(Xout + o + 1);
+                int k = idx / R, j = idx % R;
+                zr[k * MAX_RHS + j] = __ldcg(Xout + o);
+                zi[k * MAX_RHS + j] = __ldcg(Xout + o + 1);
             }
+            asm volatile("cp.async.wait_all;" ::: "memory");
             __syncthreads();
-            const T* lr = A.re + row * A.ld + (size_t)c * NB;
-            const T* li = A.im + row * A.ld + (size_t)c * NB;
+            const T* lr = Lr + i * LP;
+            const T* li = Li + i * LP;
+#pragma unroll 4
             for (int k = 0; k < NB; ++k) {
                 T mr = lr[k], mi = li[k];
 #pragma unroll
                 for (int u = 0; u < JPT; ++u) {
                     int j = jq + u * TPR;
                     if (j < R) {
-                        T vr = zr[k * R + j], vi = zi[k * R + j];
+                        T vr = zr[k * MAX_RHS + j], vi = zi[k * MAX_RHS + j];
                         ar_[u] -= mr * vr - mi * vi;
                         ai_[u] -= mr * vi + mi * vr;
                     }
@@ -371,30 +416,35 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
             }
             __syncthreads();
         }
-        // forward: x_b = z_b (unit block diagonal); backward: x_b = D_bb^-1 z_b
         if (which == 1) {
-#pragma unroll
-        for (int u = 0; u < JPT; ++u) {
-            int j = jq + u * TPR;
-            if (j < R) { zr[i * R + j] = ar_[u]; zi[i * R + j] = ai_[u]; }
-        }
-        __syncthreads();
-        const T* Mr = invr + (size_t)b * NB * NB + (size_t)i * NB;
-        const T* Mi = invi + (size_t)b * NB * NB + (size_t)i * NB;
-#pragma unroll
-        for (int u = 0; u < JPT; ++u) { ar_[u] = 0; ai_[u] = 0; }
-        for (int k = 0; k < NB; ++k) {
-            T mr = Mr[k], mi = Mi[k];
+            // x_b = D_bb^-1 z_b
+            const size_t ioff = (size_t)b * NB * NB;
+            issue_tile(invr + ioff, invi + ioff, NB);
 #pragma unroll
             for (int u = 0; u < JPT; ++u) {
                 int j = jq + u * TPR;
-                if (j < R) {
-                    T vr = zr[k * R + j], vi = zi[k * R + j];
-                    ar_[u] += mr * vr - mi * vi;
-                    ai_[u] += mr * vi + mi * vr;
+                if (j < R) { zr[i * MAX_RHS + j] = ar_[u]; zi[i * MAX_RHS + j] = ai_[u]; }
+            }
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < JPT; ++u) { ar_[u] = 0; ai_[u] = 0; }
+            const T* mrow = Lr + i * LP;
+            const T* mirow = Li + i * LP;
+#pragma unroll 4
+            for (int k = 0; k < NB; ++k) {
+                T mr = mrow[k], mi = mirow[k];
+#pragma unroll
+                for (int u = 0; u < JPT; ++u) {
+                    int j = jq + u * TPR;
+                    if (j < R) {
+                        T vr = zr[k * MAX_RHS + j], vi = zi[k * MAX_RHS + j];
+                        ar_[u] += mr * vr - mi * vi;
+                        ai_[u] += mr * vi + mi * vr;
+                    }
                 }
             }
-        }
+            __syncthreads();
         }
 #pragma unroll
         for (int u = 0; u < JPT; ++u) {
@@ -416,14 +466,17 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
                      const T* Y, T* X, int* ready, int epoch, int* flags) {
     const int nblk = n / NB;
     int dev = 0, nsm = 0, per_sm = 0;
+    constexpr int LP = NB + 16 / (int)sizeof(T);
+    const size_t smem = sizeof(T) * (2 * (size_t)NB * LP + 2 * (size_t)NB * MAX_RHS);
+    cudaFuncSetAttribute(k_trsv_coop<T, NB, TPR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_coop<T, NB, TPR>, NB * TPR, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_coop<T, NB, TPR>, NB * TPR, smem);
     int grid = std::min(nblk, std::max(1, per_sm) * nsm);
     void* args[] = {(void*)&nblk, (void*)&R, (void*)&A, (void*)&invr, (void*)&invi, (void*)&which, (void*)&Y,
                     (void*)&X, (void*)&ready, (void*)&epoch, (void*)&flags};
     ++g_launches;
-    return cudaLaunchCooperativeKernel((void*)k_trsv_coop<T, NB, TPR>, dim3(grid), dim3(NB * TPR), args, 0, st) ==
+    return cudaLaunchCooperativeKernel((void*)k_trsv_coop<T, NB, TPR>, dim3(grid), dim3(NB * TPR), args, smem, st) ==
                    cudaSuccess
                ? 0
                : 1;
@@ -434,14 +487,14 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
                  int* ready, int epoch, int* flags) {
     double* tmp = X + (size_t)2 * n * R;
-    if (trsv_coop<double, 64, 4>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
-    return trsv_coop<double, 64, 4>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
+    if (trsv_coop<double, 64, 8>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
+    return trsv_coop<double, 64, 8>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
     float* tmp = X + (size_t)2 * n * R;
-    if (trsv_coop<float, 128, 2>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
-    return trsv_coop<float, 128, 2>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
+    if (trsv_coop<float, 128, 4>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
+    return trsv_coop<float, 128, 4>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -454,6 +507,7 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
 // the chunks: out = beta * base + alpha * P  (base may alias out).
 constexpr int MX_ROWS = 64, MX_COLS = 512;
 
+template <bool CPLX>
 __global__ void __launch_bounds__(256) k_matx_partial(int N, int ld, const double* __restrict__ Mr,
                                                       const double* __restrict__ Mi, int R, int j0,
                                                       const double* __restrict__ X, int xstride,
@@ -481,17 +535,20 @@ __global__ void __launch_bounds__(256) k_matx_partial(int N, int ld, const doubl
 #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
         const double* mr = Mr + (size_t)r * ld + s0;
-        const double* mi = Mi ? Mi + (size_t)r * ld + s0 : nullptr;
+        const double* mi = CPLX ? Mi + (size_t)r * ld + s0 : nullptr;
         for (int k = lane; k < ns; k += 32) {
-            double a = mr[k], b = mi ? mi[k] : 0.0;
+            double a = mr[k];
+            double b = CPLX ? mi[k] : 0.0;
 #pragma unroll
             for (int j = 0; j < MAX_RHS; ++j) {
                 if (j < R) {
                     double xr = xs[(size_t)j * MX_COLS + k], xi = xs[(size_t)(R + j) * MX_COLS + k];
                     ar[j] = fma(a, xr, ar[j]);
-                    ar[j] = fma(-b, xi, ar[j]);
                     ai[j] = fma(a, xi, ai[j]);
-                    ai[j] = fma(b, xr, ai[j]);
+                    if (CPLX) {
+                        ar[j] = fma(-b, xi, ar[j]);
+                        ai[j] = fma(b, xr, ai[j]);
+                    }
                 }
             }
         }
@@ -589,9 +646,12 @@ void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double*
                  int ostride) {
     dim3 grd((N + MX_ROWS - 1) / MX_ROWS, (N + MX_COLS - 1) / MX_COLS);
     size_t smem = sizeof(double) * 2 * R * MX_COLS;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_matx_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    BEM_LAUNCH(k_matx_partial<<<grd, 256, smem, st>>>(N, ld, Mr, Mi, R, j0, X, xstride, part));
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_matx_partial<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_matx_partial<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    if (Mi) BEM_LAUNCH(k_matx_partial<true><<<grd, 256, smem, st>>>(N, ld, Mr, Mi, R, j0, X, xstride, part));
+    else BEM_LAUNCH(k_matx_partial<false><<<grd, 256, smem, st>>>(N, ld, Mr, Mi, R, j0, X, xstride, part));
     size_t tot = (size_t)N * R;
     BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, R, (int)grd.y, part, alpha, beta,
                                                                              base, out, j0, ostride));
