@@ -39,6 +39,7 @@ struct WaveArgs {
     // mixed mode only
     const float* xr32;    // collocation points, hi/lo split: [6][N] (xh, yh, zh, xl, yl, zl)
     const float* gq32;    // Gauss data [10][4][N]: xh, yh, zh, w, nx, ny, nz, xl, yl, zl
+    float* Dhi; float* Dlo;   // Re D as a float pair hi + lo (~48-bit) for the refinement residual [N][ld]
 };
 
 cudaError_t upload_poly_constants(int device);
@@ -93,6 +94,11 @@ size_t matx_part_doubles(int N, int R);
 void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double* Mi, int R, int j0, const double* X,
                  int xstride, double* part, double alpha, double beta, const double* base, double* out,
                  int ostride);
+// Rres = Y - (Dhi + Dlo) X for a real operator stored as float pairs, in
+// double-float arithmetic (products exact to ~2^-48, compensated sums); X is
+// FP64 and is split into float pairs first (Xdf: N x R float4 scratch).
+void launch_matx_df(cudaStream_t st, int N, int ld, const float* Dhi, const float* Dlo, int R, const double* X,
+                    float4* Xdf, double* part, const double* Y, double* Rres);
 // nrm[j] = max_r |Rres[r][j]|, nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (zero them first).
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm);
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);

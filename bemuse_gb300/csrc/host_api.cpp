@@ -47,6 +47,8 @@ struct bem_ctx {
     double *d_RS = nullptr, *d_RD = nullptr, *d_RSR = nullptr;
     double *d_D64r = nullptr, *d_D64i = nullptr;
     float *d_D32r = nullptr, *d_D32i = nullptr;
+    float *d_Dhi = nullptr, *d_Dlo = nullptr;   // Re D as float pairs (mixed refinement residual)
+    float4* d_Xdf = nullptr;
     double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
     float* d_X32 = nullptr;
     double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr, *d_mx = nullptr;
@@ -64,7 +66,8 @@ struct bem_ctx {
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
     double pw_K = -1.0;               // wave number the factors were built for
     // operator used by the refinement residual: 0 = stored D64 (re, im); 1 = stored
-    // Re(D) only (real operator, K = 0); 2 = stored Re(D) + plane-wave Im(D)
+    // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
+    // 3 = Re D as float pairs + plane-wave Im D (hydro, K != 0)
     int resid_mode = 0;
     std::vector<void*> allocs;
     // stage timing (ms) and launch counts
@@ -119,7 +122,8 @@ void free_all(bem_ctx* ctx) {
                      &ctx->d_part, &ctx->d_post, &ctx->d_mx, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
     for (auto p : dp) *p = nullptr;
     float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
-                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32};
+                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32, &ctx->d_Dhi, &ctx->d_Dlo};
+    ctx->d_Xdf = nullptr;
     for (auto p : fp) *p = nullptr;
     ctx->d_nq = nullptr;
     ctx->d_flags = nullptr;
@@ -275,13 +279,15 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
                 return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
             bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
             CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
-            if (ctx->resid_mode == 2) {
-                // r = y - Re(D) x  (stored FP64) - i Im(D) x  (plane waves, FP64)
-                bem::launch_matx(st, N, Np, ctx->d_D64r, nullptr, R, 0, ctx->d_X, R, ctx->d_mx, -1.0, 1.0, ctx->d_Y,
-                                 ctx->d_Rr, R);
-                const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
-                bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M, ctx->d_pwW,
-                                       ctx->d_pwE, ctx->d_X, ctx->d_pwT, ctx->d_Rr);
+            if (ctx->resid_mode >= 2) {
+                // r = y - Re(D) x  (float pairs, double-float products) - i Im(D) x  (plane waves, FP64)
+                bem::launch_matx_df(st, N, Np, ctx->d_Dhi, ctx->d_Dlo, R, ctx->d_X, ctx->d_Xdf, ctx->d_mx, ctx->d_Y,
+                                    ctx->d_Rr);
+                if (ctx->resid_mode == 3) {
+                    const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
+                    bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M,
+                                           ctx->d_pwW, ctx->d_pwE, ctx->d_X, ctx->d_pwT, ctx->d_Rr);
+                }
             } else {
                 bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0,
                                  ctx->d_X, R, ctx->d_mx, -1.0, 1.0, ctx->d_Y, ctx->d_Rr, R);
@@ -611,6 +617,11 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     cudaStream_t st = ctx->st;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
+    if (mixed) {
+        DA(ctx->d_Dhi, (size_t)N * Np);
+        DA(ctx->d_Dlo, (size_t)N * Np);
+        DA(ctx->d_Xdf, (size_t)N * R);
+    }
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
     for (int f = 0; f < n_freq; ++f) {
@@ -635,6 +646,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         if (mixed) {
             a.xr32 = ctx->d_xr32;
             a.gq32 = ctx->d_gq32;
+            a.Dhi = ctx->d_Dhi;
+            a.Dlo = ctx->d_Dlo;
+            a.D64r = nullptr;
+            a.D64i = nullptr;
         }
         bem::launch_wave(st, a, mixed);
         if (mixed && K != 0.0) {
@@ -645,14 +660,14 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c1 / ctx->pw_M, ctx->d_pwV,
                                    ctx->d_pwE, ctx->d_Bm, ctx->d_pwT, ctx->d_Y);
         }
-        bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, mixed ? ctx->d_D32r : nullptr,
-                                 mixed ? ctx->d_D32i : nullptr);
+        bem::launch_pad_identity(st, N, Np, mixed ? nullptr : ctx->d_D64r, mixed ? nullptr : ctx->d_D64i,
+                                 mixed ? ctx->d_D32r : nullptr, mixed ? ctx->d_D32i : nullptr);
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[5], st));
         int iters = 0;
         double resid = 0;
         double t_lu = 0, t_sv = 0;
-        ctx->resid_mode = mixed ? (K != 0.0 ? 2 : 1) : 0;
+        ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
         s = factor_and_solve(ctx, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
         ctx->resid_mode = 0;
         if (s != BEM_OK) return s;

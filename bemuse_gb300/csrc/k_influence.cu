@@ -264,8 +264,10 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
             continue;
         }
         double dre = a.RD[row + s] + fma(a.RSR[row + s], a.K, (double)wdr);
-        a.D64r[row + s] = dre;
-        a.D32r[row + s] = (float)dre;
+        const float hi = (float)dre;
+        a.Dhi[row + s] = hi;
+        a.Dlo[row + s] = (float)(dre - (double)hi);
+        a.D32r[row + s] = hi;
         a.D32i[row + s] = wdi;
         // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
         const double* b = a.Bm + (size_t)s * 2 * R;

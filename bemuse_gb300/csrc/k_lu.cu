@@ -590,6 +590,83 @@ __global__ void k_matx_reduce(int N, int R, int nchunk, const double* __restrict
     out[o + 1] = beta * bi + alpha * si;
 }
 
+// ---------------------------------------------------------------------------
+// Double-float refinement residual.  GB300's FP64 rate is 1/64 of its FP32 rate
+// and the residual needs ~2R FP64 multiply-adds per matrix element, so it is
+// computed with float pairs: d = dhi + dlo (stored by the wave kernel),
+// x = xhi + xlo; each product as p + e with e exact from an FMA, sums with
+// Knuth's two-sum compensation; per-lane partial sums go to FP64 before the
+// warp and chunk reductions.
+__global__ void k_split_df(size_t n, const double* __restrict__ X, float4* __restrict__ Xdf) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double re = X[2 * i], im = X[2 * i + 1];
+        float rh = (float)re, ih = (float)im;
+        Xdf[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+}
+
+struct DF { float s, c; };
+__device__ __forceinline__ void df_mac(DF& acc, float dh, float dl, float xh, float xl) {
+    float p = dh * xh;
+    float e = fmaf(dh, xh, -p);
+    e = fmaf(dh, xl, fmaf(dl, xh, e));
+    float t = acc.s + p;
+    float z = t - acc.s;
+    acc.c += ((acc.s - (t - z)) + (p - z)) + e;
+    acc.s = t;
+}
+
+__global__ void __launch_bounds__(256) k_matx_df_partial(int N, int ld, const float* __restrict__ Dhi,
+                                                         const float* __restrict__ Dlo, int R,
+                                                         const float4* __restrict__ Xdf, double* __restrict__ part) {
+    extern __shared__ float4 xs4[];  // [R][MX_COLS]
+    const int rt = blockIdx.x, ct = blockIdx.y;
+    const int s0 = ct * MX_COLS;
+    const int ns = min(MX_COLS, N - s0);
+    for (int idx = threadIdx.x; idx < R * MX_COLS; idx += blockDim.x) {
+        int j = idx / MX_COLS, k = idx % MX_COLS;
+        xs4[idx] = k < ns ? Xdf[(size_t)(s0 + k) * R + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int rr = warp; rr < MX_ROWS; rr += 8) {
+        const int r = rt * MX_ROWS + rr;
+        if (r >= N) break;
+        DF ar[MAX_RHS], ai[MAX_RHS];
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) { ar[j] = DF{0.f, 0.f}; ai[j] = DF{0.f, 0.f}; }
+        const float* hrow = Dhi + (size_t)r * ld + s0;
+        const float* lrow = Dlo + (size_t)r * ld + s0;
+        for (int k = lane; k < ns; k += 32) {
+            const float dh = hrow[k], dl = lrow[k];
+#pragma unroll
+            for (int j = 0; j < MAX_RHS; ++j) {
+                if (j < R) {
+                    float4 x = xs4[j * MX_COLS + k];
+                    df_mac(ar[j], dh, dl, x.x, x.y);
+                    df_mac(ai[j], dh, dl, x.z, x.w);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double vr = (double)ar[j].s + (double)ar[j].c, vi = (double)ai[j].s + (double)ai[j].c;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                    vi += __shfl_xor_sync(0xffffffffu, vi, off);
+                }
+                if (lane == 0) {
+                    double* p = part + 2 * (((size_t)ct * N + r) * R + j);
+                    p[0] = vr;
+                    p[1] = vi;
+                }
+            }
+        }
+    }
+}
+
 // Per-column max |Rres| and max |Y| (non-negative doubles compare as integers).
 __global__ void k_norms(int N, int R, const double* __restrict__ Rres, const double* __restrict__ Y,
                         unsigned long long* nrm) {
@@ -655,6 +732,19 @@ void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double*
     size_t tot = (size_t)N * R;
     BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, R, (int)grd.y, part, alpha, beta,
                                                                              base, out, j0, ostride));
+}
+
+void launch_matx_df(cudaStream_t st, int N, int ld, const float* Dhi, const float* Dlo, int R, const double* X,
+                    float4* Xdf, double* part, const double* Y, double* Rres) {
+    BEM_LAUNCH(k_split_df<<<256, 256, 0, st>>>((size_t)N * R, X, Xdf));
+    dim3 grd((N + MX_ROWS - 1) / MX_ROWS, (N + MX_COLS - 1) / MX_COLS);
+    size_t smem = sizeof(float4) * R * MX_COLS;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_matx_df_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_matx_df_partial<<<grd, 256, smem, st>>>(N, ld, Dhi, Dlo, R, Xdf, part));
+    size_t tot = (size_t)N * R;
+    BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, R, (int)grd.y, part, -1.0, 1.0, Y,
+                                                                             Rres, 0, R));
 }
 
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm) {
