@@ -126,6 +126,161 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 }
 
 // ---------------------------------------------------------------------------
+// 128 x 128 block inverse by 2 x 2 Schur complement, one CTA of 1024 threads:
+//   M = [A B; C E],  S = E - C A^-1 B,
+//   M^-1 = [A^-1 + T S^-1 T2,  -T S^-1;  -S^-1 T2,  S^-1],  T = A^-1 B, T2 = C A^-1.
+// The two 64 x 64 inverses are Gauss-Jordan with the block held in registers
+// (2 x 2 complex per thread, one barrier per pivot); the four 64^3 complex
+// products run from shared memory.  Same flags as k_gj_inv.
+constexpr int IV_LD = 132;  // padded row of the 128 x 128 tile (16-byte aligned)
+constexpr int IV_TD = 68;   // padded row of the 64 x 64 temporary
+
+// In-place Gauss-Jordan inverse of the 64 x 64 block at (r0, c0) of (Mr, Mi).
+__device__ void iv_gj64(float* Mr, float* Mi, int ld, int r0, int c0, float* rowr, float* rowi, float* colr,
+                        float* coli, int& local_flags) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float vr[2][2], vi[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            vr[a][b] = Mr[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b];
+            vi[a][b] = Mi[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b];
+        }
+    __syncthreads();
+    for (int k = 0; k < 64; ++k) {
+        const int buf = k & 1, ka = k >> 5, kt = k & 31;
+        if (ty == kt) {
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                rowr[buf * 64 + tx + 32 * b] = ka ? vr[1][b] : vr[0][b];
+                rowi[buf * 64 + tx + 32 * b] = ka ? vi[1][b] : vi[0][b];
+            }
+        }
+        if (tx == kt) {
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                colr[buf * 64 + ty + 32 * a] = ka ? vr[a][1] : vr[a][0];
+                coli[buf * 64 + ty + 32 * a] = ka ? vi[a][1] : vi[a][0];
+            }
+        }
+        __syncthreads();
+        const float pr = colr[buf * 64 + k], pi = coli[buf * 64 + k];
+        const float den = pr * pr + pi * pi;
+        if (threadIdx.x == 0 && (!(den > 0.f) || !isfinite(den))) local_flags |= FLAG_ZERO_PIVOT;
+        const float qr = pr / den, qi = -pi / den;
+        float nr[2], ni[2];
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const int j = tx + 32 * b;
+            float xr = (j == k) ? 1.f : rowr[buf * 64 + j], xi = (j == k) ? 0.f : rowi[buf * 64 + j];
+            nr[b] = xr * qr - xi * qi;
+            ni[b] = xr * qi + xi * qr;
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            const int i = ty + 32 * a;
+            if (i == k) {
+#pragma unroll
+                for (int b = 0; b < 2; ++b) { vr[a][b] = nr[b]; vi[a][b] = ni[b]; }
+            } else {
+                const float cr = colr[buf * 64 + i], ci = coli[buf * 64 + i];
+                if (tx == kt && i > k) {
+                    float lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
+                    if (lr * lr + li * li > 1.000002f) local_flags |= FLAG_PIVOT;
+                }
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const int j = tx + 32 * b;
+                    if (j == k) {
+                        vr[a][b] = -(cr * nr[b] - ci * ni[b]);
+                        vi[a][b] = -(cr * ni[b] + ci * nr[b]);
+                    } else {
+                        vr[a][b] -= cr * nr[b] - ci * ni[b];
+                        vi[a][b] -= cr * ni[b] + ci * nr[b];
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            Mr[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b] = vr[a][b];
+            Mi[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b] = vi[a][b];
+        }
+    __syncthreads();
+}
+
+// D (64 x 64) = sgn * X Y  (mode 0)  or  D += sgn * X Y  (mode 1); all in shared
+// memory with their own leading dimensions; D must not alias X or Y.
+__device__ void iv_gemm64(float* Dr, float* Di, int ldd, const float* Xr, const float* Xi, int ldx, const float* Yr,
+                          const float* Yi, int ldy, float sgn, int mode) {
+    const int r = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
+    float ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
+#pragma unroll 8
+    for (int k = 0; k < 64; ++k) {
+        const float xr = Xr[r * ldx + k], xi = Xi[r * ldx + k];
+        const float4 yr = *reinterpret_cast<const float4*>(Yr + k * ldy + c0);
+        const float4 yi = *reinterpret_cast<const float4*>(Yi + k * ldy + c0);
+        const float br[4] = {yr.x, yr.y, yr.z, yr.w}, bi[4] = {yi.x, yi.y, yi.z, yi.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            ar[q] = fmaf(xr, br[q], fmaf(-xi, bi[q], ar[q]));
+            ai[q] = fmaf(xr, bi[q], fmaf(xi, br[q], ai[q]));
+        }
+    }
+    __syncthreads();  // every read of X, Y done before D is written
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        float* dr = Dr + r * ldd + c0 + q;
+        float* di = Di + r * ldd + c0 + q;
+        if (mode) { *dr += sgn * ar[q]; *di += sgn * ai[q]; }
+        else { *dr = sgn * ar[q]; *di = sgn * ai[q]; }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_inv128(int k0, CMat<float> A, float* invr, float* invi, int* flags) {
+    extern __shared__ __align__(16) float iv_smem[];
+    float* Mr = iv_smem;                   // [128][IV_LD]
+    float* Mi = Mr + 128 * IV_LD;
+    float* Tr = Mi + 128 * IV_LD;          // [64][IV_TD]
+    float* Ti = Tr + 64 * IV_TD;
+    __shared__ float rowr[128], rowi[128], colr[128], coli[128];
+    for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
+        int i = idx >> 7, j = idx & 127;
+        size_t g = (size_t)(k0 + i) * A.ld + k0 + j;
+        Mr[i * IV_LD + j] = A.re[g];
+        Mi[i * IV_LD + j] = A.im[g];
+    }
+    __syncthreads();
+    int lf = 0;
+    float *Ar = Mr, *Ai = Mi;                                   // (0, 0)
+    float *Br = Mr + 64, *Bi = Mi + 64;                         // (0, 64)
+    float *Cr = Mr + 64 * IV_LD, *Ci = Mi + 64 * IV_LD;         // (64, 0)
+    float *Er = Mr + 64 * IV_LD + 64, *Ei = Mi + 64 * IV_LD + 64;  // (64, 64)
+    iv_gj64(Mr, Mi, IV_LD, 0, 0, rowr, rowi, colr, coli, lf);    // A^-1
+    iv_gemm64(Tr, Ti, IV_TD, Ar, Ai, IV_LD, Br, Bi, IV_LD, 1.f, 0);     // T = A^-1 B
+    iv_gemm64(Er, Ei, IV_LD, Cr, Ci, IV_LD, Tr, Ti, IV_TD, -1.f, 1);    // S = E - C T
+    iv_gj64(Mr, Mi, IV_LD, 64, 64, rowr, rowi, colr, coli, lf);  // S^-1
+    iv_gemm64(Br, Bi, IV_LD, Tr, Ti, IV_TD, Er, Ei, IV_LD, -1.f, 0);    // TR = -T S^-1
+    iv_gemm64(Tr, Ti, IV_TD, Cr, Ci, IV_LD, Ar, Ai, IV_LD, 1.f, 0);     // T2 = C A^-1
+    iv_gemm64(Ar, Ai, IV_LD, Br, Bi, IV_LD, Tr, Ti, IV_TD, -1.f, 1);    // TL = A^-1 - TR T2
+    iv_gemm64(Cr, Ci, IV_LD, Er, Ei, IV_LD, Tr, Ti, IV_TD, -1.f, 0);    // BL = -S^-1 T2
+    float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
+    float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
+    for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
+        int i = idx >> 7, j = idx & 127;
+        Or[idx] = Mr[i * IV_LD + j];
+        Oi[idx] = Mi[i * IV_LD + j];
+    }
+    if (lf) atomicOr(flags, lf);
+}
+
+// ---------------------------------------------------------------------------
 // C = beta C + sgn * A B, planar complex, row-major.  M, N multiples of 64,
 // K multiple of 16.  256 threads, 64x64 tile, 4x4 outputs per thread.
 template <typename T>
@@ -221,8 +376,16 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
     (void)wu;
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
+    constexpr size_t IV_SMEM = sizeof(float) * (2 * 128 * IV_LD + 2 * 64 * IV_TD);
+    if (NB == 128 && sizeof(T) == 4)
+        cudaFuncSetAttribute(k_inv128, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)IV_SMEM);
     for (int k0 = 0; k0 < n; k0 += NB) {
-        BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
+        if (NB == 128 && sizeof(T) == 4)
+            BEM_LAUNCH(k_inv128<<<1, 1024, IV_SMEM, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
+                                                        reinterpret_cast<float*>(invr), reinterpret_cast<float*>(invi),
+                                                        flags));
+        else
+            BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
         if (rem <= 0) break;
         const int blk = k0 / NB;
@@ -482,6 +645,227 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
                : 1;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 block triangular solve, split by rows: each 128-row block of the system
+// is shared by four CTAs of 32 rows (sub-blocks), so the product that sits on
+// the critical path (one 32 x 128 tile against the newest block of x) is a
+// quarter of a block's.  Thread (lane i, warp s) owns row i of the sub-block
+// and the 16 columns s*16.. of every tile; the tile is prefetched into
+// registers one dependency ahead, the block of x is staged in shared memory
+// (complex interleaved, RC columns, zero-padded), and the eight column slices
+// are summed once at the end.
+//   which = 0 (forward, unit block-lower L):  x_b = y_b - sum_{c<b} L_bc x_c
+//   which = 1 (backward):  w_b = y_b - sum_{c>b} U_bc x_c  (written over y_b),
+//                          x_b = Dinv_b w_b once the four sub-blocks of w_b exist.
+// xflag[u] / wflag[u] (u = sub-block) are raised to `epoch` when x / w rows of u
+// are in memory.  Waits give up at a 2 s deadline (FLAG_TIMEOUT).
+// Grid: a multiple of 4 CTAs, all co-resident (cooperative launch); sub-blocks are
+// dealt out in dependency order, so the four siblings of a block always run
+// together on distinct CTAs and every wait is on work that is placed earlier.
+constexpr int TS_NB = 128, TS_SB = 4, TS_KS = 8, TS_KC = TS_NB / TS_KS;
+
+__device__ __forceinline__ unsigned long long ts_now() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void ts_wait(const int* f, int epoch, unsigned long long deadline, int& dead,
+                                        int* gflags) {
+    if (dead) return;
+    for (;;) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+        if (v >= epoch) return;
+        if (ts_now() > deadline) { dead = 1; atomicOr(gflags, FLAG_TIMEOUT); return; }
+    }
+}
+
+__device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const float* __restrict__ gi, float* r,
+                                            float* im) {
+#pragma unroll
+    for (int v = 0; v < TS_KC / 4; ++v) {
+        float4 a = __ldg(reinterpret_cast<const float4*>(gr) + v);
+        float4 b = __ldg(reinterpret_cast<const float4*>(gi) + v);
+        r[4 * v] = a.x; r[4 * v + 1] = a.y; r[4 * v + 2] = a.z; r[4 * v + 3] = a.w;
+        im[4 * v] = b.x; im[4 * v + 1] = b.y; im[4 * v + 2] = b.z; im[4 * v + 3] = b.w;
+    }
+}
+
+template <int RC>
+__global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_sub(int nblk, int R, CMat<float> A,
+                                                         const float* __restrict__ invr,
+                                                         const float* __restrict__ invi, int which, float* Yin,
+                                                         float* Xout, int* xflag, int* wflag, int epoch,
+                                                         int* gflags) {
+    extern __shared__ __align__(16) float ts_smem[];
+    float* zs = ts_smem;                        // [2][TS_NB][RC] complex interleaved
+    float* red = zs + 2 * TS_NB * RC * 2;       // [TS_KS][32][RC] complex interleaved
+    const int tid = threadIdx.x, lane = tid & 31, s = tid >> 5;
+    const unsigned long long deadline = ts_now() + 2000000000ull;
+    int dead = 0;
+    for (int idx = tid; idx < 2 * TS_NB * RC * 2; idx += blockDim.x) zs[idx] = 0.f;
+    __syncthreads();
+    const int nsub = nblk * TS_SB;
+    for (int u0 = blockIdx.x; u0 < nsub; u0 += gridDim.x) {
+        const int bo = u0 / TS_SB, q = u0 % TS_SB;
+        const int b = which == 0 ? bo : nblk - 1 - bo;
+        const int u = b * TS_SB + q;
+        const size_t row0 = (size_t)b * TS_NB + q * 32;
+        const int cnt = which == 0 ? b : nblk - 1 - b;
+        float ar[RC], ai[RC];
+#pragma unroll
+        for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+        float cr[TS_KC], ci[TS_KC], nr[TS_KC], ni[TS_KC];
+        auto tile_ptr = [&](int t, const float*& pr, const float*& pi) {
+            const int c = which == 0 ? t : nblk - 1 - t;
+            const size_t off = (row0 + lane) * A.ld + (size_t)c * TS_NB + s * TS_KC;
+            pr = A.re + off;
+            pi = A.im + off;
+        };
+        auto inv_ptr = [&](const float*& pr, const float*& pi) {
+            const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * 32 + lane) * TS_NB + s * TS_KC;
+            pr = invr + off;
+            pi = invi + off;
+        };
+        {
+            const float *pr, *pi;
+            if (cnt > 0) tile_ptr(0, pr, pi);
+            else inv_ptr(pr, pi);
+            if (cnt > 0 || which == 1) ts_load_row(pr, pi, cr, ci);
+        }
+        for (int t = 0; t < cnt; ++t) {
+            const int c = which == 0 ? t : nblk - 1 - t;
+            if (t + 1 < cnt || which == 1) {
+                const float *pr, *pi;
+                if (t + 1 < cnt) tile_ptr(t + 1, pr, pi);
+                else inv_ptr(pr, pi);
+                ts_load_row(pr, pi, nr, ni);
+            }
+            if (tid < TS_SB) {
+                ts_wait(xflag + c * TS_SB + tid, epoch, deadline, dead, gflags);
+            }
+            __syncthreads();
+            float* z = zs + (t & 1) * TS_NB * RC * 2;
+            for (int idx = tid; idx < TS_NB * R; idx += blockDim.x) {
+                const int k = idx / R, j = idx % R;
+                const float2 v = __ldcg(reinterpret_cast<const float2*>(Xout) + ((size_t)c * TS_NB + k) * R + j);
+                *reinterpret_cast<float2*>(z + (k * RC + j) * 2) = v;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int kk = 0; kk < TS_KC; ++kk) {
+                const float lr = cr[kk], li = ci[kk];
+                const float4* zk = reinterpret_cast<const float4*>(z + (s * TS_KC + kk) * RC * 2);
+#pragma unroll
+                for (int j2 = 0; j2 < RC / 2; ++j2) {
+                    const float4 v = zk[j2];
+                    ar[2 * j2] = fmaf(-lr, v.x, fmaf(li, v.y, ar[2 * j2]));
+                    ai[2 * j2] = fmaf(-lr, v.y, fmaf(-li, v.x, ai[2 * j2]));
+                    ar[2 * j2 + 1] = fmaf(-lr, v.z, fmaf(li, v.w, ar[2 * j2 + 1]));
+                    ai[2 * j2 + 1] = fmaf(-lr, v.w, fmaf(-li, v.z, ai[2 * j2 + 1]));
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < TS_KC; ++kk) { cr[kk] = nr[kk]; ci[kk] = ni[kk]; }
+        }
+        // sum the column slices: out = y + sum_s acc_s
+        auto reduce_out = [&](const float* base, float* dst) {
+#pragma unroll
+            for (int j = 0; j < RC; ++j)
+                *reinterpret_cast<float2*>(red + ((s * 32 + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+            __syncthreads();
+            for (int idx = tid; idx < 32 * R; idx += blockDim.x) {
+                const int i = idx / R, j = idx % R;
+                float2 o = base ? reinterpret_cast<const float2*>(base)[(row0 + i) * R + j] : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int w = 0; w < TS_KS; ++w) {
+                    const float2 v = *reinterpret_cast<const float2*>(red + ((w * 32 + i) * RC + j) * 2);
+                    o.x += v.x;
+                    o.y += v.y;
+                }
+                reinterpret_cast<float2*>(dst)[(row0 + i) * R + j] = o;
+            }
+            __threadfence();
+            __syncthreads();
+        };
+        if (which == 0) {
+            reduce_out(Yin, Xout);
+            if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+            continue;
+        }
+        // backward: w rows over y, then x = Dinv_b w_b (cr/ci hold the Dinv rows)
+        reduce_out(Yin, Yin);
+        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(wflag + u), "r"(epoch) : "memory");
+        if (tid < TS_SB) {
+            ts_wait(wflag + b * TS_SB + tid, epoch, deadline, dead, gflags);
+        }
+        __syncthreads();
+        float* z = zs;
+        for (int idx = tid; idx < TS_NB * R; idx += blockDim.x) {
+            const int k = idx / R, j = idx % R;
+            const float2 v = __ldcg(reinterpret_cast<const float2*>(Yin) + ((size_t)b * TS_NB + k) * R + j);
+            *reinterpret_cast<float2*>(z + (k * RC + j) * 2) = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+#pragma unroll
+        for (int kk = 0; kk < TS_KC; ++kk) {
+            const float lr = cr[kk], li = ci[kk];
+            const float4* zk = reinterpret_cast<const float4*>(z + (s * TS_KC + kk) * RC * 2);
+#pragma unroll
+            for (int j2 = 0; j2 < RC / 2; ++j2) {
+                const float4 v = zk[j2];
+                ar[2 * j2] = fmaf(lr, v.x, fmaf(-li, v.y, ar[2 * j2]));
+                ai[2 * j2] = fmaf(lr, v.y, fmaf(li, v.x, ai[2 * j2]));
+                ar[2 * j2 + 1] = fmaf(lr, v.z, fmaf(-li, v.w, ar[2 * j2 + 1]));
+                ai[2 * j2 + 1] = fmaf(lr, v.w, fmaf(li, v.z, ai[2 * j2 + 1]));
+            }
+        }
+        reduce_out(nullptr, Xout);
+        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+    }
+}
+
+template <int RC>
+static int trsv_sub_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which,
+                           int R, float* Y, float* X, int* xflag, int* wflag, int epoch, int* flags) {
+    const int nblk = n / TS_NB;
+    const size_t smem = sizeof(float) * (2 * TS_NB * RC * 2 + TS_KS * 32 * RC * 2);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_trsv_sub<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_sub<RC>, 32 * TS_KS, smem);
+    int grid = std::min(nblk * TS_SB, std::max(1, per_sm) * nsm);
+    grid -= grid % TS_SB;
+    if (grid < TS_SB) return 1;
+    void* args[] = {(void*)&nblk, (void*)&R,     (void*)&A,     (void*)&invr,  (void*)&invi,  (void*)&which,
+                    (void*)&Y,    (void*)&X,     (void*)&xflag, (void*)&wflag, (void*)&epoch, (void*)&flags};
+    ++g_launches;
+    return cudaLaunchCooperativeKernel((void*)k_trsv_sub<RC>, dim3(grid), dim3(32 * TS_KS), args, smem, st) ==
+                   cudaSuccess
+               ? 0
+               : 1;
+}
+
+static int trsv_sub(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which, int R,
+                    float* Y, float* X, int* xflag, int* wflag, int epoch, int* flags) {
+    switch ((R + 1) / 2) {
+        case 1: return trsv_sub_launch<2>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 2: return trsv_sub_launch<4>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 3: return trsv_sub_launch<6>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 4: return trsv_sub_launch<8>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 5: return trsv_sub_launch<10>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 6: return trsv_sub_launch<12>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 7: return trsv_sub_launch<14>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 8: return trsv_sub_launch<16>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        default: return 1;
+    }
+}
+
 // The solve needs an n x R scratch; it lives right after X (caller allocates 2 n R).
 // ready: n/nb ints, zero at allocation; epoch: strictly increasing per call (2 used per call).
 int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
@@ -492,9 +876,12 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
+    // ready holds n/16 flags: x flags of the n/32 sub-blocks, then their w flags.
     float* tmp = X + (size_t)2 * n * R;
-    if (trsv_coop<float, 128, 4>(st, n, A, invr, invi, 0, R, X, tmp, ready, epoch, flags)) return 1;
-    return trsv_coop<float, 128, 4>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
+    int* xflag = ready;
+    int* wflag = ready + n / 32;
+    if (trsv_sub(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, epoch, flags)) return 1;
+    return trsv_sub(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, epoch + 1, flags);
 }
 
 // ---------------------------------------------------------------------------
