@@ -94,11 +94,15 @@ size_t matx_part_doubles(int N, int R);
 void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double* Mi, int R, int j0, const double* X,
                  int xstride, double* part, double alpha, double beta, const double* base, double* out,
                  int ostride);
-// Rres = Y - (Dhi + Dlo) X for a real operator stored as float pairs, in
-// double-float arithmetic (products exact to ~2^-48, compensated sums); X is
-// FP64 and is split into float pairs first (Xdf: N x R float4 scratch).
-void launch_matx_df(cudaStream_t st, int N, int ld, const float* Dhi, const float* Dlo, int R, const double* X,
-                    float4* Xdf, double* part, const double* Y, double* Rres);
+// Same contract as launch_matx for a real matrix stored as float pairs
+// (M = Mhi + Mlo), in double-float arithmetic (products exact to ~2^-48,
+// compensated sums); the selected columns of X are split into float pairs first
+// (Xdf: N x R float4 scratch).
+void launch_matx_df(cudaStream_t st, int N, int ld, const float* Mhi, const float* Mlo, int R, const double* X,
+                    int xstride, int j0, float4* Xdf, double* part, double alpha, double beta, const double* base,
+                    double* out, int ostride);
+// hi[i] = (float)M[i], lo[i] = (float)(M[i] - hi[i]) for n doubles.
+void launch_split_mat_df(cudaStream_t st, size_t n, const double* M, float* hi, float* lo);
 // nrm[j] = max_r |Rres[r][j]|, nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (zero them first).
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm);
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);

@@ -49,6 +49,8 @@ struct bem_ctx {
     float *d_D32r = nullptr, *d_D32i = nullptr;
     float *d_Dhi = nullptr, *d_Dlo = nullptr;   // Re D as float pairs (mixed refinement residual)
     float4* d_Xdf = nullptr;
+    float *d_RShi = nullptr, *d_RSlo = nullptr;  // Rankine source matrix as float pairs (mixed solves)
+    bool rs_df = false;
     double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
     float* d_X32 = nullptr;
     double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr, *d_mx = nullptr;
@@ -122,7 +124,9 @@ void free_all(bem_ctx* ctx) {
                      &ctx->d_part, &ctx->d_post, &ctx->d_mx, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
     for (auto p : dp) *p = nullptr;
     float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
-                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32, &ctx->d_Dhi, &ctx->d_Dlo};
+                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32, &ctx->d_Dhi, &ctx->d_Dlo,
+                    &ctx->d_RShi, &ctx->d_RSlo};
+    ctx->rs_df = false;
     ctx->d_Xdf = nullptr;
     for (auto p : fp) *p = nullptr;
     ctx->d_nq = nullptr;
@@ -281,8 +285,8 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
             CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
             if (ctx->resid_mode >= 2) {
                 // r = y - Re(D) x  (float pairs, double-float products) - i Im(D) x  (plane waves, FP64)
-                bem::launch_matx_df(st, N, Np, ctx->d_Dhi, ctx->d_Dlo, R, ctx->d_X, ctx->d_Xdf, ctx->d_mx, ctx->d_Y,
-                                    ctx->d_Rr);
+                bem::launch_matx_df(st, N, Np, ctx->d_Dhi, ctx->d_Dlo, R, ctx->d_X, R, 0, ctx->d_Xdf, ctx->d_mx,
+                                    -1.0, 1.0, ctx->d_Y, ctx->d_Rr, R);
                 if (ctx->resid_mode == 3) {
                     const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
                     bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M,
@@ -621,6 +625,12 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         DA(ctx->d_Dhi, (size_t)N * Np);
         DA(ctx->d_Dlo, (size_t)N * Np);
         DA(ctx->d_Xdf, (size_t)N * R);
+        if (NB > 0 && !ctx->rs_df) {
+            DA(ctx->d_RShi, (size_t)N * Np);
+            DA(ctx->d_RSlo, (size_t)N * Np);
+            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RS, ctx->d_RShi, ctx->d_RSlo);
+            ctx->rs_df = true;
+        }
     }
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
@@ -633,7 +643,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         // Y[:, 0:6] = RS N_k (precomputed); Y[:, 6:] = RS B_diff
         CK(cudaMemcpy2DAsync(ctx->d_Y, sizeof(double) * 2 * R, ctx->d_Ys6, sizeof(double) * 2 * R,
                              sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToDevice, st));
-        if (NB > 0)
+        if (NB > 0 && mixed)
+            bem::launch_matx_df(st, N, Np, ctx->d_RShi, ctx->d_RSlo, NB, ctx->d_Bm, R, 6, ctx->d_Xdf, ctx->d_mx, 1.0,
+                                0.0, nullptr, ctx->d_Y, R);
+        else if (NB > 0)
             bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, NB, 6, ctx->d_Bm, R, ctx->d_mx, 1.0, 0.0, nullptr,
                              ctx->d_Y, R);
         CK(cudaEventRecord(ctx->ev[1], st));

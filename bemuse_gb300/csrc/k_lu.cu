@@ -978,17 +978,34 @@ __global__ void k_matx_reduce(int N, int R, int nchunk, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Double-float refinement residual.  GB300's FP64 rate is 1/64 of its FP32 rate
-// and the residual needs ~2R FP64 multiply-adds per matrix element, so it is
-// computed with float pairs: d = dhi + dlo (stored by the wave kernel),
+// Double-float products M X for a real N x N matrix held as float pairs
+// (m = mhi + mlo) and a complex N x R block X.  GB300's FP64 rate is 1/64 of its
+// FP32 rate, so the refinement residual (M = Re D) and the static right-hand
+// side (M = the Rankine source matrix) are formed with float pairs:
 // x = xhi + xlo; each product as p + e with e exact from an FMA, sums with
-// Knuth's two-sum compensation; per-lane partial sums go to FP64 before the
-// warp and chunk reductions.
-__global__ void k_split_df(size_t n, const double* __restrict__ X, float4* __restrict__ Xdf) {
+// Knuth's two-sum compensation.  One thread per matrix row, so the X chunk is a
+// shared-memory broadcast and no cross-lane reduction is needed; each thread's
+// pair goes to FP64 once per 256-column chunk and the chunks are summed by
+// k_matx_reduce.
+constexpr int MXD_ROWS = 128, MXD_COLS = 256;
+
+__global__ void k_split_df(int N, int R, const double* __restrict__ X, int xstride, int j0,
+                           float4* __restrict__ Xdf) {
+    const size_t n = (size_t)N * R;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double re = X[2 * i], im = X[2 * i + 1];
-        float rh = (float)re, ih = (float)im;
+        const size_t r = i / R, j = i % R;
+        const double re = X[2 * (r * xstride + j0 + j)], im = X[2 * (r * xstride + j0 + j) + 1];
+        const float rh = (float)re, ih = (float)im;
         Xdf[i] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+}
+
+__global__ void k_split_mat_df(size_t n, const double* __restrict__ M, float* __restrict__ hi, float* __restrict__ lo) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = M[i];
+        const float h = (float)v;
+        hi[i] = h;
+        lo[i] = (float)(v - (double)h);
     }
 }
 
@@ -1003,54 +1020,59 @@ __device__ __forceinline__ void df_mac(DF& acc, float dh, float dl, float xh, fl
     acc.s = t;
 }
 
-__global__ void __launch_bounds__(256) k_matx_df_partial(int N, int ld, const float* __restrict__ Dhi,
-                                                         const float* __restrict__ Dlo, int R,
-                                                         const float4* __restrict__ Xdf, double* __restrict__ part) {
-    extern __shared__ float4 xs4[];  // [R][MX_COLS]
-    const int rt = blockIdx.x, ct = blockIdx.y;
-    const int s0 = ct * MX_COLS;
-    const int ns = min(MX_COLS, N - s0);
-    for (int idx = threadIdx.x; idx < R * MX_COLS; idx += blockDim.x) {
-        int j = idx / MX_COLS, k = idx % MX_COLS;
-        xs4[idx] = k < ns ? Xdf[(size_t)(s0 + k) * R + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+template <int RR>
+__global__ void __launch_bounds__(MXD_ROWS) k_matx_df(int N, int ld, const float* __restrict__ Mhi,
+                                                      const float* __restrict__ Mlo,
+                                                      const float4* __restrict__ Xdf, double* __restrict__ part) {
+    extern __shared__ float4 xs4[];  // [MXD_COLS][RR]
+    const int ct = blockIdx.y;
+    const int s0 = ct * MXD_COLS;
+    const int ns = min(MXD_COLS, N - s0);
+    for (int idx = threadIdx.x; idx < RR * MXD_COLS; idx += blockDim.x) {
+        const int k = idx / RR, j = idx % RR;
+        xs4[idx] = k < ns ? Xdf[(size_t)(s0 + k) * RR + j] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int rr = warp; rr < MX_ROWS; rr += 8) {
-        const int r = rt * MX_ROWS + rr;
-        if (r >= N) break;
-        DF ar[MAX_RHS], ai[MAX_RHS];
+    const int r = blockIdx.x * MXD_ROWS + threadIdx.x;
+    if (r >= N) return;
+    DF ar[RR], ai[RR];
 #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) { ar[j] = DF{0.f, 0.f}; ai[j] = DF{0.f, 0.f}; }
-        const float* hrow = Dhi + (size_t)r * ld + s0;
-        const float* lrow = Dlo + (size_t)r * ld + s0;
-        for (int k = lane; k < ns; k += 32) {
-            const float dh = hrow[k], dl = lrow[k];
+    for (int j = 0; j < RR; ++j) { ar[j] = DF{0.f, 0.f}; ai[j] = DF{0.f, 0.f}; }
+    const float* hrow = Mhi + (size_t)r * ld + s0;
+    const float* lrow = Mlo + (size_t)r * ld + s0;
+    const int n8 = ns & ~7;
+    for (int k = 0; k < n8; k += 8) {
+        const float4 h0 = __ldg(reinterpret_cast<const float4*>(hrow + k));
+        const float4 h1 = __ldg(reinterpret_cast<const float4*>(hrow + k + 4));
+        const float4 l0 = __ldg(reinterpret_cast<const float4*>(lrow + k));
+        const float4 l1 = __ldg(reinterpret_cast<const float4*>(lrow + k + 4));
+        const float dh[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+        const float dl[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
 #pragma unroll
-            for (int j = 0; j < MAX_RHS; ++j) {
-                if (j < R) {
-                    float4 x = xs4[j * MX_COLS + k];
-                    df_mac(ar[j], dh, dl, x.x, x.y);
-                    df_mac(ai[j], dh, dl, x.z, x.w);
-                }
+        for (int kk = 0; kk < 8; ++kk) {
+            const float4* xk = xs4 + (k + kk) * RR;
+#pragma unroll
+            for (int j = 0; j < RR; ++j) {
+                const float4 x = xk[j];
+                df_mac(ar[j], dh[kk], dl[kk], x.x, x.y);
+                df_mac(ai[j], dh[kk], dl[kk], x.z, x.w);
             }
         }
+    }
+    for (int k = n8; k < ns; ++k) {
+        const float dh = hrow[k], dl = lrow[k];
 #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) {
-            if (j < R) {
-                double vr = (double)ar[j].s + (double)ar[j].c, vi = (double)ai[j].s + (double)ai[j].c;
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    vr += __shfl_xor_sync(0xffffffffu, vr, off);
-                    vi += __shfl_xor_sync(0xffffffffu, vi, off);
-                }
-                if (lane == 0) {
-                    double* p = part + 2 * (((size_t)ct * N + r) * R + j);
-                    p[0] = vr;
-                    p[1] = vi;
-                }
-            }
+        for (int j = 0; j < RR; ++j) {
+            const float4 x = xs4[k * RR + j];
+            df_mac(ar[j], dh, dl, x.x, x.y);
+            df_mac(ai[j], dh, dl, x.z, x.w);
         }
+    }
+#pragma unroll
+    for (int j = 0; j < RR; ++j) {
+        double* p = part + 2 * (((size_t)ct * N + r) * RR + j);
+        p[0] = (double)ar[j].s + (double)ar[j].c;
+        p[1] = (double)ai[j].s + (double)ai[j].c;
     }
 }
 
@@ -1103,7 +1125,9 @@ __global__ void k_pad_rhs(int N, int Np, int R, double* X) {
         X[(size_t)N * R * 2 + i] = 0.0;
 }
 
-size_t matx_part_doubles(int N, int R) { return (size_t)2 * ((N + MX_COLS - 1) / MX_COLS) * N * R; }
+size_t matx_part_doubles(int N, int R) {
+    return (size_t)2 * ((N + std::min(MX_COLS, MXD_COLS) - 1) / std::min(MX_COLS, MXD_COLS)) * N * R;
+}
 
 void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double* Mi, int R, int j0, const double* X,
                  int xstride, double* part, double alpha, double beta, const double* base, double* out,
@@ -1121,17 +1145,44 @@ void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double*
                                                                              base, out, j0, ostride));
 }
 
-void launch_matx_df(cudaStream_t st, int N, int ld, const float* Dhi, const float* Dlo, int R, const double* X,
-                    float4* Xdf, double* part, const double* Y, double* Rres) {
-    BEM_LAUNCH(k_split_df<<<256, 256, 0, st>>>((size_t)N * R, X, Xdf));
-    dim3 grd((N + MX_ROWS - 1) / MX_ROWS, (N + MX_COLS - 1) / MX_COLS);
-    size_t smem = sizeof(float4) * R * MX_COLS;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_matx_df_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    BEM_LAUNCH(k_matx_df_partial<<<grd, 256, smem, st>>>(N, ld, Dhi, Dlo, R, Xdf, part));
-    size_t tot = (size_t)N * R;
-    BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, R, (int)grd.y, part, -1.0, 1.0, Y,
-                                                                             Rres, 0, R));
+template <int RR>
+static void matx_df_rr(cudaStream_t st, int N, int ld, const float* Mhi, const float* Mlo, const float4* Xdf,
+                       double* part) {
+    dim3 grd((N + MXD_ROWS - 1) / MXD_ROWS, (N + MXD_COLS - 1) / MXD_COLS);
+    const size_t smem = sizeof(float4) * RR * MXD_COLS;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_matx_df<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_matx_df<RR><<<grd, MXD_ROWS, smem, st>>>(N, ld, Mhi, Mlo, Xdf, part));
+}
+
+void launch_matx_df(cudaStream_t st, int N, int ld, const float* Mhi, const float* Mlo, int R, const double* X,
+                    int xstride, int j0, float4* Xdf, double* part, double alpha, double beta, const double* base,
+                    double* out, int ostride) {
+    BEM_LAUNCH(k_split_df<<<256, 256, 0, st>>>(N, R, X, xstride, j0, Xdf));
+    switch (R) {
+        case 1: matx_df_rr<1>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 2: matx_df_rr<2>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 3: matx_df_rr<3>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 4: matx_df_rr<4>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 5: matx_df_rr<5>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 6: matx_df_rr<6>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 7: matx_df_rr<7>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 8: matx_df_rr<8>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 9: matx_df_rr<9>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 10: matx_df_rr<10>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 11: matx_df_rr<11>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 12: matx_df_rr<12>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 13: matx_df_rr<13>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 14: matx_df_rr<14>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        case 15: matx_df_rr<15>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+        default: matx_df_rr<16>(st, N, ld, Mhi, Mlo, Xdf, part); break;
+    }
+    const size_t tot = (size_t)N * R;
+    BEM_LAUNCH(k_matx_reduce<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(
+        N, R, (N + MXD_COLS - 1) / MXD_COLS, part, alpha, beta, base, out, j0, ostride));
+}
+
+void launch_split_mat_df(cudaStream_t st, size_t n, const double* M, float* hi, float* lo) {
+    BEM_LAUNCH(k_split_mat_df<<<1024, 256, 0, st>>>(n, M, hi, lo));
 }
 
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm) {
