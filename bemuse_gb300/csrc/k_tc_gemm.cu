@@ -1,17 +1,21 @@
 // k_tc_gemm.cu -- tcgen05 TF32 trailing update of the complex LU:
 //     A22 -= L21 * U12      (planar complex, FP32 storage, FP32 accumulation)
 //
-// One CTA computes a 128 x 256 tile of A22.  The complex product is four real
-// TF32 MMAs into two TMEM accumulators:
+// Persistent, warp-specialised kernel over 128 x 128 tiles of A22 (or of any
+// tile-aligned rectangle of it).  The complex product is four real TF32 MMAs
+// into two TMEM accumulators:
 //     Cr = Lr Ur^T - Li Ui^T        (the minus via the instruction's negate-A bit)
 //     Ci = Lr Ui^T + Li Ur^T
-// L21 (K-major, ld = nb) and U12^T (K-major, written by the LU's copy-back) are
-// brought into shared memory by TMA with 128-byte swizzle, in a two-stage
-// mbarrier pipeline over the nb = 128 contraction (four 32-wide k-blocks).
-// Warp 0 lane 0 issues TMA, warp 1 lane 0 issues tcgen05.mma; all four warps
-// run the epilogue (tcgen05.ld from TMEM, C -= acc in global memory).
+//   warp 0      TMA producer: L21 (K-major, ld = 128) and U12^T (K-major) tiles,
+//               128-byte swizzle, three-stage mbarrier ring over the 128-deep
+//               contraction (four 32-wide k-blocks per tile, continuing across tiles)
+//   warp 1      tcgen05.mma issuer; two TMEM accumulator buffers (Cr | Ci, 256
+//               columns each), so the epilogue of tile i overlaps the MMAs of i+1
+//   warps 2-5   epilogue: tcgen05.ld of a 32-row x 32-column slice, -acc into a
+//               swizzled shared-memory box, and a TMA reduce-add of that box into
+//               A22 (cp.reduce.async.bulk.tensor ... .add): C is never loaded by the SM.
 // Every mbarrier wait has an iteration limit; on expiry the CTA sets
-// FLAG_TIMEOUT, skips the rest of its work, frees its TMEM and exits.
+// FLAG_TIMEOUT, stops issuing work, drains its bulk copies, frees TMEM and exits.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -22,12 +26,17 @@ namespace bem {
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 32, STAGES = 2;
-constexpr int L_TILE = BM * BK * 4;          // 16 KB
-constexpr int U_TILE = BN * BK * 4;          // 32 KB
-constexpr int STAGE_BYTES = 2 * L_TILE + 2 * U_TILE;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr uint32_t TMEM_COLS = 512;          // Cr: cols [0,256), Ci: [256,512)
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, KB = 128 / BK;
+constexpr int L_TILE = BM * BK * 4;                     // 16 KB
+constexpr int U_TILE = BN * BK * 4;                     // 16 KB
+constexpr int STAGE_BYTES = 2 * L_TILE + 2 * U_TILE;    // 64 KB
+constexpr int EPI_WARPS = 4;
+constexpr int SLOT_BYTES = 32 * 32 * 4;                 // one 32 x 32 FP32 box
+constexpr int EPI_BYTES = EPI_WARPS * 2 * SLOT_BYTES;   // 32 KB
+constexpr int BAR_BYTES = 256;
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + EPI_BYTES + BAR_BYTES;
+constexpr int NTHREADS = 64 + 32 * EPI_WARPS;
+constexpr uint32_t TMEM_COLS = 512;                     // 2 buffers x (Cr 128 | Ci 128)
 constexpr long WAIT_LIMIT = 1L << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -39,6 +48,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
@@ -68,6 +80,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
         : "memory");
 }
+// global[box at (x, y)] += shared box (element-wise FP32 add performed by the TMA unit)
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+    asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
 // 8-row core-matrix groups 1024 bytes apart.
@@ -81,7 +102,7 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, K-major, M = 128, N = 256.
+// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, K-major, M = 128, N = 128.
 __host__ __device__ constexpr uint32_t idesc_tf32(bool neg_a) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(BN >> 3) << 17) |
            ((uint32_t)(BM >> 4) << 24);
@@ -117,29 +138,37 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(128, 1)
-    k_tc_trailing(const __grid_constant__ CUtensorMap mapL, const __grid_constant__ CUtensorMap mapU, int n, int M,
-                  int Nc, float* __restrict__ Cr, float* __restrict__ Ci, int ldc, int* gflags) {
+// Tiles (tm, tn), tm < Mt, tn < Nt, of the rectangle whose L21 rows start at lr0
+// (rows of wl) and U12^T rows at ur0 (rows of wut); the tile lands at A rows
+// crow0 + tm*128, columns ccol0 + tn*128.  nplane: row offset of the imaginary
+// planes in the L and U maps.
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_tc_update(const __grid_constant__ CUtensorMap mapL, const __grid_constant__ CUtensorMap mapU,
+                const __grid_constant__ CUtensorMap mapCr, const __grid_constant__ CUtensorMap mapCi, int nplane,
+                int lr0, int ur0, int Mt, int Nt, int crow0, int ccol0, int* gflags) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    // 1024-byte aligned tile area
     const uint32_t raw = smem_u32(smem_raw);
-    const uint32_t base = (raw + 1023u) & ~1023u;
-    unsigned char* tiles = smem_raw + (base - raw);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + STAGES * STAGE_BYTES);  // full[2], empty[2], done
-    volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 8);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 9);
-
+    const uint32_t base = (raw + 1023u) & ~1023u;  // 1024-byte aligned (128-byte swizzle atoms)
+    unsigned char* gbase = smem_raw + (base - raw);
+    const uint32_t epi_base = base + STAGES * STAGE_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES + EPI_BYTES);
+    // bars: full[3] | empty[3] | tfull[2] | tempty[2] | TMEM address | abort flag
+    volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(bars + 10);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 11);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 3);
+    const uint32_t tfull0 = smem_u32(bars + 6), tempty0 = smem_u32(bars + 8);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 2), done = smem_u32(bars + 4);
+    const int ntiles = Mt * Nt;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) { mbar_init(full0 + 8 * s, 1); mbar_init(empty0 + 8 * s, 1); }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(tempty0 + 8 * b, EPI_WARPS); }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapL)) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapU)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapCr)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapCi)) : "memory");
     }
     __syncwarp();
     if (warp == 0) {
@@ -151,78 +180,108 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const int KB = 128 / BK;  // nb = 128
 
-    if (warp == 0 && lane == 0) {
-        // TMA producer
-        for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb % STAGES, use = kb / STAGES;
-            if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, (use - 1) & 1, abort_flag, gflags)) break;
-            const uint32_t st = base + s * STAGE_BYTES;
-            mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-            tma_load_2d(st, &mapL, kb * BK, m0, full0 + 8 * s);
-            tma_load_2d(st + L_TILE, &mapL, kb * BK, n + m0, full0 + 8 * s);
-            tma_load_2d(st + 2 * L_TILE, &mapU, kb * BK, n0, full0 + 8 * s);
-            tma_load_2d(st + 2 * L_TILE + U_TILE, &mapU, kb * BK, n + n0, full0 + 8 * s);
-        }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        const uint32_t id_pos = idesc_tf32(false), id_neg = idesc_tf32(true);
-        const uint32_t accR = tmem, accI = tmem + 256;
-        bool ok = true;
-        for (int kb = 0; kb < KB && ok; ++kb) {
-            const int s = kb % STAGES, use = kb / STAGES;
-            if (!mbar_wait(full0 + 8 * s, use & 1, abort_flag, gflags)) { ok = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t st = base + s * STAGE_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < BK / 8; ++kk) {
-                const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle atom
-                const uint64_t aR = smem_desc_sw128(st + off), aI = smem_desc_sw128(st + L_TILE + off);
-                const uint64_t bR = smem_desc_sw128(st + 2 * L_TILE + off);
-                const uint64_t bI = smem_desc_sw128(st + 2 * L_TILE + U_TILE + off);
-                const uint32_t first = (kb == 0 && kk == 0) ? 0u : 1u;
-                mma_tf32(accR, aR, bR, id_pos, first);
-                mma_tf32(accR, aI, bI, id_neg, 1u);
-                mma_tf32(accI, aR, bI, id_pos, first);
-                mma_tf32(accI, aI, bR, id_pos, 1u);
-            }
-            mma_commit(empty0 + 8 * s);
-        }
-        if (ok) mma_commit(done);
-    }
-    __syncwarp();
-    // Epilogue: all 128 threads; thread owns tile row 32*warp + lane.
-    bool have = mbar_wait(done, 0, abort_flag, gflags);
-    __syncwarp();
-    have = __all_sync(0xffffffffu, have);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (have) {
-        const int row = m0 + warp * 32 + lane;
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-        float vr[32], vi[32];
-        for (int cb = 0; cb < BN / 32; ++cb) {
-            tmem_ld32(tmem + lane_base + cb * 32, vr);
-            tmem_ld32(tmem + lane_base + 256 + cb * 32, vi);
-            const int col = n0 + cb * 32;
-            if (row < M && col < Nc) {
-                float* pr = Cr + (size_t)row * ldc + col;
-                float* pi = Ci + (size_t)row * ldc + col;
-#pragma unroll
-                for (int j = 0; j < 32; j += 4) {
-                    float4 a = *reinterpret_cast<float4*>(pr + j);
-                    float4 b = *reinterpret_cast<float4*>(pi + j);
-                    a.x -= vr[j]; a.y -= vr[j + 1]; a.z -= vr[j + 2]; a.w -= vr[j + 3];
-                    b.x -= vi[j]; b.y -= vi[j + 1]; b.z -= vi[j + 2]; b.w -= vi[j + 3];
-                    *reinterpret_cast<float4*>(pr + j) = a;
-                    *reinterpret_cast<float4*>(pi + j) = b;
+    if (warp == 0) {
+        if (lane == 0) {
+            // TMA producer
+            uint32_t it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int lrow = lr0 + (t / Nt) * BM, urow = ur0 + (t % Nt) * BN;
+                for (int kb = 0; kb < KB; ++kb, ++it) {
+                    const uint32_t s = it % STAGES, u = it / STAGES;
+                    if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
+                    const uint32_t st = base + s * STAGE_BYTES;
+                    mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
+                    tma_load_2d(st, &mapL, kb * BK, lrow, full0 + 8 * s);
+                    tma_load_2d(st + L_TILE, &mapL, kb * BK, nplane + lrow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE, &mapU, kb * BK, urow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE + U_TILE, &mapU, kb * BK, nplane + urow, full0 + 8 * s);
                 }
             }
         }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            const uint32_t id_pos = idesc_tf32(false), id_neg = idesc_tf32(true);
+            uint32_t it = 0, local = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++local) {
+                const uint32_t buf = local & 1, u = local >> 1;
+                if (u > 0 && !mbar_wait(tempty0 + 8 * buf, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t accR = tmem + buf * 256, accI = accR + 128;
+                for (int kb = 0; kb < KB; ++kb, ++it) {
+                    const uint32_t s = it % STAGES, su = it / STAGES;
+                    if (!mbar_wait(full0 + 8 * s, su & 1, abort_flag, gflags)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = base + s * STAGE_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 8; ++kk) {
+                        const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle atom
+                        const uint64_t aR = smem_desc_sw128(st + off), aI = smem_desc_sw128(st + L_TILE + off);
+                        const uint64_t bR = smem_desc_sw128(st + 2 * L_TILE + off);
+                        const uint64_t bI = smem_desc_sw128(st + 2 * L_TILE + U_TILE + off);
+                        const uint32_t first = (kb == 0 && kk == 0) ? 0u : 1u;
+                        mma_tf32(accR, aR, bR, id_pos, first);
+                        mma_tf32(accR, aI, bI, id_neg, 1u);
+                        mma_tf32(accI, aR, bI, id_pos, first);
+                        mma_tf32(accI, aI, bR, id_pos, 1u);
+                    }
+                    mma_commit(empty0 + 8 * s);
+                }
+                if (ok) mma_commit(tfull0 + 8 * buf);
+            }
+        }
+    } else {
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows q*32 + lane.
+        const int q = warp & 3;
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+        const uint32_t slot0 = epi_base + (uint32_t)(warp - 2) * 2 * SLOT_BYTES;
+        uint32_t local = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
+            const int tm = t / Nt, tn = t % Nt;
+            const uint32_t buf = local & 1, u = local >> 1;
+            bool have = mbar_wait(tfull0 + 8 * buf, u & 1, abort_flag, gflags);
+            if (!__all_sync(0xffffffffu, have)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int row = crow0 + tm * BM + q * 32;
+#pragma unroll 1
+            for (int c = 0; c < BN / 32; ++c) {
+#pragma unroll 1
+                for (int p = 0; p < 2; ++p) {
+                    float v[32];
+                    tmem_ld32(tmem + lane_base + buf * 256 + p * 128 + c * 32, v);
+                    const uint32_t slot = slot0 + p * SLOT_BYTES;
+                    if (lane == 0) bulk_wait_read1();  // the previous box from this slot has been read
+                    __syncwarp();
+                    const uint32_t rowaddr = slot + lane * 128;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const uint32_t a = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
+                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(-v[4 * j]),
+                                     "f"(-v[4 * j + 1]), "f"(-v[4 * j + 2]), "f"(-v[4 * j + 3])
+                                     : "memory");
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        tma_reduce_add_2d(p ? &mapCi : &mapCr, ccol0 + tn * BN + c * 32, row, slot);
+                        bulk_commit();
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
+        }
+        if (lane == 0) bulk_wait_all();
+        __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
+        __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
     }
@@ -265,21 +324,57 @@ int tc_gemm_supported(int device) {
     return get_encode() != nullptr ? 1 : 0;
 }
 
-// A22 -= L21 U12 for LU step k0 (nb = 128).  wl = [2][n][128] (L21 rows from 0),
-// wut = [2][n][128] (U12^T rows from 0).
+// FP32 matrix of rows x cols (row stride ld floats), 32 x 32 boxes, 128-byte swizzle:
+// the target of the epilogue's TMA reduce-add.
+static bool make_map_c(CUtensorMap* m, const float* base, int rows, int cols, int ld) {
+    EncodeTiledFn enc = get_encode();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tile rectangle of the step-k0 update (nb = 128): L21 rows [lr0, lr0 + 128 Mt) of
+// wl, U12^T rows [ur0, ur0 + 128 Nt) of wut, landing at A[k0+128+lr0.., k0+128+ur0..].
+// wl = [2][n][128] (L21 rows from 0), wut = [2][n][128] (U12^T rows from 0).
+// max_ctas caps the persistent grid (leaves SMs to a concurrent stream).
+bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags) {
+    if (Mt <= 0 || Nt <= 0) return true;
+    if (n % 128 || k0 % 128 || lr0 % 128 || ur0 % 128 || A.ld % 4) return false;
+    if (k0 + 128 + lr0 + 128 * Mt > n || k0 + 128 + ur0 + 128 * Nt > n) return false;
+    CUtensorMap mL, mU, mCr, mCi;
+    if (!make_map(&mL, wl, n, BM) || !make_map(&mU, wut, n, BN) || !make_map_c(&mCr, A.re, n, n, A.ld) ||
+        !make_map_c(&mCi, A.im, n, n, A.ld))
+        return false;
+    static int attr_done = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_done != dev) {
+        cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        attr_done = dev;
+    }
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int grid = Mt * Nt;
+    if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+    if (grid > nsm) grid = nsm;
+    BEM_LAUNCH(k_tc_update<<<grid, NTHREADS, SMEM_BYTES, st>>>(mL, mU, mCr, mCi, n, lr0, ur0, Mt, Nt, k0 + 128 + lr0,
+                                                              k0 + 128 + ur0, flags));
+    return true;
+}
+
+// A22 -= L21 U12 over the whole trailing matrix of step k0.
 bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
                         int* flags) {
     const int rem = n - k0 - nb;
     if (rem <= 0) return true;
     if (nb != 128) return false;
-    CUtensorMap mL, mU;
-    if (!make_map(&mL, wl, n, BM) || !make_map(&mU, wut, n, BN)) return false;
-    cudaFuncSetAttribute(k_tc_trailing, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    float* Cr = A.re + (size_t)(k0 + nb) * A.ld + k0 + nb;
-    float* Ci = A.im + (size_t)(k0 + nb) * A.ld + k0 + nb;
-    dim3 grid((rem + BN - 1) / BN, rem / BM);
-    BEM_LAUNCH(k_tc_trailing<<<grid, 128, SMEM_BYTES, st>>>(mL, mU, n, rem, rem, Cr, Ci, A.ld, flags));
-    return true;
+    return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags);
 }
 
 }  // namespace bem
