@@ -126,156 +126,142 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 }
 
 // ---------------------------------------------------------------------------
-// 128 x 128 block inverse by 2 x 2 Schur complement, one CTA of 1024 threads:
+// 128 x 128 block inverse by 2 x 2 Schur complement, one CTA of 512 threads:
 //   M = [A B; C E],  S = E - C A^-1 B,
 //   M^-1 = [A^-1 + T S^-1 T2,  -T S^-1;  -S^-1 T2,  S^-1],  T = A^-1 B, T2 = C A^-1.
-// The two 64 x 64 inverses are Gauss-Jordan with the block held in registers
-// (2 x 2 complex per thread, one barrier per pivot); the four 64^3 complex
-// products run from shared memory.  Same flags as k_gj_inv.
-constexpr int IV_LD = 132;  // padded row of the 128 x 128 tile (16-byte aligned)
-constexpr int IV_TD = 68;   // padded row of the 64 x 64 temporary
+// The block sits in shared memory as interleaved complex (float2), rows padded
+// to IV_LD float2 (16-byte aligned, rows four banks apart).  The two 64 x 64
+// inverses are Gauss-Jordan on four warps (128 threads, a named barrier per
+// pivot, each thread holding 32 elements of one row in registers); the four
+// 64^3 complex products use all 512 threads with 2 x 4 outputs per thread.
+// Multipliers |l| > 1 below a pivot inside A or S raise FLAG_PIVOT; a zero or
+// non-finite pivot raises FLAG_ZERO_PIVOT.
+constexpr int IV_LD = 130;   // float2 per row of the 128 x 128 tile
+constexpr int IV_TD = 66;    // float2 per row of the 64 x 64 temporary
+constexpr int IV_THREADS = 512;
 
-// In-place Gauss-Jordan inverse of the 64 x 64 block at (r0, c0) of (Mr, Mi).
-__device__ void iv_gj64(float* Mr, float* Mi, int ld, int r0, int c0, float* rowr, float* rowi, float* colr,
-                        float* coli, int& local_flags) {
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    float vr[2][2], vi[2][2];
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// In-place Gauss-Jordan inverse of the 64 x 64 block at M (row stride ld float2).
+// Threads 0..127 only; thread t owns row t >> 1, columns (t & 1) * 32 .. +31.
+__device__ __noinline__ void iv_gj64(float2* M, int ld, float2* prow, int& lf) {
+    const int t = threadIdx.x, i = t >> 1, h = t & 1, lane = t & 31;
+    float vr[32], vi[32];
+    const float2* mrow = M + i * ld + h * 32;
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+    for (int j = 0; j < 32; ++j) { const float2 v = mrow[j]; vr[j] = v.x; vi[j] = v.y; }
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            vr[a][b] = Mr[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b];
-            vi[a][b] = Mi[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b];
-        }
-    __syncthreads();
     for (int k = 0; k < 64; ++k) {
-        const int buf = k & 1, ka = k >> 5, kt = k & 31;
-        if (ty == kt) {
+        const int kh = k >> 5, kj = k & 31;
+        float2* pr = prow + (k & 1) * 64;
+        if (i == k) {
 #pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                rowr[buf * 64 + tx + 32 * b] = ka ? vr[1][b] : vr[0][b];
-                rowi[buf * 64 + tx + 32 * b] = ka ? vi[1][b] : vi[0][b];
-            }
+            for (int j = 0; j < 32; j += 2)
+                *reinterpret_cast<float4*>(pr + h * 32 + j) = make_float4(vr[j], vi[j], vr[j + 1], vi[j + 1]);
         }
-        if (tx == kt) {
-#pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                colr[buf * 64 + ty + 32 * a] = ka ? vr[a][1] : vr[a][0];
-                coli[buf * 64 + ty + 32 * a] = ka ? vi[a][1] : vi[a][0];
-            }
-        }
-        __syncthreads();
-        const float pr = colr[buf * 64 + k], pi = coli[buf * 64 + k];
-        const float den = pr * pr + pi * pi;
-        if (threadIdx.x == 0 && (!(den > 0.f) || !isfinite(den))) local_flags |= FLAG_ZERO_PIVOT;
-        const float qr = pr / den, qi = -pi / den;
-        float nr[2], ni[2];
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int j = tx + 32 * b;
-            float xr = (j == k) ? 1.f : rowr[buf * 64 + j], xi = (j == k) ? 0.f : rowi[buf * 64 + j];
-            nr[b] = xr * qr - xi * qi;
-            ni[b] = xr * qi + xi * qr;
+        const float cr = __shfl_sync(0xffffffffu, vr[kj], (lane & ~1) | kh);
+        const float ci = __shfl_sync(0xffffffffu, vi[kj], (lane & ~1) | kh);
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        const float2 p = pr[k];
+        const float den = p.x * p.x + p.y * p.y;
+        if (!(den > 0.f) || !isfinite(den)) lf |= FLAG_ZERO_PIVOT;
+        const float qr = p.x / den, qi = -p.y / den;
+        if (h == kh && i > k) {
+            const float lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
+            if (lr * lr + li * li > 1.000002f) lf |= FLAG_PIVOT;
         }
 #pragma unroll
-        for (int a = 0; a < 2; ++a) {
-            const int i = ty + 32 * a;
+        for (int j = 0; j < 32; j += 2) {
+            const float4 r4 = *reinterpret_cast<const float4*>(pr + h * 32 + j);
+            float xr0 = r4.x, xi0 = r4.y, xr1 = r4.z, xi1 = r4.w;
+            if (h * 32 + j == k) { xr0 = 1.f; xi0 = 0.f; }
+            if (h * 32 + j + 1 == k) { xr1 = 1.f; xi1 = 0.f; }
+            const float nr0 = xr0 * qr - xi0 * qi, ni0 = xr0 * qi + xi0 * qr;
+            const float nr1 = xr1 * qr - xi1 * qi, ni1 = xr1 * qi + xi1 * qr;
             if (i == k) {
-#pragma unroll
-                for (int b = 0; b < 2; ++b) { vr[a][b] = nr[b]; vi[a][b] = ni[b]; }
+                vr[j] = nr0; vi[j] = ni0; vr[j + 1] = nr1; vi[j + 1] = ni1;
             } else {
-                const float cr = colr[buf * 64 + i], ci = coli[buf * 64 + i];
-                if (tx == kt && i > k) {
-                    float lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
-                    if (lr * lr + li * li > 1.000002f) local_flags |= FLAG_PIVOT;
-                }
-#pragma unroll
-                for (int b = 0; b < 2; ++b) {
-                    const int j = tx + 32 * b;
-                    if (j == k) {
-                        vr[a][b] = -(cr * nr[b] - ci * ni[b]);
-                        vi[a][b] = -(cr * ni[b] + ci * nr[b]);
-                    } else {
-                        vr[a][b] -= cr * nr[b] - ci * ni[b];
-                        vi[a][b] -= cr * ni[b] + ci * nr[b];
-                    }
-                }
+                if (h * 32 + j == k) { vr[j] = 0.f; vi[j] = 0.f; }
+                if (h * 32 + j + 1 == k) { vr[j + 1] = 0.f; vi[j + 1] = 0.f; }
+                vr[j] -= cr * nr0 - ci * ni0;
+                vi[j] -= cr * ni0 + ci * nr0;
+                vr[j + 1] -= cr * nr1 - ci * ni1;
+                vi[j + 1] -= cr * ni1 + ci * nr1;
             }
         }
     }
-    __syncthreads();
+    float2* orow = M + i * ld + h * 32;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) orow[j] = make_float2(vr[j], vi[j]);
+}
+
+// D (64 x 64) = sgn X Y (mode 0) or D += sgn X Y (mode 1); shared memory,
+// interleaved complex; D must not alias X or Y.  512 threads, thread (tr, tc)
+// owns rows tr, tr+32 and columns tc + 16 m, m = 0..3.
+__device__ void iv_gemm64(float2* D, int ldd, const float2* X, int ldx, const float2* Y, int ldy, float sgn,
+                          int mode) {
+    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;
+    float2 acc[2][4];
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            Mr[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b] = vr[a][b];
-            Mi[(r0 + ty + 32 * a) * ld + c0 + tx + 32 * b] = vi[a][b];
-        }
-    __syncthreads();
-}
-
-// D (64 x 64) = sgn * X Y  (mode 0)  or  D += sgn * X Y  (mode 1); all in shared
-// memory with their own leading dimensions; D must not alias X or Y.
-__device__ void iv_gemm64(float* Dr, float* Di, int ldd, const float* Xr, const float* Xi, int ldx, const float* Yr,
-                          const float* Yi, int ldy, float sgn, int mode) {
-    const int r = threadIdx.x >> 4, c0 = (threadIdx.x & 15) * 4;
-    float ar[4] = {0, 0, 0, 0}, ai[4] = {0, 0, 0, 0};
-#pragma unroll 8
+        for (int m = 0; m < 4; ++m) acc[a][m] = make_float2(0.f, 0.f);
+#pragma unroll 4
     for (int k = 0; k < 64; ++k) {
-        const float xr = Xr[r * ldx + k], xi = Xi[r * ldx + k];
-        const float4 yr = *reinterpret_cast<const float4*>(Yr + k * ldy + c0);
-        const float4 yi = *reinterpret_cast<const float4*>(Yi + k * ldy + c0);
-        const float br[4] = {yr.x, yr.y, yr.z, yr.w}, bi[4] = {yi.x, yi.y, yi.z, yi.w};
+        const float2 x0 = X[tr * ldx + k], x1 = X[(tr + 32) * ldx + k];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            ar[q] = fmaf(xr, br[q], fmaf(-xi, bi[q], ar[q]));
-            ai[q] = fmaf(xr, bi[q], fmaf(xi, br[q], ai[q]));
+        for (int m = 0; m < 4; ++m) {
+            const float2 y = Y[k * ldy + tc + 16 * m];
+            acc[0][m].x = fmaf(x0.x, y.x, fmaf(-x0.y, y.y, acc[0][m].x));
+            acc[0][m].y = fmaf(x0.x, y.y, fmaf(x0.y, y.x, acc[0][m].y));
+            acc[1][m].x = fmaf(x1.x, y.x, fmaf(-x1.y, y.y, acc[1][m].x));
+            acc[1][m].y = fmaf(x1.x, y.y, fmaf(x1.y, y.x, acc[1][m].y));
         }
     }
     __syncthreads();  // every read of X, Y done before D is written
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        float* dr = Dr + r * ldd + c0 + q;
-        float* di = Di + r * ldd + c0 + q;
-        if (mode) { *dr += sgn * ar[q]; *di += sgn * ai[q]; }
-        else { *dr = sgn * ar[q]; *di = sgn * ai[q]; }
-    }
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            float2* d = D + (tr + 32 * a) * ldd + tc + 16 * m;
+            if (mode) { d->x += sgn * acc[a][m].x; d->y += sgn * acc[a][m].y; }
+            else { d->x = sgn * acc[a][m].x; d->y = sgn * acc[a][m].y; }
+        }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_inv128(int k0, CMat<float> A, float* invr, float* invi, int* flags) {
-    extern __shared__ __align__(16) float iv_smem[];
-    float* Mr = iv_smem;                   // [128][IV_LD]
-    float* Mi = Mr + 128 * IV_LD;
-    float* Tr = Mi + 128 * IV_LD;          // [64][IV_TD]
-    float* Ti = Tr + 64 * IV_TD;
-    __shared__ float rowr[128], rowi[128], colr[128], coli[128];
+__global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A, float* invr, float* invi,
+                                                          int* flags) {
+    extern __shared__ __align__(16) float2 iv_smem[];
+    float2* M = iv_smem;                 // [128][IV_LD]
+    float2* T = M + 128 * IV_LD;         // [64][IV_TD]
+    float2* prow = T + 64 * IV_TD;       // [2][64] pivot rows
     for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
-        int i = idx >> 7, j = idx & 127;
-        size_t g = (size_t)(k0 + i) * A.ld + k0 + j;
-        Mr[i * IV_LD + j] = A.re[g];
-        Mi[i * IV_LD + j] = A.im[g];
+        const int i = idx >> 7, j = idx & 127;
+        const size_t g = (size_t)(k0 + i) * A.ld + k0 + j;
+        M[i * IV_LD + j] = make_float2(A.re[g], A.im[g]);
     }
     __syncthreads();
     int lf = 0;
-    float *Ar = Mr, *Ai = Mi;                                   // (0, 0)
-    float *Br = Mr + 64, *Bi = Mi + 64;                         // (0, 64)
-    float *Cr = Mr + 64 * IV_LD, *Ci = Mi + 64 * IV_LD;         // (64, 0)
-    float *Er = Mr + 64 * IV_LD + 64, *Ei = Mi + 64 * IV_LD + 64;  // (64, 64)
-    iv_gj64(Mr, Mi, IV_LD, 0, 0, rowr, rowi, colr, coli, lf);    // A^-1
-    iv_gemm64(Tr, Ti, IV_TD, Ar, Ai, IV_LD, Br, Bi, IV_LD, 1.f, 0);     // T = A^-1 B
-    iv_gemm64(Er, Ei, IV_LD, Cr, Ci, IV_LD, Tr, Ti, IV_TD, -1.f, 1);    // S = E - C T
-    iv_gj64(Mr, Mi, IV_LD, 64, 64, rowr, rowi, colr, coli, lf);  // S^-1
-    iv_gemm64(Br, Bi, IV_LD, Tr, Ti, IV_TD, Er, Ei, IV_LD, -1.f, 0);    // TR = -T S^-1
-    iv_gemm64(Tr, Ti, IV_TD, Cr, Ci, IV_LD, Ar, Ai, IV_LD, 1.f, 0);     // T2 = C A^-1
-    iv_gemm64(Ar, Ai, IV_LD, Br, Bi, IV_LD, Tr, Ti, IV_TD, -1.f, 1);    // TL = A^-1 - TR T2
-    iv_gemm64(Cr, Ci, IV_LD, Er, Ei, IV_LD, Tr, Ti, IV_TD, -1.f, 0);    // BL = -S^-1 T2
+    float2 *Ab = M, *Bb = M + 64, *Cb = M + 64 * IV_LD, *Eb = M + 64 * IV_LD + 64;
+    if (threadIdx.x < 128) iv_gj64(Ab, IV_LD, prow, lf);        // A^-1
+    __syncthreads();
+    iv_gemm64(T, IV_TD, Ab, IV_LD, Bb, IV_LD, 1.f, 0);           // T = A^-1 B
+    iv_gemm64(Eb, IV_LD, Cb, IV_LD, T, IV_TD, -1.f, 1);          // S = E - C T
+    if (threadIdx.x < 128) iv_gj64(Eb, IV_LD, prow, lf);        // S^-1
+    __syncthreads();
+    iv_gemm64(Bb, IV_LD, T, IV_TD, Eb, IV_LD, -1.f, 0);          // TR = -T S^-1
+    iv_gemm64(T, IV_TD, Cb, IV_LD, Ab, IV_LD, 1.f, 0);           // T2 = C A^-1
+    iv_gemm64(Ab, IV_LD, Bb, IV_LD, T, IV_TD, -1.f, 1);          // TL = A^-1 - TR T2
+    iv_gemm64(Cb, IV_LD, Eb, IV_LD, T, IV_TD, -1.f, 0);          // BL = -S^-1 T2
     float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
     float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
     for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
-        int i = idx >> 7, j = idx & 127;
-        Or[idx] = Mr[i * IV_LD + j];
-        Oi[idx] = Mi[i * IV_LD + j];
+        const float2 v = M[(idx >> 7) * IV_LD + (idx & 127)];
+        Or[idx] = v.x;
+        Oi[idx] = v.y;
     }
     if (lf) atomicOr(flags, lf);
 }
@@ -376,12 +362,12 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
     (void)wu;
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
-    constexpr size_t IV_SMEM = sizeof(float) * (2 * 128 * IV_LD + 2 * 64 * IV_TD);
+    constexpr size_t IV_SMEM = sizeof(float2) * (128 * IV_LD + 64 * IV_TD + 2 * 64);
     if (NB == 128 && sizeof(T) == 4)
         cudaFuncSetAttribute(k_inv128, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)IV_SMEM);
     for (int k0 = 0; k0 < n; k0 += NB) {
         if (NB == 128 && sizeof(T) == 4)
-            BEM_LAUNCH(k_inv128<<<1, 1024, IV_SMEM, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
+            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, IV_SMEM, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
                                                         reinterpret_cast<float*>(invr), reinterpret_cast<float*>(invi),
                                                         flags));
         else
