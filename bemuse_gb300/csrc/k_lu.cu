@@ -126,142 +126,120 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 }
 
 // ---------------------------------------------------------------------------
-// 128 x 128 block inverse by 2 x 2 Schur complement, one CTA of 512 threads:
-//   M = [A B; C E],  S = E - C A^-1 B,
-//   M^-1 = [A^-1 + T S^-1 T2,  -T S^-1;  -S^-1 T2,  S^-1],  T = A^-1 B, T2 = C A^-1.
-// The block sits in shared memory as interleaved complex (float2), rows padded
-// to IV_LD float2 (16-byte aligned, rows four banks apart).  The two 64 x 64
-// inverses are Gauss-Jordan on four warps (128 threads, a named barrier per
-// pivot, each thread holding 32 elements of one row in registers); the four
-// 64^3 complex products use all 512 threads with 2 x 4 outputs per thread.
-// Multipliers |l| > 1 below a pivot inside A or S raise FLAG_PIVOT; a zero or
-// non-finite pivot raises FLAG_ZERO_PIVOT.
-constexpr int IV_LD = 130;   // float2 per row of the 128 x 128 tile
-constexpr int IV_TD = 66;    // float2 per row of the 64 x 64 temporary
+// 128 x 128 FP32 block inverse (the tensor-core LU's diagonal blocks), one CTA
+// of 512 threads, Gauss-Jordan without row exchanges, block held in registers:
+// thread (rg, cg) owns rows 4 rg .. 4 rg + 3 and columns 8 cg .. 8 cg + 7.
+// Each pivot step is branch-free.  For pivot k with value p the owners of row k
+// publish n_j = r_j / p, where r is the row with r_k replaced by p + 1, and the
+// owners of column k publish c_i = a_ik with c_k replaced by p - 1; then
+//     a_ij <- a_ij - c_i n_j
+// is exactly the in-place Gauss-Jordan update for every (i, j): for j = k it
+// gives -a_ik / p, for i = k it gives a_kj / p, and a_kk becomes 1 / p.  The
+// p +- 1 substitution costs a factor ~max(1, |p|) in rounding on row and column
+// k, irrelevant for a TF32 preconditioner.  The pivot-row owners (one
+// half-warp) compute 1/p once; everyone else does two shared loads per four
+// elements and the complex multiply-adds.  A zero or non-finite pivot raises
+// FLAG_ZERO_PIVOT.  Multipliers are not checked here: this factorization only
+// preconditions the FP64 refinement, which decides success.
 constexpr int IV_THREADS = 512;
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-
-// In-place Gauss-Jordan inverse of the 64 x 64 block at M (row stride ld float2).
-// Threads 0..127 only; thread t owns row t >> 1, columns (t & 1) * 32 .. +31.
-__device__ __noinline__ void iv_gj64(float2* M, int ld, float2* prow, int& lf) {
-    const int t = threadIdx.x, i = t >> 1, h = t & 1, lane = t & 31;
-    float vr[32], vi[32];
-    const float2* mrow = M + i * ld + h * 32;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) { const float2 v = mrow[j]; vr[j] = v.x; vi[j] = v.y; }
-#pragma unroll
-    for (int k = 0; k < 64; ++k) {
-        const int kh = k >> 5, kj = k & 31;
-        float2* pr = prow + (k & 1) * 64;
-        if (i == k) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2)
-                *reinterpret_cast<float4*>(pr + h * 32 + j) = make_float4(vr[j], vi[j], vr[j + 1], vi[j + 1]);
-        }
-        const float cr = __shfl_sync(0xffffffffu, vr[kj], (lane & ~1) | kh);
-        const float ci = __shfl_sync(0xffffffffu, vi[kj], (lane & ~1) | kh);
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        const float2 p = pr[k];
-        const float den = p.x * p.x + p.y * p.y;
-        if (!(den > 0.f) || !isfinite(den)) lf |= FLAG_ZERO_PIVOT;
-        const float qr = p.x / den, qi = -p.y / den;
-        if (h == kh && i > k) {
-            const float lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
-            if (lr * lr + li * li > 1.000002f) lf |= FLAG_PIVOT;
-        }
-#pragma unroll
-        for (int j = 0; j < 32; j += 2) {
-            const float4 r4 = *reinterpret_cast<const float4*>(pr + h * 32 + j);
-            float xr0 = r4.x, xi0 = r4.y, xr1 = r4.z, xi1 = r4.w;
-            if (h * 32 + j == k) { xr0 = 1.f; xi0 = 0.f; }
-            if (h * 32 + j + 1 == k) { xr1 = 1.f; xi1 = 0.f; }
-            const float nr0 = xr0 * qr - xi0 * qi, ni0 = xr0 * qi + xi0 * qr;
-            const float nr1 = xr1 * qr - xi1 * qi, ni1 = xr1 * qi + xi1 * qr;
-            if (i == k) {
-                vr[j] = nr0; vi[j] = ni0; vr[j + 1] = nr1; vi[j + 1] = ni1;
-            } else {
-                if (h * 32 + j == k) { vr[j] = 0.f; vi[j] = 0.f; }
-                if (h * 32 + j + 1 == k) { vr[j + 1] = 0.f; vi[j + 1] = 0.f; }
-                vr[j] -= cr * nr0 - ci * ni0;
-                vi[j] -= cr * ni0 + ci * nr0;
-                vr[j + 1] -= cr * nr1 - ci * ni1;
-                vi[j + 1] -= cr * ni1 + ci * nr1;
-            }
-        }
-    }
-    float2* orow = M + i * ld + h * 32;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) orow[j] = make_float2(vr[j], vi[j]);
-}
-
-// D (64 x 64) = sgn X Y (mode 0) or D += sgn X Y (mode 1); shared memory,
-// interleaved complex; D must not alias X or Y.  512 threads, thread (tr, tc)
-// owns rows tr, tr+32 and columns tc + 16 m, m = 0..3.
-__device__ void iv_gemm64(float2* D, int ldd, const float2* X, int ldx, const float2* Y, int ldy, float sgn,
-                          int mode) {
-    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;
-    float2 acc[2][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int m = 0; m < 4; ++m) acc[a][m] = make_float2(0.f, 0.f);
-#pragma unroll 4
-    for (int k = 0; k < 64; ++k) {
-        const float2 x0 = X[tr * ldx + k], x1 = X[(tr + 32) * ldx + k];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            const float2 y = Y[k * ldy + tc + 16 * m];
-            acc[0][m].x = fmaf(x0.x, y.x, fmaf(-x0.y, y.y, acc[0][m].x));
-            acc[0][m].y = fmaf(x0.x, y.y, fmaf(x0.y, y.x, acc[0][m].y));
-            acc[1][m].x = fmaf(x1.x, y.x, fmaf(-x1.y, y.y, acc[1][m].x));
-            acc[1][m].y = fmaf(x1.x, y.y, fmaf(x1.y, y.x, acc[1][m].y));
-        }
-    }
-    __syncthreads();  // every read of X, Y done before D is written
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            float2* d = D + (tr + 32 * a) * ldd + tc + 16 * m;
-            if (mode) { d->x += sgn * acc[a][m].x; d->y += sgn * acc[a][m].y; }
-            else { d->x = sgn * acc[a][m].x; d->y = sgn * acc[a][m].y; }
-        }
-    __syncthreads();
-}
 
 __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A, float* invr, float* invi,
                                                           int* flags) {
-    extern __shared__ __align__(16) float2 iv_smem[];
-    float2* M = iv_smem;                 // [128][IV_LD]
-    float2* T = M + 128 * IV_LD;         // [64][IV_TD]
-    float2* prow = T + 64 * IV_TD;       // [2][64] pivot rows
-    for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
-        const int i = idx >> 7, j = idx & 127;
-        const size_t g = (size_t)(k0 + i) * A.ld + k0 + j;
-        M[i * IV_LD + j] = make_float2(A.re[g], A.im[g]);
+    __shared__ __align__(16) float2 nrow[2][128];
+    __shared__ __align__(16) float2 ccol[2][128];
+    const int t = threadIdx.x, cg = t & 15, rg = t >> 4, lane = t & 31;
+    float2 v[4][8];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const size_t g = (size_t)(k0 + 4 * rg + m) * A.ld + k0 + 8 * cg;
+        const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
+        const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
+        const float4 i0 = *reinterpret_cast<const float4*>(A.im + g);
+        const float4 i1 = *reinterpret_cast<const float4*>(A.im + g + 4);
+        v[m][0] = make_float2(r0.x, i0.x); v[m][1] = make_float2(r0.y, i0.y);
+        v[m][2] = make_float2(r0.z, i0.z); v[m][3] = make_float2(r0.w, i0.w);
+        v[m][4] = make_float2(r1.x, i1.x); v[m][5] = make_float2(r1.y, i1.y);
+        v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
     }
-    __syncthreads();
     int lf = 0;
-    float2 *Ab = M, *Bb = M + 64, *Cb = M + 64 * IV_LD, *Eb = M + 64 * IV_LD + 64;
-    if (threadIdx.x < 128) iv_gj64(Ab, IV_LD, prow, lf);        // A^-1
+    // Publish pivot kp (row kp = 4 (kp >> 2) + m1, column kp = 8 (kp >> 3) + c1) into buffer b.
+    auto publish = [&](int kp, int m1, int c1, int b) {
+        const int gr = kp >> 2, gc = kp >> 3;
+        if ((rg >> 1) == (gr >> 1)) {  // the warp holding row kp
+            const float2 pv = v[m1][c1];
+            const int src = (lane & 16) | gc;
+            const float px = __shfl_sync(0xffffffffu, pv.x, src), py = __shfl_sync(0xffffffffu, pv.y, src);
+            if (rg == gr) {
+                const float den = px * px + py * py;
+                if (cg == gc && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
+                const float rc = __frcp_rn(den), qr = px * rc, qi = -py * rc;
+                float o[16];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    float rx = v[m1][c].x, ry = v[m1][c].y;
+                    if (c == c1 && cg == gc) rx = px + 1.f;
+                    o[2 * c] = rx * qr - ry * qi;
+                    o[2 * c + 1] = rx * qi + ry * qr;
+                }
+                float4* dst = reinterpret_cast<float4*>(&nrow[b][8 * cg]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) dst[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+            }
+        }
+        if (cg == gc) {
+            float o[8];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                o[2 * m] = v[m][c1].x - ((m == m1 && rg == gr) ? 1.f : 0.f);
+                o[2 * m + 1] = v[m][c1].y;
+            }
+            float4* dst = reinterpret_cast<float4*>(&ccol[b][4 * rg]);
+            dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+            dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+        }
+    };
+    publish(0, 0, 0, 0);
     __syncthreads();
-    iv_gemm64(T, IV_TD, Ab, IV_LD, Bb, IV_LD, 1.f, 0);           // T = A^-1 B
-    iv_gemm64(Eb, IV_LD, Cb, IV_LD, T, IV_TD, -1.f, 1);          // S = E - C T
-    if (threadIdx.x < 128) iv_gj64(Eb, IV_LD, prow, lf);        // S^-1
-    __syncthreads();
-    iv_gemm64(Bb, IV_LD, T, IV_TD, Eb, IV_LD, -1.f, 0);          // TR = -T S^-1
-    iv_gemm64(T, IV_TD, Cb, IV_LD, Ab, IV_LD, 1.f, 0);           // T2 = C A^-1
-    iv_gemm64(Ab, IV_LD, Bb, IV_LD, T, IV_TD, -1.f, 1);          // TL = A^-1 - TR T2
-    iv_gemm64(Cb, IV_LD, Eb, IV_LD, T, IV_TD, -1.f, 0);          // BL = -S^-1 T2
+#pragma unroll 1
+    for (int kq = 0; kq < 16; ++kq) {
+#pragma unroll
+        for (int kr = 0; kr < 8; ++kr) {
+            const int k = 8 * kq + kr, b = kr & 1;
+            float2 n[8], cm[4];
+            const float4* ns = reinterpret_cast<const float4*>(&nrow[b][8 * cg]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 x = ns[q];
+                n[2 * q] = make_float2(x.x, x.y);
+                n[2 * q + 1] = make_float2(x.z, x.w);
+            }
+            const float4* cs = reinterpret_cast<const float4*>(&ccol[b][4 * rg]);
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float4 x = cs[q];
+                cm[2 * q] = make_float2(x.x, x.y);
+                cm[2 * q + 1] = make_float2(x.z, x.w);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    v[m][c].x = fmaf(-cm[m].x, n[c].x, fmaf(cm[m].y, n[c].y, v[m][c].x));
+                    v[m][c].y = fmaf(-cm[m].x, n[c].y, fmaf(-cm[m].y, n[c].x, v[m][c].y));
+                }
+            if (k < 127) publish(k + 1, (kr + 1) & 3, (kr + 1) & 7, b ^ 1);
+            __syncthreads();
+        }
+    }
     float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
     float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
-    for (int idx = threadIdx.x; idx < 128 * 128; idx += blockDim.x) {
-        const float2 v = M[(idx >> 7) * IV_LD + (idx & 127)];
-        Or[idx] = v.x;
-        Oi[idx] = v.y;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const size_t g = (size_t)(4 * rg + m) * 128 + 8 * cg;
+        *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
+        *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
+        *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
+        *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
     }
     if (lf) atomicOr(flags, lf);
 }
@@ -362,12 +340,9 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
     (void)wu;
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
     T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
-    constexpr size_t IV_SMEM = sizeof(float2) * (128 * IV_LD + 64 * IV_TD + 2 * 64);
-    if (NB == 128 && sizeof(T) == 4)
-        cudaFuncSetAttribute(k_inv128, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)IV_SMEM);
     for (int k0 = 0; k0 < n; k0 += NB) {
         if (NB == 128 && sizeof(T) == 4)
-            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, IV_SMEM, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
+            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
                                                         reinterpret_cast<float*>(invr), reinterpret_cast<float*>(invi),
                                                         flags));
         else
