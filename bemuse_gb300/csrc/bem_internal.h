@@ -79,6 +79,17 @@ int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* 
                   int* flags);
 int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
                   float* wut, int* flags, bool tc);
+// Lookahead schedule for the tensor-core LU: the panel of step k+1 (diagonal-block
+// inverse, W21, U12^T) runs on `panel` (a higher-priority stream) while the main
+// stream applies the rest of step k's trailing update on all but `reserve_sms` SMs.
+struct LuStreams {
+    cudaStream_t panel;
+    cudaEvent_t ev_panel, ev_cross;
+    int reserve_sms;
+};
+// wl2, wut2: two [2][n][128] buffers each (4 n 128 floats).
+int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
+                            float* wl2, float* wut2, int* flags);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place,
 // with an n x R scratch right after X.  ready: n/nb ints zeroed at allocation; epoch
 // strictly increasing across calls on the same ready array (each call uses epoch and

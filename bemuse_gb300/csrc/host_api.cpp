@@ -74,6 +74,8 @@ struct bem_ctx {
     std::vector<void*> allocs;
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
+    cudaStream_t sp = nullptr;                   // panel stream of the lookahead LU (higher priority)
+    cudaEvent_t ev_panel = nullptr, ev_cross = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     long long launches = 0;
 };
@@ -218,9 +220,9 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_D32i, (size_t)Np * Np);
         DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
-        DA(ctx->d_wl32, (size_t)2 * Np * nb32);
+        DA(ctx->d_wl32, (size_t)4 * Np * nb32);  // two [2][Np][128] buffers (lookahead)
         DA(ctx->d_wu32, (size_t)2 * Np * nb32);
-        DA(ctx->d_wut32, (size_t)2 * Np * nb32);
+        DA(ctx->d_wut32, (size_t)4 * Np * nb32);
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
     }
@@ -265,9 +267,16 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
     } else {
         CMat<float> A{ctx->d_D32r, ctx->d_D32i, Np};
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
-        if (bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32, ctx->d_wut32,
-                               ctx->d_flags, tc) != 0)
-            return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
+        int rc_lu;
+        if (tc) {
+            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, 8};
+            rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
+                                                 ctx->d_wut32, ctx->d_flags);
+        } else {
+            rc_lu = bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32,
+                                       ctx->d_wut32, ctx->d_flags, false);
+        }
+        if (rc_lu != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[3], st));
         // x0 = LU^-1 y
@@ -399,6 +408,11 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
     for (auto& ev : ctx->ev) CK(cudaEventCreate(&ev));
+    int prio_lo = 0, prio_hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    CK(cudaStreamCreateWithPriority(&ctx->sp, cudaStreamNonBlocking, prio_hi));
+    CK(cudaEventCreateWithFlags(&ctx->ev_panel, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
     CK(bem::upload_poly_constants(device));
     *out = ctx;
     return BEM_OK;
@@ -409,8 +423,12 @@ void bem_destroy(bem_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_all(ctx);
+    if (ctx->sp) cudaStreamSynchronize(ctx->sp);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
+    if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
+    if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
+    if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }

@@ -22,6 +22,8 @@ namespace bem {
 
 bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
                         int* flags);
+bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -372,6 +374,83 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
             BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, A12, A22, (T)-1, 1));
         }
     }
+    return 0;
+}
+
+// wut[j][i] = A[r0 + i][c0 + j] for i < 128, j < cols (both planes; wut rows of 128 floats).
+__global__ void k_panel_transpose(int cols, CMat<float> A, int r0, int c0, float* wtr, float* wti) {
+    __shared__ float tr[32][33], ti[32][33];
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int j = j0 + threadIdx.x;
+        const size_t g = (size_t)(r0 + i0 + y) * A.ld + c0 + j;
+        tr[y][threadIdx.x] = j < cols ? A.re[g] : 0.f;
+        ti[y][threadIdx.x] = j < cols ? A.im[g] : 0.f;
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int j = j0 + y;
+        if (j < cols) {
+            wtr[(size_t)j * 128 + i0 + threadIdx.x] = tr[threadIdx.x][y];
+            wti[(size_t)j * 128 + i0 + threadIdx.x] = ti[threadIdx.x][y];
+        }
+    }
+}
+
+int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
+                            float* wl2, float* wut2, int* flags) {
+    constexpr int NB = 128;
+    const int nblk = n / NB;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int rest_ctas = std::max(1, nsm - ls.reserve_sms);
+    auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
+    auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };
+    cudaStream_t sp = ls.panel;
+    // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl), U12^T (into wut);
+    // ev_panel marks the operands ready; W21 is then stored into A for the solves.
+    auto panel = [&](int k) {
+        const int k0 = k * NB, rem = n - k0 - NB;
+        BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, flags));
+        float *wlr = wlb(k), *wli = wlb(k) + (size_t)n * NB;
+        if (rem > 0) {
+            CMat<float> Dinv{invr + (size_t)k * NB * NB, invi + (size_t)k * NB * NB, NB};
+            CMat<float> A21{A.re + (size_t)(k0 + NB) * A.ld + k0, A.im + (size_t)(k0 + NB) * A.ld + k0, A.ld};
+            CMat<float> WL{wlr, wli, NB};
+            BEM_LAUNCH(k_cgemm<float><<<dim3(NB / 64, rem / 64), 256, 0, sp>>>(rem, NB, NB, A21, Dinv, WL, 1.0f, 0));
+            float* wtr = wutb(k);
+            BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
+                rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
+        }
+        cudaEventRecord(ls.ev_panel, sp);
+        if (rem > 0) {
+            int nb_ = (int)(((size_t)rem * NB + 255) / 256);
+            if (nb_ > 4096) nb_ = 4096;
+            BEM_LAUNCH(k_copy_back<float><<<nb_, 256, 0, sp>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 0, (float*)nullptr,
+                                                              (float*)nullptr, 0, flags));
+        }
+    };
+    cudaEventRecord(ls.ev_cross, st);
+    cudaStreamWaitEvent(sp, ls.ev_cross, 0);
+    panel(0);
+    for (int k = 0; k < nblk; ++k) {
+        cudaStreamWaitEvent(st, ls.ev_panel, 0);
+        const int k0 = k * NB, rem = n - k0 - NB;
+        if (rem <= 0) break;
+        const int mt = rem / NB;
+        // block column k+1 and block row k+1 first: they are the next panel's input
+        if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, 1, 0, flags)) return 1;
+        if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, NB, 1, mt - 1, 0, flags)) return 1;
+        cudaEventRecord(ls.ev_cross, st);
+        cudaStreamWaitEvent(sp, ls.ev_cross, 0);
+        panel(k + 1);
+        if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags))
+            return 1;
+    }
+    // the last stores of W21 into A precede the solves
+    cudaEventRecord(ls.ev_panel, sp);
+    cudaStreamWaitEvent(st, ls.ev_panel, 0);
     return 0;
 }
 
