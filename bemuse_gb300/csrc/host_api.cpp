@@ -49,7 +49,9 @@ struct bem_ctx {
     float *d_D32r = nullptr, *d_D32i = nullptr;
     float *d_Dhi = nullptr, *d_Dlo = nullptr;   // Re D as float pairs (mixed refinement residual)
     float4* d_Xdf = nullptr;
-    float *d_RShi = nullptr, *d_RSlo = nullptr;  // Rankine source matrix as float pairs (mixed solves)
+    float *d_RShi = nullptr, *d_RSlo = nullptr;  // Rankine matrices as float pairs (mixed solves)
+    float *d_RDhi = nullptr, *d_RDlo = nullptr, *d_RSRhi = nullptr, *d_RSRlo = nullptr;
+    float* d_Bm32 = nullptr;                     // B as floats
     bool rs_df = false;
     double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
     float* d_X32 = nullptr;
@@ -127,7 +129,8 @@ void free_all(bem_ctx* ctx) {
     for (auto p : dp) *p = nullptr;
     float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
                     &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32, &ctx->d_Dhi, &ctx->d_Dlo,
-                    &ctx->d_RShi, &ctx->d_RSlo};
+                    &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi,
+                    &ctx->d_RSRlo, &ctx->d_Bm32};
     ctx->rs_df = false;
     ctx->d_Xdf = nullptr;
     for (auto p : fp) *p = nullptr;
@@ -643,10 +646,17 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         DA(ctx->d_Dhi, (size_t)N * Np);
         DA(ctx->d_Dlo, (size_t)N * Np);
         DA(ctx->d_Xdf, (size_t)N * R);
-        if (NB > 0 && !ctx->rs_df) {
+        DA(ctx->d_Bm32, (size_t)2 * N * R);
+        if (!ctx->rs_df) {
             DA(ctx->d_RShi, (size_t)N * Np);
             DA(ctx->d_RSlo, (size_t)N * Np);
+            DA(ctx->d_RDhi, (size_t)N * Np);
+            DA(ctx->d_RDlo, (size_t)N * Np);
+            DA(ctx->d_RSRhi, (size_t)N * Np);
+            DA(ctx->d_RSRlo, (size_t)N * Np);
             bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RS, ctx->d_RShi, ctx->d_RSlo);
+            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RD, ctx->d_RDhi, ctx->d_RDlo);
+            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RSR, ctx->d_RSRhi, ctx->d_RSRlo);
             ctx->rs_df = true;
         }
     }
@@ -675,6 +685,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         a.Bm = ctx->d_Bm; a.Y = ctx->d_Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
         a.D32r = mixed ? ctx->d_D32r : nullptr; a.D32i = mixed ? ctx->d_D32i : nullptr;
         if (mixed) {
+            bem::launch_to_f32(st, (size_t)2 * N * R, ctx->d_Bm, ctx->d_Bm32);
+            a.Bm32 = ctx->d_Bm32;
+            a.RDhi = ctx->d_RDhi; a.RDlo = ctx->d_RDlo;
+            a.RSRhi = ctx->d_RSRhi; a.RSRlo = ctx->d_RSRlo;
             a.xr32 = ctx->d_xr32;
             a.gq32 = ctx->d_gq32;
             a.Dhi = ctx->d_Dhi;

@@ -218,6 +218,7 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
     const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
     const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
     const float K = (float)a.K;
+    const float Kh = K, Kl = (float)(a.K - (double)K);
     const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
     const float twopi = 6.28318530717959f;
     float acc_re[MAX_RHS], acc_im[MAX_RHS];
@@ -263,19 +264,30 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
             a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
             continue;
         }
-        double dre = a.RD[row + s] + fma(a.RSR[row + s], a.K, (double)wdr);
-        const float hi = (float)dre;
+        // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
+        // FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
+        const float rdh = a.RDhi[row + s], rdl = a.RDlo[row + s];
+        const float rsh = a.RSRhi[row + s], rsl = a.RSRlo[row + s];
+        const float ph = Kh * rsh;
+        const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
+        const float sh = rdh + ph;
+        float bb = sh - rdh;
+        const float se = ((rdh - (sh - bb)) + (ph - bb)) + (rdl + pe);
+        const float th = sh + wdr;
+        bb = th - sh;
+        const float te = ((sh - (th - bb)) + (wdr - bb)) + se;
+        const float hi = th + te;
         a.Dhi[row + s] = hi;
-        a.Dlo[row + s] = (float)(dre - (double)hi);
+        a.Dlo[row + s] = te - (hi - th);
         a.D32r[row + s] = hi;
         a.D32i[row + s] = wdi;
         // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
-        const double* b = a.Bm + (size_t)s * 2 * R;
+        const float* b = a.Bm32 + (size_t)s * 2 * R;
 #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) {
             if (j < R) {
-                acc_re[j] = fmaf(-wsr, (float)b[2 * j], acc_re[j]);
-                acc_im[j] = fmaf(-wsr, (float)b[2 * j + 1], acc_im[j]);
+                acc_re[j] = fmaf(-wsr, b[2 * j], acc_re[j]);
+                acc_im[j] = fmaf(-wsr, b[2 * j + 1], acc_im[j]);
             }
         }
     }
