@@ -49,12 +49,16 @@ cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
                     double* o0, double* o1, double* o2, double* o3);
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
-// Plane-wave factors of the imaginary wave influence (M angles) and the exact
-// FP64 product out += i * scale * Re-part operator applied to Z (k_influence.cu).
+// Plane-wave factors of the imaginary wave influence (M angles, stored as float
+// pairs) and the product out += i * scale * Re-part operator applied to Z, in
+// double-float arithmetic (k_influence.cu).  Zdf: Z split by launch_split_df;
+// T: scratch of 4 M R doubles.
 void launch_pw_build(cudaStream_t st, int N, int M, double K, const double* xr, const double* gq, const int* nq,
-                     double2* E, double2* V, double2* W);
-void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const double2* P, const double2* E,
-                       const double* Z, double2* T, double* out);
+                     float4* E, float4* V, float4* W);
+void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const float4* P, const float4* E,
+                       const float4* Zdf, double* T, double* out);
+// Xdf[r][j] = X[r][j0 + j] (complex, row stride xstride) split into float pairs.
+void launch_split_df(cudaStream_t st, int N, int R, const double* X, int xstride, int j0, float4* Xdf);
 void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i);
 void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,

@@ -65,7 +65,8 @@ struct bem_ctx {
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
     // plane-wave factors of the exact imaginary parts: E, V, W [Mmax][N], T [Mmax][R][2]
-    double2 *d_pwE = nullptr, *d_pwV = nullptr, *d_pwW = nullptr, *d_pwT = nullptr;
+    float4 *d_pwE = nullptr, *d_pwV = nullptr, *d_pwW = nullptr;  // plane-wave factors (float pairs)
+    double* d_pwT = nullptr;
     int pw_Mmax = 0, pw_M = 0;
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
     double pw_K = -1.0;               // wave number the factors were built for
@@ -141,7 +142,8 @@ void free_all(bem_ctx* ctx) {
     ctx->d_norms = nullptr;
     ctx->d_xr32 = nullptr;
     ctx->d_gq32 = nullptr;
-    ctx->d_pwE = ctx->d_pwV = ctx->d_pwW = ctx->d_pwT = nullptr;
+    ctx->d_pwE = ctx->d_pwV = ctx->d_pwW = nullptr;
+    ctx->d_pwT = nullptr;
     ctx->pw_Mmax = ctx->pw_M = 0;
     ctx->pw_K = -1.0;
     ctx->ready = false;
@@ -164,8 +166,8 @@ bem_status pw_prepare(bem_ctx* ctx, double K) {
     if (M > ctx->pw_Mmax) {
         if (ctx->d_pwE) {
             // grow: release the old factor buffers
-            for (double2** p : {&ctx->d_pwE, &ctx->d_pwV, &ctx->d_pwW, &ctx->d_pwT}) {
-                auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), (void*)*p);
+            for (void** p : {(void**)&ctx->d_pwE, (void**)&ctx->d_pwV, (void**)&ctx->d_pwW, (void**)&ctx->d_pwT}) {
+                auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), *p);
                 if (it != ctx->allocs.end()) ctx->allocs.erase(it);
                 cudaFree(*p);
                 *p = nullptr;
@@ -175,7 +177,7 @@ bem_status pw_prepare(bem_ctx* ctx, double K) {
         DA(ctx->d_pwE, (size_t)Mmax * ctx->N);
         DA(ctx->d_pwV, (size_t)Mmax * ctx->N);
         DA(ctx->d_pwW, (size_t)Mmax * ctx->N);
-        DA(ctx->d_pwT, (size_t)Mmax * bem::MAX_RHS * 2);
+        DA(ctx->d_pwT, (size_t)Mmax * bem::MAX_RHS * 4);
         ctx->pw_Mmax = Mmax;
     }
     bem::launch_pw_build(ctx->st, ctx->N, M, K, ctx->d_xr, ctx->d_gq, ctx->d_nq, ctx->d_pwE, ctx->d_pwV, ctx->d_pwW);
@@ -302,7 +304,7 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
                 if (ctx->resid_mode == 3) {
                     const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
                     bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M,
-                                           ctx->d_pwW, ctx->d_pwE, ctx->d_X, ctx->d_pwT, ctx->d_Rr);
+                                           ctx->d_pwW, ctx->d_pwE, ctx->d_Xdf, ctx->d_pwT, ctx->d_Rr);
                 }
             } else {
                 bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0,
@@ -702,8 +704,9 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             s = pw_prepare(ctx, K);
             if (s != BEM_OK) return s;
             const double c1 = K * 0.25 / 3.14159265358979323846;
+            bem::launch_split_df(st, N, R, ctx->d_Bm, R, 0, ctx->d_Xdf);
             bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c1 / ctx->pw_M, ctx->d_pwV,
-                                   ctx->d_pwE, ctx->d_Bm, ctx->d_pwT, ctx->d_Y);
+                                   ctx->d_pwE, ctx->d_Xdf, ctx->d_pwT, ctx->d_Y);
         }
         bem::launch_pad_identity(st, N, Np, mixed ? nullptr : ctx->d_D64r, mixed ? nullptr : ctx->d_D64i,
                                  mixed ? ctx->d_D32r : nullptr, mixed ? ctx->d_D32i : nullptr);

@@ -322,9 +322,15 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
 //   Im wd(r,s) = -(2 pi c2 / M) Re sum_m E_r(m) Wd_s(m),  Wd_s = sum_q w_q (nz + i(cos t nx + sin t ny)) F_q
 // (c1 = K/4pi, c2 = K^2/4pi; Panel.cpp:632-634).  The operator products then
 // cost O(N M R) instead of O(N^2).
+__device__ __forceinline__ float4 df_pack(double re, double im) {
+    const float rh = (float)re, ih = (float)im;
+    return make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+}
+
+// Factors are stored as float pairs per component: float4 = (re hi, re lo, im hi, im lo).
 __global__ void k_pw_build(int N, int M, double K, const double* __restrict__ xr, const double* __restrict__ gq,
-                           const int* __restrict__ nq, double2* __restrict__ E, double2* __restrict__ V,
-                           double2* __restrict__ W) {
+                           const int* __restrict__ nq, float4* __restrict__ E, float4* __restrict__ V,
+                           float4* __restrict__ W) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y;
     if (i >= N) return;
@@ -336,7 +342,7 @@ __global__ void k_pw_build(int N, int M, double K, const double* __restrict__ xr
         double amp = exp(K * xr[2 * N + i]);
         double sp, cp;
         sincos(ph, &sp, &cp);
-        E[(size_t)m * N + i] = make_double2(amp * cp, amp * sp);
+        E[(size_t)m * N + i] = df_pack(amp * cp, amp * sp);
     }
     // source panel i: sums over its Gauss points
     double vr = 0, vi = 0, wr = 0, wi = 0;
@@ -357,81 +363,98 @@ __global__ void k_pw_build(int N, int M, double K, const double* __restrict__ xr
             wi += tr * fi + ti * fr;
         }
     }
-    V[(size_t)m * N + i] = make_double2(vr, vi);
-    W[(size_t)m * N + i] = make_double2(wr, wi);
+    V[(size_t)m * N + i] = df_pack(vr, vi);
+    W[(size_t)m * N + i] = df_pack(wr, wi);
 }
 
-// T1[m][j] = sum_s P_s(m) Z[s][j],  T2[m][j] = sum_s conj(P_s(m)) Z[s][j]   (Z: N x R complex)
-__global__ void __launch_bounds__(256) k_pw_project(int N, int R, const double2* __restrict__ P,
-                                                    const double* __restrict__ Z, double2* __restrict__ T) {
-    const int m = blockIdx.x;
-    __shared__ double red[8][4 * MAX_RHS];
-    double a[4 * MAX_RHS];
+// Double-float helpers: a * b ~ p + e (e from an FMA), (s, c) += p + e with Knuth's two-sum.
+__device__ __forceinline__ void pw_prod(float ah, float al, float bh, float bl, float& p, float& e) {
+    p = ah * bh;
+    e = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -p)));
+}
+__device__ __forceinline__ void pw_acc(float& s, float& c, float p, float e) {
+    const float t = s + p, z = t - s;
+    c += ((s - (t - z)) + (p - z)) + e;
+    s = t;
+}
+
+// T[m][j] += {T1.re, T1.im, T2.re, T2.im} with T1 = sum_s P_s(m) Z[s][j], T2 = sum_s conj(P_s(m)) Z[s][j]
+// (Z: N x R complex as float pairs).  CTA (m, chunk of PW_CHUNK panels); double-float
+// sums per thread, FP64 across the CTA and FP64 atomics across chunks (T zeroed first).
+constexpr int PW_CHUNK = 1024, PW_THREADS = 128;
+
+template <int RR>
+__global__ void __launch_bounds__(PW_THREADS) k_pw_project(int N, const float4* __restrict__ P,
+                                                           const float4* __restrict__ Z, double* __restrict__ T) {
+    extern __shared__ double pw_red[];  // [4 RR][PW_THREADS + 1]
+    const int m = blockIdx.x, s0 = blockIdx.y * PW_CHUNK, t = threadIdx.x;
+    float as[4 * RR], ac[4 * RR];
 #pragma unroll
-    for (int k = 0; k < 4 * MAX_RHS; ++k) a[k] = 0.0;
-    const double2* pm = P + (size_t)m * N;
-    for (int s = threadIdx.x; s < N; s += blockDim.x) {
-        double2 p = pm[s];
-        const double* z = Z + 2 * (size_t)s * R;
+    for (int k = 0; k < 4 * RR; ++k) { as[k] = 0.f; ac[k] = 0.f; }
+    const float4* pm = P + (size_t)m * N;
+    const int s1 = min(N, s0 + PW_CHUNK);
+    for (int s = s0 + t; s < s1; s += PW_THREADS) {
+        const float4 p = pm[s];
+        const float4* z = Z + (size_t)s * RR;
 #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) {
-            if (j < R) {
-                double zr = z[2 * j], zi = z[2 * j + 1];
-                a[4 * j] += p.x * zr - p.y * zi;      // P Z
-                a[4 * j + 1] += p.x * zi + p.y * zr;
-                a[4 * j + 2] += p.x * zr + p.y * zi;  // conj(P) Z
-                a[4 * j + 3] += p.x * zi - p.y * zr;
-            }
+        for (int j = 0; j < RR; ++j) {
+            const float4 zz = z[j];
+            float Ap, Ae, Bp, Be, Cp, Ce, Dp, De;
+            pw_prod(p.x, p.y, zz.x, zz.y, Ap, Ae);  // pr zr
+            pw_prod(p.z, p.w, zz.z, zz.w, Bp, Be);  // pi zi
+            pw_prod(p.x, p.y, zz.z, zz.w, Cp, Ce);  // pr zi
+            pw_prod(p.z, p.w, zz.x, zz.y, Dp, De);  // pi zr
+            pw_acc(as[4 * j], ac[4 * j], Ap, Ae);          // T1.re = pr zr - pi zi
+            pw_acc(as[4 * j], ac[4 * j], -Bp, -Be);
+            pw_acc(as[4 * j + 1], ac[4 * j + 1], Cp, Ce);  // T1.im = pr zi + pi zr
+            pw_acc(as[4 * j + 1], ac[4 * j + 1], Dp, De);
+            pw_acc(as[4 * j + 2], ac[4 * j + 2], Ap, Ae);  // T2.re = pr zr + pi zi
+            pw_acc(as[4 * j + 2], ac[4 * j + 2], Bp, Be);
+            pw_acc(as[4 * j + 3], ac[4 * j + 3], Cp, Ce);  // T2.im = pr zi - pi zr
+            pw_acc(as[4 * j + 3], ac[4 * j + 3], -Dp, -De);
         }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < 4 * MAX_RHS; ++k) {
-        double v = a[k];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) red[warp][k] = v;
-    }
+    for (int k = 0; k < 4 * RR; ++k) pw_red[k * (PW_THREADS + 1) + t] = (double)as[k] + (double)ac[k];
     __syncthreads();
-    for (int k = threadIdx.x; k < 4 * R; k += blockDim.x) {
-        double v = 0;
-        for (int w = 0; w < 8; ++w) v += red[w][k];
-        int j = k / 4, c = k % 4;
-        double* t = reinterpret_cast<double*>(T + ((size_t)m * R + j) * 2);
-        t[c] = v;  // T[m][j] = {T1.re, T1.im, T2.re, T2.im}
+    for (int k = t; k < 4 * RR; k += PW_THREADS) {
+        double v = 0.0;
+        for (int i = 0; i < PW_THREADS; ++i) v += pw_red[k * (PW_THREADS + 1) + i];
+        atomicAdd(T + (size_t)m * RR * 4 + k, v);
     }
 }
 
-// out[r][j] += i * scale * sum_m (E_r(m) T1[m][j] + conj(E_r(m)) T2[m][j])
-__global__ void __launch_bounds__(256) k_pw_apply(int N, int M, int R, double scale, const double2* __restrict__ E,
-                                                  const double2* __restrict__ T, double* __restrict__ out) {
-    extern __shared__ double2 Ts[];  // M * R * 2
-    for (int k = threadIdx.x; k < M * R * 2; k += blockDim.x) Ts[k] = T[k];
+// out[r][j] += i * scale * sum_m (E_r(m) T1[m][j] + conj(E_r(m)) T2[m][j]), one thread per (r, j).
+// With T1 = a + ib, T2 = c + id and E = er + i ei the sum is
+//   er (a + c) + ei (d - b)  +  i (er (b + d) + ei (a - c)),
+// formed per (m, j) once in shared memory as float pairs.
+__global__ void __launch_bounds__(256) k_pw_apply(int N, int M, int R, double scale, const float4* __restrict__ E,
+                                                  const double* __restrict__ T, double* __restrict__ out) {
+    extern __shared__ float4 U[];  // [M * R][2]: (s1 hi, s1 lo, s2 hi, s2 lo), (s3 .., s4 ..)
+    for (int k = threadIdx.x; k < M * R; k += blockDim.x) {
+        const double* tt = T + (size_t)k * 4;
+        const double a = tt[0], b = tt[1], c = tt[2], d = tt[3];
+        U[2 * k] = df_pack(a + c, d - b);
+        U[2 * k + 1] = df_pack(b + d, a - c);
+    }
     __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= N) return;
-    double ar[MAX_RHS], ai[MAX_RHS];
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N * R) return;
+    const int r = idx / R, j = idx % R;
+    float rs = 0.f, rc = 0.f, is = 0.f, ic = 0.f;
     for (int m = 0; m < M; ++m) {
-        double2 e = E[(size_t)m * N + r];
-#pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) {
-            if (j < R) {
-                double2 t1 = Ts[(m * R + j) * 2], t2 = Ts[(m * R + j) * 2 + 1];
-                ar[j] += e.x * t1.x - e.y * t1.y + e.x * t2.x + e.y * t2.y;
-                ai[j] += e.x * t1.y + e.y * t1.x + e.x * t2.y - e.y * t2.x;
-            }
-        }
+        const float4 e = E[(size_t)m * N + r];
+        const float4 u0 = U[2 * (m * R + j)], u1 = U[2 * (m * R + j) + 1];
+        float p, q;
+        pw_prod(e.x, e.y, u0.x, u0.y, p, q); pw_acc(rs, rc, p, q);  // er s1
+        pw_prod(e.z, e.w, u0.z, u0.w, p, q); pw_acc(rs, rc, p, q);  // ei s2
+        pw_prod(e.x, e.y, u1.x, u1.y, p, q); pw_acc(is, ic, p, q);  // er s3
+        pw_prod(e.z, e.w, u1.z, u1.w, p, q); pw_acc(is, ic, p, q);  // ei s4
     }
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) {
-        if (j < R) {
-            // i * scale * (ar + i ai) = -scale ai + i scale ar
-            out[2 * ((size_t)r * R + j)] += -scale * ai[j];
-            out[2 * ((size_t)r * R + j) + 1] += scale * ar[j];
-        }
-    }
+    const double ar = (double)rs + (double)rc, ai = (double)is + (double)ic;
+    // i * scale * (ar + i ai) = -scale ai + i scale ar
+    out[2 * (size_t)idx] += -scale * ai;
+    out[2 * (size_t)idx + 1] += scale * ar;
 }
 
 // Padding rows/columns of the working matrices: identity (so the padded LU
@@ -619,17 +642,44 @@ void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
 }
 
 void launch_pw_build(cudaStream_t st, int N, int M, double K, const double* xr, const double* gq, const int* nq,
-                     double2* E, double2* V, double2* W) {
+                     float4* E, float4* V, float4* W) {
     dim3 grd((N + 127) / 128, M);
     BEM_LAUNCH(k_pw_build<<<grd, 128, 0, st>>>(N, M, K, xr, gq, nq, E, V, W));
 }
 
-void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const double2* P, const double2* E,
-                       const double* Z, double2* T, double* out) {
-    BEM_LAUNCH(k_pw_project<<<M, 256, 0, st>>>(N, R, P, Z, T));
-    size_t smem = sizeof(double2) * (size_t)M * R * 2;
+template <int RR>
+static void pw_project_rr(cudaStream_t st, int N, int M, const float4* P, const float4* Z, double* T) {
+    const size_t smem = sizeof(double) * 4 * RR * (PW_THREADS + 1);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_pw_project<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_pw_project<RR><<<dim3(M, (N + PW_CHUNK - 1) / PW_CHUNK), PW_THREADS, smem, st>>>(N, P, Z, T));
+}
+
+void launch_pw_correct(cudaStream_t st, int N, int M, int R, double scale, const float4* P, const float4* E,
+                       const float4* Zdf, double* T, double* out) {
+    cudaMemsetAsync(T, 0, sizeof(double) * 4 * (size_t)M * R, st);
+    switch (R) {
+        case 1: pw_project_rr<1>(st, N, M, P, Zdf, T); break;
+        case 2: pw_project_rr<2>(st, N, M, P, Zdf, T); break;
+        case 3: pw_project_rr<3>(st, N, M, P, Zdf, T); break;
+        case 4: pw_project_rr<4>(st, N, M, P, Zdf, T); break;
+        case 5: pw_project_rr<5>(st, N, M, P, Zdf, T); break;
+        case 6: pw_project_rr<6>(st, N, M, P, Zdf, T); break;
+        case 7: pw_project_rr<7>(st, N, M, P, Zdf, T); break;
+        case 8: pw_project_rr<8>(st, N, M, P, Zdf, T); break;
+        case 9: pw_project_rr<9>(st, N, M, P, Zdf, T); break;
+        case 10: pw_project_rr<10>(st, N, M, P, Zdf, T); break;
+        case 11: pw_project_rr<11>(st, N, M, P, Zdf, T); break;
+        case 12: pw_project_rr<12>(st, N, M, P, Zdf, T); break;
+        case 13: pw_project_rr<13>(st, N, M, P, Zdf, T); break;
+        case 14: pw_project_rr<14>(st, N, M, P, Zdf, T); break;
+        case 15: pw_project_rr<15>(st, N, M, P, Zdf, T); break;
+        default: pw_project_rr<16>(st, N, M, P, Zdf, T); break;
+    }
+    const size_t smem = sizeof(float4) * 2 * (size_t)M * R;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_pw_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    BEM_LAUNCH(k_pw_apply<<<(N + 255) / 256, 256, smem, st>>>(N, M, R, scale, E, T, out));
+    const int total = N * R;
+    BEM_LAUNCH(k_pw_apply<<<(total + 255) / 256, 256, smem, st>>>(N, M, R, scale, E, T, out));
 }
 
 void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D64i, float* D32r, float* D32i) {

@@ -1221,6 +1221,10 @@ void launch_matx_df(cudaStream_t st, int N, int ld, const float* Mhi, const floa
         N, R, (N + MXD_COLS - 1) / MXD_COLS, part, alpha, beta, base, out, j0, ostride));
 }
 
+void launch_split_df(cudaStream_t st, int N, int R, const double* X, int xstride, int j0, float4* Xdf) {
+    BEM_LAUNCH(k_split_df<<<256, 256, 0, st>>>(N, R, X, xstride, j0, Xdf));
+}
+
 void launch_split_mat_df(cudaStream_t st, size_t n, const double* M, float* hi, float* lo) {
     BEM_LAUNCH(k_split_mat_df<<<1024, 256, 0, st>>>(n, M, hi, lo));
 }

@@ -216,7 +216,13 @@ def main():
     s.Setup(mesh)
     setup_s = time.perf_counter() - t0
     my = OMEGAS[rank::world]
-    seq = [my[i % len(my)] for i in range(args.warmup + args.steps)]
+    # timed steps sample this rank's frequencies evenly over the whole sweep (the
+    # plane-wave angle count, and so the work, grows with frequency)
+    n_my = len(my)
+    timed = [my[(i * n_my) // max(1, args.steps) + (n_my // max(1, args.steps)) // 2] if args.steps <= n_my
+             else my[i % n_my] for i in range(args.steps)]
+    warm = [my[(7 * i + 3) % n_my] for i in range(args.warmup)]
+    seq = warm + timed
     for om in seq[:args.warmup]:
         s.solve_omegas([om])
     s.stage_times(reset=True)
@@ -239,7 +245,14 @@ def main():
     e2e = total / wall_max
     iters = [int(r["iters"][0]) for r in results]
     # plain FP64 GPU path on the first frequencies of this rank, and accuracy of mixed vs plain
-    plain_om = seq[args.warmup:args.warmup + args.plain_steps]
+    # plain FP64 reference at frequencies spread over the timed ones (lowest and highest first)
+    pick = []
+    if args.plain_steps > 0 and args.steps > 0:
+        cand = [0, args.steps - 1] + [(i * args.steps) // max(1, args.plain_steps) for i in range(args.plain_steps)]
+        for c in cand:
+            if c not in pick and len(pick) < min(args.plain_steps, args.steps):
+                pick.append(c)
+    plain_om = [timed[i] for i in pick]
     sp = bg.Hydrodynamic_Radiation_Solver(device=local, precision=bg.PLAIN_FP64)
     sp.Set_Parameters([bg.Parameter("WaveAngle", b) for b in BETAS])
     if plain_om:
@@ -249,7 +262,7 @@ def main():
     t0 = time.perf_counter()
     for i, om in enumerate(plain_om):
         rp = sp.solve_omegas([om])
-        rm = results[i]
+        rm = results[pick[i]]
         errA = max(errA, normwise(rm["A"][0], rp["A"][0]))
         errB = max(errB, normwise(rm["B"][0], rp["B"][0]))
         errF = max(errF, normwise(rm["F"][0], rp["F"][0]))
