@@ -129,8 +129,8 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 
 // ---------------------------------------------------------------------------
 // 128 x 128 FP32 block inverse (the tensor-core LU's diagonal blocks), one CTA
-// of 512 threads, Gauss-Jordan without row exchanges, block held in registers:
-// thread (rg, cg) owns rows 4 rg .. 4 rg + 3 and columns 8 cg .. 8 cg + 7.
+// of 256 threads, Gauss-Jordan without row exchanges, block held in registers:
+// thread (rg, cg) owns rows 8 rg .. 8 rg + 7 and columns 8 cg .. 8 cg + 7.
 // Each pivot step is branch-free.  For pivot k with value p the owners of row k
 // publish n_j = r_j / p, where r is the row with r_k replaced by p + 1, and the
 // owners of column k publish c_i = a_ik with c_k replaced by p - 1; then
@@ -138,22 +138,23 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 // is exactly the in-place Gauss-Jordan update for every (i, j): for j = k it
 // gives -a_ik / p, for i = k it gives a_kj / p, and a_kk becomes 1 / p.  The
 // p +- 1 substitution costs a factor ~max(1, |p|) in rounding on row and column
-// k, irrelevant for a TF32 preconditioner.  The pivot-row owners (one
-// half-warp) compute 1/p once; everyone else does two shared loads per four
-// elements and the complex multiply-adds.  A zero or non-finite pivot raises
+// k, irrelevant for a TF32 preconditioner.  The published row and column are
+// stored chunk-major (16-byte chunk q of thread group g at [q][g]), so the
+// per-pivot shared loads are free of bank conflicts; the pivot-row owners (one
+// half-warp) compute 1/p once.  A zero or non-finite pivot raises
 // FLAG_ZERO_PIVOT.  Multipliers are not checked here: this factorization only
 // preconditions the FP64 refinement, which decides success.
-constexpr int IV_THREADS = 512;
+constexpr int IV_THREADS = 256;
 
 __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A, float* invr, float* invi,
                                                           int* flags) {
-    __shared__ __align__(16) float2 nrow[2][128];
-    __shared__ __align__(16) float2 ccol[2][128];
+    __shared__ __align__(16) float4 nrow[2][4 * 16];  // [buffer][chunk q][column group]
+    __shared__ __align__(16) float4 ccol[2][4 * 16];  // [buffer][chunk q][row group]
     const int t = threadIdx.x, cg = t & 15, rg = t >> 4, lane = t & 31;
-    float2 v[4][8];
+    float2 v[8][8];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const size_t g = (size_t)(k0 + 4 * rg + m) * A.ld + k0 + 8 * cg;
+    for (int m = 0; m < 8; ++m) {
+        const size_t g = (size_t)(k0 + 8 * rg + m) * A.ld + k0 + 8 * cg;
         const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
         const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
         const float4 i0 = *reinterpret_cast<const float4*>(A.im + g);
@@ -164,80 +165,75 @@ __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A,
         v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
     }
     int lf = 0;
-    // Publish pivot kp (row kp = 4 (kp >> 2) + m1, column kp = 8 (kp >> 3) + c1) into buffer b.
-    auto publish = [&](int kp, int m1, int c1, int b) {
-        const int gr = kp >> 2, gc = kp >> 3;
-        if ((rg >> 1) == (gr >> 1)) {  // the warp holding row kp
-            const float2 pv = v[m1][c1];
-            const int src = (lane & 16) | gc;
+    // Publish pivot kp (row and column kp = 8 g + m1, g = kp >> 3) into buffer b.
+    auto publish = [&](int kp, int m1, int b) {
+        const int g = kp >> 3;
+        if ((rg >> 1) == (g >> 1)) {  // the warp holding row kp
+            const float2 pv = v[m1][m1];
+            const int src = ((g & 1) << 4) | g;
             const float px = __shfl_sync(0xffffffffu, pv.x, src), py = __shfl_sync(0xffffffffu, pv.y, src);
-            if (rg == gr) {
+            if (rg == g) {
                 const float den = px * px + py * py;
-                if (cg == gc && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
+                if (cg == g && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
                 const float rc = __frcp_rn(den), qr = px * rc, qi = -py * rc;
                 float o[16];
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                     float rx = v[m1][c].x, ry = v[m1][c].y;
-                    if (c == c1 && cg == gc) rx = px + 1.f;
+                    if (c == m1 && cg == g) rx = px + 1.f;
                     o[2 * c] = rx * qr - ry * qi;
                     o[2 * c + 1] = rx * qi + ry * qr;
                 }
-                float4* dst = reinterpret_cast<float4*>(&nrow[b][8 * cg]);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) dst[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+                for (int q = 0; q < 4; ++q)
+                    nrow[b][q * 16 + cg] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
             }
         }
-        if (cg == gc) {
-            float o[8];
+        if (cg == g) {
+            float o[16];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                o[2 * m] = v[m][c1].x - ((m == m1 && rg == gr) ? 1.f : 0.f);
-                o[2 * m + 1] = v[m][c1].y;
+            for (int m = 0; m < 8; ++m) {
+                o[2 * m] = v[m][m1].x - ((m == m1 && rg == g) ? 1.f : 0.f);
+                o[2 * m + 1] = v[m][m1].y;
             }
-            float4* dst = reinterpret_cast<float4*>(&ccol[b][4 * rg]);
-            dst[0] = make_float4(o[0], o[1], o[2], o[3]);
-            dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                ccol[b][q * 16 + rg] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
         }
     };
-    publish(0, 0, 0, 0);
+    publish(0, 0, 0);
     __syncthreads();
 #pragma unroll 1
     for (int kq = 0; kq < 16; ++kq) {
 #pragma unroll
         for (int kr = 0; kr < 8; ++kr) {
             const int k = 8 * kq + kr, b = kr & 1;
-            float2 n[8], cm[4];
-            const float4* ns = reinterpret_cast<const float4*>(&nrow[b][8 * cg]);
+            float2 n[8], cm[8];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const float4 x = ns[q];
+                const float4 x = nrow[b][q * 16 + cg];
                 n[2 * q] = make_float2(x.x, x.y);
                 n[2 * q + 1] = make_float2(x.z, x.w);
-            }
-            const float4* cs = reinterpret_cast<const float4*>(&ccol[b][4 * rg]);
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const float4 x = cs[q];
-                cm[2 * q] = make_float2(x.x, x.y);
-                cm[2 * q + 1] = make_float2(x.z, x.w);
+                const float4 y = ccol[b][q * 16 + rg];
+                cm[2 * q] = make_float2(y.x, y.y);
+                cm[2 * q + 1] = make_float2(y.z, y.w);
             }
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
+            for (int m = 0; m < 8; ++m)
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                     v[m][c].x = fmaf(-cm[m].x, n[c].x, fmaf(cm[m].y, n[c].y, v[m][c].x));
                     v[m][c].y = fmaf(-cm[m].x, n[c].y, fmaf(-cm[m].y, n[c].x, v[m][c].y));
                 }
-            if (k < 127) publish(k + 1, (kr + 1) & 3, (kr + 1) & 7, b ^ 1);
+            if (k < 127) publish(k + 1, (kr + 1) & 7, b ^ 1);
             __syncthreads();
         }
     }
     float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
     float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const size_t g = (size_t)(4 * rg + m) * 128 + 8 * cg;
+    for (int m = 0; m < 8; ++m) {
+        const size_t g = (size_t)(8 * rg + m) * 128 + 8 * cg;
         *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
         *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
         *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
