@@ -159,6 +159,77 @@ __device__ __forceinline__ float struve_h1_32(float x, float y1x) {
     return __fdividef(c1, c2) + y1x;
 }
 
+// ---- FP32 Bessel functions J0, J1, Y0, Y1 -----------------------------------
+// Polynomial approximations of Abramowitz & Stegun 9.4.1-9.4.6 (E. E. Allen):
+// for 0 < x <= 3 power series in (x/3)^2; for x >= 3 the modulus/phase forms
+//   J_n = x^-1/2 f_n(3/x) cos theta_n,  Y_n = x^-1/2 f_n(3/x) sin theta_n,
+//   theta_0 = x - pi/4 + d_0(3/x),  theta_1 = x - 3 pi/4 + d_1(3/x),
+// absolute errors ~1e-8 (x^-1/2 * 1e-7 for x >= 3).  The large-argument phase is
+// reduced in double-float arithmetic from the argument as a float pair (xh, xl),
+// so the oscillatory far field keeps ~1e-7 relative accuracy for x in the
+// hundreds, where an FP32 argument alone would carry a phase error ~x * 6e-8.
+__device__ __forceinline__ void bessel_j01_small(float x, float& j0, float& j1) {
+    const float y = (x * (1.0f / 3.0f)) * (x * (1.0f / 3.0f));
+    j0 = fmaf(y, fmaf(y, fmaf(y, fmaf(y, fmaf(y, fmaf(y, 0.0002100f, -0.0039444f), 0.0444479f), -0.3163866f),
+                                1.2656208f), -2.2499997f), 1.0f);
+    j1 = x * fmaf(y, fmaf(y, fmaf(y, fmaf(y, fmaf(y, fmaf(y, 0.00001109f, -0.00031761f), 0.00443319f), -0.03954289f),
+                                  0.21093573f), -0.56249985f), 0.5f);
+}
+
+__device__ __forceinline__ void bessel_large(float xh, float xl, float& j0, float& j1, float& y0, float& y1) {
+    const float TWOPI_H = 6.28318548f, TWOPI_L = -1.74845553e-7f;  // 2 pi = H + L
+    const float PI4_H = 0.785398185f, PI4_L = -2.18556949e-8f;     // pi / 4 = H + L
+    const float t = 3.0f * __frcp_rn(xh);
+    const float f0 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00014476f, -0.00072805f), 0.00137237f),
+                                                -0.00009512f), -0.00552740f), -0.00000077f), 0.79788456f);
+    const float d0 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00013558f, -0.00029333f), -0.00054125f),
+                                           0.00262573f), -0.00003954f), -0.04166397f);
+    const float f1 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00020033f, 0.00113653f), -0.00249511f),
+                                                0.00017105f), 0.01659667f), 0.00000156f), 0.79788456f);
+    const float d1 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -0.00029166f, 0.00079824f), 0.00074348f),
+                                           -0.00637879f), 0.00005650f), 0.12499612f);
+    // theta_0 = x - pi/4 + d0 - 2 pi k, as a float pair (ph, pl)
+    const float k = rintf((xh - PI4_H) * 0.159154943f);
+    const float a = fmaf(-k, TWOPI_H, xh);  // exact: |a| < 8 and a is a multiple of ulp(TWOPI_H)
+    const float s = a - PI4_H;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (-PI4_H - bb);
+    float pl = e + (fmaf(-k, TWOPI_L, xl) - PI4_L + d0);
+    const float ph = s + pl;
+    pl -= ph - s;
+    float sn, cs;
+    sincosf(ph, &sn, &cs);
+    const float s0 = fmaf(cs, pl, sn), c0 = fmaf(-sn, pl, cs);  // sin, cos theta_0
+    // theta_1 = theta_0 - pi/2 + (d1 - d0)
+    float se, ce;
+    sincosf(d1 - d0, &se, &ce);
+    const float sa = fmaf(s0, ce, c0 * se);   // sin(theta_0 + d1 - d0) =  cos theta_1
+    const float ca = fmaf(c0, ce, -s0 * se);  // cos(theta_0 + d1 - d0) = -sin theta_1
+    const float rs = rsqrtf(xh);
+    j0 = rs * f0 * c0;
+    y0 = rs * f0 * s0;
+    j1 = rs * f1 * sa;
+    y1 = -rs * f1 * ca;
+}
+
+// Horizontal wave-number distance h = K sqrt(dx^2 + dy^2) as a float pair from
+// coordinate differences given as float pairs (K = kh + kl).
+__device__ __forceinline__ void df_hdist(float dxh, float dxl, float dyh, float dyl, float kh, float kl, float& hh,
+                                         float& hl) {
+    const float p = dxh * dxh, q = dyh * dyh;
+    const float ep = fmaf(dxh, dxh, -p) + 2.0f * dxh * dxl;
+    const float eq = fmaf(dyh, dyh, -q) + 2.0f * dyh * dyl;
+    const float r2 = p + q;
+    const float bb = r2 - p;
+    const float r2l = ((p - (r2 - bb)) + (q - bb)) + (ep + eq);
+    const float rh = sqrtf(r2);
+    const float rl = r2 > 0.0f ? (fmaf(-rh, rh, r2) + r2l) * (0.5f * __frcp_rn(rh)) : 0.0f;
+    const float h = kh * rh;
+    const float h2 = fmaf(kh, rh, -h) + fmaf(kh, rl, kl * rh);
+    hh = h + h2;
+    hl = h2 - (hh - h);
+}
+
 __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf& G, cf& Gh) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
@@ -184,8 +255,9 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
     bool far = hh > 3.0f;
-    float j0v = j0f(hh), j1v = j1f(hh);
-    float y0v = far ? y0f(hh) : 0.0f, y1v = far ? y1f(hh) : 0.0f;
+    float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
+    if (far) bessel_large(hh, 0.0f, j0v, j1v, y0v, y1v);
+    else bessel_j01_small(hh, j0v, j1v);
     float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
     float E = 2.0f * PI * ev;
     G.re = fmaf(E, H0, L0);
@@ -206,7 +278,9 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
 
 // ---- FP32 real parts + imaginary-part remainders ----------------------------
 // Real parts of G and dG/dh (as gf32 computes them).
-__device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float& Gr, float& Ghr) {
+// y0v, y1v: Y0(hh), Y1(hh) (used when hh > 3).
+__device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float y0v, float y1v,
+                                        float& Gr, float& Ghr) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
@@ -229,8 +303,6 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     RR = fmaf(beta * (1.0f - beta), D, RR);
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
-    bool far = hh > 3.0f;
-    float y0v = far ? y0f(hh) : 0.0f, y1v = far ? y1f(hh) : 0.0f;
     float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
     float E = 2.0f * PI * ev;
     Gr = fmaf(E, H0, L0);

@@ -234,16 +234,23 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
         for (int q = 0; q < 4; ++q) {
             if (q < nq) {
                 const float* g = a.gq32 + (size_t)q * N + s;
-                float dx = (xh - g[0]) + (xl - g[7 * fs]);
-                float dy = (yh - g[fs]) + (yl - g[8 * fs]);
+                // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
+                const float gx = g[0], gy = g[fs];
+                const float sx = xh - gx, sy = yh - gy;
+                float bx = sx - xh, by = sy - yh;
+                const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - g[7 * fs]);
+                const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - g[8 * fs]);
                 float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
                 float w = g[3 * fs], nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
-                float XX = dx * K, YY = dy * K, VV = dz * K;
-                float hh = sqrtf(fmaf(XX, XX, YY * YY));
+                float XX = (sx + lx) * K, YY = (sy + ly) * K, VV = dz * K;
+                float hh, hl;
+                df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
                 float ev = expf(VV);
+                float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
+                if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
+                else bessel_j01_small(hh, j0v, j1v);
                 float Gr, Ghr;
-                gf32_re(c_poly32, hh, VV, ev, Gr, Ghr);
-                float j0v = j0f(hh), j1v = j1f(hh);
+                gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr);
                 float proj = fmaf(XX, nx, YY * ny);
                 float dgr = 0.f, dgi = 0.f;
                 if (hh > 1.0e-6f) {
