@@ -83,6 +83,7 @@ def lib():
         "bem_havelock": ([c_int, c_int, _dp, _dp, _dp, c_int, _dp], c_int),
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
+        "bem_kernel_times": ([vp, _dp, c_int], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
         "bem_mesh_wing": ([c_double, c_double, c_double, c_int, c_int, c_int, _dp, _ip], c_int),
@@ -347,6 +348,12 @@ class Hydrodynamic_Radiation_Solver:
     def stage_times(self, reset=False):
         t = np.zeros(6)
         _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
+        return t
+
+    def kernel_times(self, reset=False):
+        """[wave-assembly kernel ms (summed), launches, panel pairs per launch, 0]."""
+        t = np.zeros(4)
+        _check(lib().bem_kernel_times(self._h, _p(t), int(reset)), self._h)
         return t
 
 

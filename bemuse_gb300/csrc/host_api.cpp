@@ -80,6 +80,8 @@ struct bem_ctx {
     cudaStream_t sp = nullptr;                   // panel stream of the lookahead LU (higher priority)
     cudaEvent_t ev_panel = nullptr, ev_cross = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
+    cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
+    double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
 };
 
@@ -418,6 +420,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->sp, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_panel, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
+    for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(bem::upload_poly_constants(device));
     *out = ctx;
     return BEM_OK;
@@ -430,6 +433,8 @@ void bem_destroy(bem_ctx* ctx) {
     free_all(ctx);
     if (ctx->sp) cudaStreamSynchronize(ctx->sp);
     for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto& ev : ctx->ev_wk)
         if (ev) cudaEventDestroy(ev);
     if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
     if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
@@ -698,7 +703,9 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             a.D64r = nullptr;
             a.D64i = nullptr;
         }
+        CK(cudaEventRecord(ctx->ev_wk[0], st));
         bem::launch_wave(st, a, mixed);
+        CK(cudaEventRecord(ctx->ev_wk[1], st));
         if (mixed && K != 0.0) {
             // exact FP64 imaginary part of S applied to B:  Y += -i Im(ws) B
             s = pw_prepare(ctx, K);
@@ -733,6 +740,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         ctx->stage_ms[3] += t_sv;
         cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); ctx->stage_ms[4] += ms;
         ctx->stage_ms[5] += 1;
+        cudaEventElapsedTime(&ms, ctx->ev_wk[0], ctx->ev_wk[1]);
+        ctx->kernel_ms[0] += ms;
+        ctx->kernel_ms[1] += 1;
+        ctx->kernel_ms[2] = (double)N * N;
         // 6x6 algebra (Hydrodynamic_Solver.cpp:463-487)
         if (!out) continue;
         const cplx I(0.0, 1.0);
@@ -999,6 +1010,13 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
 // Stage times (ms, accumulated since the last reset) of bem_solve:
 // [0] incident + static RHS, [1] wave assembly, [2] LU, [3] solve/refine,
 // [4] post, [5] number of frequency-solves.
+bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (out4) memcpy(out4, ctx->kernel_ms, sizeof(ctx->kernel_ms));
+    if (reset) memset(ctx->kernel_ms, 0, sizeof(ctx->kernel_ms));
+    return BEM_OK;
+}
+
 bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
     if (out6) memcpy(out6, ctx->stage_ms, sizeof(ctx->stage_ms));

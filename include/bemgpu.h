@@ -201,6 +201,11 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
  * reset != 0 zeroes the counters after reading. */
 bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
 
+/* Device time of the wave-assembly kernel alone (CUDA events on the solve stream
+ * around its launch): out4[0] milliseconds summed over launches, [1] launches,
+ * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
+bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
+
 /* ---- dense complex solve that allocates nothing --------------------------------
  * This entry point has no counterpart in the reference.  It is the FP64 solve of
  * bem_dense_solve (same kernels, same results) for callers that cannot call
