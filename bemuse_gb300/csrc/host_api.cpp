@@ -29,6 +29,29 @@ using bem::CMat;
 unsigned long long bem::g_launches = 0;
 using cplx = std::complex<double>;
 
+// Per-frequency state of a mixed-precision solve.  Two of them let the
+// assembly of frequency f+1 (on its own stream) overlap the factorization and
+// solves of frequency f; the plain path, the aero path and single-frequency
+// calls use slot 0 only.
+struct FreqState {
+    float *D32r = nullptr, *D32i = nullptr;   // FP32 copy of D, factored in place [Np][Np]
+    float *Dhi = nullptr, *Dlo = nullptr;     // Re D as float pairs [N][Np]
+    float4* Xdf = nullptr;                    // float-pair scratch (N x R)
+    float* Bm32 = nullptr;                    // B as floats
+    double *Bm = nullptr, *Y = nullptr;       // RHS block B and S*B (N x R complex)
+    double *phiI = nullptr, *dphiI = nullptr; // incident potential and its normal derivative (N x NB)
+    double* mx = nullptr;                     // matrix-product partial sums
+    float4 *pwE = nullptr, *pwV = nullptr, *pwW = nullptr;  // plane-wave factors (float pairs) [Mmax][N]
+    double* pwT = nullptr;                    // plane-wave projections [Mmax][R][4]
+    int pw_Mmax = 0, pw_M = 0;
+    double pw_K = -1.0;                       // wave number the factors were built for
+    double Om = 0.0, K = 0.0;                 // frequency held by this slot
+    cudaEvent_t ev_asm = nullptr;             // assembly of this slot done
+    cudaEvent_t ev_free = nullptr;            // solves of this slot done: buffers reusable
+    cudaEvent_t ev_t[4] = {};                 // timing: assembly start, static RHS done, wave kernel start/end
+    cudaEvent_t ev_t5 = nullptr;              // timing: assembly end
+};
+
 struct bem_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
@@ -46,16 +69,12 @@ struct bem_ctx {
     double *d_cen = nullptr, *d_nrm = nullptr, *d_area = nullptr, *d_Nk = nullptr, *d_betas = nullptr;
     double *d_RS = nullptr, *d_RD = nullptr, *d_RSR = nullptr;
     double *d_D64r = nullptr, *d_D64i = nullptr;
-    float *d_D32r = nullptr, *d_D32i = nullptr;
-    float *d_Dhi = nullptr, *d_Dlo = nullptr;   // Re D as float pairs (mixed refinement residual)
-    float4* d_Xdf = nullptr;
     float *d_RShi = nullptr, *d_RSlo = nullptr;  // Rankine matrices as float pairs (mixed solves)
     float *d_RDhi = nullptr, *d_RDlo = nullptr, *d_RSRhi = nullptr, *d_RSRlo = nullptr;
-    float* d_Bm32 = nullptr;                     // B as floats
     bool rs_df = false;
-    double *d_Bm = nullptr, *d_Y = nullptr, *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
+    double *d_Ys6 = nullptr, *d_X = nullptr, *d_Rr = nullptr;
     float* d_X32 = nullptr;
-    double *d_phiI = nullptr, *d_dphiI = nullptr, *d_part = nullptr, *d_post = nullptr, *d_mx = nullptr;
+    double *d_part = nullptr, *d_post = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
     float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
     int* d_flags = nullptr;
@@ -64,16 +83,13 @@ struct bem_ctx {
     unsigned long long* d_norms = nullptr;
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
-    // plane-wave factors of the exact imaginary parts: E, V, W [Mmax][N], T [Mmax][R][2]
-    float4 *d_pwE = nullptr, *d_pwV = nullptr, *d_pwW = nullptr;  // plane-wave factors (float pairs)
-    double* d_pwT = nullptr;
-    int pw_Mmax = 0, pw_M = 0;
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
-    double pw_K = -1.0;               // wave number the factors were built for
     // operator used by the refinement residual: 0 = stored D64 (re, im); 1 = stored
     // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
     // 3 = Re D as float pairs + plane-wave Im D (hydro, K != 0)
     int resid_mode = 0;
+    FreqState fs[2];
+    cudaStream_t sa = nullptr;        // assembly stream of the pipelined mixed path (lowest priority)
     std::vector<void*> allocs;
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
@@ -122,21 +138,28 @@ template <typename T> bem_status dalloc(bem_ctx* ctx, T** p, size_t count) {
         if (s_ != BEM_OK) return s_;                           \
     } while (0)
 
+// Forgets a slot's device buffers (they are owned by ctx->allocs); keeps its events.
+void reset_slot(FreqState& F) {
+    F.D32r = F.D32i = F.Dhi = F.Dlo = F.Bm32 = nullptr;
+    F.Xdf = F.pwE = F.pwV = F.pwW = nullptr;
+    F.Bm = F.Y = F.phiI = F.dphiI = F.mx = F.pwT = nullptr;
+    F.pw_Mmax = F.pw_M = 0;
+    F.pw_K = -1.0;
+}
+
 void free_all(bem_ctx* ctx) {
     for (void* p : ctx->allocs) cudaFree(p);
     ctx->allocs.clear();
     double** dp[] = {&ctx->d_rec, &ctx->d_xr, &ctx->d_gq, &ctx->d_rn, &ctx->d_cen, &ctx->d_nrm, &ctx->d_area,
                      &ctx->d_Nk, &ctx->d_betas, &ctx->d_RS, &ctx->d_RD, &ctx->d_RSR, &ctx->d_D64r, &ctx->d_D64i,
-                     &ctx->d_Bm, &ctx->d_Y, &ctx->d_Ys6, &ctx->d_X, &ctx->d_Rr, &ctx->d_phiI, &ctx->d_dphiI,
-                     &ctx->d_part, &ctx->d_post, &ctx->d_mx, &ctx->d_inv64r, &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
+                     &ctx->d_Ys6, &ctx->d_X, &ctx->d_Rr, &ctx->d_part, &ctx->d_post, &ctx->d_inv64r,
+                     &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
     for (auto p : dp) *p = nullptr;
-    float** fp[] = {&ctx->d_D32r, &ctx->d_D32i, &ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i,
-                    &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32, &ctx->d_Dhi, &ctx->d_Dlo,
-                    &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi,
-                    &ctx->d_RSRlo, &ctx->d_Bm32};
-    ctx->rs_df = false;
-    ctx->d_Xdf = nullptr;
+    float** fp[] = {&ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i, &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32,
+                    &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi, &ctx->d_RSRlo};
     for (auto p : fp) *p = nullptr;
+    for (FreqState& F : ctx->fs) reset_slot(F);
+    ctx->rs_df = false;
     ctx->d_nq = nullptr;
     ctx->d_flags = nullptr;
     ctx->d_ready = nullptr;
@@ -144,10 +167,6 @@ void free_all(bem_ctx* ctx) {
     ctx->d_norms = nullptr;
     ctx->d_xr32 = nullptr;
     ctx->d_gq32 = nullptr;
-    ctx->d_pwE = ctx->d_pwV = ctx->d_pwW = nullptr;
-    ctx->d_pwT = nullptr;
-    ctx->pw_Mmax = ctx->pw_M = 0;
-    ctx->pw_K = -1.0;
     ctx->ready = false;
 }
 
@@ -159,16 +178,16 @@ int pw_angles(double K, double D) {
 }
 
 // Builds (once per wave number) the plane-wave factors E, V, W on the device.
-bem_status pw_prepare(bem_ctx* ctx, double K) {
-    if (ctx->pw_K == K) return BEM_OK;
+bem_status pw_prepare(bem_ctx* ctx, FreqState& F, double K, cudaStream_t st) {
+    if (F.pw_K == K) return BEM_OK;
     const int M = pw_angles(K, ctx->pw_D);
     if ((size_t)M * bem::MAX_RHS * 2 * sizeof(double2) > 220 * 1024)
         return fail(ctx, BEM_ERR_UNSUPPORTED, "K * D too large for the plane-wave imaginary part (M = " +
                                                   std::to_string(M) + " angles)");
-    if (M > ctx->pw_Mmax) {
-        if (ctx->d_pwE) {
+    if (M > F.pw_Mmax) {
+        if (F.pwE) {
             // grow: release the old factor buffers
-            for (void** p : {(void**)&ctx->d_pwE, (void**)&ctx->d_pwV, (void**)&ctx->d_pwW, (void**)&ctx->d_pwT}) {
+            for (void** p : {(void**)&F.pwE, (void**)&F.pwV, (void**)&F.pwW, (void**)&F.pwT}) {
                 auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), *p);
                 if (it != ctx->allocs.end()) ctx->allocs.erase(it);
                 cudaFree(*p);
@@ -176,16 +195,16 @@ bem_status pw_prepare(bem_ctx* ctx, double K) {
             }
         }
         int Mmax = std::max(M, 128);
-        DA(ctx->d_pwE, (size_t)Mmax * ctx->N);
-        DA(ctx->d_pwV, (size_t)Mmax * ctx->N);
-        DA(ctx->d_pwW, (size_t)Mmax * ctx->N);
-        DA(ctx->d_pwT, (size_t)Mmax * bem::MAX_RHS * 4);
-        ctx->pw_Mmax = Mmax;
+        DA(F.pwE, (size_t)Mmax * ctx->N);
+        DA(F.pwV, (size_t)Mmax * ctx->N);
+        DA(F.pwW, (size_t)Mmax * ctx->N);
+        DA(F.pwT, (size_t)Mmax * bem::MAX_RHS * 4);
+        F.pw_Mmax = Mmax;
     }
-    bem::launch_pw_build(ctx->st, ctx->N, M, K, ctx->d_xr, ctx->d_gq, ctx->d_nq, ctx->d_pwE, ctx->d_pwV, ctx->d_pwW);
+    bem::launch_pw_build(st, ctx->N, M, K, ctx->d_xr, ctx->d_gq, ctx->d_nq, F.pwE, F.pwV, F.pwW);
     CK(cudaGetLastError());
-    ctx->pw_M = M;
-    ctx->pw_K = K;
+    F.pw_M = M;
+    F.pw_K = K;
     return BEM_OK;
 }
 
@@ -223,8 +242,8 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_wl64, (size_t)2 * Np * nb64);
         DA(ctx->d_wu64, (size_t)2 * Np * nb64);
     } else {
-        DA(ctx->d_D32r, (size_t)Np * Np);
-        DA(ctx->d_D32i, (size_t)Np * Np);
+        DA(ctx->fs[0].D32r, (size_t)Np * Np);
+        DA(ctx->fs[0].D32i, (size_t)Np * Np);
         DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_wl32, (size_t)4 * Np * nb32);  // two [2][Np][128] buffers (lookahead)
@@ -234,7 +253,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_Rr, (size_t)2 * Np * R);
     }
     DA(ctx->d_X, (size_t)4 * Np * R);
-    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    DA(ctx->fs[0].mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
     DA(ctx->d_flags, 1);
     if (!ctx->d_ready) {
         DA(ctx->d_ready, Np / 16);
@@ -248,7 +267,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
 // Factor + solve.  D64 (planar, ld = Np) holds the operator; Y (N x R, interleaved)
 // the right-hand sides; the solution lands in d_X.  mixed: TF32 LU of the FP32
 // copy + FP64 refinement against D64; plain: FP64 LU of D64 (destroyed).
-bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
+bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
                             double* resid_out, double* t_lu, double* t_solve) {
     cudaStream_t st = ctx->st;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
@@ -263,7 +282,7 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
         bem::lu_factor_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, ctx->d_wl64, ctx->d_wu64, ctx->d_flags);
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[3], st));
-        CK(cudaMemcpyAsync(ctx->d_X, ctx->d_Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(ctx->d_X, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
         bem::launch_pad_rhs(st, N, Np, R, ctx->d_X);
         ctx->solve_epoch += 2;
         if (bem::lu_solve_f64(st, Np, A, ctx->d_inv64r, ctx->d_inv64i, R, ctx->d_X, ctx->d_ready, ctx->solve_epoch - 1,
@@ -272,7 +291,7 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[4], st));
     } else {
-        CMat<float> A{ctx->d_D32r, ctx->d_D32i, Np};
+        CMat<float> A{F.D32r, F.D32i, Np};
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
         int rc_lu;
         if (tc) {
@@ -288,7 +307,7 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
         CK(cudaEventRecord(ctx->ev[3], st));
         // x0 = LU^-1 y
         CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * nr2, st));
-        CK(cudaMemcpyAsync(ctx->d_Rr, ctx->d_Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(ctx->d_Rr, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
         bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
         std::vector<unsigned long long> hn(2 * R);
         for (;;) {
@@ -301,18 +320,18 @@ bem_status factor_and_solve(bem_ctx* ctx, int N, int Np, int R, bool mixed, doub
             CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
             if (ctx->resid_mode >= 2) {
                 // r = y - Re(D) x  (float pairs, double-float products) - i Im(D) x  (plane waves, FP64)
-                bem::launch_matx_df(st, N, Np, ctx->d_Dhi, ctx->d_Dlo, R, ctx->d_X, R, 0, ctx->d_Xdf, ctx->d_mx,
-                                    -1.0, 1.0, ctx->d_Y, ctx->d_Rr, R);
+                bem::launch_matx_df(st, N, Np, F.Dhi, F.Dlo, R, ctx->d_X, R, 0, F.Xdf, F.mx,
+                                    -1.0, 1.0, F.Y, ctx->d_Rr, R);
                 if (ctx->resid_mode == 3) {
-                    const double c2 = ctx->pw_K * ctx->pw_K * 0.25 / 3.14159265358979323846;
-                    bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c2 / ctx->pw_M,
-                                           ctx->d_pwW, ctx->d_pwE, ctx->d_Xdf, ctx->d_pwT, ctx->d_Rr);
+                    const double c2 = F.pw_K * F.pw_K * 0.25 / 3.14159265358979323846;
+                    bem::launch_pw_correct(st, N, F.pw_M, R, 3.14159265358979323846 * c2 / F.pw_M,
+                                           F.pwW, F.pwE, F.Xdf, F.pwT, ctx->d_Rr);
                 }
             } else {
                 bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0,
-                                 ctx->d_X, R, ctx->d_mx, -1.0, 1.0, ctx->d_Y, ctx->d_Rr, R);
+                                 ctx->d_X, R, F.mx, -1.0, 1.0, F.Y, ctx->d_Rr, R);
             }
-            bem::launch_norms(st, N, R, ctx->d_Rr, ctx->d_Y, ctx->d_norms);
+            bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
@@ -413,14 +432,22 @@ bem_status bem_create(bem_ctx** out, int device) {
     ctx = new bem_ctx();
     ctx->device = device;
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
-    for (auto& ev : ctx->ev) CK(cudaEventCreate(&ev));
+    // stream priorities (numerically lower = higher): LU panel > factor/solve > assembly
     int prio_lo = 0, prio_hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    CK(cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
+    for (auto& ev : ctx->ev) CK(cudaEventCreate(&ev));
     CK(cudaStreamCreateWithPriority(&ctx->sp, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_panel, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
+    CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
+    for (FreqState& F : ctx->fs) {
+        CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&F.ev_free, cudaEventDisableTiming));
+        for (auto& ev : F.ev_t) CK(cudaEventCreate(&ev));
+        CK(cudaEventCreate(&F.ev_t5));
+    }
     CK(bem::upload_poly_constants(device));
     *out = ctx;
     return BEM_OK;
@@ -432,6 +459,12 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_all(ctx);
     if (ctx->sp) cudaStreamSynchronize(ctx->sp);
+    if (ctx->sa) cudaStreamSynchronize(ctx->sa);
+    for (FreqState& F : ctx->fs) {
+        for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5})
+            if (e) cudaEventDestroy(e);
+    }
+    if (ctx->sa) cudaStreamDestroy(ctx->sa);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : ctx->ev_wk)
@@ -578,11 +611,11 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_RSR, (size_t)N * Np);
     DA(ctx->d_D64r, (size_t)Np * Np);
     DA(ctx->d_D64i, (size_t)Np * Np);
-    DA(ctx->d_Bm, 2 * (size_t)N * R);
-    DA(ctx->d_Y, 2 * (size_t)N * R);
+    DA(ctx->fs[0].Bm, 2 * (size_t)N * R);
+    DA(ctx->fs[0].Y, 2 * (size_t)N * R);
     DA(ctx->d_Ys6, 2 * (size_t)N * R);
-    DA(ctx->d_phiI, 2 * (size_t)N * std::max(NB, 1));
-    DA(ctx->d_dphiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(ctx->fs[0].phiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(ctx->fs[0].dphiI, 2 * (size_t)N * std::max(NB, 1));
     DA(ctx->d_part, 2 * (size_t)((N + 255) / 256) * (36 + 12 * NB));
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
     DA(ctx->d_xr32, xr32.size());
@@ -604,12 +637,12 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     std::vector<double> B((size_t)2 * N * R, 0.0);
     for (int i = 0; i < N; ++i)
         for (int j = 0; j < 6; ++j) B[2 * ((size_t)i * R + j)] = ctx->Nk[(size_t)i * 6 + j];
-    CK(cudaMemcpyAsync(ctx->d_Bm, B.data(), B.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->fs[0].Bm, B.data(), B.size() * 8, cudaMemcpyHostToDevice, st));
     // K1: Rankine influence (once per body), then Ys6 = RS * N_k
     bem::launch_rankine(st, N, Np, ctx->d_rec, ctx->d_xr, ctx->d_rn, 0, ctx->d_RS, ctx->d_RD, ctx->d_RSR, nullptr);
     CK(cudaGetLastError());
-    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
-    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 6, 0, ctx->d_Bm, R, ctx->d_mx, 1.0, 0.0, nullptr, ctx->d_Ys6, R);
+    DA(ctx->fs[0].mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 6, 0, ctx->fs[0].Bm, R, ctx->fs[0].mx, 1.0, 0.0, nullptr, ctx->d_Ys6, R);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->ready = true;
@@ -635,6 +668,94 @@ bem_status bem_get_body_matrices(const bem_ctx* cctx, double* M, double* C, doub
     return BEM_OK;
 }
 
+namespace {
+
+// Slot buffers of a mixed solve (slot 0's B columns 0-5 come from bem_setup).
+bem_status ensure_slot(bem_ctx* ctx, FreqState& F, bool mixed) {
+    const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R;
+    DA(F.Bm, 2 * (size_t)N * R);
+    DA(F.Y, 2 * (size_t)N * R);
+    DA(F.phiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(F.dphiI, 2 * (size_t)N * std::max(NB, 1));
+    DA(F.mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    if (mixed) {
+        DA(F.D32r, (size_t)Np * Np);
+        DA(F.D32i, (size_t)Np * Np);
+        DA(F.Dhi, (size_t)N * Np);
+        DA(F.Dlo, (size_t)N * Np);
+        DA(F.Xdf, (size_t)N * R);
+        DA(F.Bm32, (size_t)2 * N * R);
+    }
+    if (&F != &ctx->fs[0])  // radiation columns of B (set once by bem_setup)
+        CK(cudaMemcpyAsync(F.Bm, ctx->fs[0].Bm, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice,
+                           ctx->st));
+    return BEM_OK;
+}
+
+// Right-hand sides and operator of one frequency into slot F, on stream st:
+// incident wave, S*B (static Rankine part, wave part), D (FP64, or for the
+// mixed path the FP32 copy plus Re D as float pairs and the plane-wave factors).
+bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStream_t st) {
+    const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R;
+    const double K = Om * Om / 9.81;  // Kappa uses the global Gravity (Hydrodynamic_Solver.cpp:409)
+    F.Om = Om;
+    F.K = K;
+    CK(cudaEventRecord(F.ev_t[0], st));
+    bem::launch_incident(st, N, NB, R, ctx->d_betas, K, Om, ctx->d_cen, ctx->d_nrm, ctx->d_area, F.phiI, F.dphiI,
+                         F.Bm);
+    // Y[:, 0:6] = RS N_k (precomputed); Y[:, 6:] = RS B_diff
+    CK(cudaMemcpy2DAsync(F.Y, sizeof(double) * 2 * R, ctx->d_Ys6, sizeof(double) * 2 * R, sizeof(double) * 2 * 6, N,
+                         cudaMemcpyDeviceToDevice, st));
+    if (NB > 0 && mixed)
+        bem::launch_matx_df(st, N, Np, ctx->d_RShi, ctx->d_RSlo, NB, F.Bm, R, 6, F.Xdf, F.mx, 1.0, 0.0, nullptr, F.Y,
+                            R);
+    else if (NB > 0)
+        bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, NB, 6, F.Bm, R, F.mx, 1.0, 0.0, nullptr, F.Y, R);
+    CK(cudaEventRecord(F.ev_t[1], st));
+    bem::WaveArgs a;
+    memset(&a, 0, sizeof(a));
+    a.N = N; a.ld = Np; a.R = R; a.mode = 0; a.K = K;
+    a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.RD = ctx->d_RD; a.RSR = ctx->d_RSR;
+    a.Bm = F.Bm; a.Y = F.Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
+    if (mixed) {
+        bem::launch_to_f32(st, (size_t)2 * N * R, F.Bm, F.Bm32);
+        a.D32r = F.D32r; a.D32i = F.D32i;
+        a.Bm32 = F.Bm32;
+        a.RDhi = ctx->d_RDhi; a.RDlo = ctx->d_RDlo;
+        a.RSRhi = ctx->d_RSRhi; a.RSRlo = ctx->d_RSRlo;
+        a.xr32 = ctx->d_xr32;
+        a.gq32 = ctx->d_gq32;
+        a.Dhi = F.Dhi;
+        a.Dlo = F.Dlo;
+        a.D64r = nullptr;
+        a.D64i = nullptr;
+    }
+    CK(cudaEventRecord(F.ev_t[2], st));
+    bem::launch_wave(st, a, mixed);
+    CK(cudaEventRecord(F.ev_t[3], st));
+    if (mixed && K != 0.0) {
+        // exact imaginary part of S applied to B:  Y += -i Im(ws) B
+        bem_status s = pw_prepare(ctx, F, K, st);
+        if (s != BEM_OK) return s;
+        const double c1 = K * 0.25 / 3.14159265358979323846;
+        bem::launch_split_df(st, N, R, F.Bm, R, 0, F.Xdf);
+        bem::launch_pw_correct(st, N, F.pw_M, R, 3.14159265358979323846 * c1 / F.pw_M, F.pwV, F.pwE, F.Xdf, F.pwT,
+                               F.Y);
+    }
+    bem::launch_pad_identity(st, N, Np, mixed ? nullptr : ctx->d_D64r, mixed ? nullptr : ctx->d_D64i,
+                             mixed ? F.D32r : nullptr, mixed ? F.D32i : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(F.ev_t5, st));
+    CK(cudaEventRecord(F.ev_asm, st));
+    return BEM_OK;
+}
+
+}  // namespace
+
+// Mixed calls with several frequencies run as a two-stage pipeline: the
+// assembly of frequency f+1 (slot (f+1) & 1, assembly stream, lowest priority)
+// overlaps the factorization and refinement of frequency f (slot f & 1, solve
+// stream).  A slot is reassembled only after its previous solve has finished.
 bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double tol, bem_result* out) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
     if (!ctx->ready || ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_solve before bem_setup");
@@ -649,143 +770,130 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     cudaStream_t st = ctx->st;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
-    if (mixed) {
-        DA(ctx->d_Dhi, (size_t)N * Np);
-        DA(ctx->d_Dlo, (size_t)N * Np);
-        DA(ctx->d_Xdf, (size_t)N * R);
-        DA(ctx->d_Bm32, (size_t)2 * N * R);
-        if (!ctx->rs_df) {
-            DA(ctx->d_RShi, (size_t)N * Np);
-            DA(ctx->d_RSlo, (size_t)N * Np);
-            DA(ctx->d_RDhi, (size_t)N * Np);
-            DA(ctx->d_RDlo, (size_t)N * Np);
-            DA(ctx->d_RSRhi, (size_t)N * Np);
-            DA(ctx->d_RSRlo, (size_t)N * Np);
-            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RS, ctx->d_RShi, ctx->d_RSlo);
-            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RD, ctx->d_RDhi, ctx->d_RDlo);
-            bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RSR, ctx->d_RSRhi, ctx->d_RSRlo);
-            ctx->rs_df = true;
-        }
+    const bool pipe = mixed && n_freq > 1;
+    s = ensure_slot(ctx, ctx->fs[0], mixed);
+    if (s != BEM_OK) return s;
+    if (pipe) {
+        s = ensure_slot(ctx, ctx->fs[1], mixed);
+        if (s != BEM_OK) return s;
     }
+    if (mixed && !ctx->rs_df) {
+        DA(ctx->d_RShi, (size_t)N * Np);
+        DA(ctx->d_RSlo, (size_t)N * Np);
+        DA(ctx->d_RDhi, (size_t)N * Np);
+        DA(ctx->d_RDlo, (size_t)N * Np);
+        DA(ctx->d_RSRhi, (size_t)N * Np);
+        DA(ctx->d_RSRlo, (size_t)N * Np);
+        bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RS, ctx->d_RShi, ctx->d_RSlo);
+        bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RD, ctx->d_RDhi, ctx->d_RDlo);
+        bem::launch_split_mat_df(st, (size_t)N * Np, ctx->d_RSR, ctx->d_RSRhi, ctx->d_RSRlo);
+        ctx->rs_df = true;
+    }
+    cudaStream_t sa = pipe ? ctx->sa : st;
+    if (pipe) {  // the assembly stream starts after everything queued on the solve stream so far
+        CK(cudaEventRecord(ctx->ev[0], st));
+        CK(cudaStreamWaitEvent(sa, ctx->ev[0], 0));
+    }
+    auto slot = [&](int f) -> FreqState& { return ctx->fs[pipe ? (f & 1) : 0]; };
+    auto enqueue_assembly = [&](int f) -> bem_status {
+        FreqState& F = slot(f);
+        if (pipe) CK(cudaStreamWaitEvent(sa, F.ev_free, 0));
+        return assemble(ctx, F, omega[f], mixed, sa);
+    };
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
+    if (n_freq > 0) {
+        s = enqueue_assembly(0);
+        if (s != BEM_OK) return s;
+    }
+    cudaEvent_t span0 = slot(0).ev_t[0];
     for (int f = 0; f < n_freq; ++f) {
+        FreqState& F = slot(f);
         const double Om = omega[f];
-        const double K = Om * Om / 9.81;  // Kappa uses the global Gravity (Hydrodynamic_Solver.cpp:409)
-        CK(cudaEventRecord(ctx->ev[0], st));
-        bem::launch_incident(st, N, NB, R, ctx->d_betas, K, Om, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_phiI,
-                             ctx->d_dphiI, ctx->d_Bm);
-        // Y[:, 0:6] = RS N_k (precomputed); Y[:, 6:] = RS B_diff
-        CK(cudaMemcpy2DAsync(ctx->d_Y, sizeof(double) * 2 * R, ctx->d_Ys6, sizeof(double) * 2 * R,
-                             sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToDevice, st));
-        if (NB > 0 && mixed)
-            bem::launch_matx_df(st, N, Np, ctx->d_RShi, ctx->d_RSlo, NB, ctx->d_Bm, R, 6, ctx->d_Xdf, ctx->d_mx, 1.0,
-                                0.0, nullptr, ctx->d_Y, R);
-        else if (NB > 0)
-            bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, NB, 6, ctx->d_Bm, R, ctx->d_mx, 1.0, 0.0, nullptr,
-                             ctx->d_Y, R);
-        CK(cudaEventRecord(ctx->ev[1], st));
-        bem::WaveArgs a;
-        memset(&a, 0, sizeof(a));
-        a.N = N; a.ld = Np; a.R = R; a.mode = 0; a.K = K;
-        a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.RD = ctx->d_RD; a.RSR = ctx->d_RSR;
-        a.Bm = ctx->d_Bm; a.Y = ctx->d_Y; a.D64r = ctx->d_D64r; a.D64i = ctx->d_D64i;
-        a.D32r = mixed ? ctx->d_D32r : nullptr; a.D32i = mixed ? ctx->d_D32i : nullptr;
-        if (mixed) {
-            bem::launch_to_f32(st, (size_t)2 * N * R, ctx->d_Bm, ctx->d_Bm32);
-            a.Bm32 = ctx->d_Bm32;
-            a.RDhi = ctx->d_RDhi; a.RDlo = ctx->d_RDlo;
-            a.RSRhi = ctx->d_RSRhi; a.RSRlo = ctx->d_RSRlo;
-            a.xr32 = ctx->d_xr32;
-            a.gq32 = ctx->d_gq32;
-            a.Dhi = ctx->d_Dhi;
-            a.Dlo = ctx->d_Dlo;
-            a.D64r = nullptr;
-            a.D64i = nullptr;
-        }
-        CK(cudaEventRecord(ctx->ev_wk[0], st));
-        bem::launch_wave(st, a, mixed);
-        CK(cudaEventRecord(ctx->ev_wk[1], st));
-        if (mixed && K != 0.0) {
-            // exact FP64 imaginary part of S applied to B:  Y += -i Im(ws) B
-            s = pw_prepare(ctx, K);
+        const double K = F.K;
+        if (pipe && f + 1 < n_freq) {
+            s = enqueue_assembly(f + 1);
             if (s != BEM_OK) return s;
-            const double c1 = K * 0.25 / 3.14159265358979323846;
-            bem::launch_split_df(st, N, R, ctx->d_Bm, R, 0, ctx->d_Xdf);
-            bem::launch_pw_correct(st, N, ctx->pw_M, R, 3.14159265358979323846 * c1 / ctx->pw_M, ctx->d_pwV,
-                                   ctx->d_pwE, ctx->d_Xdf, ctx->d_pwT, ctx->d_Y);
+        } else if (!pipe && f > 0) {
+            s = enqueue_assembly(f);
+            if (s != BEM_OK) return s;
         }
-        bem::launch_pad_identity(st, N, Np, mixed ? nullptr : ctx->d_D64r, mixed ? nullptr : ctx->d_D64i,
-                                 mixed ? ctx->d_D32r : nullptr, mixed ? ctx->d_D32i : nullptr);
-        CK(cudaGetLastError());
-        CK(cudaEventRecord(ctx->ev[5], st));
+        if (pipe) CK(cudaStreamWaitEvent(st, F.ev_asm, 0));
         int iters = 0;
         double resid = 0;
         double t_lu = 0, t_sv = 0;
         ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
-        s = factor_and_solve(ctx, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
+        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
         ctx->resid_mode = 0;
-        if (s != BEM_OK) return s;
+        if (s != BEM_OK) {
+            if (pipe) cudaStreamSynchronize(sa);
+            return s;
+        }
         CK(cudaEventRecord(ctx->ev[6], st));
-        bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, ctx->d_phiI, ctx->d_dphiI, ctx->d_part,
-                         ctx->d_post);
+        bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, st));
         CK(cudaEventRecord(ctx->ev[7], st));
+        CK(cudaEventRecord(F.ev_free, st));
         CK(cudaStreamSynchronize(st));
         float ms;
-        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); ctx->stage_ms[0] += ms;
-        cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[5]); ctx->stage_ms[1] += ms;
+        cudaEventElapsedTime(&ms, F.ev_t[0], F.ev_t[1]); ctx->stage_ms[0] += ms;
+        cudaEventElapsedTime(&ms, F.ev_t[1], F.ev_t5); ctx->stage_ms[1] += ms;
         ctx->stage_ms[2] += t_lu;
         ctx->stage_ms[3] += t_sv;
         cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]); ctx->stage_ms[4] += ms;
         ctx->stage_ms[5] += 1;
-        cudaEventElapsedTime(&ms, ctx->ev_wk[0], ctx->ev_wk[1]);
+        cudaEventElapsedTime(&ms, F.ev_t[2], F.ev_t[3]);
         ctx->kernel_ms[0] += ms;
         ctx->kernel_ms[1] += 1;
         ctx->kernel_ms[2] = (double)N * N;
-        // 6x6 algebra (Hydrodynamic_Solver.cpp:463-487)
-        if (!out) continue;
-        const cplx I(0.0, 1.0);
-        cplx AM[36];
-        for (int i = 0; i < 36; ++i) AM[i] = cplx(post[2 * i], post[2 * i + 1]);
-        if (out->A) for (int i = 0; i < 36; ++i) out->A[36 * (size_t)f + i] = AM[i].real();
-        if (out->B) for (int i = 0; i < 36; ++i) out->B[36 * (size_t)f + i] = AM[i].imag();
-        std::vector<cplx> F(6 * (size_t)NB);
-        for (int i = 0; i < 6; ++i)
-            for (int b = 0; b < NB; ++b) {
-                int u = i * NB + b;
-                cplx F1(post[2 * (36 + u)], post[2 * (36 + u) + 1]);
-                cplx F2(post[2 * (36 + 6 * NB + u)], post[2 * (36 + 6 * NB + u) + 1]);
-                cplx FK = -I * Om * F1, SC = I * Om * F2;
-                cplx Fv = std::conj(FK + SC);
-                if (Om == 0.0) { FK = 0; SC = 0; Fv = 0; }
-                size_t o = 2 * ((size_t)f * 6 * NB + u);
-                if (out->FK) { out->FK[o] = FK.real(); out->FK[o + 1] = FK.imag(); }
-                if (out->SC) { out->SC[o] = SC.real(); out->SC[o + 1] = SC.imag(); }
-                if (out->F) { out->F[o] = Fv.real(); out->F[o + 1] = Fv.imag(); }
-                F[u] = Fv;
-            }
-        if (out->RAO) {
-            // B_ijOm := Omega * B_ij (Hydrodynamic_Solver.h:57 declares it but never sets it)
-            cplx L[36], Li[36];
-            for (int i = 0; i < 36; ++i)
-                L[i] = -Om * Om * (AM[i].real() + ctx->M[i] / 1025.0) + Om * I * (Om * AM[i].imag()) +
-                       ctx->C[i] / 1025.0;
-            bool ok = inv6(L, Li);
+        if (f == n_freq - 1) {
+            cudaEventElapsedTime(&ms, span0, ctx->ev[7]);
+            ctx->kernel_ms[3] += ms;  // device span of the whole call
+        }
+        if (out) {
+            // 6x6 algebra (Hydrodynamic_Solver.cpp:463-487)
+            const cplx I(0.0, 1.0);
+            cplx AM[36];
+            for (int i = 0; i < 36; ++i) AM[i] = cplx(post[2 * i], post[2 * i + 1]);
+            if (out->A) for (int i = 0; i < 36; ++i) out->A[36 * (size_t)f + i] = AM[i].real();
+            if (out->B) for (int i = 0; i < 36; ++i) out->B[36 * (size_t)f + i] = AM[i].imag();
+            std::vector<cplx> Fx(6 * (size_t)NB);
             for (int i = 0; i < 6; ++i)
                 for (int b = 0; b < NB; ++b) {
-                    cplx acc(0, 0);
-                    if (ok) for (int k = 0; k < 6; ++k) acc += Li[i * 6 + k] * F[k * NB + b];
-                    else acc = cplx(NAN, NAN);
-                    size_t o = 2 * ((size_t)f * 6 * NB + i * NB + b);
-                    out->RAO[o] = acc.real();
-                    out->RAO[o + 1] = acc.imag();
+                    int u = i * NB + b;
+                    cplx F1(post[2 * (36 + u)], post[2 * (36 + u) + 1]);
+                    cplx F2(post[2 * (36 + 6 * NB + u)], post[2 * (36 + 6 * NB + u) + 1]);
+                    cplx FK = -I * Om * F1, SC = I * Om * F2;
+                    cplx Fv = std::conj(FK + SC);
+                    if (Om == 0.0) { FK = 0; SC = 0; Fv = 0; }
+                    size_t o = 2 * ((size_t)f * 6 * NB + u);
+                    if (out->FK) { out->FK[o] = FK.real(); out->FK[o + 1] = FK.imag(); }
+                    if (out->SC) { out->SC[o] = SC.real(); out->SC[o + 1] = SC.imag(); }
+                    if (out->F) { out->F[o] = Fv.real(); out->F[o + 1] = Fv.imag(); }
+                    Fx[u] = Fv;
                 }
+            if (out->RAO) {
+                // B_ijOm := Omega * B_ij (Hydrodynamic_Solver.h:57 declares it but never sets it)
+                cplx L[36], Li[36];
+                for (int i = 0; i < 36; ++i)
+                    L[i] = -Om * Om * (AM[i].real() + ctx->M[i] / 1025.0) + Om * I * (Om * AM[i].imag()) +
+                           ctx->C[i] / 1025.0;
+                bool ok = inv6(L, Li);
+                for (int i = 0; i < 6; ++i)
+                    for (int b = 0; b < NB; ++b) {
+                        cplx acc(0, 0);
+                        if (ok) for (int k = 0; k < 6; ++k) acc += Li[i * 6 + k] * Fx[k * NB + b];
+                        else acc = cplx(NAN, NAN);
+                        size_t o = 2 * ((size_t)f * 6 * NB + i * NB + b);
+                        out->RAO[o] = acc.real();
+                        out->RAO[o + 1] = acc.imag();
+                    }
+            }
+            if (out->refine_iters) out->refine_iters[f] = mixed ? iters : 0;
+            if (out->residual) out->residual[f] = resid;
         }
-        if (out->refine_iters) out->refine_iters[f] = mixed ? iters : 0;
-        if (out->residual) out->residual[f] = resid;
-        if (f == n_freq - 1) {
+        if (out && f == n_freq - 1) {
             if (out->phi_rad)
                 CK(cudaMemcpy2D(out->phi_rad, sizeof(double) * 2 * 6, ctx->d_X, sizeof(double) * 2 * R,
                                 sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToHost));
@@ -828,7 +936,7 @@ bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, 
     bem::WaveArgs a;
     memset(&a, 0, sizeof(a));
     a.N = N; a.ld = N; a.R = ctx->R; a.mode = 1; a.K = K;
-    a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.Bm = ctx->d_Bm;
+    a.xr = ctx->d_xr; a.gq = ctx->d_gq; a.nq = ctx->d_nq; a.Bm = ctx->fs[0].Bm;
     a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
     a.xr32 = ctx->d_xr32;
     a.gq32 = ctx->d_gq32;
@@ -879,7 +987,7 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
     const bool mixed = precision == BEM_MIXED;
     DA(ctx->d_D64r, (size_t)Np * Np);
     DA(ctx->d_D64i, (size_t)Np * Np);
-    DA(ctx->d_Y, 2 * (size_t)Np * nrhs);
+    DA(ctx->fs[0].Y, 2 * (size_t)Np * nrhs);
     std::vector<double> re((size_t)Np * Np, 0.0), im((size_t)Np * Np, 0.0);
     for (int i = 0; i < Np; ++i)
         for (int j = 0; j < Np; ++j) {
@@ -893,15 +1001,15 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
     cudaStream_t st = ctx->st;
     CK(cudaMemcpyAsync(ctx->d_D64r, re.data(), re.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_D64i, im.data(), im.size() * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(ctx->d_Y, B, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->fs[0].Y, B, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyHostToDevice, st));
     bem_status s = ensure_lu_buffers(ctx, Np, nrhs, mixed);
     if (s != BEM_OK) return s;
     if (mixed) {
-        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->d_D32r);
-        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64i, ctx->d_D32i);
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->fs[0].D32r);
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64i, ctx->fs[0].D32i);
     }
     double t0 = 0, t1 = 0;
-    s = factor_and_solve(ctx, n, Np, nrhs, mixed, tol, 60, iters, resid, &t0, &t1);
+    s = factor_and_solve(ctx, ctx->fs[0], n, Np, nrhs, mixed, tol, 60, iters, resid, &t0, &t1);
     if (s != BEM_OK) { free_all(ctx); return s; }
     cudaError_t e = cudaMemcpyAsync(B, ctx->d_X, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -949,9 +1057,9 @@ bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh) {
     DA(ctx->d_RD, (size_t)N * Np);
     DA(ctx->d_D64r, (size_t)Np * Np);
     DA(ctx->d_D64i, (size_t)Np * Np);
-    DA(ctx->d_Bm, 2 * (size_t)N);
-    DA(ctx->d_Y, 2 * (size_t)N);
-    DA(ctx->d_mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
+    DA(ctx->fs[0].Bm, 2 * (size_t)N);
+    DA(ctx->fs[0].Y, 2 * (size_t)N);
+    DA(ctx->fs[0].mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
     cudaStream_t st = ctx->st;
     CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
@@ -983,21 +1091,21 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
     cudaStream_t st = ctx->st;
     bem_status s = ensure_lu_buffers(ctx, Np, 1, mixed);
     if (s != BEM_OK) return s;
-    CK(cudaMemcpyAsync(ctx->d_Bm, bcz.data(), bcz.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->fs[0].Bm, bcz.data(), bcz.size() * 8, cudaMemcpyHostToDevice, st));
     // Solve_Steady (:169-180): S = G BC, X = H^-1 S
-    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 1, 0, ctx->d_Bm, 1, ctx->d_mx, 1.0, 0.0, nullptr, ctx->d_Y, 1);
+    bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 1, 0, ctx->fs[0].Bm, 1, ctx->fs[0].mx, 1.0, 0.0, nullptr, ctx->fs[0].Y, 1);
     CK(cudaMemcpyAsync(ctx->d_D64r, ctx->d_RD, sizeof(double) * (size_t)N * Np, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(ctx->d_D64i, 0, sizeof(double) * (size_t)Np * Np, st));
     bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, nullptr, nullptr);
     if (mixed) {
-        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->d_D32r);
-        CK(cudaMemsetAsync(ctx->d_D32i, 0, sizeof(float) * (size_t)Np * Np, st));
+        bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64r, ctx->fs[0].D32r);
+        CK(cudaMemsetAsync(ctx->fs[0].D32i, 0, sizeof(float) * (size_t)Np * Np, st));
     }
     CK(cudaGetLastError());
     int iters = 0;
     double resid = 0, t0 = 0, t1 = 0;
     ctx->resid_mode = mixed ? 1 : 0;
-    s = factor_and_solve(ctx, N, Np, 1, mixed, tol, 60, &iters, &resid, &t0, &t1);
+    s = factor_and_solve(ctx, ctx->fs[0], N, Np, 1, mixed, tol, 60, &iters, &resid, &t0, &t1);
     ctx->resid_mode = 0;
     if (s != BEM_OK) return s;
     std::vector<double> x(2 * (size_t)N);
