@@ -97,6 +97,7 @@ struct bem_ctx {
     cudaEvent_t ev_panel = nullptr, ev_cross = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
+    cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
 };
@@ -441,6 +442,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaEventCreateWithFlags(&ctx->ev_panel, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
+    CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
     for (FreqState& F : ctx->fs) {
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
@@ -469,6 +471,7 @@ void bem_destroy(bem_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : ctx->ev_wk)
         if (ev) cudaEventDestroy(ev);
+    if (ctx->ev_call) cudaEventDestroy(ctx->ev_call);
     if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
     if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
@@ -790,10 +793,8 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         ctx->rs_df = true;
     }
     cudaStream_t sa = pipe ? ctx->sa : st;
-    if (pipe) {  // the assembly stream starts after everything queued on the solve stream so far
-        CK(cudaEventRecord(ctx->ev[0], st));
-        CK(cudaStreamWaitEvent(sa, ctx->ev[0], 0));
-    }
+    CK(cudaEventRecord(ctx->ev_call, st));
+    if (pipe) CK(cudaStreamWaitEvent(sa, ctx->ev_call, 0));  // assembly starts after the work queued so far
     auto slot = [&](int f) -> FreqState& { return ctx->fs[pipe ? (f & 1) : 0]; };
     auto enqueue_assembly = [&](int f) -> bem_status {
         FreqState& F = slot(f);
@@ -806,7 +807,6 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         s = enqueue_assembly(0);
         if (s != BEM_OK) return s;
     }
-    cudaEvent_t span0 = slot(0).ev_t[0];
     for (int f = 0; f < n_freq; ++f) {
         FreqState& F = slot(f);
         const double Om = omega[f];
@@ -848,7 +848,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         ctx->kernel_ms[1] += 1;
         ctx->kernel_ms[2] = (double)N * N;
         if (f == n_freq - 1) {
-            cudaEventElapsedTime(&ms, span0, ctx->ev[7]);
+            cudaEventElapsedTime(&ms, ctx->ev_call, ctx->ev[7]);
             ctx->kernel_ms[3] += ms;  // device span of the whole call
         }
         if (out) {
