@@ -46,6 +46,12 @@ class _Props(ctypes.Structure):
                 ("mass_matrix", _dp), ("stiffness", _dp), ("aux", ctypes.POINTER(_Mesh))]
 
 
+class _WamitInfo(ctypes.Structure):
+    _fields_ = [("n_beta", ctypes.c_int), ("betas", _dp), ("rho", ctypes.c_double), ("gravity", ctypes.c_double),
+                ("M", ctypes.c_double * 36), ("C", ctypes.c_double * 36), ("volume", ctypes.c_double),
+                ("cob", ctypes.c_double * 3), ("cog", ctypes.c_double * 3)]
+
+
 class _Result(ctypes.Structure):
     _fields_ = [("A", _dp), ("B", _dp), ("FK", _dp), ("SC", _dp), ("F", _dp), ("RAO", _dp),
                 ("refine_iters", _ip), ("residual", _dp), ("phi_rad", _dp), ("phi_scat", _dp)]
@@ -84,6 +90,7 @@ def lib():
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
         "bem_kernel_times": ([vp, _dp, c_int], c_int),
+        "bem_write_wamit": ([ctypes.c_char_p, ctypes.POINTER(_WamitInfo), c_int, _dp, ctypes.POINTER(_Result)], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
         "bem_mesh_wing": ([c_double, c_double, c_double, c_int, c_int, c_int, _dp, _ip], c_int),
@@ -215,6 +222,32 @@ def unify(meshes, origins):
     return Mesh(np.concatenate(nodes), np.concatenate(elems), first, org, aux=aux)
 
 
+def write_wamit(prefix, omegas, out, betas, M, C, volume, cob, cog, rho=1025.0, gravity=9.81):
+    """WAMIT-format result files (.1 .2 .2fk .2sc .4 .hst .mmx) as the reference's
+    Generate/Update_Output_File_WAMIT write them (Hydrodynamic_Solver_IO.cpp:430-646).
+    omegas are the internal angular frequencies; out holds A, B (nf x 6 x 6) and
+    FK, SC, F, RAO (nf x 6 x nb complex)."""
+    om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
+    betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
+    info = _WamitInfo()
+    info.n_beta = betas.size
+    info.betas = _p(betas)
+    info.rho, info.gravity, info.volume = float(rho), float(gravity), float(volume)
+    info.M[:] = list(np.asarray(M, dtype=np.float64).ravel())
+    info.C[:] = list(np.asarray(C, dtype=np.float64).ravel())
+    info.cob[:] = list(np.asarray(cob, dtype=np.float64).ravel())
+    info.cog[:] = list(np.asarray(cog, dtype=np.float64).ravel())
+    keep = {k: np.ascontiguousarray(out[k]) for k in ("A", "B", "FK", "SC", "F", "RAO") if k in out}
+    res = _Result()
+    res.A = _p(keep["A"]) if "A" in keep else None
+    res.B = _p(keep["B"]) if "B" in keep else None
+    for k in ("FK", "SC", "F", "RAO"):
+        setattr(res, k, _p(keep[k].view(np.float64)) if k in keep else None)
+    rc = lib().bem_write_wamit(str(prefix).encode(), ctypes.byref(info), om.size, _p(om), ctypes.byref(res))
+    if rc != 0:
+        raise BEMError("bem_write_wamit failed (status %d)" % rc)
+
+
 class Hydrodynamic_Radiation_Solver:
     """Drop-in for BEMUse::Hydrodynamic_Radiation_Solver (Hydrodynamic_Solver.h:35-160).
 
@@ -296,6 +329,11 @@ class Hydrodynamic_Radiation_Solver:
         _check(lib().bem_get_body_matrices(self._h, _p(M), _p(C), _p(vc)), self._h)
         self.M_ij, self.C_ij = M, C
         self.Volume, self.Centre_Buoyancy = vc[0], vc[1:]
+
+    def write_wamit(self, prefix, omegas, out):
+        """Result files of solve_omegas(omegas) in the reference's WAMIT formats."""
+        write_wamit(prefix, omegas, out, self.BetaArray, self.M_ij, self.C_ij,
+                    self.Volume, self.Centre_Buoyancy, self.cog, rho=self.Rho, gravity=self.Grav)
 
     def Set_Real(self, D):
         self.Frequency = float(D)

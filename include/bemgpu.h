@@ -95,6 +95,19 @@ typedef struct {
     double* phi_scat;
 } bem_result;
 
+/* Body and environment data for the result files (host only). */
+typedef struct {
+    int n_beta;
+    const double* betas;   /* headings [rad] */
+    double rho;            /* the solver's Density parameter */
+    double gravity;        /* the solver's Gravity parameter (printed in .mmx) */
+    double M[36];          /* mass matrix, row-major (bem_get_body_matrices) */
+    double C[36];          /* hydrostatic stiffness, row-major */
+    double volume;         /* displaced volume */
+    double cob[3];         /* centre of buoyancy */
+    double cog[3];         /* centre of gravity */
+} bem_wamit_info;
+
 /* ---- mesh generators (host only; no device needed) ------------------------ */
 
 /* Half_Cylinder (Volume_of_Revolution.cpp:167-199, 12-41, 92-130): radius R,
@@ -205,6 +218,17 @@ bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
  * around its launch): out4[0] milliseconds summed over launches, [1] launches,
  * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
+
+/* ---- result files ----------------------------------------------------------
+ * Writes <prefix>.1 .2 .2fk .2sc .4 .hst .mmx in the WAMIT formats of
+ * Generate_Output_File_WAMIT / Update_Output_File_WAMIT
+ * (Hydrodynamic_Solver_IO.cpp:430-646) for the frequencies omega[0..n_freq) and
+ * the results r of bem_solve (A, B, FK, SC, F, RAO; NULL blocks are skipped).
+ * The frequency column is the reference's input Frequency = 2 pi Omega; forces
+ * are divided by g = 9.81; .hst holds C / (rho g), .mmx holds M / rho.  Omega = 0
+ * writes added mass only.  Host only; no device needed. */
+bem_status bem_write_wamit(const char* prefix, const bem_wamit_info* info, int n_freq, const double* omega,
+                           const bem_result* r);
 
 /* ---- dense complex solve that allocates nothing --------------------------------
  * This entry point has no counterpart in the reference.  It is the FP64 solve of
