@@ -90,6 +90,18 @@ def lib():
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
         "bem_kernel_times": ([vp, _dp, c_int], c_int),
+        "bem_mlp_num_params": ([], c_int),
+        "bem_mlp_create": ([ctypes.POINTER(vp), c_int, ctypes.c_ulonglong], c_int),
+        "bem_mlp_destroy": ([vp], None),
+        "bem_mlp_last_error": ([vp], ctypes.c_char_p),
+        "bem_mlp_set_normalization": ([vp, _dp, _dp, _dp, _dp], c_int),
+        "bem_mlp_get_params": ([vp, _dp], c_int),
+        "bem_mlp_set_params": ([vp, _dp], c_int),
+        "bem_mlp_eval": ([vp, c_int, _dp, _dp], c_int),
+        "bem_mlp_grad": ([vp, c_int, _dp, _dp, _dp, _dp], c_int),
+        "bem_mlp_train": ([vp, c_int, _dp, _dp, c_int, c_int, ctypes.c_double, ctypes.c_ulonglong, _dp], c_int),
+        "bem_mlp_throughput": ([vp, c_int, _dp], c_int),
+        "bem_havelock_throughput": ([c_int, c_int, c_int, _dp], c_int),
         "bem_write_wamit": ([ctypes.c_char_p, ctypes.POINTER(_WamitInfo), c_int, _dp, ctypes.POINTER(_Result)], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
@@ -444,6 +456,87 @@ def havelock_gf(x, y, v, precision=PLAIN_FP64, device=0):
     out = np.zeros((x.size, 8))
     _check(lib().bem_havelock(int(device), x.size, _p(x), _p(y), _p(v), int(precision), _p(out)))
     return out[:, 0::2] + 1j * out[:, 1::2]
+
+
+class HavelockSurrogate:
+    """MLP stand-in for HavelockGF (Kernels.cpp:342-412): inputs (log10 KR, KZ),
+    outputs Re/Im of G, dG/dR, dG/dZ; BF16 weights, FP32 accumulation, trained on
+    the GPU by the library's own forward/backward kernels (k_mlp.cu)."""
+
+    def __init__(self, device=0, seed=0):
+        h = ctypes.c_void_p()
+        rc = lib().bem_mlp_create(ctypes.byref(h), int(device), int(seed))
+        if rc != 0:
+            raise BEMError(rc, lib().bem_last_error(None).decode())
+        self._h = h
+        self.n_params = int(lib().bem_mlp_num_params())
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().bem_mlp_destroy(self._h)
+            self._h = None
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise BEMError(rc, lib().bem_mlp_last_error(self._h).decode())
+
+    def set_normalization(self, in_shift, in_scale, out_shift, out_scale):
+        a = [np.ascontiguousarray(v, dtype=np.float64).ravel() for v in (in_shift, in_scale, out_shift, out_scale)]
+        self._chk(lib().bem_mlp_set_normalization(self._h, *[_p(v) for v in a]))
+
+    def params(self):
+        w = np.zeros(self.n_params)
+        self._chk(lib().bem_mlp_get_params(self._h, _p(w)))
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        self._chk(lib().bem_mlp_set_params(self._h, _p(w)))
+
+    def eval(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)
+        y = np.zeros((x.shape[0], 6))
+        self._chk(lib().bem_mlp_eval(self._h, x.shape[0], _p(x), _p(y)))
+        return y
+
+    def grad(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1, 6)
+        g = np.zeros(self.n_params)
+        loss = np.zeros(1)
+        self._chk(lib().bem_mlp_grad(self._h, x.shape[0], _p(x), _p(y), _p(g), _p(loss)))
+        return float(loss[0]), g
+
+    def train(self, x, y, epochs, batch=4096, lr=1e-3, seed=0):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1, 6)
+        losses = np.zeros(max(1, int(epochs)))
+        self._chk(lib().bem_mlp_train(self._h, x.shape[0], _p(x), _p(y), int(epochs), int(batch), float(lr),
+                                      int(seed), _p(losses)))
+        return losses[:int(epochs)]
+
+    def throughput(self, n=1 << 20):
+        r = np.zeros(1)
+        self._chk(lib().bem_mlp_throughput(self._h, int(n), _p(r)))
+        return float(r[0])
+
+    @staticmethod
+    def training_set(n, seed=0, device=0, kr=(1e-3, 200.0), kz=(-100.0, 0.0)):
+        """Inputs (log10 KR, KZ) with KR log-uniform and KZ uniform, and targets from the
+        plain FP64 integrator: Re/Im of G, dG/dR (= dG/dx at y = 0), dG/dZ."""
+        rng = np.random.default_rng(seed)
+        lkr = rng.uniform(np.log10(kr[0]), np.log10(kr[1]), n)
+        z = rng.uniform(kz[0], kz[1], n)
+        g = havelock_gf(10.0 ** lkr, np.zeros(n), z, PLAIN_FP64, device)
+        y = np.stack([g[:, 0].real, g[:, 0].imag, g[:, 1].real, g[:, 1].imag, g[:, 3].real, g[:, 3].imag], axis=1)
+        return np.stack([lkr, z], axis=1), y
+
+
+def havelock_throughput(n=1 << 22, precision=MIXED, device=0):
+    """Closed-form HavelockGF evaluations per second of device time."""
+    r = np.zeros(1)
+    _check(lib().bem_havelock_throughput(int(device), int(n), int(precision), _p(r)))
+    return float(r[0])
 
 
 def launch_count():

@@ -973,6 +973,46 @@ bem_status bem_havelock(int device, int n, const double* x, const double* y, con
     return BEM_OK;
 }
 
+bem_status bem_havelock_throughput(int device, int n, int precision, double* evals_per_s) {
+    bem_ctx* ctx = nullptr;
+    if (n <= 0 || !evals_per_s) return fail(nullptr, BEM_ERR_ARG, "bem_havelock_throughput: bad arguments");
+    CK(cudaSetDevice(device));
+    CK(bem::upload_poly_constants(device));
+    // far-field points spread like the wave assembly's: h log-uniform on [1e-3, 200], v on [-100, 0]
+    std::vector<double> h(3 * (size_t)n);
+    unsigned long long st = 88172645463325252ull;
+    auto uni = [&]() { st ^= st << 13; st ^= st >> 7; st ^= st << 17; return (double)(st >> 11) * 0x1.0p-53; };
+    for (int i = 0; i < n; ++i) {
+        h[i] = std::pow(10.0, -3.0 + uni() * (std::log10(200.0) + 3.0));
+        h[n + (size_t)i] = 0.0;
+        h[2 * (size_t)n + i] = -100.0 * uni();
+    }
+    double* buf = nullptr;
+    CK(cudaMalloc(&buf, sizeof(double) * 11 * (size_t)n));
+    cudaError_t e = cudaMemcpy(buf, h.data(), 24 * (size_t)n, cudaMemcpyHostToDevice);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0;
+    const int reps = 5;
+    if (e == cudaSuccess) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        bem::launch_havelock(0, n, buf, buf + n, buf + 2 * (size_t)n, buf + 3 * (size_t)n, precision == BEM_MIXED);
+        cudaEventRecord(e0, 0);
+        for (int r = 0; r < reps; ++r)
+            bem::launch_havelock(0, n, buf, buf + n, buf + 2 * (size_t)n, buf + 3 * (size_t)n, precision == BEM_MIXED);
+        cudaEventRecord(e1, 0);
+        e = cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    cudaFree(buf);
+    if (e != cudaSuccess)
+        return fail(nullptr, BEM_ERR_CUDA, std::string("bem_havelock_throughput: ") + cudaGetErrorString(e));
+    *evals_per_s = (double)n * reps / (ms / 1000.0);
+    return BEM_OK;
+}
+
 bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, double* B, int precision, double tol,
                            int* iters, double* resid) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");

@@ -219,6 +219,34 @@ bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
  * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
 
+/* ---- MLP surrogate of the wave Green function (k_mlp.cu) -------------------
+ * Inputs (log10 KR, KZ), 4 hidden layers of width 128 with SiLU, 6 outputs:
+ * Re/Im of G, dG/dR, dG/dZ of HavelockGF (Kernels.cpp:342-412; dG/dZ = G there).
+ * BF16 weights (FP32 master copy), FP32 accumulation, Adam on the MSE of the
+ * normalised outputs; forward and backward kernels are this library's own.
+ * Parameters are ordered W0 (128x2), b0, W1 (128x128), b1, ..., W4 (6x128), b4,
+ * W row-major [out][in].  Host arrays throughout: x is n x 2, y is n x 6. */
+typedef struct bem_mlp bem_mlp;
+int bem_mlp_num_params(void);
+bem_status bem_mlp_create(bem_mlp** out, int device, unsigned long long seed);
+void bem_mlp_destroy(bem_mlp* m);
+const char* bem_mlp_last_error(const bem_mlp* m);
+/* x_n = (x - in_shift) / in_scale, y_n = (y - out_shift) / out_scale (2 and 6 entries). */
+bem_status bem_mlp_set_normalization(bem_mlp* m, const double* in_shift, const double* in_scale,
+                                     const double* out_shift, const double* out_scale);
+bem_status bem_mlp_get_params(bem_mlp* m, double* w);
+bem_status bem_mlp_set_params(bem_mlp* m, const double* w);
+bem_status bem_mlp_eval(bem_mlp* m, int n, const double* x, double* y);
+/* Loss (MSE of normalised outputs) and its gradient with respect to the parameters on one batch. */
+bem_status bem_mlp_grad(bem_mlp* m, int n, const double* x, const double* y, double* grad, double* loss);
+bem_status bem_mlp_train(bem_mlp* m, int n, const double* x, const double* y, int epochs, int batch, double lr,
+                         unsigned long long seed, double* loss_per_epoch);
+/* Forward-pass throughput (evaluations per second of device time) on n resident samples. */
+bem_status bem_mlp_throughput(bem_mlp* m, int n, double* mlp_evals_per_s);
+/* Throughput of the closed-form HavelockGF kernel (evaluations per second of device
+ * time) on n resident points; precision as for bem_havelock. */
+bem_status bem_havelock_throughput(int device, int n, int precision, double* evals_per_s);
+
 /* ---- result files ----------------------------------------------------------
  * Writes <prefix>.1 .2 .2fk .2sc .4 .hst .mmx in the WAMIT formats of
  * Generate_Output_File_WAMIT / Update_Output_File_WAMIT

@@ -1,0 +1,87 @@
+"""Green-function surrogate (k_mlp.cu): the network's own forward/backward kernels
+against the CPU oracle (oracle/mlp_oracle.py), training on samples from the plain
+integrator, and what the trained network gains over the closed form it replaces."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+
+
+def _rand_params(seed=1):
+    rng = np.random.default_rng(seed)
+    p = []
+    for l in range(len(mo.DIMS) - 1):
+        i, n = mo.DIMS[l], mo.DIMS[l + 1]
+        p.append(rng.uniform(-1, 1, n * i) * np.sqrt(6.0 / (i + n)))
+        p.append(rng.normal(0, 0.1, n))
+    return np.concatenate(p)
+
+
+def test_oracle_gradient_finite_differences():
+    """The oracle's backward pass against central differences (unquantised weights)."""
+    rng = np.random.default_rng(0)
+    p = _rand_params()
+    x = rng.normal(size=(7, 2))
+    t = rng.normal(size=(7, 6))
+    loss, g = mo.loss_and_grad(p, x, t, quantize=False)
+    idx = rng.choice(p.size, 40, replace=False)
+    for k in idx:
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        fd = (mo.loss_and_grad(pp, x, t, False)[0] - mo.loss_and_grad(pm, x, t, False)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)), (k, fd, g[k])
+
+
+def test_bf16_rounding():
+    v = np.array([1.0, 1.00390625, 1.005859375, -3.14159265, 0.0], dtype=np.float32)
+    q = mo.bf16(v)
+    assert q[0] == 1.0 and q[1] == 1.0  # ties to even
+    assert q[2] == np.float32(1.0078125)
+    assert abs(q[3] + 3.140625) < 1e-7
+
+
+@pytest.mark.gpu
+def test_gpu_forward_backward_match_oracle():
+    import bemuse_gb300 as bg
+    s = bg.HavelockSurrogate(seed=3)
+    p = _rand_params(5)
+    s.set_params(p)
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=(300, 2))
+    t = rng.normal(size=(300, 6))
+    # identity normalisation: eval sees x, y directly
+    s.set_normalization([0, 0], [1, 1], np.zeros(6), np.ones(6))
+    y_gpu = s.eval(x)
+    y_ref = mo.forward(p, x)[0]
+    err = np.max(np.abs(y_gpu - y_ref)) / np.max(np.abs(y_ref))
+    print("surrogate forward vs oracle:", err)
+    assert err < 2e-5
+    loss_gpu, g_gpu = s.grad(x, t)
+    loss_ref, g_ref = mo.loss_and_grad(p, x, t)
+    print("loss", loss_gpu, loss_ref, "grad rel", np.max(np.abs(g_gpu - g_ref)) / np.max(np.abs(g_ref)))
+    assert abs(loss_gpu - loss_ref) <= 1e-5 * loss_ref
+    assert np.max(np.abs(g_gpu - g_ref)) <= 1e-4 * np.max(np.abs(g_ref))
+
+
+@pytest.mark.gpu
+def test_training_and_gain_report():
+    """Trains on the plain integrator's samples and reports accuracy and throughput
+    against the FP32 closed form; the closed form is expected to win (a negative
+    result for the surrogate is the expected, reported outcome)."""
+    import bemuse_gb300 as bg
+    x, y = bg.HavelockSurrogate.training_set(1 << 16, seed=0)
+    xv, yv = bg.HavelockSurrogate.training_set(1 << 12, seed=1)
+    s = bg.HavelockSurrogate(seed=0)
+    s.set_normalization(x.mean(0), x.std(0), y.mean(0), y.std(0) + 1e-12)
+    losses = s.train(x, y, epochs=8, batch=2048, lr=2e-3)
+    print("losses", losses)
+    assert losses[-1] < 0.5 * losses[0]
+    pred = s.eval(xv)
+    rel = np.max(np.abs(pred - yv), axis=0) / np.max(np.abs(yv), axis=0)
+    print("max error / max |target| per output:", rel)
+    mlp = s.throughput(1 << 18)
+    closed = bg.havelock_throughput(1 << 20, bg.MIXED)
+    print("evaluations/s: surrogate %.3e, FP32 closed form %.3e" % (mlp, closed))
+    assert mlp > 0 and closed > 0
