@@ -102,6 +102,8 @@ def lib():
         "bem_mlp_train": ([vp, c_int, _dp, _dp, c_int, c_int, ctypes.c_double, ctypes.c_ulonglong, _dp], c_int),
         "bem_mlp_throughput": ([vp, c_int, _dp], c_int),
         "bem_havelock_throughput": ([c_int, c_int, c_int, _dp], c_int),
+        "bem_batch_solve": ([c_int, c_int, ctypes.POINTER(_Mesh), ctypes.POINTER(_Props), c_double, c_double, c_int,
+                             _dp, c_int, _dp, c_int, c_double, c_int, ctypes.POINTER(_Result), _dp], c_int),
         "bem_write_wamit": ([ctypes.c_char_p, ctypes.POINTER(_WamitInfo), c_int, _dp, ctypes.POINTER(_Result)], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
@@ -530,6 +532,38 @@ class HavelockSurrogate:
         g = havelock_gf(10.0 ** lkr, np.zeros(n), z, PLAIN_FP64, device)
         y = np.stack([g[:, 0].real, g[:, 0].imag, g[:, 1].real, g[:, 1].imag, g[:, 3].real, g[:, 3].imag], axis=1)
         return np.stack([lkr, z], axis=1), y
+
+
+def batch_solve(meshes, omegas, betas=(0.0,), precision=MIXED, n_workers=8, refine_tol=1e-12, density=1025.0,
+                gravity=9.81, device=0):
+    """Independent bodies at the same frequencies (bem_batch_solve): returns a list of
+    per-body dicts (A, B, FK, SC, F, RAO, iters) and the wall time in seconds."""
+    om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
+    b = np.ascontiguousarray(betas, dtype=np.float64).ravel()
+    nf, nb, n = om.size, b.size, len(meshes)
+    structs = (_Mesh * n)()
+    keep = []
+    for i, m in enumerate(meshes):
+        ms = m._struct()
+        keep.append(ms)
+        structs[i] = ms
+    outs, res = [], (_Result * n)()
+    for i in range(n):
+        o = dict(A=np.zeros((nf, 6, 6)), B=np.zeros((nf, 6, 6)), FK=np.zeros((nf, 6, nb), np.complex128),
+                 SC=np.zeros((nf, 6, nb), np.complex128), F=np.zeros((nf, 6, nb), np.complex128),
+                 RAO=np.zeros((nf, 6, nb), np.complex128), iters=np.zeros(nf, np.int32), residual=np.zeros(nf))
+        outs.append(o)
+        r = res[i]
+        r.A, r.B = _p(o["A"]), _p(o["B"])
+        for k in ("FK", "SC", "F", "RAO"):
+            setattr(r, k, _p(o[k].view(np.float64)))
+        r.refine_iters = _p(o["iters"], _ip)
+        r.residual = _p(o["residual"])
+    sec = np.zeros(1)
+    _check(lib().bem_batch_solve(int(device), n, structs, None, float(density), float(gravity), nb,
+                                 _p(b) if nb else None, nf, _p(om), int(precision), float(refine_tol),
+                                 int(n_workers), res, _p(sec)))
+    return outs, float(sec[0])
 
 
 def havelock_throughput(n=1 << 22, precision=MIXED, device=0):

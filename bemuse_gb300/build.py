@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(OUT_DIR, "libbemgpu.so")
 
-SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "noalloc.cu", "k_mlp.cu"]
+SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "host_batch.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "noalloc.cu", "k_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -59,7 +59,7 @@ def build(verbose=False, force=False):
             if log:
                 sys.stderr.write(log)
     objs = [o for o, _ in results]
-    cmd = [nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -1,5 +1,6 @@
 // bem_internal.h -- declarations shared by the host runtime and the kernels.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
@@ -7,7 +8,7 @@
 namespace bem {
 
 // Count of kernel launches issued by this library (all contexts).
-extern unsigned long long g_launches;
+extern std::atomic<unsigned long long> g_launches;  // kernel launches (all threads)
 #define BEM_LAUNCH(...) (++::bem::g_launches, __VA_ARGS__)
 
 constexpr int RK_STRIDE = 32;   // doubles per Rankine panel record

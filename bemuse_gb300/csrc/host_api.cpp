@@ -26,7 +26,7 @@
 
 using bem::CMat;
 
-unsigned long long bem::g_launches = 0;
+std::atomic<unsigned long long> bem::g_launches{0};
 using cplx = std::complex<double>;
 
 // Per-frequency state of a mixed-precision solve.  Two of them let the
@@ -384,7 +384,7 @@ extern "C" {
 
 const char* bem_version(void) { return "bemgpu 0.1 (sm_103a)"; }
 
-unsigned long long bem_launch_count(void) { return bem::g_launches; }
+unsigned long long bem_launch_count(void) { return bem::g_launches.load(); }
 
 double bem_selftest_tc(int device, int n) { return bem::tc_selftest(device, n); }
 

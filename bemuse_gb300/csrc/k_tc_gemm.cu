@@ -293,14 +293,14 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 static EncodeTiledFn get_encode() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    static const EncodeTiledFn fn = [] {  // resolved once, thread-safe
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
+            return reinterpret_cast<EncodeTiledFn>(p);
+        return (EncodeTiledFn) nullptr;
+    }();
     return fn;
 }
 
@@ -351,13 +351,9 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
     if (!make_map(&mL, wl, n, BM) || !make_map(&mU, wut, n, BN) || !make_map_c(&mCr, A.re, n, n, A.ld) ||
         !make_map_c(&mCi, A.im, n, n, A.ld))
         return false;
-    static int attr_done = -1;
     int dev = 0;
     cudaGetDevice(&dev);
-    if (attr_done != dev) {
-        cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        attr_done = dev;
-    }
+    cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int grid = Mt * Nt;

@@ -219,6 +219,20 @@ bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
  * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
 
+/* ---- many bodies --------------------------------------------------------------
+ * Solves n_bodies independent bodies at the same frequencies: for each body the
+ * Setup + per-frequency Solve sequence of the reference's console loop
+ * (BEMUser_Console.cpp:242-262).  n_workers host threads (0: 8), each with its own
+ * context on `device`, run bodies concurrently, largest first.  props may be NULL
+ * (default mass properties).  results[b] receives body b's outputs as bem_solve
+ * fills them; *seconds (may be NULL) the wall time.  The first failure is
+ * returned (message in bem_last_error(NULL)); a worker that meets a failure
+ * stops, the others finish their bodies. */
+bem_status bem_batch_solve(int device, int n_bodies, const bem_mesh* meshes, const bem_body_props* props,
+                           double density, double gravity, int n_beta, const double* betas, int n_freq,
+                           const double* omega, int precision, double tol, int n_workers, bem_result* results,
+                           double* seconds);
+
 /* ---- MLP surrogate of the wave Green function (k_mlp.cu) -------------------
  * Inputs (log10 KR, KZ), 4 hidden layers of width 128 with SiLU, 6 outputs:
  * Re/Im of G, dG/dR, dG/dZ of HavelockGF (Kernels.cpp:342-412; dG/dZ = G there).
