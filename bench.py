@@ -217,7 +217,7 @@ def batched_bodies(bg, n_bodies=64, seed=0):
             L, B, D = rng.uniform(5, 40), rng.uniform(5, 40), rng.uniform(5, 30)
             side = np.sqrt((L * B + 2 * (L + B) * D) / target)
             NX, NY, NZ = (max(2, int(round(v / side))) for v in (L, B, D))
-            bodies.append(("box", (L, B, D, NX, NY, NZ), bg.Barge(L, B, D, NX, NY, NZ, False)))
+            bodies.append(("box", (L, B, D, NX, NY, NZ), bg.Barge(L, B, D, NX, NY, NZ, True)))
     return bodies
 
 

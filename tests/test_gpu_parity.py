@@ -195,7 +195,7 @@ def test_aero_steady_solve_matches_oracle(bg, orc):
 def test_batch_solve_matches_single_bodies(bg):
     """bem_batch_solve (concurrent per-body pipelines) gives each body the results
     of its own single-context solve."""
-    meshes = [bg.Half_Cylinder(5.0, 8.0, 12, 3, 4, 0, False), bg.Barge(20.0, 8.0, 4.0, 8, 4, 3, False),
+    meshes = [bg.Half_Cylinder(5.0, 8.0, 12, 3, 4, 0, False), bg.Barge(20.0, 8.0, 4.0, 8, 4, 3, True),
               bg.Half_Cylinder(3.0, 6.0, 16, 2, 5, 0, False)]
     om = np.array([0.3, 0.9])
     outs, sec = bg.batch_solve(meshes, om, [0.0, 0.5], bg.MIXED, n_workers=3)
