@@ -90,6 +90,7 @@ def lib():
         "bem_dense_solve": ([vp, c_int, _dp, c_int, _dp, c_int, c_double, _ip, _dp], c_int),
         "bem_stage_times": ([vp, _dp, c_int], c_int),
         "bem_kernel_times": ([vp, _dp, c_int], c_int),
+        "bem_lu_timeline": ([vp, c_int, c_int, _dp, _ip], c_int),
         "bem_mlp_num_params": ([], c_int),
         "bem_mlp_create": ([ctypes.POINTER(vp), c_int, ctypes.c_ulonglong], c_int),
         "bem_mlp_destroy": ([vp], None),
@@ -401,6 +402,15 @@ class Hydrodynamic_Radiation_Solver:
         t = np.zeros(6)
         _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
         return t
+
+    def lu_timeline(self, enable=-1):
+        """Per block step of the last mixed LU: ms of [cross start, cross done, inverse done,
+        W21 done, panel ready, rest done] (enable=1 starts recording)."""
+        n = ctypes.c_int()
+        _check(lib().bem_lu_timeline(self._h, int(enable), 0, None, ctypes.byref(n)), self._h)
+        out = np.zeros((max(n.value, 1), 6))
+        _check(lib().bem_lu_timeline(self._h, -1, n.value, _p(out), ctypes.byref(n)), self._h)
+        return out[:n.value]
 
     def kernel_times(self, reset=False):
         """[wave-assembly kernel ms (summed), launches, panel pairs per launch, 0]."""

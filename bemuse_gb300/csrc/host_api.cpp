@@ -98,6 +98,8 @@ struct bem_ctx {
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
+    std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
+    std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
 };
@@ -296,7 +298,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
         int rc_lu;
         if (tc) {
-            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, 8};
+            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, 8,
+                                    ctx->lu_tl.size() >= (size_t)6 * (Np / 128) ? ctx->lu_tl.data() : nullptr};
             rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                  ctx->d_wut32, ctx->d_flags);
         } else {
@@ -360,6 +363,17 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
     int hflags = 0;
     CK(cudaMemcpyAsync(&hflags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (mixed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)) {
+        const int steps = Np / 128 - 1;
+        ctx->lu_tl_ms.assign((size_t)6 * std::max(steps, 0), 0.0);
+        for (int k = 0; k < steps; ++k)
+            for (int j = 0; j < 6; ++j) {
+                float ms = 0;
+                const bool ok = cudaEventElapsedTime(&ms, ctx->lu_tl[0], ctx->lu_tl[6 * k + j]) == cudaSuccess;
+                ctx->lu_tl_ms[6 * (size_t)k + j] = ok ? ms : NAN;
+            }
+        cudaGetLastError();  // an unrecorded event only leaves a NaN
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
     *t_lu += ms;
@@ -472,6 +486,7 @@ void bem_destroy(bem_ctx* ctx) {
     for (auto& ev : ctx->ev_wk)
         if (ev) cudaEventDestroy(ev);
     if (ctx->ev_call) cudaEventDestroy(ctx->ev_call);
+    for (auto e : ctx->lu_tl) cudaEventDestroy(e);
     if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
     if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
@@ -1158,6 +1173,24 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
 // Stage times (ms, accumulated since the last reset) of bem_solve:
 // [0] incident + static RHS, [1] wave assembly, [2] LU, [3] solve/refine,
 // [4] post, [5] number of frequency-solves.
+bem_status bem_lu_timeline(bem_ctx* ctx, int enable, int max_steps, double* out, int* steps) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    CK(cudaSetDevice(ctx->device));
+    if (enable > 0 && ctx->lu_tl.empty()) {
+        ctx->lu_tl.resize((size_t)6 * 512);  // up to 512 block steps (65,536 unknowns)
+        for (auto& e : ctx->lu_tl) CK(cudaEventCreate(&e));
+    } else if (enable == 0) {
+        for (auto e : ctx->lu_tl) cudaEventDestroy(e);
+        ctx->lu_tl.clear();
+    }
+    const int have = (int)(ctx->lu_tl_ms.size() / 6);
+    if (steps) *steps = have;
+    if (out)
+        for (int k = 0; k < std::min(have, max_steps); ++k)
+            for (int j = 0; j < 6; ++j) out[6 * k + j] = ctx->lu_tl_ms[6 * (size_t)k + j];
+    return BEM_OK;
+}
+
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
     if (out4) memcpy(out4, ctx->kernel_ms, sizeof(ctx->kernel_ms));

@@ -406,9 +406,15 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     cudaStream_t sp = ls.panel;
     // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl), U12^T (into wut);
     // ev_panel marks the operands ready; W21 is then stored into A for the solves.
+    // timeline (optional): per step k, [0] cross update start, [1] cross done (main stream),
+    // [2] inverse of block k+1 done, [3] W21 done, [4] panel k+1 ready (panel stream), [5] rest done
+    auto mark = [&](int k, int slot, cudaStream_t s) {
+        if (ls.timeline && k >= 0 && k < nblk) cudaEventRecord(ls.timeline[6 * k + slot], s);
+    };
     auto panel = [&](int k) {
         const int k0 = k * NB, rem = n - k0 - NB;
         BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, flags));
+        mark(k - 1, 2, sp);
         float *wlr = wlb(k), *wli = wlb(k) + (size_t)n * NB;
         if (rem > 0) {
             CMat<float> Dinv{invr + (size_t)k * NB * NB, invi + (size_t)k * NB * NB, NB};
@@ -419,7 +425,9 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
             BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
                 rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
         }
+        mark(k - 1, 3, sp);
         cudaEventRecord(ls.ev_panel, sp);
+        mark(k - 1, 4, sp);
         if (rem > 0) {
             int nb_ = (int)(((size_t)rem * NB + 255) / 256);
             if (nb_ > 4096) nb_ = 4096;
@@ -435,14 +443,17 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         const int k0 = k * NB, rem = n - k0 - NB;
         if (rem <= 0) break;
         const int mt = rem / NB;
+        mark(k, 0, st);
         // block column k+1 and block row k+1 first: they are the next panel's input
         if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, 1, 0, flags)) return 1;
         if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, NB, 1, mt - 1, 0, flags)) return 1;
         cudaEventRecord(ls.ev_cross, st);
+        mark(k, 1, st);
         cudaStreamWaitEvent(sp, ls.ev_cross, 0);
         panel(k + 1);
         if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags))
             return 1;
+        mark(k, 5, st);
     }
     // the last stores of W21 into A precede the solves
     cudaEventRecord(ls.ev_panel, sp);

@@ -219,6 +219,15 @@ bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
  * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
 
+/* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
+ * turns recording on (events at every block step of later mixed factorizations),
+ * 0 turns it off, -1 leaves it unchanged.  out receives, for the last recorded
+ * factorization, up to max_steps rows of 6 times in ms from its first event:
+ * cross update of step k started / done (main stream), inverse of block k+1 done,
+ * W21 done, panel k+1 ready (panel stream), rest of step k's update done.
+ * *steps = rows available. */
+bem_status bem_lu_timeline(bem_ctx* ctx, int enable, int max_steps, double* out, int* steps);
+
 /* ---- many bodies --------------------------------------------------------------
  * Solves n_bodies independent bodies at the same frequencies: for each body the
  * Setup + per-frequency Solve sequence of the reference's console loop
