@@ -91,6 +91,7 @@ def lib():
         "bem_stage_times": ([vp, _dp, c_int], c_int),
         "bem_kernel_times": ([vp, _dp, c_int], c_int),
         "bem_lu_timeline": ([vp, c_int, c_int, _dp, _ip], c_int),
+        "bem_set_tuning": ([vp, ctypes.c_char_p, c_double], c_int),
         "bem_mlp_num_params": ([], c_int),
         "bem_mlp_create": ([ctypes.POINTER(vp), c_int, ctypes.c_ulonglong], c_int),
         "bem_mlp_destroy": ([vp], None),
@@ -402,6 +403,9 @@ class Hydrodynamic_Radiation_Solver:
         t = np.zeros(6)
         _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
         return t
+
+    def set_tuning(self, key, value):
+        _check(lib().bem_set_tuning(self._h, key.encode(), float(value)), self._h)
 
     def lu_timeline(self, enable=-1):
         """Per block step of the last mixed LU: ms of [cross start, cross done, inverse done,

@@ -99,6 +99,7 @@ struct bem_ctx {
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
+    int lu_reserve_sms = 8;                     // SMs the lookahead LU keeps free of the trailing update
     std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
@@ -298,7 +299,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
         int rc_lu;
         if (tc) {
-            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, 8,
+            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms,
                                     ctx->lu_tl.size() >= (size_t)6 * (Np / 128) ? ctx->lu_tl.data() : nullptr};
             rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                  ctx->d_wut32, ctx->d_flags);
@@ -1173,6 +1174,17 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
 // Stage times (ms, accumulated since the last reset) of bem_solve:
 // [0] incident + static RHS, [1] wave assembly, [2] LU, [3] solve/refine,
 // [4] post, [5] number of frequency-solves.
+bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
+    if (!ctx || !key) return fail(ctx, BEM_ERR_ARG, "bem_set_tuning: bad arguments");
+    const std::string k(key);
+    if (k == "lu_reserve_sms") {
+        if (!(value >= 0 && value <= 144)) return fail(ctx, BEM_ERR_ARG, "lu_reserve_sms must be in [0, 144]");
+        ctx->lu_reserve_sms = (int)value;
+        return BEM_OK;
+    }
+    return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);
+}
+
 bem_status bem_lu_timeline(bem_ctx* ctx, int enable, int max_steps, double* out, int* steps) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
     CK(cudaSetDevice(ctx->device));

@@ -23,7 +23,7 @@ namespace bem {
 bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
                         int* flags);
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
-                    int ur0, int Mt, int Nt, int max_ctas, int* flags);
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -444,14 +444,14 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         if (rem <= 0) break;
         const int mt = rem / NB;
         mark(k, 0, st);
-        // block column k+1 and block row k+1 first: they are the next panel's input
-        if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, 1, 0, flags)) return 1;
-        if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, NB, 1, mt - 1, 0, flags)) return 1;
+        // block column k+1 and block row k+1 first (one L-shaped launch): the next panel's input
+        if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, mt, 0, flags, true)) return 1;
         cudaEventRecord(ls.ev_cross, st);
         mark(k, 1, st);
         cudaStreamWaitEvent(sp, ls.ev_cross, 0);
         panel(k + 1);
-        if (mt > 1 && !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags))
+        if (mt > 1 &&
+            !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags, false))
             return 1;
         mark(k, 5, st);
     }

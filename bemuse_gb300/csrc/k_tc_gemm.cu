@@ -145,7 +145,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_tc_update(const __grid_constant__ CUtensorMap mapL, const __grid_constant__ CUtensorMap mapU,
                 const __grid_constant__ CUtensorMap mapCr, const __grid_constant__ CUtensorMap mapCi, int nplane,
-                int lr0, int ur0, int Mt, int Nt, int crow0, int ccol0, int* gflags) {
+                int lr0, int ur0, int Mt, int Nt, int lshape, int crow0, int ccol0, int* gflags) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;  // 1024-byte aligned (128-byte swizzle atoms)
@@ -158,7 +158,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 3);
     const uint32_t tfull0 = smem_u32(bars + 6), tempty0 = smem_u32(bars + 8);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntiles = Mt * Nt;
+    // rectangle: Mt x Nt tiles; L-shape: tile column 0 (Mt tiles) and tile row 0 (Nt - 1 more)
+    const int ntiles = lshape ? Mt + Nt - 1 : Mt * Nt;
+    auto tile_of = [&](int t, int& tm, int& tn) {
+        if (lshape) { tm = t < Mt ? t : 0; tn = t < Mt ? 0 : t - Mt + 1; }
+        else { tm = t / Nt; tn = t % Nt; }
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) { mbar_init(full0 + 8 * s, 1); mbar_init(empty0 + 8 * s, 1); }
@@ -187,7 +192,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int lrow = lr0 + (t / Nt) * BM, urow = ur0 + (t % Nt) * BN;
+                int tm, tn;
+                tile_of(t, tm, tn);
+                const int lrow = lr0 + tm * BM, urow = ur0 + tn * BN;
                 for (int kb = 0; kb < KB; ++kb, ++it) {
                     const uint32_t s = it % STAGES, u = it / STAGES;
                     if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
@@ -240,7 +247,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t slot0 = epi_base + (uint32_t)(warp - 2) * 2 * SLOT_BYTES;
         uint32_t local = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
-            const int tm = t / Nt, tn = t % Nt;
+            int tm, tn;
+            tile_of(t, tm, tn);
             const uint32_t buf = local & 1, u = local >> 1;
             bool have = mbar_wait(tfull0 + 8 * buf, u & 1, abort_flag, gflags);
             if (!__all_sync(0xffffffffu, have)) break;
@@ -341,9 +349,10 @@ static bool make_map_c(CUtensorMap* m, const float* base, int rows, int cols, in
 // Tile rectangle of the step-k0 update (nb = 128): L21 rows [lr0, lr0 + 128 Mt) of
 // wl, U12^T rows [ur0, ur0 + 128 Nt) of wut, landing at A[k0+128+lr0.., k0+128+ur0..].
 // wl = [2][n][128] (L21 rows from 0), wut = [2][n][128] (U12^T rows from 0).
-// max_ctas caps the persistent grid (leaves SMs to a concurrent stream).
+// max_ctas caps the persistent grid (leaves SMs to a concurrent stream).  lshape:
+// only tile column 0 (Mt tiles) and tile row 0 (Nt tiles) of the rectangle.
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
-                    int ur0, int Mt, int Nt, int max_ctas, int* flags) {
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape) {
     if (Mt <= 0 || Nt <= 0) return true;
     if (n % 128 || k0 % 128 || lr0 % 128 || ur0 % 128 || A.ld % 4) return false;
     if (k0 + 128 + lr0 + 128 * Mt > n || k0 + 128 + ur0 + 128 * Nt > n) return false;
@@ -356,11 +365,11 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
     cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    int grid = Mt * Nt;
+    int grid = lshape ? Mt + Nt - 1 : Mt * Nt;
     if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
     if (grid > nsm) grid = nsm;
-    BEM_LAUNCH(k_tc_update<<<grid, NTHREADS, SMEM_BYTES, st>>>(mL, mU, mCr, mCi, n, lr0, ur0, Mt, Nt, k0 + 128 + lr0,
-                                                              k0 + 128 + ur0, flags));
+    BEM_LAUNCH(k_tc_update<<<grid, NTHREADS, SMEM_BYTES, st>>>(mL, mU, mCr, mCi, n, lr0, ur0, Mt, Nt, lshape ? 1 : 0,
+                                                              k0 + 128 + lr0, k0 + 128 + ur0, flags));
     return true;
 }
 
@@ -370,7 +379,7 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
     const int rem = n - k0 - nb;
     if (rem <= 0) return true;
     if (nb != 128) return false;
-    return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags);
+    return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags, false);
 }
 
 }  // namespace bem

@@ -219,6 +219,11 @@ bem_status bem_stage_times(bem_ctx* ctx, double* out6, int reset);
  * [2] panel pairs per launch (N^2), [3] reserved.  reset != 0 zeroes after reading. */
 bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
 
+/* Tuning knobs (defaults are the measured best on GB300):
+ *   "lu_reserve_sms"  SMs the lookahead LU keeps free of the trailing update for
+ *                     the panel chain (inverse, W21, transpose); default 8. */
+bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
+
 /* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
  * turns recording on (events at every block step of later mixed factorizations),
  * 0 turns it off, -1 leaves it unchanged.  out receives, for the last recorded
