@@ -400,7 +400,9 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int rest_ctas = std::max(1, nsm - ls.reserve_sms);
+    // reserve_sms > 0: persistent rest update on nsm - reserve_sms CTAs; 0: CTAs of about
+    // four tiles each, which retire during the update and hand SMs to the panel stream
+    const int rest_ctas = ls.reserve_sms > 0 ? std::max(1, nsm - ls.reserve_sms) : -4;
     auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
     auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };
     cudaStream_t sp = ls.panel;

@@ -349,8 +349,10 @@ static bool make_map_c(CUtensorMap* m, const float* base, int rows, int cols, in
 // Tile rectangle of the step-k0 update (nb = 128): L21 rows [lr0, lr0 + 128 Mt) of
 // wl, U12^T rows [ur0, ur0 + 128 Nt) of wut, landing at A[k0+128+lr0.., k0+128+ur0..].
 // wl = [2][n][128] (L21 rows from 0), wut = [2][n][128] (U12^T rows from 0).
-// max_ctas caps the persistent grid (leaves SMs to a concurrent stream).  lshape:
-// only tile column 0 (Mt tiles) and tile row 0 (Nt tiles) of the rectangle.
+// max_ctas > 0 caps the persistent grid at that many CTAs; max_ctas < 0 launches
+// ceil(tiles / -max_ctas) CTAs of about -max_ctas tiles each, so CTAs retire
+// while the update runs and a higher-priority stream can take the freed SMs.
+// lshape: only tile column 0 (Mt tiles) and tile row 0 (Nt tiles) of the rectangle.
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
                     int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape) {
     if (Mt <= 0 || Nt <= 0) return true;
@@ -365,9 +367,14 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
     cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    int grid = lshape ? Mt + Nt - 1 : Mt * Nt;
-    if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-    if (grid > nsm) grid = nsm;
+    const int ntiles = lshape ? Mt + Nt - 1 : Mt * Nt;
+    int grid = ntiles;
+    if (max_ctas < 0) {
+        grid = (ntiles + (-max_ctas) - 1) / (-max_ctas);
+    } else {
+        if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+        if (grid > nsm) grid = nsm;
+    }
     BEM_LAUNCH(k_tc_update<<<grid, NTHREADS, SMEM_BYTES, st>>>(mL, mU, mCr, mCi, n, lr0, ur0, Mt, Nt, lshape ? 1 : 0,
                                                               k0 + 128 + lr0, k0 + 128 + ur0, flags));
     return true;
