@@ -200,9 +200,11 @@ __device__ __forceinline__ void bessel_large(float xh, float xl, float& j0, floa
     float sn, cs;
     sincosf(ph, &sn, &cs);
     const float s0 = fmaf(cs, pl, sn), c0 = fmaf(-sn, pl, cs);  // sin, cos theta_0
-    // theta_1 = theta_0 - pi/2 + (d1 - d0)
-    float se, ce;
-    sincosf(d1 - d0, &se, &ce);
+    // theta_1 = theta_0 - pi/2 + (d1 - d0); |d1 - d0| < 0.17 for x >= 3, where the
+    // Taylor series below are exact to ~1e-12
+    const float dl = d1 - d0, dl2 = dl * dl;
+    const float se = dl * fmaf(dl2, fmaf(dl2, fmaf(dl2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
+    const float ce = fmaf(dl2, fmaf(dl2, fmaf(dl2, fmaf(dl2, 1.0f / 40320.0f, -1.0f / 720.0f), 1.0f / 24.0f), -0.5f), 1.0f);
     const float sa = fmaf(s0, ce, c0 * se);   // sin(theta_0 + d1 - d0) =  cos theta_1
     const float ca = fmaf(c0, ce, -s0 * se);  // cos(theta_0 + d1 - d0) = -sin theta_1
     const float rs = rsqrtf(xh);
@@ -284,14 +286,14 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
-    float inv_d = 1.0f / dd;
+    float inv_d = __frcp_rn(dd);
     float alpha = -vv * inv_d;
     float beta = hh * inv_d;
-    float rho = dd / (1.0f + dd);
+    float rho = __fdividef(dd, 1.0f + dd);
     float u = rho - 0.5f;
     float d2 = dd * dd;
     float d3 = d2 * dd;
-    float inv_1d3 = 1.0f / (1.0f + d3);
+    float inv_1d3 = __frcp_rn(1.0f + d3);
     float dmv = dd - vv;
     float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
     PP = fmaf(PP, ev, d2 - vv);
@@ -299,14 +301,14 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
     float omr = 1.0f - rho;
     float RR = (1.0f - beta) * A - beta * B;
-    RR -= alpha * C / fmaf(6.0f * alpha * rho, omr, 1.0f);
+    RR -= __fdividef(alpha * C, fmaf(6.0f * alpha * rho, omr, 1.0f));
     RR = fmaf(beta * (1.0f - beta), D, RR);
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
     float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
     float E = 2.0f * PI * ev;
     Gr = fmaf(E, H0, L0);
-    float PS = (beta + hh) / dmv;
+    float PS = __fdividef(beta + hh, dmv);
     PS -= 2.0f * beta;
     PS = fmaf(2.0f * dd, ev, PS);
     PS -= hh;

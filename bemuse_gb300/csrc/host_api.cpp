@@ -99,7 +99,7 @@ struct bem_ctx {
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
-    int lu_reserve_sms = 8;                     // SMs the lookahead LU keeps free of the trailing update
+    int lu_reserve_sms = 0;                     // 0: short-lived trailing-update CTAs (see bem_set_tuning)
     std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
 // here: it is applied exactly, in FP64, by the plane-wave kernels below
 // (k_pw_*), because the radiation damping at low K is a small difference of
 // O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
-__global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
+__global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (r >= a.N) return;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) k_wave_mixed(WaveArgs a) {
                 float proj = fmaf(XX, nx, YY * ny);
                 float dgr = 0.f, dgi = 0.f;
                 if (hh > 1.0e-6f) {
-                    float inv_h = 1.0f / hh;
+                    float inv_h = __frcp_rn(hh);
                     dgr = Ghr * proj * inv_h;
                     dgi = twopi * ev * j1v * proj * inv_h;
                 }
