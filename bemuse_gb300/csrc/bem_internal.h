@@ -94,6 +94,7 @@ struct LuStreams {
     cudaStream_t panel;
     cudaEvent_t ev_panel, ev_cross;
     int reserve_sms;
+    int rest_tiles;         // tiles per trailing-update CTA when reserve_sms == 0
     cudaEvent_t* timeline;  // optional, 6 timing events per block step (see lu_factor_f32_lookahead)
 };
 // wl2, wut2: two [2][n][128] buffers each (4 n 128 floats).

@@ -100,6 +100,7 @@ struct bem_ctx {
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 0;                     // 0: short-lived trailing-update CTAs (see bem_set_tuning)
+    int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
     std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
@@ -299,7 +300,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
         int rc_lu;
         if (tc) {
-            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms,
+            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms, ctx->lu_rest_tiles,
                                     ctx->lu_tl.size() >= (size_t)6 * (Np / 128) ? ctx->lu_tl.data() : nullptr};
             rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                  ctx->d_wut32, ctx->d_flags);
@@ -1180,6 +1181,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_reserve_sms") {
         if (!(value >= 0 && value <= 144)) return fail(ctx, BEM_ERR_ARG, "lu_reserve_sms must be in [0, 144]");
         ctx->lu_reserve_sms = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_rest_tiles") {
+        if (!(value >= 1 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "lu_rest_tiles must be in [1, 64]");
+        ctx->lu_rest_tiles = (int)value;
         return BEM_OK;
     }
     return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);

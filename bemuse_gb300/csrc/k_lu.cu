@@ -486,7 +486,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     // reserve_sms > 0: persistent rest update on nsm - reserve_sms CTAs; 0: CTAs of about
     // four tiles each, which retire during the update and hand SMs to the panel stream
-    const int rest_ctas = ls.reserve_sms > 0 ? std::max(1, nsm - ls.reserve_sms) : -4;
+    const int rest_ctas = ls.reserve_sms > 0 ? std::max(1, nsm - ls.reserve_sms) : -std::max(1, ls.rest_tiles);
     cudaFuncSetAttribute(k_w21, cudaFuncAttributeMaxDynamicSharedMemorySize, W21_SMEM);
     auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
     auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };

@@ -223,7 +223,8 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *   "lu_reserve_sms"  > 0: SMs the lookahead LU keeps free of its persistent trailing
  *                     update for the panel chain (inverse, W21, transpose); 0: the
  *                     trailing update runs as short-lived CTAs of ~4 tiles that hand
- *                     SMs to the higher-priority panel stream as they retire (default). */
+ *                     SMs to the higher-priority panel stream as they retire (default).
+ *   "lu_rest_tiles"   tiles per such CTA (default 4). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
