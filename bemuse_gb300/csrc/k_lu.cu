@@ -374,43 +374,44 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
 }
 
 // W21 = A21 D^-1 for the FP32 LU (rows x 128 times 128 x 128, planar complex):
-// CTA of 256 threads per 32 rows; thread (ty, tx) owns rows 2 ty, 2 ty + 1 and
-// columns 8 tx .. 8 tx + 7.  The contraction runs in 4 chunks of 32, staged by
-// cp.async into a double buffer (A chunk 32 x 32, D^-1 chunk 32 x 128, both planes).
-constexpr int W21_ROWS = 32, W21_KC = 32;
-constexpr int W21_SMEM = 2 * (2 * W21_ROWS * W21_KC + 2 * W21_KC * 128) * 4;  // 80 KB
+// CTA of 128 threads per 32 x 32 output block (grid rows/32 x 4, so the late,
+// short steps of the LU still spread over many SMs); thread (ty, tx) owns rows
+// 2 ty, 2 ty + 1 and columns 4 tx .. 4 tx + 3 of the block.  The contraction runs
+// in 4 chunks of 32, staged by cp.async into a double buffer (both planes).
+constexpr int W21_ROWS = 32, W21_COLS = 32, W21_KC = 32;
+constexpr int W21_STAGE = 2 * W21_ROWS * W21_KC + 2 * W21_KC * W21_COLS;  // floats
+constexpr int W21_SMEM = 2 * W21_STAGE * 4;                               // 32 KB
 
-__global__ void __launch_bounds__(256, 2) k_w21(int rows, CMat<float> A21, const float* __restrict__ Dr,
-                                                const float* __restrict__ Di, float* __restrict__ Wr,
-                                                float* __restrict__ Wi) {
+__global__ void __launch_bounds__(128) k_w21(int rows, CMat<float> A21, const float* __restrict__ Dr,
+                                             const float* __restrict__ Di, float* __restrict__ Wr,
+                                             float* __restrict__ Wi) {
     extern __shared__ __align__(16) float w21_smem[];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int r0 = blockIdx.x * W21_ROWS;
-    auto stage = [&](int b) { return w21_smem + (size_t)b * (2 * W21_ROWS * W21_KC + 2 * W21_KC * 128); };
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
+    const int r0 = blockIdx.x * W21_ROWS, c0 = blockIdx.y * W21_COLS;
     auto issue = [&](int c, int b) {
-        float* sA = stage(b);              // [2][32 rows][32 k]
-        float* sB = sA + 2 * W21_ROWS * W21_KC;  // [2][32 k][128]
+        float* sA = w21_smem + (size_t)b * W21_STAGE;   // [2][32 rows][32 k]
+        float* sB = sA + 2 * W21_ROWS * W21_KC;          // [2][32 k][32 cols]
         const int k0 = c * W21_KC;
-        for (int e = tid; e < 2 * W21_ROWS * (W21_KC / 4); e += 256) {
-            const int pl = e / (W21_ROWS * 8), rem = e % (W21_ROWS * 8), r = rem / 8, q = rem % 8;
+        for (int e = tid; e < 2 * W21_ROWS * (W21_KC / 4); e += 128) {
+            const int pl = e / (W21_ROWS * 8), rm = e % (W21_ROWS * 8), r = rm / 8, q = rm % 8;
             const int gr = min(r0 + r, rows - 1);  // rows past the end copy a valid row; never stored
             const float* src = (pl ? A21.im : A21.re) + (size_t)gr * A21.ld + k0 + 4 * q;
             const unsigned dst = (unsigned)__cvta_generic_to_shared(sA + (size_t)pl * W21_ROWS * W21_KC + r * W21_KC + 4 * q);
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
         }
-        for (int e = tid; e < 2 * W21_KC * 32; e += 256) {
-            const int pl = e / (W21_KC * 32), rem = e % (W21_KC * 32), k = rem / 32, q = rem % 32;
-            const float* src = (pl ? Di : Dr) + (size_t)(k0 + k) * 128 + 4 * q;
-            const unsigned dst = (unsigned)__cvta_generic_to_shared(sB + (size_t)pl * W21_KC * 128 + k * 128 + 4 * q);
+        for (int e = tid; e < 2 * W21_KC * (W21_COLS / 4); e += 128) {
+            const int pl = e / (W21_KC * 8), rm = e % (W21_KC * 8), k = rm / 8, q = rm % 8;
+            const float* src = (pl ? Di : Dr) + (size_t)(k0 + k) * 128 + c0 + 4 * q;
+            const unsigned dst = (unsigned)__cvta_generic_to_shared(sB + (size_t)pl * W21_KC * W21_COLS + k * W21_COLS + 4 * q);
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    float cr[2][8], ci[2][8];
+    float cr[2][4], ci[2][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { cr[i][j] = 0.f; ci[i][j] = 0.f; }
+        for (int j = 0; j < 4; ++j) { cr[i][j] = 0.f; ci[i][j] = 0.f; }
     issue(0, 0);
     constexpr int NC = 128 / W21_KC;
     for (int c = 0; c < NC; ++c) {
@@ -421,21 +422,18 @@ __global__ void __launch_bounds__(256, 2) k_w21(int rows, CMat<float> A21, const
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        const float* sA = stage(c & 1);
+        const float* sA = w21_smem + (size_t)(c & 1) * W21_STAGE;
         const float* sB = sA + 2 * W21_ROWS * W21_KC;
-#pragma unroll 4
+#pragma unroll 8
         for (int k = 0; k < W21_KC; ++k) {
             const float ar0 = sA[(2 * ty) * W21_KC + k], ar1 = sA[(2 * ty + 1) * W21_KC + k];
             const float ai0 = sA[W21_ROWS * W21_KC + (2 * ty) * W21_KC + k];
             const float ai1 = sA[W21_ROWS * W21_KC + (2 * ty + 1) * W21_KC + k];
-            const float4 b0 = *reinterpret_cast<const float4*>(sB + k * 128 + 8 * tx);
-            const float4 b1 = *reinterpret_cast<const float4*>(sB + k * 128 + 8 * tx + 4);
-            const float4 c0 = *reinterpret_cast<const float4*>(sB + W21_KC * 128 + k * 128 + 8 * tx);
-            const float4 c1 = *reinterpret_cast<const float4*>(sB + W21_KC * 128 + k * 128 + 8 * tx + 4);
-            const float br[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-            const float bi[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+            const float4 b = *reinterpret_cast<const float4*>(sB + k * W21_COLS + 4 * tx);
+            const float4 d = *reinterpret_cast<const float4*>(sB + W21_KC * W21_COLS + k * W21_COLS + 4 * tx);
+            const float br[4] = {b.x, b.y, b.z, b.w}, bi[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < 4; ++j) {
                 cr[0][j] = fmaf(ar0, br[j], fmaf(-ai0, bi[j], cr[0][j]));
                 ci[0][j] = fmaf(ar0, bi[j], fmaf(ai0, br[j], ci[0][j]));
                 cr[1][j] = fmaf(ar1, br[j], fmaf(-ai1, bi[j], cr[1][j]));
@@ -448,12 +446,8 @@ __global__ void __launch_bounds__(256, 2) k_w21(int rows, CMat<float> A21, const
     for (int i = 0; i < 2; ++i) {
         const int r = r0 + 2 * ty + i;
         if (r >= rows) continue;
-        float* wr = Wr + (size_t)r * 128 + 8 * tx;
-        float* wi = Wi + (size_t)r * 128 + 8 * tx;
-        *reinterpret_cast<float4*>(wr) = make_float4(cr[i][0], cr[i][1], cr[i][2], cr[i][3]);
-        *reinterpret_cast<float4*>(wr + 4) = make_float4(cr[i][4], cr[i][5], cr[i][6], cr[i][7]);
-        *reinterpret_cast<float4*>(wi) = make_float4(ci[i][0], ci[i][1], ci[i][2], ci[i][3]);
-        *reinterpret_cast<float4*>(wi + 4) = make_float4(ci[i][4], ci[i][5], ci[i][6], ci[i][7]);
+        *reinterpret_cast<float4*>(Wr + (size_t)r * 128 + c0 + 4 * tx) = make_float4(cr[i][0], cr[i][1], cr[i][2], cr[i][3]);
+        *reinterpret_cast<float4*>(Wi + (size_t)r * 128 + c0 + 4 * tx) = make_float4(ci[i][0], ci[i][1], ci[i][2], ci[i][3]);
     }
 }
 
@@ -506,8 +500,8 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         if (rem > 0) {
             CMat<float> Dinv{invr + (size_t)k * NB * NB, invi + (size_t)k * NB * NB, NB};
             CMat<float> A21{A.re + (size_t)(k0 + NB) * A.ld + k0, A.im + (size_t)(k0 + NB) * A.ld + k0, A.ld};
-            BEM_LAUNCH(k_w21<<<(rem + W21_ROWS - 1) / W21_ROWS, 256, W21_SMEM, sp>>>(rem, A21, Dinv.re, Dinv.im, wlr,
-                                                                                     wli));
+            BEM_LAUNCH(k_w21<<<dim3((rem + W21_ROWS - 1) / W21_ROWS, 128 / W21_COLS), 128, W21_SMEM, sp>>>(
+                rem, A21, Dinv.re, Dinv.im, wlr, wli));
             float* wtr = wutb(k);
             BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
                 rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
