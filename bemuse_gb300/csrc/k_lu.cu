@@ -745,10 +745,11 @@ __global__ void __launch_bounds__(NB * TPR) k_trsv_coop(int nblk, int R, CMat<T>
                 Xout[2 * (row * R + j) + 1] = ai_[u];
             }
         }
-        __threadfence();
-        __syncthreads();
-        if (tid == 0)
+        __syncthreads();  // all stores of the block, then one fence + release store of its flag
+        if (tid == 0) {
+            __threadfence();
             asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(ready + b), "r"(epoch) : "memory");
+        }
     }
 }
 
@@ -914,8 +915,10 @@ __global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_sub(int nblk, int R, CMa
                 }
                 reinterpret_cast<float2*>(dst)[(row0 + i) * R + j] = o;
             }
-            __threadfence();
+            // the CTA barrier orders every thread's stores before thread 0's fence and
+            // release store of the flag (release is cumulative), as in a grid barrier
             __syncthreads();
+            if (tid == 0) __threadfence();
         };
         if (which == 0) {
             reduce_out(Yin, Xout);
