@@ -17,7 +17,8 @@ from . import build as _build
 __all__ = [
     "BEMError", "lib", "Parameter", "Mesh", "Half_Cylinder", "Barge", "unify",
     "Hydrodynamic_Radiation_Solver", "Aerodynamic_Solver", "NACA_Wing", "havelock_gf", "dense_solve",
-    "PLAIN_FP64", "MIXED",
+    "PLAIN_FP64", "MIXED", "read_mesh", "GDF_Geometry", "MAR_Geometry", "STL_Geometry", "PNL_Geometry",
+    "write_wamit",
 ]
 
 PLAIN_FP64 = 0
@@ -106,6 +107,8 @@ def lib():
         "bem_havelock_throughput": ([c_int, c_int, c_int, _dp], c_int),
         "bem_batch_solve": ([c_int, c_int, ctypes.POINTER(_Mesh), ctypes.POINTER(_Props), c_double, c_double, c_int,
                              _dp, c_int, _dp, c_int, c_double, c_int, ctypes.POINTER(_Result), _dp], c_int),
+        "bem_read_mesh": ([ctypes.c_char_p, c_int, _ip, _dp, _ip, _ip], c_int),
+        "bem_read_mesh_error": ([], ctypes.c_char_p),
         "bem_write_wamit": ([ctypes.c_char_p, ctypes.POINTER(_WamitInfo), c_int, _dp, ctypes.POINTER(_Result)], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
@@ -236,6 +239,46 @@ def unify(meshes, origins):
     if an and len(an) == len(meshes):
         aux = Mesh(np.concatenate(an), np.concatenate(ae), afirst, org)
     return Mesh(np.concatenate(nodes), np.concatenate(elems), first, org, aux=aux)
+
+
+MESH_FORMATS = {"auto": 0, "gdf": 1, "mar": 2, "stl": 3, "pnl": 4}
+
+
+def read_mesh(path, fmt="auto"):
+    """A mesh file as a Mesh, read by the rules of the reference's importers:
+    GDF (GDF_Geo.cpp:12-103), MAR (MAR_Geo.cpp:12-96), ASCII STL (STL_Geo.cpp:12-94,
+    positions x 100) and PNL (PNL_Geo.cpp:17-129); ``fmt="auto"`` picks by extension."""
+    code = MESH_FORMATS[fmt.lower()]
+    nn, ne = ctypes.c_int(), ctypes.c_int()
+    rc = lib().bem_read_mesh(str(path).encode(), code, ctypes.byref(nn), None, ctypes.byref(ne), None)
+    if rc != 0:
+        raise BEMError(rc, lib().bem_read_mesh_error().decode())
+    nodes = np.zeros((max(nn.value, 1), 3))
+    elems = np.zeros((max(ne.value, 1), 4), np.int32)
+    rc = lib().bem_read_mesh(str(path).encode(), code, ctypes.byref(nn), _p(nodes), ctypes.byref(ne), _p(elems, _ip))
+    if rc != 0:
+        raise BEMError(rc, lib().bem_read_mesh_error().decode())
+    return Mesh(nodes[:nn.value], elems[:ne.value])
+
+
+def GDF_Geometry(path):
+    """The reference's GDF_Geometry importer (GDF_Geo.cpp)."""
+    return read_mesh(path, "gdf")
+
+
+def MAR_Geometry(path):
+    """The reference's MAR_Geometry importer (MAR_Geo.cpp), NEMOH meshes."""
+    return read_mesh(path, "mar")
+
+
+def STL_Geometry(path):
+    """The reference's STL_Geometry importer (STL_Geo.cpp), ASCII STL scaled by 100."""
+    return read_mesh(path, "stl")
+
+
+def PNL_Geometry(path):
+    """The reference's PNL_Geometry importer (PNL_Geo.cpp), HAMS meshes."""
+    return read_mesh(path, "pnl")
 
 
 def write_wamit(prefix, omegas, out, betas, M, C, volume, cob, cog, rho=1025.0, gravity=9.81):

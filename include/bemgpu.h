@@ -278,6 +278,22 @@ bem_status bem_mlp_throughput(bem_mlp* m, int n, double* mlp_evals_per_s);
  * time) on n resident points; precision as for bem_havelock. */
 bem_status bem_havelock_throughput(int device, int n, int precision, double* evals_per_s);
 
+/* ---- mesh import --------------------------------------------------------------
+ * Reads the mesh files the reference imports, with the reference readers'
+ * rules: GDF (GDF_Geometry, GDF_Geo.cpp:12-103), MAR (NEMOH; MAR_Geometry,
+ * MAR_Geo.cpp:12-96), ASCII STL (STL_Geometry, STL_Geo.cpp:12-94: positions x
+ * 100, corners stored C3 C2 C1) and PNL (HAMS; PNL_Geometry, PNL_Geo.cpp:17-129).
+ * BEM_MESH_AUTO picks the reader from ".gdf" / ".mar" / ".stl" / ".pnl" in
+ * the path, as the console does (BEMUser_Console.cpp:40-42).  Elements follow
+ * the bem_mesh convention (four 0-based node indices, -1 for a triangle's
+ * fourth).  Call with nodes == NULL or elems == NULL for the sizes, then with
+ * arrays of *n_nodes x 3 doubles and *n_elems x 4 ints.  A malformed line (the
+ * reference's std::stod / std::stoi throw) or a panel naming a missing node
+ * returns BEM_ERR_ARG, with the reason in bem_read_mesh_error().  Host only. */
+enum { BEM_MESH_AUTO = 0, BEM_MESH_GDF = 1, BEM_MESH_MAR = 2, BEM_MESH_STL = 3, BEM_MESH_PNL = 4 };
+bem_status bem_read_mesh(const char* path, int format, int* n_nodes, double* nodes, int* n_elems, int* elems);
+const char* bem_read_mesh_error(void);
+
 /* ---- result files ----------------------------------------------------------
  * Writes <prefix>.1 .2 .2fk .2sc .4 .hst .mmx in the WAMIT formats of
  * Generate_Output_File_WAMIT / Update_Output_File_WAMIT

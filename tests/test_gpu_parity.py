@@ -206,3 +206,28 @@ def test_batch_solve_matches_single_bodies(bg):
         ref = s.solve_omegas(om)
         for k in ("A", "B", "F"):
             assert normwise(o[k], ref[k]) < 1e-12, k
+
+
+@pytest.mark.gpu
+def test_gdf_import_solves_like_generated_mesh(bg, tmp_path):
+    """A body written to .gdf and read back (GDF_Geo.cpp: unshared nodes per panel)
+    solves to the generated body's coefficients."""
+    m = bg.Half_Cylinder(5.0, 8.0, 16, 3, 5, 0, False)
+    lines = ["gdf round trip", "1.0 9.81", "0 0", str(m.n)]
+    for e in m.elems:
+        ids = [int(i) for i in e if i >= 0]
+        ids += [ids[2]] * (4 - len(ids))
+        lines += ["%.17g %.17g %.17g" % tuple(m.nodes[i]) for i in ids]
+    p = tmp_path / "cyl.gdf"
+    p.write_text("\n".join(lines) + "\n")
+    g = bg.read_mesh(p)
+    assert g.n == m.n
+    om = np.array([0.2, 0.7])
+    out = []
+    for mesh in (m, g):
+        s = bg.Hydrodynamic_Radiation_Solver(precision=bg.PLAIN_FP64)
+        s.Set_Parameters([bg.Parameter("WaveAngle", 0.0)])
+        s.Setup(mesh)
+        out.append(s.solve_omegas(om))
+    for k in ("A", "B", "F"):
+        assert normwise(out[1][k], out[0][k]) < 1e-12, k

@@ -92,3 +92,95 @@ def test_number_format(tmp_path):
         second = f.readline()
     assert first.startswith(" 0" + " " * 13 + "1     1      1234.57")
     assert "-0.000123456" in second
+
+
+def test_read_gdf(tmp_path):
+    """GDF import (GDF_Geo.cpp:12-103): three-field lines are vertices, four make a
+    panel, a repeated third vertex makes a triangle, header lines are skipped."""
+    p = tmp_path / "box.gdf"
+    p.write_text("WAMIT-style header line with words\n"
+                 "1.0 9.80665\n"
+                 "0 0\n"
+                 "2\n"
+                 " 0.0  0.0 -1.0\n"
+                 " 1.0  0.0 -1.0\n"
+                 " 1.0  1.0 -1.0\n"
+                 " 0.0  1.0 -1.0\n"
+                 "0.0 0.0 0.0\r\n"
+                 "0.0 0.0 -1.0\r\n"
+                 "1.0 0.0 -1.0\r\n"
+                 "1.0 0.0 -1.0\r\n"
+                 "9 9 9 \n")          # trailing blank: four fields, not a vertex
+    m = bg.read_mesh(p)
+    assert m.n == 2
+    assert m.nodes.shape == (7, 3)
+    assert list(m.elems[0]) == [0, 1, 2, 3]
+    assert list(m.elems[1]) == [4, 5, 6, -1]
+    assert np.allclose(m.nodes[2], [1.0, 1.0, -1.0])
+    bad = tmp_path / "bad.gdf"
+    bad.write_text("a b c\n")
+    with pytest.raises(bg.BEMError):
+        bg.GDF_Geometry(bad)
+
+
+def test_read_mar(tmp_path):
+    """NEMOH .mar (MAR_Geo.cpp:12-96): nodes until a four-field line with id 0, then
+    1-based panels; third == fourth (as text) is a triangle."""
+    p = tmp_path / "hull.mar"
+    p.write_text("2 0\n"
+                 "1 0.0 0.0 -1.0\n"
+                 "2 1.0 0.0 -1.0\n"
+                 "3 1.0 1.0 -1.0\n"
+                 "4 0.0 1.0 -1.0\n"
+                 "0 0.00 0.00 0.00\n"
+                 "1 2 3 4\n"
+                 "1 3 4 4\n"
+                 "0 0 0 0\n")
+    m = bg.MAR_Geometry(p)
+    assert m.nodes.shape == (4, 3)
+    assert m.elems.tolist() == [[0, 1, 2, 3], [0, 2, 3, -1]]
+    q = tmp_path / "broken.mar"
+    q.write_text("1 0 0 0\n0 0 0 0\n1 2 3 4\n")
+    with pytest.raises(bg.BEMError, match="does not exist"):
+        bg.read_mesh(q)
+
+
+def test_read_stl(tmp_path):
+    """ASCII STL (STL_Geo.cpp:12-94): positions x 100, corners stored C3 C2 C1."""
+    p = tmp_path / "tri.stl"
+    p.write_text("solid t\n"
+                 "  facet normal 0 0 1\n"
+                 "    outer loop\n"
+                 "      vertex 0 0 -0.01\n"
+                 "      vertex 0.01 0 -0.01\n"
+                 "      vertex 0 0.01 -0.01\n"
+                 "    endloop\n"
+                 "  endfacet\n"
+                 "endsolid t\n")
+    m = bg.read_mesh(p)
+    assert m.nodes.shape == (3, 3)
+    assert np.allclose(m.nodes, [[0, 0, -1], [1, 0, -1], [0, 1, -1]])
+    assert m.elems.tolist() == [[2, 1, 0, -1]]
+
+
+def test_read_pnl(tmp_path):
+    """HAMS .pnl (PNL_Geo.cpp:17-129): sections by marker lines, 1-based panels with
+    their vertex count."""
+    p = tmp_path / "hull.pnl"
+    p.write_text("    --------------Hull Mesh File---------------\n\n"
+                 "    # Number of Panels, Nodes, X-Symmetry and Y-Symmetry\n"
+                 "         2         5         0         0\n\n"
+                 "    #Start Definition of Node Coordinates     ! node_number   x   y   z\n"
+                 "    1   0.0  0.0  -1.0\n"
+                 "    2   1.0  0.0  -1.0\n"
+                 "    3   1.0  1.0  -1.0\n"
+                 "    4   0.0  1.0  -1.0\n"
+                 "    5   2.0  0.0  -1.0\n"
+                 "    #End Definition of Node Coordinates\n\n"
+                 "    #Start Definition of Node Relations   ! panel_number  number_of_vertices   Vertex1_ID\n"
+                 "    1   4   1   2   3   4\n"
+                 "    2   3   2   5   3\n"
+                 "    #End Definition of Node Relations\n")
+    m = bg.PNL_Geometry(p)
+    assert m.nodes.shape == (5, 3)
+    assert m.elems.tolist() == [[0, 1, 2, 3], [1, 4, 2, -1]]
