@@ -97,7 +97,8 @@ struct LuStreams {
     int rest_tiles;         // tiles per trailing-update CTA when reserve_sms == 0
     cudaEvent_t* timeline;  // optional, 6 timing events per block step (see lu_factor_f32_lookahead)
 };
-// wl2, wut2: two [2][n][128] buffers each (4 n 128 floats).
+// wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus a [2][128][128]
+// transposed diagonal-block inverse (4 n 128 + 32768 floats).
 int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                             float* wl2, float* wut2, int* flags);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place,

@@ -253,7 +253,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_wl32, (size_t)4 * Np * nb32);  // two [2][Np][128] buffers (lookahead)
         DA(ctx->d_wu32, (size_t)2 * Np * nb32);
-        DA(ctx->d_wut32, (size_t)4 * Np * nb32);
+        DA(ctx->d_wut32, (size_t)4 * Np * nb32 + 2 * 128 * 128);  // + transposed D^-1 block
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
     }

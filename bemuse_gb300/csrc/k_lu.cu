@@ -24,6 +24,7 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
                         int* flags);
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
                     int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape);
+bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
 constexpr int IV_THREADS = 256;
 
 __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A, float* invr, float* invi,
-                                                          int* flags) {
+                                                          float* dT, int* flags) {
     __shared__ __align__(16) float4 nrow[2][4 * 16];  // [buffer][chunk q][column group]
     __shared__ __align__(16) float4 ccol[2][4 * 16];  // [buffer][chunk q][row group]
     const int t = threadIdx.x, cg = t & 15, rg = t >> 4, lane = t & 31;
@@ -239,8 +240,19 @@ __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A,
         *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
         *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
     }
+    if (dT) {  // the transpose, [2][128][128]: the K-major B operand of W21 = A21 D^-1
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const size_t g = (size_t)(8 * cg + c) * 128 + 8 * rg;
+            *reinterpret_cast<float4*>(dT + g) = make_float4(v[0][c].x, v[1][c].x, v[2][c].x, v[3][c].x);
+            *reinterpret_cast<float4*>(dT + g + 4) = make_float4(v[4][c].x, v[5][c].x, v[6][c].x, v[7][c].x);
+            *reinterpret_cast<float4*>(dT + 16384 + g) = make_float4(v[0][c].y, v[1][c].y, v[2][c].y, v[3][c].y);
+            *reinterpret_cast<float4*>(dT + 16384 + g + 4) = make_float4(v[4][c].y, v[5][c].y, v[6][c].y, v[7][c].y);
+        }
+    }
     if (lf) atomicOr(flags, lf);
 }
+
 
 // ---------------------------------------------------------------------------
 // C = beta C + sgn * A B, planar complex, row-major.  M, N multiples of 64,
@@ -342,7 +354,7 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
         if (NB == 128 && sizeof(T) == 4)
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
                                                         reinterpret_cast<float*>(invr), reinterpret_cast<float*>(invi),
-                                                        flags));
+                                                        nullptr, flags));
         else
             BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
@@ -371,84 +383,6 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
         }
     }
     return 0;
-}
-
-// W21 = A21 D^-1 for the FP32 LU (rows x 128 times 128 x 128, planar complex):
-// CTA of 128 threads per 32 x 32 output block (grid rows/32 x 4, so the late,
-// short steps of the LU still spread over many SMs); thread (ty, tx) owns rows
-// 2 ty, 2 ty + 1 and columns 4 tx .. 4 tx + 3 of the block.  The contraction runs
-// in 4 chunks of 32, staged by cp.async into a double buffer (both planes).
-constexpr int W21_ROWS = 32, W21_COLS = 32, W21_KC = 32;
-constexpr int W21_STAGE = 2 * W21_ROWS * W21_KC + 2 * W21_KC * W21_COLS;  // floats
-constexpr int W21_SMEM = 2 * W21_STAGE * 4;                               // 32 KB
-
-__global__ void __launch_bounds__(128) k_w21(int rows, CMat<float> A21, const float* __restrict__ Dr,
-                                             const float* __restrict__ Di, float* __restrict__ Wr,
-                                             float* __restrict__ Wi) {
-    extern __shared__ __align__(16) float w21_smem[];
-    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
-    const int r0 = blockIdx.x * W21_ROWS, c0 = blockIdx.y * W21_COLS;
-    auto issue = [&](int c, int b) {
-        float* sA = w21_smem + (size_t)b * W21_STAGE;   // [2][32 rows][32 k]
-        float* sB = sA + 2 * W21_ROWS * W21_KC;          // [2][32 k][32 cols]
-        const int k0 = c * W21_KC;
-        for (int e = tid; e < 2 * W21_ROWS * (W21_KC / 4); e += 128) {
-            const int pl = e / (W21_ROWS * 8), rm = e % (W21_ROWS * 8), r = rm / 8, q = rm % 8;
-            const int gr = min(r0 + r, rows - 1);  // rows past the end copy a valid row; never stored
-            const float* src = (pl ? A21.im : A21.re) + (size_t)gr * A21.ld + k0 + 4 * q;
-            const unsigned dst = (unsigned)__cvta_generic_to_shared(sA + (size_t)pl * W21_ROWS * W21_KC + r * W21_KC + 4 * q);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-        }
-        for (int e = tid; e < 2 * W21_KC * (W21_COLS / 4); e += 128) {
-            const int pl = e / (W21_KC * 8), rm = e % (W21_KC * 8), k = rm / 8, q = rm % 8;
-            const float* src = (pl ? Di : Dr) + (size_t)(k0 + k) * 128 + c0 + 4 * q;
-            const unsigned dst = (unsigned)__cvta_generic_to_shared(sB + (size_t)pl * W21_KC * W21_COLS + k * W21_COLS + 4 * q);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    float cr[2][4], ci[2][4];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) { cr[i][j] = 0.f; ci[i][j] = 0.f; }
-    issue(0, 0);
-    constexpr int NC = 128 / W21_KC;
-    for (int c = 0; c < NC; ++c) {
-        if (c + 1 < NC) {
-            issue(c + 1, (c + 1) & 1);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
-        __syncthreads();
-        const float* sA = w21_smem + (size_t)(c & 1) * W21_STAGE;
-        const float* sB = sA + 2 * W21_ROWS * W21_KC;
-#pragma unroll 8
-        for (int k = 0; k < W21_KC; ++k) {
-            const float ar0 = sA[(2 * ty) * W21_KC + k], ar1 = sA[(2 * ty + 1) * W21_KC + k];
-            const float ai0 = sA[W21_ROWS * W21_KC + (2 * ty) * W21_KC + k];
-            const float ai1 = sA[W21_ROWS * W21_KC + (2 * ty + 1) * W21_KC + k];
-            const float4 b = *reinterpret_cast<const float4*>(sB + k * W21_COLS + 4 * tx);
-            const float4 d = *reinterpret_cast<const float4*>(sB + W21_KC * W21_COLS + k * W21_COLS + 4 * tx);
-            const float br[4] = {b.x, b.y, b.z, b.w}, bi[4] = {d.x, d.y, d.z, d.w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                cr[0][j] = fmaf(ar0, br[j], fmaf(-ai0, bi[j], cr[0][j]));
-                ci[0][j] = fmaf(ar0, bi[j], fmaf(ai0, br[j], ci[0][j]));
-                cr[1][j] = fmaf(ar1, br[j], fmaf(-ai1, bi[j], cr[1][j]));
-                ci[1][j] = fmaf(ar1, bi[j], fmaf(ai1, br[j], ci[1][j]));
-            }
-        }
-        __syncthreads();  // the buffer is refilled two chunks later
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const int r = r0 + 2 * ty + i;
-        if (r >= rows) continue;
-        *reinterpret_cast<float4*>(Wr + (size_t)r * 128 + c0 + 4 * tx) = make_float4(cr[i][0], cr[i][1], cr[i][2], cr[i][3]);
-        *reinterpret_cast<float4*>(Wi + (size_t)r * 128 + c0 + 4 * tx) = make_float4(ci[i][0], ci[i][1], ci[i][2], ci[i][3]);
-    }
 }
 
 // wut[j][i] = A[r0 + i][c0 + j] for i < 128, j < cols (both planes; wut rows of 128 floats).
@@ -481,27 +415,24 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     // reserve_sms > 0: persistent rest update on nsm - reserve_sms CTAs; 0: CTAs of about
     // four tiles each, which retire during the update and hand SMs to the panel stream
     const int rest_ctas = ls.reserve_sms > 0 ? std::max(1, nsm - ls.reserve_sms) : -std::max(1, ls.rest_tiles);
-    cudaFuncSetAttribute(k_w21, cudaFuncAttributeMaxDynamicSharedMemorySize, W21_SMEM);
     auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
     auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };
     cudaStream_t sp = ls.panel;
-    // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl), U12^T (into wut);
-    // ev_panel marks the operands ready; W21 is then stored into A for the solves.
+    // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl and A21), U12^T
+    // (into wut); ev_panel marks the operands of the step-k updates ready.
     // timeline (optional): per step k, [0] cross update start, [1] cross done (main stream),
     // [2] inverse of block k+1 done, [3] W21 done, [4] panel k+1 ready (panel stream), [5] rest done
     auto mark = [&](int k, int slot, cudaStream_t s) {
         if (ls.timeline && k >= 0 && k < nblk) cudaEventRecord(ls.timeline[6 * k + slot], s);
     };
+    float* dT = wut2 + (size_t)4 * n * NB;  // D_kk^-1 transposed, [2][128][128]
     auto panel = [&](int k) {
         const int k0 = k * NB, rem = n - k0 - NB;
-        BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, flags));
+        BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dT, flags));
         mark(k - 1, 2, sp);
-        float *wlr = wlb(k), *wli = wlb(k) + (size_t)n * NB;
         if (rem > 0) {
-            CMat<float> Dinv{invr + (size_t)k * NB * NB, invi + (size_t)k * NB * NB, NB};
-            CMat<float> A21{A.re + (size_t)(k0 + NB) * A.ld + k0, A.im + (size_t)(k0 + NB) * A.ld + k0, A.ld};
-            BEM_LAUNCH(k_w21<<<dim3((rem + W21_ROWS - 1) / W21_ROWS, 128 / W21_COLS), 128, W21_SMEM, sp>>>(
-                rem, A21, Dinv.re, Dinv.im, wlr, wli));
+            // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)
+            if (!tc_w21(sp, n, k0, A, dT, wlb(k), flags)) return false;
             float* wtr = wutb(k);
             BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
                 rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
@@ -509,16 +440,11 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         mark(k - 1, 3, sp);
         cudaEventRecord(ls.ev_panel, sp);
         mark(k - 1, 4, sp);
-        if (rem > 0) {
-            int nb_ = (int)(((size_t)rem * NB + 255) / 256);
-            if (nb_ > 4096) nb_ = 4096;
-            BEM_LAUNCH(k_copy_back<float><<<nb_, 256, 0, sp>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 0, (float*)nullptr,
-                                                              (float*)nullptr, 0, flags));
-        }
+        return true;
     };
     cudaEventRecord(ls.ev_cross, st);
     cudaStreamWaitEvent(sp, ls.ev_cross, 0);
-    panel(0);
+    if (!panel(0)) return 1;
     for (int k = 0; k < nblk; ++k) {
         cudaStreamWaitEvent(st, ls.ev_panel, 0);
         const int k0 = k * NB, rem = n - k0 - NB;
@@ -530,13 +456,13 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         cudaEventRecord(ls.ev_cross, st);
         mark(k, 1, st);
         cudaStreamWaitEvent(sp, ls.ev_cross, 0);
-        panel(k + 1);
+        if (!panel(k + 1)) return 1;
         if (mt > 1 &&
             !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags, false))
             return 1;
         mark(k, 5, st);
     }
-    // the last stores of W21 into A precede the solves
+    // the last W21 stores into A precede the solves
     cudaEventRecord(ls.ev_panel, sp);
     cudaStreamWaitEvent(st, ls.ev_panel, 0);
     return 0;

@@ -1,5 +1,6 @@
-// k_tc_gemm.cu -- tcgen05 TF32 trailing update of the complex LU:
-//     A22 -= L21 * U12      (planar complex, FP32 storage, FP32 accumulation)
+// k_tc_gemm.cu -- tcgen05 TF32 products of the complex block LU:
+//     A22 -= L21 * U12      (trailing update; planar complex, FP32 storage and accumulation)
+//     W21  = A21 * D^-1     (block-column multipliers, stored to two places)
 //
 // Persistent, warp-specialised kernel over 128 x 128 tiles of A22 (or of any
 // tile-aligned rectangle of it).  The complex product is four real TF32 MMAs
@@ -11,9 +12,10 @@
 //               contraction (four 32-wide k-blocks per tile, continuing across tiles)
 //   warp 1      tcgen05.mma issuer; two TMEM accumulator buffers (Cr | Ci, 256
 //               columns each), so the epilogue of tile i overlaps the MMAs of i+1
-//   warps 2-5   epilogue: tcgen05.ld of a 32-row x 32-column slice, -acc into a
-//               swizzled shared-memory box, and a TMA reduce-add of that box into
-//               A22 (cp.reduce.async.bulk.tensor ... .add): C is never loaded by the SM.
+//   warps 2-5   epilogue: tcgen05.ld of a 32-row x 32-column slice into a swizzled
+//               shared-memory box, then either a TMA reduce-add of -acc into A22
+//               (cp.reduce.async.bulk.tensor ... .add: C is never loaded by the SM)
+//               or TMA stores of +acc into two destinations (the W21 product).
 // Every mbarrier wait has an iteration limit; on expiry the CTA sets
 // FLAG_TIMEOUT, stops issuing work, drains its bulk copies, frees TMEM and exits.
 #include <cuda.h>
@@ -86,6 +88,14 @@ __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x,
                  ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
                  : "memory");
 }
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* m) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
@@ -138,14 +148,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 
 }  // namespace
 
-// Tiles (tm, tn), tm < Mt, tn < Nt, of the rectangle whose L21 rows start at lr0
-// (rows of wl) and U12^T rows at ur0 (rows of wut); the tile lands at A rows
-// crow0 + tm*128, columns ccol0 + tn*128.  nplane: row offset of the imaginary
-// planes in the L and U maps.
+// Tile rectangle and destination of one k_tc_update launch.
+struct TcTiles {
+    int lr0, ur0, Mt, Nt, lshape, crow0, ccol0, mode, c2row0, c2col0;
+};
+
+// Tiles (tm, tn), tm < Mt, tn < Nt, of the rectangle whose L rows start at lr0
+// (rows of mapLr / mapLi) and U rows at ur0 (rows of mapUr / mapUi).  mode 0:
+// the tile's -acc is reduce-added into mapCr / mapCi at rows crow0 + tm*128,
+// columns ccol0 + tn*128.  mode 1: +acc is stored there and at c2row0 + tm*128,
+// c2col0 + tn*128 of mapC2r / mapC2i.
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_tc_update(const __grid_constant__ CUtensorMap mapL, const __grid_constant__ CUtensorMap mapU,
-                const __grid_constant__ CUtensorMap mapCr, const __grid_constant__ CUtensorMap mapCi, int nplane,
-                int lr0, int ur0, int Mt, int Nt, int lshape, int crow0, int ccol0, int* gflags) {
+    k_tc_update(const __grid_constant__ CUtensorMap mapLr, const __grid_constant__ CUtensorMap mapLi,
+                const __grid_constant__ CUtensorMap mapUr, const __grid_constant__ CUtensorMap mapUi,
+                const __grid_constant__ CUtensorMap mapCr, const __grid_constant__ CUtensorMap mapCi,
+                const __grid_constant__ CUtensorMap mapC2r, const __grid_constant__ CUtensorMap mapC2i,
+                const TcTiles a, int* gflags) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;  // 1024-byte aligned (128-byte swizzle atoms)
@@ -159,9 +177,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t tfull0 = smem_u32(bars + 6), tempty0 = smem_u32(bars + 8);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // rectangle: Mt x Nt tiles; L-shape: tile column 0 (Mt tiles) and tile row 0 (Nt - 1 more)
-    const int ntiles = lshape ? Mt + Nt - 1 : Mt * Nt;
+    const int Mt = a.Mt, Nt = a.Nt;
+    const int ntiles = a.lshape ? Mt + Nt - 1 : Mt * Nt;
     auto tile_of = [&](int t, int& tm, int& tn) {
-        if (lshape) { tm = t < Mt ? t : 0; tn = t < Mt ? 0 : t - Mt + 1; }
+        if (a.lshape) { tm = t < Mt ? t : 0; tn = t < Mt ? 0 : t - Mt + 1; }
         else { tm = t / Nt; tn = t % Nt; }
     };
 
@@ -170,10 +189,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(tempty0 + 8 * b, EPI_WARPS); }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapL)) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapU)) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapCr)) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapCi)) : "memory");
+        prefetch_map(&mapLr); prefetch_map(&mapLi); prefetch_map(&mapUr); prefetch_map(&mapUi);
+        prefetch_map(&mapCr); prefetch_map(&mapCi);
+        if (a.mode) { prefetch_map(&mapC2r); prefetch_map(&mapC2i); }
     }
     __syncwarp();
     if (warp == 0) {
@@ -194,16 +212,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 int tm, tn;
                 tile_of(t, tm, tn);
-                const int lrow = lr0 + tm * BM, urow = ur0 + tn * BN;
+                const int lrow = a.lr0 + tm * BM, urow = a.ur0 + tn * BN;
                 for (int kb = 0; kb < KB; ++kb, ++it) {
                     const uint32_t s = it % STAGES, u = it / STAGES;
                     if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
                     const uint32_t st = base + s * STAGE_BYTES;
                     mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-                    tma_load_2d(st, &mapL, kb * BK, lrow, full0 + 8 * s);
-                    tma_load_2d(st + L_TILE, &mapL, kb * BK, nplane + lrow, full0 + 8 * s);
-                    tma_load_2d(st + 2 * L_TILE, &mapU, kb * BK, urow, full0 + 8 * s);
-                    tma_load_2d(st + 2 * L_TILE + U_TILE, &mapU, kb * BK, nplane + urow, full0 + 8 * s);
+                    tma_load_2d(st, &mapLr, kb * BK, lrow, full0 + 8 * s);
+                    tma_load_2d(st + L_TILE, &mapLi, kb * BK, lrow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE, &mapUr, kb * BK, urow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE + U_TILE, &mapUi, kb * BK, urow, full0 + 8 * s);
                 }
             }
         }
@@ -253,7 +271,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             bool have = mbar_wait(tfull0 + 8 * buf, u & 1, abort_flag, gflags);
             if (!__all_sync(0xffffffffu, have)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int row = crow0 + tm * BM + q * 32;
+            const int row = a.crow0 + tm * BM + q * 32, row2 = a.c2row0 + tm * BM + q * 32;
+            const float sgn = a.mode ? 1.f : -1.f;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
 #pragma unroll 1
@@ -266,15 +285,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const uint32_t rowaddr = slot + lane * 128;
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const uint32_t a = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
-                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(-v[4 * j]),
-                                     "f"(-v[4 * j + 1]), "f"(-v[4 * j + 2]), "f"(-v[4 * j + 3])
+                        const uint32_t sa = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
+                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(sgn * v[4 * j]),
+                                     "f"(sgn * v[4 * j + 1]), "f"(sgn * v[4 * j + 2]), "f"(sgn * v[4 * j + 3])
                                      : "memory");
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) {
-                        tma_reduce_add_2d(p ? &mapCi : &mapCr, ccol0 + tn * BN + c * 32, row, slot);
+                        const int col = a.ccol0 + tn * BN + c * 32;
+                        if (a.mode) {
+                            tma_store_2d(p ? &mapCi : &mapCr, col, row, slot);
+                            tma_store_2d(p ? &mapC2i : &mapC2r, a.c2col0 + tn * BN + c * 32, row2, slot);
+                        } else {
+                            tma_reduce_add_2d(p ? &mapCi : &mapCr, col, row, slot);
+                        }
                         bulk_commit();
                     }
                 }
@@ -312,12 +337,13 @@ static EncodeTiledFn get_encode() {
     return fn;
 }
 
-// 2D FP32 tensor of 2n rows x 128 columns (rows [0,n) real part, [n,2n) imaginary).
-static bool make_map(CUtensorMap* m, const float* base, int n, int box_rows) {
+// FP32 operand of rows x 128 columns (row stride ld floats), 32-column x
+// box_rows boxes, 128-byte swizzle: one plane of an L or U operand.
+static bool make_map(CUtensorMap* m, const float* base, int rows, int ld, int box_rows) {
     EncodeTiledFn enc = get_encode();
     if (!enc) return false;
-    cuuint64_t dims[2] = {128, (cuuint64_t)2 * n};
-    cuuint64_t strides[1] = {128 * sizeof(float)};
+    cuuint64_t dims[2] = {128, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
     cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
@@ -333,7 +359,7 @@ int tc_gemm_supported(int device) {
 }
 
 // FP32 matrix of rows x cols (row stride ld floats), 32 x 32 boxes, 128-byte swizzle:
-// the target of the epilogue's TMA reduce-add.
+// the target of the epilogue's TMA reduce-add or store.
 static bool make_map_c(CUtensorMap* m, const float* base, int rows, int cols, int ld) {
     EncodeTiledFn enc = get_encode();
     if (!enc) return false;
@@ -344,6 +370,17 @@ static bool make_map_c(CUtensorMap* m, const float* base, int rows, int cols, in
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static int tc_grid(int ntiles, int max_ctas) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (max_ctas < 0) return (ntiles + (-max_ctas) - 1) / (-max_ctas);
+    int grid = ntiles;
+    if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+    return grid > nsm ? nsm : grid;
 }
 
 // Tile rectangle of the step-k0 update (nb = 128): L21 rows [lr0, lr0 + 128 Mt) of
@@ -358,25 +395,38 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
     if (Mt <= 0 || Nt <= 0) return true;
     if (n % 128 || k0 % 128 || lr0 % 128 || ur0 % 128 || A.ld % 4) return false;
     if (k0 + 128 + lr0 + 128 * Mt > n || k0 + 128 + ur0 + 128 * Nt > n) return false;
-    CUtensorMap mL, mU, mCr, mCi;
-    if (!make_map(&mL, wl, n, BM) || !make_map(&mU, wut, n, BN) || !make_map_c(&mCr, A.re, n, n, A.ld) ||
-        !make_map_c(&mCi, A.im, n, n, A.ld))
+    CUtensorMap mLr, mLi, mUr, mUi, mCr, mCi;
+    const size_t plane = (size_t)n * 128;
+    if (!make_map(&mLr, wl, n, 128, BM) || !make_map(&mLi, wl + plane, n, 128, BM) ||
+        !make_map(&mUr, wut, n, 128, BN) || !make_map(&mUi, wut + plane, n, 128, BN) ||
+        !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
         return false;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    int nsm = 0;
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int ntiles = lshape ? Mt + Nt - 1 : Mt * Nt;
-    int grid = ntiles;
-    if (max_ctas < 0) {
-        grid = (ntiles + (-max_ctas) - 1) / (-max_ctas);
-    } else {
-        if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-        if (grid > nsm) grid = nsm;
-    }
-    BEM_LAUNCH(k_tc_update<<<grid, NTHREADS, SMEM_BYTES, st>>>(mL, mU, mCr, mCi, n, lr0, ur0, Mt, Nt, lshape ? 1 : 0,
-                                                              k0 + 128 + lr0, k0 + 128 + ur0, flags));
+    const TcTiles a{lr0, ur0, Mt, Nt, lshape ? 1 : 0, k0 + 128 + lr0, k0 + 128 + ur0, 0, 0, 0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi,
+                                                                                   mCr, mCi, a, flags));
+    return true;
+}
+
+// W21 = A21 D^-1 for the block column at k0 (nb = 128, rem = n - k0 - 128 rows):
+// A21 is read in place from A, D^-1 as its transpose dT ([2][128][128], row j =
+// column j of D^-1); the product is stored into w ([2][n][128], rows from 0)
+// and over A21 in A.  Each tile reads its A21 rows before it overwrites them.
+bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags) {
+    const int rem = n - k0 - 128;
+    if (rem <= 0) return true;
+    if (n % 128 || k0 % 128 || A.ld % 4) return false;
+    CUtensorMap mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i;
+    const size_t plane = (size_t)n * 128;
+    if (!make_map(&mLr, A.re + k0, n, A.ld, BM) || !make_map(&mLi, A.im + k0, n, A.ld, BM) ||
+        !make_map(&mUr, dT, 128, 128, BN) || !make_map(&mUi, dT + 128 * 128, 128, 128, BN) ||
+        !make_map_c(&mCr, w, n, 128, 128) || !make_map_c(&mCi, w + plane, n, 128, 128) ||
+        !make_map_c(&mC2r, A.re, n, n, A.ld) || !make_map_c(&mC2i, A.im, n, n, A.ld))
+        return false;
+    const int mt = rem / 128;
+    const TcTiles a{k0 + 128, 0, mt, 1, 0, 0, 0, 1, k0 + 128, k0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, 0), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i, a,
+                                                                        flags));
     return true;
 }
 

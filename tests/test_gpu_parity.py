@@ -213,7 +213,7 @@ def test_gdf_import_solves_like_generated_mesh(bg, tmp_path):
     """A body written to .gdf and read back (GDF_Geo.cpp: unshared nodes per panel)
     solves to the generated body's coefficients."""
     m = bg.Half_Cylinder(5.0, 8.0, 16, 3, 5, 0, False)
-    lines = ["gdf round trip", "1.0 9.81", "0 0", str(m.n)]
+    lines = ["round trip of a cylinder mesh", "1.0 9.81", "0 0", str(m.n)]
     for e in m.elems:
         ids = [int(i) for i in e if i >= 0]
         ids += [ids[2]] * (4 - len(ids))
