@@ -50,12 +50,20 @@ class _Props(ctypes.Structure):
 class _WamitInfo(ctypes.Structure):
     _fields_ = [("n_beta", ctypes.c_int), ("betas", _dp), ("rho", ctypes.c_double), ("gravity", ctypes.c_double),
                 ("M", ctypes.c_double * 36), ("C", ctypes.c_double * 36), ("volume", ctypes.c_double),
-                ("cob", ctypes.c_double * 3), ("cog", ctypes.c_double * 3)]
+                ("cob", ctypes.c_double * 3), ("cog", ctypes.c_double * 3), ("n_kochin", ctypes.c_int),
+                ("n_wave", ctypes.c_int), ("wave_points", _dp)]
+
+
+class _SummaryInfo(ctypes.Structure):
+    _fields_ = [("w", ctypes.POINTER(_WamitInfo)), ("n_nodes", ctypes.c_int), ("n_elems", ctypes.c_int),
+                ("n_aux_elems", ctypes.c_int), ("surface_area", ctypes.c_double), ("mass", ctypes.c_double),
+                ("file_info", ctypes.c_char_p)]
 
 
 class _Result(ctypes.Structure):
     _fields_ = [("A", _dp), ("B", _dp), ("FK", _dp), ("SC", _dp), ("F", _dp), ("RAO", _dp),
-                ("refine_iters", _ip), ("residual", _dp), ("phi_rad", _dp), ("phi_scat", _dp)]
+                ("refine_iters", _ip), ("residual", _dp), ("phi_rad", _dp), ("phi_scat", _dp),
+                ("fs_rad", _dp), ("fs_diff", _dp), ("kochin_rad", _dp), ("kochin_diff", _dp)]
 
 
 _LIB = None
@@ -108,7 +116,11 @@ def lib():
         "bem_batch_solve": ([c_int, c_int, ctypes.POINTER(_Mesh), ctypes.POINTER(_Props), c_double, c_double, c_int,
                              _dp, c_int, _dp, c_int, c_double, c_int, ctypes.POINTER(_Result), _dp], c_int),
         "bem_read_mesh": ([ctypes.c_char_p, c_int, _ip, _dp, _ip, _ip], c_int),
+        "bem_set_wave_points": ([vp, c_int, _dp], c_int),
+        "bem_set_kochin": ([vp, c_int], c_int),
         "bem_read_mesh_error": ([], ctypes.c_char_p),
+        "bem_write_bem": ([ctypes.c_char_p, ctypes.POINTER(_SummaryInfo), c_int, _dp, ctypes.POINTER(_Result)],
+                          c_int),
         "bem_write_wamit": ([ctypes.c_char_p, ctypes.POINTER(_WamitInfo), c_int, _dp, ctypes.POINTER(_Result)], c_int),
         "bem_launch_count": ([], ctypes.c_ulonglong),
         "bem_mesh_wing_sizes": ([c_int, c_int, _ip, _ip], c_int),
@@ -281,11 +293,13 @@ def PNL_Geometry(path):
     return read_mesh(path, "pnl")
 
 
-def write_wamit(prefix, omegas, out, betas, M, C, volume, cob, cog, rho=1025.0, gravity=9.81):
-    """WAMIT-format result files (.1 .2 .2fk .2sc .4 .hst .mmx) as the reference's
+def write_wamit(prefix, omegas, out, betas, M, C, volume, cob, cog, rho=1025.0, gravity=9.81, wave_points=None):
+    """WAMIT-format result files (.1 .2 .2fk .2sc .4 .6 .hst .mmx, _KochinRad.bem,
+    _KochinDiff.bem, and with wave points .6r and _WaveElPos.bem) as the reference's
     Generate/Update_Output_File_WAMIT write them (Hydrodynamic_Solver_IO.cpp:430-646).
-    omegas are the internal angular frequencies; out holds A, B (nf x 6 x 6) and
-    FK, SC, F, RAO (nf x 6 x nb complex)."""
+    omegas are the internal angular frequencies; out holds A, B (nf x 6 x 6),
+    FK, SC, F, RAO (nf x 6 x nb complex) and optionally kochin_rad / kochin_diff and
+    fs_rad from solve_omegas."""
     om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
     betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
     info = _WamitInfo()
@@ -296,15 +310,82 @@ def write_wamit(prefix, omegas, out, betas, M, C, volume, cob, cog, rho=1025.0, 
     info.C[:] = list(np.asarray(C, dtype=np.float64).ravel())
     info.cob[:] = list(np.asarray(cob, dtype=np.float64).ravel())
     info.cog[:] = list(np.asarray(cog, dtype=np.float64).ravel())
-    keep = {k: np.ascontiguousarray(out[k]) for k in ("A", "B", "FK", "SC", "F", "RAO") if k in out}
+    keys = ("A", "B", "FK", "SC", "F", "RAO", "kochin_rad", "kochin_diff", "fs_rad")
+    keep = {k: np.ascontiguousarray(out[k]) for k in keys if k in out}
     res = _Result()
     res.A = _p(keep["A"]) if "A" in keep else None
     res.B = _p(keep["B"]) if "B" in keep else None
-    for k in ("FK", "SC", "F", "RAO"):
+    for k in keys[2:]:
         setattr(res, k, _p(keep[k].view(np.float64)) if k in keep else None)
+    if "kochin_rad" in keep:
+        info.n_kochin = keep["kochin_rad"].shape[1]
+    elif "kochin_diff" in keep:
+        info.n_kochin = keep["kochin_diff"].shape[1]
+    wp = None
+    if wave_points is not None and "fs_rad" in keep:
+        wp = np.ascontiguousarray(wave_points, dtype=np.float64).reshape(-1, 3)
+        info.n_wave = wp.shape[0]
+        info.wave_points = _p(wp)
+    elif "fs_rad" in keep:
+        res.fs_rad = None
     rc = lib().bem_write_wamit(str(prefix).encode(), ctypes.byref(info), om.size, _p(om), ctypes.byref(res))
     if rc != 0:
-        raise BEMError("bem_write_wamit failed (status %d)" % rc)
+        raise BEMError(rc, "bem_write_wamit could not write %s.*" % prefix)
+
+
+def panel_areas(mesh):
+    """Flat-panel areas (Geo_Elements.cpp: quads 1/2 |d1 x d2|, triangles 1/2 |e1 x e2|)."""
+    nodes = mesh.nodes
+    e = mesh.elems
+    p0, p1, p2 = nodes[e[:, 0]], nodes[e[:, 1]], nodes[e[:, 2]]
+    p3 = nodes[np.where(e[:, 3] >= 0, e[:, 3], e[:, 0])]
+    quad = 0.5 * np.linalg.norm(np.cross(p2 - p0, p3 - p1), axis=1)
+    tri = 0.5 * np.linalg.norm(np.cross(p1 - p0, p2 - p0), axis=1)
+    return np.where(e[:, 3] >= 0, quad, tri)
+
+
+def write_bem(prefix, omegas, out, betas, M, C, volume, cob, cog, mesh=None, mass=0.0, n_aux=0, file_info=""):
+    """The .bem summary file of Generate/Update_Output_File_BEMUse
+    (Hydrodynamic_Solver_IO.cpp:107-426)."""
+    om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
+    betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
+    w = _WamitInfo()
+    w.n_beta = betas.size
+    w.betas = _p(betas)
+    w.rho, w.gravity, w.volume = 1025.0, 9.81, float(volume)
+    w.M[:] = list(np.asarray(M, dtype=np.float64).ravel())
+    w.C[:] = list(np.asarray(C, dtype=np.float64).ravel())
+    w.cob[:] = list(np.asarray(cob, dtype=np.float64).ravel())
+    w.cog[:] = list(np.asarray(cog, dtype=np.float64).ravel())
+    info = _SummaryInfo()
+    info.w = ctypes.pointer(w)
+    if mesh is not None:
+        info.n_nodes, info.n_elems = mesh.nodes.shape[0], mesh.elems.shape[0]
+        info.surface_area = float(np.sum(panel_areas(mesh)))
+    info.n_aux_elems = int(n_aux)
+    info.mass = float(mass)
+    info.file_info = file_info.encode()
+    keep = {k: np.ascontiguousarray(out[k]) for k in ("A", "B", "FK", "F") if k in out}
+    res = _Result()
+    res.A = _p(keep["A"]) if "A" in keep else None
+    res.B = _p(keep["B"]) if "B" in keep else None
+    res.FK = _p(keep["FK"].view(np.float64)) if "FK" in keep else None
+    res.F = _p(keep["F"].view(np.float64)) if "F" in keep else None
+    rc = lib().bem_write_bem(str(prefix).encode(), ctypes.byref(info), om.size, _p(om), ctypes.byref(res))
+    if rc != 0:
+        raise BEMError(rc, "bem_write_bem could not write %s.bem" % prefix)
+
+
+def barge_free_surface_points(LFS, WFS, NXFS, NYFS):
+    """The Barge free-surface grid (Barge.cpp:125-140): (NXFS+1) x (NYFS+1) nodes over
+    LFS x WFS, x-major, pushed out by the factor 1.001, at z = 0."""
+    pts = []
+    for i in range(NXFS + 1):
+        for j in range(NYFS + 1):
+            x = -0.5 * LFS + LFS * i / NXFS
+            y = -0.5 * WFS + WFS * j / NYFS
+            pts.append((1.001 * x, 1.001 * y, 0.0))
+    return np.array(pts)
 
 
 class Hydrodynamic_Radiation_Solver:
@@ -357,6 +438,9 @@ class Hydrodynamic_Radiation_Solver:
                 self.Grav = float(val)
             elif name == "IFR" and val:
                 raise BEMError(6, "irregular-frequency removal is not implemented")
+            elif name == "NKochin":
+                self.NKochin = int(val)
+                _check(lib().bem_set_kochin(self._h, self.NKochin), self._h)
         b = np.asarray(self.BetaArray, dtype=np.float64)
         _check(lib().bem_set_params(self._h, self.Rho, self.Grav, b.size, _p(b) if b.size else None), self._h)
 
@@ -392,7 +476,15 @@ class Hydrodynamic_Radiation_Solver:
     def write_wamit(self, prefix, omegas, out):
         """Result files of solve_omegas(omegas) in the reference's WAMIT formats."""
         write_wamit(prefix, omegas, out, self.BetaArray, self.M_ij, self.C_ij,
-                    self.Volume, self.Centre_Buoyancy, self.cog, rho=self.Rho, gravity=self.Grav)
+                    self.Volume, self.Centre_Buoyancy, self.cog, rho=self.Rho, gravity=self.Grav,
+                    wave_points=getattr(self, "wave_points", None))
+
+    def write_bem(self, prefix, omegas, out, file_info=""):
+        """The .bem summary file of solve_omegas(omegas) (Hydrodynamic_Solver_IO.cpp:107-426)."""
+        aux = getattr(self.mesh, "aux", None)
+        write_bem(prefix, omegas, out, self.BetaArray, self.M_ij, self.C_ij, self.Volume, self.Centre_Buoyancy,
+                  self.cog, mesh=self.mesh, mass=self.M_ij[0][0], n_aux=0 if aux is None else aux.n,
+                  file_info=file_info)
 
     def Set_Real(self, D):
         self.Frequency = float(D)
@@ -405,7 +497,17 @@ class Hydrodynamic_Radiation_Solver:
         self.DiffSolArray.append(r["phiS"])
         return r
 
-    def solve_omegas(self, omegas, want_phi=False, precision=None):
+    def set_wave_points(self, xyz):
+        """Exterior free-surface points (n x 3) for the elevation outputs (the
+        reference's Wave_Nodes, Hydrodynamic_Solver.cpp:208-213)."""
+        self.wave_points = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = self.wave_points.shape[0]
+        _check(lib().bem_set_wave_points(self._h, n, _p(self.wave_points) if n else None), self._h)
+
+    def solve_omegas(self, omegas, want_phi=False, precision=None, want_fs=False, want_kochin=False):
+        """Solve at the internal angular frequencies `omegas`.  want_fs adds fs_rad
+        [f][nw][6] and fs_diff [f][nw][nb] (ExtRadMat / ExtDiffMat at the wave points);
+        want_kochin adds kochin_rad [f][nk][6] and kochin_diff [f][nk][nb]."""
         om = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
         nf, nb, N = om.size, self.NBeta, self.N
         out = dict(A=np.zeros((nf, 6, 6)), B=np.zeros((nf, 6, 6)), FK=np.zeros((nf, 6, nb), np.complex128),
@@ -423,6 +525,18 @@ class Hydrodynamic_Radiation_Solver:
             out["phiS"] = np.zeros((N, nb), np.complex128)
             res.phi_rad = _p(out["phiJ"].view(np.float64))
             res.phi_scat = _p(out["phiS"].view(np.float64)) if nb else None
+        if want_fs:
+            nw = getattr(self, "wave_points", np.zeros((0, 3))).shape[0]
+            out["fs_rad"] = np.zeros((nf, nw, 6), np.complex128)
+            out["fs_diff"] = np.zeros((nf, nw, nb), np.complex128)
+            res.fs_rad = _p(out["fs_rad"].view(np.float64))
+            res.fs_diff = _p(out["fs_diff"].view(np.float64)) if nb else None
+        if want_kochin:
+            nk = getattr(self, "NKochin", 36)
+            out["kochin_rad"] = np.zeros((nf, nk, 6), np.complex128)
+            out["kochin_diff"] = np.zeros((nf, nk, nb), np.complex128)
+            res.kochin_rad = _p(out["kochin_rad"].view(np.float64))
+            res.kochin_diff = _p(out["kochin_diff"].view(np.float64)) if nb else None
         prec = self.precision if precision is None else precision
         _check(lib().bem_solve(self._h, nf, _p(om), int(prec), float(self.refine_tol), ctypes.byref(res)), self._h)
         return out

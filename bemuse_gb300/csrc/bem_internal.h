@@ -50,6 +50,14 @@ cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
                     double* o0, double* o1, double* o2, double* o3);
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
+// Exterior outputs after a solve (X = [Phi_J | Phi_S], N x (6 + NB) complex):
+// free-surface elevation at NW points wp ([3][NW]) and Kochin functions at NK angles;
+// out: [NW or NK][6 + NB] complex interleaved.
+void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int NW, const double* wp, const double* rec,
+                         const double* rn, double Omega, int NB, const double* Nk, const double* dphiI,
+                         const double* X, double* out);
+void launch_kochin(cudaStream_t st, int N, int NK, int NB, double K, const double* cen, const double* nrm,
+                   const double* area, const double* Nk, const double* dphiI, const double* X, double* out);
 // Plane-wave factors of the imaginary wave influence (M angles, stored as float
 // pairs) and the product out += i * scale * Re-part operator applied to Z, in
 // double-float arithmetic (k_influence.cu).  Zdf: Z split by launch_split_df;

@@ -104,6 +104,12 @@ struct bem_ctx {
     std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
+    // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
+    std::vector<double> wave_pts;               // free-surface points [3][NW] (bem_set_wave_points)
+    int n_kochin = 36;                          // NKochin (Hydrodynamic_Solver.h:119)
+    double *d_wpts = nullptr, *d_ext = nullptr; // device copy of wave_pts; [max(NW, NK)][R] complex
+    size_t wpts_cap = 0, ext_cap = 0;           // their sizes in doubles
+    bool wpts_dirty = true;
 };
 
 namespace {
@@ -172,6 +178,9 @@ void free_all(bem_ctx* ctx) {
     ctx->d_norms = nullptr;
     ctx->d_xr32 = nullptr;
     ctx->d_gq32 = nullptr;
+    ctx->d_wpts = ctx->d_ext = nullptr;
+    ctx->wpts_cap = ctx->ext_cap = 0;
+    ctx->wpts_dirty = true;
     ctx->ready = false;
 }
 
@@ -827,7 +836,6 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     for (int f = 0; f < n_freq; ++f) {
         FreqState& F = slot(f);
         const double Om = omega[f];
-        const double K = F.K;
         if (pipe && f + 1 < n_freq) {
             s = enqueue_assembly(f + 1);
             if (s != BEM_OK) return s;
@@ -835,6 +843,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             s = enqueue_assembly(f);
             if (s != BEM_OK) return s;
         }
+        const double K = F.K;  // set by this frequency's assemble()
         if (pipe) CK(cudaStreamWaitEvent(st, F.ev_asm, 0));
         int iters = 0;
         double resid = 0;
@@ -850,9 +859,60 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, st));
+        // exterior outputs of this frequency (Hydrodynamic_Solver.cpp:489-505)
+        const int NW = (int)(ctx->wave_pts.size() / 3), NK = ctx->n_kochin;
+        const bool want_fs = out && (out->fs_rad || out->fs_diff) && NW > 0;
+        const bool want_k = out && (out->kochin_rad || out->kochin_diff) && NK > 0;
+        std::vector<double> ext_fs, ext_k;
+        if (want_fs || want_k) {
+            // grow-only buffers (a smaller earlier one stays in ctx->allocs until bem_destroy)
+            const size_t need_ext = (size_t)2 * R * std::max(NW, NK), need_w = (size_t)3 * std::max(NW, 1);
+            if (ctx->ext_cap < need_ext) {
+                ctx->d_ext = nullptr;
+                DA(ctx->d_ext, need_ext);
+                ctx->ext_cap = need_ext;
+            }
+            if (ctx->wpts_cap < need_w) {
+                ctx->d_wpts = nullptr;
+                DA(ctx->d_wpts, need_w);
+                ctx->wpts_cap = need_w;
+                ctx->wpts_dirty = true;
+            }
+        }
+        if (want_fs) {
+            if (ctx->wpts_dirty) {
+                CK(cudaMemcpyAsync(ctx->d_wpts, ctx->wave_pts.data(), ctx->wave_pts.size() * 8,
+                                   cudaMemcpyHostToDevice, st));
+                ctx->wpts_dirty = false;
+            }
+            bem::WaveArgs a = {};
+            a.N = N; a.K = K; a.gq = ctx->d_gq; a.nq = ctx->d_nq;
+            bem::launch_fs_elevation(st, a, NW, ctx->d_wpts, ctx->d_rec, ctx->d_rn, Om, NB, ctx->d_Nk, F.dphiI,
+                                     ctx->d_X, ctx->d_ext);
+            CK(cudaGetLastError());
+            ext_fs.resize((size_t)2 * R * NW);
+            CK(cudaMemcpyAsync(ext_fs.data(), ctx->d_ext, ext_fs.size() * 8, cudaMemcpyDeviceToHost, st));
+        }
+        if (want_k) {
+            bem::launch_kochin(st, N, NK, NB, K, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_Nk, F.dphiI, ctx->d_X,
+                               ctx->d_ext);
+            CK(cudaGetLastError());
+            ext_k.resize((size_t)2 * R * NK);
+            CK(cudaMemcpyAsync(ext_k.data(), ctx->d_ext, ext_k.size() * 8, cudaMemcpyDeviceToHost, st));
+        }
         CK(cudaEventRecord(ctx->ev[7], st));
         CK(cudaEventRecord(F.ev_free, st));
         CK(cudaStreamSynchronize(st));
+        // split [n][R] rows into the radiation [f][n][6] and diffraction [f][n][NB] blocks
+        auto split_ext = [&](const std::vector<double>& e, int n, double* rad, double* diff) {
+            for (int w = 0; w < n; ++w) {
+                const double* row = e.data() + (size_t)2 * R * w;
+                if (rad) std::copy(row, row + 12, rad + (size_t)2 * 6 * ((size_t)f * n + w));
+                if (diff && NB > 0) std::copy(row + 12, row + 2 * R, diff + (size_t)2 * NB * ((size_t)f * n + w));
+            }
+        };
+        if (want_fs) split_ext(ext_fs, NW, out->fs_rad, out->fs_diff);
+        if (want_k) split_ext(ext_k, NK, out->kochin_rad, out->kochin_diff);
         float ms;
         cudaEventElapsedTime(&ms, F.ev_t[0], F.ev_t[1]); ctx->stage_ms[0] += ms;
         cudaEventElapsedTime(&ms, F.ev_t[1], F.ev_t5); ctx->stage_ms[1] += ms;
@@ -1189,6 +1249,25 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);
+}
+
+bem_status bem_set_wave_points(bem_ctx* ctx, int n, const double* xyz) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (n < 0 || (n > 0 && !xyz)) return fail(ctx, BEM_ERR_ARG, "bem_set_wave_points: bad arguments");
+    for (int i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(xyz[i])) return fail(ctx, BEM_ERR_ARG, "bem_set_wave_points: non-finite coordinate");
+    ctx->wave_pts.assign((size_t)3 * n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c) ctx->wave_pts[(size_t)c * n + i] = xyz[3 * i + c];  // [3][NW]
+    ctx->wpts_dirty = true;
+    return BEM_OK;
+}
+
+bem_status bem_set_kochin(bem_ctx* ctx, int n_kochin) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (n_kochin < 0 || n_kochin > 1 << 20) return fail(ctx, BEM_ERR_ARG, "n_kochin must be in [0, 2^20]");
+    ctx->n_kochin = n_kochin;
+    return BEM_OK;
 }
 
 bem_status bem_lu_timeline(bem_ctx* ctx, int enable, int max_steps, double* out, int* steps) {

@@ -1,7 +1,8 @@
 // host_io.cpp -- result files in the WAMIT formats the reference writes
 // (Hydrodynamic_Solver_IO.cpp:430-646): .1 added mass / damping, .2 Haskind
 // excitation, .2fk Froude-Krylov, .2sc scattering, .4 RAO, .hst hydrostatic
-// stiffness, .mmx mass matrix.  Host only.
+// stiffness, .mmx mass matrix, the Kochin-function files and the free-surface
+// elevation (.6r, _WaveElPos.bem); and the mesh importers.  Host only.
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -68,9 +69,20 @@ extern "C" bem_status bem_write_wamit(const char* prefix, const bem_wamit_info* 
             for (int j = 0; j < 6; ++j)
                 f << "     " << i + 1 << "     " << j + 1 << "   " << num(info->M[6 * i + j] / info->rho) << "\n";
     }
+    const int nk = info->n_kochin, nw = info->n_wave;
+    if (nk < 0 || nw < 0 || (nw > 0 && !info->wave_points)) return BEM_ERR_ARG;
     std::ofstream f1(p + ".1", std::ios::trunc), f2(p + ".2", std::ios::trunc), ffk(p + ".2fk", std::ios::trunc),
-        fsc(p + ".2sc", std::ios::trunc), f4(p + ".4", std::ios::trunc);
-    if (!f1 || !f2 || !ffk || !fsc || !f4) return BEM_ERR_ARG;
+        fsc(p + ".2sc", std::ios::trunc), f4(p + ".4", std::ios::trunc), f6(p + ".6", std::ios::trunc),
+        fkr(p + "_KochinRad.bem", std::ios::trunc), fkd(p + "_KochinDiff.bem", std::ios::trunc);
+    if (!f1 || !f2 || !ffk || !fsc || !f4 || !f6 || !fkr || !fkd) return BEM_ERR_ARG;
+    std::ofstream f6r;
+    if (nw > 0) {
+        std::ofstream fp(p + "_WaveElPos.bem", std::ios::trunc);
+        f6r.open(p + ".6r", std::ios::trunc);
+        if (!fp || !f6r) return BEM_ERR_ARG;
+        for (int i = 0; i < nw; ++i)
+            fp << i << "     " << num(info->wave_points[3 * i]) << num(info->wave_points[3 * i + 1]) << "\n";
+    }
     for (int k = 0; k < n_freq; ++k) {
         const double Om = omega[k], freq = twopi * Om;
         if (r->A && r->B)
@@ -96,6 +108,139 @@ extern "C" bem_status bem_write_wamit(const char* prefix, const bem_wamit_info* 
                          << num(std::arg(z)) << num(z.real() / o.scale) << num(z.imag() / o.scale) << "\n";
                 }
         }
+        // Kochin functions (Hydrodynamic_Solver_IO.cpp:589-623), theta in degrees
+        auto kget = [&](const double* v, int n, int i, int j) {
+            const size_t o = 2 * (((size_t)k * nk + i) * n + j);
+            return std::complex<double>(v[o], v[o + 1]);
+        };
+        auto kline = [&](std::ostream& s, std::complex<double> z) {
+            s << num(std::abs(z)) << num(std::arg(z)) << num(z.real()) << num(z.imag()) << "\n";
+        };
+        if (r->kochin_rad)
+            for (int i = 0; i < nk; ++i) {
+                const double th = (0.5 + i) * twopi / nk;
+                for (int d = 0; d < 6; ++d) {
+                    fkr << num(freq) << d + 1 << "  " << num(th * kR2D);
+                    kline(fkr, kget(r->kochin_rad, 6, i, d));
+                }
+            }
+        if (r->kochin_diff)
+            for (int d = 0; d < nb; ++d)
+                for (int i = 0; i < nk; ++i) {
+                    const double th = (0.5 + i) * twopi / nk;
+                    fkd << num(freq) << num(info->betas[d] * kR2D) << "  " << num(th * kR2D);
+                    kline(fkd, kget(r->kochin_diff, nb, i, d));
+                }
+        // radiation wave elevation at the wave points (:625-645): |eta| and phase per dof
+        if (nw > 0 && r->fs_rad)
+            for (int i = 0; i < nw; ++i) {
+                f6r << num(freq) << i << "     ";
+                for (int d = 0; d < 6; ++d) {
+                    const size_t o = 2 * (((size_t)k * nw + i) * 6 + d);
+                    const std::complex<double> z(r->fs_rad[o], r->fs_rad[o + 1]);
+                    f6r << num(std::abs(z)) << num(std::arg(z));
+                }
+                f6r << "\n";
+            }
+    }
+    return BEM_OK;
+}
+
+namespace {
+
+// Text field padded with blanks to `pad` characters (PST, BEMUse_IO.h:69-74).
+std::string txt(const std::string& t, int pad = 15) {
+    std::string o = t;
+    if ((int)o.size() < pad) o.append(pad - o.size(), ' ');
+    return o;
+}
+
+}  // namespace
+
+extern "C" bem_status bem_write_bem(const char* prefix, const bem_summary_info* info, int n_freq,
+                                    const double* omega, const bem_result* r) {
+    if (!prefix || !info || !info->w || n_freq < 0 || (n_freq > 0 && (!omega || !r))) return BEM_ERR_ARG;
+    const bem_wamit_info& w = *info->w;
+    const int nb = w.n_beta;
+    if (nb < 0 || (nb > 0 && !w.betas)) return BEM_ERR_ARG;
+    std::ofstream f(std::string(prefix) + ".bem", std::ios::trunc);
+    if (!f) return BEM_ERR_ARG;
+    f << "---------------------------------------------------------------\n";
+    f << "------------------------ BEMUse Output ------------------------\n";
+    f << "---------------------------------------------------------------\n\n";
+    f << "------------ Environmental Parameters ------------\n";
+    f << "Gravity:                 " << kGravity << " m s^{-2}.\n";
+    f << "Density of Water:        " << 1025 << " kg m^{-3}.\n";
+    f << "Atmospheric Pressure:    " << 101325.0 << " Pa.\n";
+    f << "Water Depth:             Infinite.\n\n";
+    f << "------------ Wave Parameters ------------\n";
+    f << "Incoming wave angles: (deg)        ";
+    for (int b = 0; b < nb; ++b) f << num(w.betas[b] * kR2D);
+    f << "\n\n------------ Grid Summary ------------\n";
+    f << (info->file_info ? info->file_info : "") << "\n";
+    f << "Input Mesh has:          " << info->n_nodes << " nodes.\n";
+    f << "Input Mesh has:          " << info->n_elems << " panels.\n";
+    f << "Input Mesh has:          " << info->n_aux_elems << " auxiliary panels.\n\n";
+    f << "------------ Geometry Summary ------------\n";
+    f << "Nb: This is calculated by BEMUse with the approximation of flat surface panels.\n";
+    f << "With increasing mesh refinement the values are expected to approach those of the continuous geometry.\n";
+    f << "Volume:                  " << w.volume << " m^3.\n";
+    f << "Surface area:            " << info->surface_area << " m^2.\n";
+    f << "Mass:                    " << info->mass << " kg. (Assuming not pre-specified),\n";
+    f << "Centre of Mass:          [" << w.cog[0] << ", " << w.cog[1] << ", " << w.cog[2] << "] m.\n";
+    f << "Centre of Buoyancy:      [" << w.cob[0] << ", " << w.cob[1] << ", " << w.cob[2] << "] m.\n\n";
+    f << "------------ Inertial Summary ------------\n\n";
+    auto mat = [&](const char* title, const double* m) {
+        f << title << " \n";
+        for (int i = 0; i < 6; ++i) {
+            f << "|";
+            for (int j = 0; j < 6; ++j) f << num(m[6 * i + j]);
+            f << " |\n";
+        }
+        f << "\n";
+    };
+    mat("Mass Matrix:", w.M);
+    mat("Hydrostatic stiffness Matrix:", w.C);
+    f << "------------ Output of Hydrodynamic Analysis: ------------\n\n\n";
+    static const char* rows_ab[6] = {"Surge", "Sway", "Heave", "Roll", "Pitch", "Yaw"};
+    static const char* rows_f[6] = {"Surge: ", "Sway: ", "Heave: ", "Pitch: ", "Roll: ", "Yaw: "};
+    for (int k = 0; k < n_freq; ++k) {
+        const double Om = omega[k], freq = 2.0 * M_PI * Om;
+        f << "----------\n";
+        f << "Frequency:       " << Om << " s^{-1}.\n";
+        f << "Period:          " << 1.0 / freq << " s.\n";
+        f << "Wavenumber:      " << Om * Om / kGravity << " m^{-1}.\n\n";
+        f << txt("Motion") << txt(" A_x") << txt(" B_x") << txt(" A_y") << txt(" B_y") << txt(" A_z") << txt(" B_z")
+          << txt(" A_pitch") << txt(" B_pitch") << txt(" A_roll") << txt(" B_roll") << txt(" A_yaw") << txt(" B_yaw")
+          << "\n";
+        for (int i = 0; i < 6; ++i) {
+            f << txt(rows_ab[i]);
+            for (int j = 0; j < 6; ++j) {
+                const size_t o = 36 * (size_t)k + 6 * i + j;
+                f << num(r->A ? r->A[o] : 0.0) << num(r->B ? r->B[o] : 0.0);
+            }
+            f << "\n";
+        }
+        f << "\n\n";
+        std::string heading = txt("Wave Heading: (deg) ", 30);
+        for (int b = 0; b < nb; ++b) heading += num(w.betas[b] * kR2D, 30);
+        auto table = [&](const char* title, const double* v, const char* lab) {
+            f << title << "\n" << heading << "\n" << txt("Motion: ", 30);
+            for (int b = 0; b < nb; ++b) f << txt(std::string(" Mag(") + lab + ")") << txt(std::string(" Arg(") + lab + ")");
+            f << "\n";
+            for (int i = 0; i < 6; ++i) {
+                f << txt(rows_f[i], 30);
+                for (int b = 0; b < nb; ++b) {
+                    const std::complex<double> z = v ? cget(v, k, i, b, nb) : std::complex<double>(0, 0);
+                    f << num(std::abs(z) / kGravity) << num(std::arg(z));
+                }
+                f << "\n";
+            }
+            f << "\n\n";
+        };
+        table("Froude-Krylov Forces:", r->FK, "Fh");
+        table("Excitation Forces:", r->F, "Xh");
+        f << "----------\n\n";
     }
     return BEM_OK;
 }

@@ -576,6 +576,129 @@ __global__ void k_post_reduce(int nblk, int nout, const double* __restrict__ par
     out[2 * t + 1] = si;
 }
 
+// ---------------------------------------------------------------------------
+// Exterior free-surface elevation (Hydrodynamic_Solver.cpp:205-266, 498-505).
+// One warp per wave point w, lanes over body panels s.  Per pair the Rankine
+// source/dipole of the body panel and of its mirror image (Prepare_FS_Linear_System)
+// and the wave term of the mirrored panel (Prepare_FS_Linear_System_Wave_Terms):
+//     WS = -s - sr - ws                      (SMatExt + SMatReflExt + SWaveMatExt)
+//     WD = d + dr + wd + (-sr) 2 n_z(s) K    (DMatExt + DMatReflExt + DWaveMatExt)
+// then, with X = [Phi_J | Phi_S] (N x R),
+//     ExtRad  = -i Omega / g (WS N_k   - WD Phi_J)      (:503)
+//     ExtDiff = -i Omega / g (WS dPhiI/dn + WD Phi_S)  (:504)
+// g is the global Gravity = 9.81.  out: [NW][R] complex interleaved.
+__global__ void __launch_bounds__(256) k_fs_elevation(WaveArgs a, int NW, const double* __restrict__ wp,
+                                                      const double* __restrict__ rec, const double* __restrict__ rn,
+                                                      double Omega, int NB, const double* __restrict__ Nk,
+                                                      const double* __restrict__ dphiI, const double* __restrict__ X,
+                                                      double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (w >= NW) return;
+    const int N = a.N, R = 6 + NB;
+    const double Px = wp[w], Py = wp[NW + w], Pz = wp[2 * NW + w];
+    double ar[MAX_RHS], ai[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+    for (int s = lane; s < N; s += 32) {
+        double sd, dd, sm, dm, wsr, wsi, wdr, wdi;
+        source_kernel(rec + (size_t)s * RK_STRIDE, Px, Py, Pz, sd, dd);
+        source_kernel(rec + ((size_t)N + s) * RK_STRIDE, Px, Py, Pz, sm, dm);
+        wave_pair<double>(a, s, Px, Py, Pz, wsr, wsi, wdr, wdi);
+        const double WSr = (-sd) + (-sm) + (-wsr), WSi = -wsi;
+        const double WDr = dd + dm + (wdr + (-sm) * rn[s] * a.K), WDi = wdi;
+        const double* x = X + (size_t)s * 2 * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double ur, ui;
+                if (j < 6) { ur = Nk[(size_t)s * 6 + j]; ui = 0.0; }
+                else { ur = dphiI[2 * ((size_t)s * NB + j - 6)]; ui = dphiI[2 * ((size_t)s * NB + j - 6) + 1]; }
+                const double sg = j < 6 ? -1.0 : 1.0;
+                const double xr = x[2 * j], xi = x[2 * j + 1];
+                ar[j] += (WSr * ur - WSi * ui) + sg * (WDr * xr - WDi * xi);
+                ai[j] += (WSr * ui + WSi * ur) + sg * (WDr * xi + WDi * xr);
+            }
+        }
+    }
+    const double c = Omega / 9.81;
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            double vr = ar[j], vi = ai[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {  // -i c (vr + i vi) = c vi - i c vr
+                out[2 * ((size_t)w * R + j)] = c * vi;
+                out[2 * ((size_t)w * R + j) + 1] = -c * vr;
+            }
+        }
+    }
+}
+
+// Kochin functions (Set_Kochin_Mats, Hydrodynamic_Solver.cpp:598-642, and :492-494)
+// at theta_i = (i + 1/2) 2 pi / NK.  The reference reads an uninitialised E
+// (:626-627); this computes the evident intent E = exp(K z + i K (x cos t + y sin t))
+// at the panel centroids, so that
+//     KochinRad(i, j)  = sum_P A_P (E N_k(P, j)     - dE/dn Phi_J(P, j))
+//     KochinDiff(i, b) = sum_P A_P (E dPhiI/dn(P, b) - dE/dn Phi_S(P, b))
+// with dE/dn = (i K (n_x cos t + n_y sin t) + K n_z) E.  One warp per angle.
+__global__ void __launch_bounds__(256) k_kochin(int N, int NK, int NB, double K, const double* __restrict__ cen,
+                                                const double* __restrict__ nrm, const double* __restrict__ area,
+                                                const double* __restrict__ Nk, const double* __restrict__ dphiI,
+                                                const double* __restrict__ X, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (i >= NK) return;
+    const int R = 6 + NB;
+    const double th = (0.5 + (double)i) * 6.283185307179586 / NK;
+    double st, ct;
+    sincos(th, &st, &ct);
+    double ar[MAX_RHS], ai[MAX_RHS];
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
+    for (int p = lane; p < N; p += 32) {
+        const double x = cen[p], y = cen[N + p], z = cen[2 * N + p];
+        const double nx = nrm[p], ny = nrm[N + p], nz = nrm[2 * N + p];
+        double sa, ca;
+        sincos(K * (x * ct + y * st), &sa, &ca);
+        const double m = exp(K * z) * area[p];
+        const double Er = m * ca, Ei = m * sa;
+        const double tr = K * nz, ti = K * (nx * ct + ny * st);  // dE/dn = (tr + i ti) E
+        const double Gr = tr * Er - ti * Ei, Gi = tr * Ei + ti * Er;
+        const double* xp = X + (size_t)p * 2 * R;
+#pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) {
+            if (j < R) {
+                double ur, ui;
+                if (j < 6) { ur = Nk[(size_t)p * 6 + j]; ui = 0.0; }
+                else { ur = dphiI[2 * ((size_t)p * NB + j - 6)]; ui = dphiI[2 * ((size_t)p * NB + j - 6) + 1]; }
+                const double xr = xp[2 * j], xi = xp[2 * j + 1];
+                ar[j] += (Er * ur - Ei * ui) - (Gr * xr - Gi * xi);
+                ai[j] += (Er * ui + Ei * ur) - (Gr * xi + Gi * xr);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MAX_RHS; ++j) {
+        if (j < R) {
+            double vr = ar[j], vi = ai[j];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                vi += __shfl_xor_sync(0xffffffffu, vi, off);
+            }
+            if (lane == 0) {
+                out[2 * ((size_t)i * R + j)] = vr;
+                out[2 * ((size_t)i * R + j) + 1] = vi;
+            }
+        }
+    }
+}
+
 // Batch HavelockGF (Kernels.cpp:342-412) for the C ABI and tests.
 template <typename T>
 __global__ void k_havelock(int n, const double* __restrict__ x, const double* __restrict__ y,
@@ -706,6 +829,19 @@ void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const d
     int nout = 36 + 12 * NB;
     BEM_LAUNCH(k_post_partial<<<nblk, 256, 0, st>>>(N, NB, R, X, Nk, area, phiI, dphiI, part));
     BEM_LAUNCH(k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out));
+}
+
+void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int NW, const double* wp, const double* rec,
+                         const double* rn, double Omega, int NB, const double* Nk, const double* dphiI,
+                         const double* X, double* out) {
+    if (NW <= 0) return;
+    BEM_LAUNCH(k_fs_elevation<<<(NW + 7) / 8, 256, 0, st>>>(a, NW, wp, rec, rn, Omega, NB, Nk, dphiI, X, out));
+}
+
+void launch_kochin(cudaStream_t st, int N, int NK, int NB, double K, const double* cen, const double* nrm,
+                   const double* area, const double* Nk, const double* dphiI, const double* X, double* out) {
+    if (NK <= 0) return;
+    BEM_LAUNCH(k_kochin<<<(NK + 7) / 8, 256, 0, st>>>(N, NK, NB, K, cen, nrm, area, Nk, dphiI, X, out));
 }
 
 void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,

@@ -81,7 +81,15 @@ typedef struct {
  *   refine_iters    [f] refinement sweeps used (0 for BEM_PLAIN_FP64)
  *   residual        [f] final max relative residual ||b - D x|| / ||b|| over RHS
  *   phi_rad         N x 6 complex (radiation potentials Phi_J), last frequency
- *   phi_scat        N x nb complex (scattering potentials Phi_S), last frequency */
+ *   phi_scat        N x nb complex (scattering potentials Phi_S), last frequency
+ *   fs_rad          [f][nw][6] complex  ExtRadMat, free-surface elevation of the
+ *                   radiation problems at the bem_set_wave_points points
+ *                   (Hydrodynamic_Solver.cpp:498-505)
+ *   fs_diff         [f][nw][nb] complex ExtDiffMat
+ *   kochin_rad      [f][nk][6] complex  KochinRad (:492-494) at theta_i = (i + 1/2) 2 pi / nk
+ *   kochin_diff     [f][nk][nb] complex KochinDiff
+ * The last four exist for the hydrodynamic solve only; a caller that zero-fills
+ * the struct (or initialises only the first ten members) skips them. */
 typedef struct {
     double* A;
     double* B;
@@ -93,6 +101,10 @@ typedef struct {
     double* residual;
     double* phi_rad;
     double* phi_scat;
+    double* fs_rad;
+    double* fs_diff;
+    double* kochin_rad;
+    double* kochin_diff;
 } bem_result;
 
 /* Body and environment data for the result files (host only). */
@@ -106,7 +118,31 @@ typedef struct {
     double volume;         /* displaced volume */
     double cob[3];         /* centre of buoyancy */
     double cog[3];         /* centre of gravity */
+    /* optional exterior outputs (zero-filled = none): Kochin angles of
+     * bem_result.kochin_rad/diff, and the wave points (n_wave x 3 row-major) of
+     * bem_result.fs_rad; they add _KochinRad.bem, _KochinDiff.bem,
+     * _WaveElPos.bem and .6r (Hydrodynamic_Solver_IO.cpp:488-500, 589-645). */
+    int n_kochin;
+    int n_wave;
+    const double* wave_points;
 } bem_wamit_info;
+
+/* The .bem summary file (Generate_Output_File_BEMUse / Update_Output_File_BEMUse,
+ * Hydrodynamic_Solver_IO.cpp:107-426): environment, headings, grid and geometry
+ * summary, M and C, then per frequency Omega, period 1 / (2 pi Omega),
+ * wavenumber, the A/B table and the Froude-Krylov and excitation tables
+ * (|F| / g and phase).  The reference's Setup also writes a block for its
+ * Frequency = -1 solve; a caller who wants that block passes omega = -1 / (2 pi)
+ * first.  Host only. */
+typedef struct {
+    const bem_wamit_info* w;   /* headings, M, C, volume, centres */
+    int n_nodes, n_elems, n_aux_elems;
+    double surface_area;
+    double mass;
+    const char* file_info;     /* Boundary::FileInfo line (NULL = empty) */
+} bem_summary_info;
+bem_status bem_write_bem(const char* prefix, const bem_summary_info* info, int n_freq, const double* omega,
+                         const bem_result* r);
 
 /* ---- mesh generators (host only; no device needed) ------------------------ */
 
@@ -277,6 +313,18 @@ bem_status bem_mlp_throughput(bem_mlp* m, int n, double* mlp_evals_per_s);
 /* Throughput of the closed-form HavelockGF kernel (evaluations per second of device
  * time) on n resident points; precision as for bem_havelock. */
 bem_status bem_havelock_throughput(int device, int n, int precision, double* evals_per_s);
+
+/* ---- exterior outputs (Hydrodynamic_Solver.cpp:205-266, 489-505, 598-642) ----
+ * bem_set_wave_points: the exterior free-surface points (x, y, z), n x 3
+ * row-major, at which bem_solve evaluates ExtRadMat / ExtDiffMat when the
+ * result asks for fs_rad / fs_diff (the reference's Wave_Nodes, e.g. the
+ * Barge free-surface grid of Barge.cpp:125-140).  n = 0 clears them.
+ * bem_set_kochin: NKochin, the number of Kochin angles (default 36,
+ * Hydrodynamic_Solver.h:119).  The reference's Kochin matrices read an
+ * uninitialised value (Hydrodynamic_Solver.cpp:626-627); this library computes
+ * E = exp(K z + i K (x cos t + y sin t)) at the panel centroids. */
+bem_status bem_set_wave_points(bem_ctx* ctx, int n, const double* xyz);
+bem_status bem_set_kochin(bem_ctx* ctx, int n_kochin);
 
 /* ---- mesh import --------------------------------------------------------------
  * Reads the mesh files the reference imports, with the reference readers'

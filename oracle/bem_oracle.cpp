@@ -1081,4 +1081,88 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
     }
 }
 
+
+// Exterior outputs of one frequency from given potentials Phi_J (N x 6) and
+// Phi_S (N x nb), complex interleaved:
+//   * free-surface elevation at nw points (Prepare_FS_Linear_System :205-231,
+//     Prepare_FS_Linear_System_Wave_Terms :233-266, Solve :498-505)
+//       ExtRad  = -i Omega/g ((Sext + Srefl + Swave) N_k   - (Dext + Drefl + Dwave) Phi_J)
+//       ExtDiff = -i Omega/g ((Sext + Srefl + Swave) dPhiI  + (Dext + Drefl + Dwave) Phi_S)
+//     with Swave = -ws, Dwave = wd + Srefl 2 n_z K;
+//   * Kochin functions (Set_Kochin_Mats :598-642, Solve :492-494) at
+//     theta_i = (i + 1/2) 2 pi / nk, with E = exp(K z + i K (x cos t + y sin t)) at the
+//     panel centroids -- the reference reads an uninitialised E there (:626-627).
+// Outputs: fs_rad [nw][6], fs_diff [nw][nb], k_rad [nk][6], k_diff [nk][nb].
+void orc_exterior(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+                  const double* comp_origin, double Omega, int nbeta, const double* betas, const double* phiJ,
+                  const double* phiS, int nw, const double* wpts, int nk, double* fs_rad, double* fs_diff,
+                  double* k_rad, double* k_diff) {
+    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
+    std::vector<Panel> body, mir;
+    build_panels(m, body, mir);
+    const int N = ne, NB = nbeta;
+    const double Kappa = Omega * Omega / Gravity;
+    const cplx Im(0.0, 1.0);
+    std::vector<double> Nk((size_t)N * 6);
+    std::vector<cplx> dPhiI((size_t)N * NB), PJ((size_t)N * 6), PS((size_t)N * NB);
+    for (int i = 0; i < N; ++i) {
+        V3 P = body[i].c, Nn = body[i].ez, PCN = cross(P, Nn);
+        double* r = &Nk[(size_t)i * 6];
+        r[0] = Nn.x; r[1] = Nn.y; r[2] = Nn.z; r[3] = PCN.x; r[4] = PCN.y; r[5] = PCN.z;
+        for (int j = 0; j < 6; ++j) PJ[(size_t)i * 6 + j] = cplx(phiJ[2 * (i * 6 + j)], phiJ[2 * (i * 6 + j) + 1]);
+        for (int b = 0; b < NB; ++b) {
+            PS[(size_t)i * NB + b] = cplx(phiS[2 * (i * NB + b)], phiS[2 * (i * NB + b) + 1]);
+            if (Omega == 0.0) continue;  // k_incident: no incident wave at Omega = 0
+            double CB = std::cos(betas[b]), SB = std::sin(betas[b]);
+            cplx phi = Im * Gravity / Omega * std::exp(Im * Kappa * (P.x * CB + P.y * SB)) * std::exp(Kappa * P.z);
+            cplx dpx = Im * Kappa * CB * phi, dpy = Im * Kappa * SB * phi, dpz = Kappa * phi;
+            dPhiI[(size_t)i * NB + b] = Nn.x * dpx + Nn.y * dpy + Nn.z * dpz;
+        }
+    }
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int w = 0; w < nw; ++w) {
+        V3 P = v3(wpts[3 * w], wpts[3 * w + 1], wpts[3 * w + 2]);
+        std::vector<cplx> acc(6 + NB, cplx(0, 0));
+        for (int S = 0; S < N; ++S) {
+            double s, d, sr, dr;
+            inf_source_kernel(body[S], P, s, d);
+            inf_source_kernel(mir[S], P, sr, dr);
+            cplx ws(0, 0), wd(0, 0);
+            wave_panel_influence(mir[S], P, Kappa, ws, wd);
+            const double rn = body[S].ez.z * 2.0;
+            cplx WS = cplx(-s, 0.0) + cplx(-sr, 0.0) + (-ws);
+            cplx WD = cplx(d, 0.0) + cplx(dr, 0.0) + (wd + cplx(-sr, 0.0) * rn * Kappa);
+            for (int j = 0; j < 6; ++j) acc[j] += WS * Nk[(size_t)S * 6 + j] - WD * PJ[(size_t)S * 6 + j];
+            for (int b = 0; b < NB; ++b) acc[6 + b] += WS * dPhiI[(size_t)S * NB + b] + WD * PS[(size_t)S * NB + b];
+        }
+        const cplx c = -Im * Omega / Gravity;
+        for (int j = 0; j < 6; ++j) {
+            cplx v = c * acc[j];
+            fs_rad[2 * (w * 6 + j)] = v.real(); fs_rad[2 * (w * 6 + j) + 1] = v.imag();
+        }
+        for (int b = 0; b < NB; ++b) {
+            cplx v = c * acc[6 + b];
+            fs_diff[2 * (w * NB + b)] = v.real(); fs_diff[2 * (w * NB + b) + 1] = v.imag();
+        }
+    }
+    for (int i = 0; i < nk; ++i) {
+        double th = (0.5 + 1.0 * i) * TwoPI / nk, CTH = std::cos(th), STH = std::sin(th);
+        std::vector<cplx> acc(6 + NB, cplx(0, 0));
+        for (int p = 0; p < N; ++p) {
+            V3 P = body[p].c, Nn = body[p].ez;
+            cplx E = std::exp(cplx(Kappa * P.z, Kappa * (P.x * CTH + P.y * STH)));
+            cplx dEdx = Im * Kappa * CTH * E, dEdy = Im * Kappa * STH * E, dEdz = Kappa * E;
+            cplx KE = E * body[p].area;
+            cplx KdE = (Nn.x * dEdx + Nn.y * dEdy + Nn.z * dEdz) * body[p].area;
+            for (int j = 0; j < 6; ++j) acc[j] += KE * Nk[(size_t)p * 6 + j] - KdE * PJ[(size_t)p * 6 + j];
+            for (int b = 0; b < NB; ++b) acc[6 + b] += KE * dPhiI[(size_t)p * NB + b] - KdE * PS[(size_t)p * NB + b];
+        }
+        for (int j = 0; j < 6; ++j) { k_rad[2 * (i * 6 + j)] = acc[j].real(); k_rad[2 * (i * 6 + j) + 1] = acc[j].imag(); }
+        for (int b = 0; b < NB; ++b) {
+            k_diff[2 * (i * NB + b)] = acc[6 + b].real();
+            k_diff[2 * (i * NB + b) + 1] = acc[6 + b].imag();
+        }
+    }
+}
+
 }  // extern "C"

@@ -98,6 +98,7 @@ class Oracle:
         L.orc_mass_hydrostatics.argtypes = mesh_args + mesh_args + [_d, _d, _d, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve.argtypes = mesh_args + [_i, _dp, _i, _dp, _d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                             _dp, _dp]
+        L.orc_exterior.argtypes = mesh_args + [_d, _i, _dp, _dp, _dp, _i, _dp, _i, _dp, _dp, _dp, _dp]
         L.orc_num_threads.restype = _i
         L.orc_set_threads.argtypes = [_i]
 
@@ -213,6 +214,25 @@ class Oracle:
             out["phiJ"] = pj
             out["phiS"] = ps
         return out
+
+    def exterior(self, mesh, omega, betas, phiJ, phiS, wave_points, n_kochin):
+        """Free-surface elevation at wave_points (n x 3) and Kochin functions at
+        n_kochin angles for one frequency from the potentials phiJ (N x 6) and
+        phiS (N x nb): (fs_rad, fs_diff, kochin_rad, kochin_diff)."""
+        betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
+        nb, N = betas.size, mesh.n
+        pj = np.ascontiguousarray(phiJ, dtype=np.complex128).reshape(N, 6)
+        ps = np.ascontiguousarray(phiS, dtype=np.complex128).reshape(N, nb)
+        wp = np.ascontiguousarray(wave_points, dtype=np.float64).reshape(-1, 3)
+        nw = wp.shape[0]
+        fr = np.zeros((nw, 6), np.complex128)
+        fd = np.zeros((nw, nb), np.complex128)
+        kr = np.zeros((n_kochin, 6), np.complex128)
+        kd = np.zeros((n_kochin, nb), np.complex128)
+        self.L.orc_exterior(*mesh.args(), float(omega), nb, _p(betas), _p(pj.view(np.float64)),
+                            _p(ps.view(np.float64)), nw, _p(wp), int(n_kochin), _p(fr.view(np.float64)),
+                            _p(fd.view(np.float64)), _p(kr.view(np.float64)), _p(kd.view(np.float64)))
+        return fr, fd, kr, kd
 
     def aero(self, mesh, vel):
         """Aerodynamic_Solver steady constant-panel solve: returns (X, BC)."""

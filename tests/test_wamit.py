@@ -80,6 +80,77 @@ def test_wamit_files(orc, tmp_path):
             assert rel(float(body[6 * i + j][2]), M[i, j] / 1025.0)
 
 
+def test_kochin_and_wave_files(orc, tmp_path):
+    """_KochinRad.bem (freq, dof, theta deg, |H|, arg, Re, Im), _KochinDiff.bem
+    (freq, beta deg, theta deg, ...), .6r (freq, point, |eta|, arg per dof) and
+    _WaveElPos.bem (Hydrodynamic_Solver_IO.cpp:488-500, 589-645)."""
+    mesh, _ = orc.cylinder(5.0, 8.0, 12, 3, 4)
+    om = np.array([0.0, 0.7])
+    betas = np.deg2rad([0.0, 30.0])
+    wp = np.array([[15.0, 0.0, 0.0], [0.0, 15.0, 0.0], [-10.0, -10.0, 0.0]])
+    nk = 8
+    out = dict(kochin_rad=np.zeros((2, nk, 6), complex), kochin_diff=np.zeros((2, nk, 2), complex),
+               fs_rad=np.zeros((2, 3, 6), complex))
+    for k, w in enumerate(om):
+        r = orc.solve(mesh, [w], betas, want_phi=True)
+        fr, _, kr, kd = orc.exterior(mesh, w, betas, r["phiJ"], r["phiS"], wp, nk)
+        out["kochin_rad"][k], out["kochin_diff"][k], out["fs_rad"][k] = kr, kd, fr
+    prefix = str(tmp_path / "ext")
+    bg.write_wamit(prefix, om, out, betas, np.eye(6), np.eye(6), 1.0, (0, 0, 0), (0, 0, 0), wave_points=wp)
+    rel = lambda a, b: abs(a - b) <= 1e-5 * max(1.0, abs(b))
+    kr = _rows(prefix + "_KochinRad.bem")
+    assert len(kr) == nk * 6  # the Omega = 0 frequency writes no rows
+    for i in range(nk):
+        for d in range(6):
+            row = [float(x) for x in kr[6 * i + d]]
+            z = out["kochin_rad"][1, i, d]
+            assert rel(row[0], 2 * np.pi * 0.7) and row[1] == d + 1 and rel(row[2], (0.5 + i) * 360.0 / nk)
+            assert rel(row[3], abs(z)) and abs(row[5] - z.real) <= 1e-5 * abs(z)
+    kd = _rows(prefix + "_KochinDiff.bem")
+    assert len(kd) == 2 * nk
+    row = [float(x) for x in kd[nk + 3]]  # heading 1, angle 3
+    z = out["kochin_diff"][1, 3, 1]
+    assert rel(row[1], 30.0) and rel(row[2], 3.5 * 360.0 / nk) and rel(row[3], abs(z))
+    r6 = _rows(prefix + ".6r")
+    assert len(r6) == 3 and int(r6[2][1]) == 2 and len(r6[0]) == 14
+    z = out["fs_rad"][1, 2, 2]
+    assert rel(float(r6[2][6]), abs(z)) and abs(float(r6[2][7]) - np.angle(z)) < 1e-5
+    pos = _rows(prefix + "_WaveElPos.bem")
+    assert [int(p[0]) for p in pos] == [0, 1, 2] and float(pos[2][1]) == -10.0
+    assert os.path.exists(prefix + ".6")
+
+
+def test_bem_summary_file(orc, tmp_path):
+    """.bem summary (Hydrodynamic_Solver_IO.cpp:107-426): header, M and C tables, and per
+    frequency Omega, period 1/(2 pi Omega), wavenumber, the A/B table and the FK and
+    excitation tables (|F|/g, phase)."""
+    om, betas, out, M, C, vc = _orc_case(orc)
+    mesh, _ = orc.cylinder(5.0, 8.0, 12, 3, 4)
+    prefix = str(tmp_path / "sum")
+    bg.write_bem(prefix, om, out, betas, M, C, vc[0], vc[1:], (0.0, 0.0, -1.0), mesh=bg.Mesh(mesh.nodes, mesh.elems),
+                 mass=M[0, 0], file_info="generated")
+    text = open(prefix + ".bem").read()
+    lines = text.split("\n")
+    assert lines[1].startswith("------------------------ BEMUse Output")
+    assert "Gravity:                 9.81 m s^{-2}." in text and "Incoming wave angles: (deg)" in text
+    assert "Input Mesh has:          %d panels." % mesh.n in text
+    area = float([ln for ln in lines if ln.startswith("Surface area:")][0].split()[2])
+    assert abs(area - np.sum(bg.panel_areas(bg.Mesh(mesh.nodes, mesh.elems)))) < 1e-3 * area
+    blocks = text.split("----------\nFrequency:")[1:]
+    assert len(blocks) == len(om)
+    rel = lambda a, b: abs(a - b) <= 1e-5 * max(1e-12, abs(b))
+    for k, blk in enumerate(blocks):
+        bl = blk.split("\n")
+        assert rel(float(bl[0].split()[0]), om[k])
+        assert rel(float(bl[2].split()[1]), om[k] ** 2 / 9.81) or om[k] == 0
+        heave = [ln for ln in bl if ln.startswith("Heave ")][0].split()
+        assert rel(float(heave[5]), out["A"][k, 2, 2]) and (rel(float(heave[6]), out["B"][k, 2, 2])
+                                                             or abs(out["B"][k, 2, 2]) < 1e-9)
+        ex = blk.split("Excitation Forces:")[1].split("\n")
+        hv = [ln for ln in ex if ln.startswith("Heave: ")][0].split()
+        assert rel(float(hv[1]), abs(out["F"][k, 2, 0]) / 9.81) or abs(out["F"][k, 2, 0]) < 1e-9
+
+
 def test_number_format(tmp_path):
     """Fields: 6 significant digits, a leading blank for values >= 0, padded to 15."""
     z = np.zeros((1, 6, 6))
