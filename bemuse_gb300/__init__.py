@@ -118,6 +118,7 @@ def lib():
         "bem_read_mesh": ([ctypes.c_char_p, c_int, _ip, _dp, _ip, _ip], c_int),
         "bem_set_wave_points": ([vp, c_int, _dp], c_int),
         "bem_set_kochin": ([vp, c_int], c_int),
+        "bem_set_ifr": ([vp, c_int], c_int),
         "bem_read_mesh_error": ([], ctypes.c_char_p),
         "bem_write_bem": ([ctypes.c_char_p, ctypes.POINTER(_SummaryInfo), c_int, _dp, ctypes.POINTER(_Result)],
                           c_int),
@@ -436,8 +437,9 @@ class Hydrodynamic_Radiation_Solver:
                 self.Rho = float(val)
             elif name == "Gravity":
                 self.Grav = float(val)
-            elif name == "IFR" and val:
-                raise BEMError(6, "irregular-frequency removal is not implemented")
+            elif name == "IFR":
+                self.IFR = bool(val)
+                _check(lib().bem_set_ifr(self._h, int(self.IFR)), self._h)
             elif name == "NKochin":
                 self.NKochin = int(val)
                 _check(lib().bem_set_kochin(self._h, self.NKochin), self._h)

@@ -22,6 +22,7 @@ enum DevFlag : int {
     FLAG_ZERO_PIVOT = 2, // a zero (or non-finite) pivot
     FLAG_NONFINITE = 4,  // non-finite residual
     FLAG_TIMEOUT = 8,    // a bounded device-side wait expired (kernel abandoned its tile)
+    FLAG_GROWTH = 16,    // a multiplier |l_ik| > 16 (element growth a solve should not accept)
 };
 
 struct WaveArgs {
@@ -53,10 +54,11 @@ void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
 // Exterior outputs after a solve (X = [Phi_J | Phi_S], N x (6 + NB) complex):
 // free-surface elevation at NW points wp ([3][NW]) and Kochin functions at NK angles;
 // out: [NW or NK][6 + NB] complex interleaved.
-void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int NW, const double* wp, const double* rec,
+// Sources are the first nsrc panels (the hull; a.N is the panel-array stride).
+void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int nsrc, int NW, const double* wp, const double* rec,
                          const double* rn, double Omega, int NB, const double* Nk, const double* dphiI,
                          const double* X, double* out);
-void launch_kochin(cudaStream_t st, int N, int NK, int NB, double K, const double* cen, const double* nrm,
+void launch_kochin(cudaStream_t st, int N, int nsrc, int NK, int NB, double K, const double* cen, const double* nrm,
                    const double* area, const double* Nk, const double* dphiI, const double* X, double* out);
 // Plane-wave factors of the imaginary wave influence (M angles, stored as float
 // pairs) and the product out += i * scale * Re-part operator applied to Z, in

@@ -60,7 +60,9 @@ struct bem_ctx {
     std::vector<double> betas;
     bool ready = false;
     bool aero = false;                // set up by bem_aero_setup (G in d_RS, H in d_RD)
+    bool ifr = false;                 // irregular-frequency removal (bem_set_ifr)
     int N = 0, Np = 0, NB = 0, R = 6;
+    int NPA = 0;                      // hull panels; N = NPA + interior free-surface panels with IFR
     std::vector<double> cen, nrm, area, Nk;  // host copies
     double M[36], C[36], volcob[4];
     // device buffers
@@ -395,7 +397,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
     if (hflags & bem::FLAG_TIMEOUT)
         return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the tensor-core LU update expired");
     if (hflags & bem::FLAG_ZERO_PIVOT) return fail(ctx, BEM_ERR_NUMERIC, "zero or non-finite pivot in the LU");
-    if (hflags & bem::FLAG_PIVOT)
+    // With IFR the interior free-surface rows follow the hull rows; their Schur complement
+    // gives multipliers a little above 1 (growth checked against partial pivoting on the
+    // CPU), so only |l_ik| > 16 fails there.
+    if ((hflags & bem::FLAG_GROWTH) || (!ctx->ifr && (hflags & bem::FLAG_PIVOT)))
         return fail(ctx, BEM_ERR_NUMERIC,
                     "a multiplier |l_ik| > 1 occurred: partial pivoting would exchange rows for this matrix");
     return BEM_OK;
@@ -533,7 +538,24 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     std::vector<bem::PanelGeom> body, mirror;
     std::string gerr;
     if (!bem::build_geometry(mv, body, mirror, gerr)) return fail(ctx, BEM_ERR_ARG, "mesh: " + gerr);
-    const int N = mesh->n_elems;
+    std::vector<bem::PanelGeom> auxb, auxm;
+    if (props && props->aux && props->aux->n_elems > 0) {
+        bem::MeshView av{props->aux->n_nodes, props->aux->nodes, props->aux->n_elems, props->aux->elems,
+                         props->aux->n_comp, props->aux->comp_first, props->aux->comp_origin};
+        if (!bem::build_geometry(av, auxb, auxm, gerr)) return fail(ctx, BEM_ERR_ARG, "aux mesh: " + gerr);
+    }
+    const int NPA = mesh->n_elems;
+    std::vector<bem::PanelGeom> hull;
+    if (ctx->ifr) {
+        // IFR (Create_Panels, Hydrodynamic_Solver.cpp:45-55): the interior free-surface
+        // panels and their mirror images join the system after the hull panels
+        if (auxb.empty()) return fail(ctx, BEM_ERR_ARG, "IFR needs the interior free-surface (aux) mesh");
+        hull = body;
+        body.insert(body.end(), auxb.begin(), auxb.end());
+        mirror.insert(mirror.end(), auxm.begin(), auxm.end());
+    }
+    const int N = (int)body.size();
+    ctx->NPA = NPA;
     const int Np = round_up(N, bem::LD_ALIGN);
     const int NB = (int)ctx->betas.size();
     const int R = 6 + NB;
@@ -608,20 +630,14 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     }
     // mass properties
     double cog[3] = {0, 0, 0}, gyr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, mass = 0;
-    std::vector<bem::PanelGeom> auxb, auxm;
-    const std::vector<bem::PanelGeom>* auxp = nullptr;
+    const std::vector<bem::PanelGeom>* auxp = auxb.empty() ? nullptr : &auxb;
     if (props) {
         mass = props->mass;
         memcpy(cog, props->cog, sizeof(cog));
         memcpy(gyr, props->gyration, sizeof(gyr));
-        if (props->aux && props->aux->n_elems > 0) {
-            bem::MeshView av{props->aux->n_nodes, props->aux->nodes, props->aux->n_elems, props->aux->elems,
-                             props->aux->n_comp, props->aux->comp_first, props->aux->comp_origin};
-            if (!bem::build_geometry(av, auxb, auxm, gerr)) return fail(ctx, BEM_ERR_ARG, "aux mesh: " + gerr);
-            auxp = &auxb;
-        }
     }
-    bem::mass_and_stiffness(body, auxp, ctx->rho, ctx->grav, mass, cog, gyr, ctx->M, ctx->C, ctx->volcob);
+    bem::mass_and_stiffness(ctx->ifr ? hull : body, auxp, ctx->rho, ctx->grav, mass, cog, gyr, ctx->M, ctx->C,
+                            ctx->volcob);
     if (props && props->mass_matrix) memcpy(ctx->M, props->mass_matrix, sizeof(ctx->M));
     if (props && props->stiffness) memcpy(ctx->C, props->stiffness, sizeof(ctx->C));
     // device upload
@@ -682,7 +698,7 @@ bem_status bem_get_sizes(const bem_ctx* cctx, int* n, int* nb) {
     bem_ctx* ctx = const_cast<bem_ctx*>(cctx);
     if (!ctx || !n || !nb) return fail(ctx, BEM_ERR_ARG, "null argument");
     if (!ctx->ready) return fail(ctx, BEM_ERR_STATE, "bem_setup has not run");
-    *n = ctx->N;
+    *n = ctx->NPA;  // hull panels (rows of phi_rad / phi_scat)
     *nb = ctx->NB;
     return BEM_OK;
 }
@@ -795,8 +811,16 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     CK(cudaSetDevice(ctx->device));
     const bool mixed = precision == BEM_MIXED;
     if (!(tol > 0)) tol = 1e-12;
-    const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R;
+    const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R, NPA = ctx->NPA;
     cudaStream_t st = ctx->st;
+    // with IFR a zero frequency is solved at Omega = 1e-3 (Hydrodynamic_Solver.cpp:406)
+    std::vector<double> om_ifr;
+    if (ctx->ifr) {
+        om_ifr.assign(omega, omega + n_freq);
+        for (double& w : om_ifr)
+            if (w == 0.0) w = 1.0e-3;
+        omega = om_ifr.data();
+    }
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
     const bool pipe = mixed && n_freq > 1;
@@ -856,7 +880,8 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             return s;
         }
         CK(cudaEventRecord(ctx->ev[6], st));
-        bem::launch_post(st, N, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
+        // hull panels only: Phi_J, Phi_S, Phi_I are cut to NPA rows (:452-457)
+        bem::launch_post(st, NPA, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, st));
         // exterior outputs of this frequency (Hydrodynamic_Solver.cpp:489-505)
@@ -887,15 +912,15 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
             }
             bem::WaveArgs a = {};
             a.N = N; a.K = K; a.gq = ctx->d_gq; a.nq = ctx->d_nq;
-            bem::launch_fs_elevation(st, a, NW, ctx->d_wpts, ctx->d_rec, ctx->d_rn, Om, NB, ctx->d_Nk, F.dphiI,
-                                     ctx->d_X, ctx->d_ext);
+            bem::launch_fs_elevation(st, a, NPA, NW, ctx->d_wpts, ctx->d_rec, ctx->d_rn, Om, NB, ctx->d_Nk,
+                                     F.dphiI, ctx->d_X, ctx->d_ext);
             CK(cudaGetLastError());
             ext_fs.resize((size_t)2 * R * NW);
             CK(cudaMemcpyAsync(ext_fs.data(), ctx->d_ext, ext_fs.size() * 8, cudaMemcpyDeviceToHost, st));
         }
         if (want_k) {
-            bem::launch_kochin(st, N, NK, NB, K, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_Nk, F.dphiI, ctx->d_X,
-                               ctx->d_ext);
+            bem::launch_kochin(st, N, NPA, NK, NB, K, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_Nk, F.dphiI,
+                               ctx->d_X, ctx->d_ext);
             CK(cudaGetLastError());
             ext_k.resize((size_t)2 * R * NK);
             CK(cudaMemcpyAsync(ext_k.data(), ctx->d_ext, ext_k.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -973,10 +998,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         if (out && f == n_freq - 1) {
             if (out->phi_rad)
                 CK(cudaMemcpy2D(out->phi_rad, sizeof(double) * 2 * 6, ctx->d_X, sizeof(double) * 2 * R,
-                                sizeof(double) * 2 * 6, N, cudaMemcpyDeviceToHost));
+                                sizeof(double) * 2 * 6, NPA, cudaMemcpyDeviceToHost));
             if (out->phi_scat && NB > 0)
                 CK(cudaMemcpy2D(out->phi_scat, sizeof(double) * 2 * NB, ctx->d_X + 2 * 6, sizeof(double) * 2 * R,
-                                sizeof(double) * 2 * NB, N, cudaMemcpyDeviceToHost));
+                                sizeof(double) * 2 * NB, NPA, cudaMemcpyDeviceToHost));
         }
     }
     return BEM_OK;
@@ -1160,7 +1185,7 @@ bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh) {
     std::string gerr;
     if (!bem::build_geometry(mv, body, mirror, gerr)) return fail(ctx, BEM_ERR_ARG, "mesh: " + gerr);
     const int N = mesh->n_elems, Np = round_up(N, bem::LD_ALIGN);
-    ctx->N = N; ctx->Np = Np; ctx->NB = 0; ctx->R = 1;
+    ctx->N = N; ctx->Np = Np; ctx->NB = 0; ctx->R = 1; ctx->NPA = N;
     std::vector<double> rec((size_t)2 * N * bem::RK_STRIDE, 0.0), xr;
     ctx->nrm.assign(3 * (size_t)N, 0.0);
     for (int i = 0; i < N; ++i) {
@@ -1260,6 +1285,14 @@ bem_status bem_set_wave_points(bem_ctx* ctx, int n, const double* xyz) {
     for (int i = 0; i < n; ++i)
         for (int c = 0; c < 3; ++c) ctx->wave_pts[(size_t)c * n + i] = xyz[3 * i + c];  // [3][NW]
     ctx->wpts_dirty = true;
+    return BEM_OK;
+}
+
+bem_status bem_set_ifr(bem_ctx* ctx, int enable) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (ctx->ready && (enable != 0) != ctx->ifr)
+        return fail(ctx, BEM_ERR_STATE, "IFR must be set before bem_setup (Set_Parameters precedes Setup)");
+    ctx->ifr = enable != 0;
     return BEM_OK;
 }
 

@@ -586,8 +586,10 @@ __global__ void k_post_reduce(int nblk, int nout, const double* __restrict__ par
 // then, with X = [Phi_J | Phi_S] (N x R),
 //     ExtRad  = -i Omega / g (WS N_k   - WD Phi_J)      (:503)
 //     ExtDiff = -i Omega / g (WS dPhiI/dn + WD Phi_S)  (:504)
-// g is the global Gravity = 9.81.  out: [NW][R] complex interleaved.
-__global__ void __launch_bounds__(256) k_fs_elevation(WaveArgs a, int NW, const double* __restrict__ wp,
+// g is the global Gravity = 9.81.  Sources are the nsrc hull panels (with IFR the
+// interior free-surface panels follow them and are not sources here, :218-229).
+// out: [NW][R] complex interleaved.
+__global__ void __launch_bounds__(256) k_fs_elevation(WaveArgs a, int nsrc, int NW, const double* __restrict__ wp,
                                                       const double* __restrict__ rec, const double* __restrict__ rn,
                                                       double Omega, int NB, const double* __restrict__ Nk,
                                                       const double* __restrict__ dphiI, const double* __restrict__ X,
@@ -600,7 +602,7 @@ __global__ void __launch_bounds__(256) k_fs_elevation(WaveArgs a, int NW, const 
     double ar[MAX_RHS], ai[MAX_RHS];
 #pragma unroll
     for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
-    for (int s = lane; s < N; s += 32) {
+    for (int s = lane; s < nsrc; s += 32) {
         double sd, dd, sm, dm, wsr, wsi, wdr, wdi;
         source_kernel(rec + (size_t)s * RK_STRIDE, Px, Py, Pz, sd, dd);
         source_kernel(rec + ((size_t)N + s) * RK_STRIDE, Px, Py, Pz, sm, dm);
@@ -645,8 +647,9 @@ __global__ void __launch_bounds__(256) k_fs_elevation(WaveArgs a, int NW, const 
 // at the panel centroids, so that
 //     KochinRad(i, j)  = sum_P A_P (E N_k(P, j)     - dE/dn Phi_J(P, j))
 //     KochinDiff(i, b) = sum_P A_P (E dPhiI/dn(P, b) - dE/dn Phi_S(P, b))
-// with dE/dn = (i K (n_x cos t + n_y sin t) + K n_z) E.  One warp per angle.
-__global__ void __launch_bounds__(256) k_kochin(int N, int NK, int NB, double K, const double* __restrict__ cen,
+// with dE/dn = (i K (n_x cos t + n_y sin t) + K n_z) E, over the nsrc hull panels
+// (N is the stride of cen / nrm).  One warp per angle.
+__global__ void __launch_bounds__(256) k_kochin(int N, int nsrc, int NK, int NB, double K, const double* __restrict__ cen,
                                                 const double* __restrict__ nrm, const double* __restrict__ area,
                                                 const double* __restrict__ Nk, const double* __restrict__ dphiI,
                                                 const double* __restrict__ X, double* __restrict__ out) {
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(256) k_kochin(int N, int NK, int NB, double K,
     double ar[MAX_RHS], ai[MAX_RHS];
 #pragma unroll
     for (int j = 0; j < MAX_RHS; ++j) { ar[j] = 0; ai[j] = 0; }
-    for (int p = lane; p < N; p += 32) {
+    for (int p = lane; p < nsrc; p += 32) {
         const double x = cen[p], y = cen[N + p], z = cen[2 * N + p];
         const double nx = nrm[p], ny = nrm[N + p], nz = nrm[2 * N + p];
         double sa, ca;
@@ -831,17 +834,18 @@ void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const d
     BEM_LAUNCH(k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out));
 }
 
-void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int NW, const double* wp, const double* rec,
+void launch_fs_elevation(cudaStream_t st, const WaveArgs& a, int nsrc, int NW, const double* wp, const double* rec,
                          const double* rn, double Omega, int NB, const double* Nk, const double* dphiI,
                          const double* X, double* out) {
     if (NW <= 0) return;
-    BEM_LAUNCH(k_fs_elevation<<<(NW + 7) / 8, 256, 0, st>>>(a, NW, wp, rec, rn, Omega, NB, Nk, dphiI, X, out));
+    BEM_LAUNCH(k_fs_elevation<<<(NW + 7) / 8, 256, 0, st>>>(a, nsrc, NW, wp, rec, rn, Omega, NB, Nk, dphiI, X,
+                                                           out));
 }
 
-void launch_kochin(cudaStream_t st, int N, int NK, int NB, double K, const double* cen, const double* nrm,
+void launch_kochin(cudaStream_t st, int N, int nsrc, int NK, int NB, double K, const double* cen, const double* nrm,
                    const double* area, const double* Nk, const double* dphiI, const double* X, double* out) {
     if (NK <= 0) return;
-    BEM_LAUNCH(k_kochin<<<(NK + 7) / 8, 256, 0, st>>>(N, NK, NB, K, cen, nrm, area, Nk, dphiI, X, out));
+    BEM_LAUNCH(k_kochin<<<(NK + 7) / 8, 256, 0, st>>>(N, nsrc, NK, NB, K, cen, nrm, area, Nk, dphiI, X, out));
 }
 
 void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,

@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(1024) k_gj_inv(int k0, CMat<T> A, T* invr, T* 
                 if (tx == kt && i > k) {
                     T lr = cr * qr - ci * qi, li = cr * qi + ci * qr;
                     if (lr * lr + li * li > (T)(1.000002)) local_flags |= FLAG_PIVOT;
+                    if (lr * lr + li * li > (T)256) local_flags |= FLAG_GROWTH;
                 }
 #pragma unroll
                 for (int b = 0; b < G; ++b) {

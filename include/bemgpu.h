@@ -324,6 +324,15 @@ bem_status bem_havelock_throughput(int device, int n, int precision, double* eva
  * uninitialised value (Hydrodynamic_Solver.cpp:626-627); this library computes
  * E = exp(K z + i K (x cos t + y sin t)) at the panel centroids. */
 bem_status bem_set_wave_points(bem_ctx* ctx, int n, const double* xyz);
+
+/* Irregular-frequency removal, the IFR parameter (Hydrodynamic_Solver.cpp:17,
+ * 45-55, 406): with enable != 0 the next bem_setup appends the interior
+ * free-surface panels of bem_body_props.aux (and their mirror images) to the
+ * system after the hull panels, so bem_solve solves for hull + lid unknowns
+ * and integrates forces over the hull; a zero frequency is solved at
+ * Omega = 1e-3.  bem_get_sizes still reports the hull panel count.  Set before
+ * bem_setup. */
+bem_status bem_set_ifr(bem_ctx* ctx, int enable);
 bem_status bem_set_kochin(bem_ctx* ctx, int n_kochin);
 
 /* ---- mesh import --------------------------------------------------------------

@@ -939,17 +939,16 @@ void orc_mass_hydrostatics(int nn, const double* nodes, int ne, const int* elems
 //   row-major, interleaved), and optionally phiJ (N x 6) / phiS (N x nb) of the
 //   last frequency.  M, C: 6x6 row-major mass and stiffness.
 // RAO uses B_ijOm := Omega * B_ij (Hydrodynamic_Solver.h:57 leaves it unset).
-void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
-               const double* comp_origin, int nfreq, const double* omegas, int nbeta, const double* betas,
-               double grav_unused, const double* Mmat, const double* Cmat,
-               double* A_out, double* B_out, double* FK_out, double* SC_out, double* F_out, double* RAO_out,
-               double* phiJ_out, double* phiS_out) {
-    (void)grav_unused;
-    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
-    std::vector<Panel> body, mir;
-    build_panels(m, body, mir);
+// The frequency loop of Solve() over the system panels `body` (mirror images `mir`);
+// forces integrate over the first NPA (hull) panels.  IFR (Create_Panels :45-55)
+// appends the interior free-surface panels after the hull and solves a zero
+// frequency at Omega = 1e-3 (:406).
+static void solve_panels(const std::vector<Panel>& body, const std::vector<Panel>& mir, int NPA, bool ifr,
+                         int nfreq, const double* omegas, int nbeta, const double* betas, const double* Mmat,
+                         const double* Cmat, double* A_out, double* B_out, double* FK_out, double* SC_out,
+                         double* F_out, double* RAO_out, double* phiJ_out, double* phiS_out) {
     std::vector<V3> x = collocation(body);
-    const int N = ne, NB = nbeta;
+    const int N = (int)body.size(), NB = nbeta;
     std::vector<double> s((size_t)N * N), sr((size_t)N * N), d((size_t)N * N), dr((size_t)N * N), rn(N);
     #pragma omp parallel for schedule(dynamic, 4)
     for (int S = 0; S < N; ++S) {
@@ -972,6 +971,7 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
     std::vector<int> piv(N);
     for (int f = 0; f < nfreq; ++f) {
         double Omega = omegas[f];
+        if (Omega == 0.0 && ifr) Omega = 1.0e-3;
         double Kappa = Omega * Omega / Gravity;  // :409 uses the global Gravity
         bool wave = Omega != 0.0;
         #pragma omp parallel for schedule(dynamic, 4)
@@ -1021,12 +1021,12 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
             }
         }
         lu_solve(N, Dmat.data(), piv.data(), NR, rhs.data());
-        // Post (:462-487).  NPA = N (no IFR panels).
+        // Post (:462-487) over the NPA hull panels (:452-457 cut the solutions)
         cplx AM[36];
         for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) {
                 cplx acc(0, 0);
-                for (int p = 0; p < N; ++p) acc += (Nk[(size_t)p * 6 + i] * area[p]) * rhs[(size_t)p * NR + j];
+                for (int p = 0; p < NPA; ++p) acc += (Nk[(size_t)p * 6 + i] * area[p]) * rhs[(size_t)p * NR + j];
                 AM[i * 6 + j] = acc;
             }
         for (int i = 0; i < 36; ++i) { A_out[36 * f + i] = AM[i].real(); B_out[36 * f + i] = AM[i].imag(); }
@@ -1035,7 +1035,7 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
         for (int i = 0; i < 6; ++i)
             for (int b = 0; b < NB; ++b) {
                 cplx f1(0, 0), f2(0, 0);
-                for (int p = 0; p < N; ++p) {
+                for (int p = 0; p < NPA; ++p) {
                     f1 += (Nk[(size_t)p * 6 + i] * area[p]) * PhiI[(size_t)p * NB + b];
                     f2 += rhs[(size_t)p * NR + i] * (dPhiI[(size_t)p * NB + b] * area[p]);
                 }
@@ -1066,13 +1066,13 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
             }
         if (f == nfreq - 1) {
             if (phiJ_out)
-                for (int p = 0; p < N; ++p)
+                for (int p = 0; p < NPA; ++p)
                     for (int j = 0; j < 6; ++j) {
                         phiJ_out[2 * ((size_t)p * 6 + j)] = rhs[(size_t)p * NR + j].real();
                         phiJ_out[2 * ((size_t)p * 6 + j) + 1] = rhs[(size_t)p * NR + j].imag();
                     }
             if (phiS_out)
-                for (int p = 0; p < N; ++p)
+                for (int p = 0; p < NPA; ++p)
                     for (int b = 0; b < NB; ++b) {
                         phiS_out[2 * ((size_t)p * NB + b)] = rhs[(size_t)p * NR + 6 + b].real();
                         phiS_out[2 * ((size_t)p * NB + b) + 1] = rhs[(size_t)p * NR + 6 + b].imag();
@@ -1081,6 +1081,37 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
     }
 }
 
+
+void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+               const double* comp_origin, int nfreq, const double* omegas, int nbeta, const double* betas,
+               double grav_unused, const double* Mmat, const double* Cmat,
+               double* A_out, double* B_out, double* FK_out, double* SC_out, double* F_out, double* RAO_out,
+               double* phiJ_out, double* phiS_out) {
+    (void)grav_unused;
+    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
+    std::vector<Panel> body, mir;
+    build_panels(m, body, mir);
+    solve_panels(body, mir, ne, false, nfreq, omegas, nbeta, betas, Mmat, Cmat, A_out, B_out, FK_out, SC_out, F_out,
+                 RAO_out, phiJ_out, phiS_out);
+}
+
+// IFR: the hull mesh and the interior free-surface (aux) mesh.
+void orc_solve_ifr(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+                   const double* comp_origin, int ann, const double* anodes, int ane, const int* aelems, int ancomp,
+                   const int* acomp_first, const double* acomp_origin, int nfreq, const double* omegas, int nbeta,
+                   const double* betas, const double* Mmat, const double* Cmat, double* A_out, double* B_out,
+                   double* FK_out, double* SC_out, double* F_out, double* RAO_out, double* phiJ_out,
+                   double* phiS_out) {
+    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
+    Mesh am = make_mesh(ann, anodes, ane, aelems, ancomp, acomp_first, acomp_origin);
+    std::vector<Panel> body, mir, abody, amir;
+    build_panels(m, body, mir);
+    build_panels(am, abody, amir);
+    body.insert(body.end(), abody.begin(), abody.end());
+    mir.insert(mir.end(), amir.begin(), amir.end());
+    solve_panels(body, mir, ne, true, nfreq, omegas, nbeta, betas, Mmat, Cmat, A_out, B_out, FK_out, SC_out, F_out,
+                 RAO_out, phiJ_out, phiS_out);
+}
 
 // Exterior outputs of one frequency from given potentials Phi_J (N x 6) and
 // Phi_S (N x nb), complex interleaved:

@@ -98,6 +98,8 @@ class Oracle:
         L.orc_mass_hydrostatics.argtypes = mesh_args + mesh_args + [_d, _d, _d, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve.argtypes = mesh_args + [_i, _dp, _i, _dp, _d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                             _dp, _dp]
+        L.orc_solve_ifr.argtypes = mesh_args + mesh_args + [_i, _dp, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                                            _dp, _dp, _dp]
         L.orc_exterior.argtypes = mesh_args + [_d, _i, _dp, _dp, _dp, _i, _dp, _i, _dp, _dp, _dp, _dp]
         L.orc_num_threads.restype = _i
         L.orc_set_threads.argtypes = [_i]
@@ -193,8 +195,9 @@ class Oracle:
                                      _p(vc))
         return M, C, vc
 
-    def solve(self, mesh, omegas, betas, M=None, C=None, want_phi=False):
-        """Full FP64 frequency loop; omegas are the internal angular frequencies."""
+    def solve(self, mesh, omegas, betas, M=None, C=None, want_phi=False, ifr_aux=None):
+        """Full FP64 frequency loop; omegas are the internal angular frequencies.
+        ifr_aux: the interior free-surface mesh, solved with IFR (hull + lid panels)."""
         omegas = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
         betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
         nf, nb, N = omegas.size, betas.size, mesh.n
@@ -205,10 +208,13 @@ class Oracle:
         FK, SC, F, RAO = (np.zeros((nf, 6, nb), np.complex128) for _ in range(4))
         pj = np.zeros((N, 6), np.complex128) if want_phi else None
         ps = np.zeros((N, nb), np.complex128) if want_phi else None
-        self.L.orc_solve(*mesh.args(), nf, _p(omegas), nb, _p(betas), 9.81, _p(M), _p(C), _p(A), _p(B),
-                         _p(FK.view(np.float64)), _p(SC.view(np.float64)), _p(F.view(np.float64)),
-                         _p(RAO.view(np.float64)), _p(pj.view(np.float64)) if want_phi else None,
-                         _p(ps.view(np.float64)) if want_phi else None)
+        tail = (_p(M), _p(C), _p(A), _p(B), _p(FK.view(np.float64)), _p(SC.view(np.float64)),
+                _p(F.view(np.float64)), _p(RAO.view(np.float64)), _p(pj.view(np.float64)) if want_phi else None,
+                _p(ps.view(np.float64)) if want_phi else None)
+        if ifr_aux is None:
+            self.L.orc_solve(*mesh.args(), nf, _p(omegas), nb, _p(betas), 9.81, *tail)
+        else:
+            self.L.orc_solve_ifr(*mesh.args(), *ifr_aux.args(), nf, _p(omegas), nb, _p(betas), *tail)
         out = dict(A=A, B=B, FK=FK, SC=SC, F=F, RAO=RAO)
         if want_phi:
             out["phiJ"] = pj
