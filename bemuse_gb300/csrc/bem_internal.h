@@ -25,6 +25,16 @@ enum DevFlag : int {
     FLAG_GROWTH = 16,    // a multiplier |l_ik| > 16 (element growth a solve should not accept)
 };
 
+#ifdef __CUDACC__
+// Round-to-nearest TF32 value of x (10-bit mantissa, the low 13 bits cleared).  The
+// tensor cores truncate FP32 operands; operands rounded here carry unbiased errors.
+__device__ __forceinline__ float tf32_rn(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+#endif
+
 struct WaveArgs {
     int N, ld, R, mode;   // mode 0: assemble D and S*B; 1: raw ws/wd (N x N interleaved)
     double K;

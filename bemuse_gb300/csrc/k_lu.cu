@@ -241,14 +241,17 @@ __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A,
         *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
         *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
     }
-    if (dT) {  // the transpose, [2][128][128]: the K-major B operand of W21 = A21 D^-1
+    if (dT) {  // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const size_t g = (size_t)(8 * cg + c) * 128 + 8 * rg;
-            *reinterpret_cast<float4*>(dT + g) = make_float4(v[0][c].x, v[1][c].x, v[2][c].x, v[3][c].x);
-            *reinterpret_cast<float4*>(dT + g + 4) = make_float4(v[4][c].x, v[5][c].x, v[6][c].x, v[7][c].x);
-            *reinterpret_cast<float4*>(dT + 16384 + g) = make_float4(v[0][c].y, v[1][c].y, v[2][c].y, v[3][c].y);
-            *reinterpret_cast<float4*>(dT + 16384 + g + 4) = make_float4(v[4][c].y, v[5][c].y, v[6][c].y, v[7][c].y);
+            auto rn4 = [](float a, float b, float c_, float d) {
+                return make_float4(tf32_rn(a), tf32_rn(b), tf32_rn(c_), tf32_rn(d));
+            };
+            *reinterpret_cast<float4*>(dT + g) = rn4(v[0][c].x, v[1][c].x, v[2][c].x, v[3][c].x);
+            *reinterpret_cast<float4*>(dT + g + 4) = rn4(v[4][c].x, v[5][c].x, v[6][c].x, v[7][c].x);
+            *reinterpret_cast<float4*>(dT + 16384 + g) = rn4(v[0][c].y, v[1][c].y, v[2][c].y, v[3][c].y);
+            *reinterpret_cast<float4*>(dT + 16384 + g + 4) = rn4(v[4][c].y, v[5][c].y, v[6][c].y, v[7][c].y);
         }
     }
     if (lf) atomicOr(flags, lf);
@@ -400,8 +403,8 @@ __global__ void k_panel_transpose(int cols, CMat<float> A, int r0, int c0, float
     for (int y = threadIdx.y; y < 32; y += blockDim.y) {
         const int j = j0 + y;
         if (j < cols) {
-            wtr[(size_t)j * 128 + i0 + threadIdx.x] = tr[threadIdx.x][y];
-            wti[(size_t)j * 128 + i0 + threadIdx.x] = ti[threadIdx.x][y];
+            wtr[(size_t)j * 128 + i0 + threadIdx.x] = tf32_rn(tr[threadIdx.x][y]);
+            wti[(size_t)j * 128 + i0 + threadIdx.x] = tf32_rn(ti[threadIdx.x][y]);
         }
     }
 }
@@ -707,17 +710,21 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 // the critical path (one 32 x 128 tile against the newest block of x) is a
 // quarter of a block's.  Thread (lane i, warp s) owns row i of the sub-block
 // and the 16 columns s*16.. of every tile; the tile is prefetched into
-// registers one dependency ahead, the block of x is staged in shared memory
-// (complex interleaved, RC columns, zero-padded), and the eight column slices
-// are summed once at the end.
+// registers one dependency ahead, and the blocks of x are staged in shared
+// memory by cp.async, double-buffered: while a CTA multiplies one tile, the
+// x block of the next tile is already in flight whenever its producer has
+// published it.  The eight column slices are summed once at the end.
 //   which = 0 (forward, unit block-lower L):  x_b = y_b - sum_{c<b} L_bc x_c
 //   which = 1 (backward):  w_b = y_b - sum_{c>b} U_bc x_c  (written over y_b),
 //                          x_b = Dinv_b w_b once the four sub-blocks of w_b exist.
 // xflag[u] / wflag[u] (u = sub-block) are raised to `epoch` when x / w rows of u
 // are in memory.  Waits give up at a 2 s deadline (FLAG_TIMEOUT).
-// Grid: a multiple of 4 CTAs, all co-resident (cooperative launch); sub-blocks are
-// dealt out in dependency order, so the four siblings of a block always run
-// together on distinct CTAs and every wait is on work that is placed earlier.
+// Scheduling needs no co-residency (plain launch, one CTA per sub-block): each
+// CTA draws a ticket when it starts and tickets map to sub-blocks in dependency
+// order, so a CTA waits only on sub-blocks of CTAs that started before it, or
+// on its three siblings, which start no later than any CTA of a later block.
+// The lowest unfinished ticket therefore always progresses, whatever else runs
+// on the GPU.  The CTA that draws the last ticket resets the counter.
 constexpr int TS_NB = 128, TS_SB = 4, TS_KS = 8, TS_KC = TS_NB / TS_KS;
 
 __device__ __forceinline__ unsigned long long ts_now() {
@@ -737,6 +744,12 @@ __device__ __forceinline__ void ts_wait(const int* f, int epoch, unsigned long l
     }
 }
 
+__device__ __forceinline__ bool ts_ready(const int* f, int epoch) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+    return v >= epoch;
+}
+
 __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const float* __restrict__ gi, float* r,
                                             float* im) {
 #pragma unroll
@@ -748,178 +761,188 @@ __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const 
     }
 }
 
+// Floats of one staging buffer: a 128 x R complex block in its global layout, plus
+// RC complex of zero padding (rows are read RC wide), rounded to 16 bytes.
+__host__ __device__ constexpr int ts_zstride(int R, int RC) { return ((2 * (TS_NB * R + RC)) + 3) & ~3; }
+
 template <int RC>
-__global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_sub(int nblk, int R, CMat<float> A,
-                                                         const float* __restrict__ invr,
-                                                         const float* __restrict__ invi, int which, float* Yin,
-                                                         float* Xout, int* xflag, int* wflag, int epoch,
-                                                         int* gflags) {
+__global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat<float> A,
+                                                        const float* __restrict__ invr,
+                                                        const float* __restrict__ invi, int which, float* Yin,
+                                                        float* Xout, int* xflag, int* wflag, int* ticket,
+                                                        int epoch, int* gflags) {
     extern __shared__ __align__(16) float ts_smem[];
-    float* zs = ts_smem;                        // [2][TS_NB][RC] complex interleaved
-    float* red = zs + 2 * TS_NB * RC * 2;       // [TS_KS][32][RC] complex interleaved
+    __shared__ int s_ticket, s_go;
+    const int zs = ts_zstride(R, RC);
+    float* zb = ts_smem;                        // [2][zs]
+    float* red = zb + 2 * zs;                   // [TS_KS][32][RC] complex interleaved
+    float* ybase = red + TS_KS * 32 * RC * 2;   // [32][R] complex: this sub-block's rows of Yin
     const int tid = threadIdx.x, lane = tid & 31, s = tid >> 5;
     const unsigned long long deadline = ts_now() + 2000000000ull;
     int dead = 0;
-    for (int idx = tid; idx < 2 * TS_NB * RC * 2; idx += blockDim.x) zs[idx] = 0.f;
+    if (tid == 0) {
+        const int t = atomicAdd(ticket, 1);
+        if (t == (int)gridDim.x - 1) atomicExch(ticket, 0);  // every ticket of this launch is drawn
+        s_ticket = t;
+    }
+    for (int idx = 2 * TS_NB * R + tid; idx < zs; idx += blockDim.x) { zb[idx] = 0.f; zb[zs + idx] = 0.f; }
     __syncthreads();
-    const int nsub = nblk * TS_SB;
-    for (int u0 = blockIdx.x; u0 < nsub; u0 += gridDim.x) {
-        const int bo = u0 / TS_SB, q = u0 % TS_SB;
-        const int b = which == 0 ? bo : nblk - 1 - bo;
-        const int u = b * TS_SB + q;
-        const size_t row0 = (size_t)b * TS_NB + q * 32;
-        const int cnt = which == 0 ? b : nblk - 1 - b;
-        float ar[RC], ai[RC];
+    const int tk = s_ticket;
+    const int bo = tk / TS_SB, q = tk % TS_SB;
+    const int b = which == 0 ? bo : nblk - 1 - bo;
+    const int u = b * TS_SB + q;
+    const size_t row0 = (size_t)b * TS_NB + q * 32;
+    const int cnt = which == 0 ? b : nblk - 1 - b;
+    auto cidx = [&](int t) { return which == 0 ? t : nblk - 1 - t; };
+    // the sub-block's rows of Yin are static during the launch: fetch them now, off the
+    // critical path of the final reduction
+    for (int idx = tid; idx < 32 * R; idx += blockDim.x)
+        reinterpret_cast<float2*>(ybase)[idx] = reinterpret_cast<const float2*>(Yin)[row0 * R + idx];
+    // stage the 128 x R block of x (or w) at block c into buffer buf, 16 bytes per cp.async
+    auto issue_copy = [&](const float* src_base, int c, int buf) {
+        const float* src = src_base + (size_t)c * TS_NB * R * 2;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(zb + buf * zs);
+        for (int i = tid; i < TS_NB * R / 2; i += blockDim.x)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 4 * i)
+                         : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    float ar[RC], ai[RC];
 #pragma unroll
-        for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
-        float cr[TS_KC], ci[TS_KC], nr[TS_KC], ni[TS_KC];
-        auto tile_ptr = [&](int t, const float*& pr, const float*& pi) {
-            const int c = which == 0 ? t : nblk - 1 - t;
-            const size_t off = (row0 + lane) * A.ld + (size_t)c * TS_NB + s * TS_KC;
-            pr = A.re + off;
-            pi = A.im + off;
-        };
-        auto inv_ptr = [&](const float*& pr, const float*& pi) {
-            const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * 32 + lane) * TS_NB + s * TS_KC;
-            pr = invr + off;
-            pi = invi + off;
-        };
-        {
-            const float *pr, *pi;
-            if (cnt > 0) tile_ptr(0, pr, pi);
-            else inv_ptr(pr, pi);
-            if (cnt > 0 || which == 1) ts_load_row(pr, pi, cr, ci);
-        }
-        for (int t = 0; t < cnt; ++t) {
-            const int c = which == 0 ? t : nblk - 1 - t;
-            if (t + 1 < cnt || which == 1) {
-                const float *pr, *pi;
-                if (t + 1 < cnt) tile_ptr(t + 1, pr, pi);
-                else inv_ptr(pr, pi);
-                ts_load_row(pr, pi, nr, ni);
-            }
-            if (tid < TS_SB) {
-                ts_wait(xflag + c * TS_SB + tid, epoch, deadline, dead, gflags);
-            }
-            __syncthreads();
-            float* z = zs + (t & 1) * TS_NB * RC * 2;
-            for (int idx = tid; idx < TS_NB * R; idx += blockDim.x) {
-                const int k = idx / R, j = idx % R;
-                const float2 v = __ldcg(reinterpret_cast<const float2*>(Xout) + ((size_t)c * TS_NB + k) * R + j);
-                *reinterpret_cast<float2*>(z + (k * RC + j) * 2) = v;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int kk = 0; kk < TS_KC; ++kk) {
-                const float lr = cr[kk], li = ci[kk];
-                const float4* zk = reinterpret_cast<const float4*>(z + (s * TS_KC + kk) * RC * 2);
-#pragma unroll
-                for (int j2 = 0; j2 < RC / 2; ++j2) {
-                    const float4 v = zk[j2];
-                    ar[2 * j2] = fmaf(-lr, v.x, fmaf(li, v.y, ar[2 * j2]));
-                    ai[2 * j2] = fmaf(-lr, v.y, fmaf(-li, v.x, ai[2 * j2]));
-                    ar[2 * j2 + 1] = fmaf(-lr, v.z, fmaf(li, v.w, ar[2 * j2 + 1]));
-                    ai[2 * j2 + 1] = fmaf(-lr, v.w, fmaf(-li, v.z, ai[2 * j2 + 1]));
-                }
-            }
-#pragma unroll
-            for (int kk = 0; kk < TS_KC; ++kk) { cr[kk] = nr[kk]; ci[kk] = ni[kk]; }
-        }
-        // sum the column slices: out = y + sum_s acc_s
-        auto reduce_out = [&](const float* base, float* dst) {
-#pragma unroll
-            for (int j = 0; j < RC; ++j)
-                *reinterpret_cast<float2*>(red + ((s * 32 + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
-            __syncthreads();
-            for (int idx = tid; idx < 32 * R; idx += blockDim.x) {
-                const int i = idx / R, j = idx % R;
-                float2 o = base ? reinterpret_cast<const float2*>(base)[(row0 + i) * R + j] : make_float2(0.f, 0.f);
-#pragma unroll
-                for (int w = 0; w < TS_KS; ++w) {
-                    const float2 v = *reinterpret_cast<const float2*>(red + ((w * 32 + i) * RC + j) * 2);
-                    o.x += v.x;
-                    o.y += v.y;
-                }
-                reinterpret_cast<float2*>(dst)[(row0 + i) * R + j] = o;
-            }
-            // the CTA barrier orders every thread's stores before thread 0's fence and
-            // release store of the flag (release is cumulative), as in a grid barrier
-            __syncthreads();
-            if (tid == 0) __threadfence();
-        };
-        if (which == 0) {
-            reduce_out(Yin, Xout);
-            if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
-            continue;
-        }
-        // backward: w rows over y, then x = Dinv_b w_b (cr/ci hold the Dinv rows)
-        reduce_out(Yin, Yin);
-        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(wflag + u), "r"(epoch) : "memory");
-        if (tid < TS_SB) {
-            ts_wait(wflag + b * TS_SB + tid, epoch, deadline, dead, gflags);
-        }
-        __syncthreads();
-        float* z = zs;
-        for (int idx = tid; idx < TS_NB * R; idx += blockDim.x) {
-            const int k = idx / R, j = idx % R;
-            const float2 v = __ldcg(reinterpret_cast<const float2*>(Yin) + ((size_t)b * TS_NB + k) * R + j);
-            *reinterpret_cast<float2*>(z + (k * RC + j) * 2) = v;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+    for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+    float cr[TS_KC], ci[TS_KC], nr[TS_KC], ni[TS_KC];
+    auto tile_ptr = [&](int t, const float*& pr, const float*& pi) {
+        const size_t off = (row0 + lane) * A.ld + (size_t)cidx(t) * TS_NB + s * TS_KC;
+        pr = A.re + off;
+        pi = A.im + off;
+    };
+    auto inv_ptr = [&](const float*& pr, const float*& pi) {
+        const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * 32 + lane) * TS_NB + s * TS_KC;
+        pr = invr + off;
+        pi = invi + off;
+    };
+    // z (a staged block) times the register tile: acc += sgn * tile * z
+    auto mac = [&](const float* z, float sg) {
 #pragma unroll
         for (int kk = 0; kk < TS_KC; ++kk) {
-            const float lr = cr[kk], li = ci[kk];
-            const float4* zk = reinterpret_cast<const float4*>(z + (s * TS_KC + kk) * RC * 2);
+            const float lr = sg * cr[kk], li = sg * ci[kk];
+            const float2* zk = reinterpret_cast<const float2*>(z) + (size_t)(s * TS_KC + kk) * R;
 #pragma unroll
-            for (int j2 = 0; j2 < RC / 2; ++j2) {
-                const float4 v = zk[j2];
-                ar[2 * j2] = fmaf(lr, v.x, fmaf(-li, v.y, ar[2 * j2]));
-                ai[2 * j2] = fmaf(lr, v.y, fmaf(li, v.x, ai[2 * j2]));
-                ar[2 * j2 + 1] = fmaf(lr, v.z, fmaf(-li, v.w, ar[2 * j2 + 1]));
-                ai[2 * j2 + 1] = fmaf(lr, v.w, fmaf(li, v.z, ai[2 * j2 + 1]));
+            for (int j = 0; j < RC; ++j) {  // columns j >= R read padding or the next row: never stored
+                const float2 v = zk[j];
+                ar[j] = fmaf(lr, v.x, fmaf(-li, v.y, ar[j]));
+                ai[j] = fmaf(lr, v.y, fmaf(li, v.x, ai[j]));
             }
         }
-        reduce_out(nullptr, Xout);
-        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+    };
+    {
+        const float *pr, *pi;
+        if (cnt > 0) tile_ptr(0, pr, pi);
+        else inv_ptr(pr, pi);
+        if (cnt > 0 || which == 1) ts_load_row(pr, pi, cr, ci);
     }
+    if (cnt > 0) {
+        if (tid < TS_SB) ts_wait(xflag + cidx(0) * TS_SB + tid, epoch, deadline, dead, gflags);
+        __syncthreads();
+        issue_copy(Xout, cidx(0), 0);
+    }
+    for (int t = 0; t < cnt; ++t) {
+        if (t + 1 < cnt || which == 1) {
+            const float *pr, *pi;
+            if (t + 1 < cnt) tile_ptr(t + 1, pr, pi);
+            else inv_ptr(pr, pi);
+            ts_load_row(pr, pi, nr, ni);
+        }
+        // start the next block's copy now if its producer is done
+        bool early = false;
+        if (t + 1 < cnt) {
+            if (tid == 0) {
+                bool ok = true;
+                for (int k = 0; k < TS_SB; ++k) ok = ok && ts_ready(xflag + cidx(t + 1) * TS_SB + k, epoch);
+                s_go = ok ? 1 : 0;
+            }
+            __syncthreads();
+            early = s_go != 0;
+            if (early) issue_copy(Xout, cidx(t + 1), (t + 1) & 1);
+        }
+        if (early) asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();
+        mac(zb + (t & 1) * zs, -1.f);
+        __syncthreads();  // buffer t & 1 is refilled for tile t + 2
+        if (t + 1 < cnt && !early) {
+            if (tid < TS_SB) ts_wait(xflag + cidx(t + 1) * TS_SB + tid, epoch, deadline, dead, gflags);
+            __syncthreads();
+            issue_copy(Xout, cidx(t + 1), (t + 1) & 1);
+        }
+#pragma unroll
+        for (int kk = 0; kk < TS_KC; ++kk) { cr[kk] = nr[kk]; ci[kk] = ni[kk]; }
+    }
+    // sum the column slices: out = y + sum_s acc_s
+    auto reduce_out = [&](bool add_y, float* dst) {
+#pragma unroll
+        for (int j = 0; j < RC; ++j)
+            *reinterpret_cast<float2*>(red + ((s * 32 + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+        __syncthreads();
+        for (int idx = tid; idx < 32 * R; idx += blockDim.x) {
+            const int i = idx / R, j = idx % R;
+            float2 o = add_y ? reinterpret_cast<const float2*>(ybase)[idx] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int w = 0; w < TS_KS; ++w) {
+                const float2 v = *reinterpret_cast<const float2*>(red + ((w * 32 + i) * RC + j) * 2);
+                o.x += v.x;
+                o.y += v.y;
+            }
+            reinterpret_cast<float2*>(dst)[(row0 + i) * R + j] = o;
+        }
+        // the CTA barrier orders every thread's stores before thread 0's fence and
+        // release store of the flag (release is cumulative), as in a grid barrier
+        __syncthreads();
+        if (tid == 0) __threadfence();
+    };
+    if (which == 0) {
+        reduce_out(true, Xout);
+        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+        return;
+    }
+    // backward: w rows over y, then x = Dinv_b w_b (cr/ci hold the Dinv rows)
+    reduce_out(true, Yin);
+    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(wflag + u), "r"(epoch) : "memory");
+    if (tid < TS_SB) ts_wait(wflag + b * TS_SB + tid, epoch, deadline, dead, gflags);
+    __syncthreads();
+    issue_copy(Yin, b, 0);
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+    mac(zb, 1.f);
+    reduce_out(false, Xout);
+    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
 }
 
 template <int RC>
-static int trsv_sub_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which,
-                           int R, float* Y, float* X, int* xflag, int* wflag, int epoch, int* flags) {
+static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which,
+                          int R, float* Y, float* X, int* xflag, int* wflag, int* ticket, int epoch, int* flags) {
     const int nblk = n / TS_NB;
-    const size_t smem = sizeof(float) * (2 * TS_NB * RC * 2 + TS_KS * 32 * RC * 2);
+    const size_t smem = sizeof(float) * (2 * (size_t)ts_zstride(R, RC) + TS_KS * 32 * RC * 2 + 32 * 2 * R);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_trsv_sub<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int dev = 0, nsm = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trsv_sub<RC>, 32 * TS_KS, smem);
-    int grid = std::min(nblk * TS_SB, std::max(1, per_sm) * nsm);
-    grid -= grid % TS_SB;
-    if (grid < TS_SB) return 1;
-    void* args[] = {(void*)&nblk, (void*)&R,     (void*)&A,     (void*)&invr,  (void*)&invi,  (void*)&which,
-                    (void*)&Y,    (void*)&X,     (void*)&xflag, (void*)&wflag, (void*)&epoch, (void*)&flags};
-    ++g_launches;
-    return cudaLaunchCooperativeKernel((void*)k_trsv_sub<RC>, dim3(grid), dim3(32 * TS_KS), args, smem, st) ==
-                   cudaSuccess
-               ? 0
-               : 1;
+        cudaFuncSetAttribute(k_trsv_tk<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, 32 * TS_KS, smem, st>>>(nblk, R, A, invr, invi, which, Y, X, xflag,
+                                                                      wflag, ticket, epoch, flags));
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
 
-static int trsv_sub(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which, int R,
-                    float* Y, float* X, int* xflag, int* wflag, int epoch, int* flags) {
+static int trsv_tk(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which, int R,
+                   float* Y, float* X, int* xflag, int* wflag, int* ticket, int epoch, int* flags) {
     switch ((R + 1) / 2) {
-        case 1: return trsv_sub_launch<2>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 2: return trsv_sub_launch<4>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 3: return trsv_sub_launch<6>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 4: return trsv_sub_launch<8>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 5: return trsv_sub_launch<10>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 6: return trsv_sub_launch<12>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 7: return trsv_sub_launch<14>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
-        case 8: return trsv_sub_launch<16>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, epoch, flags);
+        case 1: return trsv_tk_launch<2>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 2: return trsv_tk_launch<4>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 3: return trsv_tk_launch<6>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 4: return trsv_tk_launch<8>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 5: return trsv_tk_launch<10>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 6: return trsv_tk_launch<12>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 7: return trsv_tk_launch<14>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 8: return trsv_tk_launch<16>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
         default: return 1;
     }
 }
@@ -934,12 +957,14 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
-    // ready holds n/16 flags: x flags of the n/32 sub-blocks, then their w flags.
+    // ready holds n/16 flags (x flags of the n/32 sub-blocks, then their w flags) and a
+    // ticket counter, zero between launches.
     float* tmp = X + (size_t)2 * n * R;
     int* xflag = ready;
     int* wflag = ready + n / 32;
-    if (trsv_sub(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, epoch, flags)) return 1;
-    return trsv_sub(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, epoch + 1, flags);
+    int* ticket = ready + n / 16;
+    if (trsv_tk(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, ticket, epoch, flags)) return 1;
+    return trsv_tk(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, ticket, epoch + 1, flags);
 }
 
 // ---------------------------------------------------------------------------

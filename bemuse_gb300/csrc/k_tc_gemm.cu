@@ -286,8 +286,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const uint32_t sa = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
-                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(sgn * v[4 * j]),
-                                     "f"(sgn * v[4 * j + 1]), "f"(sgn * v[4 * j + 2]), "f"(sgn * v[4 * j + 3])
+                        float o0 = sgn * v[4 * j], o1 = sgn * v[4 * j + 1], o2 = sgn * v[4 * j + 2],
+                              o3 = sgn * v[4 * j + 3];
+                        if (a.mode) {  // W21 is the L operand of later updates: round it once, to nearest
+                            o0 = tf32_rn(o0); o1 = tf32_rn(o1); o2 = tf32_rn(o2); o3 = tf32_rn(o3);
+                        }
+                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(o0), "f"(o1),
+                                     "f"(o2), "f"(o3)
                                      : "memory");
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
