@@ -15,6 +15,7 @@
 #include <atomic>
 #include <cmath>
 #include <complex>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -100,9 +101,14 @@ struct bem_ctx {
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
+    cudaEvent_t ev_lu_done = nullptr;           // LU of the current frequency done (pipelined solves)
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 0;                     // 0: short-lived trailing-update CTAs (see bem_set_tuning)
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
+    // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
+    // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
+    int asm_overlap = 1, asm_reserve = 8, asm_per_sm = 3;
+    int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
@@ -182,6 +188,7 @@ void free_all(bem_ctx* ctx) {
     ctx->d_gq32 = nullptr;
     ctx->d_wpts = ctx->d_ext = nullptr;
     ctx->wpts_cap = ctx->ext_cap = 0;
+    ctx->d_wctr = nullptr;
     ctx->wpts_dirty = true;
     ctx->ready = false;
 }
@@ -284,7 +291,8 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
 // the right-hand sides; the solution lands in d_X.  mixed: TF32 LU of the FP32
 // copy + FP64 refinement against D64; plain: FP64 LU of D64 (destroyed).
 bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
-                            double* resid_out, double* t_lu, double* t_solve) {
+                            double* resid_out, double* t_lu, double* t_solve,
+                            const std::function<bem_status()>& after_lu = nullptr) {
     cudaStream_t st = ctx->st;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
@@ -322,6 +330,11 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         if (rc_lu != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev[3], st));
+        if (after_lu) {
+            // work that should overlap the solves rather than the factorization
+            const bem_status sa = after_lu();
+            if (sa != BEM_OK) return sa;
+        }
         // x0 = LU^-1 y
         CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * nr2, st));
         CK(cudaMemcpyAsync(ctx->d_Rr, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
@@ -473,6 +486,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
+    CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
     CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
     for (FreqState& F : ctx->fs) {
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
@@ -502,6 +516,7 @@ void bem_destroy(bem_ctx* ctx) {
     for (auto& ev : ctx->ev_wk)
         if (ev) cudaEventDestroy(ev);
     if (ctx->ev_call) cudaEventDestroy(ctx->ev_call);
+    if (ctx->ev_lu_done) cudaEventDestroy(ctx->ev_lu_done);
     for (auto e : ctx->lu_tl) cudaEventDestroy(e);
     if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
     if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
@@ -651,6 +666,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_area, N);
     DA(ctx->d_Nk, 6 * (size_t)N);
     DA(ctx->d_betas, std::max(NB, 1));
+    DA(ctx->d_wctr, 1 + bem::WAVE_SM_SLOTS);
     DA(ctx->d_RS, (size_t)N * Np);
     DA(ctx->d_RD, (size_t)N * Np);
     DA(ctx->d_RSR, (size_t)N * Np);
@@ -774,6 +790,10 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         a.Dlo = F.Dlo;
         a.D64r = nullptr;
         a.D64i = nullptr;
+        a.row_ctr = ctx->d_wctr;
+        a.sm_ctr = ctx->d_wctr + 1;
+        a.reserve = ctx->asm_overlap ? ctx->asm_reserve : 0;
+        a.per_sm = ctx->asm_overlap ? ctx->asm_per_sm : 3;
     }
     CK(cudaEventRecord(F.ev_t[2], st));
     bem::launch_wave(st, a, mixed);
@@ -860,20 +880,31 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     for (int f = 0; f < n_freq; ++f) {
         FreqState& F = slot(f);
         const double Om = omega[f];
-        if (pipe && f + 1 < n_freq) {
-            s = enqueue_assembly(f + 1);
+        if (pipe && ctx->asm_overlap && f + 1 < n_freq) {
+            s = enqueue_assembly(f + 1);  // overlaps this frequency's LU and solve
             if (s != BEM_OK) return s;
         } else if (!pipe && f > 0) {
             s = enqueue_assembly(f);
             if (s != BEM_OK) return s;
         }
+        // Pipelined: the assembly of frequency f + 1 (stream sa) starts when the LU of f
+        // has been queued and finished: it then shares the GPU with the latency-bound
+        // solves of f instead of slowing the LU's panel chain (whose one-SM block
+        // inverse cannot start on an SM filled with assembly CTAs).
+        std::function<bem_status()> next_asm;
+        if (pipe && !ctx->asm_overlap && f + 1 < n_freq)
+            next_asm = [&, f]() -> bem_status {
+                CK(cudaEventRecord(ctx->ev_lu_done, st));
+                CK(cudaStreamWaitEvent(sa, ctx->ev_lu_done, 0));
+                return enqueue_assembly(f + 1);
+            };
         const double K = F.K;  // set by this frequency's assemble()
         if (pipe) CK(cudaStreamWaitEvent(st, F.ev_asm, 0));
         int iters = 0;
         double resid = 0;
         double t_lu = 0, t_sv = 0;
         ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
-        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv);
+        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv, next_asm);
         ctx->resid_mode = 0;
         if (s != BEM_OK) {
             if (pipe) cudaStreamSynchronize(sa);
@@ -1042,6 +1073,10 @@ bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, 
     a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
     a.xr32 = ctx->d_xr32;
     a.gq32 = ctx->d_gq32;
+    a.row_ctr = ctx->d_wctr;
+    a.sm_ctr = ctx->d_wctr + 1;
+    a.reserve = 0;
+    a.per_sm = 3;
     bem::launch_wave(ctx->st, a, precision == BEM_MIXED);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(ws, buf, sizeof(double) * 2 * N * N, cudaMemcpyDeviceToHost, ctx->st);
@@ -1271,6 +1306,21 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_rest_tiles") {
         if (!(value >= 1 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "lu_rest_tiles must be in [1, 64]");
         ctx->lu_rest_tiles = (int)value;
+        return BEM_OK;
+    }
+    if (k == "asm_overlap") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "asm_overlap must be 0 or 1");
+        ctx->asm_overlap = (int)value;
+        return BEM_OK;
+    }
+    if (k == "asm_reserve_sms") {
+        if (!(value >= 0 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "asm_reserve_sms must be in [0, 64]");
+        ctx->asm_reserve = (int)value;
+        return BEM_OK;
+    }
+    if (k == "asm_ctas_per_sm") {
+        if (!(value >= 1 && value <= 3)) return fail(ctx, BEM_ERR_ARG, "asm_ctas_per_sm must be in [1, 3]");
+        ctx->asm_per_sm = (int)value;
         return BEM_OK;
     }
     return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);

@@ -16,6 +16,7 @@
 // panel, leading dimension ld (a multiple of 128).  Complex matrices are planar
 // (separate re and im arrays).
 #include "bem_internal.h"
+#include <algorithm>
 #include "green.cuh"
 
 namespace bem {
@@ -212,109 +213,132 @@ __global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
 // O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
 __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (r >= a.N) return;
-    const int N = a.N, R = a.R;
-    const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
-    const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
-    const float K = (float)a.K;
-    const float Kh = K, Kl = (float)(a.K - (double)K);
-    const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
-    const float twopi = 6.28318530717959f;
-    float acc_re[MAX_RHS], acc_im[MAX_RHS];
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
-    const size_t row = (size_t)r * a.ld;
-    const bool live = a.K != 0.0;
-    const size_t fs = (size_t)4 * N;
-    for (int s = lane; s < N; s += 32) {
-        float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
-        const int nq = live ? a.nq[s] : 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (q < nq) {
-                const float* g = a.gq32 + (size_t)q * N + s;
-                // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
-                const float gx = g[0], gy = g[fs];
-                const float sx = xh - gx, sy = yh - gy;
-                float bx = sx - xh, by = sy - yh;
-                const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - g[7 * fs]);
-                const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - g[8 * fs]);
-                float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
-                float w = g[3 * fs], nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
-                float XX = (sx + lx) * K, YY = (sy + ly) * K, VV = dz * K;
-                float hh, hl;
-                df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
-                float ev = expf(VV);
-                float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
-                if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
-                else bessel_j01_small(hh, j0v, j1v);
-                float Gr, Ghr;
-                gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr);
-                float proj = fmaf(XX, nx, YY * ny);
-                float dgr = 0.f, dgi = 0.f;
-                if (hh > 1.0e-6f) {
-                    float inv_h = __frcp_rn(hh);
-                    dgr = Ghr * proj * inv_h;
-                    dgi = twopi * ev * j1v * proj * inv_h;
-                }
-                float Gi = -twopi * ev * j0v;
-                wsr = fmaf(w * c1, Gr, wsr);
-                wsi = fmaf(w * c1, Gi, wsi);
-                wdr = fmaf(w * c2, fmaf(Gr, nz, dgr), wdr);
-                wdi = fmaf(w * c2, fmaf(Gi, nz, dgi), wdi);
+    __shared__ int s_admit;
+    uint32_t smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    if (smid >= (uint32_t)WAVE_SM_SLOTS) smid = WAVE_SM_SLOTS - 1;  // only the admission policy shares a slot
+    if (threadIdx.x == 0) {
+        int ok = (int)smid >= a.reserve;
+        if (ok) {
+            if (atomicAdd(a.sm_ctr + smid, 1) >= a.per_sm) {
+                atomicSub(a.sm_ctr + smid, 1);
+                ok = 0;
             }
         }
-        if (a.mode == 1) {
-            size_t o = 2 * ((size_t)r * N + s);
-            a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = (double)wsi;
-            a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
-            continue;
+        s_admit = ok;
+    }
+    __syncthreads();
+    if (!s_admit) return;
+    for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(a.row_ctr, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= a.N) break;
+        const int N = a.N, R = a.R;
+        const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
+        const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
+        const float K = (float)a.K;
+        const float Kh = K, Kl = (float)(a.K - (double)K);
+        const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
+        const float twopi = 6.28318530717959f;
+        float acc_re[MAX_RHS], acc_im[MAX_RHS];
+    #pragma unroll
+        for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
+        const size_t row = (size_t)r * a.ld;
+        const bool live = a.K != 0.0;
+        const size_t fs = (size_t)4 * N;
+        for (int s = lane; s < N; s += 32) {
+            float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
+            const int nq = live ? a.nq[s] : 0;
+    #pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q < nq) {
+                    const float* g = a.gq32 + (size_t)q * N + s;
+                    // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
+                    const float gx = g[0], gy = g[fs];
+                    const float sx = xh - gx, sy = yh - gy;
+                    float bx = sx - xh, by = sy - yh;
+                    const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - g[7 * fs]);
+                    const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - g[8 * fs]);
+                    float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
+                    float w = g[3 * fs], nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
+                    float XX = (sx + lx) * K, YY = (sy + ly) * K, VV = dz * K;
+                    float hh, hl;
+                    df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
+                    float ev = expf(VV);
+                    float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
+                    if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
+                    else bessel_j01_small(hh, j0v, j1v);
+                    float Gr, Ghr;
+                    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr);
+                    float proj = fmaf(XX, nx, YY * ny);
+                    float dgr = 0.f, dgi = 0.f;
+                    if (hh > 1.0e-6f) {
+                        float inv_h = __frcp_rn(hh);
+                        dgr = Ghr * proj * inv_h;
+                        dgi = twopi * ev * j1v * proj * inv_h;
+                    }
+                    float Gi = -twopi * ev * j0v;
+                    wsr = fmaf(w * c1, Gr, wsr);
+                    wsi = fmaf(w * c1, Gi, wsi);
+                    wdr = fmaf(w * c2, fmaf(Gr, nz, dgr), wdr);
+                    wdi = fmaf(w * c2, fmaf(Gi, nz, dgi), wdi);
+                }
+            }
+            if (a.mode == 1) {
+                size_t o = 2 * ((size_t)r * N + s);
+                a.ws_out[o] = (double)wsr; a.ws_out[o + 1] = (double)wsi;
+                a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
+                continue;
+            }
+            // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
+            // FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
+            const float rdh = a.RDhi[row + s], rdl = a.RDlo[row + s];
+            const float rsh = a.RSRhi[row + s], rsl = a.RSRlo[row + s];
+            const float ph = Kh * rsh;
+            const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
+            const float sh = rdh + ph;
+            float bb = sh - rdh;
+            const float se = ((rdh - (sh - bb)) + (ph - bb)) + (rdl + pe);
+            const float th = sh + wdr;
+            bb = th - sh;
+            const float te = ((sh - (th - bb)) + (wdr - bb)) + se;
+            const float hi = th + te;
+            a.Dhi[row + s] = hi;
+            a.Dlo[row + s] = te - (hi - th);
+            a.D32r[row + s] = hi;
+            a.D32i[row + s] = wdi;
+            // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
+            const float* b = a.Bm32 + (size_t)s * 2 * R;
+    #pragma unroll
+            for (int j = 0; j < MAX_RHS; ++j) {
+                if (j < R) {
+                    acc_re[j] = fmaf(-wsr, b[2 * j], acc_re[j]);
+                    acc_im[j] = fmaf(-wsr, b[2 * j + 1], acc_im[j]);
+                }
+            }
         }
-        // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
-        // FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
-        const float rdh = a.RDhi[row + s], rdl = a.RDlo[row + s];
-        const float rsh = a.RSRhi[row + s], rsl = a.RSRlo[row + s];
-        const float ph = Kh * rsh;
-        const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
-        const float sh = rdh + ph;
-        float bb = sh - rdh;
-        const float se = ((rdh - (sh - bb)) + (ph - bb)) + (rdl + pe);
-        const float th = sh + wdr;
-        bb = th - sh;
-        const float te = ((sh - (th - bb)) + (wdr - bb)) + se;
-        const float hi = th + te;
-        a.Dhi[row + s] = hi;
-        a.Dlo[row + s] = te - (hi - th);
-        a.D32r[row + s] = hi;
-        a.D32i[row + s] = wdi;
-        // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
-        const float* b = a.Bm32 + (size_t)s * 2 * R;
-#pragma unroll
+        if (a.mode == 1) continue;
+    #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) {
             if (j < R) {
-                acc_re[j] = fmaf(-wsr, b[2 * j], acc_re[j]);
-                acc_im[j] = fmaf(-wsr, b[2 * j + 1], acc_im[j]);
+                float vr = acc_re[j], vi = acc_im[j];
+    #pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    vr += __shfl_xor_sync(0xffffffffu, vr, off);
+                    vi += __shfl_xor_sync(0xffffffffu, vi, off);
+                }
+                if (lane == 0) {
+                    a.Y[2 * ((size_t)r * R + j)] += (double)vr;
+                    a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
+                }
             }
         }
     }
-    if (a.mode == 1) return;
-#pragma unroll
-    for (int j = 0; j < MAX_RHS; ++j) {
-        if (j < R) {
-            float vr = acc_re[j], vi = acc_im[j];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                vr += __shfl_xor_sync(0xffffffffu, vr, off);
-                vi += __shfl_xor_sync(0xffffffffu, vi, off);
-            }
-            if (lane == 0) {
-                a.Y[2 * ((size_t)r * R + j)] += (double)vr;
-                a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
-            }
-        }
-    }
+    __syncthreads();
+    if (threadIdx.x == 0) atomicSub(a.sm_ctr + smid, 1);
 }
+
 
 // ---------------------------------------------------------------------------
 // Exact FP64 imaginary parts by plane waves.  With Bessel's integral
@@ -769,9 +793,16 @@ void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const dou
 }
 
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
-    dim3 grd((a.N + 7) / 8);
-    if (fp32) BEM_LAUNCH(k_wave_mixed<<<grd, 256, 0, st>>>(a));
-    else BEM_LAUNCH(k_wave<double><<<grd, 256, 0, st>>>(a));
+    if (fp32) {
+        // persistent: three CTAs per SM when the GPU is free (the occupancy limit)
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (1 + WAVE_SM_SLOTS), st);
+        BEM_LAUNCH(k_wave_mixed<<<std::min(3 * nsm, (a.N + 7) / 8), 256, 0, st>>>(a));
+    } else {
+        BEM_LAUNCH(k_wave<double><<<(a.N + 7) / 8, 256, 0, st>>>(a));
+    }
 }
 
 void launch_pw_build(cudaStream_t st, int N, int M, double K, const double* xr, const double* gq, const int* nq,
