@@ -63,7 +63,13 @@ struct WaveArgs {
     int* row_ctr;
     int* sm_ctr;
     int reserve, per_sm;
+    // FP32 constants of the mixed kernel, computed on the host so that no FP64 instruction
+    // (slow on this GPU) can be rematerialised inside its inner loop: K = kh + kl,
+    // c1 = K / (4 pi), c2 = K^2 / (4 pi), live = (K != 0)
+    float kh, kl, c1f, c2f;
+    int live;
 };
+void set_wave_f32_constants(WaveArgs& a);
 
 cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,

@@ -237,15 +237,15 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         const int N = a.N, R = a.R;
         const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
         const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
-        const float K = (float)a.K;
-        const float Kh = K, Kl = (float)(a.K - (double)K);
-        const float c1 = (float)(a.K * kFourPIinv), c2 = (float)(a.K * a.K * kFourPIinv);
+        const float K = a.kh;
+        const float Kh = a.kh, Kl = a.kl;
+        const float c1 = a.c1f, c2 = a.c2f;
         const float twopi = 6.28318530717959f;
         float acc_re[MAX_RHS], acc_im[MAX_RHS];
     #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
         const size_t row = (size_t)r * a.ld;
-        const bool live = a.K != 0.0;
+        const bool live = a.live != 0;
         const size_t fs = (size_t)4 * N;
         for (int s = lane; s < N; s += 32) {
             float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
@@ -792,14 +792,24 @@ void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const dou
     BEM_LAUNCH(k_rankine<<<grd, blk, 0, st>>>(N, ld, rec, xr, rn, mode, o0, o1, o2, o3));
 }
 
+void set_wave_f32_constants(WaveArgs& a) {
+    a.kh = (float)a.K;
+    a.kl = (float)(a.K - (double)a.kh);
+    a.c1f = (float)(a.K * kFourPIinv);
+    a.c2f = (float)(a.K * a.K * kFourPIinv);
+    a.live = a.K != 0.0 ? 1 : 0;
+}
+
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
     if (fp32) {
+        WaveArgs b = a;
+        set_wave_f32_constants(b);
         // persistent: three CTAs per SM when the GPU is free (the occupancy limit)
         int dev = 0, nsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (1 + WAVE_SM_SLOTS), st);
-        BEM_LAUNCH(k_wave_mixed<<<std::min(3 * nsm, (a.N + 7) / 8), 256, 0, st>>>(a));
+        BEM_LAUNCH(k_wave_mixed<<<std::min(3 * nsm, (b.N + 7) / 8), 256, 0, st>>>(b));
     } else {
         BEM_LAUNCH(k_wave<double><<<(a.N + 7) / 8, 256, 0, st>>>(a));
     }
