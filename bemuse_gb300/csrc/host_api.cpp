@@ -279,8 +279,8 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     DA(ctx->fs[0].mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
     DA(ctx->d_flags, 1);
     if (!ctx->d_ready) {
-        DA(ctx->d_ready, Np / 16 + 32);  // sub-block flags + the FP32 solve's ticket counter
-        CK(cudaMemsetAsync(ctx->d_ready, 0, sizeof(int) * (Np / 16 + 32), ctx->st));
+        DA(ctx->d_ready, Np / 8 + 32);  // sub-block flags + the FP32 solve's ticket counter
+        CK(cudaMemsetAsync(ctx->d_ready, 0, sizeof(int) * (Np / 8 + 32), ctx->st));
         ctx->solve_epoch = 0;
     }
     DA(ctx->d_norms, 2 * bem::MAX_RHS);

@@ -706,10 +706,10 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 
 // ---------------------------------------------------------------------------
 // FP32 block triangular solve, split by rows: each 128-row block of the system
-// is shared by four CTAs of 32 rows (sub-blocks), so the product that sits on
-// the critical path (one 32 x 128 tile against the newest block of x) is a
-// quarter of a block's.  Thread (lane i, warp s) owns row i of the sub-block
-// and the 16 columns s*16.. of every tile; the tile is prefetched into
+// is shared by eight CTAs of 16 rows (sub-blocks), so the product that sits on
+// the critical path (one 16 x 128 tile against the newest block of x) is an
+// eighth of a block's.  Thread (i, s) = (tid % 16, tid / 16) owns row i of the
+// sub-block and the 8 columns s*8.. of every tile; the tile is prefetched into
 // registers one dependency ahead, and the blocks of x are staged in shared
 // memory by cp.async, double-buffered: while a CTA multiplies one tile, the
 // x block of the next tile is already in flight whenever its producer has
@@ -724,8 +724,12 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 // order, so a CTA waits only on sub-blocks of CTAs that started before it, or
 // on its three siblings, which start no later than any CTA of a later block.
 // The lowest unfinished ticket therefore always progresses, whatever else runs
-// on the GPU.  The CTA that draws the last ticket resets the counter.
-constexpr int TS_NB = 128, TS_SB = 4, TS_KS = 8, TS_KC = TS_NB / TS_KS;
+// on the GPU (given room for the eight siblings).  The CTA that draws the last
+// ticket resets the counter.
+// TS_SB sub-blocks of TS_RW rows per 128-row block; a CTA's 256 threads are TS_RW rows x
+// TS_SL column slices of TS_KC columns.
+constexpr int TS_NB = 128, TS_SB = 8, TS_RW = TS_NB / TS_SB, TS_THREADS = 256, TS_SL = TS_THREADS / TS_RW,
+              TS_KC = TS_NB / TS_SL;
 
 __device__ __forceinline__ unsigned long long ts_now() {
     unsigned long long t;
@@ -766,7 +770,7 @@ __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const 
 __host__ __device__ constexpr int ts_zstride(int R, int RC) { return ((2 * (TS_NB * R + RC)) + 3) & ~3; }
 
 template <int RC>
-__global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat<float> A,
+__global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat<float> A,
                                                         const float* __restrict__ invr,
                                                         const float* __restrict__ invi, int which, float* Yin,
                                                         float* Xout, int* xflag, int* wflag, int* ticket,
@@ -775,9 +779,9 @@ __global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat
     __shared__ int s_ticket, s_go;
     const int zs = ts_zstride(R, RC);
     float* zb = ts_smem;                        // [2][zs]
-    float* red = zb + 2 * zs;                   // [TS_KS][32][RC] complex interleaved
-    float* ybase = red + TS_KS * 32 * RC * 2;   // [32][R] complex: this sub-block's rows of Yin
-    const int tid = threadIdx.x, lane = tid & 31, s = tid >> 5;
+    float* red = zb + 2 * zs;                   // [TS_SL][TS_RW][RC] complex interleaved
+    float* ybase = red + TS_SL * TS_RW * RC * 2;  // [TS_RW][R] complex: this sub-block's rows of Yin
+    const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW;
     const unsigned long long deadline = ts_now() + 2000000000ull;
     int dead = 0;
     if (tid == 0) {
@@ -791,12 +795,12 @@ __global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat
     const int bo = tk / TS_SB, q = tk % TS_SB;
     const int b = which == 0 ? bo : nblk - 1 - bo;
     const int u = b * TS_SB + q;
-    const size_t row0 = (size_t)b * TS_NB + q * 32;
+    const size_t row0 = (size_t)b * TS_NB + q * TS_RW;
     const int cnt = which == 0 ? b : nblk - 1 - b;
     auto cidx = [&](int t) { return which == 0 ? t : nblk - 1 - t; };
     // the sub-block's rows of Yin are static during the launch: fetch them now, off the
     // critical path of the final reduction
-    for (int idx = tid; idx < 32 * R; idx += blockDim.x)
+    for (int idx = tid; idx < TS_RW * R; idx += blockDim.x)
         reinterpret_cast<float2*>(ybase)[idx] = reinterpret_cast<const float2*>(Yin)[row0 * R + idx];
     // stage the 128 x R block of x (or w) at block c into buffer buf, 16 bytes per cp.async
     auto issue_copy = [&](const float* src_base, int c, int buf) {
@@ -817,7 +821,7 @@ __global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat
         pi = A.im + off;
     };
     auto inv_ptr = [&](const float*& pr, const float*& pi) {
-        const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * 32 + lane) * TS_NB + s * TS_KC;
+        const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * TS_RW + lane) * TS_NB + s * TS_KC;
         pr = invr + off;
         pi = invi + off;
     };
@@ -882,14 +886,14 @@ __global__ void __launch_bounds__(32 * TS_KS, 2) k_trsv_tk(int nblk, int R, CMat
     auto reduce_out = [&](bool add_y, float* dst) {
 #pragma unroll
         for (int j = 0; j < RC; ++j)
-            *reinterpret_cast<float2*>(red + ((s * 32 + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+            *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
         __syncthreads();
-        for (int idx = tid; idx < 32 * R; idx += blockDim.x) {
+        for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
             const int i = idx / R, j = idx % R;
             float2 o = add_y ? reinterpret_cast<const float2*>(ybase)[idx] : make_float2(0.f, 0.f);
 #pragma unroll
-            for (int w = 0; w < TS_KS; ++w) {
-                const float2 v = *reinterpret_cast<const float2*>(red + ((w * 32 + i) * RC + j) * 2);
+            for (int w = 0; w < TS_SL; ++w) {
+                const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
                 o.x += v.x;
                 o.y += v.y;
             }
@@ -924,10 +928,10 @@ template <int RC>
 static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which,
                           int R, float* Y, float* X, int* xflag, int* wflag, int* ticket, int epoch, int* flags) {
     const int nblk = n / TS_NB;
-    const size_t smem = sizeof(float) * (2 * (size_t)ts_zstride(R, RC) + TS_KS * 32 * RC * 2 + 32 * 2 * R);
+    const size_t smem = sizeof(float) * (2 * (size_t)ts_zstride(R, RC) + TS_SL * TS_RW * RC * 2 + TS_RW * 2 * R);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_trsv_tk<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, 32 * TS_KS, smem, st>>>(nblk, R, A, invr, invi, which, Y, X, xflag,
+    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, invr, invi, which, Y, X, xflag,
                                                                       wflag, ticket, epoch, flags));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
@@ -957,12 +961,12 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
-    // ready holds n/16 flags (x flags of the n/32 sub-blocks, then their w flags) and a
-    // ticket counter, zero between launches.
+    // ready holds 2 n / TS_RW flags (x flags of the n / TS_RW sub-blocks, then their w
+    // flags) and a ticket counter, zero between launches.
     float* tmp = X + (size_t)2 * n * R;
     int* xflag = ready;
-    int* wflag = ready + n / 32;
-    int* ticket = ready + n / 16;
+    int* wflag = ready + n / TS_RW;
+    int* ticket = ready + 2 * n / TS_RW;
     if (trsv_tk(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, ticket, epoch, flags)) return 1;
     return trsv_tk(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, ticket, epoch + 1, flags);
 }
