@@ -229,11 +229,16 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     }
     __syncthreads();
     if (!s_admit) return;
+    // work item = one receiver row x one of WAVE_SPLIT source ranges, so the last items
+    // are short and the tail of the launch leaves few SMs idle
+    const int chunk = ((a.N + WAVE_SPLIT - 1) / WAVE_SPLIT + 31) & ~31;
     for (;;) {
-        int r = 0;
-        if (lane == 0) r = atomicAdd(a.row_ctr, 1);
-        r = __shfl_sync(0xffffffffu, r, 0);
-        if (r >= a.N) break;
+        int item = 0;
+        if (lane == 0) item = atomicAdd(a.row_ctr, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= a.N * WAVE_SPLIT) break;
+        const int r = item / WAVE_SPLIT, s_begin = (item % WAVE_SPLIT) * chunk;
+        const int s_end = min(a.N, s_begin + chunk);
         const int N = a.N, R = a.R;
         const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
         const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
@@ -247,7 +252,7 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         const size_t row = (size_t)r * a.ld;
         const bool live = a.live != 0;
         const size_t fs = (size_t)4 * N;
-        for (int s = lane; s < N; s += 32) {
+        for (int s = s_begin + lane; s < s_end; s += 32) {
             float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
             const int nq = live ? a.nq[s] : 0;
     #pragma unroll
@@ -329,8 +334,8 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
                     vi += __shfl_xor_sync(0xffffffffu, vi, off);
                 }
                 if (lane == 0) {
-                    a.Y[2 * ((size_t)r * R + j)] += (double)vr;
-                    a.Y[2 * ((size_t)r * R + j) + 1] += (double)vi;
+                    atomicAdd(a.Y + 2 * ((size_t)r * R + j), (double)vr);
+                    atomicAdd(a.Y + 2 * ((size_t)r * R + j) + 1, (double)vi);
                 }
             }
         }
