@@ -109,7 +109,8 @@ struct bem_ctx {
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 8, asm_per_sm = 3;
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
-    std::vector<double> lu_tl_ms;               // last LU's timeline, ms from its first event
+    std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
+    bool lu_tl_armed = false;                   // the next LU records the timeline
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
     // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
@@ -320,7 +321,9 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         int rc_lu;
         if (tc) {
             const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms, ctx->lu_rest_tiles,
-                                    ctx->lu_tl.size() >= (size_t)6 * (Np / 128) ? ctx->lu_tl.data() : nullptr};
+                                    ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)
+                                        ? ctx->lu_tl.data()
+                                        : nullptr};
             rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                  ctx->d_wut32, ctx->d_flags);
         } else {
@@ -389,7 +392,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
     int hflags = 0;
     CK(cudaMemcpyAsync(&hflags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (mixed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)) {
+    if (mixed && ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)) {
+        ctx->lu_tl_armed = false;
         const int steps = Np / 128 - 1;
         ctx->lu_tl_ms.assign((size_t)6 * std::max(steps, 0), 0.0);
         for (int k = 0; k < steps; ++k)
@@ -864,6 +868,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     }
     cudaStream_t sa = pipe ? ctx->sa : st;
     CK(cudaEventRecord(ctx->ev_call, st));
+    ctx->lu_tl_armed = true;  // the timeline (if enabled) follows this call's first LU
     if (pipe) CK(cudaStreamWaitEvent(sa, ctx->ev_call, 0));  // assembly starts after the work queued so far
     auto slot = [&](int f) -> FreqState& { return ctx->fs[pipe ? (f & 1) : 0]; };
     auto enqueue_assembly = [&](int f) -> bem_status {

@@ -271,8 +271,9 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
  * turns recording on (events at every block step of later mixed factorizations),
- * 0 turns it off, -1 leaves it unchanged.  out receives, for the last recorded
- * factorization, up to max_steps rows of 6 times in ms from its first event:
+ * 0 turns it off, -1 leaves it unchanged.  out receives, for the first
+ * factorization of the last bem_solve call (in a pipelined call it runs beside the
+ * next frequency's assembly), up to max_steps rows of 6 times in ms from its first event:
  * cross update of step k started / done (main stream), inverse of block k+1 done,
  * W21 done, panel k+1 ready (panel stream), rest of step k's update done.
  * *steps = rows available. */
