@@ -103,11 +103,11 @@ struct bem_ctx {
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
     cudaEvent_t ev_lu_done = nullptr;           // LU of the current frequency done (pipelined solves)
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
-    int lu_reserve_sms = 0;                     // 0: short-lived trailing-update CTAs (see bem_set_tuning)
+    int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
-    int asm_overlap = 1, asm_reserve = 8, asm_per_sm = 3;
+    int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline

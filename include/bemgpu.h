@@ -257,15 +257,15 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
 
 /* Tuning knobs (defaults are the measured best on GB300):
  *   "lu_reserve_sms"  > 0: SMs the lookahead LU keeps free of its persistent trailing
- *                     update for the panel chain (inverse, W21, transpose); 0: the
- *                     trailing update runs as short-lived CTAs of ~4 tiles that hand
- *                     SMs to the higher-priority panel stream as they retire (default).
- *   "lu_rest_tiles"   tiles per such CTA (default 4).
+ *                     update for the panel chain (inverse, W21, transpose; default 32);
+ *                     0: the trailing update runs as short-lived CTAs that hand SMs to
+ *                     the higher-priority panel stream as they retire.
+ *   "lu_rest_tiles"   tiles per such short-lived CTA (default 4).
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
- *                     LU when it overlaps it (default 8).
+ *                     LU when it overlaps it (default 24).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
