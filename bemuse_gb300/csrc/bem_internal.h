@@ -37,6 +37,7 @@ __device__ __forceinline__ float tf32_rn(float x) {
 
 constexpr int WAVE_SM_SLOTS = 256;  // per-SM admission counters of the persistent wave kernel (>= %nsmid)
 constexpr int WAVE_SPLIT = 4;       // source ranges per receiver row (work items of the persistent wave kernel)
+constexpr int WAVE_ALWAYS = 16;     // CTAs of each wave launch admitted wherever they land
 
 struct WaveArgs {
     int N, ld, R, mode;   // mode 0: assemble D and S*B; 1: raw ws/wd (N x N interleaved)
@@ -60,7 +61,8 @@ struct WaveArgs {
     const float* RSRhi; const float* RSRlo;  // RSR as float pairs [N][ld]
     // persistent mixed kernel: work items (row x source range) are drawn from *row_ctr (zero at
     // launch); a CTA stays only if its SM id is >= reserve and fewer than per_sm of its CTAs are
-    // on that SM (sm_ctr[smid], zero at launch), so a concurrent LU keeps SMs for its own CTAs
+    // on that SM (sm_ctr[smid], zero at launch; sm_ctr[WAVE_SM_SLOTS] counts arrivals), so a
+    // concurrent LU keeps SMs for its own CTAs
     int* row_ctr;
     int* sm_ctr;
     int reserve, per_sm;

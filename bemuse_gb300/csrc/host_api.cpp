@@ -670,7 +670,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_area, N);
     DA(ctx->d_Nk, 6 * (size_t)N);
     DA(ctx->d_betas, std::max(NB, 1));
-    DA(ctx->d_wctr, 1 + bem::WAVE_SM_SLOTS);
+    DA(ctx->d_wctr, 2 + bem::WAVE_SM_SLOTS);  // item counter, per-SM counters, arrivals
     DA(ctx->d_RS, (size_t)N * Np);
     DA(ctx->d_RD, (size_t)N * Np);
     DA(ctx->d_RSR, (size_t)N * Np);

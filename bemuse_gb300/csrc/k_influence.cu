@@ -218,12 +218,15 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     if (smid >= (uint32_t)WAVE_SM_SLOTS) smid = WAVE_SM_SLOTS - 1;  // only the admission policy shares a slot
     if (threadIdx.x == 0) {
-        int ok = (int)smid >= a.reserve;
-        if (ok) {
-            if (atomicAdd(a.sm_ctr + smid, 1) >= a.per_sm) {
-                atomicSub(a.sm_ctr + smid, 1);
-                ok = 0;
-            }
+        // The first WAVE_ALWAYS CTAs to start always work, wherever they land, so that a
+        // launch whose CTAs all find room only on reserved SMs (the GPU full of other work)
+        // still assembles the frequency; later CTAs stay only on unreserved SMs with room.
+        const int arrival = atomicAdd(a.sm_ctr + WAVE_SM_SLOTS, 1);
+        const int here = atomicAdd(a.sm_ctr + smid, 1);
+        int ok = 1;
+        if (arrival >= WAVE_ALWAYS && ((int)smid < a.reserve || here >= a.per_sm)) {
+            atomicSub(a.sm_ctr + smid, 1);
+            ok = 0;
         }
         s_admit = ok;
     }
@@ -813,7 +816,7 @@ void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
         int dev = 0, nsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (1 + WAVE_SM_SLOTS), st);
+        cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (2 + WAVE_SM_SLOTS), st);
         BEM_LAUNCH(k_wave_mixed<<<std::min(3 * nsm, (b.N + 7) / 8), 256, 0, st>>>(b));
     } else {
         BEM_LAUNCH(k_wave<double><<<(a.N + 7) / 8, 256, 0, st>>>(a));

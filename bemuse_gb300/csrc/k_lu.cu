@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <mutex>
 
 namespace bem {
 
@@ -967,8 +968,22 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
     int* xflag = ready;
     int* wflag = ready + n / TS_RW;
     int* ticket = ready + 2 * n / TS_RW;
+    // Two of these solves running at once (contexts of bem_batch_solve on one GPU) could
+    // fill every SM with CTAs that wait on sub-blocks of their own launch which then find no
+    // SM.  The solves of all contexts on a device are therefore chained through one event:
+    // a launch starts after the previous one has finished.  Other kernels, which never wait
+    // on other CTAs, still run beside them.
+    static std::mutex mtx;
+    static cudaEvent_t chain[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mtx);
+    cudaEvent_t& ev = chain[dev & 63];
+    if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return 1;
+    if (cudaStreamWaitEvent(st, ev, 0) != cudaSuccess) return 1;
     if (trsv_tk(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, ticket, epoch, flags)) return 1;
-    return trsv_tk(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, ticket, epoch + 1, flags);
+    if (trsv_tk(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, ticket, epoch + 1, flags)) return 1;
+    return cudaEventRecord(ev, st) == cudaSuccess ? 0 : 1;
 }
 
 // ---------------------------------------------------------------------------

@@ -231,3 +231,20 @@ def test_gdf_import_solves_like_generated_mesh(bg, tmp_path):
         out.append(s.solve_omegas(om))
     for k in ("A", "B", "F"):
         assert normwise(out[1][k], out[0][k]) < 1e-12, k
+
+
+@pytest.mark.gpu
+def test_batch_solve_many_concurrent_contexts(bg):
+    """Eight contexts at once on one GPU (the bench's batched form in small): every body
+    gets its single-context result.  Catches work lost to SM admission or cross-context
+    waits when the GPU is full of other contexts' kernels."""
+    meshes = [bg.Half_Cylinder(4.0 + 0.5 * i, 10.0 + i, 32, 4, 12 + i, 0, False) for i in range(8)]
+    om = np.array([0.3, 0.7, 1.1, 1.5, 1.9, 2.3])
+    outs, sec = bg.batch_solve(meshes, om, [0.0], bg.MIXED, n_workers=8)
+    for m, o in zip(meshes, outs):
+        s = bg.Hydrodynamic_Radiation_Solver(precision=bg.MIXED)
+        s.Set_Parameters([bg.Parameter("WaveAngle", 0.0)])
+        s.Setup(m)
+        ref = s.solve_omegas(om)
+        for k in ("A", "B", "F"):
+            assert normwise(o[k], ref[k]) < 1e-9, k
