@@ -9,7 +9,8 @@ namespace bem {
 
 // Count of kernel launches issued by this library (all contexts).
 extern std::atomic<unsigned long long> g_launches;  // kernel launches (all threads)
-#define BEM_LAUNCH(...) (++::bem::g_launches, __VA_ARGS__)
+extern thread_local unsigned long long t_launches;  // kernel launches of this host thread
+#define BEM_LAUNCH(...) (++::bem::g_launches, ++::bem::t_launches, __VA_ARGS__)
 
 constexpr int RK_STRIDE = 32;   // doubles per Rankine panel record
 constexpr int MAX_RHS = 16;     // 6 radiation + up to 10 headings

@@ -28,6 +28,7 @@
 using bem::CMat;
 
 std::atomic<unsigned long long> bem::g_launches{0};
+thread_local unsigned long long bem::t_launches = 0;
 using cplx = std::complex<double>;
 
 // Per-frequency state of a mixed-precision solve.  Two of them let the
@@ -51,6 +52,14 @@ struct FreqState {
     cudaEvent_t ev_free = nullptr;            // solves of this slot done: buffers reusable
     cudaEvent_t ev_t[4] = {};                 // timing: assembly start, static RHS done, wave kernel start/end
     cudaEvent_t ev_t5 = nullptr;              // timing: assembly end
+};
+
+// One captured tensor-core LU (per frequency slot) and what it was captured for.
+struct LuGraph {
+    cudaGraphExec_t exec = nullptr;
+    const float* A = nullptr;
+    int Np = 0, reserve = -1, rest = -1;
+    long long launches = 0;
 };
 
 struct bem_ctx {
@@ -107,10 +116,11 @@ struct bem_ctx {
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
-    int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
+    int asm_overlap = 1, asm_reserve = 48, asm_per_sm = 3;
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
+    LuGraph lu_graph[2];                        // captured LU per frequency slot
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
     // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
@@ -189,6 +199,10 @@ void free_all(bem_ctx* ctx) {
     ctx->d_gq32 = nullptr;
     ctx->d_wpts = ctx->d_ext = nullptr;
     ctx->wpts_cap = ctx->ext_cap = 0;
+    for (LuGraph& g : ctx->lu_graph) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = LuGraph();
+    }
     ctx->d_wctr = nullptr;
     ctx->wpts_dirty = true;
     ctx->ready = false;
@@ -324,8 +338,43 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)
                                         ? ctx->lu_tl.data()
                                         : nullptr};
-            rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
-                                                 ctx->d_wut32, ctx->d_flags);
+            if (ls.timeline) {
+                rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
+                                                     ctx->d_wut32, ctx->d_flags);
+            } else {
+                // The ~320 launches and 128 cross-stream event edges of one factorization are
+                // captured once per slot into a CUDA graph and replayed, which removes the host
+                // enqueue work (tensor-map encodes) and most launch gaps of the panel chain.
+                LuGraph& g = ctx->lu_graph[&F == &ctx->fs[1] ? 1 : 0];
+                if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
+                    g.rest != ctx->lu_rest_tiles) {
+                    if (g.exec) cudaGraphExecDestroy(g.exec);
+                    g.exec = nullptr;
+                    const unsigned long long l0 = bem::t_launches;
+                    cudaGraph_t graph = nullptr;
+                    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+                    rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
+                                                         ctx->d_wut32, ctx->d_flags);
+                    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+                    if (rc_lu == 0 && ec == cudaSuccess) {
+                        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+                        cudaGraphDestroy(graph);
+                        CK(ei);
+                    } else {
+                        if (graph) cudaGraphDestroy(graph);
+                        cudaGetLastError();
+                        if (rc_lu == 0) rc_lu = 1;
+                    }
+                    g.launches = (long long)(bem::t_launches - l0);
+                    bem::g_launches -= (unsigned long long)g.launches;  // counted when the graph runs
+                    g.A = A.re; g.Np = Np; g.reserve = ctx->lu_reserve_sms; g.rest = ctx->lu_rest_tiles;
+                }
+                if (g.exec) {
+                    CK(cudaGraphLaunch(g.exec, st));
+                    bem::g_launches += (unsigned long long)g.launches;
+                    rc_lu = 0;
+                }
+            }
         } else {
             rc_lu = bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32,
                                        ctx->d_wut32, ctx->d_flags, false);
@@ -1319,7 +1368,7 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "asm_reserve_sms") {
-        if (!(value >= 0 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "asm_reserve_sms must be in [0, 64]");
+        if (!(value >= 0 && value <= 144)) return fail(ctx, BEM_ERR_ARG, "asm_reserve_sms must be in [0, 144]");
         ctx->asm_reserve = (int)value;
         return BEM_OK;
     }

@@ -699,6 +699,7 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
     void* args[] = {(void*)&nblk, (void*)&R, (void*)&A, (void*)&invr, (void*)&invi, (void*)&which, (void*)&Y,
                     (void*)&X, (void*)&ready, (void*)&epoch, (void*)&flags};
     ++g_launches;
+    ++t_launches;
     return cudaLaunchCooperativeKernel((void*)k_trsv_coop<T, NB, TPR>, dim3(grid), dim3(NB * TPR), args, smem, st) ==
                    cudaSuccess
                ? 0
