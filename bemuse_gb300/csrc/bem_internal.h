@@ -134,6 +134,7 @@ struct LuStreams {
     int reserve_sms;
     int rest_tiles;         // tiles per trailing-update CTA when reserve_sms == 0
     cudaEvent_t* timeline;  // optional, 6 timing events per block step (see lu_factor_f32_lookahead)
+    int cluster_inverse;    // 1: block inverses on a cluster of two CTAs (k_inv128c), 0: one CTA
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus a [2][128][128]
 // transposed diagonal-block inverse (4 n 128 + 32768 floats).

@@ -58,7 +58,7 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1;
     long long launches = 0;
 };
 
@@ -114,6 +114,7 @@ struct bem_ctx {
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
+    int lu_cluster_inverse = 1;                 // block inverses on two-CTA clusters
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 48, asm_per_sm = 3;
@@ -337,7 +338,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms, ctx->lu_rest_tiles,
                                     ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)
                                         ? ctx->lu_tl.data()
-                                        : nullptr};
+                                        : nullptr,
+                                    ctx->lu_cluster_inverse};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);
@@ -347,7 +349,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 // enqueue work (tensor-map encodes) and most launch gaps of the panel chain.
                 LuGraph& g = ctx->lu_graph[&F == &ctx->fs[1] ? 1 : 0];
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
-                    g.rest != ctx->lu_rest_tiles) {
+                    g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -368,6 +370,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.launches = (long long)(bem::t_launches - l0);
                     bem::g_launches -= (unsigned long long)g.launches;  // counted when the graph runs
                     g.A = A.re; g.Np = Np; g.reserve = ctx->lu_reserve_sms; g.rest = ctx->lu_rest_tiles;
+                    g.cluster = ctx->lu_cluster_inverse;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -1360,6 +1363,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_rest_tiles") {
         if (!(value >= 1 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "lu_rest_tiles must be in [1, 64]");
         ctx->lu_rest_tiles = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_cluster_inverse") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_cluster_inverse must be 0 or 1");
+        ctx->lu_cluster_inverse = (int)value;
         return BEM_OK;
     }
     if (k == "asm_overlap") {

@@ -260,6 +260,193 @@ __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A,
 
 
 // ---------------------------------------------------------------------------
+// The same inverse on a cluster of two CTAs, split by rows: CTA q owns rows
+// 64 q .. 64 q + 63 of the block (thread (rg, cg): rows 4 rg .. 4 rg + 3, columns
+// 8 cg .. 8 cg + 7), so each pivot costs each SM half the FMAs.  The pivot rows of
+// 64 consecutive pivots belong to one CTA, which normalises them (the p + 1
+// substitution above) and writes each one both into its own shared memory and,
+// by st.async, into the peer's, completing a per-pivot mbarrier there.  Every
+// pivot row has its own 1 KB slot, so the owner never waits for the peer; the
+// peer follows one remote-store latency behind and the roles swap at pivot 64.
+// The column of each pivot is local to each CTA.  Waits on the peer give up at a
+// 2 s deadline (FLAG_TIMEOUT); both CTAs always reach the final cluster barrier.
+constexpr int IC_THREADS = 256;
+constexpr int IC_SMEM = 128 * 64 * 16       // pivot rows [128][chunk q][column group] float4
+                        + 2 * 32 * 16       // pivot-column values [buffer][q][row group] float4
+                        + 128 * 8;          // one mbarrier per pivot row
+
+__device__ __forceinline__ uint32_t ic_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t ic_peer_addr(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void ic_cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Bounded wait for a pivot row written by the peer (acquire at cluster scope).
+__device__ __forceinline__ bool ic_wait(uint32_t bar, unsigned long long deadline) {
+    for (int i = 0;; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+        if (done) return true;
+        if ((i & 15) == 15) {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t > deadline) return false;
+        }
+    }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
+    k_inv128c(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    extern __shared__ __align__(16) float4 ic_smem[];
+    float4* nrow = ic_smem;                                   // [128][4 * 16]
+    float4* ccol = nrow + 128 * 64;                           // [2][2 * 16]
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(ccol + 2 * 32);  // [128]
+    const uint32_t rank = ic_rank(), peer = rank ^ 1u;
+    const int t = threadIdx.x, cg = t & 15, rg = t >> 4;
+    const uint32_t nrow_s = (uint32_t)__cvta_generic_to_shared(nrow);
+    const uint32_t bars_s = (uint32_t)__cvta_generic_to_shared(bars);
+    const uint32_t nrow_peer = ic_peer_addr(nrow_s, peer), bars_peer = ic_peer_addr(bars_s, peer);
+    float2 v[4][8];
+    const int row_base = 64 * (int)rank + 4 * rg;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const size_t g = (size_t)(k0 + row_base + m) * A.ld + k0 + 8 * cg;
+        const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
+        const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
+        const float4 i0 = *reinterpret_cast<const float4*>(A.im + g);
+        const float4 i1 = *reinterpret_cast<const float4*>(A.im + g + 4);
+        v[m][0] = make_float2(r0.x, i0.x); v[m][1] = make_float2(r0.y, i0.y);
+        v[m][2] = make_float2(r0.z, i0.z); v[m][3] = make_float2(r0.w, i0.w);
+        v[m][4] = make_float2(r1.x, i1.x); v[m][5] = make_float2(r1.y, i1.y);
+        v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
+    }
+    if (t < 128) {
+        // rows this CTA receives: one arrival now, completed by 1 KB of the peer's stores
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars_s + 8 * t) : "memory");
+        if ((t >> 6) != (int)rank)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], 1024;" ::"r"(bars_s + 8 * t)
+                         : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ic_cluster_sync();
+    unsigned long long deadline;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(deadline));
+    deadline += 2000000000ull;
+    int lf = 0;
+    bool dead = false;
+    // Publish pivot kp: m1 = its row inside a 4-row tile, c1 = its column inside an 8-column tile.
+    auto publish = [&](int kp, int m1, int c1, int b) {
+        const int kl = kp & 63, grow = kl >> 2, gcol = kp >> 3;
+        const bool mine = (kp >> 6) == (int)rank;
+        if (mine && (rg >> 1) == (grow >> 1)) {  // the warp holding row kp
+            const float2 pv = v[m1][c1];
+            const int src = ((grow & 1) << 4) | gcol;
+            const float px = __shfl_sync(0xffffffffu, pv.x, src), py = __shfl_sync(0xffffffffu, pv.y, src);
+            if (rg == grow) {
+                const float den = px * px + py * py;
+                if (cg == gcol && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
+                const float rc = __frcp_rn(den), qr = px * rc, qi = -py * rc;
+                float o[16];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    float rx = v[m1][c].x, ry = v[m1][c].y;
+                    if (c == c1 && cg == gcol) rx = px + 1.f;
+                    o[2 * c] = rx * qr - ry * qi;
+                    o[2 * c + 1] = rx * qi + ry * qr;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 w = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+                    nrow[kp * 64 + q * 16 + cg] = w;
+                    const uint32_t dst = nrow_peer + (uint32_t)((kp * 64 + q * 16 + cg) * 16);
+                    asm volatile(
+                        "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];"
+                        ::"r"(dst), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w), "r"(bars_peer + 8 * kp)
+                        : "memory");
+                }
+            }
+        }
+        if (cg == gcol) {
+            float o[8];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                o[2 * m] = v[m][c1].x - ((mine && m == m1 && rg == grow) ? 1.f : 0.f);
+                o[2 * m + 1] = v[m][c1].y;
+            }
+            ccol[b * 32 + rg] = make_float4(o[0], o[1], o[2], o[3]);
+            ccol[b * 32 + 16 + rg] = make_float4(o[4], o[5], o[6], o[7]);
+        }
+    };
+    publish(0, 0, 0, 0);
+    __syncthreads();
+#pragma unroll 1
+    for (int kq = 0; kq < 16; ++kq) {
+#pragma unroll
+        for (int kr = 0; kr < 8; ++kr) {
+            const int k = 8 * kq + kr, b = kr & 1;
+            if ((k >> 6) != (int)rank && !dead && !ic_wait(bars_s + 8 * k, deadline)) dead = true;
+            float2 n[8], cm[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 x = nrow[k * 64 + q * 16 + cg];
+                n[2 * q] = make_float2(x.x, x.y);
+                n[2 * q + 1] = make_float2(x.z, x.w);
+            }
+            {
+                const float4 y0 = ccol[b * 32 + rg], y1 = ccol[b * 32 + 16 + rg];
+                cm[0] = make_float2(y0.x, y0.y); cm[1] = make_float2(y0.z, y0.w);
+                cm[2] = make_float2(y1.x, y1.y); cm[3] = make_float2(y1.z, y1.w);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    v[m][c].x = fmaf(-cm[m].x, n[c].x, fmaf(cm[m].y, n[c].y, v[m][c].x));
+                    v[m][c].y = fmaf(-cm[m].x, n[c].y, fmaf(-cm[m].y, n[c].x, v[m][c].y));
+                }
+            if (k < 127) publish(k + 1, (kr + 1) & 3, (kr + 1) & 7, b ^ 1);
+            __syncthreads();
+        }
+    }
+    if (dead) lf |= FLAG_TIMEOUT;
+    float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
+    float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const size_t g = (size_t)(row_base + m) * 128 + 8 * cg;
+        *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
+        *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
+        *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
+        *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
+    }
+    if (dT) {  // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const size_t g = (size_t)(8 * cg + c) * 128 + row_base;
+            *reinterpret_cast<float4*>(dT + g) =
+                make_float4(tf32_rn(v[0][c].x), tf32_rn(v[1][c].x), tf32_rn(v[2][c].x), tf32_rn(v[3][c].x));
+            *reinterpret_cast<float4*>(dT + 16384 + g) =
+                make_float4(tf32_rn(v[0][c].y), tf32_rn(v[1][c].y), tf32_rn(v[2][c].y), tf32_rn(v[3][c].y));
+        }
+    }
+    if (lf) atomicOr(flags, lf);
+    ic_cluster_sync();  // neither CTA leaves while the other may still address its shared memory
+}
+
+// ---------------------------------------------------------------------------
 // C = beta C + sgn * A B, planar complex, row-major.  M, N multiples of 64,
 // K multiple of 16.  256 threads, 64x64 tile, 4x4 outputs per thread.
 template <typename T>
@@ -423,6 +610,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
     auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };
     cudaStream_t sp = ls.panel;
+    if (ls.cluster_inverse) cudaFuncSetAttribute(k_inv128c, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
     // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl and A21), U12^T
     // (into wut); ev_panel marks the operands of the step-k updates ready.
     // timeline (optional): per step k, [0] cross update start, [1] cross done (main stream),
@@ -433,7 +621,10 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     float* dT = wut2 + (size_t)4 * n * NB;  // D_kk^-1 transposed, [2][128][128]
     auto panel = [&](int k) {
         const int k0 = k * NB, rem = n - k0 - NB;
-        BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dT, flags));
+        if (ls.cluster_inverse)
+            BEM_LAUNCH(k_inv128c<<<2, IC_THREADS, IC_SMEM, sp>>>(k0, A, invr, invi, dT, flags));
+        else
+            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dT, flags));
         mark(k - 1, 2, sp);
         if (rem > 0) {
             // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)

@@ -261,6 +261,8 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     0: the trailing update runs as short-lived CTAs that hand SMs to
  *                     the higher-priority panel stream as they retire.
  *   "lu_rest_tiles"   tiles per such short-lived CTA (default 4).
+ *   "lu_cluster_inverse" 1: diagonal-block inverses on a cluster of two CTAs (default),
+ *                     0: on one CTA.
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
