@@ -117,7 +117,7 @@ struct bem_ctx {
     int lu_cluster_inverse = 1;                 // block inverses on two-CTA clusters
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
-    int asm_overlap = 1, asm_reserve = 48, asm_per_sm = 3;
+    int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline

@@ -267,7 +267,7 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
- *                     LU when it overlaps it (default 48).
+ *                     LU when it overlaps it (default 24).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
