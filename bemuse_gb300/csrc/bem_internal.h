@@ -119,25 +119,28 @@ struct LUWork;  // opaque workspace (host_api.cpp)
 
 // Blocked LU without row exchanges of the n x n (n % nb == 0) planar matrix;
 // diagonal-block inverses go to inv (re/im, [n/nb][2][nb][nb]: L^-1 then U^-1).
-// tc = true uses the tcgen05 TF32 trailing update (float only).
-// Returns 0 on success, nonzero if the tensor-core path could not be set up.
 int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
                   int* flags);
-int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu,
-                  float* wut, int* flags, bool tc);
 // Lookahead schedule for the tensor-core LU: the panel of step k+1 (diagonal-block
 // inverse, W21, U12^T) runs on `panel` (a higher-priority stream) while the main
 // stream applies the rest of step k's trailing update on all but `reserve_sms` SMs.
 struct LuStreams {
     cudaStream_t panel;
-    cudaEvent_t ev_panel, ev_cross;
+    cudaEvent_t ev_panel, ev_cross, ev_rest;
+    cudaStream_t ucol;      // U-column transforms (U D^-1) behind the panel chain
+    cudaEvent_t ev_ucol;
     int reserve_sms;
     int rest_tiles;         // tiles per trailing-update CTA when reserve_sms == 0
     cudaEvent_t* timeline;  // optional, 6 timing events per block step (see lu_factor_f32_lookahead)
     int cluster_inverse;    // 1: block inverses on a cluster of two CTAs (k_inv128c), 0: one CTA
+    int ucol_own;           // 1: U-column transforms on `ucol`, 0: on `panel` after each W21
+    int ucol_ctas;          // CTAs per U-column transform (0: one per tile)
 };
-// wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus a [2][128][128]
-// transposed diagonal-block inverse (4 n 128 + 32768 floats).
+// wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
+// diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The
+// factorization leaves L as W blocks below the diagonal, the diagonal-block
+// inverses in inv, and above the diagonal U D^-1 (each column block right-multiplied
+// by the inverse of its diagonal block), the form lu_solve_f32 uses.
 int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                             float* wl2, float* wut2, int* flags);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place,

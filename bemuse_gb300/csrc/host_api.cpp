@@ -58,7 +58,7 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1, cluster = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1;
     long long launches = 0;
 };
 
@@ -106,7 +106,8 @@ struct bem_ctx {
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
     cudaStream_t sp = nullptr;                   // panel stream of the lookahead LU (higher priority)
-    cudaEvent_t ev_panel = nullptr, ev_cross = nullptr;
+    cudaEvent_t ev_panel = nullptr, ev_cross = nullptr, ev_rest = nullptr, ev_ucol = nullptr;
+    cudaStream_t su = nullptr;  // U-column transforms of the LU
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
@@ -115,6 +116,8 @@ struct bem_ctx {
     int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
     int lu_cluster_inverse = 1;                 // block inverses on two-CTA clusters
+    int lu_ucol_stream = 1;                     // U D^-1 transforms on their own stream (0: panel stream)
+    int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
@@ -287,7 +290,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_wl32, (size_t)4 * Np * nb32);  // two [2][Np][128] buffers (lookahead)
         DA(ctx->d_wu32, (size_t)2 * Np * nb32);
-        DA(ctx->d_wut32, (size_t)4 * Np * nb32 + 2 * 128 * 128);  // + transposed D^-1 block
+        DA(ctx->d_wut32, (size_t)4 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
     }
@@ -335,11 +338,13 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
         int rc_lu;
         if (tc) {
-            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->lu_reserve_sms, ctx->lu_rest_tiles,
+            const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->ev_rest, ctx->su, ctx->ev_ucol,
+                                    ctx->lu_reserve_sms,
+                                    ctx->lu_rest_tiles,
                                     ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)
                                         ? ctx->lu_tl.data()
                                         : nullptr,
-                                    ctx->lu_cluster_inverse};
+                                    ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);
@@ -349,7 +354,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 // enqueue work (tensor-map encodes) and most launch gaps of the panel chain.
                 LuGraph& g = ctx->lu_graph[&F == &ctx->fs[1] ? 1 : 0];
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
-                    g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse) {
+                    g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
+                    g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -371,6 +377,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     bem::g_launches -= (unsigned long long)g.launches;  // counted when the graph runs
                     g.A = A.re; g.Np = Np; g.reserve = ctx->lu_reserve_sms; g.rest = ctx->lu_rest_tiles;
                     g.cluster = ctx->lu_cluster_inverse;
+                    g.ucol = ctx->lu_ucol_stream;
+                    g.ucol_ctas = ctx->lu_ucol_ctas;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -379,8 +387,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 }
             }
         } else {
-            rc_lu = bem::lu_factor_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32, ctx->d_wu32,
-                                       ctx->d_wut32, ctx->d_flags, false);
+            return fail(ctx, BEM_ERR_UNSUPPORTED, "mixed precision needs the tcgen05 LU (sm_103a and a CUDA driver "
+                                                  "with cuTensorMapEncodeTiled)");
         }
         if (rc_lu != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
         CK(cudaGetLastError());
@@ -540,6 +548,9 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->sp, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_panel, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_cross, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_rest, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_ucol, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithPriority(&ctx->su, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
@@ -562,6 +573,7 @@ void bem_destroy(bem_ctx* ctx) {
     free_all(ctx);
     if (ctx->sp) cudaStreamSynchronize(ctx->sp);
     if (ctx->sa) cudaStreamSynchronize(ctx->sa);
+    if (ctx->su) cudaStreamSynchronize(ctx->su);
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5})
             if (e) cudaEventDestroy(e);
@@ -576,6 +588,9 @@ void bem_destroy(bem_ctx* ctx) {
     for (auto e : ctx->lu_tl) cudaEventDestroy(e);
     if (ctx->ev_panel) cudaEventDestroy(ctx->ev_panel);
     if (ctx->ev_cross) cudaEventDestroy(ctx->ev_cross);
+    if (ctx->ev_rest) cudaEventDestroy(ctx->ev_rest);
+    if (ctx->ev_ucol) cudaEventDestroy(ctx->ev_ucol);
+    if (ctx->su) cudaStreamDestroy(ctx->su);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1368,6 +1383,16 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_cluster_inverse") {
         if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_cluster_inverse must be 0 or 1");
         ctx->lu_cluster_inverse = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_ucol_stream") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_stream must be 0 or 1");
+        ctx->lu_ucol_stream = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_ucol_ctas") {
+        if (!(value >= 0 && value <= 1024)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_ctas must be in [0, 1024]");
+        ctx->lu_ucol_ctas = (int)value;
         return BEM_OK;
     }
     if (k == "asm_overlap") {

@@ -24,8 +24,9 @@ namespace bem {
 bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
                         int* flags);
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
-                    int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape);
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags, int lshape);
 bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags);
+bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -537,18 +538,10 @@ __global__ void k_copy_back(int rows, int cols, const T* wr, const T* wi, int wl
 // Then D = L U with L = I + (strictly lower blocks W), U = block upper with the
 // diagonal blocks D_bb, whose inverses are kept in inv[blk].
 template <typename T, int NB>
-static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, T* wu, T* wut, int* flags,
-                       bool tc) {
-    (void)wu;
+static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* wl, int* flags) {
     T* wlr = wl; T* wli = wl + (size_t)n * NB;
-    T* wtr = wut; T* wti = wut ? wut + (size_t)n * NB : nullptr;
     for (int k0 = 0; k0 < n; k0 += NB) {
-        if (NB == 128 && sizeof(T) == 4)
-            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, st>>>(k0, *reinterpret_cast<CMat<float>*>(&A),
-                                                        reinterpret_cast<float*>(invr), reinterpret_cast<float*>(invi),
-                                                        nullptr, flags));
-        else
-            BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
+        BEM_LAUNCH(k_gj_inv<T, NB><<<1, 1024, 0, st>>>(k0, A, invr, invi, flags));
         const int rem = n - k0 - NB;
         if (rem <= 0) break;
         const int blk = k0 / NB;
@@ -563,16 +556,7 @@ static int lu_factor_t(cudaStream_t st, int n, CMat<T> A, T* invr, T* invi, T* w
         BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(rem, NB, wlr, wli, NB, A, k0 + NB, k0, 0, (T*)nullptr,
                                                         (T*)nullptr, 0, flags));
         CMat<T> A22{A.re + (size_t)(k0 + NB) * A.ld + k0 + NB, A.im + (size_t)(k0 + NB) * A.ld + k0 + NB, A.ld};
-        if (tc) {
-            // the tensor-core update wants A12^T (K-major): copy A12 onto itself and transpose into wut
-            BEM_LAUNCH(k_copy_back<T><<<nblk, 256, 0, st>>>(NB, rem, A12.re, A12.im, A.ld, A, k0, k0 + NB, 0, wtr,
-                                                            wti, NB, flags));
-            if (!tc_trailing_update(st, n, k0, NB, *reinterpret_cast<CMat<float>*>(&A),
-                                    reinterpret_cast<const float*>(wl), reinterpret_cast<const float*>(wut), flags))
-                return 1;
-        } else {
-            BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, A12, A22, (T)-1, 1));
-        }
+        BEM_LAUNCH(k_cgemm<T><<<dim3(rem / 64, rem / 64), 256, 0, st>>>(rem, rem, NB, WL, A12, A22, (T)-1, 1));
     }
     return 0;
 }
@@ -618,17 +602,26 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto mark = [&](int k, int slot, cudaStream_t s) {
         if (ls.timeline && k >= 0 && k < nblk) cudaEventRecord(ls.timeline[6 * k + slot], s);
     };
-    float* dT = wut2 + (size_t)4 * n * NB;  // D_kk^-1 transposed, [2][128][128]
-    auto panel = [&](int k) {
-        const int k0 = k * NB, rem = n - k0 - NB;
+    // D_kk^-1 transposed, [nblk][2][128][128]: block k's copy feeds W21 of step k and the
+    // U-column transform, which runs on its own stream behind the panel chain
+    auto dTb = [&](int k) { return wut2 + (size_t)4 * n * NB + (size_t)k * 2 * NB * NB; };
+    // Panel k+1 on the panel stream, in two parts: the inverse of block k+1 (after its
+    // own update by step k, the single corner tile, also run on this stream), then W21
+    // and the transpose, which need the rest of block column / row k+1 (the main
+    // stream's L-shaped update of step k).
+    auto inverse = [&](int k) {
+        const int k0 = k * NB;
         if (ls.cluster_inverse)
-            BEM_LAUNCH(k_inv128c<<<2, IC_THREADS, IC_SMEM, sp>>>(k0, A, invr, invi, dT, flags));
+            BEM_LAUNCH(k_inv128c<<<2, IC_THREADS, IC_SMEM, sp>>>(k0, A, invr, invi, dTb(k), flags));
         else
-            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dT, flags));
+            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
         mark(k - 1, 2, sp);
+    };
+    auto w21 = [&](int k) {
+        const int k0 = k * NB, rem = n - k0 - NB;
         if (rem > 0) {
             // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)
-            if (!tc_w21(sp, n, k0, A, dT, wlb(k), flags)) return false;
+            if (!tc_w21(sp, n, k0, A, dTb(k), wlb(k), flags)) return false;
             float* wtr = wutb(k);
             BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
                 rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
@@ -636,41 +629,56 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         mark(k - 1, 3, sp);
         cudaEventRecord(ls.ev_panel, sp);
         mark(k - 1, 4, sp);
+        if (k > 0) {
+            // U_{0:k, k} <- U_{0:k, k} D_kk^-1 (the backward solve's operator); those rows are
+            // final and no longer read by the factorization
+            if (ls.ucol_own) cudaStreamWaitEvent(ls.ucol, ls.ev_panel, 0);
+            if (!tc_ucol(ls.ucol_own ? ls.ucol : sp, n, k0, A, dTb(k), ls.ucol_ctas, flags)) return false;
+        }
         return true;
     };
     cudaEventRecord(ls.ev_cross, st);
     cudaStreamWaitEvent(sp, ls.ev_cross, 0);
-    if (!panel(0)) return 1;
+    inverse(0);
+    if (!w21(0)) return 1;
+    cudaEventRecord(ls.ev_rest, st);
     for (int k = 0; k < nblk; ++k) {
         cudaStreamWaitEvent(st, ls.ev_panel, 0);
         const int k0 = k * NB, rem = n - k0 - NB;
         if (rem <= 0) break;
         const int mt = rem / NB;
         mark(k, 0, st);
-        // block column k+1 and block row k+1 first (one L-shaped launch): the next panel's input
-        if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, mt, 0, flags, true)) return 1;
+        // panel stream: block (k+1, k+1) needs the rest update of step k-1 and step k's
+        // operands, then its inverse
+        cudaStreamWaitEvent(sp, ls.ev_rest, 0);
+        if (!tc_update_rect(sp, n, k0, A, wlb(k), wutb(k), 0, 0, 1, 1, 0, flags, 0)) return 1;
+        inverse(k + 1);
+        // main stream: the rest of block column k+1 and block row k+1 (one L-shaped launch)
+        if (!tc_update_rect(st, n, k0, A, wlb(k), wutb(k), 0, 0, mt, mt, 0, flags, 2)) return 1;
         cudaEventRecord(ls.ev_cross, st);
         mark(k, 1, st);
         cudaStreamWaitEvent(sp, ls.ev_cross, 0);
-        if (!panel(k + 1)) return 1;
+        if (!w21(k + 1)) return 1;
         if (mt > 1 &&
-            !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags, false))
+            !tc_update_rect(st, n, k0, A, wlb(k), wutb(k), NB, NB, mt - 1, mt - 1, rest_ctas, flags, 0))
             return 1;
+        cudaEventRecord(ls.ev_rest, st);
         mark(k, 5, st);
     }
-    // the last W21 stores into A precede the solves
+    // the last W21 stores and U-column transforms precede the solves
     cudaEventRecord(ls.ev_panel, sp);
     cudaStreamWaitEvent(st, ls.ev_panel, 0);
+    if (nblk > 1 && ls.ucol_own) {
+        cudaEventRecord(ls.ev_ucol, ls.ucol);
+        cudaStreamWaitEvent(st, ls.ev_ucol, 0);
+    }
     return 0;
 }
 
 int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
                   int* flags) {
-    return lu_factor_t<double, 64>(st, n, A, invr, invi, wl, wu, nullptr, flags, false);
-}
-int lu_factor_f32(cudaStream_t st, int n, CMat<float> A, float* invr, float* invi, float* wl, float* wu, float* wut,
-                  int* flags, bool tc) {
-    return lu_factor_t<float, 128>(st, n, A, invr, invi, wl, wu, wut, flags, tc);
+    (void)wu;
+    return lu_factor_t<double, 64>(st, n, A, invr, invi, wl, flags);
 }
 
 // Self-test of the tensor-core trailing update: A22 -= L21 U12 on random data
@@ -908,17 +916,20 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 // x block of the next tile is already in flight whenever its producer has
 // published it.  The eight column slices are summed once at the end.
 //   which = 0 (forward, unit block-lower L):  x_b = y_b - sum_{c<b} L_bc x_c
-//   which = 1 (backward):  w_b = y_b - sum_{c>b} U_bc x_c  (written over y_b),
-//                          x_b = Dinv_b w_b once the four sub-blocks of w_b exist.
-// xflag[u] / wflag[u] (u = sub-block) are raised to `epoch` when x / w rows of u
-// are in memory.  Waits give up at a 2 s deadline (FLAG_TIMEOUT).
+//   which = 1 (backward, unit block-upper U D^-1, as the factorization leaves it):
+//                          z_b = y_b - sum_{c>b} (U D^-1)_bc z_c
+// Both directions are the same chain; the block-diagonal x = D^-1 z that completes
+// the backward solve is one parallel launch afterwards (k_dinv_apply), so nothing on
+// the chain waits for a whole 128-row block.  Yin and Xout may be the same array:
+// a CTA reads its own rows of Yin before it writes them, and other blocks' rows of
+// Xout only after their flags.
+// xflag[u] (u = sub-block) is raised to `epoch` when the rows of u are in memory.
+// Waits give up at a 2 s deadline (FLAG_TIMEOUT).
 // Scheduling needs no co-residency (plain launch, one CTA per sub-block): each
 // CTA draws a ticket when it starts and tickets map to sub-blocks in dependency
 // order, so a CTA waits only on sub-blocks of CTAs that started before it, or
-// on its three siblings, which start no later than any CTA of a later block.
 // The lowest unfinished ticket therefore always progresses, whatever else runs
-// on the GPU (given room for the eight siblings).  The CTA that draws the last
-// ticket resets the counter.
+// on the GPU.  The CTA that draws the last ticket resets the counter.
 // TS_SB sub-blocks of TS_RW rows per 128-row block; a CTA's 256 threads are TS_RW rows x
 // TS_SL column slices of TS_KC columns.
 constexpr int TS_NB = 128, TS_SB = 8, TS_RW = TS_NB / TS_SB, TS_THREADS = 256, TS_SL = TS_THREADS / TS_RW,
@@ -963,10 +974,8 @@ __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const 
 __host__ __device__ constexpr int ts_zstride(int R, int RC) { return ((2 * (TS_NB * R + RC)) + 3) & ~3; }
 
 template <int RC>
-__global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat<float> A,
-                                                        const float* __restrict__ invr,
-                                                        const float* __restrict__ invi, int which, float* Yin,
-                                                        float* Xout, int* xflag, int* wflag, int* ticket,
+__global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat<float> A, int which,
+                                                        float* Yin, float* Xout, int* xflag, int* ticket,
                                                         int epoch, int* gflags) {
     extern __shared__ __align__(16) float ts_smem[];
     __shared__ int s_ticket, s_go;
@@ -1013,11 +1022,6 @@ __global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat
         pr = A.re + off;
         pi = A.im + off;
     };
-    auto inv_ptr = [&](const float*& pr, const float*& pi) {
-        const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * TS_RW + lane) * TS_NB + s * TS_KC;
-        pr = invr + off;
-        pi = invi + off;
-    };
     // z (a staged block) times the register tile: acc += sgn * tile * z
     auto mac = [&](const float* z, float sg) {
 #pragma unroll
@@ -1032,22 +1036,18 @@ __global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat
             }
         }
     };
-    {
-        const float *pr, *pi;
-        if (cnt > 0) tile_ptr(0, pr, pi);
-        else inv_ptr(pr, pi);
-        if (cnt > 0 || which == 1) ts_load_row(pr, pi, cr, ci);
-    }
     if (cnt > 0) {
+        const float *pr, *pi;
+        tile_ptr(0, pr, pi);
+        ts_load_row(pr, pi, cr, ci);
         if (tid < TS_SB) ts_wait(xflag + cidx(0) * TS_SB + tid, epoch, deadline, dead, gflags);
         __syncthreads();
         issue_copy(Xout, cidx(0), 0);
     }
     for (int t = 0; t < cnt; ++t) {
-        if (t + 1 < cnt || which == 1) {
+        if (t + 1 < cnt) {
             const float *pr, *pi;
-            if (t + 1 < cnt) tile_ptr(t + 1, pr, pi);
-            else inv_ptr(pr, pi);
+            tile_ptr(t + 1, pr, pi);
             ts_load_row(pr, pi, nr, ni);
         }
         // start the next block's copy now if its producer is done
@@ -1076,70 +1076,113 @@ __global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat
         for (int kk = 0; kk < TS_KC; ++kk) { cr[kk] = nr[kk]; ci[kk] = ni[kk]; }
     }
     // sum the column slices: out = y + sum_s acc_s
-    auto reduce_out = [&](bool add_y, float* dst) {
 #pragma unroll
-        for (int j = 0; j < RC; ++j)
-            *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
-        __syncthreads();
-        for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
-            const int i = idx / R, j = idx % R;
-            float2 o = add_y ? reinterpret_cast<const float2*>(ybase)[idx] : make_float2(0.f, 0.f);
+    for (int j = 0; j < RC; ++j)
+        *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+    __syncthreads();
+    for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
+        const int i = idx / R, j = idx % R;
+        float2 o = reinterpret_cast<const float2*>(ybase)[idx];
 #pragma unroll
-            for (int w = 0; w < TS_SL; ++w) {
-                const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
-                o.x += v.x;
-                o.y += v.y;
-            }
-            reinterpret_cast<float2*>(dst)[(row0 + i) * R + j] = o;
+        for (int w = 0; w < TS_SL; ++w) {
+            const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
+            o.x += v.x;
+            o.y += v.y;
         }
-        // the CTA barrier orders every thread's stores before thread 0's fence and
-        // release store of the flag (release is cumulative), as in a grid barrier
-        __syncthreads();
-        if (tid == 0) __threadfence();
-    };
-    if (which == 0) {
-        reduce_out(true, Xout);
-        if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
-        return;
+        reinterpret_cast<float2*>(Xout)[(row0 + i) * R + j] = o;
     }
-    // backward: w rows over y, then x = Dinv_b w_b (cr/ci hold the Dinv rows)
-    reduce_out(true, Yin);
-    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(wflag + u), "r"(epoch) : "memory");
-    if (tid < TS_SB) ts_wait(wflag + b * TS_SB + tid, epoch, deadline, dead, gflags);
+    // the CTA barrier orders every thread's stores before thread 0's fence and
+    // release store of the flag (release is cumulative), as in a grid barrier
     __syncthreads();
-    issue_copy(Yin, b, 0);
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
-    mac(zb, 1.f);
-    reduce_out(false, Xout);
-    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+    if (tid == 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
+    }
 }
 
+// x_b = D_b^-1 z_b for every 128-row block b: CTA (b, 16-row group q), thread
+// (i, s) = (tid % 16, tid / 16) multiplies row q*16 + i of D_b^-1, columns s*8..,
+// against the staged block of z; the 16 column slices are summed through shared
+// memory.  Z and X must not overlap.
 template <int RC>
-static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which,
-                          int R, float* Y, float* X, int* xflag, int* wflag, int* ticket, int epoch, int* flags) {
+__global__ void __launch_bounds__(TS_THREADS) k_dinv_apply(int R, const float* __restrict__ invr,
+                                                           const float* __restrict__ invi,
+                                                           const float* __restrict__ Z, float* __restrict__ X) {
+    extern __shared__ __align__(16) float da_smem[];
+    const int zs = ts_zstride(R, RC);
+    float* zb = da_smem;       // the 128 x R complex block of z, then RC complex of zeros
+    float* red = zb + zs;      // [TS_SL][TS_RW][RC] complex interleaved
+    const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW;
+    const int b = blockIdx.x / TS_SB, q = blockIdx.x % TS_SB;
+    const size_t row0 = (size_t)b * TS_NB + q * TS_RW;
+    const float4* src = reinterpret_cast<const float4*>(Z + (size_t)b * TS_NB * R * 2);
+    for (int i = tid; i < TS_NB * R / 2; i += blockDim.x) reinterpret_cast<float4*>(zb)[i] = __ldg(src + i);
+    for (int idx = 2 * TS_NB * R + tid; idx < zs; idx += blockDim.x) zb[idx] = 0.f;
+    float cr[TS_KC], ci[TS_KC];
+    const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * TS_RW + lane) * TS_NB + s * TS_KC;
+    ts_load_row(invr + off, invi + off, cr, ci);
+    __syncthreads();
+    float ar[RC], ai[RC];
+#pragma unroll
+    for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+#pragma unroll
+    for (int kk = 0; kk < TS_KC; ++kk) {
+        const float2* zk = reinterpret_cast<const float2*>(zb) + (size_t)(s * TS_KC + kk) * R;
+#pragma unroll
+        for (int j = 0; j < RC; ++j) {  // columns j >= R read padding or the next row: never stored
+            const float2 v = zk[j];
+            ar[j] = fmaf(cr[kk], v.x, fmaf(-ci[kk], v.y, ar[j]));
+            ai[j] = fmaf(cr[kk], v.y, fmaf(ci[kk], v.x, ai[j]));
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < RC; ++j)
+        *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+    __syncthreads();
+    for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
+        const int i = idx / R, j = idx % R;
+        float2 o = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int w = 0; w < TS_SL; ++w) {
+            const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
+            o.x += v.x;
+            o.y += v.y;
+        }
+        reinterpret_cast<float2*>(X)[(row0 + i) * R + j] = o;
+    }
+}
+
+// Forward chain, backward chain (in place over the forward's output) and the
+// block-diagonal apply, for one column count RC >= R.
+template <int RC>
+static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R,
+                          float* X, float* tmp, int* xflag, int* ticket, int epoch, int* flags) {
     const int nblk = n / TS_NB;
     const size_t smem = sizeof(float) * (2 * (size_t)ts_zstride(R, RC) + TS_SL * TS_RW * RC * 2 + TS_RW * 2 * R);
+    const size_t smem_d = sizeof(float) * ((size_t)ts_zstride(R, RC) + TS_SL * TS_RW * RC * 2);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_trsv_tk<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, invr, invi, which, Y, X, xflag,
-                                                                      wflag, ticket, epoch, flags));
+    if (smem_d > 48 * 1024)
+        cudaFuncSetAttribute(k_dinv_apply<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d);
+    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, 0, X, tmp, xflag, ticket, epoch,
+                                                                      flags));
+    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, 1, tmp, tmp, xflag, ticket,
+                                                                      epoch + 1, flags));
+    BEM_LAUNCH(k_dinv_apply<RC><<<nblk * TS_SB, TS_THREADS, smem_d, st>>>(R, invr, invi, tmp, X));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
 
-static int trsv_tk(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int which, int R,
-                   float* Y, float* X, int* xflag, int* wflag, int* ticket, int epoch, int* flags) {
+static int trsv_tk(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
+                   float* tmp, int* xflag, int* ticket, int epoch, int* flags) {
     switch ((R + 1) / 2) {
-        case 1: return trsv_tk_launch<2>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 2: return trsv_tk_launch<4>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 3: return trsv_tk_launch<6>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 4: return trsv_tk_launch<8>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 5: return trsv_tk_launch<10>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 6: return trsv_tk_launch<12>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 7: return trsv_tk_launch<14>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
-        case 8: return trsv_tk_launch<16>(st, n, A, invr, invi, which, R, Y, X, xflag, wflag, ticket, epoch, flags);
+        case 1: return trsv_tk_launch<2>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 2: return trsv_tk_launch<4>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 3: return trsv_tk_launch<6>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 4: return trsv_tk_launch<8>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 5: return trsv_tk_launch<10>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 6: return trsv_tk_launch<12>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 7: return trsv_tk_launch<14>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 8: return trsv_tk_launch<16>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
         default: return 1;
     }
 }
@@ -1154,11 +1197,11 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
-    // ready holds 2 n / TS_RW flags (x flags of the n / TS_RW sub-blocks, then their w
-    // flags) and a ticket counter, zero between launches.
+    // ready holds n / TS_RW flags (one per sub-block), n / TS_RW unused words and a
+    // ticket counter, zero between launches.  A is in the factorization's form: W blocks
+    // below the diagonal, U D^-1 above it, D^-1 in invr / invi.
     float* tmp = X + (size_t)2 * n * R;
     int* xflag = ready;
-    int* wflag = ready + n / TS_RW;
     int* ticket = ready + 2 * n / TS_RW;
     // Two of these solves running at once (contexts of bem_batch_solve on one GPU) could
     // fill every SM with CTAs that wait on sub-blocks of their own launch which then find no
@@ -1173,8 +1216,7 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
     cudaEvent_t& ev = chain[dev & 63];
     if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return 1;
     if (cudaStreamWaitEvent(st, ev, 0) != cudaSuccess) return 1;
-    if (trsv_tk(st, n, A, invr, invi, 0, R, X, tmp, xflag, wflag, ticket, epoch, flags)) return 1;
-    if (trsv_tk(st, n, A, invr, invi, 1, R, tmp, X, xflag, wflag, ticket, epoch + 1, flags)) return 1;
+    if (trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags)) return 1;
     return cudaEventRecord(ev, st) == cudaSuccess ? 0 : 1;
 }
 

@@ -157,7 +157,7 @@ struct TcTiles {
 // (rows of mapLr / mapLi) and U rows at ur0 (rows of mapUr / mapUi).  mode 0:
 // the tile's -acc is reduce-added into mapCr / mapCi at rows crow0 + tm*128,
 // columns ccol0 + tn*128.  mode 1: +acc is stored there and at c2row0 + tm*128,
-// c2col0 + tn*128 of mapC2r / mapC2i.
+// c2col0 + tn*128 of mapC2r / mapC2i.  mode 2: +acc is stored there only.
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_tc_update(const __grid_constant__ CUtensorMap mapLr, const __grid_constant__ CUtensorMap mapLi,
                 const __grid_constant__ CUtensorMap mapUr, const __grid_constant__ CUtensorMap mapUi,
@@ -178,10 +178,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // rectangle: Mt x Nt tiles; L-shape: tile column 0 (Mt tiles) and tile row 0 (Nt - 1 more)
     const int Mt = a.Mt, Nt = a.Nt;
-    const int ntiles = a.lshape ? Mt + Nt - 1 : Mt * Nt;
+    // lshape 1: tile column 0 and tile row 0; lshape 2: the same without the corner tile
+    const int ntiles = a.lshape ? Mt + Nt - a.lshape : Mt * Nt;
     auto tile_of = [&](int t, int& tm, int& tn) {
-        if (a.lshape) { tm = t < Mt ? t : 0; tn = t < Mt ? 0 : t - Mt + 1; }
-        else { tm = t / Nt; tn = t % Nt; }
+        if (a.lshape) {
+            t += a.lshape - 1;
+            tm = t < Mt ? t : 0;
+            tn = t < Mt ? 0 : t - Mt + 1;
+        } else {
+            tm = t / Nt; tn = t % Nt;
+        }
     };
 
     if (threadIdx.x == 0) {
@@ -191,7 +197,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         prefetch_map(&mapLr); prefetch_map(&mapLi); prefetch_map(&mapUr); prefetch_map(&mapUi);
         prefetch_map(&mapCr); prefetch_map(&mapCi);
-        if (a.mode) { prefetch_map(&mapC2r); prefetch_map(&mapC2i); }
+        if (a.mode == 1) { prefetch_map(&mapC2r); prefetch_map(&mapC2i); }
     }
     __syncwarp();
     if (warp == 0) {
@@ -288,7 +294,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const uint32_t sa = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
                         float o0 = sgn * v[4 * j], o1 = sgn * v[4 * j + 1], o2 = sgn * v[4 * j + 2],
                               o3 = sgn * v[4 * j + 3];
-                        if (a.mode) {  // W21 is the L operand of later updates: round it once, to nearest
+                        if (a.mode == 1) {  // W21 is the L operand of later updates: round it once, to nearest
                             o0 = tf32_rn(o0); o1 = tf32_rn(o1); o2 = tf32_rn(o2); o3 = tf32_rn(o3);
                         }
                         asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(o0), "f"(o1),
@@ -301,7 +307,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const int col = a.ccol0 + tn * BN + c * 32;
                         if (a.mode) {
                             tma_store_2d(p ? &mapCi : &mapCr, col, row, slot);
-                            tma_store_2d(p ? &mapC2i : &mapC2r, a.c2col0 + tn * BN + c * 32, row2, slot);
+                            if (a.mode == 1)
+                                tma_store_2d(p ? &mapC2i : &mapC2r, a.c2col0 + tn * BN + c * 32, row2, slot);
                         } else {
                             tma_reduce_add_2d(p ? &mapCi : &mapCr, col, row, slot);
                         }
@@ -394,9 +401,10 @@ static int tc_grid(int ntiles, int max_ctas) {
 // max_ctas > 0 caps the persistent grid at that many CTAs; max_ctas < 0 launches
 // ceil(tiles / -max_ctas) CTAs of about -max_ctas tiles each, so CTAs retire
 // while the update runs and a higher-priority stream can take the freed SMs.
-// lshape: only tile column 0 (Mt tiles) and tile row 0 (Nt tiles) of the rectangle.
+// lshape 1: only tile column 0 (Mt tiles) and tile row 0 (Nt tiles) of the rectangle;
+// lshape 2: the same without the corner tile (0, 0).
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
-                    int ur0, int Mt, int Nt, int max_ctas, int* flags, bool lshape) {
+                    int ur0, int Mt, int Nt, int max_ctas, int* flags, int lshape) {
     if (Mt <= 0 || Nt <= 0) return true;
     if (n % 128 || k0 % 128 || lr0 % 128 || ur0 % 128 || A.ld % 4) return false;
     if (k0 + 128 + lr0 + 128 * Mt > n || k0 + 128 + ur0 + 128 * Nt > n) return false;
@@ -406,8 +414,9 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
         !make_map(&mUr, wut, n, 128, BN) || !make_map(&mUi, wut + plane, n, 128, BN) ||
         !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
         return false;
-    const int ntiles = lshape ? Mt + Nt - 1 : Mt * Nt;
-    const TcTiles a{lr0, ur0, Mt, Nt, lshape ? 1 : 0, k0 + 128 + lr0, k0 + 128 + ur0, 0, 0, 0};
+    const int ntiles = lshape ? Mt + Nt - lshape : Mt * Nt;
+    if (ntiles <= 0) return true;
+    const TcTiles a{lr0, ur0, Mt, Nt, lshape, k0 + 128 + lr0, k0 + 128 + ur0, 0, 0, 0};
     BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi,
                                                                                    mCr, mCi, a, flags));
     return true;
@@ -435,13 +444,31 @@ bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, floa
     return true;
 }
 
+// U_{0:c, c} <- U_{0:c, c} D_cc^-1 in place for the column block at c0 (c0 / 128 row
+// tiles above the diagonal), dT = D_cc^-1 transposed ([2][128][128]).  Each tile reads
+// its rows before it overwrites them.
+bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags) {
+    if (c0 <= 0) return true;
+    if (n % 128 || c0 % 128 || A.ld % 4) return false;
+    CUtensorMap mLr, mLi, mUr, mUi, mCr, mCi;
+    if (!make_map(&mLr, A.re + c0, n, A.ld, BM) || !make_map(&mLi, A.im + c0, n, A.ld, BM) ||
+        !make_map(&mUr, dT, 128, 128, BN) || !make_map(&mUi, dT + 128 * 128, 128, 128, BN) ||
+        !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
+        return false;
+    const int mt = c0 / 128;
+    const TcTiles a{0, 0, mt, 1, 0, 0, c0, 2, 0, 0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, max_ctas), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, a,
+                                                                        flags));
+    return true;
+}
+
 // A22 -= L21 U12 over the whole trailing matrix of step k0.
 bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, const float* wl, const float* wut,
                         int* flags) {
     const int rem = n - k0 - nb;
     if (rem <= 0) return true;
     if (nb != 128) return false;
-    return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags, false);
+    return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags, 0);
 }
 
 }  // namespace bem

@@ -263,6 +263,10 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *   "lu_rest_tiles"   tiles per such short-lived CTA (default 4).
  *   "lu_cluster_inverse" 1: diagonal-block inverses on a cluster of two CTAs (default),
  *                     0: on one CTA.
+ *   "lu_ucol_stream"  1: the U D^-1 transform of each finished column block (the
+ *                     backward solve's operator) runs on its own stream (default),
+ *                     0: on the panel stream behind each W21.
+ *   "lu_ucol_ctas"    CTAs of each such transform (0 = one per 128 x 128 tile).
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
