@@ -132,9 +132,11 @@ struct LuStreams {
     int reserve_sms;
     int rest_tiles;         // tiles per trailing-update CTA when reserve_sms == 0
     cudaEvent_t* timeline;  // optional, 6 timing events per block step (see lu_factor_f32_lookahead)
-    int cluster_inverse;    // 1: block inverses on a cluster of two CTAs (k_inv128c), 0: one CTA
+    int cluster_inverse;    // CTAs per block inverse: 2, 4 or 8 (a cluster, k_inv128c), 1: one CTA
     int ucol_own;           // 1: U-column transforms on `ucol`, 0: on `panel` after each W21
     int ucol_ctas;          // CTAs per U-column transform (0: one per tile)
+    cudaStream_t panel_tail;  // optional: W21 / transpose tiles beyond the first, off the inverse chain
+    cudaEvent_t ev_head;
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
 // diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The

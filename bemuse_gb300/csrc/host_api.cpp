@@ -58,7 +58,7 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1;
     long long launches = 0;
 };
 
@@ -108,6 +108,8 @@ struct bem_ctx {
     cudaStream_t sp = nullptr;                   // panel stream of the lookahead LU (higher priority)
     cudaEvent_t ev_panel = nullptr, ev_cross = nullptr, ev_rest = nullptr, ev_ucol = nullptr;
     cudaStream_t su = nullptr;  // U-column transforms of the LU
+    cudaStream_t sq = nullptr;  // panel tail of the LU (W21 / transpose tiles beyond the first)
+    cudaEvent_t ev_head = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
@@ -115,9 +117,10 @@ struct bem_ctx {
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
-    int lu_cluster_inverse = 1;                 // block inverses on two-CTA clusters
+    int lu_cluster_inverse = 4;                 // CTAs per block inverse (2, 4, 8: a cluster; 1: one CTA)
     int lu_ucol_stream = 1;                     // U D^-1 transforms on their own stream (0: panel stream)
     int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
+    int lu_split_panel = 1;                     // panel tiles beyond the first on their own stream
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
@@ -344,7 +347,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)
                                         ? ctx->lu_tl.data()
                                         : nullptr,
-                                    ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas};
+                                    ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
+                                    ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);
@@ -355,7 +359,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 LuGraph& g = ctx->lu_graph[&F == &ctx->fs[1] ? 1 : 0];
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
-                    g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas) {
+                    g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
+                    g.split != ctx->lu_split_panel) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -379,6 +384,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.cluster = ctx->lu_cluster_inverse;
                     g.ucol = ctx->lu_ucol_stream;
                     g.ucol_ctas = ctx->lu_ucol_ctas;
+                    g.split = ctx->lu_split_panel;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -551,6 +557,8 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaEventCreateWithFlags(&ctx->ev_rest, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_ucol, cudaEventDisableTiming));
     CK(cudaStreamCreateWithPriority(&ctx->su, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
+    CK(cudaStreamCreateWithPriority(&ctx->sq, cudaStreamNonBlocking, prio_hi));
+    CK(cudaEventCreateWithFlags(&ctx->ev_head, cudaEventDisableTiming));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
@@ -574,6 +582,7 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sp) cudaStreamSynchronize(ctx->sp);
     if (ctx->sa) cudaStreamSynchronize(ctx->sa);
     if (ctx->su) cudaStreamSynchronize(ctx->su);
+    if (ctx->sq) cudaStreamSynchronize(ctx->sq);
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5})
             if (e) cudaEventDestroy(e);
@@ -591,6 +600,8 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->ev_rest) cudaEventDestroy(ctx->ev_rest);
     if (ctx->ev_ucol) cudaEventDestroy(ctx->ev_ucol);
     if (ctx->su) cudaStreamDestroy(ctx->su);
+    if (ctx->sq) cudaStreamDestroy(ctx->sq);
+    if (ctx->ev_head) cudaEventDestroy(ctx->ev_head);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1381,7 +1392,8 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "lu_cluster_inverse") {
-        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_cluster_inverse must be 0 or 1");
+        if (!(value == 1 || value == 2 || value == 4 || value == 8))
+            return fail(ctx, BEM_ERR_ARG, "lu_cluster_inverse must be 1, 2, 4 or 8");
         ctx->lu_cluster_inverse = (int)value;
         return BEM_OK;
     }
@@ -1393,6 +1405,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_ucol_ctas") {
         if (!(value >= 0 && value <= 1024)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_ctas must be in [0, 1024]");
         ctx->lu_ucol_ctas = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_split_panel") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_split_panel must be 0 or 1");
+        ctx->lu_split_panel = (int)value;
         return BEM_OK;
     }
     if (k == "asm_overlap") {

@@ -17,7 +17,6 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
-#include <mutex>
 
 namespace bem {
 
@@ -25,7 +24,8 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
                         int* flags);
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
                     int ur0, int Mt, int Nt, int max_ctas, int* flags, int lshape);
-bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags);
+bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
+            int count);
 bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
@@ -261,19 +261,21 @@ __global__ void __launch_bounds__(IV_THREADS, 1) k_inv128(int k0, CMat<float> A,
 
 
 // ---------------------------------------------------------------------------
-// The same inverse on a cluster of two CTAs, split by rows: CTA q owns rows
-// 64 q .. 64 q + 63 of the block (thread (rg, cg): rows 4 rg .. 4 rg + 3, columns
-// 8 cg .. 8 cg + 7), so each pivot costs each SM half the FMAs.  The pivot rows of
-// 64 consecutive pivots belong to one CTA, which normalises them (the p + 1
-// substitution above) and writes each one both into its own shared memory and,
-// by st.async, into the peer's, completing a per-pivot mbarrier there.  Every
-// pivot row has its own 1 KB slot, so the owner never waits for the peer; the
-// peer follows one remote-store latency behind and the roles swap at pivot 64.
-// The column of each pivot is local to each CTA.  Waits on the peer give up at a
-// 2 s deadline (FLAG_TIMEOUT); both CTAs always reach the final cluster barrier.
+// The same inverse on a cluster of CL CTAs (CL = 2, 4 or 8), split by rows: CTA q
+// owns rows RPC q .. RPC q + RPC - 1 of the block (RPC = 128 / CL; thread (rg, cg):
+// rows RPT rg .. RPT rg + RPT - 1 with RPT = RPC / 16, columns 8 cg .. 8 cg + 7), so
+// each pivot costs each SM 1 / CL of the FMAs.  The pivot rows of RPC consecutive
+// pivots belong to one CTA, which normalises them (the p + 1 substitution above) and
+// writes each one both into its own shared memory and, by st.async, into every
+// peer's, completing a per-pivot mbarrier there.  Every pivot row has its own 1 KB
+// slot, so the owner never waits for the others; they follow one remote-store
+// latency behind and the roles pass on every RPC pivots.  The column of each pivot
+// is local to each CTA.  Waits on a peer give up at a 2 s deadline (FLAG_TIMEOUT);
+// every CTA always reaches the final cluster barrier.  Launched with the cluster
+// size as a launch attribute (inv128_cluster).
 constexpr int IC_THREADS = 256;
 constexpr int IC_SMEM = 128 * 64 * 16       // pivot rows [128][chunk q][column group] float4
-                        + 2 * 32 * 16       // pivot-column values [buffer][q][row group] float4
+                        + 2 * 32 * 16       // pivot-column values [buffer][row group][RPT <= 4] float2
                         + 128 * 8;          // one mbarrier per pivot row
 
 __device__ __forceinline__ uint32_t ic_rank() {
@@ -309,21 +311,23 @@ __device__ __forceinline__ bool ic_wait(uint32_t bar, unsigned long long deadlin
     }
 }
 
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
+template <int CL>
+__global__ void __launch_bounds__(IC_THREADS, 1)
     k_inv128c(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    constexpr int RPC = 128 / CL, RPT = RPC / 16;
+    static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 ic_smem[];
-    float4* nrow = ic_smem;                                   // [128][4 * 16]
-    float4* ccol = nrow + 128 * 64;                           // [2][2 * 16]
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(ccol + 2 * 32);  // [128]
-    const uint32_t rank = ic_rank(), peer = rank ^ 1u;
+    float4* nrow = ic_smem;                                                   // [128][4 * 16]
+    float2* ccol = reinterpret_cast<float2*>(nrow + 128 * 64);                // [2][16][RPT]
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(nrow + 128 * 64 + 2 * 32);  // [128]
+    const uint32_t rank = ic_rank();
     const int t = threadIdx.x, cg = t & 15, rg = t >> 4;
     const uint32_t nrow_s = (uint32_t)__cvta_generic_to_shared(nrow);
     const uint32_t bars_s = (uint32_t)__cvta_generic_to_shared(bars);
-    const uint32_t nrow_peer = ic_peer_addr(nrow_s, peer), bars_peer = ic_peer_addr(bars_s, peer);
-    float2 v[4][8];
-    const int row_base = 64 * (int)rank + 4 * rg;
+    float2 v[RPT][8];
+    const int row_base = RPC * (int)rank + RPT * rg;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < RPT; ++m) {
         const size_t g = (size_t)(k0 + row_base + m) * A.ld + k0 + 8 * cg;
         const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
         const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
@@ -335,9 +339,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
         v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
     }
     if (t < 128) {
-        // rows this CTA receives: one arrival now, completed by 1 KB of the peer's stores
+        // rows this CTA receives: one arrival now, completed by 1 KB of the owner's stores
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars_s + 8 * t) : "memory");
-        if ((t >> 6) != (int)rank)
+        if (t / RPC != (int)rank)
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], 1024;" ::"r"(bars_s + 8 * t)
                          : "memory");
     }
@@ -348,10 +352,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
     deadline += 2000000000ull;
     int lf = 0;
     bool dead = false;
-    // Publish pivot kp: m1 = its row inside a 4-row tile, c1 = its column inside an 8-column tile.
+    // Publish pivot kp: m1 = its row inside an RPT-row tile, c1 = its column inside an 8-column tile.
     auto publish = [&](int kp, int m1, int c1, int b) {
-        const int kl = kp & 63, grow = kl >> 2, gcol = kp >> 3;
-        const bool mine = (kp >> 6) == (int)rank;
+        const int kl = kp % RPC, grow = kl / RPT, gcol = kp >> 3;
+        const bool mine = kp / RPC == (int)rank;
         if (mine && (rg >> 1) == (grow >> 1)) {  // the warp holding row kp
             const float2 pv = v[m1][c1];
             const int src = ((grow & 1) << 4) | gcol;
@@ -371,54 +375,60 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const float4 w = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+                    const uint32_t off = (uint32_t)((kp * 64 + q * 16 + cg) * 16);
                     nrow[kp * 64 + q * 16 + cg] = w;
-                    const uint32_t dst = nrow_peer + (uint32_t)((kp * 64 + q * 16 + cg) * 16);
-                    asm volatile(
-                        "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];"
-                        ::"r"(dst), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w), "r"(bars_peer + 8 * kp)
-                        : "memory");
+#pragma unroll
+                    for (int p = 1; p < CL; ++p) {
+                        const uint32_t peer = (rank + (uint32_t)p) % CL;
+                        const uint32_t dst = ic_peer_addr(nrow_s + off, peer), bar = ic_peer_addr(bars_s + 8 * kp, peer);
+                        asm volatile(
+                            "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, "
+                            "[%5];" ::"r"(dst), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w), "r"(bar)
+                            : "memory");
+                    }
                 }
             }
         }
         if (cg == gcol) {
-            float o[8];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                o[2 * m] = v[m][c1].x - ((mine && m == m1 && rg == grow) ? 1.f : 0.f);
-                o[2 * m + 1] = v[m][c1].y;
-            }
-            ccol[b * 32 + rg] = make_float4(o[0], o[1], o[2], o[3]);
-            ccol[b * 32 + 16 + rg] = make_float4(o[4], o[5], o[6], o[7]);
+            for (int m = 0; m < RPT; ++m)
+                ccol[(b * 16 + rg) * RPT + m] =
+                    make_float2(v[m][c1].x - ((mine && m == m1 && rg == grow) ? 1.f : 0.f), v[m][c1].y);
         }
     };
+    // Thread 0 alone waits for a pivot row written by a peer; the CTA barrier that
+    // follows orders every thread's reads of it after that acquire.
+    auto await_row = [&](int kp) {
+        if (t == 0 && kp / RPC != (int)rank && !dead && !ic_wait(bars_s + 8 * kp, deadline)) dead = true;
+    };
     publish(0, 0, 0, 0);
+    await_row(0);
     __syncthreads();
 #pragma unroll 1
     for (int kq = 0; kq < 16; ++kq) {
 #pragma unroll
         for (int kr = 0; kr < 8; ++kr) {
             const int k = 8 * kq + kr, b = kr & 1;
-            if ((k >> 6) != (int)rank && !dead && !ic_wait(bars_s + 8 * k, deadline)) dead = true;
-            float2 n[8], cm[4];
+            float2 n[8], cm[RPT];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const float4 x = nrow[k * 64 + q * 16 + cg];
                 n[2 * q] = make_float2(x.x, x.y);
                 n[2 * q + 1] = make_float2(x.z, x.w);
             }
-            {
-                const float4 y0 = ccol[b * 32 + rg], y1 = ccol[b * 32 + 16 + rg];
-                cm[0] = make_float2(y0.x, y0.y); cm[1] = make_float2(y0.z, y0.w);
-                cm[2] = make_float2(y1.x, y1.y); cm[3] = make_float2(y1.z, y1.w);
-            }
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
+            for (int m = 0; m < RPT; ++m) cm[m] = ccol[(b * 16 + rg) * RPT + m];
+#pragma unroll
+            for (int m = 0; m < RPT; ++m)
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                     v[m][c].x = fmaf(-cm[m].x, n[c].x, fmaf(cm[m].y, n[c].y, v[m][c].x));
                     v[m][c].y = fmaf(-cm[m].x, n[c].y, fmaf(-cm[m].y, n[c].x, v[m][c].y));
                 }
-            if (k < 127) publish(k + 1, (kr + 1) & 3, (kr + 1) & 7, b ^ 1);
+            if (k < 127) {
+                publish(k + 1, (kr + 1) % RPT, (kr + 1) & 7, b ^ 1);
+                await_row(k + 1);
+            }
             __syncthreads();
         }
     }
@@ -426,7 +436,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
     float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
     float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < RPT; ++m) {
         const size_t g = (size_t)(row_base + m) * 128 + 8 * cg;
         *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
         *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
@@ -437,14 +447,42 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(IC_THREADS, 1)
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const size_t g = (size_t)(8 * cg + c) * 128 + row_base;
-            *reinterpret_cast<float4*>(dT + g) =
-                make_float4(tf32_rn(v[0][c].x), tf32_rn(v[1][c].x), tf32_rn(v[2][c].x), tf32_rn(v[3][c].x));
-            *reinterpret_cast<float4*>(dT + 16384 + g) =
-                make_float4(tf32_rn(v[0][c].y), tf32_rn(v[1][c].y), tf32_rn(v[2][c].y), tf32_rn(v[3][c].y));
+#pragma unroll
+            for (int m = 0; m < RPT; ++m) {
+                dT[g + m] = tf32_rn(v[m][c].x);
+                dT[16384 + g + m] = tf32_rn(v[m][c].y);
+            }
         }
     }
     if (lf) atomicOr(flags, lf);
-    ic_cluster_sync();  // neither CTA leaves while the other may still address its shared memory
+    ic_cluster_sync();  // no CTA leaves while another may still address its shared memory
+}
+
+// One cluster of cl CTAs (2, 4 or 8) inverting the diagonal block at k0.
+static void inv128_cluster(cudaStream_t st, int cl, int k0, CMat<float> A, float* invr, float* invi, float* dT,
+                           int* flags) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(IC_THREADS);
+    cfg.dynamicSmemBytes = IC_SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    switch (cl) {
+        case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128c<2>, k0, A, invr, invi, dT, flags)); break;
+        case 4: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128c<4>, k0, A, invr, invi, dT, flags)); break;
+        default: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128c<8>, k0, A, invr, invi, dT, flags)); break;
+    }
+}
+static void inv128_cluster_setup() {
+    cudaFuncSetAttribute(k_inv128c<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
+    cudaFuncSetAttribute(k_inv128c<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
+    cudaFuncSetAttribute(k_inv128c<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
 }
 
 // ---------------------------------------------------------------------------
@@ -594,7 +632,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto wlb = [&](int k) { return wl2 + (size_t)(k & 1) * 2 * n * NB; };
     auto wutb = [&](int k) { return wut2 + (size_t)(k & 1) * 2 * n * NB; };
     cudaStream_t sp = ls.panel;
-    if (ls.cluster_inverse) cudaFuncSetAttribute(k_inv128c, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
+    if (ls.cluster_inverse >= 2) inv128_cluster_setup();
     // Panel k on the panel stream: D_kk^-1, W21 = A21 D_kk^-1 (into wl and A21), U12^T
     // (into wut); ev_panel marks the operands of the step-k updates ready.
     // timeline (optional): per step k, [0] cross update start, [1] cross done (main stream),
@@ -605,35 +643,47 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     // D_kk^-1 transposed, [nblk][2][128][128]: block k's copy feeds W21 of step k and the
     // U-column transform, which runs on its own stream behind the panel chain
     auto dTb = [&](int k) { return wut2 + (size_t)4 * n * NB + (size_t)k * 2 * NB * NB; };
-    // Panel k+1 on the panel stream, in two parts: the inverse of block k+1 (after its
-    // own update by step k, the single corner tile, also run on this stream), then W21
-    // and the transpose, which need the rest of block column / row k+1 (the main
-    // stream's L-shaped update of step k).
+    // Panel k+1 on the panel stream: the inverse of block k+1 (after its own update by
+    // step k, the single corner tile, also run on this stream), then W21 and the
+    // transpose, which need the rest of block column / row k+1 (the main stream's
+    // L-shaped update of step k).  Only their first tiles (block (k+2, k+1) of W21 and
+    // block (k+1, k+2) of U) feed the next corner tile and so the next inverse; with
+    // ls.panel_tail the other tiles run on that second stream, off the inverse chain.
     auto inverse = [&](int k) {
         const int k0 = k * NB;
-        if (ls.cluster_inverse)
-            BEM_LAUNCH(k_inv128c<<<2, IC_THREADS, IC_SMEM, sp>>>(k0, A, invr, invi, dTb(k), flags));
+        if (ls.cluster_inverse >= 2)
+            inv128_cluster(sp, ls.cluster_inverse, k0, A, invr, invi, dTb(k), flags);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
         mark(k - 1, 2, sp);
     };
+    cudaStream_t sq = ls.panel_tail ? ls.panel_tail : sp;
     auto w21 = [&](int k) {
         const int k0 = k * NB, rem = n - k0 - NB;
-        if (rem > 0) {
-            // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)
-            if (!tc_w21(sp, n, k0, A, dTb(k), wlb(k), flags)) return false;
-            float* wtr = wutb(k);
-            BEM_LAUNCH(k_panel_transpose<<<dim3((rem + 31) / 32, NB / 32), dim3(32, 8), 0, sp>>>(
-                rem, A, k0, k0 + NB, wtr, wtr + (size_t)n * NB));
+        // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)
+        auto part = [&](cudaStream_t s, int t0, int count) {
+            const int c0 = t0 * NB, cols = std::min(rem - c0, count < 0 ? rem : count * NB);
+            if (cols <= 0) return true;
+            if (!tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count)) return false;
+            float* wtr = wutb(k) + (size_t)c0 * NB;
+            BEM_LAUNCH(k_panel_transpose<<<dim3((cols + 31) / 32, NB / 32), dim3(32, 8), 0, s>>>(
+                cols, A, k0, k0 + NB + c0, wtr, wtr + (size_t)n * NB));
+            return true;
+        };
+        if (!part(sp, 0, 1)) return false;
+        if (ls.panel_tail) {
+            cudaEventRecord(ls.ev_head, sp);
+            cudaStreamWaitEvent(sq, ls.ev_head, 0);
         }
-        mark(k - 1, 3, sp);
-        cudaEventRecord(ls.ev_panel, sp);
-        mark(k - 1, 4, sp);
+        if (!part(sq, 1, -1)) return false;
+        mark(k - 1, 3, sq);
+        cudaEventRecord(ls.ev_panel, sq);
+        mark(k - 1, 4, sq);
         if (k > 0) {
             // U_{0:k, k} <- U_{0:k, k} D_kk^-1 (the backward solve's operator); those rows are
             // final and no longer read by the factorization
             if (ls.ucol_own) cudaStreamWaitEvent(ls.ucol, ls.ev_panel, 0);
-            if (!tc_ucol(ls.ucol_own ? ls.ucol : sp, n, k0, A, dTb(k), ls.ucol_ctas, flags)) return false;
+            if (!tc_ucol(ls.ucol_own ? ls.ucol : sq, n, k0, A, dTb(k), ls.ucol_ctas, flags)) return false;
         }
         return true;
     };
@@ -668,6 +718,10 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     // the last W21 stores and U-column transforms precede the solves
     cudaEventRecord(ls.ev_panel, sp);
     cudaStreamWaitEvent(st, ls.ev_panel, 0);
+    if (ls.panel_tail) {
+        cudaEventRecord(ls.ev_panel, sq);
+        cudaStreamWaitEvent(st, ls.ev_panel, 0);
+    }
     if (nblk > 1 && ls.ucol_own) {
         cudaEventRecord(ls.ev_ucol, ls.ucol);
         cudaStreamWaitEvent(st, ls.ev_ucol, 0);
@@ -1203,21 +1257,9 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
     float* tmp = X + (size_t)2 * n * R;
     int* xflag = ready;
     int* ticket = ready + 2 * n / TS_RW;
-    // Two of these solves running at once (contexts of bem_batch_solve on one GPU) could
-    // fill every SM with CTAs that wait on sub-blocks of their own launch which then find no
-    // SM.  The solves of all contexts on a device are therefore chained through one event:
-    // a launch starts after the previous one has finished.  Other kernels, which never wait
-    // on other CTAs, still run beside them.
-    static std::mutex mtx;
-    static cudaEvent_t chain[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lock(mtx);
-    cudaEvent_t& ev = chain[dev & 63];
-    if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return 1;
-    if (cudaStreamWaitEvent(st, ev, 0) != cudaSuccess) return 1;
-    if (trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags)) return 1;
-    return cudaEventRecord(ev, st) == cudaSuccess ? 0 : 1;
+    // Solves of several contexts may run at once on one GPU: a CTA waits only on
+    // sub-blocks of lower tickets of its own launch, which are already running.
+    return trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
 }
 
 // ---------------------------------------------------------------------------

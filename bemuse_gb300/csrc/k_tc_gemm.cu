@@ -426,7 +426,9 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
 // A21 is read in place from A, D^-1 as its transpose dT ([2][128][128], row j =
 // column j of D^-1); the product is stored into w ([2][n][128], rows from 0)
 // and over A21 in A.  Each tile reads its A21 rows before it overwrites them.
-bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags) {
+// Row tiles t0 .. t0 + count - 1 of A21 (count < 0: all from t0).
+bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
+            int count) {
     const int rem = n - k0 - 128;
     if (rem <= 0) return true;
     if (n % 128 || k0 % 128 || A.ld % 4) return false;
@@ -437,8 +439,9 @@ bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, floa
         !make_map_c(&mCr, w, n, 128, 128) || !make_map_c(&mCi, w + plane, n, 128, 128) ||
         !make_map_c(&mC2r, A.re, n, n, A.ld) || !make_map_c(&mC2i, A.im, n, n, A.ld))
         return false;
-    const int mt = rem / 128;
-    const TcTiles a{k0 + 128, 0, mt, 1, 0, 0, 0, 1, k0 + 128, k0};
+    const int mt = std::min(rem / 128 - t0, count < 0 ? rem / 128 : count);
+    if (t0 < 0 || mt <= 0) return true;
+    const TcTiles a{k0 + 128 + 128 * t0, 0, mt, 1, 0, 128 * t0, 0, 1, k0 + 128 + 128 * t0, k0};
     BEM_LAUNCH(k_tc_update<<<tc_grid(mt, 0), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i, a,
                                                                         flags));
     return true;

@@ -261,12 +261,15 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     0: the trailing update runs as short-lived CTAs that hand SMs to
  *                     the higher-priority panel stream as they retire.
  *   "lu_rest_tiles"   tiles per such short-lived CTA (default 4).
- *   "lu_cluster_inverse" 1: diagonal-block inverses on a cluster of two CTAs (default),
- *                     0: on one CTA.
+ *   "lu_cluster_inverse" CTAs per diagonal-block inverse: 2, 4 or 8 (a thread-block
+ *                     cluster, rows split between the CTAs; default 4) or 1 (one CTA).
  *   "lu_ucol_stream"  1: the U D^-1 transform of each finished column block (the
  *                     backward solve's operator) runs on its own stream (default),
  *                     0: on the panel stream behind each W21.
  *   "lu_ucol_ctas"    CTAs of each such transform (0 = one per 128 x 128 tile).
+ *   "lu_split_panel"  1: only the first tile of each panel's W21 and U transpose runs on
+ *                     the inverse chain, the rest on a second panel stream (default);
+ *                     0: the whole panel on the panel stream.
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
