@@ -136,7 +136,8 @@ struct LuStreams {
     int ucol_own;           // 1: U-column transforms on `ucol`, 0: on `panel` after each W21
     int ucol_ctas;          // CTAs per U-column transform (0: one per tile)
     cudaStream_t panel_tail;  // optional: W21 / transpose tiles beyond the first, off the inverse chain
-    cudaEvent_t ev_head;
+    cudaEvent_t ev_head, ev_t0;
+    int block_inverse;      // cluster inverse taken 8 pivots at a time (k_inv128b), 0: one at a time
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
 // diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The

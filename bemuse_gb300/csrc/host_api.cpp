@@ -58,7 +58,7 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1, blocked = -1;
     long long launches = 0;
 };
 
@@ -109,7 +109,7 @@ struct bem_ctx {
     cudaEvent_t ev_panel = nullptr, ev_cross = nullptr, ev_rest = nullptr, ev_ucol = nullptr;
     cudaStream_t su = nullptr;  // U-column transforms of the LU
     cudaStream_t sq = nullptr;  // panel tail of the LU (W21 / transpose tiles beyond the first)
-    cudaEvent_t ev_head = nullptr;
+    cudaEvent_t ev_head = nullptr, ev_t0 = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
@@ -121,6 +121,7 @@ struct bem_ctx {
     int lu_ucol_stream = 1;                     // U D^-1 transforms on their own stream (0: panel stream)
     int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
     int lu_split_panel = 1;                     // panel tiles beyond the first on their own stream
+    int lu_block_inverse = 1;                   // cluster inverse in panels of 8 pivots
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
@@ -348,7 +349,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                         ? ctx->lu_tl.data()
                                         : nullptr,
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
-                                    ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head};
+                                    ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
+                                    ctx->lu_block_inverse};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);
@@ -360,7 +362,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
                     g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
-                    g.split != ctx->lu_split_panel) {
+                    g.split != ctx->lu_split_panel || g.blocked != ctx->lu_block_inverse) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -385,6 +387,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.ucol = ctx->lu_ucol_stream;
                     g.ucol_ctas = ctx->lu_ucol_ctas;
                     g.split = ctx->lu_split_panel;
+                    g.blocked = ctx->lu_block_inverse;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -559,6 +562,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->su, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     CK(cudaStreamCreateWithPriority(&ctx->sq, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_head, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_t0, cudaEventDisableTiming));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
@@ -602,6 +606,7 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->su) cudaStreamDestroy(ctx->su);
     if (ctx->sq) cudaStreamDestroy(ctx->sq);
     if (ctx->ev_head) cudaEventDestroy(ctx->ev_head);
+    if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1405,6 +1410,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_ucol_ctas") {
         if (!(value >= 0 && value <= 1024)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_ctas must be in [0, 1024]");
         ctx->lu_ucol_ctas = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_block_inverse") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_block_inverse must be 0 or 1");
+        ctx->lu_block_inverse = (int)value;
         return BEM_OK;
     }
     if (k == "lu_split_panel") {

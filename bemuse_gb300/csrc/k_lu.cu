@@ -443,15 +443,262 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
         *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
         *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
     }
-    if (dT) {  // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1
+    if (dT) {
+        // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1.
+        // Staged through the (now free) panel-row buffer as [2][128 columns][RPC + 4 rows] so
+        // that each CTA writes its RPC-row stripe of every dT row with float4 stores.
+        constexpr int SL = RPC + 4;
+        float* st = reinterpret_cast<float*>(nrow);
+        __syncthreads();
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const size_t g = (size_t)(8 * cg + c) * 128 + row_base;
+        for (int c = 0; c < 8; ++c)
 #pragma unroll
             for (int m = 0; m < RPT; ++m) {
-                dT[g + m] = tf32_rn(v[m][c].x);
-                dT[16384 + g + m] = tf32_rn(v[m][c].y);
+                st[(8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].x);
+                st[128 * SL + (8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].y);
             }
+        __syncthreads();
+        constexpr int V = RPC / 4;  // float4 per stripe row
+        for (int idx = t; idx < 2 * 128 * V; idx += IC_THREADS) {
+            const int pl = idx / (128 * V), col = (idx / V) % 128, f = idx % V;
+            const float4 w = *reinterpret_cast<const float4*>(st + pl * 128 * SL + col * SL + 4 * f);
+            *reinterpret_cast<float4*>(dT + pl * 16384 + col * 128 + RPC * (int)rank + 4 * f) = w;
+        }
+    }
+    if (lf) atomicOr(flags, lf);
+    ic_cluster_sync();  // no CTA leaves while another may still address its shared memory
+}
+
+// Blocked form of the same Gauss-Jordan inverse on a cluster of CL CTAs, with the
+// rows split as in k_inv128c: the 128 pivots are taken 8 at a time (16 panels), so
+// the CTAs synchronise 16 times instead of 128.  Panel p (pivot rows / columns
+// P = 8p .. 8p + 7) belongs to the CTA owning those rows, which
+//   1. inverts the 8 x 8 pivot block D = M[P][P] in one warp (in-place Gauss-Jordan,
+//      the p + 1 substitution, shuffles only): X = D^-1;
+//   2. forms the panel row R = X M[P][:] with R[:, P] = X (8 x 128) and writes it into
+//      its own shared memory and, by st.async, into every peer's (one mbarrier per
+//      panel, 8 KB);
+// then every CTA updates its other rows i: M[i][j] <- M[i][j] [j not in P] - M[i][P] R[:, j]
+// and the owner copies R into rows P.  This is the composition of the 8 single-pivot
+// steps.  Waits on a peer give up at a 2 s deadline (FLAG_TIMEOUT); every CTA always
+// reaches the final cluster barrier.
+constexpr int IB_SMEM = 128 * 64 * 16      // panel rows R, [128][4][16] float4 as in k_inv128c
+                        + 64 * 8 * 8       // M[i][P] of this CTA's rows, [<= 64][8] float2
+                        + 8 * 128 * 8      // the owner's rows P, [8][128] float2
+                        + 64 * 8           // X, [8][8] float2
+                        + 16 * 8;          // one mbarrier per panel
+
+template <int CL>
+__global__ void __launch_bounds__(IC_THREADS, 1)
+    k_inv128b(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    constexpr int RPC = 128 / CL, RPT = RPC / 16;
+    static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
+    extern __shared__ __align__(16) float4 ib_smem[];
+    float4* nrow = ib_smem;                                              // [128][4][16]
+    float2* ccol = reinterpret_cast<float2*>(nrow + 128 * 64);           // [RPC][8]
+    float2* prow = ccol + 64 * 8;                                        // [8][128]
+    float2* xblk = prow + 8 * 128;                                       // [8][8]
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(xblk + 64);  // [16]
+    const uint32_t rank = ic_rank();
+    const int t = threadIdx.x, cg = t & 15, rg = t >> 4, warp = t >> 5, lane = t & 31;
+    const uint32_t nrow_s = (uint32_t)__cvta_generic_to_shared(nrow);
+    const uint32_t bars_s = (uint32_t)__cvta_generic_to_shared(bars);
+    float2 v[RPT][8];
+    const int row_base = RPC * (int)rank + RPT * rg;
+#pragma unroll
+    for (int m = 0; m < RPT; ++m) {
+        const size_t g = (size_t)(k0 + row_base + m) * A.ld + k0 + 8 * cg;
+        const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
+        const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
+        const float4 i0 = *reinterpret_cast<const float4*>(A.im + g);
+        const float4 i1 = *reinterpret_cast<const float4*>(A.im + g + 4);
+        v[m][0] = make_float2(r0.x, i0.x); v[m][1] = make_float2(r0.y, i0.y);
+        v[m][2] = make_float2(r0.z, i0.z); v[m][3] = make_float2(r0.w, i0.w);
+        v[m][4] = make_float2(r1.x, i1.x); v[m][5] = make_float2(r1.y, i1.y);
+        v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
+    }
+    if (t < 16) {
+        // panels this CTA receives: one arrival now, completed by the owner's 8 KB
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars_s + 8 * t) : "memory");
+        if ((8 * t) / RPC != (int)rank)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], 8192;" ::"r"(bars_s + 8 * t)
+                         : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ic_cluster_sync();
+    unsigned long long deadline;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(deadline));
+    deadline += 2000000000ull;
+    int lf = 0;
+    bool dead = false;
+#pragma unroll 1
+    for (int p = 0; p < 16; ++p) {
+        const bool owner = (8 * p) / RPC == (int)rank;
+        const int lp = 8 * p - RPC * (int)rank;  // first local row of P (owner only)
+        // M[i][P] of this CTA's rows: the threads holding column group p
+        if (cg == p) {
+#pragma unroll
+            for (int m = 0; m < RPT; ++m)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) ccol[(RPT * rg + m) * 8 + j] = v[m][j];
+        }
+        if (owner) {
+#pragma unroll
+            for (int m = 0; m < RPT; ++m) {
+                const int li = RPT * rg + m - lp;
+                if (li >= 0 && li < 8)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) prow[li * 128 + 8 * cg + c] = v[m][c];
+            }
+            __syncthreads();
+            if (warp == 0) {
+                // X = D^-1: lane (i, q) = (lane / 4, lane % 4) holds D[i][q] and D[i][q + 4]
+                const int i = lane >> 2, q = lane & 3;
+                float2 a0 = ccol[(lp + i) * 8 + q], a1 = ccol[(lp + i) * 8 + q + 4];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int kc = k & 3;
+                    const float2 s0 = k < 4 ? a0 : a1;  // this lane's value in column k
+                    const float px = __shfl_sync(0xffffffffu, s0.x, k * 4 + kc);
+                    const float py = __shfl_sync(0xffffffffu, s0.y, k * 4 + kc);
+                    const float den = px * px + py * py;
+                    if (lane == 0 && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
+                    const float rc = __frcp_rn(den), qr = px * rc, qi = -py * rc;
+                    // pivot row k, this lane's columns q and q + 4 (column k carries p + 1)
+                    float2 n0 = make_float2(__shfl_sync(0xffffffffu, a0.x, k * 4 + q),
+                                            __shfl_sync(0xffffffffu, a0.y, k * 4 + q));
+                    float2 n1 = make_float2(__shfl_sync(0xffffffffu, a1.x, k * 4 + q),
+                                            __shfl_sync(0xffffffffu, a1.y, k * 4 + q));
+                    if (q == kc) {
+                        if (k < 4) n0.x += 1.f;
+                        else n1.x += 1.f;
+                    }
+                    const float2 m0 = make_float2(n0.x * qr - n0.y * qi, n0.x * qi + n0.y * qr);
+                    const float2 m1 = make_float2(n1.x * qr - n1.y * qi, n1.x * qi + n1.y * qr);
+                    // column k of row i (minus 1 on the pivot row)
+                    float cx = __shfl_sync(0xffffffffu, s0.x, i * 4 + kc);
+                    const float cy = __shfl_sync(0xffffffffu, s0.y, i * 4 + kc);
+                    if (i == k) cx -= 1.f;
+                    a0.x = fmaf(-cx, m0.x, fmaf(cy, m0.y, a0.x));
+                    a0.y = fmaf(-cx, m0.y, fmaf(-cy, m0.x, a0.y));
+                    a1.x = fmaf(-cx, m1.x, fmaf(cy, m1.y, a1.x));
+                    a1.y = fmaf(-cx, m1.y, fmaf(-cy, m1.x, a1.y));
+                }
+                xblk[i * 8 + q] = a0;
+                xblk[i * 8 + q + 4] = a1;
+            }
+            __syncthreads();
+            {
+                // R[i][c0 .. c0 + 3] for i = t / 32, c0 = 4 (t % 32); R[:, P] = X
+                const int i = t >> 5, c0 = 4 * (t & 31);
+                float2 r[4];
+                if ((c0 >> 3) == p) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) r[c] = xblk[i * 8 + (c0 & 7) + c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) r[c] = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float2 x = xblk[i * 8 + j];
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const float2 y = prow[j * 128 + c0 + c];
+                            r[c].x = fmaf(x.x, y.x, fmaf(-x.y, y.y, r[c].x));
+                            r[c].y = fmaf(x.x, y.y, fmaf(x.y, y.x, r[c].y));
+                        }
+                    }
+                }
+                const int row = 8 * p + i, qq = (c0 & 7) >> 1, cgc = c0 >> 3;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float4 w = make_float4(r[2 * h].x, r[2 * h].y, r[2 * h + 1].x, r[2 * h + 1].y);
+                    const int idx = row * 64 + (qq + h) * 16 + cgc;
+                    nrow[idx] = w;
+#pragma unroll
+                    for (int pp = 1; pp < CL; ++pp) {
+                        const uint32_t peer = (rank + (uint32_t)pp) % CL;
+                        const uint32_t dst = ic_peer_addr(nrow_s + 16u * (uint32_t)idx, peer);
+                        const uint32_t bar = ic_peer_addr(bars_s + 8u * (uint32_t)p, peer);
+                        asm volatile(
+                            "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, "
+                            "[%5];" ::"r"(dst), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w), "r"(bar)
+                            : "memory");
+                    }
+                }
+            }
+            __syncthreads();
+        } else {
+            if (t == 0 && !dead && !ic_wait(bars_s + 8 * p, deadline)) dead = true;
+            __syncthreads();
+        }
+        // rows of this CTA: M[i][j] <- M[i][j] [j not in P] - M[i][P] R[:, j]; rows P <- R
+        bool inP[RPT];
+        float2 cm[RPT][8];
+#pragma unroll
+        for (int m = 0; m < RPT; ++m) {
+            const int li = RPT * rg + m - lp;
+            inP[m] = owner && li >= 0 && li < 8;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) cm[m][j] = ccol[(RPT * rg + m) * 8 + j];
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (inP[m] || cg == p) v[m][c] = make_float2(0.f, 0.f);
+            if (inP[m]) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) cm[m][j] = make_float2(j == li ? -1.f : 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            float2 rr[8];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 x = nrow[(8 * p + j) * 64 + q * 16 + cg];
+                rr[2 * q] = make_float2(x.x, x.y);
+                rr[2 * q + 1] = make_float2(x.z, x.w);
+            }
+#pragma unroll
+            for (int m = 0; m < RPT; ++m)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    v[m][c].x = fmaf(-cm[m][j].x, rr[c].x, fmaf(cm[m][j].y, rr[c].y, v[m][c].x));
+                    v[m][c].y = fmaf(-cm[m][j].x, rr[c].y, fmaf(-cm[m][j].y, rr[c].x, v[m][c].y));
+                }
+        }
+        __syncthreads();  // ccol, prow and xblk are rewritten for the next panel
+    }
+    if (dead) lf |= FLAG_TIMEOUT;
+    float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
+    float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
+#pragma unroll
+    for (int m = 0; m < RPT; ++m) {
+        const size_t g = (size_t)(row_base + m) * 128 + 8 * cg;
+        *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
+        *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
+        *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
+        *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
+    }
+    if (dT) {
+        // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1.
+        // Staged through the (now free) panel-row buffer as [2][128 columns][RPC + 4 rows] so
+        // that each CTA writes its RPC-row stripe of every dT row with float4 stores.
+        constexpr int SL = RPC + 4;
+        float* st = reinterpret_cast<float*>(nrow);
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+#pragma unroll
+            for (int m = 0; m < RPT; ++m) {
+                st[(8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].x);
+                st[128 * SL + (8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].y);
+            }
+        __syncthreads();
+        constexpr int V = RPC / 4;  // float4 per stripe row
+        for (int idx = t; idx < 2 * 128 * V; idx += IC_THREADS) {
+            const int pl = idx / (128 * V), col = (idx / V) % 128, f = idx % V;
+            const float4 w = *reinterpret_cast<const float4*>(st + pl * 128 * SL + col * SL + 4 * f);
+            *reinterpret_cast<float4*>(dT + pl * 16384 + col * 128 + RPC * (int)rank + 4 * f) = w;
         }
     }
     if (lf) atomicOr(flags, lf);
@@ -459,12 +706,12 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
 }
 
 // One cluster of cl CTAs (2, 4 or 8) inverting the diagonal block at k0.
-static void inv128_cluster(cudaStream_t st, int cl, int k0, CMat<float> A, float* invr, float* invi, float* dT,
-                           int* flags) {
+static void inv128_cluster(cudaStream_t st, int cl, bool blocked, int k0, CMat<float> A, float* invr, float* invi,
+                           float* dT, int* flags) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
     cfg.blockDim = dim3(IC_THREADS);
-    cfg.dynamicSmemBytes = IC_SMEM;
+    cfg.dynamicSmemBytes = blocked ? IB_SMEM : IC_SMEM;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -473,6 +720,14 @@ static void inv128_cluster(cudaStream_t st, int cl, int k0, CMat<float> A, float
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
+    if (blocked) {
+        switch (cl) {
+            case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128b<2>, k0, A, invr, invi, dT, flags)); break;
+            case 4: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128b<4>, k0, A, invr, invi, dT, flags)); break;
+            default: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128b<8>, k0, A, invr, invi, dT, flags)); break;
+        }
+        return;
+    }
     switch (cl) {
         case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128c<2>, k0, A, invr, invi, dT, flags)); break;
         case 4: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128c<4>, k0, A, invr, invi, dT, flags)); break;
@@ -480,6 +735,9 @@ static void inv128_cluster(cudaStream_t st, int cl, int k0, CMat<float> A, float
     }
 }
 static void inv128_cluster_setup() {
+    cudaFuncSetAttribute(k_inv128b<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
+    cudaFuncSetAttribute(k_inv128b<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
+    cudaFuncSetAttribute(k_inv128b<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
     cudaFuncSetAttribute(k_inv128c<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
     cudaFuncSetAttribute(k_inv128c<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
     cudaFuncSetAttribute(k_inv128c<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, IC_SMEM);
@@ -652,7 +910,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto inverse = [&](int k) {
         const int k0 = k * NB;
         if (ls.cluster_inverse >= 2)
-            inv128_cluster(sp, ls.cluster_inverse, k0, A, invr, invi, dTb(k), flags);
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse != 0, k0, A, invr, invi, dTb(k), flags);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
         mark(k - 1, 2, sp);
@@ -660,22 +918,34 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     cudaStream_t sq = ls.panel_tail ? ls.panel_tail : sp;
     auto w21 = [&](int k) {
         const int k0 = k * NB, rem = n - k0 - NB;
-        // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves)
-        auto part = [&](cudaStream_t s, int t0, int count) {
+        // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves), and
+        // U12^T into wut, for row / column tiles t0 .. t0 + count - 1 (count < 0: to the end)
+        auto w21_tiles = [&](cudaStream_t s, int t0, int count) {
+            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count);
+        };
+        auto tr_tiles = [&](cudaStream_t s, int t0, int count) {
             const int c0 = t0 * NB, cols = std::min(rem - c0, count < 0 ? rem : count * NB);
-            if (cols <= 0) return true;
-            if (!tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count)) return false;
+            if (cols <= 0) return;
             float* wtr = wutb(k) + (size_t)c0 * NB;
             BEM_LAUNCH(k_panel_transpose<<<dim3((cols + 31) / 32, NB / 32), dim3(32, 8), 0, s>>>(
                 cols, A, k0, k0 + NB + c0, wtr, wtr + (size_t)n * NB));
-            return true;
         };
-        if (!part(sp, 0, 1)) return false;
         if (ls.panel_tail) {
+            // the first U tile needs only the cross update, not the inverse: transposed on
+            // the tail stream while the inverse runs
+            cudaStreamWaitEvent(sq, ls.ev_cross, 0);
+            tr_tiles(sq, 0, 1);
+            cudaEventRecord(ls.ev_t0, sq);
+            if (!w21_tiles(sp, 0, 1)) return false;
+            cudaStreamWaitEvent(sp, ls.ev_t0, 0);
             cudaEventRecord(ls.ev_head, sp);
             cudaStreamWaitEvent(sq, ls.ev_head, 0);
+        } else {
+            if (!w21_tiles(sp, 0, 1)) return false;
+            tr_tiles(sp, 0, 1);
         }
-        if (!part(sq, 1, -1)) return false;
+        if (!w21_tiles(sq, 1, -1)) return false;
+        tr_tiles(sq, 1, -1);
         mark(k - 1, 3, sq);
         cudaEventRecord(ls.ev_panel, sq);
         mark(k - 1, 4, sq);

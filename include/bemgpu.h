@@ -267,6 +267,8 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     backward solve's operator) runs on its own stream (default),
  *                     0: on the panel stream behind each W21.
  *   "lu_ucol_ctas"    CTAs of each such transform (0 = one per 128 x 128 tile).
+ *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation
+ *                     (default), 0: one pivot per synchronisation.
  *   "lu_split_panel"  1: only the first tile of each panel's W21 and U transpose runs on
  *                     the inverse chain, the rest on a second panel stream (default);
  *                     0: the whole panel on the panel stream.
