@@ -303,7 +303,7 @@ __device__ __forceinline__ bool ic_wait(uint32_t bar, unsigned long long deadlin
             : "r"(bar)
             : "memory");
         if (done) return true;
-        if ((i & 15) == 15) {
+        if ((i & 255) == 255) {  // a %globaltimer read costs far more than a poll
             unsigned long long t;
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
             if (t > deadline) return false;
@@ -1268,11 +1268,12 @@ __device__ __forceinline__ unsigned long long ts_now() {
 __device__ __forceinline__ void ts_wait(const int* f, int epoch, unsigned long long deadline, int& dead,
                                         int* gflags) {
     if (dead) return;
-    for (;;) {
+    // the timer is read once per 256 polls: a %globaltimer read costs far more than a poll
+    for (int i = 1;; ++i) {
         int v;
         asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
         if (v >= epoch) return;
-        if (ts_now() > deadline) { dead = 1; atomicOr(gflags, FLAG_TIMEOUT); return; }
+        if ((i & 255) == 0 && ts_now() > deadline) { dead = 1; atomicOr(gflags, FLAG_TIMEOUT); return; }
     }
 }
 
@@ -1415,13 +1416,10 @@ __global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat
         }
         reinterpret_cast<float2*>(Xout)[(row0 + i) * R + j] = o;
     }
-    // the CTA barrier orders every thread's stores before thread 0's fence and
-    // release store of the flag (release is cumulative), as in a grid barrier
+    // the CTA barrier orders every thread's stores before thread 0's release store of
+    // the flag, and release is cumulative: a consumer that acquires the flag sees them
     __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
-    }
+    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
 }
 
 // x_b = D_b^-1 z_b for every 128-row block b: CTA (b, 16-row group q), thread
