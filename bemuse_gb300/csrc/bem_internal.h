@@ -172,6 +172,18 @@ void launch_matx_df(cudaStream_t st, int N, int ld, const float* Mhi, const floa
 void launch_split_mat_df(cudaStream_t st, size_t n, const double* M, float* hi, float* lo);
 // nrm[j] = max_r |Rres[r][j]|, nrm[R + j] = max_r |Y[r][j]| as ordered bit patterns (zero them first).
 void launch_norms(cudaStream_t st, int N, int R, const double* Rres, const double* Y, unsigned long long* nrm);
+// Flexible-GMRES vector kernels (k_gmres.cu).  Vectors are Np x R complex blocks
+// (interleaved, R columns); a set of nvec vectors lies vstride doubles apart.
+//   gm_dots:    h[v][r] = sum_n conj(V_v[n][r]) w[n][r]   (part: gm_part_doubles(Np, nvec))
+//   gm_combine: out = beta out + sign sum_v c[v][r] V_v
+//   gm_scale:   out = w / sqrt(Re nrm2[r]) per column (0 for a vanishing norm)
+size_t gm_part_doubles(int Np, int nvec);
+void launch_gm_dots(cudaStream_t st, int Np, int R, int nvec, const double* V, size_t vstride, const double* w,
+                    double* part, double* h);
+void launch_gm_combine(cudaStream_t st, int Np, int R, int nvec, const double* V, size_t vstride, const double* c,
+                       double sign, double beta, double* out);
+void launch_gm_scale(cudaStream_t st, int Np, int R, const double* w, const double* nrm2, double* out);
+void launch_f32_to_f64(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
 void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);

@@ -93,6 +93,13 @@ struct bem_ctx {
     int* d_ready = nullptr;           // block-ready flags of the cooperative triangular solves
     int solve_epoch = 0;
     unsigned long long* d_norms = nullptr;
+    // flexible GMRES refinement: Krylov basis V, preconditioned vectors Z, work vector W,
+    // partial sums, Hessenberg columns (h1, h2, norm) and combination coefficients; pinned
+    // host mirror of the Hessenberg block
+    double *d_gmV = nullptr, *d_gmZ = nullptr, *d_gmW = nullptr, *d_gmPart = nullptr, *d_gmH = nullptr,
+           *d_gmC = nullptr;
+    double* h_gm = nullptr;
+    int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
@@ -191,7 +198,8 @@ void free_all(bem_ctx* ctx) {
     double** dp[] = {&ctx->d_rec, &ctx->d_xr, &ctx->d_gq, &ctx->d_rn, &ctx->d_cen, &ctx->d_nrm, &ctx->d_area,
                      &ctx->d_Nk, &ctx->d_betas, &ctx->d_RS, &ctx->d_RD, &ctx->d_RSR, &ctx->d_D64r, &ctx->d_D64i,
                      &ctx->d_Ys6, &ctx->d_X, &ctx->d_Rr, &ctx->d_part, &ctx->d_post, &ctx->d_inv64r,
-                     &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64};
+                     &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64, &ctx->d_gmV, &ctx->d_gmZ, &ctx->d_gmW,
+                     &ctx->d_gmPart, &ctx->d_gmH, &ctx->d_gmC};
     for (auto p : dp) *p = nullptr;
     float** fp[] = {&ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i, &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32,
                     &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi, &ctx->d_RSRlo};
@@ -280,6 +288,8 @@ bool inv6(const cplx* M, cplx* out) {
     return true;
 }
 
+constexpr int GM_M = 16;  // restart length of the flexible GMRES refinement
+
 bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     const int nb64 = 64, nb32 = 128;
     if (!mixed) {
@@ -297,6 +307,13 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_wut32, (size_t)4 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
+        const size_t vs = (size_t)2 * Np * bem::MAX_RHS;
+        DA(ctx->d_gmV, (size_t)(GM_M + 1) * vs);
+        DA(ctx->d_gmZ, (size_t)GM_M * vs);
+        DA(ctx->d_gmW, vs);
+        DA(ctx->d_gmPart, bem::gm_part_doubles(Np, GM_M + 1));
+        DA(ctx->d_gmH, (size_t)3 * (GM_M + 1) * bem::MAX_RHS * 2);
+        DA(ctx->d_gmC, (size_t)(GM_M + 1) * bem::MAX_RHS * 2);
     }
     DA(ctx->d_X, (size_t)4 * Np * R);
     DA(ctx->fs[0].mx, bem::matx_part_doubles(Np, bem::MAX_RHS));
@@ -308,6 +325,188 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     }
     DA(ctx->d_norms, 2 * bem::MAX_RHS);
     return BEM_OK;
+}
+
+// Flexible GMRES (restart GM_M) on D x = y in FP64, right-preconditioned with the FP32
+// factors, all right-hand sides at once (one Krylov basis per column, one complex Givens
+// sequence per column on the host).  Each iteration costs one preconditioner solve and
+// one operator product, as a classic refinement sweep does, and its residual is the
+// smallest over the Krylov space that holds the classic iterate, so it never needs more
+// iterations; near-singular systems (frequencies close to an irregular frequency of the
+// body) converge in far fewer.  Orthogonalisation: classical Gram-Schmidt, twice, on the
+// device.  Convergence: the same test as classic refinement, max_r |r_r|_inf / |y_r|_inf
+// <= tol, on the residual r = V (beta e1 - H y) (the Arnoldi relation D Z = V H), checked
+// once the recurrence estimate is near the tolerance; a restart recomputes the residual
+// from x.  On entry d_X holds x and d_Rr = y - D x (rows N..Np zero); iters counts on.
+bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double tol, int max_iter,
+                        const std::function<void(const double*, const double*, double, double, double*)>& apply_op,
+                        const std::function<bem_status(const double*, double*)>& precond, int& iters,
+                        double& resid) {
+    using C = std::complex<double>;
+    cudaStream_t st = ctx->st;
+    const size_t vs = (size_t)2 * Np * R;
+    const int M = GM_M;
+    double* V = ctx->d_gmV;
+    double* Z = ctx->d_gmZ;
+    double* W = ctx->d_gmW;
+    double* h1 = ctx->d_gmH;
+    double* h2 = h1 + (size_t)(M + 1) * R * 2;
+    double* hn = h2 + (size_t)(M + 1) * R * 2;
+    double* hh = ctx->h_gm;  // pinned mirror of h1 | h2 | hn
+    const size_t hblock = (size_t)3 * (M + 1) * R * 2;
+    // |y|_inf and |y|_2 per column
+    std::vector<double> yinf(R), y2(R);
+    {
+        std::vector<unsigned long long> nn(2 * R);
+        CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+        bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
+        bem::launch_gm_dots(st, N, R, 1, F.Y, vs, F.Y, ctx->d_gmPart, hn);
+        CK(cudaMemcpyAsync(nn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hh, hn, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int r = 0; r < R; ++r) {
+            memcpy(&yinf[r], &nn[R + r], 8);
+            y2[r] = std::sqrt(std::max(hh[2 * r], 0.0));
+        }
+    }
+    std::vector<C> Hu((size_t)R * (M + 1) * M), Hr((size_t)R * (M + 1) * M), g((size_t)R * (M + 1)), sn((size_t)R * M);
+    std::vector<double> cs((size_t)R * M), beta(R);
+    std::vector<C> yv((size_t)R * M);
+    std::vector<double> coef((size_t)(M + 1) * R * 2);
+    std::vector<unsigned long long> nn(2 * R);
+    auto hu = [&](int r, int i, int j) -> C& { return Hu[((size_t)r * (M + 1) + i) * M + j]; };
+    auto hr = [&](int r, int i, int j) -> C& { return Hr[((size_t)r * (M + 1) + i) * M + j]; };
+    for (;;) {
+        // cycle start: d_Rr holds the residual of x; V_0 = r / |r|_2
+        bem::launch_gm_dots(st, Np, R, 1, ctx->d_Rr, vs, ctx->d_Rr, ctx->d_gmPart, hn);
+        bem::launch_gm_scale(st, Np, R, ctx->d_Rr, hn, V);
+        CK(cudaMemcpyAsync(hh, hn, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int r = 0; r < R; ++r) {
+            beta[r] = std::sqrt(std::max(hh[2 * r], 0.0));
+            for (int i = 0; i <= M; ++i) g[(size_t)r * (M + 1) + i] = 0.0;
+            g[(size_t)r * (M + 1)] = beta[r];
+        }
+        int j = 0;
+        bool done = false;
+        for (; j < M; ++j) {
+            double* Vj = V + (size_t)j * vs;
+            double* Zj = Z + (size_t)j * vs;
+            bem_status ps = precond(Vj, Zj);
+            if (ps != BEM_OK) return ps;
+            apply_op(Zj, nullptr, 1.0, 0.0, W);
+            bem::launch_pad_rhs(st, N, Np, R, W);
+            // W -= V h1, W -= V h2 (classical Gram-Schmidt, twice); V_{j+1} = W / |W|
+            bem::launch_gm_dots(st, Np, R, j + 1, V, vs, W, ctx->d_gmPart, h1);
+            bem::launch_gm_combine(st, Np, R, j + 1, V, vs, h1, -1.0, 1.0, W);
+            bem::launch_gm_dots(st, Np, R, j + 1, V, vs, W, ctx->d_gmPart, h2);
+            bem::launch_gm_combine(st, Np, R, j + 1, V, vs, h2, -1.0, 1.0, W);
+            bem::launch_gm_dots(st, Np, R, 1, W, vs, W, ctx->d_gmPart, hn);
+            bem::launch_gm_scale(st, Np, R, W, hn, V + (size_t)(j + 1) * vs);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(hh, h1, sizeof(double) * hblock, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            ++iters;
+            double est = 0.0;
+            for (int r = 0; r < R; ++r) {
+                for (int i = 0; i <= j; ++i) {
+                    const size_t o = 2 * ((size_t)i * R + r);
+                    const size_t o2 = o + (size_t)(M + 1) * R * 2;
+                    hu(r, i, j) = C(hh[o] + hh[o2], hh[o + 1] + hh[o2 + 1]);
+                }
+                hu(r, j + 1, j) = C(std::sqrt(std::max(hh[2 * ((size_t)2 * (M + 1) * R + r)], 0.0)), 0.0);
+                for (int i = 0; i <= j + 1; ++i) hr(r, i, j) = hu(r, i, j);
+                // earlier rotations, then a new one that zeroes H[j+1][j]
+                for (int i = 0; i < j; ++i) {
+                    const double c = cs[(size_t)r * M + i];
+                    const C s = sn[(size_t)r * M + i];
+                    const C a = hr(r, i, j), b = hr(r, i + 1, j);
+                    hr(r, i, j) = c * a + s * b;
+                    hr(r, i + 1, j) = -std::conj(s) * a + c * b;
+                }
+                const C a = hr(r, j, j), b = hr(r, j + 1, j);
+                const double rho = std::sqrt(std::norm(a) + std::norm(b));
+                double c = 1.0;
+                C s = 0.0;
+                if (rho > 0.0) {
+                    if (std::abs(a) > 0.0) {
+                        c = std::abs(a) / rho;
+                        s = (a / std::abs(a)) * std::conj(b) / rho;
+                    } else {
+                        c = 0.0;
+                        s = std::conj(b) / std::abs(b);
+                    }
+                }
+                cs[(size_t)r * M + j] = c;
+                sn[(size_t)r * M + j] = s;
+                hr(r, j, j) = c * a + s * b;
+                hr(r, j + 1, j) = 0.0;
+                C& gj = g[(size_t)r * (M + 1) + j];
+                g[(size_t)r * (M + 1) + j + 1] = -std::conj(s) * gj;
+                gj = c * gj;
+                const double e = std::abs(g[(size_t)r * (M + 1) + j + 1]);
+                est = std::max(est, y2[r] > 0 ? e / y2[r] : e);
+            }
+            if (!(est < 1e300)) {
+                resid = est;
+                return fail(ctx, BEM_ERR_NUMERIC, "GMRES refinement: non-finite residual");
+            }
+            const bool last = j + 1 == M || iters >= max_iter;
+            if (est > 10.0 * tol && !last) continue;
+            // y = R^-1 g per column
+            for (int r = 0; r < R; ++r)
+                for (int i = j; i >= 0; --i) {
+                    C t = g[(size_t)r * (M + 1) + i];
+                    for (int k = i + 1; k <= j; ++k) t -= hr(r, i, k) * yv[(size_t)r * M + k];
+                    const C d = hr(r, i, i);
+                    yv[(size_t)r * M + i] = std::abs(d) > 0.0 ? t / d : C(0.0);
+                }
+            // residual r = V_{0..j+1} (beta e1 - H y), then the classic test
+            for (int r = 0; r < R; ++r)
+                for (int i = 0; i <= j + 1; ++i) {
+                    C t = i == 0 ? C(beta[r]) : C(0.0);
+                    for (int k = std::max(i - 1, 0); k <= j; ++k) t -= hu(r, i, k) * yv[(size_t)r * M + k];
+                    coef[2 * ((size_t)i * R + r)] = t.real();
+                    coef[2 * ((size_t)i * R + r) + 1] = t.imag();
+                }
+            CK(cudaMemcpyAsync(ctx->d_gmC, coef.data(), sizeof(double) * 2 * (size_t)(j + 2) * R,
+                               cudaMemcpyHostToDevice, st));
+            bem::launch_gm_combine(st, Np, R, j + 2, V, vs, ctx->d_gmC, 1.0, 0.0, W);
+            CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+            bem::launch_norms(st, N, R, W, F.Y, ctx->d_norms);
+            CK(cudaMemcpyAsync(nn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost,
+                               st));
+            CK(cudaStreamSynchronize(st));
+            resid = 0.0;
+            for (int r = 0; r < R; ++r) {
+                double rn;
+                memcpy(&rn, &nn[r], 8);
+                resid = std::max(resid, yinf[r] > 0 ? rn / yinf[r] : rn);
+            }
+            if (resid <= tol || last) {
+                done = resid <= tol;
+                break;
+            }
+        }
+        // x += Z y
+        const int nz = std::min(j + 1, M);
+        for (int r = 0; r < R; ++r)
+            for (int i = 0; i < nz; ++i) {
+                coef[2 * ((size_t)i * R + r)] = yv[(size_t)r * M + i].real();
+                coef[2 * ((size_t)i * R + r) + 1] = yv[(size_t)r * M + i].imag();
+            }
+        CK(cudaMemcpyAsync(ctx->d_gmC, coef.data(), sizeof(double) * 2 * (size_t)nz * R, cudaMemcpyHostToDevice, st));
+        bem::launch_gm_combine(st, Np, R, nz, Z, vs, ctx->d_gmC, 1.0, 1.0, ctx->d_X);
+        CK(cudaGetLastError());
+        if (done) return BEM_OK;
+        if (iters >= max_iter || !(resid < 1e300))
+            return fail(ctx, BEM_ERR_NUMERIC, "GMRES refinement did not reach the tolerance (residual " +
+                                                  std::to_string(resid) + " after " + std::to_string(iters) +
+                                                  " iterations)");
+        // restart from the true residual of x
+        apply_op(ctx->d_X, F.Y, -1.0, 1.0, ctx->d_Rr);
+        bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+    }
 }
 
 // Factor + solve.  D64 (planar, ld = Np) holds the operator; Y (N x R, interleaved)
@@ -407,54 +606,91 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             const bem_status sa = after_lu();
             if (sa != BEM_OK) return sa;
         }
-        // x0 = LU^-1 y
-        CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * nr2, st));
-        CK(cudaMemcpyAsync(ctx->d_Rr, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
-        bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
-        std::vector<unsigned long long> hn(2 * R);
-        for (;;) {
-            bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
+        // out = beta base + alpha D x over the N rows (the refinement's FP64-accurate operator):
+        // Re D x from the float pairs (double-float products), i Im D x from the plane waves
+        auto apply_op = [&](const double* x, const double* base, double alpha, double beta, double* out) {
+            if (ctx->resid_mode >= 2) {
+                bem::launch_matx_df(st, N, Np, F.Dhi, F.Dlo, R, x, R, 0, F.Xdf, F.mx, alpha, beta, base, out, R);
+                if (ctx->resid_mode == 3) {
+                    const double c2 = F.pw_K * F.pw_K * 0.25 / 3.14159265358979323846;
+                    bem::launch_pw_correct(st, N, F.pw_M, R, -alpha * 3.14159265358979323846 * c2 / F.pw_M, F.pwW,
+                                           F.pwE, F.Xdf, F.pwT, out);
+                }
+            } else {
+                bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0, x, R,
+                                 F.mx, alpha, beta, base, out, R);
+            }
+        };
+        // M^-1 v with the FP32 factors (v, z: Np x R FP64)
+        auto precond = [&](const double* v, double* z) -> bem_status {
+            bem::launch_to_f32(st, nr2, v, ctx->d_X32);
             ctx->solve_epoch += 2;
             if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
                                   ctx->solve_epoch - 1, ctx->d_flags))
-                return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
-            bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
-            CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
-            if (ctx->resid_mode >= 2) {
-                // r = y - Re(D) x  (float pairs, double-float products) - i Im(D) x  (plane waves, FP64)
-                bem::launch_matx_df(st, N, Np, F.Dhi, F.Dlo, R, ctx->d_X, R, 0, F.Xdf, F.mx,
-                                    -1.0, 1.0, F.Y, ctx->d_Rr, R);
-                if (ctx->resid_mode == 3) {
-                    const double c2 = F.pw_K * F.pw_K * 0.25 / 3.14159265358979323846;
-                    bem::launch_pw_correct(st, N, F.pw_M, R, 3.14159265358979323846 * c2 / F.pw_M,
-                                           F.pwW, F.pwE, F.Xdf, F.pwT, ctx->d_Rr);
-                }
-            } else {
-                bem::launch_matx(st, N, Np, ctx->d_D64r, ctx->resid_mode == 1 ? nullptr : ctx->d_D64i, R, 0,
-                                 ctx->d_X, R, F.mx, -1.0, 1.0, F.Y, ctx->d_Rr, R);
-            }
-            bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
-            CK(cudaGetLastError());
-            CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            ++iters;
-            resid = 0.0;
-            for (int j = 0; j < R; ++j) {
-                double rn, yn;
-                memcpy(&rn, &hn[j], 8);
-                memcpy(&yn, &hn[R + j], 8);
-                double rel = yn > 0 ? rn / yn : rn;
-                resid = std::max(resid, rel);
-            }
-            if (resid <= tol) break;
-            if (iters >= max_iter || !(resid < 1e300)) {
+                return fail(ctx, BEM_ERR_CUDA, "triangular-solve launch failed");
+            bem::launch_f32_to_f64(st, nr2, ctx->d_X32, z);
+            return BEM_OK;
+        };
+        CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * nr2, st));
+        CK(cudaMemcpyAsync(ctx->d_Rr, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
+        bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+        auto gmres = [&]() -> bem_status {
+            const bem_status gs = refine_gmres(ctx, F, N, Np, R, tol, max_iter, apply_op, precond, iters, resid);
+            if (gs != BEM_OK) {
                 if (iters_out) *iters_out = iters;
                 if (resid_out) *resid_out = resid;
-                return fail(ctx, BEM_ERR_NUMERIC, "iterative refinement did not reach the tolerance (residual " +
-                                                      std::to_string(resid) + " after " + std::to_string(iters) +
-                                                      " sweeps)");
             }
-            bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+            return gs;
+        };
+        if (ctx->refine_gmres == 1) {
+            const bem_status gs = gmres();
+            if (gs != BEM_OK) return gs;
+        } else {
+            // classic refinement: x <- x + M^-1 (y - D x).  With refine_gmres = 2 a sweep
+            // that reduces the residual by less than 20x (a nearly singular system, e.g. a
+            // frequency close to an irregular frequency of the body) hands x and its
+            // residual over to flexible GMRES.
+            std::vector<unsigned long long> hn(2 * R);
+            double prev = 0.0;
+            for (;;) {
+                bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
+                ctx->solve_epoch += 2;
+                if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
+                                      ctx->solve_epoch - 1, ctx->d_flags))
+                    return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
+                bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
+                CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+                apply_op(ctx->d_X, F.Y, -1.0, 1.0, ctx->d_Rr);
+                bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
+                CK(cudaGetLastError());
+                CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R,
+                                   cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                ++iters;
+                resid = 0.0;
+                for (int j = 0; j < R; ++j) {
+                    double rn, yn;
+                    memcpy(&rn, &hn[j], 8);
+                    memcpy(&yn, &hn[R + j], 8);
+                    double rel = yn > 0 ? rn / yn : rn;
+                    resid = std::max(resid, rel);
+                }
+                if (resid <= tol) break;
+                if (iters >= max_iter || !(resid < 1e300)) {
+                    if (iters_out) *iters_out = iters;
+                    if (resid_out) *resid_out = resid;
+                    return fail(ctx, BEM_ERR_NUMERIC, "iterative refinement did not reach the tolerance (residual " +
+                                                          std::to_string(resid) + " after " + std::to_string(iters) +
+                                                          " sweeps)");
+                }
+                bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+                if (ctx->refine_gmres == 2 && iters >= 2 && resid > 0.05 * prev) {
+                    const bem_status gs = gmres();
+                    if (gs != BEM_OK) return gs;
+                    break;
+                }
+                prev = resid;
+            }
         }
         CK(cudaEventRecord(ctx->ev[4], st));
     }
@@ -563,6 +799,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->sq, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_head, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_t0, cudaEventDisableTiming));
+    CK(cudaMallocHost(&ctx->h_gm, sizeof(double) * 3 * (GM_M + 1) * bem::MAX_RHS * 2));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
@@ -607,6 +844,7 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sq) cudaStreamDestroy(ctx->sq);
     if (ctx->ev_head) cudaEventDestroy(ctx->ev_head);
     if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
+    if (ctx->h_gm) cudaFreeHost(ctx->h_gm);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1410,6 +1648,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_ucol_ctas") {
         if (!(value >= 0 && value <= 1024)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_ctas must be in [0, 1024]");
         ctx->lu_ucol_ctas = (int)value;
+        return BEM_OK;
+    }
+    if (k == "refine_gmres") {
+        if (!(value == 0 || value == 1 || value == 2)) return fail(ctx, BEM_ERR_ARG, "refine_gmres must be 0, 1 or 2");
+        ctx->refine_gmres = (int)value;
         return BEM_OK;
     }
     if (k == "lu_block_inverse") {

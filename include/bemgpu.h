@@ -267,6 +267,11 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     backward solve's operator) runs on its own stream (default),
  *                     0: on the panel stream behind each W21.
  *   "lu_ucol_ctas"    CTAs of each such transform (0 = one per 128 x 128 tile).
+ *   "refine_gmres"    refinement of the mixed path, all stopping at the same residual
+ *                     test: 0 classic x <- x + LU^-1 (y - D x); 1 flexible GMRES
+ *                     (restart 16) with the TF32 factors as preconditioner, which never
+ *                     needs more preconditioner solves; 2 (default) classic sweeps while
+ *                     each reduces the residual more than 20x, then GMRES from there.
  *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation
  *                     (default), 0: one pivot per synchronisation.
  *   "lu_split_panel"  1: only the first tile of each panel's W21 and U transpose runs on

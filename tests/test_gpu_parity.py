@@ -122,6 +122,27 @@ def test_mixed_solve_matches_oracle_cylinder(bg, orc):
     _compare(got, ref, 1e-6)
 
 
+def test_refinement_variants_agree_near_irregular_frequency(bg, orc):
+    # The 144-panel cylinder (R = 10, draft 20) has its first irregular frequency near
+    # K R = 2.405 coth(2.405 draft / R), Omega ~ 1.54: the system is nearly singular there
+    # and classic refinement contracts slowly.  Classic (0), flexible GMRES (1) and the
+    # default switch from classic to GMRES (2) must meet the same residual test, agree
+    # with the oracle, and GMRES must not need more preconditioner solves than classic.
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    om = np.linspace(1.45, 1.65, 9)
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL), precision=bg.MIXED)
+    ref = _oracle_solve(orc, m, aux, om, cases.BETAS, s)
+    got = {}
+    for mode in (0, 1, 2):
+        s.set_tuning("refine_gmres", mode)
+        got[mode] = s.solve_omegas(om)
+        print("refine_gmres", mode, "iterations", got[mode]["iters"], "residual", got[mode]["residual"].max())
+        assert np.all(got[mode]["residual"] <= 1e-12)
+        _compare(got[mode], ref, 1e-6)
+    assert np.all(got[1]["iters"] <= got[0]["iters"] + 1)
+    assert np.all(got[2]["iters"] <= got[0]["iters"] + 1)
+
+
 def test_plain_fp64_solve_matches_oracle_array(bg, orc):
     c = cases.ARRAY_SMALL
     om, _ = orc.cylinder(c["R"], c["draft"], c["NA"], c["NR"], c["NV"], cosine=False)
