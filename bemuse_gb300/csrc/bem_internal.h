@@ -138,6 +138,8 @@ struct LuStreams {
     cudaStream_t panel_tail;  // optional: W21 / transpose tiles beyond the first, off the inverse chain
     cudaEvent_t ev_head, ev_t0;
     int block_inverse;      // cluster inverse taken 8 pivots at a time (k_inv128b), 0: one at a time
+    cudaStream_t rest;      // paired schedule: trailing updates of two steps at a time
+    cudaEvent_t ev_panel2, ev_cross2;
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
 // diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The
@@ -146,6 +148,10 @@ struct LuStreams {
 // by the inverse of its diagonal block), the form lu_solve_f32 uses.
 int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                             float* wl2, float* wut2, int* flags);
+// Paired schedule (two elimination steps per pass over the trailing matrix); needs
+// ls.panel_tail, ls.rest and ls.ucol_own.  wl4: 8 n 128 floats; wut4: 8 n 128 + 256 n.
+int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
+                         float* wl4, float* wut4, int* flags);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place,
 // with an n x R scratch right after X.  ready: n/nb ints zeroed at allocation; epoch
 // strictly increasing across calls on the same ready array (each call uses epoch and

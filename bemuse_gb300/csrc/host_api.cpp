@@ -58,7 +58,7 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1, blocked = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1, blocked = -1, pair = -1;
     long long launches = 0;
 };
 
@@ -117,6 +117,8 @@ struct bem_ctx {
     cudaStream_t su = nullptr;  // U-column transforms of the LU
     cudaStream_t sq = nullptr;  // panel tail of the LU (W21 / transpose tiles beyond the first)
     cudaEvent_t ev_head = nullptr, ev_t0 = nullptr;
+    cudaStream_t sr = nullptr;  // trailing updates of the paired LU schedule
+    cudaEvent_t ev_panel2 = nullptr, ev_cross2 = nullptr;
     double stage_ms[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev_wk[2] = {};                  // around the wave-assembly kernel launch
     cudaEvent_t ev_call = nullptr;              // start of a bem_solve call (device span)
@@ -129,9 +131,10 @@ struct bem_ctx {
     int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
     int lu_split_panel = 1;                     // panel tiles beyond the first on their own stream
     int lu_block_inverse = 1;                   // cluster inverse in panels of 8 pivots
+    int lu_pair_update = 1;                     // trailing updates of two steps per pass
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
-    int asm_overlap = 1, asm_reserve = 24, asm_per_sm = 3;
+    int asm_overlap = 1, asm_reserve = 72, asm_per_sm = 3;
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
@@ -302,9 +305,9 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->fs[0].D32i, (size_t)Np * Np);
         DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
-        DA(ctx->d_wl32, (size_t)4 * Np * nb32);  // two [2][Np][128] buffers (lookahead)
+        DA(ctx->d_wl32, (size_t)8 * Np * nb32);  // four [2][Np][128] buffers (lookahead; two steps per pass)
         DA(ctx->d_wu32, (size_t)2 * Np * nb32);
-        DA(ctx->d_wut32, (size_t)4 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
+        DA(ctx->d_wut32, (size_t)8 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
         const size_t vs = (size_t)2 * Np * bem::MAX_RHS;
@@ -549,7 +552,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                         : nullptr,
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
                                     ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
-                                    ctx->lu_block_inverse};
+                                    ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);
@@ -561,14 +564,18 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
                     g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
-                    g.split != ctx->lu_split_panel || g.blocked != ctx->lu_block_inverse) {
+                    g.split != ctx->lu_split_panel || g.blocked != ctx->lu_block_inverse ||
+                    g.pair != ctx->lu_pair_update) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
                     cudaGraph_t graph = nullptr;
                     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-                    rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
-                                                         ctx->d_wut32, ctx->d_flags);
+                    const bool paired = ctx->lu_pair_update && ls.panel_tail && ls.ucol_own;
+                    rc_lu = paired ? bem::lu_factor_f32_paired(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i,
+                                                               ctx->d_wl32, ctx->d_wut32, ctx->d_flags)
+                                   : bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i,
+                                                                  ctx->d_wl32, ctx->d_wut32, ctx->d_flags);
                     const cudaError_t ec = cudaStreamEndCapture(st, &graph);
                     if (rc_lu == 0 && ec == cudaSuccess) {
                         const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
@@ -587,6 +594,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.ucol_ctas = ctx->lu_ucol_ctas;
                     g.split = ctx->lu_split_panel;
                     g.blocked = ctx->lu_block_inverse;
+                    g.pair = ctx->lu_pair_update;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -799,6 +807,9 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->sq, cudaStreamNonBlocking, prio_hi));
     CK(cudaEventCreateWithFlags(&ctx->ev_head, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ctx->ev_t0, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithPriority(&ctx->sr, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
+    CK(cudaEventCreateWithFlags(&ctx->ev_panel2, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_cross2, cudaEventDisableTiming));
     CK(cudaMallocHost(&ctx->h_gm, sizeof(double) * 3 * (GM_M + 1) * bem::MAX_RHS * 2));
     for (auto& ev : ctx->ev_wk) CK(cudaEventCreate(&ev));
     CK(cudaEventCreate(&ctx->ev_call));
@@ -824,6 +835,7 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sa) cudaStreamSynchronize(ctx->sa);
     if (ctx->su) cudaStreamSynchronize(ctx->su);
     if (ctx->sq) cudaStreamSynchronize(ctx->sq);
+    if (ctx->sr) cudaStreamSynchronize(ctx->sr);
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5})
             if (e) cudaEventDestroy(e);
@@ -844,6 +856,9 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sq) cudaStreamDestroy(ctx->sq);
     if (ctx->ev_head) cudaEventDestroy(ctx->ev_head);
     if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
+    if (ctx->ev_panel2) cudaEventDestroy(ctx->ev_panel2);
+    if (ctx->ev_cross2) cudaEventDestroy(ctx->ev_cross2);
+    if (ctx->sr) cudaStreamDestroy(ctx->sr);
     if (ctx->h_gm) cudaFreeHost(ctx->h_gm);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -1648,6 +1663,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_ucol_ctas") {
         if (!(value >= 0 && value <= 1024)) return fail(ctx, BEM_ERR_ARG, "lu_ucol_ctas must be in [0, 1024]");
         ctx->lu_ucol_ctas = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_pair_update") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_pair_update must be 0 or 1");
+        ctx->lu_pair_update = (int)value;
         return BEM_OK;
     }
     if (k == "refine_gmres") {

@@ -27,6 +27,9 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
 bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
             int count);
 bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags);
+bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
+                    int max_ctas, int* flags, const float* wl_a, const float* wut_a, int lr_a, int ur_a,
+                    const float* wl_b, const float* wut_b, int lr_b, int ur_b);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 
@@ -993,6 +996,133 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         cudaStreamWaitEvent(st, ls.ev_panel, 0);
     }
     if (nblk > 1 && ls.ucol_own) {
+        cudaEventRecord(ls.ev_ucol, ls.ucol);
+        cudaStreamWaitEvent(st, ls.ev_ucol, 0);
+    }
+    return 0;
+}
+
+// The same factorization with the trailing updates of two consecutive steps applied
+// in one pass over the trailing matrix (K = 256), which halves the HBM traffic of the
+// update-bound first half of the LU.  Per pair of steps (k, k+1), k even:
+//   main stream:  L1(k): block column / row k+1 by step k (width-1 L, corner excluded);
+//                 L2(k): block columns / rows k+2, k+3 by steps k and k+1 (width-2 L,
+//                 corner (k+2, k+2) excluded), once the previous pair's rest is done;
+//   panel stream: corner (k+1, k+1) by step k, inverse k+1, first W21 tile of k+1;
+//                 then corner (k+2, k+2) by steps k and k+1, inverse k+2, first tile of k+2;
+//   tail stream:  the other W21 / U^T tiles of each panel;
+//   rest stream:  blocks >= k+4 by steps k and k+1, beside L1(k+2) and panel k+3.
+// Operand buffers rotate over four slots (step k uses slot k & 3): a slot is rewritten
+// by panel k+4, which follows L2(k+2), which waits for the rest of pair (k, k+1).
+// wl4: 4 [2][n][128] buffers (8 n 128 floats); wut4: the same plus the transposed
+// block inverses (8 n 128 + 256 n floats).
+int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
+                         float* wl4, float* wut4, int* flags) {
+    constexpr int NB = 128;
+    const int nblk = n / NB;
+    if (!ls.panel_tail || !ls.rest || !ls.ucol_own) return 1;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int rest_ctas = ls.reserve_sms > 0 ? std::max(1, nsm - ls.reserve_sms) : -std::max(1, ls.rest_tiles);
+    auto wlb = [&](int k) { return wl4 + (size_t)(k & 3) * 2 * n * NB; };
+    auto wutb = [&](int k) { return wut4 + (size_t)(k & 3) * 2 * n * NB; };
+    auto dTb = [&](int k) { return wut4 + (size_t)8 * n * NB + (size_t)k * 2 * NB * NB; };
+    cudaStream_t sp = ls.panel, sq = ls.panel_tail, sr = ls.rest;
+    cudaEvent_t ev_pan[2] = {ls.ev_panel, ls.ev_panel2};
+    if (ls.cluster_inverse >= 2) inv128_cluster_setup();
+    auto inverse = [&](int k) {
+        const int k0 = k * NB;
+        if (ls.cluster_inverse >= 2)
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse != 0, k0, A, invr, invi, dTb(k), flags);
+        else
+            BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
+    };
+    // panel k after the update that completed block column / row k (event ready; sp has
+    // waited for it): first W21 tile on sp, first U^T tile on sq, the rest on sq
+    auto panel = [&](int k, cudaEvent_t ready) -> bool {
+        const int k0 = k * NB, rem = n - k0 - NB;
+        auto w21_tiles = [&](cudaStream_t s, int t0, int count) {
+            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count);
+        };
+        auto tr_tiles = [&](cudaStream_t s, int t0, int count) {
+            const int c0 = t0 * NB, cols = std::min(rem - c0, count < 0 ? rem : count * NB);
+            if (cols <= 0) return;
+            float* wtr = wutb(k) + (size_t)c0 * NB;
+            BEM_LAUNCH(k_panel_transpose<<<dim3((cols + 31) / 32, NB / 32), dim3(32, 8), 0, s>>>(
+                cols, A, k0, k0 + NB + c0, wtr, wtr + (size_t)n * NB));
+        };
+        cudaStreamWaitEvent(sq, ready, 0);
+        tr_tiles(sq, 0, 1);
+        cudaEventRecord(ls.ev_t0, sq);
+        if (!w21_tiles(sp, 0, 1)) return false;
+        cudaStreamWaitEvent(sp, ls.ev_t0, 0);
+        cudaEventRecord(ls.ev_head, sp);
+        cudaStreamWaitEvent(sq, ls.ev_head, 0);
+        if (!w21_tiles(sq, 1, -1)) return false;
+        tr_tiles(sq, 1, -1);
+        cudaEventRecord(ev_pan[k & 1], sq);
+        if (k > 0) {
+            cudaStreamWaitEvent(ls.ucol, ev_pan[k & 1], 0);
+            if (!tc_ucol(ls.ucol, n, k0, A, dTb(k), ls.ucol_ctas, flags)) return false;
+        }
+        return true;
+    };
+    bool rest_used = false;
+    cudaEventRecord(ls.ev_cross, st);
+    cudaEventRecord(ls.ev_rest, st);
+    cudaStreamWaitEvent(sp, ls.ev_cross, 0);
+    inverse(0);
+    if (!panel(0, ls.ev_cross)) return 1;
+    for (int k = 0; k <= nblk - 2; k += 2) {
+        const bool pair = k + 1 <= nblk - 2;
+        const int mt = nblk - k - 1;
+        // step k on block column / row k+1
+        cudaStreamWaitEvent(st, ev_pan[k & 1], 0);
+        if (!tc_update_pair(st, n, A, (k + 1) * NB, (k + 1) * NB, mt, mt, 1, 1, 0, flags, wlb(k), wutb(k), 0, 0,
+                            nullptr, nullptr, 0, 0))
+            return 1;
+        cudaEventRecord(ls.ev_cross, st);
+        if (!tc_update_pair(sp, n, A, (k + 1) * NB, (k + 1) * NB, 1, 1, 0, 0, 0, flags, wlb(k), wutb(k), 0, 0,
+                            nullptr, nullptr, 0, 0))
+            return 1;
+        inverse(k + 1);
+        cudaStreamWaitEvent(sp, ls.ev_cross, 0);
+        if (!panel(k + 1, ls.ev_cross)) return 1;
+        if (!pair) break;
+        // steps k and k+1 on block columns / rows k+2, k+3
+        const int o = k + 2, nr = nblk - o, w = std::min(2, nr);
+        cudaStreamWaitEvent(st, ev_pan[(k + 1) & 1], 0);
+        cudaStreamWaitEvent(st, ls.ev_rest, 0);
+        if (!tc_update_pair(st, n, A, o * NB, o * NB, nr, nr, w, 1, 0, flags, wlb(k), wutb(k), NB, NB, wlb(k + 1),
+                            wutb(k + 1), 0, 0))
+            return 1;
+        cudaEventRecord(ls.ev_cross2, st);
+        cudaStreamWaitEvent(sp, ls.ev_rest, 0);
+        cudaStreamWaitEvent(sp, ev_pan[k & 1], 0);
+        if (!tc_update_pair(sp, n, A, o * NB, o * NB, 1, 1, 0, 0, 0, flags, wlb(k), wutb(k), NB, NB, wlb(k + 1),
+                            wutb(k + 1), 0, 0))
+            return 1;
+        inverse(o);
+        cudaStreamWaitEvent(sp, ls.ev_cross2, 0);
+        if (!panel(o, ls.ev_cross2)) return 1;
+        // steps k and k+1 on blocks >= k+4
+        if (nr > 2) {
+            cudaStreamWaitEvent(sr, ev_pan[(k + 1) & 1], 0);
+            if (!tc_update_pair(sr, n, A, (o + 2) * NB, (o + 2) * NB, nr - 2, nr - 2, 0, 0, rest_ctas, flags, wlb(k),
+                                wutb(k), 3 * NB, 3 * NB, wlb(k + 1), wutb(k + 1), 2 * NB, 2 * NB))
+                return 1;
+            cudaEventRecord(ls.ev_rest, sr);
+            rest_used = true;
+        }
+    }
+    // join every stream back into st: the last W21 stores, transforms and updates precede the solves
+    cudaEventRecord(ls.ev_cross, sp);
+    cudaStreamWaitEvent(st, ls.ev_cross, 0);
+    cudaEventRecord(ls.ev_cross2, sq);
+    cudaStreamWaitEvent(st, ls.ev_cross2, 0);
+    if (rest_used) cudaStreamWaitEvent(st, ls.ev_rest, 0);
+    if (nblk > 1) {
         cudaEventRecord(ls.ev_ucol, ls.ucol);
         cudaStreamWaitEvent(st, ls.ev_ucol, 0);
     }

@@ -150,19 +150,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 
 // Tile rectangle and destination of one k_tc_update launch.
 struct TcTiles {
-    int lr0, ur0, Mt, Nt, lshape, crow0, ccol0, mode, c2row0, c2col0;
+    int lr0, ur0, Mt, Nt, lw, lskip, crow0, ccol0, mode, c2row0, c2col0;
+    int npair, lr0b, ur0b;  // second operand pair (npair = 2): L rows from lr0b, U rows from ur0b
 };
 
 // Tiles (tm, tn), tm < Mt, tn < Nt, of the rectangle whose L rows start at lr0
-// (rows of mapLr / mapLi) and U rows at ur0 (rows of mapUr / mapUi).  mode 0:
-// the tile's -acc is reduce-added into mapCr / mapCi at rows crow0 + tm*128,
-// columns ccol0 + tn*128.  mode 1: +acc is stored there and at c2row0 + tm*128,
-// c2col0 + tn*128 of mapC2r / mapC2i.  mode 2: +acc is stored there only.
+// (rows of mapLr / mapLi) and U rows at ur0 (rows of mapUr / mapUi); lw > 0 keeps
+// only the L of width lw (tile columns < lw, then tile rows < lw), without its first
+// lskip tiles.  With npair = 2 the product also sums the second pair of operands
+// (mapL2*, rows from lr0b; mapU2*, rows from ur0b): K = 256, two elimination steps
+// applied in one pass over C.  mode 0: the tile's -acc is reduce-added into
+// mapCr / mapCi at rows crow0 + tm*128, columns ccol0 + tn*128.  mode 1: +acc is
+// stored there and at c2row0 + tm*128, c2col0 + tn*128 of mapC2r / mapC2i.  mode 2:
+// +acc is stored there only.
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_tc_update(const __grid_constant__ CUtensorMap mapLr, const __grid_constant__ CUtensorMap mapLi,
                 const __grid_constant__ CUtensorMap mapUr, const __grid_constant__ CUtensorMap mapUi,
                 const __grid_constant__ CUtensorMap mapCr, const __grid_constant__ CUtensorMap mapCi,
                 const __grid_constant__ CUtensorMap mapC2r, const __grid_constant__ CUtensorMap mapC2i,
+                const __grid_constant__ CUtensorMap mapL2r, const __grid_constant__ CUtensorMap mapL2i,
+                const __grid_constant__ CUtensorMap mapU2r, const __grid_constant__ CUtensorMap mapU2i,
                 const TcTiles a, int* gflags) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
@@ -176,19 +183,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + 3);
     const uint32_t tfull0 = smem_u32(bars + 6), tempty0 = smem_u32(bars + 8);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // rectangle: Mt x Nt tiles; L-shape: tile column 0 (Mt tiles) and tile row 0 (Nt - 1 more)
-    const int Mt = a.Mt, Nt = a.Nt;
-    // lshape 1: tile column 0 and tile row 0; lshape 2: the same without the corner tile
-    const int ntiles = a.lshape ? Mt + Nt - a.lshape : Mt * Nt;
+    // rectangle: Mt x Nt tiles; an L of width lw: tile columns < lw (Mt lw tiles), then
+    // tile rows < lw right of them (lw (Nt - lw) tiles), the first lskip tiles dropped
+    const int Mt = a.Mt, Nt = a.Nt, lw = a.lw;
+    const int ncol = Mt * lw, nrow = lw * max(Nt - lw, 0);
+    const int ntiles = lw ? ncol + nrow - a.lskip : Mt * Nt;
     auto tile_of = [&](int t, int& tm, int& tn) {
-        if (a.lshape) {
-            t += a.lshape - 1;
-            tm = t < Mt ? t : 0;
-            tn = t < Mt ? 0 : t - Mt + 1;
+        if (lw) {
+            t += a.lskip;
+            if (t < ncol) {
+                tm = t / lw; tn = t % lw;
+            } else {
+                t -= ncol;
+                tm = t / (Nt - lw); tn = lw + t % (Nt - lw);
+            }
         } else {
             tm = t / Nt; tn = t % Nt;
         }
     };
+    const int KBT = KB * a.npair;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) { mbar_init(full0 + 8 * s, 1); mbar_init(empty0 + 8 * s, 1); }
@@ -198,6 +211,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         prefetch_map(&mapLr); prefetch_map(&mapLi); prefetch_map(&mapUr); prefetch_map(&mapUi);
         prefetch_map(&mapCr); prefetch_map(&mapCi);
         if (a.mode == 1) { prefetch_map(&mapC2r); prefetch_map(&mapC2i); }
+        if (a.npair == 2) { prefetch_map(&mapL2r); prefetch_map(&mapL2i); prefetch_map(&mapU2r); prefetch_map(&mapU2i); }
     }
     __syncwarp();
     if (warp == 0) {
@@ -218,16 +232,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 int tm, tn;
                 tile_of(t, tm, tn);
-                const int lrow = a.lr0 + tm * BM, urow = a.ur0 + tn * BN;
-                for (int kb = 0; kb < KB; ++kb, ++it) {
+                for (int kb = 0; kb < KBT; ++kb, ++it) {
                     const uint32_t s = it % STAGES, u = it / STAGES;
                     if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
                     const uint32_t st = base + s * STAGE_BYTES;
+                    const bool second = kb >= KB;
+                    const int x = (second ? kb - KB : kb) * BK;
+                    const int lrow = (second ? a.lr0b : a.lr0) + tm * BM, urow = (second ? a.ur0b : a.ur0) + tn * BN;
                     mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-                    tma_load_2d(st, &mapLr, kb * BK, lrow, full0 + 8 * s);
-                    tma_load_2d(st + L_TILE, &mapLi, kb * BK, lrow, full0 + 8 * s);
-                    tma_load_2d(st + 2 * L_TILE, &mapUr, kb * BK, urow, full0 + 8 * s);
-                    tma_load_2d(st + 2 * L_TILE + U_TILE, &mapUi, kb * BK, urow, full0 + 8 * s);
+                    tma_load_2d(st, second ? &mapL2r : &mapLr, x, lrow, full0 + 8 * s);
+                    tma_load_2d(st + L_TILE, second ? &mapL2i : &mapLi, x, lrow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE, second ? &mapU2r : &mapUr, x, urow, full0 + 8 * s);
+                    tma_load_2d(st + 2 * L_TILE + U_TILE, second ? &mapU2i : &mapUi, x, urow, full0 + 8 * s);
                 }
             }
         }
@@ -242,7 +258,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (u > 0 && !mbar_wait(tempty0 + 8 * buf, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t accR = tmem + buf * 256, accI = accR + 128;
-                for (int kb = 0; kb < KB; ++kb, ++it) {
+                for (int kb = 0; kb < KBT; ++kb, ++it) {
                     const uint32_t s = it % STAGES, su = it / STAGES;
                     if (!mbar_wait(full0 + 8 * s, su & 1, abort_flag, gflags)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -416,9 +432,10 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
         return false;
     const int ntiles = lshape ? Mt + Nt - lshape : Mt * Nt;
     if (ntiles <= 0) return true;
-    const TcTiles a{lr0, ur0, Mt, Nt, lshape, k0 + 128 + lr0, k0 + 128 + ur0, 0, 0, 0};
-    BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi,
-                                                                                   mCr, mCi, a, flags));
+    const TcTiles a{lr0, ur0, Mt, Nt, lshape ? 1 : 0, lshape == 2 ? 1 : 0, k0 + 128 + lr0, k0 + 128 + ur0, 0, 0, 0,
+                    1, 0, 0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(
+        mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mLr, mLi, mUr, mUi, a, flags));
     return true;
 }
 
@@ -441,9 +458,9 @@ bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, floa
         return false;
     const int mt = std::min(rem / 128 - t0, count < 0 ? rem / 128 : count);
     if (t0 < 0 || mt <= 0) return true;
-    const TcTiles a{k0 + 128 + 128 * t0, 0, mt, 1, 0, 128 * t0, 0, 1, k0 + 128 + 128 * t0, k0};
-    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, 0), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i, a,
-                                                                        flags));
+    const TcTiles a{k0 + 128 + 128 * t0, 0, mt, 1, 0, 0, 128 * t0, 0, 1, k0 + 128 + 128 * t0, k0, 1, 0, 0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, 0), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i,
+                                                                        mLr, mLi, mUr, mUi, a, flags));
     return true;
 }
 
@@ -459,9 +476,46 @@ bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int
         !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
         return false;
     const int mt = c0 / 128;
-    const TcTiles a{0, 0, mt, 1, 0, 0, c0, 2, 0, 0};
-    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, max_ctas), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, a,
-                                                                        flags));
+    const TcTiles a{0, 0, mt, 1, 0, 0, 0, c0, 2, 0, 0, 1, 0, 0};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(mt, max_ctas), NTHREADS, SMEM_BYTES, st>>>(
+        mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mLr, mLi, mUr, mUi, a, flags));
+    return true;
+}
+
+// C -= W_a U_a [+ W_b U_b] over tiles of the Mt x Nt block rectangle whose first element
+// is A[row0][col0] (both multiples of 128): W_a rows (of wl_a, [2][n][128]) start at
+// lr_a for the rectangle's first row, U_a^T rows (of wut_a) at ur_a for its first
+// column, and likewise for the optional second step b (wl_b != nullptr: K = 256, both
+// steps applied in one pass over C).  lw > 0: only the L of width lw, first lskip tiles
+// dropped (see k_tc_update).
+bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
+                    int max_ctas, int* flags, const float* wl_a, const float* wut_a, int lr_a, int ur_a,
+                    const float* wl_b, const float* wut_b, int lr_b, int ur_b) {
+    if (Mt <= 0 || Nt <= 0) return true;
+    if (n % 128 || row0 % 128 || col0 % 128 || lr_a % 128 || ur_a % 128 || A.ld % 4) return false;
+    if (row0 + 128 * Mt > n || col0 + 128 * Nt > n || lr_a < 0 || ur_a < 0) return false;
+    if (lr_a + 128 * Mt > n || ur_a + 128 * Nt > n) return false;
+    if (wl_b && (lr_b % 128 || ur_b % 128 || lr_b < 0 || ur_b < 0 || lr_b + 128 * Mt > n || ur_b + 128 * Nt > n))
+        return false;
+    const int ntiles = lw ? Mt * lw + lw * std::max(Nt - lw, 0) - lskip : Mt * Nt;
+    if (ntiles <= 0) return true;
+    CUtensorMap mLr, mLi, mUr, mUi, mCr, mCi, mL2r, mL2i, mU2r, mU2i;
+    const size_t plane = (size_t)n * 128;
+    if (!make_map(&mLr, wl_a, n, 128, BM) || !make_map(&mLi, wl_a + plane, n, 128, BM) ||
+        !make_map(&mUr, wut_a, n, 128, BN) || !make_map(&mUi, wut_a + plane, n, 128, BN) ||
+        !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
+        return false;
+    const int npair = wl_b ? 2 : 1;
+    if (wl_b) {
+        if (!make_map(&mL2r, wl_b, n, 128, BM) || !make_map(&mL2i, wl_b + plane, n, 128, BM) ||
+            !make_map(&mU2r, wut_b, n, 128, BN) || !make_map(&mU2i, wut_b + plane, n, 128, BN))
+            return false;
+    } else {
+        mL2r = mLr; mL2i = mLi; mU2r = mUr; mU2i = mUi;
+    }
+    const TcTiles a{lr_a, ur_a, Mt, Nt, lw, lskip, row0, col0, 0, 0, 0, npair, lr_b, ur_b};
+    BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(
+        mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mL2r, mL2i, mU2r, mU2i, a, flags));
     return true;
 }
 

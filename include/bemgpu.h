@@ -267,6 +267,9 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     backward solve's operator) runs on its own stream (default),
  *                     0: on the panel stream behind each W21.
  *   "lu_ucol_ctas"    CTAs of each such transform (0 = one per 128 x 128 tile).
+ *   "lu_pair_update"  1: the trailing updates of two elimination steps are applied in
+ *                     one pass over the trailing matrix (K = 256; default), 0: one step
+ *                     per pass.
  *   "refine_gmres"    refinement of the mixed path, all stopping at the same residual
  *                     test: 0 classic x <- x + LU^-1 (y - D x); 1 flexible GMRES
  *                     (restart 16) with the TF32 factors as preconditioner, which never
@@ -281,7 +284,7 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
- *                     LU when it overlaps it (default 24).
+ *                     LU when it overlaps it (default 72).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
