@@ -53,6 +53,13 @@ extern "C" bem_status bem_batch_solve(int device, int n_bodies, const bem_mesh* 
         }
         s = bem_set_params(ctx, density, gravity, n_beta, betas);
         if (s != BEM_OK) record(s, bem_last_error(ctx));
+        // The default share of SMs kept free of a context's assembly suits one pipeline
+        // on the GPU; with several, the other contexts' work fills those SMs anyway, and
+        // a smaller reserve measured faster (24 SMs).
+        if (s == BEM_OK && n_workers > 1) {
+            s = bem_set_tuning(ctx, "asm_reserve_sms", 24);
+            if (s != BEM_OK) record(s, bem_last_error(ctx));
+        }
         while (s == BEM_OK) {
             const int k = next.fetch_add(1);
             if (k >= n_bodies) break;
