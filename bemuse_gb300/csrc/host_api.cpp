@@ -1096,7 +1096,9 @@ bem_status ensure_slot(bem_ctx* ctx, FreqState& F, bool mixed) {
 // Right-hand sides and operator of one frequency into slot F, on stream st:
 // incident wave, S*B (static Rankine part, wave part), D (FP64, or for the
 // mixed path the FP32 copy plus Re D as float pairs and the plane-wave factors).
-bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStream_t st) {
+// overlapped: the assembly runs beside an earlier frequency's LU and solves, so it
+// keeps off the SMs reserved for them; otherwise it uses the whole GPU.
+bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStream_t st, bool overlapped = false) {
     const int N = ctx->N, Np = ctx->Np, NB = ctx->NB, R = ctx->R;
     const double K = Om * Om / 9.81;  // Kappa uses the global Gravity (Hydrodynamic_Solver.cpp:409)
     F.Om = Om;
@@ -1132,8 +1134,8 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         a.D64i = nullptr;
         a.row_ctr = ctx->d_wctr;
         a.sm_ctr = ctx->d_wctr + 1;
-        a.reserve = ctx->asm_overlap ? ctx->asm_reserve : 0;
-        a.per_sm = ctx->asm_overlap ? ctx->asm_per_sm : 3;
+        a.reserve = overlapped && ctx->asm_overlap ? ctx->asm_reserve : 0;
+        a.per_sm = overlapped && ctx->asm_overlap ? ctx->asm_per_sm : 3;
     }
     CK(cudaEventRecord(F.ev_t[2], st));
     bem::launch_wave(st, a, mixed);
@@ -1210,7 +1212,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     auto enqueue_assembly = [&](int f) -> bem_status {
         FreqState& F = slot(f);
         if (pipe) CK(cudaStreamWaitEvent(sa, F.ev_free, 0));
-        return assemble(ctx, F, omega[f], mixed, sa);
+        return assemble(ctx, F, omega[f], mixed, sa, f > 0);
     };
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
