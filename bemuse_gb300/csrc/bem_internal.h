@@ -67,6 +67,7 @@ struct WaveArgs {
     int* row_ctr;
     int* sm_ctr;
     int reserve, per_sm;
+    int split;            // source ranges per receiver row (work items); 0: WAVE_SPLIT
     // FP32 constants of the mixed kernel, computed on the host so that no FP64 instruction
     // (slow on this GPU) can be rematerialised inside its inner loop: K = kh + kl,
     // c1 = K / (4 pi), c2 = K^2 / (4 pi), live = (K != 0)

@@ -135,6 +135,7 @@ struct bem_ctx {
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
     int asm_overlap = 1, asm_reserve = 72, asm_per_sm = 3;
+    int asm_split = bem::WAVE_SPLIT;            // work items per receiver row of the assembly kernel
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
@@ -1136,6 +1137,7 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         a.sm_ctr = ctx->d_wctr + 1;
         a.reserve = overlapped && ctx->asm_overlap ? ctx->asm_reserve : 0;
         a.per_sm = overlapped && ctx->asm_overlap ? ctx->asm_per_sm : 3;
+        a.split = ctx->asm_split;
     }
     CK(cudaEventRecord(F.ev_t[2], st));
     bem::launch_wave(st, a, mixed);
@@ -1690,6 +1692,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "asm_overlap") {
         if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "asm_overlap must be 0 or 1");
         ctx->asm_overlap = (int)value;
+        return BEM_OK;
+    }
+    if (k == "asm_split") {
+        if (!(value >= 1 && value <= 64)) return fail(ctx, BEM_ERR_ARG, "asm_split must be in [1, 64]");
+        ctx->asm_split = (int)value;
         return BEM_OK;
     }
     if (k == "asm_reserve_sms") {

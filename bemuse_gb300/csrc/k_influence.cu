@@ -232,15 +232,16 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     }
     __syncthreads();
     if (!s_admit) return;
-    // work item = one receiver row x one of WAVE_SPLIT source ranges, so the last items
+    // work item = one receiver row x one of a.split source ranges, so the last items
     // are short and the tail of the launch leaves few SMs idle
-    const int chunk = ((a.N + WAVE_SPLIT - 1) / WAVE_SPLIT + 31) & ~31;
+    const int split = a.split > 0 ? a.split : WAVE_SPLIT;
+    const int chunk = ((a.N + split - 1) / split + 31) & ~31;
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.row_ctr, 1);
         item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= a.N * WAVE_SPLIT) break;
-        const int r = item / WAVE_SPLIT, s_begin = (item % WAVE_SPLIT) * chunk;
+        if (item >= a.N * split) break;
+        const int r = item / split, s_begin = (item % split) * chunk;
         const int s_end = min(a.N, s_begin + chunk);
         const int N = a.N, R = a.R;
         const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
@@ -257,19 +258,28 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         const size_t fs = (size_t)4 * N;
         for (int s = s_begin + lane; s < s_end; s += 32) {
             float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
-            const int nq = live ? a.nq[s] : 0;
+            // the pair's Rankine float pairs come from HBM: issued first, so that their latency
+            // overlaps the Green-function arithmetic below
+            float rdh = 0.f, rdl = 0.f, rsh = 0.f, rsl = 0.f;
+            if (a.mode != 1) {
+                rdh = __ldcs(a.RDhi + row + s); rdl = __ldcs(a.RDlo + row + s);
+                rsh = __ldcs(a.RSRhi + row + s); rsl = __ldcs(a.RSRlo + row + s);
+            }
+            const int nq = live ? __ldg(a.nq + s) : 0;
     #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (q < nq) {
                     const float* g = a.gq32 + (size_t)q * N + s;
                     // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
-                    const float gx = g[0], gy = g[fs];
+                    // source data is read by every row: read-only path
+                    const float gx = __ldg(g), gy = __ldg(g + fs);
                     const float sx = xh - gx, sy = yh - gy;
                     float bx = sx - xh, by = sy - yh;
-                    const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - g[7 * fs]);
-                    const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - g[8 * fs]);
-                    float dz = (zh - g[2 * fs]) + (zl - g[9 * fs]);
-                    float w = g[3 * fs], nx = g[4 * fs], ny = g[5 * fs], nz = g[6 * fs];
+                    const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - __ldg(g + 7 * fs));
+                    const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - __ldg(g + 8 * fs));
+                    float dz = (zh - __ldg(g + 2 * fs)) + (zl - __ldg(g + 9 * fs));
+                    float w = __ldg(g + 3 * fs), nx = __ldg(g + 4 * fs), ny = __ldg(g + 5 * fs),
+                          nz = __ldg(g + 6 * fs);
                     float XX = (sx + lx) * K, YY = (sy + ly) * K, VV = dz * K;
                     float hh, hl;
                     df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
@@ -301,8 +311,6 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
             }
             // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
             // FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
-            const float rdh = a.RDhi[row + s], rdl = a.RDlo[row + s];
-            const float rsh = a.RSRhi[row + s], rsl = a.RSRlo[row + s];
             const float ph = Kh * rsh;
             const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
             const float sh = rdh + ph;
@@ -321,8 +329,8 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     #pragma unroll
             for (int j = 0; j < MAX_RHS; ++j) {
                 if (j < R) {
-                    acc_re[j] = fmaf(-wsr, b[2 * j], acc_re[j]);
-                    acc_im[j] = fmaf(-wsr, b[2 * j + 1], acc_im[j]);
+                    acc_re[j] = fmaf(-wsr, __ldg(b + 2 * j), acc_re[j]);
+                    acc_im[j] = fmaf(-wsr, __ldg(b + 2 * j + 1), acc_im[j]);
                 }
             }
         }

@@ -285,7 +285,9 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     the solves only.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
  *                     LU when it overlaps it (default 72).
- *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3). */
+ *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
+ *   "asm_split"       work items per receiver row of the persistent assembly kernel
+ *                     (1..64, default 4; finer items measured slower). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
