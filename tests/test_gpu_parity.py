@@ -143,6 +143,30 @@ def test_refinement_variants_agree_near_irregular_frequency(bg, orc):
     assert np.all(got[2]["iters"] <= got[0]["iters"] + 1)
 
 
+def test_lu_schedule_variants_agree(bg):
+    # 1200 panels: the TF32 LU has 10 block steps, so the paired schedule runs four full
+    # pairs and a final single step.  Every schedule / inverse variant must meet the
+    # refinement test and agree with the plain FP64 GPU solve (itself pinned to the
+    # oracle above) to the mixed-path tolerance.
+    mesh = bg.Half_Cylinder(10.0, 20.0, 40, 6, 24, 0, False)
+    om = np.array([0.6, 1.4])
+    ref = _solver(bg, mesh).solve_omegas(om)
+    s = _solver(bg, mesh, precision=bg.MIXED)
+    variants = [
+        # (two steps per pass, CTAs per inverse, blocked inverse, split panel)
+        (1, 4, 1, 1), (0, 4, 1, 1), (1, 2, 0, 1), (1, 8, 1, 1), (1, 1, 0, 1), (1, 4, 1, 0), (0, 2, 1, 0),
+    ]
+    for pair, cl, blk, split in variants:
+        s.set_tuning("lu_pair_update", pair)
+        s.set_tuning("lu_cluster_inverse", cl)
+        s.set_tuning("lu_block_inverse", blk)
+        s.set_tuning("lu_split_panel", split)
+        got = s.solve_omegas(om)
+        print((pair, cl, blk, split), "iterations", got["iters"], "residual", got["residual"].max())
+        assert np.all(got["residual"] <= 1e-12)
+        _compare(got, ref, 1e-6, keys=("A", "B", "F"))
+
+
 def test_plain_fp64_solve_matches_oracle_array(bg, orc):
     c = cases.ARRAY_SMALL
     om, _ = orc.cylinder(c["R"], c["draft"], c["NA"], c["NR"], c["NV"], cosine=False)
