@@ -478,9 +478,10 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
 // P = 8p .. 8p + 7) belongs to the CTA owning those rows, which
 //   1. inverts the 8 x 8 pivot block D = M[P][P] in one warp (in-place Gauss-Jordan,
 //      the p + 1 substitution, shuffles only): X = D^-1;
-//   2. forms the panel row R = X M[P][:] with R[:, P] = X (8 x 128) and writes it into
-//      its own shared memory and, by st.async, into every peer's (one mbarrier per
-//      panel, 8 KB);
+//   2. forms the panel row R = X M[P][:] with R[:, P] = X (8 x 128; a warp reads the
+//      staged rows as contiguous 16-byte words) in its own shared memory and sends it to
+//      every peer as one 8 KB bulk copy (cp.async.bulk, shared::cta -> shared::cluster),
+//      completing one mbarrier per panel there;
 // then every CTA updates its other rows i: M[i][j] <- M[i][j] [j not in P] - M[i][P] R[:, j]
 // and the owner copies R into rows P.  This is the composition of the 8 single-pivot
 // steps.  Waits on a peer give up at a 2 s deadline (FLAG_TIMEOUT); every CTA always
@@ -592,45 +593,52 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
             }
             __syncthreads();
             {
-                // R[i][c0 .. c0 + 3] for i = t / 32, c0 = 4 (t % 32); R[:, P] = X
-                const int i = t >> 5, c0 = 4 * (t & 31);
-                float2 r[4];
+                // R[i0 + ii][c0 + cc] (ii, cc < 2) for c0 = 2 (t % 64), i0 = 2 (t / 64); R[:, P] = X.
+                // A warp reads each staged pivot row as contiguous 16-byte words (no bank conflicts).
+                const int c0 = 2 * (t & 63), i0 = 2 * (t >> 6);
+                float2 r[2][2];
                 if ((c0 >> 3) == p) {
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) r[c] = xblk[i * 8 + (c0 & 7) + c];
+                    for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+                        for (int cc = 0; cc < 2; ++cc) r[ii][cc] = xblk[(i0 + ii) * 8 + (c0 & 7) + cc];
                 } else {
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) r[c] = make_float2(0.f, 0.f);
+                    for (int ii = 0; ii < 2; ++ii) { r[ii][0] = make_float2(0.f, 0.f); r[ii][1] = make_float2(0.f, 0.f); }
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const float2 x = xblk[i * 8 + j];
+                        const float4 y = *reinterpret_cast<const float4*>(prow + j * 128 + c0);
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const float2 y = prow[j * 128 + c0 + c];
-                            r[c].x = fmaf(x.x, y.x, fmaf(-x.y, y.y, r[c].x));
-                            r[c].y = fmaf(x.x, y.y, fmaf(x.y, y.x, r[c].y));
+                        for (int ii = 0; ii < 2; ++ii) {
+                            const float2 x = xblk[(i0 + ii) * 8 + j];
+                            r[ii][0].x = fmaf(x.x, y.x, fmaf(-x.y, y.y, r[ii][0].x));
+                            r[ii][0].y = fmaf(x.x, y.y, fmaf(x.y, y.x, r[ii][0].y));
+                            r[ii][1].x = fmaf(x.x, y.z, fmaf(-x.y, y.w, r[ii][1].x));
+                            r[ii][1].y = fmaf(x.x, y.w, fmaf(x.y, y.z, r[ii][1].y));
                         }
                     }
                 }
-                const int row = 8 * p + i, qq = (c0 & 7) >> 1, cgc = c0 >> 3;
+                const int qq = (c0 & 7) >> 1, cgc = c0 >> 3;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const float4 w = make_float4(r[2 * h].x, r[2 * h].y, r[2 * h + 1].x, r[2 * h + 1].y);
-                    const int idx = row * 64 + (qq + h) * 16 + cgc;
-                    nrow[idx] = w;
-#pragma unroll
-                    for (int pp = 1; pp < CL; ++pp) {
-                        const uint32_t peer = (rank + (uint32_t)pp) % CL;
-                        const uint32_t dst = ic_peer_addr(nrow_s + 16u * (uint32_t)idx, peer);
-                        const uint32_t bar = ic_peer_addr(bars_s + 8u * (uint32_t)p, peer);
-                        asm volatile(
-                            "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, "
-                            "[%5];" ::"r"(dst), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w), "r"(bar)
-                            : "memory");
-                    }
-                }
+                for (int ii = 0; ii < 2; ++ii)
+                    nrow[(8 * p + i0 + ii) * 64 + qq * 16 + cgc] =
+                        make_float4(r[ii][0].x, r[ii][0].y, r[ii][1].x, r[ii][1].y);
+                // the panel row goes to the peers as one 8 KB bulk copy each (async proxy)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             }
             __syncthreads();
+            if (t == 0) {
+                const uint32_t src = nrow_s + 16u * (uint32_t)(8 * p * 64);
+#pragma unroll
+                for (int pp = 1; pp < CL; ++pp) {
+                    const uint32_t peer = (rank + (uint32_t)pp) % CL;
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], 8192, [%2];"
+                        ::"r"(ic_peer_addr(src, peer)), "r"(src), "r"(ic_peer_addr(bars_s + 8u * (uint32_t)p, peer))
+                        : "memory");
+                }
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
         } else {
             if (t == 0 && !dead && !ic_wait(bars_s + 8 * p, deadline)) dead = true;
             __syncthreads();
@@ -682,6 +690,9 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
         *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
         *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
     }
+    // the bulk copies out of the panel rows have read their sources before the shared
+    // memory is reused or released
+    if (t == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     if (dT) {
         // the transpose, [2][128][128], TF32-rounded: the K-major B operand of W21 = A21 D^-1.
         // Staged through the (now free) panel-row buffer as [2][128 columns][RPC + 4 rows] so
