@@ -138,7 +138,8 @@ struct LuStreams {
     int ucol_ctas;          // CTAs per U-column transform (0: one per tile)
     cudaStream_t panel_tail;  // optional: W21 / transpose tiles beyond the first, off the inverse chain
     cudaEvent_t ev_head, ev_t0;
-    int block_inverse;      // cluster inverse taken 8 pivots at a time (k_inv128b), 0: one at a time
+    int block_inverse;      // cluster inverse: 0 one pivot at a time (k_inv128c), 1 eight at a time
+                            // (k_inv128b), 2 eight at a time with the next pivot block ahead (k_inv128l)
     cudaStream_t rest;      // paired schedule: trailing updates of two steps at a time
     cudaEvent_t ev_panel2, ev_cross2;
 };

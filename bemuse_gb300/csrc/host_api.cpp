@@ -126,11 +126,11 @@ struct bem_ctx {
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
-    int lu_cluster_inverse = 4;                 // CTAs per block inverse (2, 4, 8: a cluster; 1: one CTA)
+    int lu_cluster_inverse = 8;                 // CTAs per block inverse (2, 4, 8: a cluster; 1: one CTA)
     int lu_ucol_stream = 1;                     // U D^-1 transforms on their own stream (0: panel stream)
     int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
     int lu_split_panel = 1;                     // panel tiles beyond the first on their own stream
-    int lu_block_inverse = 1;                   // cluster inverse in panels of 8 pivots
+    int lu_block_inverse = 2;                   // cluster inverse in panels of 8 pivots, next pivot block ahead
     int lu_pair_update = 1;                     // trailing updates of two steps per pass
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
@@ -1680,7 +1680,8 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "lu_block_inverse") {
-        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_block_inverse must be 0 or 1");
+        if (!(value == 0 || value == 1 || value == 2))
+            return fail(ctx, BEM_ERR_ARG, "lu_block_inverse must be 0, 1 or 2");
         ctx->lu_block_inverse = (int)value;
         return BEM_OK;
     }

@@ -719,13 +719,318 @@ __global__ void __launch_bounds__(IC_THREADS, 1)
     ic_cluster_sync();  // no CTA leaves while another may still address its shared memory
 }
 
+// The blocked cluster inverse with the next panel's chain taken ahead of the bulk of each
+// rank-8 update.  The CTA has a ninth warp (the pivot warp) that holds no rows.  For panel
+// q the owner of panel q+1 first applies R_q to its 8 pivot rows of q+1 and stages their
+// 8 x 8 pivot block and 8 x 128 panel rows; then the pivot warp inverts that block while
+// the 256 row threads apply R_q to every other row; then the row threads form R_{q+1}
+// and send it.  The chain per panel is the pivot-row update, the 8 x 8 inverse and the
+// panel row; the bulk update runs beside the inverse.  Same arithmetic as k_inv128b.
+constexpr int IL_THREADS = IC_THREADS + 32;
+constexpr int IL_SMEM = 128 * 64 * 16       // panel rows R, [128][4][16] float4
+                        + 2 * 64 * 8 * 8    // M[i][P] of this CTA's rows, two buffers [2][<= 64][8] float2
+                        + 8 * 128 * 8       // staged pivot rows of the next panel, [8][128] float2
+                        + 64 * 8            // X, [8][8] float2
+                        + 64 * 8            // next pivot block, [8][8] float2
+                        + 16 * 8;           // one mbarrier per panel
+
+template <int CL>
+__global__ void __launch_bounds__(IL_THREADS, 1)
+    k_inv128l(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    constexpr int RPC = 128 / CL, RPT = RPC / 16;
+    static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
+    extern __shared__ __align__(16) float4 il_smem[];
+    float4* nrow = il_smem;                                              // [128][4][16]
+    float2* ccol = reinterpret_cast<float2*>(nrow + 128 * 64);           // [2][64][8]
+    float2* prow = ccol + 2 * 64 * 8;                                    // [8][128]
+    float2* xblk = prow + 8 * 128;                                       // [8][8]
+    float2* dblk = xblk + 64;                                            // [8][8]
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(dblk + 64);  // [16]
+    const uint32_t rank = ic_rank();
+    const int t = threadIdx.x, cg = t & 15, rg = (t >> 4) & 15, warp = t >> 5, lane = t & 31;
+    const bool rowthr = t < IC_THREADS;  // warp 8 is the pivot warp
+    const uint32_t nrow_s = (uint32_t)__cvta_generic_to_shared(nrow);
+    const uint32_t bars_s = (uint32_t)__cvta_generic_to_shared(bars);
+    float2 v[RPT][8];
+    const int row_base = RPC * (int)rank + RPT * rg;
+    if (rowthr) {
+#pragma unroll
+        for (int m = 0; m < RPT; ++m) {
+            const size_t g = (size_t)(k0 + row_base + m) * A.ld + k0 + 8 * cg;
+            const float4 r0 = *reinterpret_cast<const float4*>(A.re + g);
+            const float4 r1 = *reinterpret_cast<const float4*>(A.re + g + 4);
+            const float4 i0 = *reinterpret_cast<const float4*>(A.im + g);
+            const float4 i1 = *reinterpret_cast<const float4*>(A.im + g + 4);
+            v[m][0] = make_float2(r0.x, i0.x); v[m][1] = make_float2(r0.y, i0.y);
+            v[m][2] = make_float2(r0.z, i0.z); v[m][3] = make_float2(r0.w, i0.w);
+            v[m][4] = make_float2(r1.x, i1.x); v[m][5] = make_float2(r1.y, i1.y);
+            v[m][6] = make_float2(r1.z, i1.z); v[m][7] = make_float2(r1.w, i1.w);
+        }
+    }
+    if (t < 16) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars_s + 8 * t) : "memory");
+        if ((8 * t) / RPC != (int)rank)
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], 8192;" ::"r"(bars_s + 8 * t)
+                         : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ic_cluster_sync();
+    unsigned long long deadline;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(deadline));
+    deadline += 2000000000ull;
+    int lf = 0;
+    bool dead = false;
+    auto owns = [&](int q) { return (8 * q) / RPC == (int)rank; };
+    // rows (local index RPT rg + m - 8 q + RPC rank) of panel q held by this thread
+    auto in_panel = [&](int q, int m) {
+        const int li = RPT * rg + m - (8 * q - RPC * (int)rank);
+        return li >= 0 && li < 8;
+    };
+    // this thread's M[i][P_q] into ccol buffer q & 1 (threads of column group q)
+    auto put_ccol = [&](int q) {
+        if (rowthr && cg == q) {
+#pragma unroll
+            for (int m = 0; m < RPT; ++m)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) ccol[((q & 1) * 64 + RPT * rg + m) * 8 + j] = v[m][j];
+        }
+    };
+    // the owner's pivot rows of panel q into prow, their 8 x 8 pivot block into dblk
+    auto stage = [&](int q) {
+        if (rowthr) {
+#pragma unroll
+            for (int m = 0; m < RPT; ++m) {
+                if (!in_panel(q, m)) continue;
+                const int li = RPT * rg + m - (8 * q - RPC * (int)rank);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) prow[li * 128 + 8 * cg + c] = v[m][c];
+                if (cg == q) {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) dblk[li * 8 + c] = v[m][c];
+                }
+            }
+        }
+    };
+    // X = D^-1 of the staged pivot block (pivot warp; lane (i, c) = (lane / 4, lane % 4)
+    // holds D[i][c] and D[i][c + 4]; in-place Gauss-Jordan with the p + 1 substitution)
+    auto pivot_inverse = [&]() {
+        const int i = lane >> 2, q = lane & 3;
+        float2 a0 = dblk[i * 8 + q], a1 = dblk[i * 8 + q + 4];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int kc = k & 3;
+            const float2 s0 = k < 4 ? a0 : a1;
+            const float px = __shfl_sync(0xffffffffu, s0.x, k * 4 + kc);
+            const float py = __shfl_sync(0xffffffffu, s0.y, k * 4 + kc);
+            const float den = px * px + py * py;
+            if (lane == 0 && (!(den > 0.f) || !isfinite(den))) lf |= FLAG_ZERO_PIVOT;
+            const float rc = __frcp_rn(den), qr = px * rc, qi = -py * rc;
+            float2 n0 = make_float2(__shfl_sync(0xffffffffu, a0.x, k * 4 + q), __shfl_sync(0xffffffffu, a0.y, k * 4 + q));
+            float2 n1 = make_float2(__shfl_sync(0xffffffffu, a1.x, k * 4 + q), __shfl_sync(0xffffffffu, a1.y, k * 4 + q));
+            if (q == kc) {
+                if (k < 4) n0.x += 1.f;
+                else n1.x += 1.f;
+            }
+            const float2 m0 = make_float2(n0.x * qr - n0.y * qi, n0.x * qi + n0.y * qr);
+            const float2 m1 = make_float2(n1.x * qr - n1.y * qi, n1.x * qi + n1.y * qr);
+            float cx = __shfl_sync(0xffffffffu, s0.x, i * 4 + kc);
+            const float cy = __shfl_sync(0xffffffffu, s0.y, i * 4 + kc);
+            if (i == k) cx -= 1.f;
+            a0.x = fmaf(-cx, m0.x, fmaf(cy, m0.y, a0.x));
+            a0.y = fmaf(-cx, m0.y, fmaf(-cy, m0.x, a0.y));
+            a1.x = fmaf(-cx, m1.x, fmaf(cy, m1.y, a1.x));
+            a1.y = fmaf(-cx, m1.y, fmaf(-cy, m1.x, a1.y));
+        }
+        xblk[i * 8 + q] = a0;
+        xblk[i * 8 + q + 4] = a1;
+    };
+    // R_q = X prow with R[:, P_q] = X (row threads), into nrow; then one bulk copy per peer
+    auto form_and_send = [&](int q) {
+        if (rowthr) {
+            const int c0 = 2 * (t & 63), i0 = 2 * (t >> 6);
+            float2 r[2][2];
+            if ((c0 >> 3) == q) {
+#pragma unroll
+                for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) r[ii][cc] = xblk[(i0 + ii) * 8 + (c0 & 7) + cc];
+            } else {
+#pragma unroll
+                for (int ii = 0; ii < 2; ++ii) { r[ii][0] = make_float2(0.f, 0.f); r[ii][1] = make_float2(0.f, 0.f); }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float4 y = *reinterpret_cast<const float4*>(prow + j * 128 + c0);
+#pragma unroll
+                    for (int ii = 0; ii < 2; ++ii) {
+                        const float2 x = xblk[(i0 + ii) * 8 + j];
+                        r[ii][0].x = fmaf(x.x, y.x, fmaf(-x.y, y.y, r[ii][0].x));
+                        r[ii][0].y = fmaf(x.x, y.y, fmaf(x.y, y.x, r[ii][0].y));
+                        r[ii][1].x = fmaf(x.x, y.z, fmaf(-x.y, y.w, r[ii][1].x));
+                        r[ii][1].y = fmaf(x.x, y.w, fmaf(x.y, y.z, r[ii][1].y));
+                    }
+                }
+            }
+            const int qq = (c0 & 7) >> 1, cgc = c0 >> 3;
+#pragma unroll
+            for (int ii = 0; ii < 2; ++ii)
+                nrow[(8 * q + i0 + ii) * 64 + qq * 16 + cgc] = make_float4(r[ii][0].x, r[ii][0].y, r[ii][1].x, r[ii][1].y);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncthreads();
+        if (t == 0) {
+            const uint32_t src = nrow_s + 16u * (uint32_t)(8 * q * 64);
+#pragma unroll
+            for (int pp = 1; pp < CL; ++pp) {
+                const uint32_t peer = (rank + (uint32_t)pp) % CL;
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], 8192, [%2];"
+                    ::"r"(ic_peer_addr(src, peer)), "r"(src), "r"(ic_peer_addr(bars_s + 8u * (uint32_t)q, peer))
+                    : "memory");
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
+    };
+    // apply R_q to this thread's rows (rows of P_q become R_q; rows already done are skipped)
+    auto update = [&](int q, bool skip_next) {
+        if (!rowthr) return;
+#pragma unroll
+        for (int m = 0; m < RPT; ++m) {
+            if (skip_next && in_panel(q + 1, m)) continue;
+            const bool inP = owns(q) && in_panel(q, m);
+            const int li = RPT * rg + m - (8 * q - RPC * (int)rank);
+            float2 cm[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                cm[j] = inP ? make_float2(j == li ? -1.f : 0.f, 0.f) : ccol[((q & 1) * 64 + RPT * rg + m) * 8 + j];
+            if (inP || cg == q) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) v[m][c] = make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float2 rr[8];
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const float4 x = nrow[(8 * q + j) * 64 + qq * 16 + cg];
+                    rr[2 * qq] = make_float2(x.x, x.y);
+                    rr[2 * qq + 1] = make_float2(x.z, x.w);
+                }
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    v[m][c].x = fmaf(-cm[j].x, rr[c].x, fmaf(cm[j].y, rr[c].y, v[m][c].x));
+                    v[m][c].y = fmaf(-cm[j].x, rr[c].y, fmaf(-cm[j].y, rr[c].x, v[m][c].y));
+                }
+            }
+        }
+    };
+    // panel 0
+    put_ccol(0);
+    if (owns(0)) {
+        stage(0);
+        __syncthreads();
+        if (warp == 8) pivot_inverse();
+        __syncthreads();
+        form_and_send(0);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int q = 0; q < 16; ++q) {
+        if (!owns(q)) {
+            if (t == 0 && !dead && !ic_wait(bars_s + 8 * q, deadline)) dead = true;
+        }
+        __syncthreads();  // R_q in nrow (local or received); ccol buffer q & 1 complete
+        const bool next = q + 1 < 16, own_next = next && owns(q + 1);
+        if (own_next) {
+            // the pivot rows of panel q+1 first, then their block and panel rows
+            if (rowthr) {
+#pragma unroll
+                for (int m = 0; m < RPT; ++m) {
+                    if (!in_panel(q + 1, m)) continue;
+                    const bool inP = owns(q) && in_panel(q, m);  // never: panels are disjoint
+                    (void)inP;
+                    float2 cm[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) cm[j] = ccol[((q & 1) * 64 + RPT * rg + m) * 8 + j];
+                    if (cg == q) {
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) v[m][c] = make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        float2 rr[8];
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const float4 x = nrow[(8 * q + j) * 64 + qq * 16 + cg];
+                            rr[2 * qq] = make_float2(x.x, x.y);
+                            rr[2 * qq + 1] = make_float2(x.z, x.w);
+                        }
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            v[m][c].x = fmaf(-cm[j].x, rr[c].x, fmaf(cm[j].y, rr[c].y, v[m][c].x));
+                            v[m][c].y = fmaf(-cm[j].x, rr[c].y, fmaf(-cm[j].y, rr[c].x, v[m][c].y));
+                        }
+                    }
+                }
+            }
+            stage(q + 1);
+            __syncthreads();
+            if (warp == 8) pivot_inverse();
+        }
+        update(q, own_next);
+        if (next) put_ccol(q + 1);
+        __syncthreads();  // every row updated by R_q; X of panel q+1 ready
+        if (own_next) form_and_send(q + 1);
+    }
+    if (dead) lf |= FLAG_TIMEOUT;
+    // the bulk copies out of the panel rows have read their sources before the shared
+    // memory is reused or released
+    if (t == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    float* Or = invr + (size_t)(k0 / 128) * 128 * 128;
+    float* Oi = invi + (size_t)(k0 / 128) * 128 * 128;
+    if (rowthr) {
+#pragma unroll
+        for (int m = 0; m < RPT; ++m) {
+            const size_t g = (size_t)(row_base + m) * 128 + 8 * cg;
+            *reinterpret_cast<float4*>(Or + g) = make_float4(v[m][0].x, v[m][1].x, v[m][2].x, v[m][3].x);
+            *reinterpret_cast<float4*>(Or + g + 4) = make_float4(v[m][4].x, v[m][5].x, v[m][6].x, v[m][7].x);
+            *reinterpret_cast<float4*>(Oi + g) = make_float4(v[m][0].y, v[m][1].y, v[m][2].y, v[m][3].y);
+            *reinterpret_cast<float4*>(Oi + g + 4) = make_float4(v[m][4].y, v[m][5].y, v[m][6].y, v[m][7].y);
+        }
+    }
+    if (dT) {
+        // the transpose, TF32-rounded, staged through the panel-row buffer as in k_inv128b
+        constexpr int SL = RPC + 4;
+        float* stg = reinterpret_cast<float*>(nrow);
+        __syncthreads();
+        if (rowthr) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+#pragma unroll
+                for (int m = 0; m < RPT; ++m) {
+                    stg[(8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].x);
+                    stg[128 * SL + (8 * cg + c) * SL + RPT * rg + m] = tf32_rn(v[m][c].y);
+                }
+        }
+        __syncthreads();
+        constexpr int V = RPC / 4;
+        for (int idx = t; idx < 2 * 128 * V; idx += IL_THREADS) {
+            const int pl = idx / (128 * V), col = (idx / V) % 128, f = idx % V;
+            const float4 w = *reinterpret_cast<const float4*>(stg + pl * 128 * SL + col * SL + 4 * f);
+            *reinterpret_cast<float4*>(dT + pl * 16384 + col * 128 + RPC * (int)rank + 4 * f) = w;
+        }
+    }
+    if (lf) atomicOr(flags, lf);
+    ic_cluster_sync();  // no CTA leaves while another may still address its shared memory
+}
+
 // One cluster of cl CTAs (2, 4 or 8) inverting the diagonal block at k0.
-static void inv128_cluster(cudaStream_t st, int cl, bool blocked, int k0, CMat<float> A, float* invr, float* invi,
+static void inv128_cluster(cudaStream_t st, int cl, int blocked, int k0, CMat<float> A, float* invr, float* invi,
                            float* dT, int* flags) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
     cfg.blockDim = dim3(IC_THREADS);
-    cfg.dynamicSmemBytes = blocked ? IB_SMEM : IC_SMEM;
+    cfg.dynamicSmemBytes = blocked == 2 ? IL_SMEM : blocked ? IB_SMEM : IC_SMEM;
+    if (blocked == 2) cfg.blockDim = dim3(IL_THREADS);
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -734,6 +1039,14 @@ static void inv128_cluster(cudaStream_t st, int cl, bool blocked, int k0, CMat<f
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
+    if (blocked == 2) {
+        switch (cl) {
+            case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128l<2>, k0, A, invr, invi, dT, flags)); break;
+            case 4: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128l<4>, k0, A, invr, invi, dT, flags)); break;
+            default: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128l<8>, k0, A, invr, invi, dT, flags)); break;
+        }
+        return;
+    }
     if (blocked) {
         switch (cl) {
             case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128b<2>, k0, A, invr, invi, dT, flags)); break;
@@ -749,6 +1062,9 @@ static void inv128_cluster(cudaStream_t st, int cl, bool blocked, int k0, CMat<f
     }
 }
 static void inv128_cluster_setup() {
+    cudaFuncSetAttribute(k_inv128l<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, IL_SMEM);
+    cudaFuncSetAttribute(k_inv128l<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, IL_SMEM);
+    cudaFuncSetAttribute(k_inv128l<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, IL_SMEM);
     cudaFuncSetAttribute(k_inv128b<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
     cudaFuncSetAttribute(k_inv128b<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
     cudaFuncSetAttribute(k_inv128b<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, IB_SMEM);
@@ -924,7 +1240,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto inverse = [&](int k) {
         const int k0 = k * NB;
         if (ls.cluster_inverse >= 2)
-            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse != 0, k0, A, invr, invi, dTb(k), flags);
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
         mark(k - 1, 2, sp);
@@ -1045,7 +1361,7 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
     auto inverse = [&](int k) {
         const int k0 = k * NB;
         if (ls.cluster_inverse >= 2)
-            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse != 0, k0, A, invr, invi, dTb(k), flags);
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
     };

@@ -262,7 +262,7 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     the higher-priority panel stream as they retire.
  *   "lu_rest_tiles"   tiles per such short-lived CTA (default 4).
  *   "lu_cluster_inverse" CTAs per diagonal-block inverse: 2, 4 or 8 (a thread-block
- *                     cluster, rows split between the CTAs; default 4) or 1 (one CTA).
+ *                     cluster, rows split between the CTAs; default 8) or 1 (one CTA).
  *   "lu_ucol_stream"  1: the U D^-1 transform of each finished column block (the
  *                     backward solve's operator) runs on its own stream (default),
  *                     0: on the panel stream behind each W21.
@@ -275,8 +275,10 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     (restart 16) with the TF32 factors as preconditioner, which never
  *                     needs more preconditioner solves; 2 (default) classic sweeps while
  *                     each reduces the residual more than 20x, then GMRES from there.
- *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation
- *                     (default), 0: one pivot per synchronisation.
+ *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation,
+ *                     2 (default): the same with the next panel's pivot block inverted
+ *                     by a dedicated warp beside each rank-8 update, 0: one pivot per
+ *                     synchronisation.
  *   "lu_split_panel"  1: only the first tile of each panel's W21 and U transpose runs on
  *                     the inverse chain, the rest on a second panel stream (default);
  *                     0: the whole panel on the panel stream.

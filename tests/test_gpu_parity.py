@@ -155,6 +155,7 @@ def test_lu_schedule_variants_agree(bg):
     variants = [
         # (two steps per pass, CTAs per inverse, blocked inverse, split panel)
         (1, 4, 1, 1), (0, 4, 1, 1), (1, 2, 0, 1), (1, 8, 1, 1), (1, 1, 0, 1), (1, 4, 1, 0), (0, 2, 1, 0),
+        (1, 4, 2, 1), (1, 2, 2, 1), (1, 8, 2, 1), (0, 4, 2, 0),
     ]
     for pair, cl, blk, split in variants:
         s.set_tuning("lu_pair_update", pair)
