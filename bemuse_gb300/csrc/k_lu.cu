@@ -1712,7 +1712,8 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 // The lowest unfinished ticket therefore always progresses, whatever else runs
 // on the GPU.  The CTA that draws the last ticket resets the counter.
 // TS_SB sub-blocks of TS_RW rows per 128-row block; a CTA's 256 threads are TS_RW rows x
-// TS_SL column slices of TS_KC columns.
+// TS_SL column slices of TS_KC columns.  Three CTAs fit on an SM (80 registers): a chain
+// that shares the GPU with a persistent assembly kernel keeps more of its CTAs resident.
 constexpr int TS_NB = 128, TS_SB = 8, TS_RW = TS_NB / TS_SB, TS_THREADS = 256, TS_SL = TS_THREADS / TS_RW,
               TS_KC = TS_NB / TS_SL;
 
@@ -1756,7 +1757,7 @@ __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const 
 __host__ __device__ constexpr int ts_zstride(int R, int RC) { return ((2 * (TS_NB * R + RC)) + 3) & ~3; }
 
 template <int RC>
-__global__ void __launch_bounds__(TS_THREADS, 2) k_trsv_tk(int nblk, int R, CMat<float> A, int which,
+__global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int nblk, int R, CMat<float> A, int which,
                                                         float* Yin, float* Xout, int* xflag, int* ticket,
                                                         int epoch, int* gflags) {
     extern __shared__ __align__(16) float ts_smem[];
