@@ -101,6 +101,7 @@ def lib():
         "bem_kernel_times": ([vp, _dp, c_int], c_int),
         "bem_lu_timeline": ([vp, c_int, c_int, _dp, _ip], c_int),
         "bem_set_tuning": ([vp, ctypes.c_char_p, c_double], c_int),
+        "bem_autotune": ([vp, c_int, _dp, _dp, ctypes.c_char_p, c_int], c_int),
         "bem_mlp_num_params": ([], c_int),
         "bem_mlp_create": ([ctypes.POINTER(vp), c_int, ctypes.c_ulonglong], c_int),
         "bem_mlp_destroy": ([vp], None),
@@ -565,6 +566,18 @@ class Hydrodynamic_Radiation_Solver:
 
     def set_tuning(self, key, value):
         _check(lib().bem_set_tuning(self._h, key.encode(), float(value)), self._h)
+
+    def autotune(self, omegas):
+        """Times the mixed pipelined solve on the sample frequencies for a small grid of
+        schedule settings (bem_autotune) and keeps the fastest on this solver.  Returns
+        (ms per frequency of the chosen setting, one report line per setting)."""
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        ms = ctypes.c_double()
+        buf = ctypes.create_string_buffer(4096)
+        _check(lib().bem_autotune(self._h, int(om.size), om.ctypes.data_as(_dp), ctypes.byref(ms), buf, 4096),
+               self._h)
+        self.stage_times(reset=True)
+        return ms.value, buf.value.decode().splitlines()
 
     def lu_timeline(self, enable=-1):
         """Per block step of the last mixed LU: ms of [cross start, cross done, inverse done,

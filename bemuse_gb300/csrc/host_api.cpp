@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <chrono>
 #include <complex>
 #include <functional>
 #include <cstdio>
@@ -1711,6 +1712,67 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);
+}
+
+// Autotuner of the pipelined mixed solve over the schedule knobs of bem_set_tuning.
+bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* ms_per_freq, char* report,
+                        int report_len) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready || ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_autotune before bem_setup");
+    if (n_freq < 2 || !omega) return fail(ctx, BEM_ERR_ARG, "bem_autotune needs at least 2 sample frequencies");
+    struct Setting {
+        int asm_reserve, cluster, block, pair;
+    };
+    // the default first; the others move one knob at a time
+    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_cluster_inverse, ctx->lu_block_inverse, ctx->lu_pair_update},
+                            {56, 8, 2, 1}, {64, 8, 2, 1}, {80, 8, 2, 1}, {88, 8, 2, 1}, {72, 4, 1, 1}, {72, 8, 2, 0}};
+    const int ng = (int)(sizeof(grid) / sizeof(grid[0]));
+    std::vector<double> best(ng, 1e300);
+    auto apply = [&](const Setting& g) {
+        ctx->asm_reserve = g.asm_reserve;
+        ctx->lu_cluster_inverse = g.cluster;
+        ctx->lu_block_inverse = g.block;
+        ctx->lu_pair_update = g.pair;
+    };
+    bem_result none;
+    memset(&none, 0, sizeof(none));
+    // warm-up with the first setting (graph capture, buffers), then two timed rounds in
+    // alternation, so that a drift of the GPU's state affects every setting alike
+    apply(grid[0]);
+    bem_status s = bem_solve(ctx, std::min(n_freq, 2), omega, BEM_MIXED, 0.0, &none);
+    if (s != BEM_OK) return s;
+    for (int round = 0; round < 2; ++round)
+        for (int g = 0; g < ng; ++g) {
+            apply(grid[g]);
+            s = bem_solve(ctx, 1, omega, BEM_MIXED, 0.0, &none);  // recapture the LU graph untimed
+            const auto t0 = std::chrono::steady_clock::now();
+            if (s == BEM_OK) s = bem_solve(ctx, n_freq, omega, BEM_MIXED, 0.0, &none);
+            const auto t1 = std::chrono::steady_clock::now();
+            if (s != BEM_OK) {
+                apply(grid[0]);  // leave the caller's setting in place
+                return s;
+            }
+            best[g] = std::min(best[g], std::chrono::duration<double, std::milli>(t1 - t0).count() / n_freq);
+        }
+    int pick = 0;
+    for (int g = 1; g < ng; ++g)
+        if (best[g] < best[pick]) pick = g;
+    apply(grid[pick]);
+    if (ms_per_freq) *ms_per_freq = best[pick];
+    if (report && report_len > 0) {
+        std::string r;
+        for (int g = 0; g < ng; ++g) {
+            char line[160];
+            snprintf(line, sizeof(line), "%sasm_reserve_sms=%d lu_cluster_inverse=%d lu_block_inverse=%d "
+                     "lu_pair_update=%d: %.3f ms/frequency\n", g == pick ? "* " : "  ", grid[g].asm_reserve,
+                     grid[g].cluster, grid[g].block, grid[g].pair, best[g]);
+            r += line;
+        }
+        const size_t n = std::min(r.size(), (size_t)report_len - 1);
+        memcpy(report, r.data(), n);
+        report[n] = '\0';
+    }
+    return BEM_OK;
 }
 
 bem_status bem_set_wave_points(bem_ctx* ctx, int n, const double* xyz) {

@@ -44,6 +44,9 @@ def parse():
     p.add_argument("--na", type=int, default=64, help="azimuthal panels per cylinder (64 -> 8192 panels)")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     p.add_argument("--batched", type=int, default=1, help="1: also run the 64-body batched form")
+    p.add_argument("--autotune", type=int, default=1,
+                   help="1: time a small grid of schedule settings on 8 sample frequencies before the "
+                        "warm-up (outside the timed region) and keep the fastest")
     p.add_argument("--surrogate-seconds", type=float, default=20.0,
                    help="training budget of the Green-function surrogate report (0 skips it)")
     return p.parse_args()
@@ -304,6 +307,13 @@ def main():
              else my[i % n_my] for i in range(args.steps)]
     warm = [my[(7 * i + 3) % n_my] for i in range(args.warmup)]
     seq = warm + timed
+    tune = None
+    if args.autotune and n_my >= 2:
+        t0 = time.perf_counter()
+        sample = [my[(i * n_my) // 8 + n_my // 16] for i in range(8)] if n_my >= 8 else list(my)
+        tune_ms, tune_rep = s.autotune(sample)
+        tune = {"ms_per_freq": tune_ms, "sample_omegas": len(sample), "settings": tune_rep,
+                "wall_s": time.perf_counter() - t0}
     if args.warmup > 0:
         s.solve_omegas(seq[:args.warmup])
     s.stage_times(reset=True)
@@ -413,7 +423,8 @@ def main():
             "batched": batched,
             "stage_ms": dict(zip(names, [float(x) for x in per])),
             "stage_ms_note": "per frequency; assembly of f+1 overlaps factor+solve of f, so stages sum to more than ms_per_step",
-            "setup_s": setup_s}
+            "setup_s": setup_s,
+            "autotune": tune}
     print(json.dumps(line))
 
 

@@ -292,6 +292,18 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     (1..64, default 4; finer items measured slower). */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
+/* Autotuner of the pipelined mixed solve: times bem_solve (BEM_MIXED, outputs skipped)
+ * on the n_freq >= 2 sample frequencies for each of a small grid of the schedule knobs
+ * above (the current setting, assembly reserves of 56-88 SMs, the 4-CTA blocked and
+ * the 8-CTA pivot-warp block inverse, one or two elimination steps per pass), every
+ * setting twice in alternation, and keeps the fastest on the context.  ms_per_freq
+ * (optional) receives its time per frequency; report (optional, report_len bytes) one
+ * line per setting, the chosen one marked '*'.  Needs bem_setup.  The project's
+ * replacement for hand-picked launch shapes: the best split of the GPU between the
+ * overlapping assembly and the LU varies between GPUs of one pool. */
+bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* ms_per_freq, char* report,
+                        int report_len);
+
 /* Timeline of the tensor-core LU's lookahead schedule (tracing aid).  enable = 1
  * turns recording on (events at every block step of later mixed factorizations),
  * 0 turns it off, -1 leaves it unchanged.  out receives, for the first

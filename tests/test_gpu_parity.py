@@ -168,6 +168,25 @@ def test_lu_schedule_variants_agree(bg):
         _compare(got, ref, 1e-6, keys=("A", "B", "F"))
 
 
+def test_autotune_picks_a_setting(bg):
+    # the autotuner times seven schedule settings on the sample frequencies, marks the one
+    # it keeps, and the solver then solves with it to the mixed-path tolerance
+    mesh = bg.Half_Cylinder(10.0, 20.0, 40, 6, 24, 0, False)
+    om = np.array([0.6, 1.4])
+    ref = _solver(bg, mesh).solve_omegas(om)
+    s = _solver(bg, mesh, precision=bg.MIXED)
+    ms, report = s.autotune([0.4, 0.9, 1.6, 2.4])
+    print("\n".join(report))
+    assert ms > 0.0
+    assert len(report) == 7
+    assert sum(line.startswith("*") for line in report) == 1
+    got = s.solve_omegas(om)
+    assert np.all(got["residual"] <= 1e-12)
+    _compare(got, ref, 1e-6, keys=("A", "B", "F"))
+    with pytest.raises(bg.BEMError):
+        s.autotune([0.5])
+
+
 def test_plain_fp64_solve_matches_oracle_array(bg, orc):
     c = cases.ARRAY_SMALL
     om, _ = orc.cylinder(c["R"], c["draft"], c["NA"], c["NR"], c["NV"], cosine=False)
