@@ -142,12 +142,14 @@ struct LuStreams {
                             // (k_inv128b), 2 eight at a time with the next pivot block ahead (k_inv128l)
     cudaStream_t rest;      // paired schedule: trailing updates of two steps at a time
     cudaEvent_t ev_panel2, ev_cross2;
+    float* pair_t;          // 4 (n / 256) 128 128 floats: transposed pair blocks of the pair fold
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
 // diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The
 // factorization leaves L as W blocks below the diagonal, the diagonal-block
 // inverses in inv, and above the diagonal U D^-1 (each column block right-multiplied
-// by the inverse of its diagonal block), the form lu_solve_f32 uses.
+// by the inverse of its diagonal block); then the pair fold (lu_pair_fold) puts both
+// factors in the form lu_solve_f32 uses.
 int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                             float* wl2, float* wut2, int* flags);
 // Paired schedule (two elimination steps per pass over the trailing matrix); needs

@@ -89,7 +89,7 @@ struct bem_ctx {
     float* d_X32 = nullptr;
     double *d_part = nullptr, *d_post = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
-    float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_wu32 = nullptr, *d_wut32 = nullptr;
+    float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_pairT = nullptr, *d_wut32 = nullptr;
     int* d_flags = nullptr;
     int* d_ready = nullptr;           // block-ready flags of the cooperative triangular solves
     int solve_epoch = 0;
@@ -206,7 +206,7 @@ void free_all(bem_ctx* ctx) {
                      &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64, &ctx->d_gmV, &ctx->d_gmZ, &ctx->d_gmW,
                      &ctx->d_gmPart, &ctx->d_gmH, &ctx->d_gmC};
     for (auto p : dp) *p = nullptr;
-    float** fp[] = {&ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i, &ctx->d_wl32, &ctx->d_wu32, &ctx->d_wut32,
+    float** fp[] = {&ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i, &ctx->d_wl32, &ctx->d_pairT, &ctx->d_wut32,
                     &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi, &ctx->d_RSRlo};
     for (auto p : fp) *p = nullptr;
     for (FreqState& F : ctx->fs) reset_slot(F);
@@ -308,7 +308,7 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->d_wl32, (size_t)8 * Np * nb32);  // four [2][Np][128] buffers (lookahead; two steps per pass)
-        DA(ctx->d_wu32, (size_t)2 * Np * nb32);
+        DA(ctx->d_pairT, (size_t)2 * Np * nb32);  // transposed pair blocks of the pair fold (4 (Np/256) 128^2)
         DA(ctx->d_wut32, (size_t)8 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
@@ -554,7 +554,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                         : nullptr,
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
                                     ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
-                                    ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2};
+                                    ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2,
+                                    ctx->d_pairT};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, ctx->d_flags);

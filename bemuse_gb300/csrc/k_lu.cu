@@ -27,6 +27,7 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
 bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
             int count);
 bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags);
+bool tc_pair_fold(cudaStream_t st, int n, CMat<float> A, const float* T, int which, int* flags);
 bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
                     int max_ctas, int* flags, const float* wl_a, const float* wut_a, int lr_a, int ur_a,
                     const float* wl_b, const float* wut_b, int lr_b, int ur_b);
@@ -1207,6 +1208,47 @@ __global__ void k_panel_transpose(int cols, CMat<float> A, int r0, int c0, float
     }
 }
 
+// T[which][plane][p][j][i] = B_p[i][j] for the off-diagonal blocks of the 128-block pairs
+// (2p, 2p+1): which 0: B_p = L_{2p+1,2p}, which 1: B_p = (U D^-1)_{2p,2p+1}; rounded to
+// TF32 (nearest).  Grid (4, 4, 2 np), 32 x 8 threads.
+__global__ void k_pair_transpose(int np, CMat<float> A, float* T) {
+    __shared__ float tr[32][33], ti[32][33];
+    const int p = blockIdx.z % np, which = blockIdx.z / np;
+    const size_t r0 = (size_t)(which == 0 ? 2 * p + 1 : 2 * p) * 128, c0 = (size_t)(which == 0 ? 2 * p : 2 * p + 1) * 128;
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const size_t g = (r0 + i0 + y) * A.ld + c0 + j0 + threadIdx.x;
+        tr[y][threadIdx.x] = A.re[g];
+        ti[y][threadIdx.x] = A.im[g];
+    }
+    __syncthreads();
+    const size_t plane = (size_t)np * 128 * 128;
+    float* Tr = T + 2 * which * plane + (size_t)p * 128 * 128;
+    float* Ti = Tr + plane;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const size_t o = (size_t)(j0 + y) * 128 + i0 + threadIdx.x;
+        Tr[o] = tf32_rn(tr[threadIdx.x][y]);
+        Ti[o] = tf32_rn(ti[threadIdx.x][y]);
+    }
+}
+
+// Pair fold: with P = blockdiag([I 0; L_{2p+1,2p} I]) and Q = blockdiag([I U_{2p,2p+1}; 0 I])
+// over the 128-block pairs, L = L'' P and U D^-1 = U'' Q, where L'' and U'' have identity
+// diagonal blocks of 256 rows.  A forward solve is then a chain of n / 256 steps over L''
+// followed by x = P^-1 y (one independent 128 x 128 product per pair), and likewise the
+// backward solve; see k_trsv_tk and k_pair_apply.  L'' and U'' replace L and U D^-1 in A
+// (the pair blocks themselves are kept).  T: 4 np 128 128 floats.
+int lu_pair_fold(cudaStream_t st, int n, CMat<float> A, float* T, int* flags) {
+    const int np = n / 256;
+    if (np == 0) return 0;
+    if (!T) return 1;
+    BEM_LAUNCH(k_pair_transpose<<<dim3(4, 4, 2 * np), dim3(32, 8), 0, st>>>(np, A, T));
+    const size_t plane = (size_t)np * 128 * 128;
+    if (!tc_pair_fold(st, n, A, T, 1, flags)) return 1;
+    if (!tc_pair_fold(st, n, A, T + 2 * plane, 2, flags)) return 1;
+    return 0;
+}
+
 int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                             float* wl2, float* wut2, int* flags) {
     constexpr int NB = 128;
@@ -1326,7 +1368,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         cudaEventRecord(ls.ev_ucol, ls.ucol);
         cudaStreamWaitEvent(st, ls.ev_ucol, 0);
     }
-    return 0;
+    return lu_pair_fold(st, n, A, ls.pair_t, flags);
 }
 
 // The same factorization with the trailing updates of two consecutive steps applied
@@ -1453,7 +1495,7 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
         cudaEventRecord(ls.ev_ucol, ls.ucol);
         cudaStreamWaitEvent(st, ls.ev_ucol, 0);
     }
-    return 0;
+    return lu_pair_fold(st, n, A, ls.pair_t, flags);
 }
 
 int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
@@ -1687,35 +1729,37 @@ static int trsv_coop(cudaStream_t st, int n, CMat<T> A, const T* invr, const T* 
 }
 
 // ---------------------------------------------------------------------------
-// FP32 block triangular solve, split by rows: each 128-row block of the system
-// is shared by eight CTAs of 16 rows (sub-blocks), so the product that sits on
-// the critical path (one 16 x 128 tile against the newest block of x) is an
-// eighth of a block's.  Thread (i, s) = (tid % 16, tid / 16) owns row i of the
-// sub-block and the 8 columns s*8.. of every tile; the tile is prefetched into
-// registers one dependency ahead, and the blocks of x are staged in shared
-// memory by cp.async, double-buffered: while a CTA multiplies one tile, the
-// x block of the next tile is already in flight whenever its producer has
-// published it.  The eight column slices are summed once at the end.
-//   which = 0 (forward, unit block-lower L):  x_b = y_b - sum_{c<b} L_bc x_c
-//   which = 1 (backward, unit block-upper U D^-1, as the factorization leaves it):
-//                          z_b = y_b - sum_{c>b} (U D^-1)_bc z_c
-// Both directions are the same chain; the block-diagonal x = D^-1 z that completes
-// the backward solve is one parallel launch afterwards (k_dinv_apply), so nothing on
-// the chain waits for a whole 128-row block.  Yin and Xout may be the same array:
-// a CTA reads its own rows of Yin before it writes them, and other blocks' rows of
-// Xout only after their flags.
-// xflag[u] (u = sub-block) is raised to `epoch` when the rows of u are in memory.
-// Waits give up at a 2 s deadline (FLAG_TIMEOUT).
-// Scheduling needs no co-residency (plain launch, one CTA per sub-block): each
-// CTA draws a ticket when it starts and tickets map to sub-blocks in dependency
-// order, so a CTA waits only on sub-blocks of CTAs that started before it, or
-// The lowest unfinished ticket therefore always progresses, whatever else runs
-// on the GPU.  The CTA that draws the last ticket resets the counter.
-// TS_SB sub-blocks of TS_RW rows per 128-row block; a CTA's 256 threads are TS_RW rows x
-// TS_SL column slices of TS_KC columns.  Three CTAs fit on an SM (80 registers): a chain
-// that shares the GPU with a persistent assembly kernel keeps more of its CTAs resident.
-constexpr int TS_NB = 128, TS_SB = 8, TS_RW = TS_NB / TS_SB, TS_THREADS = 256, TS_SL = TS_THREADS / TS_RW,
-              TS_KC = TS_NB / TS_SL;
+// FP32 block triangular solves of the pair-folded factors (lu_pair_fold).  Both are
+// chains over super-blocks of 256 rows whose diagonal blocks are the identity:
+//   which = 0 (forward, L''):   y_b = v_b - sum_{c<b} L''_bc y_c
+//   which = 1 (backward, U''):  z_b = v_b - sum_{c>b} U''_bc z_c
+// k_pair_apply then applies P^-1 (resp. Q^-1), one independent 128 x 128 product per
+// pair, and the backward solve ends with the block-diagonal D^-1 (k_dinv_apply), so
+// nothing on either chain waits for a block inverse.  The last super-block has 128 rows
+// when n / 128 is odd.
+// A super-block is shared by 32 CTAs of 8 rows (sub-blocks), so the product on the
+// critical path (one 8 x 256 tile against the newest super-block of x) is small.
+// Thread (i, s) = (tid % 8, tid / 8) owns row i of the sub-block and the 8 columns s*8..
+// of every tile; the tile is prefetched into registers one dependency ahead, and the
+// super-blocks of x are staged in shared memory by cp.async, double-buffered: while a
+// CTA multiplies one tile, the next is already in flight whenever its producer has
+// published it.  The 32 column slices are summed once at the end (warp shuffles, then
+// shared memory).  Yin and Xout may be the same array: a CTA reads its own rows of Yin
+// before it writes them, and other super-blocks' rows of Xout only after their flags.
+// xflag[u] (u = sub-block) is raised to `epoch` when the rows of u are in memory; one
+// warp polls the 32 flags of a super-block at once.  Waits give up at a 2 s deadline
+// (FLAG_TIMEOUT).
+// Scheduling needs no co-residency (plain launch, one CTA per sub-block): each CTA
+// draws a ticket when it starts and tickets map to sub-blocks in dependency order, so
+// a CTA waits only on sub-blocks of CTAs that started before it.  The lowest unfinished
+// ticket therefore always progresses, whatever else runs on the GPU.  The CTA that
+// draws the last ticket resets the counter.  Three CTAs fit on an SM (80 registers): a
+// chain that shares the GPU with a persistent assembly kernel keeps more CTAs resident.
+constexpr int TS_NB = 256, TS_RW = 8, TS_SB = TS_NB / TS_RW, TS_THREADS = 256, TS_SL = TS_THREADS / TS_RW,
+              TS_KC = TS_NB / TS_SL, TS_WARPS = TS_THREADS / 32;
+// k_pair_apply and k_dinv_apply: 128-row blocks, 8 CTAs of 16 rows, 16 column slices of 8
+constexpr int DA_NB = 128, DA_RW = 16, DA_SB = DA_NB / DA_RW, DA_SL = TS_THREADS / DA_RW, DA_KC = DA_NB / DA_SL;
+static_assert(TS_KC == 8 && DA_KC == 8 && TS_SB == 32, "rows are read 8 floats at a time; one warp polls a super-block");
 
 __device__ __forceinline__ unsigned long long ts_now() {
     unsigned long long t;
@@ -1741,10 +1785,10 @@ __device__ __forceinline__ bool ts_ready(const int* f, int epoch) {
     return v >= epoch;
 }
 
-__device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const float* __restrict__ gi, float* r,
-                                            float* im) {
+__device__ __forceinline__ void ld_row8(const float* __restrict__ gr, const float* __restrict__ gi, float* r,
+                                        float* im) {
 #pragma unroll
-    for (int v = 0; v < TS_KC / 4; ++v) {
+    for (int v = 0; v < 2; ++v) {
         float4 a = __ldg(reinterpret_cast<const float4*>(gr) + v);
         float4 b = __ldg(reinterpret_cast<const float4*>(gi) + v);
         r[4 * v] = a.x; r[4 * v + 1] = a.y; r[4 * v + 2] = a.z; r[4 * v + 3] = a.w;
@@ -1752,21 +1796,22 @@ __device__ __forceinline__ void ts_load_row(const float* __restrict__ gr, const 
     }
 }
 
-// Floats of one staging buffer: a 128 x R complex block in its global layout, plus
-// RC complex of zero padding (rows are read RC wide), rounded to 16 bytes.
-__host__ __device__ constexpr int ts_zstride(int R, int RC) { return ((2 * (TS_NB * R + RC)) + 3) & ~3; }
+// Floats of one staging buffer: a rows x R complex block in its global layout, plus RC
+// complex of zero padding (rows are read RC wide), rounded to 16 bytes.
+__host__ __device__ constexpr int ts_zstride(int rows, int R, int RC) { return ((2 * (rows * R + RC)) + 3) & ~3; }
 
 template <int RC>
-__global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int nblk, int R, CMat<float> A, int which,
+__global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int n, int R, CMat<float> A, int which,
                                                         float* Yin, float* Xout, int* xflag, int* ticket,
                                                         int epoch, int* gflags) {
     extern __shared__ __align__(16) float ts_smem[];
     __shared__ int s_ticket, s_go;
-    const int zs = ts_zstride(R, RC);
-    float* zb = ts_smem;                        // [2][zs]
-    float* red = zb + 2 * zs;                   // [TS_SL][TS_RW][RC] complex interleaved
-    float* ybase = red + TS_SL * TS_RW * RC * 2;  // [TS_RW][R] complex: this sub-block's rows of Yin
-    const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW;
+    const int zs = ts_zstride(TS_NB, R, RC);
+    float* zb = ts_smem;                             // [2][zs]
+    float* red = zb + 2 * zs;                        // [TS_WARPS][TS_RW][RC] complex interleaved
+    float* ybase = red + TS_WARPS * TS_RW * RC * 2;  // [TS_RW][R] complex: this sub-block's rows of Yin
+    const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW, wl = tid & 31;
+    const int nsub = n / TS_RW, nsb = (n + TS_NB - 1) / TS_NB;
     const unsigned long long deadline = ts_now() + 2000000000ull;
     int dead = 0;
     if (tid == 0) {
@@ -1777,39 +1822,53 @@ __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int nblk, int R, CMat
     for (int idx = 2 * TS_NB * R + tid; idx < zs; idx += blockDim.x) { zb[idx] = 0.f; zb[zs + idx] = 0.f; }
     __syncthreads();
     const int tk = s_ticket;
-    const int bo = tk / TS_SB, q = tk % TS_SB;
-    const int b = which == 0 ? bo : nblk - 1 - bo;
-    const int u = b * TS_SB + q;
-    const size_t row0 = (size_t)b * TS_NB + q * TS_RW;
-    const int cnt = which == 0 ? b : nblk - 1 - b;
-    auto cidx = [&](int t) { return which == 0 ? t : nblk - 1 - t; };
+    const int u = which == 0 ? tk : nsub - 1 - tk;
+    const int b = u / TS_SB;
+    const size_t row0 = (size_t)u * TS_RW;
+    const int cnt = which == 0 ? b : nsb - 1 - b;
+    auto cidx = [&](int t) { return which == 0 ? t : nsb - 1 - t; };
+    auto width = [&](int c) { return min(TS_NB, n - c * TS_NB); };
     // the sub-block's rows of Yin are static during the launch: fetch them now, off the
     // critical path of the final reduction
     for (int idx = tid; idx < TS_RW * R; idx += blockDim.x)
         reinterpret_cast<float2*>(ybase)[idx] = reinterpret_cast<const float2*>(Yin)[row0 * R + idx];
-    // stage the 128 x R block of x (or w) at block c into buffer buf, 16 bytes per cp.async
-    auto issue_copy = [&](const float* src_base, int c, int buf) {
-        const float* src = src_base + (size_t)c * TS_NB * R * 2;
+    // stage the width(c) x R block of x at super-block c into buffer buf, 16 bytes per cp.async
+    auto issue_copy = [&](int c, int buf) {
+        const float* src = Xout + (size_t)c * TS_NB * R * 2;
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(zb + buf * zs);
-        for (int i = tid; i < TS_NB * R / 2; i += blockDim.x)
+        const int chunks = width(c) * R / 2;
+        for (int i = tid; i < chunks; i += blockDim.x)
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 4 * i)
                          : "memory");
         asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // every sub-block of super-block c is published: one flag per lane of warp 0
+    auto probe = [&](int c) {
+        const int k = wl, subs = width(c) / TS_RW;
+        const bool ok = k >= subs || ts_ready(xflag + c * TS_SB + k, epoch);
+        return __all_sync(0xffffffffu, ok);
+    };
+    auto wait_block = [&](int c) {
+        if (tid < width(c) / TS_RW) ts_wait(xflag + c * TS_SB + tid, epoch, deadline, dead, gflags);
     };
     float ar[RC], ai[RC];
 #pragma unroll
     for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
     float cr[TS_KC], ci[TS_KC], nr[TS_KC], ni[TS_KC];
-    auto tile_ptr = [&](int t, const float*& pr, const float*& pi) {
-        const size_t off = (row0 + lane) * A.ld + (size_t)cidx(t) * TS_NB + s * TS_KC;
-        pr = A.re + off;
-        pi = A.im + off;
+    // row lane of this sub-block, columns s*8.. of super-block c (only where c is that wide)
+    auto load_tile = [&](int t, float* r, float* im) {
+        const int c = cidx(t);
+        if (s * TS_KC < width(c)) {
+            const size_t off = (row0 + lane) * A.ld + (size_t)c * TS_NB + s * TS_KC;
+            ld_row8(A.re + off, A.im + off, r, im);
+        }
     };
-    // z (a staged block) times the register tile: acc += sgn * tile * z
-    auto mac = [&](const float* z, float sg) {
+    // acc -= tile * z (z: a staged super-block)
+    auto mac = [&](const float* z, int c) {
+        if (s * TS_KC >= width(c)) return;
 #pragma unroll
         for (int kk = 0; kk < TS_KC; ++kk) {
-            const float lr = sg * cr[kk], li = sg * ci[kk];
+            const float lr = -cr[kk], li = -ci[kk];
             const float2* zk = reinterpret_cast<const float2*>(z) + (size_t)(s * TS_KC + kk) * R;
 #pragma unroll
             for (int j = 0; j < RC; ++j) {  // columns j >= R read padding or the next row: never stored
@@ -1820,54 +1879,58 @@ __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int nblk, int R, CMat
         }
     };
     if (cnt > 0) {
-        const float *pr, *pi;
-        tile_ptr(0, pr, pi);
-        ts_load_row(pr, pi, cr, ci);
-        if (tid < TS_SB) ts_wait(xflag + cidx(0) * TS_SB + tid, epoch, deadline, dead, gflags);
+        load_tile(0, cr, ci);
+        wait_block(cidx(0));
         __syncthreads();
-        issue_copy(Xout, cidx(0), 0);
+        issue_copy(cidx(0), 0);
     }
     for (int t = 0; t < cnt; ++t) {
-        if (t + 1 < cnt) {
-            const float *pr, *pi;
-            tile_ptr(t + 1, pr, pi);
-            ts_load_row(pr, pi, nr, ni);
-        }
-        // start the next block's copy now if its producer is done
+        if (t + 1 < cnt) load_tile(t + 1, nr, ni);
+        // start the next super-block's copy now if its producers are done
         bool early = false;
         if (t + 1 < cnt) {
-            if (tid == 0) {
-                bool ok = true;
-                for (int k = 0; k < TS_SB; ++k) ok = ok && ts_ready(xflag + cidx(t + 1) * TS_SB + k, epoch);
-                s_go = ok ? 1 : 0;
+            if (tid < 32) {
+                const bool ok = probe(cidx(t + 1));
+                if (tid == 0) s_go = ok ? 1 : 0;
             }
             __syncthreads();
             early = s_go != 0;
-            if (early) issue_copy(Xout, cidx(t + 1), (t + 1) & 1);
+            if (early) issue_copy(cidx(t + 1), (t + 1) & 1);
         }
         if (early) asm volatile("cp.async.wait_group 1;" ::: "memory");
         else asm volatile("cp.async.wait_group 0;" ::: "memory");
         __syncthreads();
-        mac(zb + (t & 1) * zs, -1.f);
+        mac(zb + (t & 1) * zs, cidx(t));
         __syncthreads();  // buffer t & 1 is refilled for tile t + 2
         if (t + 1 < cnt && !early) {
-            if (tid < TS_SB) ts_wait(xflag + cidx(t + 1) * TS_SB + tid, epoch, deadline, dead, gflags);
+            wait_block(cidx(t + 1));
             __syncthreads();
-            issue_copy(Xout, cidx(t + 1), (t + 1) & 1);
+            issue_copy(cidx(t + 1), (t + 1) & 1);
         }
 #pragma unroll
         for (int kk = 0; kk < TS_KC; ++kk) { cr[kk] = nr[kk]; ci[kk] = ni[kk]; }
     }
-    // sum the column slices: out = y + sum_s acc_s
+    // sum the column slices: the four slices of a warp by shuffles (lanes l, l+8, l+16,
+    // l+24 hold row l % 8), then the eight warps through shared memory: out = y + sum
 #pragma unroll
-    for (int j = 0; j < RC; ++j)
-        *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+    for (int j = 0; j < RC; ++j) {
+        ar[j] += __shfl_xor_sync(0xffffffffu, ar[j], 8);
+        ai[j] += __shfl_xor_sync(0xffffffffu, ai[j], 8);
+        ar[j] += __shfl_xor_sync(0xffffffffu, ar[j], 16);
+        ai[j] += __shfl_xor_sync(0xffffffffu, ai[j], 16);
+    }
+    if (wl < TS_RW) {
+        const int w = tid >> 5;
+#pragma unroll
+        for (int j = 0; j < RC; ++j)
+            *reinterpret_cast<float2*>(red + ((w * TS_RW + wl) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+    }
     __syncthreads();
     for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
         const int i = idx / R, j = idx % R;
         float2 o = reinterpret_cast<const float2*>(ybase)[idx];
 #pragma unroll
-        for (int w = 0; w < TS_SL; ++w) {
+        for (int w = 0; w < TS_WARPS; ++w) {
             const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
             o.x += v.x;
             o.y += v.y;
@@ -1880,51 +1943,97 @@ __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int nblk, int R, CMat
     if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(xflag + u), "r"(epoch) : "memory");
 }
 
-// x_b = D_b^-1 z_b for every 128-row block b: CTA (b, 16-row group q), thread
-// (i, s) = (tid % 16, tid / 16) multiplies row q*16 + i of D_b^-1, columns s*8..,
-// against the staged block of z; the 16 column slices are summed through shared
-// memory.  Z and X must not overlap.
+// The 128-row block products after a chain: CTA (pair or block, 16-row group q),
+// thread (i, s) = (tid % 16, tid / 16) multiplies row q*16 + i of a 128 x 128 matrix,
+// columns s*8.., against a staged 128 x R block; the 16 column slices are summed
+// through shared memory.
+template <int RC>
+struct BlockRowProduct {
+    float ar[RC], ai[RC];
+    __device__ void run(const float* __restrict__ mr, const float* __restrict__ mi, const float* zb, float* red,
+                        int R, int lane, int s) {
+        float cr[DA_KC], ci[DA_KC];
+        ld_row8(mr, mi, cr, ci);
+        __syncthreads();  // the staged block is complete
+#pragma unroll
+        for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
+#pragma unroll
+        for (int kk = 0; kk < DA_KC; ++kk) {
+            const float2* zk = reinterpret_cast<const float2*>(zb) + (size_t)(s * DA_KC + kk) * R;
+#pragma unroll
+            for (int j = 0; j < RC; ++j) {  // columns j >= R read padding or the next row: never stored
+                const float2 v = zk[j];
+                ar[j] = fmaf(cr[kk], v.x, fmaf(-ci[kk], v.y, ar[j]));
+                ai[j] = fmaf(cr[kk], v.y, fmaf(ci[kk], v.x, ai[j]));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < RC; ++j)
+            *reinterpret_cast<float2*>(red + ((s * DA_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
+        __syncthreads();
+    }
+};
+
+__device__ __forceinline__ void stage_block(const float* __restrict__ src, float* zb, int R, int zs) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    for (int i = threadIdx.x; i < DA_NB * R / 2; i += blockDim.x) reinterpret_cast<float4*>(zb)[i] = __ldg(s4 + i);
+    for (int idx = 2 * DA_NB * R + threadIdx.x; idx < zs; idx += blockDim.x) zb[idx] = 0.f;
+}
+
+// The pair products of the folded factors, in place (one 128 x 128 product per pair):
+//   which = 0:  x_{2p+1} -= L_{2p+1,2p} x_{2p}               (x = P^-1 y)
+//   which = 1:  x_{2p}   -= (U D^-1)_{2p,2p+1} x_{2p+1}      (x = Q^-1 z)
+// The pair blocks are in A (the fold keeps them).  A CTA writes rows of its target block
+// only and reads the source block, which no CTA of the launch writes.
+template <int RC>
+__global__ void __launch_bounds__(TS_THREADS) k_pair_apply(int R, CMat<float> A, int which, float* X) {
+    extern __shared__ __align__(16) float pa_smem[];
+    const int zs = ts_zstride(DA_NB, R, RC);
+    float* zb = pa_smem;  // the 128 x R complex source block, then RC complex of zeros
+    float* red = zb + zs; // [DA_SL][DA_RW][RC] complex interleaved
+    const int tid = threadIdx.x, lane = tid % DA_RW, s = tid / DA_RW;
+    const int p = blockIdx.x / DA_SB, q = blockIdx.x % DA_SB;
+    const int tgt = which == 0 ? 2 * p + 1 : 2 * p, src = which == 0 ? 2 * p : 2 * p + 1;
+    stage_block(X + (size_t)src * DA_NB * R * 2, zb, R, zs);
+    const size_t row0 = (size_t)tgt * DA_NB + q * DA_RW;
+    const size_t off = (row0 + lane) * A.ld + (size_t)src * DA_NB + s * DA_KC;
+    BlockRowProduct<RC> prod;
+    prod.run(A.re + off, A.im + off, zb, red, R, lane, s);
+    for (int idx = tid; idx < DA_RW * R; idx += blockDim.x) {
+        const int i = idx / R, j = idx % R;
+        float2 o = reinterpret_cast<const float2*>(X)[(row0 + i) * R + j];
+#pragma unroll
+        for (int w = 0; w < DA_SL; ++w) {
+            const float2 v = *reinterpret_cast<const float2*>(red + ((w * DA_RW + i) * RC + j) * 2);
+            o.x -= v.x;
+            o.y -= v.y;
+        }
+        reinterpret_cast<float2*>(X)[(row0 + i) * R + j] = o;
+    }
+}
+
+// x_b = D_b^-1 z_b for every 128-row block b.  Z and X must not overlap.
 template <int RC>
 __global__ void __launch_bounds__(TS_THREADS) k_dinv_apply(int R, const float* __restrict__ invr,
                                                            const float* __restrict__ invi,
                                                            const float* __restrict__ Z, float* __restrict__ X) {
     extern __shared__ __align__(16) float da_smem[];
-    const int zs = ts_zstride(R, RC);
-    float* zb = da_smem;       // the 128 x R complex block of z, then RC complex of zeros
-    float* red = zb + zs;      // [TS_SL][TS_RW][RC] complex interleaved
-    const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW;
-    const int b = blockIdx.x / TS_SB, q = blockIdx.x % TS_SB;
-    const size_t row0 = (size_t)b * TS_NB + q * TS_RW;
-    const float4* src = reinterpret_cast<const float4*>(Z + (size_t)b * TS_NB * R * 2);
-    for (int i = tid; i < TS_NB * R / 2; i += blockDim.x) reinterpret_cast<float4*>(zb)[i] = __ldg(src + i);
-    for (int idx = 2 * TS_NB * R + tid; idx < zs; idx += blockDim.x) zb[idx] = 0.f;
-    float cr[TS_KC], ci[TS_KC];
-    const size_t off = (size_t)b * TS_NB * TS_NB + (size_t)(q * TS_RW + lane) * TS_NB + s * TS_KC;
-    ts_load_row(invr + off, invi + off, cr, ci);
-    __syncthreads();
-    float ar[RC], ai[RC];
-#pragma unroll
-    for (int j = 0; j < RC; ++j) { ar[j] = 0.f; ai[j] = 0.f; }
-#pragma unroll
-    for (int kk = 0; kk < TS_KC; ++kk) {
-        const float2* zk = reinterpret_cast<const float2*>(zb) + (size_t)(s * TS_KC + kk) * R;
-#pragma unroll
-        for (int j = 0; j < RC; ++j) {  // columns j >= R read padding or the next row: never stored
-            const float2 v = zk[j];
-            ar[j] = fmaf(cr[kk], v.x, fmaf(-ci[kk], v.y, ar[j]));
-            ai[j] = fmaf(cr[kk], v.y, fmaf(ci[kk], v.x, ai[j]));
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < RC; ++j)
-        *reinterpret_cast<float2*>(red + ((s * TS_RW + lane) * RC + j) * 2) = make_float2(ar[j], ai[j]);
-    __syncthreads();
-    for (int idx = tid; idx < TS_RW * R; idx += blockDim.x) {
+    const int zs = ts_zstride(DA_NB, R, RC);
+    float* zb = da_smem;  // the 128 x R complex block of z, then RC complex of zeros
+    float* red = zb + zs; // [DA_SL][DA_RW][RC] complex interleaved
+    const int tid = threadIdx.x, lane = tid % DA_RW, s = tid / DA_RW;
+    const int b = blockIdx.x / DA_SB, q = blockIdx.x % DA_SB;
+    const size_t row0 = (size_t)b * DA_NB + q * DA_RW;
+    stage_block(Z + (size_t)b * DA_NB * R * 2, zb, R, zs);
+    const size_t off = (size_t)b * DA_NB * DA_NB + (size_t)(q * DA_RW + lane) * DA_NB + s * DA_KC;
+    BlockRowProduct<RC> prod;
+    prod.run(invr + off, invi + off, zb, red, R, lane, s);
+    for (int idx = tid; idx < DA_RW * R; idx += blockDim.x) {
         const int i = idx / R, j = idx % R;
         float2 o = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int w = 0; w < TS_SL; ++w) {
-            const float2 v = *reinterpret_cast<const float2*>(red + ((w * TS_RW + i) * RC + j) * 2);
+        for (int w = 0; w < DA_SL; ++w) {
+            const float2 v = *reinterpret_cast<const float2*>(red + ((w * DA_RW + i) * RC + j) * 2);
             o.x += v.x;
             o.y += v.y;
         }
@@ -1932,23 +2041,27 @@ __global__ void __launch_bounds__(TS_THREADS) k_dinv_apply(int R, const float* _
     }
 }
 
-// Forward chain, backward chain (in place over the forward's output) and the
-// block-diagonal apply, for one column count RC >= R.
+// Forward chain, P^-1, backward chain (in place over the forward's output), Q^-1 and
+// the block-diagonal D^-1, for one column count RC >= R.
 template <int RC>
 static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R,
                           float* X, float* tmp, int* xflag, int* ticket, int epoch, int* flags) {
-    const int nblk = n / TS_NB;
-    const size_t smem = sizeof(float) * (2 * (size_t)ts_zstride(R, RC) + TS_SL * TS_RW * RC * 2 + TS_RW * 2 * R);
-    const size_t smem_d = sizeof(float) * ((size_t)ts_zstride(R, RC) + TS_SL * TS_RW * RC * 2);
+    const int nsub = n / TS_RW, np = n / 256, nblk = n / DA_NB;
+    const size_t smem =
+        sizeof(float) * (2 * (size_t)ts_zstride(TS_NB, R, RC) + TS_WARPS * TS_RW * RC * 2 + TS_RW * 2 * R);
+    const size_t smem_d = sizeof(float) * ((size_t)ts_zstride(DA_NB, R, RC) + DA_SL * DA_RW * RC * 2);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_trsv_tk<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (smem_d > 48 * 1024)
+    if (smem_d > 48 * 1024) {
         cudaFuncSetAttribute(k_dinv_apply<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d);
-    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, 0, X, tmp, xflag, ticket, epoch,
-                                                                      flags));
-    BEM_LAUNCH(k_trsv_tk<RC><<<nblk * TS_SB, TS_THREADS, smem, st>>>(nblk, R, A, 1, tmp, tmp, xflag, ticket,
-                                                                      epoch + 1, flags));
-    BEM_LAUNCH(k_dinv_apply<RC><<<nblk * TS_SB, TS_THREADS, smem_d, st>>>(R, invr, invi, tmp, X));
+        cudaFuncSetAttribute(k_pair_apply<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d);
+    }
+    BEM_LAUNCH(k_trsv_tk<RC><<<nsub, TS_THREADS, smem, st>>>(n, R, A, 0, X, tmp, xflag, ticket, epoch, flags));
+    if (np > 0) BEM_LAUNCH(k_pair_apply<RC><<<np * DA_SB, TS_THREADS, smem_d, st>>>(R, A, 0, tmp));
+    BEM_LAUNCH(k_trsv_tk<RC><<<nsub, TS_THREADS, smem, st>>>(n, R, A, 1, tmp, tmp, xflag, ticket, epoch + 1,
+                                                              flags));
+    if (np > 0) BEM_LAUNCH(k_pair_apply<RC><<<np * DA_SB, TS_THREADS, smem_d, st>>>(R, A, 1, tmp));
+    BEM_LAUNCH(k_dinv_apply<RC><<<nblk * DA_SB, TS_THREADS, smem_d, st>>>(R, invr, invi, tmp, X));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
 
@@ -1977,12 +2090,11 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
                  int* ready, int epoch, int* flags) {
-    // ready holds n / TS_RW flags (one per sub-block), n / TS_RW unused words and a
-    // ticket counter, zero between launches.  A is in the factorization's form: W blocks
-    // below the diagonal, U D^-1 above it, D^-1 in invr / invi.
+    // ready holds n / TS_RW flags (one per 8-row sub-block) and a ticket counter, zero
+    // between launches.  A is in the pair-folded form of lu_pair_fold, D^-1 in invr / invi.
     float* tmp = X + (size_t)2 * n * R;
     int* xflag = ready;
-    int* ticket = ready + 2 * n / TS_RW;
+    int* ticket = ready + n / TS_RW;
     // Solves of several contexts may run at once on one GPU: a CTA waits only on
     // sub-blocks of lower tickets of its own launch, which are already running.
     return trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);

@@ -152,6 +152,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 struct TcTiles {
     int lr0, ur0, Mt, Nt, lw, lskip, crow0, ccol0, mode, c2row0, c2col0;
     int npair, lr0b, ur0b;  // second operand pair (npair = 2): L rows from lr0b, U rows from ur0b
+    int fold, nblk;         // pair fold of the triangular factors (1: L, 2: U; nblk 128-blocks)
 };
 
 // Tiles (tm, tn), tm < Mt, tn < Nt, of the rectangle whose L rows start at lr0
@@ -162,7 +163,12 @@ struct TcTiles {
 // applied in one pass over C.  mode 0: the tile's -acc is reduce-added into
 // mapCr / mapCi at rows crow0 + tm*128, columns ccol0 + tn*128.  mode 1: +acc is
 // stored there and at c2row0 + tm*128, c2col0 + tn*128 of mapC2r / mapC2i.  mode 2:
-// +acc is stored there only.
+// +acc is stored there, rounded to TF32 (nearest).  fold = 1 / 2 (pair fold, Mt tiles
+// in all, Nt = 1): tile t is tile m of pair p, p = 0, 1, .. in turn:
+//   fold 1 (m < nblk - 2p - 2): C = block (2p+2+m, 2p), L operand = block (2p+2+m, 2p+1)
+//   fold 2 (m < 2p):            C = block (m, 2p+1),   L operand = block (m, 2p)
+// of the matrix behind mapLr / mapLi / mapCr / mapCi, U operand = rows 128 p of mapUr /
+// mapUi; mode 0 (C -= L_op * U_op).
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_tc_update(const __grid_constant__ CUtensorMap mapLr, const __grid_constant__ CUtensorMap mapLi,
                 const __grid_constant__ CUtensorMap mapUr, const __grid_constant__ CUtensorMap mapUi,
@@ -202,6 +208,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
     };
     const int KBT = KB * a.npair;
+    // tile t -> first rows of its L and U operands, the L operand's first column, and C
+    auto place = [&](int t, int& lrow, int& lx, int& urow, int& crow, int& ccol) {
+        if (a.fold) {
+            int p = 0;
+            for (;; ++p) {
+                const int c = a.fold == 1 ? a.nblk - 2 * p - 2 : 2 * p;
+                if (t < c) break;
+                t -= c;
+            }
+            crow = (a.fold == 1 ? 2 * p + 2 + t : t) * BM;
+            ccol = (a.fold == 1 ? 2 * p : 2 * p + 1) * BN;
+            lrow = crow;
+            lx = (a.fold == 1 ? 2 * p + 1 : 2 * p) * BN;
+            urow = p * BN;
+        } else {
+            int tm, tn;
+            tile_of(t, tm, tn);
+            lrow = a.lr0 + tm * BM;
+            lx = 0;
+            urow = a.ur0 + tn * BN;
+            crow = a.crow0 + tm * BM;
+            ccol = a.ccol0 + tn * BN;
+        }
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) { mbar_init(full0 + 8 * s, 1); mbar_init(empty0 + 8 * s, 1); }
@@ -230,18 +260,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                int tm, tn;
-                tile_of(t, tm, tn);
+                int lrow1, lx, urow1, crow, ccol;
+                place(t, lrow1, lx, urow1, crow, ccol);
                 for (int kb = 0; kb < KBT; ++kb, ++it) {
                     const uint32_t s = it % STAGES, u = it / STAGES;
                     if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1, abort_flag, gflags)) { ok = false; break; }
                     const uint32_t st = base + s * STAGE_BYTES;
                     const bool second = kb >= KB;
                     const int x = (second ? kb - KB : kb) * BK;
-                    const int lrow = (second ? a.lr0b : a.lr0) + tm * BM, urow = (second ? a.ur0b : a.ur0) + tn * BN;
+                    // the second operand pair sits at the same tile offsets from lr0b / ur0b
+                    const int lrow = second ? lrow1 - a.lr0 + a.lr0b : lrow1;
+                    const int urow = second ? urow1 - a.ur0 + a.ur0b : urow1;
                     mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-                    tma_load_2d(st, second ? &mapL2r : &mapLr, x, lrow, full0 + 8 * s);
-                    tma_load_2d(st + L_TILE, second ? &mapL2i : &mapLi, x, lrow, full0 + 8 * s);
+                    tma_load_2d(st, second ? &mapL2r : &mapLr, lx + x, lrow, full0 + 8 * s);
+                    tma_load_2d(st + L_TILE, second ? &mapL2i : &mapLi, lx + x, lrow, full0 + 8 * s);
                     tma_load_2d(st + 2 * L_TILE, second ? &mapU2r : &mapUr, x, urow, full0 + 8 * s);
                     tma_load_2d(st + 2 * L_TILE + U_TILE, second ? &mapU2i : &mapUi, x, urow, full0 + 8 * s);
                 }
@@ -287,13 +319,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t slot0 = epi_base + (uint32_t)(warp - 2) * 2 * SLOT_BYTES;
         uint32_t local = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
-            int tm, tn;
-            tile_of(t, tm, tn);
+            int lrow1, lx, urow1, crow, ccol;
+            place(t, lrow1, lx, urow1, crow, ccol);
             const uint32_t buf = local & 1, u = local >> 1;
             bool have = mbar_wait(tfull0 + 8 * buf, u & 1, abort_flag, gflags);
             if (!__all_sync(0xffffffffu, have)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int row = a.crow0 + tm * BM + q * 32, row2 = a.c2row0 + tm * BM + q * 32;
+            const int row = crow + q * 32, row2 = a.c2row0 + (crow - a.crow0) + q * 32;
             const float sgn = a.mode ? 1.f : -1.f;
 #pragma unroll 1
             for (int c = 0; c < BN / 32; ++c) {
@@ -310,7 +342,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         const uint32_t sa = rowaddr + ((uint32_t)(j ^ (lane & 7)) << 4);
                         float o0 = sgn * v[4 * j], o1 = sgn * v[4 * j + 1], o2 = sgn * v[4 * j + 2],
                               o3 = sgn * v[4 * j + 3];
-                        if (a.mode == 1) {  // W21 is the L operand of later updates: round it once, to nearest
+                        if (a.mode) {  // W21 is the L operand of later updates, U D^-1 of the pair fold:
+                                       // round it once, to nearest
                             o0 = tf32_rn(o0); o1 = tf32_rn(o1); o2 = tf32_rn(o2); o3 = tf32_rn(o3);
                         }
                         asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(o0), "f"(o1),
@@ -320,11 +353,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) {
-                        const int col = a.ccol0 + tn * BN + c * 32;
+                        const int col = ccol + c * 32;
                         if (a.mode) {
                             tma_store_2d(p ? &mapCi : &mapCr, col, row, slot);
                             if (a.mode == 1)
-                                tma_store_2d(p ? &mapC2i : &mapC2r, a.c2col0 + tn * BN + c * 32, row2, slot);
+                                tma_store_2d(p ? &mapC2i : &mapC2r, a.c2col0 + (ccol - a.ccol0) + c * 32, row2, slot);
                         } else {
                             tma_reduce_add_2d(p ? &mapCi : &mapCr, col, row, slot);
                         }
@@ -365,12 +398,12 @@ static EncodeTiledFn get_encode() {
     return fn;
 }
 
-// FP32 operand of rows x 128 columns (row stride ld floats), 32-column x
+// FP32 operand of rows x cols columns (row stride ld floats), 32-column x
 // box_rows boxes, 128-byte swizzle: one plane of an L or U operand.
-static bool make_map(CUtensorMap* m, const float* base, int rows, int ld, int box_rows) {
+static bool make_map(CUtensorMap* m, const float* base, int rows, int ld, int box_rows, int cols = 128) {
     EncodeTiledFn enc = get_encode();
     if (!enc) return false;
-    cuuint64_t dims[2] = {128, (cuuint64_t)rows};
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
     cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
@@ -516,6 +549,32 @@ bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, i
     const TcTiles a{lr_a, ur_a, Mt, Nt, lw, lskip, row0, col0, 0, 0, 0, npair, lr_b, ur_b};
     BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(
         mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mL2r, mL2i, mU2r, mU2i, a, flags));
+    return true;
+}
+
+// Pair fold of the block-unit triangular factors left in A by the LU (which = 1: the
+// block-lower L, which = 2: the block-upper U D^-1), over the pairs of 128-blocks
+// (2p, 2p+1):
+//   which 1:  L_{r,2p}   -= L_{r,2p+1} L_{2p+1,2p}     block rows r >= 2p + 2
+//   which 2:  U_{r,2p+1} -= U_{r,2p}   U_{2p,2p+1}     block rows r <  2p
+// T: the transposed pair blocks, [2 planes][np][128][128] (T[p][j][i] = L_{2p+1,2p}[i][j],
+// resp. U_{2p,2p+1}[i][j]).  Each launch reads only blocks it does not write.
+bool tc_pair_fold(cudaStream_t st, int n, CMat<float> A, const float* T, int which, int* flags) {
+    if (n % 128 || A.ld % 4 || (which != 1 && which != 2)) return false;
+    const int nblk = n / 128, np = nblk / 2;
+    long long ntiles = 0;
+    for (int p = 0; p < np; ++p) ntiles += which == 1 ? nblk - 2 * p - 2 : 2 * p;
+    if (ntiles <= 0) return true;
+    if (ntiles > (1LL << 30)) return false;
+    CUtensorMap mLr, mLi, mUr, mUi, mCr, mCi;
+    const size_t plane = (size_t)np * 128 * 128;
+    if (!make_map(&mLr, A.re, n, A.ld, BM, n) || !make_map(&mLi, A.im, n, A.ld, BM, n) ||
+        !make_map(&mUr, T, np * 128, 128, BN) || !make_map(&mUi, T + plane, np * 128, 128, BN) ||
+        !make_map_c(&mCr, A.re, n, n, A.ld) || !make_map_c(&mCi, A.im, n, n, A.ld))
+        return false;
+    const TcTiles a{0, 0, (int)ntiles, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, which, nblk};
+    BEM_LAUNCH(k_tc_update<<<tc_grid((int)ntiles, 0), NTHREADS, SMEM_BYTES, st>>>(
+        mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mLr, mLi, mUr, mUi, a, flags));
     return true;
 }
 

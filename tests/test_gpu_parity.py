@@ -222,7 +222,9 @@ def test_set_real_uses_frequency_over_two_pi(bg, orc):
 
 def test_dense_solve_plain_and_mixed(bg):
     rng = np.random.default_rng(3)
-    for n in (100, 300):
+    # padded sizes 128, 384, 768, 1152: one 128-block, then odd and even block counts (the
+    # triangular solves pair the 128-blocks; an odd count leaves the last one single)
+    for n in (100, 300, 700, 1100):
         A = 0.5 * np.eye(n) + 0.3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
         A += np.diag(np.sign(rng.standard_normal(n)) * 0.0)
         B = rng.standard_normal((n, 5)) + 1j * rng.standard_normal((n, 5))
