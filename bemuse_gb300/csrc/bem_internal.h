@@ -174,7 +174,8 @@ void launch_matx(cudaStream_t st, int N, int ld, const double* Mr, const double*
 // Same contract as launch_matx for a real matrix stored as float pairs
 // (M = Mhi + Mlo), in double-float arithmetic (products exact to ~2^-48,
 // compensated sums); the selected columns of X are split into float pairs first
-// (Xdf: N x R float4 scratch).
+// (Xdf: N x R float4 scratch).  Mlo = null: FP32 products of the high words, summed
+// in runs of 32 into float pairs (about 1e-7 relative; for the first refinement sweep).
 void launch_matx_df(cudaStream_t st, int N, int ld, const float* Mhi, const float* Mlo, int R, const double* X,
                     int xstride, int j0, float4* Xdf, double* part, double alpha, double beta, const double* base,
                     double* out, int ostride);

@@ -101,6 +101,9 @@ struct bem_ctx {
            *d_gmC = nullptr;
     double* h_gm = nullptr;
     int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
+    int refine_coarse_first = 1;  // 1: the first classic sweep's residual from the FP32 high words
+                                  // when the previous solve contracted weakly (last_contraction)
+    double last_contraction = 0.0;  // residual ratio of the last two full-accuracy sweeps
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
@@ -619,9 +622,19 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         }
         // out = beta base + alpha D x over the N rows (the refinement's FP64-accurate operator):
         // Re D x from the float pairs (double-float products), i Im D x from the plane waves
+        // coarse: Re D x from the high words only (about 1e-7 relative), enough for the first
+        // sweep's residual, which is about 1e-3 of y; the sweeps after it correct its error
+        // A coarse first residual leaves an error of about 1e-7 (times the condition number)
+        // in x2; with a contraction c per sweep the sweep count stays the same while c^2
+        // exceeds that, so it is used only when the previous solve of this context
+        // contracted by more than 3e-4 per sweep (neighbouring frequencies contract alike).
+        bool coarse = false;
+        const bool coarse_first =
+            ctx->refine_coarse_first && ctx->resid_mode >= 2 && ctx->last_contraction > 3e-4;
         auto apply_op = [&](const double* x, const double* base, double alpha, double beta, double* out) {
             if (ctx->resid_mode >= 2) {
-                bem::launch_matx_df(st, N, Np, F.Dhi, F.Dlo, R, x, R, 0, F.Xdf, F.mx, alpha, beta, base, out, R);
+                bem::launch_matx_df(st, N, Np, F.Dhi, coarse ? nullptr : F.Dlo, R, x, R, 0, F.Xdf, F.mx, alpha,
+                                    beta, base, out, R);
                 if (ctx->resid_mode == 3) {
                     const double c2 = F.pw_K * F.pw_K * 0.25 / 3.14159265358979323846;
                     bem::launch_pw_correct(st, N, F.pw_M, R, -alpha * 3.14159265358979323846 * c2 / F.pw_M, F.pwW,
@@ -662,7 +675,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             // frequency close to an irregular frequency of the body) hands x and its
             // residual over to flexible GMRES.
             std::vector<unsigned long long> hn(2 * R);
-            double prev = 0.0;
+            double prev = 0.0, prev_full = 0.0;
             for (;;) {
                 bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
                 ctx->solve_epoch += 2;
@@ -671,7 +684,9 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
                 bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
                 CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+                coarse = iters == 0 && coarse_first;
                 apply_op(ctx->d_X, F.Y, -1.0, 1.0, ctx->d_Rr);
+                coarse = false;
                 bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
                 CK(cudaGetLastError());
                 CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R,
@@ -686,7 +701,13 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     double rel = yn > 0 ? rn / yn : rn;
                     resid = std::max(resid, rel);
                 }
-                if (resid <= tol) break;
+                const bool full = !(iters == 1 && coarse_first);
+                if (full) {
+                    if (prev_full > 0.0) ctx->last_contraction = resid / prev_full;
+                    prev_full = resid;
+                }
+                // convergence is only ever accepted on a full-accuracy residual
+                if (resid <= tol && full) break;
                 if (iters >= max_iter || !(resid < 1e300)) {
                     if (iters_out) *iters_out = iters;
                     if (resid_out) *resid_out = resid;
@@ -1674,6 +1695,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_pair_update") {
         if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_pair_update must be 0 or 1");
         ctx->lu_pair_update = (int)value;
+        return BEM_OK;
+    }
+    if (k == "refine_coarse_first") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "refine_coarse_first must be 0 or 1");
+        ctx->refine_coarse_first = (int)value;
         return BEM_OK;
     }
     if (k == "refine_gmres") {

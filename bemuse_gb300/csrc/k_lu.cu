@@ -2292,6 +2292,80 @@ __global__ void __launch_bounds__(MXD_ROWS) k_matx_df(int N, int ld, const float
     }
 }
 
+__device__ __forceinline__ void df_add(DF& acc, float v) {
+    const float t = acc.s + v;
+    const float z = t - acc.s;
+    acc.c += (acc.s - (t - z)) + (v - z);
+    acc.s = t;
+}
+
+// The same product from the high words of the matrix and of X only, for a residual that
+// needs about 1e-7 relative accuracy (the first refinement sweep, whose residual is about
+// 1e-3 of the right-hand side; later sweeps correct what this one leaves): FP32 products
+// summed in FP32 over runs of 32 columns, each run added into a float pair.  A tenth of
+// the instructions of k_matx_df, and half its matrix bytes.
+template <int RR>
+__global__ void __launch_bounds__(MXD_ROWS) k_matx_f32(int N, int ld, const float* __restrict__ Mhi,
+                                                       const float4* __restrict__ Xdf, double* __restrict__ part) {
+    extern __shared__ float4 xs4[];  // [MXD_COLS][RR]
+    const int ct = blockIdx.y;
+    const int s0 = ct * MXD_COLS;
+    const int ns = min(MXD_COLS, N - s0);
+    for (int idx = threadIdx.x; idx < RR * MXD_COLS; idx += blockDim.x) {
+        const int k = idx / RR, j = idx % RR;
+        xs4[idx] = k < ns ? Xdf[(size_t)(s0 + k) * RR + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int r = blockIdx.x * MXD_ROWS + threadIdx.x;
+    if (r >= N) return;
+    DF ar[RR], ai[RR];
+#pragma unroll
+    for (int j = 0; j < RR; ++j) { ar[j] = DF{0.f, 0.f}; ai[j] = DF{0.f, 0.f}; }
+    const float* hrow = Mhi + (size_t)r * ld + s0;
+    constexpr int RUN = 32;
+    for (int k0 = 0; k0 < ns; k0 += RUN) {
+        float sr[RR], si[RR];
+#pragma unroll
+        for (int j = 0; j < RR; ++j) { sr[j] = 0.f; si[j] = 0.f; }
+        if (k0 + RUN <= ns) {
+#pragma unroll 1
+            for (int k = k0; k < k0 + RUN; k += 8) {
+                const float4 h0 = __ldg(reinterpret_cast<const float4*>(hrow + k));
+                const float4 h1 = __ldg(reinterpret_cast<const float4*>(hrow + k + 4));
+                const float dh[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    const float4* xk = xs4 + (k + kk) * RR;
+#pragma unroll
+                    for (int j = 0; j < RR; ++j) {
+                        const float4 x = xk[j];
+                        sr[j] = fmaf(dh[kk], x.x, sr[j]);
+                        si[j] = fmaf(dh[kk], x.z, si[j]);
+                    }
+                }
+            }
+        } else {
+            for (int k = k0; k < ns; ++k) {
+                const float dh = hrow[k];
+#pragma unroll
+                for (int j = 0; j < RR; ++j) {
+                    const float4 x = xs4[k * RR + j];
+                    sr[j] = fmaf(dh, x.x, sr[j]);
+                    si[j] = fmaf(dh, x.z, si[j]);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < RR; ++j) { df_add(ar[j], sr[j]); df_add(ai[j], si[j]); }
+    }
+#pragma unroll
+    for (int j = 0; j < RR; ++j) {
+        double* p = part + 2 * (((size_t)ct * N + r) * RR + j);
+        p[0] = (double)ar[j].s + (double)ar[j].c;
+        p[1] = (double)ai[j].s + (double)ai[j].c;
+    }
+}
+
 // Per-column max |Rres| and max |Y| (non-negative doubles compare as integers).
 __global__ void k_norms(int N, int R, const double* __restrict__ Rres, const double* __restrict__ Y,
                         unsigned long long* nrm) {
@@ -2366,6 +2440,12 @@ static void matx_df_rr(cudaStream_t st, int N, int ld, const float* Mhi, const f
                        double* part) {
     dim3 grd((N + MXD_ROWS - 1) / MXD_ROWS, (N + MXD_COLS - 1) / MXD_COLS);
     const size_t smem = sizeof(float4) * RR * MXD_COLS;
+    if (!Mlo) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_matx_f32<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        BEM_LAUNCH(k_matx_f32<RR><<<grd, MXD_ROWS, smem, st>>>(N, ld, Mhi, Xdf, part));
+        return;
+    }
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_matx_df<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     BEM_LAUNCH(k_matx_df<RR><<<grd, MXD_ROWS, smem, st>>>(N, ld, Mhi, Mlo, Xdf, part));
 }

@@ -275,6 +275,12 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     (restart 16) with the TF32 factors as preconditioner, which never
  *                     needs more preconditioner solves; 2 (default) classic sweeps while
  *                     each reduces the residual more than 20x, then GMRES from there.
+ *   "refine_coarse_first" 1 (default): when the previous solve of the context reduced
+ *                     its residual by less than 3e-4 per sweep, the residual of the first
+ *                     classic sweep (about 1e-3 of y) is formed from the FP32 high words of
+ *                     Re D (about 1e-7 relative), the later ones in double-float; the sweep
+ *                     count stays the same at such contraction, and convergence is only
+ *                     accepted on a double-float residual.  0: every residual double-float.
  *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation,
  *                     2 (default): the same with the next panel's pivot block inverted
  *                     by a dedicated warp beside each rank-8 update, 0: one pivot per

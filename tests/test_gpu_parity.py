@@ -143,6 +143,30 @@ def test_refinement_variants_agree_near_irregular_frequency(bg, orc):
     assert np.all(got[2]["iters"] <= got[0]["iters"] + 1)
 
 
+def test_coarse_first_residual_keeps_the_sweeps(bg, orc):
+    # The first sweep's residual from the FP32 high words of Re D (refine_coarse_first = 1,
+    # the default, used after a solve that contracted by less than 3e-4 per sweep) against
+    # every residual in double-float: the same residual test and the same results to the
+    # mixed-path tolerance.  Neighbouring frequencies contract alike, so the coarse
+    # residual adds at most one sweep where the contraction changes.
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    om = np.array([0.7, 0.8, 1.0, 1.2, 2.0])
+    s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL), precision=bg.MIXED)
+    ref = _oracle_solve(orc, m, aux, om, cases.BETAS, s)
+    got = {}
+    for coarse in (0, 1):
+        s.set_tuning("refine_coarse_first", coarse)
+        got[coarse] = s.solve_omegas(om)
+        print("refine_coarse_first", coarse, "iterations", got[coarse]["iters"], "residual",
+              got[coarse]["residual"].max())
+        assert np.all(got[coarse]["residual"] <= 1e-12)
+        _compare(got[coarse], ref, 1e-6)
+    assert np.all(got[1]["iters"] <= got[0]["iters"] + 1)
+    assert got[1]["iters"].sum() <= got[0]["iters"].sum() + 1
+    with pytest.raises(bg.BEMError):
+        s.set_tuning("refine_coarse_first", 2)
+
+
 def test_lu_schedule_variants_agree(bg):
     # 1200 panels: the TF32 LU has 10 block steps, so the paired schedule runs four full
     # pairs and a final single step.  Every schedule / inverse variant must meet the
