@@ -2302,67 +2302,89 @@ __device__ __forceinline__ void df_add(DF& acc, float v) {
 // The same product from the high words of the matrix and of X only, for a residual that
 // needs about 1e-7 relative accuracy (the first refinement sweep, whose residual is about
 // 1e-3 of the right-hand side; later sweeps correct what this one leaves): FP32 products
-// summed in FP32 over runs of 32 columns, each run added into a float pair.  A tenth of
-// the instructions of k_matx_df, and half its matrix bytes.
+// summed in FP32 over runs of 32 columns, each run added into a float pair.  A thread
+// takes two rows (r, r + 128), so each staged x word (the high words of re and im, 8
+// bytes) feeds four FMAs; a tenth of the instructions of k_matx_df, half its matrix bytes.
 template <int RR>
 __global__ void __launch_bounds__(MXD_ROWS) k_matx_f32(int N, int ld, const float* __restrict__ Mhi,
                                                        const float4* __restrict__ Xdf, double* __restrict__ part) {
-    extern __shared__ float4 xs4[];  // [MXD_COLS][RR]
+    extern __shared__ float2 xs2[];  // [MXD_COLS][RR]
     const int ct = blockIdx.y;
     const int s0 = ct * MXD_COLS;
     const int ns = min(MXD_COLS, N - s0);
     for (int idx = threadIdx.x; idx < RR * MXD_COLS; idx += blockDim.x) {
         const int k = idx / RR, j = idx % RR;
-        xs4[idx] = k < ns ? Xdf[(size_t)(s0 + k) * RR + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (k < ns) {
+            const float4 x = Xdf[(size_t)(s0 + k) * RR + j];
+            v = make_float2(x.x, x.z);
+        }
+        xs2[idx] = v;
     }
     __syncthreads();
-    const int r = blockIdx.x * MXD_ROWS + threadIdx.x;
-    if (r >= N) return;
-    DF ar[RR], ai[RR];
+    const int r0 = blockIdx.x * 2 * MXD_ROWS + threadIdx.x, r1 = r0 + MXD_ROWS;
+    if (r0 >= N) return;
+    const bool two = r1 < N;
+    DF a0r[RR], a0i[RR], a1r[RR], a1i[RR];
 #pragma unroll
-    for (int j = 0; j < RR; ++j) { ar[j] = DF{0.f, 0.f}; ai[j] = DF{0.f, 0.f}; }
-    const float* hrow = Mhi + (size_t)r * ld + s0;
+    for (int j = 0; j < RR; ++j) {
+        a0r[j] = DF{0.f, 0.f}; a0i[j] = DF{0.f, 0.f}; a1r[j] = DF{0.f, 0.f}; a1i[j] = DF{0.f, 0.f};
+    }
+    const float* h0 = Mhi + (size_t)r0 * ld + s0;
+    const float* h1 = Mhi + (size_t)(two ? r1 : r0) * ld + s0;
     constexpr int RUN = 32;
     for (int k0 = 0; k0 < ns; k0 += RUN) {
-        float sr[RR], si[RR];
+        float s0r[RR], s0i[RR], s1r[RR], s1i[RR];
 #pragma unroll
-        for (int j = 0; j < RR; ++j) { sr[j] = 0.f; si[j] = 0.f; }
+        for (int j = 0; j < RR; ++j) { s0r[j] = 0.f; s0i[j] = 0.f; s1r[j] = 0.f; s1i[j] = 0.f; }
         if (k0 + RUN <= ns) {
 #pragma unroll 1
-            for (int k = k0; k < k0 + RUN; k += 8) {
-                const float4 h0 = __ldg(reinterpret_cast<const float4*>(hrow + k));
-                const float4 h1 = __ldg(reinterpret_cast<const float4*>(hrow + k + 4));
-                const float dh[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+            for (int k = k0; k < k0 + RUN; k += 4) {
+                const float4 p = __ldg(reinterpret_cast<const float4*>(h0 + k));
+                const float4 q = __ldg(reinterpret_cast<const float4*>(h1 + k));
+                const float d0[4] = {p.x, p.y, p.z, p.w}, d1[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-                for (int kk = 0; kk < 8; ++kk) {
-                    const float4* xk = xs4 + (k + kk) * RR;
+                for (int kk = 0; kk < 4; ++kk) {
+                    const float2* xk = xs2 + (k + kk) * RR;
 #pragma unroll
                     for (int j = 0; j < RR; ++j) {
-                        const float4 x = xk[j];
-                        sr[j] = fmaf(dh[kk], x.x, sr[j]);
-                        si[j] = fmaf(dh[kk], x.z, si[j]);
+                        const float2 x = xk[j];
+                        s0r[j] = fmaf(d0[kk], x.x, s0r[j]);
+                        s0i[j] = fmaf(d0[kk], x.y, s0i[j]);
+                        s1r[j] = fmaf(d1[kk], x.x, s1r[j]);
+                        s1i[j] = fmaf(d1[kk], x.y, s1i[j]);
                     }
                 }
             }
         } else {
             for (int k = k0; k < ns; ++k) {
-                const float dh = hrow[k];
+                const float d0 = h0[k], d1 = h1[k];
 #pragma unroll
                 for (int j = 0; j < RR; ++j) {
-                    const float4 x = xs4[k * RR + j];
-                    sr[j] = fmaf(dh, x.x, sr[j]);
-                    si[j] = fmaf(dh, x.z, si[j]);
+                    const float2 x = xs2[k * RR + j];
+                    s0r[j] = fmaf(d0, x.x, s0r[j]);
+                    s0i[j] = fmaf(d0, x.y, s0i[j]);
+                    s1r[j] = fmaf(d1, x.x, s1r[j]);
+                    s1i[j] = fmaf(d1, x.y, s1i[j]);
                 }
             }
         }
 #pragma unroll
-        for (int j = 0; j < RR; ++j) { df_add(ar[j], sr[j]); df_add(ai[j], si[j]); }
+        for (int j = 0; j < RR; ++j) {
+            df_add(a0r[j], s0r[j]); df_add(a0i[j], s0i[j]);
+            df_add(a1r[j], s1r[j]); df_add(a1i[j], s1i[j]);
+        }
     }
 #pragma unroll
     for (int j = 0; j < RR; ++j) {
-        double* p = part + 2 * (((size_t)ct * N + r) * RR + j);
-        p[0] = (double)ar[j].s + (double)ar[j].c;
-        p[1] = (double)ai[j].s + (double)ai[j].c;
+        double* p = part + 2 * (((size_t)ct * N + r0) * RR + j);
+        p[0] = (double)a0r[j].s + (double)a0r[j].c;
+        p[1] = (double)a0i[j].s + (double)a0i[j].c;
+        if (two) {
+            double* q = part + 2 * (((size_t)ct * N + r1) * RR + j);
+            q[0] = (double)a1r[j].s + (double)a1r[j].c;
+            q[1] = (double)a1i[j].s + (double)a1i[j].c;
+        }
     }
 }
 
@@ -2441,9 +2463,11 @@ static void matx_df_rr(cudaStream_t st, int N, int ld, const float* Mhi, const f
     dim3 grd((N + MXD_ROWS - 1) / MXD_ROWS, (N + MXD_COLS - 1) / MXD_COLS);
     const size_t smem = sizeof(float4) * RR * MXD_COLS;
     if (!Mlo) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_matx_f32<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        BEM_LAUNCH(k_matx_f32<RR><<<grd, MXD_ROWS, smem, st>>>(N, ld, Mhi, Xdf, part));
+        const size_t smem2 = sizeof(float2) * RR * MXD_COLS;
+        const dim3 grd2((N + 2 * MXD_ROWS - 1) / (2 * MXD_ROWS), (N + MXD_COLS - 1) / MXD_COLS);
+        if (smem2 > 48 * 1024)
+            cudaFuncSetAttribute(k_matx_f32<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+        BEM_LAUNCH(k_matx_f32<RR><<<grd2, MXD_ROWS, smem2, st>>>(N, ld, Mhi, Xdf, part));
         return;
     }
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_matx_df<RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
