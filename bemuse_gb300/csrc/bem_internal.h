@@ -157,9 +157,11 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
 int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float> A, float* invr, float* invi,
                          float* wl4, float* wut4, int* flags);
 // Forward/back substitution with the factors: X (n x R, interleaved complex) in place,
-// with an n x R scratch right after X.  ready: n/nb ints zeroed at allocation; epoch
+// with an n x R scratch right after X.  ready: zeroed at allocation, n/64 ints for the
+// FP64 solve, n/8 + 1 for the FP32 one (sub-block flags and a ticket counter); epoch
 // strictly increasing across calls on the same ready array (each call uses epoch and
-// epoch + 1).  Returns nonzero if the cooperative launch failed.
+// epoch + 1).  The FP32 solve expects the pair-folded factors of lu_pair_fold.
+// Returns nonzero if a launch failed.
 int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
                  int* ready, int epoch, int* flags);
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,

@@ -1,6 +1,8 @@
 // k_tc_gemm.cu -- tcgen05 TF32 products of the complex block LU:
 //     A22 -= L21 * U12      (trailing update; planar complex, FP32 storage and accumulation)
 //     W21  = A21 * D^-1     (block-column multipliers, stored to two places)
+//     U   <- U * D^-1       (column blocks of U, for the backward solve)
+//     the pair fold of both factors after the factorization (tc_pair_fold)
 //
 // Persistent, warp-specialised kernel over 128 x 128 tiles of A22 (or of any
 // tile-aligned rectangle of it).  The complex product is four real TF32 MMAs
