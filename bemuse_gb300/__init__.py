@@ -29,6 +29,7 @@ _STATUS = {0: "BEM_OK", 1: "BEM_ERR_ARG", 2: "BEM_ERR_CUDA", 3: "BEM_ERR_STATE",
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 
 class BEMError(RuntimeError):
@@ -129,7 +130,8 @@ def lib():
         "bem_mesh_wing": ([c_double, c_double, c_double, c_int, c_int, c_int, _dp, _ip], c_int),
         "bem_aero_setup": ([vp, ctypes.POINTER(_Mesh)], c_int),
         "bem_aero_solve": ([vp, c_int, _dp, c_int, c_double, _dp, _dp], c_int),
-        "bem_selftest_tc": ([c_int, c_int], c_double),
+        "bem_fp32_peak": ([c_int, _dp], c_int),
+        "bem_tc_probe": ([c_int, c_int, c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -412,6 +414,7 @@ class Hydrodynamic_Radiation_Solver:
         self.Grav = 9.81
         self.BetaArray = []
         self.Frequency = 0.0
+        self.N, self.NBeta = 0, 0  # set by Setup
         self.mass = 0.0
         self.cog = np.zeros(3)
         self.gyration = np.zeros((3, 3))
@@ -764,9 +767,32 @@ def launch_count():
     return int(lib().bem_launch_count())
 
 
-def selftest_tc(n=1024, device=0):
-    """Tensor-core trailing update vs the FP32 CUDA-core update (relative max diff)."""
-    return float(lib().bem_selftest_tc(int(device), int(n)))
+def fp32_peak(device=0):
+    """Measured FP32 FMA throughput of the device in TFLOP/s (bem_fp32_peak)."""
+    t = ctypes.c_double()
+    _check(lib().bem_fp32_peak(int(device), ctypes.byref(t)))
+    return t.value
+
+
+def _planar32(z):
+    z = np.asarray(z)
+    return np.ascontiguousarray(np.stack([z.real, z.imag]).astype(np.float32))
+
+
+def tc_probe(mode, C, Wa=None, Ua=None, Wb=None, Ub=None, T=None, device=0):
+    """One launch of the tensor-core product kernel in tile mode `mode` (bem_tc_probe)
+    on complex operands (C n x n; Wa, Ua, Wb, Ub n x 128; T 128 x 128 or
+    (n / 256) x 128 x 128), stored as FP32 planes.  Returns the updated C and, for
+    mode 3, the second destination W (n x 128)."""
+    n = C.shape[0]
+    c = _planar32(C)
+    ops = [None if x is None else _planar32(x) for x in (Wa, Ua, Wb, Ub, T)]
+    w = np.zeros((2, n, 128), np.float32)
+    fp = lambda a: None if a is None else a.ctypes.data_as(_fp)
+    st = lib().bem_tc_probe(int(device), int(mode), int(n), fp(c), *[fp(x) for x in ops], fp(w))
+    if st != 0:
+        raise BEMError(st, lib().bem_last_error(None).decode())
+    return c[0] + 1j * c[1].astype(np.float64), w[0] + 1j * w[1].astype(np.float64)
 
 
 def dense_solve(A, B, precision=PLAIN_FP64, refine_tol=1e-12, device=0):

@@ -164,8 +164,10 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
 // Returns nonzero if a launch failed.
 int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, const double* invi, int R, double* X,
                  int* ready, int epoch, int* flags);
+// wait_skew / wait_ns: the chain's waits ask for epoch + wait_skew and give up wait_ns
+// after a CTA starts (FLAG_TIMEOUT); wait_skew > 0 is for failure-detection tests only.
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
-                 int* ready, int epoch, int* flags);
+                 int* ready, int epoch, int* flags, int wait_skew = 0, unsigned long long wait_ns = 2000000000ull);
 // out[:, j0:j0+R] = beta * base[:, j0:j0+R] + alpha * M X[:, j0:j0+R] for an N x N
 // row-major matrix M (real if Mi is null, else planar complex), X, base, out
 // N x stride complex interleaved.  part: scratch of matx_part_doubles(N, R) doubles.
@@ -202,10 +204,13 @@ void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
 
 int tc_gemm_supported(int device);
+// Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA), or < 0 on failure.
+double ffma_peak_tflops(int device);
 // Sets the message returned by bem_last_error(NULL).
 void set_static_error(const char* msg);
-// C -= L U^T-trailing update on random data with the tensor-core and SIMT kernels;
-// returns max |tc - simt| / max |simt| (negative on setup failure).
-double tc_selftest(int device, int n);
+// One k_tc_update launch in tile mode `mode` on host data (bem_tc_probe); 0 on
+// success, -1 with a message in err otherwise.
+int tc_probe(int device, int mode, int n, float* C, const float* Wa, const float* Ua, const float* Wb,
+             const float* Ub, const float* T, float* Wout, char* err, int err_len);
 
 }  // namespace bem

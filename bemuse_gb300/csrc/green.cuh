@@ -8,8 +8,9 @@
 // with h = sqrt(x^2+y^2), d = sqrt(h^2+v^2), alpha = -v/d, beta = h/d,
 // rho = d/(1+d).  L0 and Ls use the polynomial fits of Liang, Wu & Noblesse,
 // Appl. Ocean Res. 74 (2018), eq. 14a-c / 16a-c; H0/H1 the Struve fits of
-// Kernels.cpp:35-116.  J0/J1/Y0/Y1 are CUDA's j0/j1/y0/y1 (FP64) and
-// j0f/j1f/y0f/y1f (FP32).
+// Kernels.cpp:35-116.  J0/J1/Y0/Y1 are CUDA's j0/j1/y0/y1 in FP64; in FP32
+// they are the Abramowitz & Stegun 9.4.1-9.4.6 polynomial forms below
+// (bessel_j01_small, bessel_large), not CUDA's j0f/j1f/y0f/y1f.
 //
 // gf64: FP64, same operation order as the reference (a common subexpression
 //       e^v is computed once; the reference recomputes the same value).
@@ -51,9 +52,18 @@ struct PolyCoef64 {
 };
 
 // Shifted-basis coefficients for FP32: p(rho) = sum_k s_k (rho - 1/2)^k.
+// h1s, h1d: the two forms of 2/pi - H1(x) that dG/dh needs (h1_gap32).
 struct PolyCoef32 {
     float A[10], B[10], C[10], D[10], dA[10], dB[10], dC[10];
+    float h1s[7];  // x <= 3: 2/pi - (x/3)^2 P((x/3)^2) as a polynomial in t = x^2 - 9/2
+    float h1d[4];  // x > 3: (2/pi) c2 - c1 of Kernels.cpp:95-97 in (3/x)^2, leading terms cancelled
 };
+
+// The reference's StruveH1 constants (Kernels.cpp:76-116): small-argument series
+// coefficients and the large-argument rational c1 / c2.
+#define BEM_H1_SMALL 1.909859286, -1.145914713, 0.294656958, -0.042070508, 0.003785727, -0.000207183
+#define BEM_H1_C1 1.00000004, 3.92205313, 2.64893033, 0.27450895
+#define BEM_H1_C2 1.0, 3.81095112, 2.26216956, 0.10885141
 
 __device__ __forceinline__ float horner32(const float* s, int n, float u) {
     float r = s[n - 1];
@@ -147,16 +157,26 @@ __device__ __forceinline__ float struve_h0_32(float x, float y0x) {
     float c2 = 3.14159265f * x * fmaf(fmaf(fmaf(0.52120508f, yy, 4.28957333f), yy, 4.88331068f), yy, 1.0f);
     return __fdividef(c1, c2) + y0x;
 }
-__device__ __forceinline__ float struve_h1_32(float x, float y1x) {
+// 2/pi - H1(x), which dG/dh multiplies by 2 pi e^v.  H1 tends to 2/pi, so the
+// plain difference of two FP32 values loses several bits (about 1e-6 of dG/dh
+// near h ~ 2.5 and h ~ 8).  The same function is evaluated without that
+// cancellation: for x <= 3 the series 2/pi - yy P(yy), yy = (x/3)^2, re-expanded
+// about yy = 1/2 with t = x^2 - 9/2 formed by one FMA; for x > 3,
+// 2/pi - c1/c2 = ((2/pi) c2 - c1) / c2 with the numerator's coefficients
+// subtracted exactly on the host, so only Y1 is added to a small, accurate term.
+__device__ __forceinline__ float h1_gap32(const PolyCoef32& P, float x, float y1x) {
     if (x <= 3.0f) {
-        float yy = (x * (1.0f / 3.0f)) * (x * (1.0f / 3.0f));
-        return fmaf(fmaf(fmaf(fmaf(fmaf(-0.000207183f, yy, 0.003785727f), yy, -0.042070508f), yy, 0.294656958f), yy, -1.145914713f), yy, 1.909859286f) * yy;
+        const float t = fmaf(x, x, -4.5f);
+        float r = P.h1s[6];
+#pragma unroll
+        for (int k = 5; k >= 0; --k) r = fmaf(r, t, P.h1s[k]);
+        return r;
     }
-    float r = 3.0f / x;
-    float yy = r * r;
-    float c1 = 2.0f * fmaf(fmaf(fmaf(0.27450895f, yy, 2.64893033f), yy, 3.92205313f), yy, 1.00000004f);
-    float c2 = 3.14159265f * fmaf(fmaf(fmaf(0.10885141f, yy, 2.26216956f), yy, 3.81095112f), yy, 1.0f);
-    return __fdividef(c1, c2) + y1x;
+    const float r = 3.0f / x;
+    const float yy = r * r;
+    const float num = fmaf(fmaf(fmaf(P.h1d[3], yy, P.h1d[2]), yy, P.h1d[1]), yy, P.h1d[0]);
+    const float c2 = 3.14159265f * fmaf(fmaf(fmaf(0.10885141f, yy, 2.26216956f), yy, 3.81095112f), yy, 1.0f);
+    return __fdividef(num, c2) - y1x;
 }
 
 // ---- FP32 Bessel functions J0, J1, Y0, Y1 -----------------------------------
@@ -260,7 +280,7 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
     if (far) bessel_large(hh, 0.0f, j0v, j1v, y0v, y1v);
     else bessel_j01_small(hh, j0v, j1v);
-    float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
+    float H0 = struve_h0_32(hh, y0v), H1g = h1_gap32(P, hh, y1v);
     float E = 2.0f * PI * ev;
     G.re = fmaf(E, H0, L0);
     G.im = -E * j0v;
@@ -274,15 +294,17 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float RS = beta * a2 - (1.0f - alpha) * b2;
     RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
     float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);
-    Gh.re = fmaf(E, 0.636619772f - H1, Ls);
+    Gh.re = fmaf(E, H1g, Ls);
     Gh.im = E * j1v;
 }
 
 // ---- FP32 real parts + imaginary-part remainders ----------------------------
 // Real parts of G and dG/dh (as gf32 computes them).
 // y0v, y1v: Y0(hh), Y1(hh) (used when hh > 3).
+// Gv: dG/dv ~ Gr - 2/d (to about 1 %: the infinite-depth wave term satisfies dG/dv = G
+// up to the Rankine image's 2/d), used for the first-order correction of the rounding of v.
 __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float y0v, float y1v,
-                                        float& Gr, float& Ghr) {
+                                        float& Gr, float& Ghr, float& Gv) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
@@ -305,9 +327,10 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     RR = fmaf(beta * (1.0f - beta), D, RR);
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
-    float H0 = struve_h0_32(hh, y0v), H1 = struve_h1_32(hh, y1v);
+    float H0 = struve_h0_32(hh, y0v), H1g = h1_gap32(P, hh, y1v);
     float E = 2.0f * PI * ev;
     Gr = fmaf(E, H0, L0);
+    Gv = fmaf(-2.0f, inv_d, Gr);
     float PS = __fdividef(beta + hh, dmv);
     PS -= 2.0f * beta;
     PS = fmaf(2.0f * dd, ev, PS);
@@ -318,7 +341,7 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     float RS = beta * a2 - (1.0f - alpha) * b2;
     RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
     float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);
-    Ghr = fmaf(E, 0.636619772f - H1, Ls);
+    Ghr = fmaf(E, H1g, Ls);
 }
 
 }  // namespace bem

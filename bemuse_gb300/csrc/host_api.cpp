@@ -102,6 +102,11 @@ struct bem_ctx {
     double* h_gm = nullptr;
     int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
     int refine_coarse_first = 1;  // 1: the first classic sweep's residual from the FP32 high words
+    int refine_max = 60;          // preconditioner solves the refinement may use before it fails
+    // failure-detection tests only: the triangular-solve chain waits for a flag value that
+    // nothing publishes (test_wait_skew > 0) and gives up after test_wait_ns
+    int test_wait_skew = 0;
+    unsigned long long test_wait_ns = 2000000000ull;
                                   // when the previous solve contracted weakly (last_contraction)
     double last_contraction = 0.0;  // residual ratio of the last two full-accuracy sweeps
     // mixed-precision wave assembly
@@ -413,8 +418,12 @@ bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double
             bem::launch_gm_scale(st, Np, R, W, hn, V + (size_t)(j + 1) * vs);
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(hh, h1, sizeof(double) * hblock, cudaMemcpyDeviceToHost, st));
+            int it_flags = 0;
+            CK(cudaMemcpyAsync(&it_flags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             ++iters;
+            if (it_flags & bem::FLAG_TIMEOUT)
+                return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the triangular solve expired");
             double est = 0.0;
             for (int r = 0; r < R; ++r) {
                 for (int i = 0; i <= j; ++i) {
@@ -650,7 +659,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             bem::launch_to_f32(st, nr2, v, ctx->d_X32);
             ctx->solve_epoch += 2;
             if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
-                                  ctx->solve_epoch - 1, ctx->d_flags))
+                                  ctx->solve_epoch - 1, ctx->d_flags, ctx->test_wait_skew, ctx->test_wait_ns))
                 return fail(ctx, BEM_ERR_CUDA, "triangular-solve launch failed");
             bem::launch_f32_to_f64(st, nr2, ctx->d_X32, z);
             return BEM_OK;
@@ -680,7 +689,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
                 ctx->solve_epoch += 2;
                 if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
-                                      ctx->solve_epoch - 1, ctx->d_flags))
+                                      ctx->solve_epoch - 1, ctx->d_flags, ctx->test_wait_skew, ctx->test_wait_ns))
                     return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
                 bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
                 CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
@@ -691,8 +700,14 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 CK(cudaGetLastError());
                 CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R,
                                    cudaMemcpyDeviceToHost, st));
+                int sweep_flags = 0;
+                CK(cudaMemcpyAsync(&sweep_flags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
                 ++iters;
+                // an expired device wait leaves this sweep's solve unfinished: report it as the
+                // CUDA-side failure it is, not as a refinement that failed to converge
+                if (sweep_flags & bem::FLAG_TIMEOUT)
+                    return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the triangular solve expired");
                 resid = 0.0;
                 for (int j = 0; j < R; ++j) {
                     double rn, yn;
@@ -770,7 +785,15 @@ const char* bem_version(void) { return "bemgpu 0.1 (sm_103a)"; }
 
 unsigned long long bem_launch_count(void) { return bem::g_launches.load(); }
 
-double bem_selftest_tc(int device, int n) { return bem::tc_selftest(device, n); }
+bem_status bem_tc_probe(int device, int mode, int n, float* C, const float* Wa, const float* Ua, const float* Wb,
+                        const float* Ub, const float* T, float* Wout) {
+    char err[256];
+    if (bem::tc_probe(device, mode, n, C, Wa, Ua, Wb, Ub, T, Wout, err, sizeof(err)) != 0) {
+        bem::set_static_error((std::string("bem_tc_probe: ") + err).c_str());
+        return BEM_ERR_ARG;
+    }
+    return BEM_OK;
+}
 
 const char* bem_last_error(const bem_ctx* ctx) { return ctx ? ctx->err.c_str() : g_static_err; }
 
@@ -1272,7 +1295,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         double resid = 0;
         double t_lu = 0, t_sv = 0;
         ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
-        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, 60, &iters, &resid, &t_lu, &t_sv, next_asm);
+        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, ctx->refine_max, &iters, &resid, &t_lu, &t_sv, next_asm);
         ctx->resid_mode = 0;
         if (s != BEM_OK) {
             if (pipe) cudaStreamSynchronize(sa);
@@ -1518,6 +1541,14 @@ bem_status bem_havelock_throughput(int device, int n, int precision, double* eva
     return BEM_OK;
 }
 
+bem_status bem_fp32_peak(int device, double* tflops) {
+    if (!tflops) return fail(nullptr, BEM_ERR_ARG, "bem_fp32_peak: null output");
+    const double t = bem::ffma_peak_tflops(device);
+    if (!(t > 0)) return fail(nullptr, BEM_ERR_CUDA, "bem_fp32_peak: the FMA probe failed");
+    *tflops = t;
+    return BEM_OK;
+}
+
 bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, double* B, int precision, double tol,
                            int* iters, double* resid) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
@@ -1554,7 +1585,7 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
         bem::launch_to_f32(st, (size_t)Np * Np, ctx->d_D64i, ctx->fs[0].D32i);
     }
     double t0 = 0, t1 = 0;
-    s = factor_and_solve(ctx, ctx->fs[0], n, Np, nrhs, mixed, tol, 60, iters, resid, &t0, &t1);
+    s = factor_and_solve(ctx, ctx->fs[0], n, Np, nrhs, mixed, tol, ctx->refine_max, iters, resid, &t0, &t1);
     if (s != BEM_OK) { free_all(ctx); return s; }
     cudaError_t e = cudaMemcpyAsync(B, ctx->d_X, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1650,7 +1681,7 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
     int iters = 0;
     double resid = 0, t0 = 0, t1 = 0;
     ctx->resid_mode = mixed ? 1 : 0;
-    s = factor_and_solve(ctx, ctx->fs[0], N, Np, 1, mixed, tol, 60, &iters, &resid, &t0, &t1);
+    s = factor_and_solve(ctx, ctx->fs[0], N, Np, 1, mixed, tol, ctx->refine_max, &iters, &resid, &t0, &t1);
     ctx->resid_mode = 0;
     if (s != BEM_OK) return s;
     std::vector<double> x(2 * (size_t)N);
@@ -1700,6 +1731,22 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "refine_coarse_first") {
         if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "refine_coarse_first must be 0 or 1");
         ctx->refine_coarse_first = (int)value;
+        return BEM_OK;
+    }
+    if (k == "refine_max_solves") {
+        if (!(value >= 0 && value <= 10000 && value == (int)value))
+            return fail(ctx, BEM_ERR_ARG, "refine_max_solves must be an integer in [0, 10000]");
+        ctx->refine_max = (int)value;
+        return BEM_OK;
+    }
+    if (k == "test_wait_skew") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "test_wait_skew must be 0 or 1");
+        ctx->test_wait_skew = (int)value;
+        return BEM_OK;
+    }
+    if (k == "test_wait_ms") {
+        if (!(value >= 0.01 && value <= 2000)) return fail(ctx, BEM_ERR_ARG, "test_wait_ms must be in [0.01, 2000]");
+        ctx->test_wait_ns = (unsigned long long)(value * 1e6);
         return BEM_OK;
     }
     if (k == "refine_gmres") {

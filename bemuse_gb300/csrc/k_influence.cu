@@ -277,18 +277,30 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
                     float bx = sx - xh, by = sy - yh;
                     const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - __ldg(g + 7 * fs));
                     const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - __ldg(g + 8 * fs));
-                    float dz = (zh - __ldg(g + 2 * fs)) + (zl - __ldg(g + 9 * fs));
+                    // v = K (z_r - z_q) as a float pair (VV, vl), like h = (hh, hl)
+                    const float gz = __ldg(g + 2 * fs);
+                    const float sz = zh - gz;
+                    const float bz = sz - zh;
+                    const float ez = ((zh - (sz - bz)) - (gz + bz)) + (zl - __ldg(g + 9 * fs));
                     float w = __ldg(g + 3 * fs), nx = __ldg(g + 4 * fs), ny = __ldg(g + 5 * fs),
                           nz = __ldg(g + 6 * fs);
-                    float XX = (sx + lx) * K, YY = (sy + ly) * K, VV = dz * K;
+                    const float vh = sz * Kh;
+                    const float vlo = fmaf(sz, Kh, -vh) + fmaf(sz, Kl, ez * Kh);
+                    const float VV = vh + vlo;
+                    const float vl = vlo - (VV - vh);
+                    float XX = (sx + lx) * K, YY = (sy + ly) * K;
                     float hh, hl;
                     df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
                     float ev = expf(VV);
                     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
                     if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
                     else bessel_j01_small(hh, j0v, j1v);
-                    float Gr, Ghr;
-                    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr);
+                    float Gr, Ghr, Gv;
+                    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr, Gv);
+                    // G at the unrounded (h, v): the first-order terms of the float pairs' low
+                    // parts.  The radiation damping is a small difference of terms that each
+                    // carry this rounding, so without it B loses ~1e-6 at the highest frequencies.
+                    Gr = fmaf(Ghr, hl, fmaf(Gv, vl, Gr));
                     float proj = fmaf(XX, nx, YY * ny);
                     float dgr = 0.f, dgi = 0.f;
                     if (hh > 1.0e-6f) {
@@ -767,6 +779,52 @@ __global__ void k_havelock(int n, const double* __restrict__ x, const double* __
 // Host launchers
 static bool g_poly_ready[64] = {false};
 
+// FP32 FMA throughput probe (the roofline denominator of the FP32-bound assembly):
+// every thread runs 8 independent FMA chains of `iters` steps, x <- x a + b, with
+// a, b chosen so the values stay bounded.  The result is stored only when it
+// equals `never`, which it does not, so the chains cannot be removed.
+__global__ void __launch_bounds__(256) k_ffma_peak(int iters, float a, float b, float never, float* out) {
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (float)(threadIdx.x + k) * 1e-3f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+        }
+    }
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum += x[k];
+    if (sum == never) out[blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+double ffma_peak_tflops(int device) {
+    if (cudaSetDevice(device) != cudaSuccess) return -1.0;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    float* out = nullptr;
+    if (cudaMalloc(&out, sizeof(float) * 256 * 8 * (size_t)nsm) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int iters = 4096, grid = 8 * nsm;
+    BEM_LAUNCH(k_ffma_peak<<<grid, 256>>>(iters, 0.9999f, 1e-4f, -12345.f, out));  // warm-up
+    cudaEventRecord(e0);
+    for (int r = 0; r < 5; ++r) BEM_LAUNCH(k_ffma_peak<<<grid, 256>>>(iters, 0.9999f, 1e-4f, -12345.f, out));
+    cudaEventRecord(e1);
+    float ms = 0.f;
+    const bool ok = cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    cudaGetLastError();
+    if (!ok || ms <= 0.f) return -1.0;
+    const double flops = 5.0 * 2.0 * 8.0 * 16.0 * iters * (double)grid * 256.0;
+    return flops / (ms * 1e-3) / 1e12;
+}
+
 cudaError_t upload_poly_constants(int device) {
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
     if (g_poly_ready[device]) return cudaSuccess;
@@ -795,6 +853,25 @@ cudaError_t upload_poly_constants(int device) {
     }
     BEM_POLY_TABLE(BEM_FILL)
 #undef BEM_FILL
+    {
+        // 2/pi - H1 (h1_gap32): x <= 3, q(yy) = 2/pi - yy P(yy) re-expanded about yy = 1/2 and
+        // rescaled to t = x^2 - 9/2 = 9 (yy - 1/2); x > 3, (2/pi) c2 - c1 coefficient by coefficient
+        const double hs[6] = {BEM_H1_SMALL}, c1[4] = {BEM_H1_C1}, c2[4] = {BEM_H1_C2};
+        long double q[7];
+        q[0] = 2.0L / 3.14159265358979323846L;
+        for (int i = 0; i < 6; ++i) q[i + 1] = -(long double)hs[i];
+        for (int j = 0; j < 7; ++j) {
+            long double a = 0;
+            for (int i = j; i < 7; ++i) {
+                long double bin = 1;
+                for (int t = 0; t < j; ++t) bin = bin * (i - t) / (t + 1);
+                a += q[i] * bin * powl(0.5L, i - j);
+            }
+            p32.h1s[j] = (float)(a / powl(9.0L, j));
+        }
+        for (int i = 0; i < 4; ++i)
+            p32.h1d[i] = (float)(2.0L * ((long double)c2[i] - (long double)c1[i]));
+    }
     cudaError_t e = cudaMemcpyToSymbol(c_poly64, &p64, sizeof(p64));
     if (e != cudaSuccess) return e;
     e = cudaMemcpyToSymbol(c_poly32, &p32, sizeof(p32));

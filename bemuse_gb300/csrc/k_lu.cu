@@ -1504,72 +1504,6 @@ int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* 
     return lu_factor_t<double, 64>(st, n, A, invr, invi, wl, flags);
 }
 
-// Self-test of the tensor-core trailing update: A22 -= L21 U12 on random data
-// (n x n, nb = 128, one step k0 = 0) with the tcgen05 kernel and with the SIMT
-// kernel; returns max |tc - simt| / max |simt|.
-__global__ void k_fill_random(size_t n, float* x, unsigned seed) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        unsigned h = (unsigned)(i * 2654435761u) ^ seed;
-        h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
-        x[i] = ((float)(h & 0xffffff) / 16777216.0f) - 0.5f;
-    }
-}
-__global__ void k_maxdiff(size_t n, const float* a, const float* b, unsigned long long* out) {
-    float m = 0.f, r = 0.f;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        m = fmaxf(m, fabsf(a[i] - b[i]));
-        r = fmaxf(r, fabsf(b[i]));
-    }
-    atomicMax(out, (unsigned long long)__float_as_uint(m));
-    atomicMax(out + 1, (unsigned long long)__float_as_uint(r));
-}
-
-double tc_selftest(int device, int n) {
-    if (cudaSetDevice(device) != cudaSuccess || n % 128 != 0 || n < 256) return -1.0;
-    const int NB = 128, rem = n - NB;
-    size_t nn = (size_t)n * n;
-    float *A1 = nullptr, *A2 = nullptr, *wl = nullptr, *wu = nullptr, *wut = nullptr;
-    unsigned long long* d = nullptr;
-    int* flags = nullptr;
-    double result = -1.0;
-    if (cudaMalloc(&A1, 2 * nn * 4) || cudaMalloc(&A2, 2 * nn * 4) || cudaMalloc(&wl, 2 * (size_t)n * NB * 4) ||
-        cudaMalloc(&wu, 2 * (size_t)n * NB * 4) || cudaMalloc(&wut, 2 * (size_t)n * NB * 4) ||
-        cudaMalloc(&d, 16) || cudaMalloc(&flags, 4)) {
-        cudaGetLastError();
-    } else {
-        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * nn, A1, 12345u));
-        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * (size_t)n * NB, wl, 777u));
-        BEM_LAUNCH(k_fill_random<<<1024, 256>>>(2 * (size_t)n * NB, wu, 999u));
-        cudaMemcpy(A2, A1, 2 * nn * 4, cudaMemcpyDeviceToDevice);
-        cudaMemset(d, 0, 16);
-        cudaMemset(flags, 0, 4);
-        // U12^T for the tensor-core operand
-        CMat<float> A{A1, A1 + nn, n};
-        BEM_LAUNCH(k_copy_back<float><<<1024, 256>>>(NB, rem, wu, wu + (size_t)n * NB, rem, A, 0, NB, 0, wut,
-                                                     wut + (size_t)n * NB, NB, flags));
-        cudaMemcpy(A2, A1, 2 * nn * 4, cudaMemcpyDeviceToDevice);
-        CMat<float> WL{wl, wl + (size_t)n * NB, NB}, WU{wu, wu + (size_t)n * NB, rem};
-        CMat<float> C1{A1 + (size_t)NB * n + NB, A1 + nn + (size_t)NB * n + NB, n};
-        BEM_LAUNCH(k_cgemm<float><<<dim3(rem / 64, rem / 64), 256>>>(rem, rem, NB, WL, WU, C1, -1.0f, 1));
-        CMat<float> B2{A2, A2 + nn, n};
-        bool ok = tc_trailing_update(0, n, 0, NB, B2, wl, wut, flags);
-        BEM_LAUNCH(k_maxdiff<<<1024, 256>>>(2 * nn, A2, A1, d));
-        unsigned long long h[2] = {0, 0};
-        int hf = 0;
-        cudaMemcpy(h, d, 16, cudaMemcpyDeviceToHost);
-        cudaMemcpy(&hf, flags, 4, cudaMemcpyDeviceToHost);
-        if (ok && cudaGetLastError() == cudaSuccess && !(hf & FLAG_TIMEOUT)) {
-            unsigned a = (unsigned)h[0], b = (unsigned)h[1];
-            float fa, fb;
-            memcpy(&fa, &a, 4);
-            memcpy(&fb, &b, 4);
-            result = fb > 0 ? (double)fa / fb : (double)fa;
-        }
-    }
-    cudaFree(A1); cudaFree(A2); cudaFree(wl); cudaFree(wu); cudaFree(wut); cudaFree(d); cudaFree(flags);
-    return result;
-}
-
 // ---------------------------------------------------------------------------
 // Cooperative block triangular solve: one CTA per diagonal block (rounds if the
 // grid is smaller than the block count).  CTA b accumulates
@@ -1803,7 +1737,8 @@ __host__ __device__ constexpr int ts_zstride(int rows, int R, int RC) { return (
 template <int RC>
 __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int n, int R, CMat<float> A, int which,
                                                         float* Yin, float* Xout, int* xflag, int* ticket,
-                                                        int epoch, int* gflags) {
+                                                        int epoch, int* gflags, int wait_skew,
+                                                        unsigned long long wait_ns) {
     extern __shared__ __align__(16) float ts_smem[];
     __shared__ int s_ticket, s_go;
     const int zs = ts_zstride(TS_NB, R, RC);
@@ -1812,7 +1747,10 @@ __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int n, int R, CMat<fl
     float* ybase = red + TS_WARPS * TS_RW * RC * 2;  // [TS_RW][R] complex: this sub-block's rows of Yin
     const int tid = threadIdx.x, lane = tid % TS_RW, s = tid / TS_RW, wl = tid & 31;
     const int nsub = n / TS_RW, nsb = (n + TS_NB - 1) / TS_NB;
-    const unsigned long long deadline = ts_now() + 2000000000ull;
+    // wait_skew > 0 (failure-detection tests only) makes every wait ask for a flag value
+    // nothing publishes, so each wait runs into its deadline (wait_ns from the CTA's start)
+    const unsigned long long deadline = ts_now() + wait_ns;
+    const int want = epoch + wait_skew;
     int dead = 0;
     if (tid == 0) {
         const int t = atomicAdd(ticket, 1);
@@ -1845,11 +1783,11 @@ __global__ void __launch_bounds__(TS_THREADS, 3) k_trsv_tk(int n, int R, CMat<fl
     // every sub-block of super-block c is published: one flag per lane of warp 0
     auto probe = [&](int c) {
         const int k = wl, subs = width(c) / TS_RW;
-        const bool ok = k >= subs || ts_ready(xflag + c * TS_SB + k, epoch);
+        const bool ok = k >= subs || ts_ready(xflag + c * TS_SB + k, want);
         return __all_sync(0xffffffffu, ok);
     };
     auto wait_block = [&](int c) {
-        if (tid < width(c) / TS_RW) ts_wait(xflag + c * TS_SB + tid, epoch, deadline, dead, gflags);
+        if (tid < width(c) / TS_RW) ts_wait(xflag + c * TS_SB + tid, want, deadline, dead, gflags);
     };
     float ar[RC], ai[RC];
 #pragma unroll
@@ -2045,7 +1983,8 @@ __global__ void __launch_bounds__(TS_THREADS) k_dinv_apply(int R, const float* _
 // the block-diagonal D^-1, for one column count RC >= R.
 template <int RC>
 static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R,
-                          float* X, float* tmp, int* xflag, int* ticket, int epoch, int* flags) {
+                          float* X, float* tmp, int* xflag, int* ticket, int epoch, int* flags, int skew,
+                          unsigned long long wait_ns) {
     const int nsub = n / TS_RW, np = n / 256, nblk = n / DA_NB;
     const size_t smem =
         sizeof(float) * (2 * (size_t)ts_zstride(TS_NB, R, RC) + TS_WARPS * TS_RW * RC * 2 + TS_RW * 2 * R);
@@ -2056,26 +1995,27 @@ static int trsv_tk_launch(cudaStream_t st, int n, CMat<float> A, const float* in
         cudaFuncSetAttribute(k_dinv_apply<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d);
         cudaFuncSetAttribute(k_pair_apply<RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_d);
     }
-    BEM_LAUNCH(k_trsv_tk<RC><<<nsub, TS_THREADS, smem, st>>>(n, R, A, 0, X, tmp, xflag, ticket, epoch, flags));
+    BEM_LAUNCH(k_trsv_tk<RC><<<nsub, TS_THREADS, smem, st>>>(n, R, A, 0, X, tmp, xflag, ticket, epoch, flags, skew,
+                                                              wait_ns));
     if (np > 0) BEM_LAUNCH(k_pair_apply<RC><<<np * DA_SB, TS_THREADS, smem_d, st>>>(R, A, 0, tmp));
     BEM_LAUNCH(k_trsv_tk<RC><<<nsub, TS_THREADS, smem, st>>>(n, R, A, 1, tmp, tmp, xflag, ticket, epoch + 1,
-                                                              flags));
+                                                              flags, skew, wait_ns));
     if (np > 0) BEM_LAUNCH(k_pair_apply<RC><<<np * DA_SB, TS_THREADS, smem_d, st>>>(R, A, 1, tmp));
     BEM_LAUNCH(k_dinv_apply<RC><<<nblk * DA_SB, TS_THREADS, smem_d, st>>>(R, invr, invi, tmp, X));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
 
 static int trsv_tk(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
-                   float* tmp, int* xflag, int* ticket, int epoch, int* flags) {
+                   float* tmp, int* xflag, int* ticket, int epoch, int* flags, int sk, unsigned long long wns) {
     switch ((R + 1) / 2) {
-        case 1: return trsv_tk_launch<2>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 2: return trsv_tk_launch<4>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 3: return trsv_tk_launch<6>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 4: return trsv_tk_launch<8>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 5: return trsv_tk_launch<10>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 6: return trsv_tk_launch<12>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 7: return trsv_tk_launch<14>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
-        case 8: return trsv_tk_launch<16>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+        case 1: return trsv_tk_launch<2>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 2: return trsv_tk_launch<4>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 3: return trsv_tk_launch<6>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 4: return trsv_tk_launch<8>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 5: return trsv_tk_launch<10>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 6: return trsv_tk_launch<12>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 7: return trsv_tk_launch<14>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
+        case 8: return trsv_tk_launch<16>(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, sk, wns);
         default: return 1;
     }
 }
@@ -2089,7 +2029,7 @@ int lu_solve_f64(cudaStream_t st, int n, CMat<double> A, const double* invr, con
     return trsv_coop<double, 64, 8>(st, n, A, invr, invi, 1, R, tmp, X, ready, epoch + 1, flags);
 }
 int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const float* invi, int R, float* X,
-                 int* ready, int epoch, int* flags) {
+                 int* ready, int epoch, int* flags, int wait_skew, unsigned long long wait_ns) {
     // ready holds n / TS_RW flags (one per 8-row sub-block) and a ticket counter, zero
     // between launches.  A is in the pair-folded form of lu_pair_fold, D^-1 in invr / invi.
     float* tmp = X + (size_t)2 * n * R;
@@ -2097,7 +2037,7 @@ int lu_solve_f32(cudaStream_t st, int n, CMat<float> A, const float* invr, const
     int* ticket = ready + n / TS_RW;
     // Solves of several contexts may run at once on one GPU: a CTA waits only on
     // sub-blocks of lower tickets of its own launch, which are already running.
-    return trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags);
+    return trsv_tk(st, n, A, invr, invi, R, X, tmp, xflag, ticket, epoch, flags, wait_skew, wait_ns);
 }
 
 // ---------------------------------------------------------------------------

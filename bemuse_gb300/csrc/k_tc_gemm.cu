@@ -589,4 +589,76 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
     return tc_update_rect(st, n, k0, A, wl, wut, 0, 0, rem / 128, rem / 128, 0, flags, 0);
 }
 
+// ---------------------------------------------------------------------------
+// Probe of k_tc_update in one tile mode on caller data (bem_tc_probe): every
+// operand and the destination are copied to the device, the product runs once,
+// and the destination (and for the W21 mode its second destination) comes back.
+int tc_probe(int device, int mode, int n, float* C, const float* Wa, const float* Ua, const float* Wb,
+             const float* Ub, const float* T, float* Wout, char* err, int err_len) {
+    auto fail = [&](const char* m) {
+        snprintf(err, err_len, "%s", m);
+        return -1;
+    };
+    if (mode < 0 || mode > 6) return fail("mode outside 0..6");
+    if (n < 512 || n % 256 != 0 || n > 8192) return fail("n must be a multiple of 256 in [512, 8192]");
+    if (!C) return fail("null destination");
+    const bool pair_op = mode <= 2;
+    if (pair_op && (!Wa || !Ua || (mode >= 1 && (!Wb || !Ub)))) return fail("null operand");
+    if (!pair_op && !T) return fail("null operand");
+    if (mode == 3 && !Wout) return fail("null second destination");
+    if (cudaSetDevice(device) != cudaSuccess || !tc_gemm_supported(device)) return fail("no sm_103 device");
+    const size_t nn = (size_t)n * n, nw = (size_t)2 * n * 128;
+    const size_t nt = mode >= 5 ? (size_t)2 * (n / 256) * 128 * 128 : (size_t)2 * 128 * 128;
+    float *dC = nullptr, *dWa = nullptr, *dUa = nullptr, *dWb = nullptr, *dUb = nullptr, *dT = nullptr,
+          *dW = nullptr;
+    int* flags = nullptr;
+    int rc = 0;
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaMalloc(&dC, 2 * nn * 4) ||
+        cudaMalloc(&dWa, nw * 4) || cudaMalloc(&dUa, nw * 4) || cudaMalloc(&dWb, nw * 4) ||
+        cudaMalloc(&dUb, nw * 4) || cudaMalloc(&dT, nt * 4) || cudaMalloc(&dW, nw * 4) || cudaMalloc(&flags, 4)) {
+        rc = fail("device allocation failed");
+    } else {
+        cudaMemcpy(dC, C, 2 * nn * 4, cudaMemcpyHostToDevice);
+        if (pair_op) {
+            cudaMemcpy(dWa, Wa, nw * 4, cudaMemcpyHostToDevice);
+            cudaMemcpy(dUa, Ua, nw * 4, cudaMemcpyHostToDevice);
+            if (mode >= 1) {
+                cudaMemcpy(dWb, Wb, nw * 4, cudaMemcpyHostToDevice);
+                cudaMemcpy(dUb, Ub, nw * 4, cudaMemcpyHostToDevice);
+            }
+        } else {
+            cudaMemcpy(dT, T, nt * 4, cudaMemcpyHostToDevice);
+        }
+        cudaMemset(dW, 0, nw * 4);
+        cudaMemset(flags, 0, 4);
+        CMat<float> A{dC, dC + nn, n};
+        const int mt = n / 128 - 1;
+        bool ok = false;
+        switch (mode) {
+            case 0: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, nullptr, nullptr, 0, 0); break;
+            case 1: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
+            case 2: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 2, 1, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
+            case 3: ok = tc_w21(st, n, 0, A, dT, dW, flags, 0, -1); break;
+            case 4: ok = tc_ucol(st, n, n - 128, A, dT, 0, flags); break;
+            default: ok = tc_pair_fold(st, n, A, dT, mode - 4, flags); break;
+        }
+        int hf = 0;
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaMemcpy(&hf, flags, 4, cudaMemcpyDeviceToHost);
+        if (!ok) rc = fail("tensor map or launch set-up failed");
+        else if (e != cudaSuccess) rc = fail(cudaGetErrorString(e));
+        else if (hf & FLAG_TIMEOUT) rc = fail("a device-side wait expired");
+        else {
+            cudaMemcpy(C, dC, 2 * nn * 4, cudaMemcpyDeviceToHost);
+            if (mode == 3) cudaMemcpy(Wout, dW, nw * 4, cudaMemcpyDeviceToHost);
+        }
+    }
+    cudaGetLastError();
+    cudaFree(dC); cudaFree(dWa); cudaFree(dUa); cudaFree(dWb); cudaFree(dUb); cudaFree(dT); cudaFree(dW);
+    cudaFree(flags);
+    if (st) cudaStreamDestroy(st);
+    return rc;
+}
+
 }  // namespace bem

@@ -143,8 +143,11 @@ bem_status bem_dense_solve_noalloc(int device, int n, const double* A, int nrhs,
     if (e == cudaSuccess) e = cudaMemcpyAsync(B, X, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return na_fail(BEM_ERR_CUDA, cudaGetErrorString(e));
-    if (hflags & (FLAG_ZERO_PIVOT | FLAG_TIMEOUT))
-        return na_fail(BEM_ERR_NUMERIC, "zero pivot or expired device wait");
+    // the same status codes as bem_dense_solve: an expired device wait is a CUDA-side
+    // failure, a zero pivot a numeric one
+    if (hflags & FLAG_TIMEOUT)
+        return na_fail(BEM_ERR_CUDA, "a device-side wait in the triangular solve expired");
+    if (hflags & FLAG_ZERO_PIVOT) return na_fail(BEM_ERR_NUMERIC, "zero or non-finite pivot in the LU");
     if (hflags & FLAG_PIVOT)
         return na_fail(BEM_ERR_NUMERIC, "a multiplier |l_ik| > 1: partial pivoting would exchange rows");
     return BEM_OK;

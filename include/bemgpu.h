@@ -295,7 +295,14 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     LU when it overlaps it (default 72).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
  *   "asm_split"       work items per receiver row of the persistent assembly kernel
- *                     (1..64, default 4; finer items measured slower). */
+ *                     (1..64, default 4; finer items measured slower).
+ *   "refine_max_solves" preconditioner solves the mixed path's refinement may use
+ *                     (default 60); when they run out bem_solve returns BEM_ERR_NUMERIC.
+ *   "test_wait_skew", "test_wait_ms"  failure-detection tests only: with skew 1 every
+ *                     wait of the triangular-solve chain asks for a flag value that nothing
+ *                     publishes and gives up after test_wait_ms (default 2000) milliseconds;
+ *                     bem_solve then returns BEM_ERR_CUDA ("device-side wait ... expired")
+ *                     and the context stays usable once the skew is set back to 0. */
 bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Autotuner of the pipelined mixed solve: times bem_solve (BEM_MIXED, outputs skipped)
@@ -422,7 +429,14 @@ bem_status bem_write_wamit(const char* prefix, const bem_wamit_info* info, int n
  *   - Orders n > BEM_NOALLOC_MAX_N or nrhs outside [1, 16] are rejected with
  *     BEM_ERR_ARG and a message.
  *   - The first call on a device looks up the array's device address (with that
- *     device current); make that first call before any stream capture.
+ *     device current); make that first call before any stream capture.  With
+ *     lazy module loading (CUDA_MODULE_LOADING=LAZY, the default) that first
+ *     call is also when the driver loads this code and reserves the array, so it
+ *     can fail with BEM_ERR_CUDA if a pool allocator has already taken all device
+ *     memory: make the first call before the pool reserves its memory, or run
+ *     with CUDA_MODULE_LOADING=EAGER.  Later calls allocate nothing.
+ *   - The address is kept per device for the life of the process; calls after a
+ *     cudaDeviceReset of that device are not supported.
  *   - All calls share the one array: calls that overlap on the GPU (other host
  *     threads, other streams) race and corrupt each other's results.
  *   - Work runs on the legacy default stream; the call returns when X is on the host.
@@ -434,11 +448,31 @@ bem_status bem_dense_solve_noalloc(int device, int n, const double* A, int nrhs,
 /* Number of kernel launches this library has issued since it was loaded. */
 unsigned long long bem_launch_count(void);
 
-/* Diagnostic: one tensor-core (tcgen05, TF32) trailing update of an n x n
- * complex block (n a multiple of 128, >= 256) on random data, compared with
- * the FP32 CUDA-core update on the same data.  Returns max|tc - fp32| /
- * max|fp32| (about 1e-3 for TF32 inputs), or a negative value on failure. */
-double bem_selftest_tc(int device, int n);
+/* Diagnostic with no reference counterpart: one launch of the tensor-core
+ * (tcgen05, TF32) product kernel of the LU in one of its tile modes, on caller
+ * data, so that its arithmetic can be checked against an exact product.  All
+ * arrays are planar complex FP32 host arrays (the real plane, then the
+ * imaginary plane); operands should hold TF32 values (the tensor cores ignore
+ * the low 13 mantissa bits).  C is n x n (row-major, n a multiple of 256 in
+ * [512, 8192]) and is updated in place; Wa, Ua, Wb, Ub are n x 128; T is
+ * 128 x 128 (modes 3, 4) or (n / 256) x 128 x 128 (modes 5, 6).
+ *   0  C[128:, 128:] -= Wa[0:n-128] Ua[0:n-128]^T                       (trailing update)
+ *   1  C[128:, 128:] -= Wa Ua^T + Wb Ub^T over the same rows, K = 256  (two steps per pass)
+ *   2  mode 1 on the L of width 2 only (tile columns 0-1, then tile rows 0-1), without
+ *      its first tile                                                  (cross update)
+ *   3  W = C[128:, 0:128] T^T, stored rounded to TF32 into Wout rows 0.. and over
+ *      C[128:, 0:128]                                                  (W21 = A21 D^-1)
+ *   4  C[0:n-128, n-128:] <- C[0:n-128, n-128:] T^T, rounded to TF32    (U D^-1)
+ *   5  for each 128-block pair p: C_{r,2p} -= C_{r,2p+1} T_p^T, block rows r >= 2p+2  (L fold)
+ *   6  for each pair p: C_{r,2p+1} -= C_{r,2p} T_p^T, block rows r < 2p              (U fold)
+ * Errors: BEM_ERR_ARG with the reason in bem_last_error(NULL). */
+bem_status bem_tc_probe(int device, int mode, int n, float* C, const float* Wa, const float* Ua, const float* Wb,
+                        const float* Ub, const float* T, float* Wout);
+
+/* Measured FP32 throughput of `device` in TFLOP/s (an FMA loop timed with CUDA
+ * events, 2 flops per FMA): the roofline denominator of the FP32-bound wave
+ * assembly.  No reference counterpart. */
+bem_status bem_fp32_peak(int device, double* tflops);
 
 /* Library version string. */
 const char* bem_version(void);

@@ -414,6 +414,19 @@ static void wave_panel_influence(const Panel& p, V3 P, double K, cplx& S, cplx& 
     D = OD;
 }
 
+// y[j] -= l x[j] for j < m, in real arithmetic: the value std::complex's product
+// gives for finite operands, without its NaN/inf recovery call in the inner loop.
+static inline void axpy_neg(cplx l, const cplx* x, cplx* y, int m) {
+    const double lr = l.real(), li = l.imag();
+    const double* xs = reinterpret_cast<const double*>(x);
+    double* ys = reinterpret_cast<double*>(y);
+    for (int j = 0; j < m; ++j) {
+        const double xr = xs[2 * j], xi = xs[2 * j + 1];
+        ys[2 * j] -= lr * xr - li * xi;
+        ys[2 * j + 1] -= lr * xi + li * xr;
+    }
+}
+
 // Partial-pivot LU of a row-major complex matrix (stand-in for
 // Eigen::PartialPivLU<MatrixXcd>, Solver_Base.h:85, Hydrodynamic_Solver.cpp:430).
 // Pivot = first index of max |a_ik|.  Blocked right-looking, OpenMP over rows.
@@ -438,7 +451,7 @@ static void lu_factor(int n, cplx* a, int* piv) {
                 const cplx* rk = a + (size_t)k * n;
                 cplx l = ri[k] * inv;
                 ri[k] = l;
-                for (int j = k + 1; j < k0 + kb; ++j) ri[j] -= l * rk[j];
+                axpy_neg(l, rk + k + 1, ri + k + 1, k0 + kb - k - 1);
             }
         }
         // U12 = L11^{-1} A12
@@ -447,19 +460,15 @@ static void lu_factor(int n, cplx* a, int* piv) {
             #pragma omp parallel for schedule(static)
             for (int i = k + 1; i < k0 + kb; ++i) {
                 cplx* ri = a + (size_t)i * n;
-                cplx l = ri[k];
-                for (int j = k0 + kb; j < n; ++j) ri[j] -= l * rk[j];
+                axpy_neg(ri[k], rk + k0 + kb, ri + k0 + kb, n - k0 - kb);
             }
         }
         // A22 -= L21 U12
         #pragma omp parallel for schedule(static)
         for (int i = k0 + kb; i < n; ++i) {
             cplx* ri = a + (size_t)i * n;
-            for (int k = k0; k < k0 + kb; ++k) {
-                cplx l = ri[k];
-                const cplx* rk = a + (size_t)k * n;
-                for (int j = k0 + kb; j < n; ++j) ri[j] -= l * rk[j];
-            }
+            for (int k = k0; k < k0 + kb; ++k)
+                axpy_neg(ri[k], a + (size_t)k * n + k0 + kb, ri + k0 + kb, n - k0 - kb);
         }
     }
 }
@@ -943,10 +952,17 @@ void orc_mass_hydrostatics(int nn, const double* nodes, int ne, const int* elems
 // forces integrate over the first NPA (hull) panels.  IFR (Create_Panels :45-55)
 // appends the interior free-surface panels after the hull and solves a zero
 // frequency at Omega = 1e-3 (:406).
+// Optional stage clock of solve_panels (orc_solve_timed): [0] setup (Rankine
+// matrices, N_k), then per frequency [1 + 3f] wave assembly + compose, [2 + 3f]
+// LU, [3 + 3f] right-hand sides, solves and post; wall seconds.
+static double* g_stage_clock = nullptr;
+
 static void solve_panels(const std::vector<Panel>& body, const std::vector<Panel>& mir, int NPA, bool ifr,
                          int nfreq, const double* omegas, int nbeta, const double* betas, const double* Mmat,
                          const double* Cmat, double* A_out, double* B_out, double* FK_out, double* SC_out,
                          double* F_out, double* RAO_out, double* phiJ_out, double* phiS_out) {
+    double* clk = g_stage_clock;
+    double t0 = omp_get_wtime();
     std::vector<V3> x = collocation(body);
     const int N = (int)body.size(), NB = nbeta;
     std::vector<double> s((size_t)N * N), sr((size_t)N * N), d((size_t)N * N), dr((size_t)N * N), rn(N);
@@ -969,7 +985,9 @@ static void solve_panels(const std::vector<Panel>& body, const std::vector<Panel
     }
     std::vector<cplx> Smat((size_t)N * N), Dmat((size_t)N * N);
     std::vector<int> piv(N);
+    if (clk) clk[0] = omp_get_wtime() - t0;
     for (int f = 0; f < nfreq; ++f) {
+        t0 = omp_get_wtime();
         double Omega = omegas[f];
         if (Omega == 0.0 && ifr) Omega = 1.0e-3;
         double Kappa = Omega * Omega / Gravity;  // :409 uses the global Gravity
@@ -989,7 +1007,11 @@ static void solve_panels(const std::vector<Panel>& body, const std::vector<Panel
                 Smat[o] = Sv;
                 Dmat[o] = Dv;
             }
+        double t1 = omp_get_wtime();
+        if (clk) clk[1 + 3 * f] = t1 - t0;
         lu_factor(N, Dmat.data(), piv.data());
+        t0 = omp_get_wtime();
+        if (clk) clk[2 + 3 * f] = t0 - t1;
         // Set_Incident_Potential_Mats (:575-596), Calc_Phi_Incident (:544-573)
         std::vector<cplx> PhiI((size_t)N * NB), dPhiI((size_t)N * NB);
         for (int P = 0; P < N; ++P) {
@@ -1078,6 +1100,7 @@ static void solve_panels(const std::vector<Panel>& body, const std::vector<Panel
                         phiS_out[2 * ((size_t)p * NB + b) + 1] = rhs[(size_t)p * NR + 6 + b].imag();
                     }
         }
+        if (clk) clk[3 + 3 * f] = omp_get_wtime() - t0;
     }
 }
 
@@ -1093,6 +1116,17 @@ void orc_solve(int nn, const double* nodes, int ne, const int* elems, int ncomp,
     build_panels(m, body, mir);
     solve_panels(body, mir, ne, false, nfreq, omegas, nbeta, betas, Mmat, Cmat, A_out, B_out, FK_out, SC_out, F_out,
                  RAO_out, phiJ_out, phiS_out);
+}
+
+// orc_solve with the stage clock of solve_panels: clock receives 1 + 3 nfreq wall times.
+void orc_solve_timed(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+                     const double* comp_origin, int nfreq, const double* omegas, int nbeta, const double* betas,
+                     const double* Mmat, const double* Cmat, double* A_out, double* B_out, double* FK_out,
+                     double* SC_out, double* F_out, double* RAO_out, double* clock) {
+    g_stage_clock = clock;
+    orc_solve(nn, nodes, ne, elems, ncomp, comp_first, comp_origin, nfreq, omegas, nbeta, betas, 9.81, Mmat, Cmat,
+              A_out, B_out, FK_out, SC_out, F_out, RAO_out, nullptr, nullptr);
+    g_stage_clock = nullptr;
 }
 
 // IFR: the hull mesh and the interior free-surface (aux) mesh.

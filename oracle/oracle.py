@@ -25,9 +25,9 @@ _d = ctypes.c_double
 def build(ref=None):
     """Compile liboracle.so (and the reference kernels when the tree exists)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_root = ref or os.environ.get("BEM_REFERENCE_ROOT", "/root/reference")
-    if os.path.isdir(os.path.join(ref_root, "src")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref_root], check=True)
+    ref_root = ref or os.environ.get("BEM_REFERENCE_ROOT")
+    args = ["REF=" + ref_root] if ref_root else []
+    subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"] + args, check=True)
 
 
 def _p(a, typ=_dp):
@@ -98,6 +98,7 @@ class Oracle:
         L.orc_mass_hydrostatics.argtypes = mesh_args + mesh_args + [_d, _d, _d, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve.argtypes = mesh_args + [_i, _dp, _i, _dp, _d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                             _dp, _dp]
+        L.orc_solve_timed.argtypes = mesh_args + [_i, _dp, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve_ifr.argtypes = mesh_args + mesh_args + [_i, _dp, _i, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                                             _dp, _dp, _dp]
         L.orc_exterior.argtypes = mesh_args + [_d, _i, _dp, _dp, _dp, _i, _dp, _i, _dp, _dp, _dp, _dp]
@@ -220,6 +221,26 @@ class Oracle:
             out["phiJ"] = pj
             out["phiS"] = ps
         return out
+
+    def solve_timed(self, mesh, omegas, betas, M=None, C=None):
+        """solve() with wall-clock seconds per stage: 'setup' (the frequency-independent
+        Rankine matrices) and per frequency 'wave' (assembly + compose), 'lu' and 'rest'
+        (right-hand sides, solves, post)."""
+        omegas = np.ascontiguousarray(omegas, dtype=np.float64).ravel()
+        betas = np.ascontiguousarray(betas, dtype=np.float64).ravel()
+        nf, nb = omegas.size, betas.size
+        M = np.ascontiguousarray(np.zeros((6, 6)) if M is None else M, dtype=np.float64)
+        C = np.ascontiguousarray(np.zeros((6, 6)) if C is None else C, dtype=np.float64)
+        A = np.zeros((nf, 6, 6))
+        B = np.zeros((nf, 6, 6))
+        FK, SC, F, RAO = (np.zeros((nf, 6, nb), np.complex128) for _ in range(4))
+        clk = np.zeros(1 + 3 * nf)
+        self.L.orc_solve_timed(*mesh.args(), nf, _p(omegas), nb, _p(betas), _p(M), _p(C), _p(A), _p(B),
+                               _p(FK.view(np.float64)), _p(SC.view(np.float64)), _p(F.view(np.float64)),
+                               _p(RAO.view(np.float64)), _p(clk))
+        t = clk[1:].reshape(nf, 3)
+        return dict(A=A, B=B, FK=FK, SC=SC, F=F, RAO=RAO), {"setup": float(clk[0]), "wave": t[:, 0], "lu": t[:, 1],
+                                                            "rest": t[:, 2]}
 
     def exterior(self, mesh, omega, betas, phiJ, phiS, wave_points, n_kochin):
         """Free-surface elevation at wave_points (n x 3) and Kochin functions at

@@ -259,13 +259,6 @@ def test_dense_solve_plain_and_mixed(bg):
         assert res <= 1e-12 and normwise(x, ref) < 1e-10
 
 
-def test_tensor_core_update_matches_fp32(bg):
-    for n in (256, 1024):
-        err = bg.selftest_tc(n)
-        print("tcgen05 vs fp32 update, n=%d: %.3e" % (n, err))
-        assert 0 <= err < 2e-2
-
-
 def test_aero_steady_solve_matches_oracle(bg, orc):
     """Aerodynamic_Solver constant-panel steady solve (Aerodynamic_Solver.cpp:42-58,
     150-180) on a 240-panel NACA 0012 wing at 5 deg: X = H^-1 (G (U . n))."""

@@ -53,6 +53,29 @@ def test_noalloc_matches_allocating_solve_twice_in_a_row(L):
         assert normwise(X, np.linalg.solve(A, B)) < 1e-11
 
 
+def _free_device_bytes():
+    """cudaMemGetInfo's free bytes on the current device, through the CUDA runtime the
+    library itself loaded (libcudart.so.13)."""
+    rt = ctypes.CDLL("libcudart.so.13")
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_call_allocates_no_device_memory(L):
+    # after one call (which, with lazy module loading, is when the scratch array
+    # itself is reserved) a further call leaves the free device memory unchanged
+    A, B = _system(400, 7, 4)
+    st, _ = _noalloc(L, A, B)
+    assert st == 0, L.bem_last_error(None)
+    before = _free_device_bytes()
+    st, X = _noalloc(L, A, B)
+    after = _free_device_bytes()
+    assert st == 0, L.bem_last_error(None)
+    assert after == before, (before, after)
+    assert normwise(X, np.linalg.solve(A, B)) < 1e-11
+
+
 def test_noalloc_rejects_orders_beyond_its_scratch(L):
     A, B = _system(8, 1, 3)
     big = np.zeros((513, 513), np.complex128)
