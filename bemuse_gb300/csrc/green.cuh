@@ -196,6 +196,29 @@ __device__ __forceinline__ void bessel_j01_small(float x, float& j0, float& j1) 
                                   0.21093573f), -0.56249985f), 0.5f);
 }
 
+// sin and cos of a phase already reduced to about [-pi, pi] (|x| < 8 keeps the
+// reduction exact): quadrant q = rint(2x / pi), r = x - q pi/2 by a two-constant
+// Cody-Waite step, then the Taylor series of sin to r^9 and of cos to r^10 on
+// |r| <= pi/4 (truncation below 3e-9), and the quadrant's swap and signs.  The
+// general sincosf also handles arguments far outside this range, which the
+// Bessel phase never is.
+__device__ __forceinline__ void sincos_reduced(float x, float& sn, float& cs) {
+    const float PIO2_H = 1.57079637f, PIO2_L = -4.37113883e-8f;  // pi / 2 = H + L
+    const float q = rintf(x * 0.636619772f);
+    float r = fmaf(-q, PIO2_H, x);
+    r = fmaf(-q, PIO2_L, r);
+    const float r2 = r * r;
+    const float ps = r * fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, 1.0f / 362880.0f, -1.0f / 5040.0f), 1.0f / 120.0f),
+                                       -1.0f / 6.0f), 1.0f);
+    const float pc = fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, fmaf(r2, -1.0f / 3628800.0f, 1.0f / 40320.0f), -1.0f / 720.0f),
+                                             1.0f / 24.0f), -0.5f), 1.0f);
+    const int iq = (int)q;
+    const bool swap = iq & 1;
+    const float s0 = swap ? pc : ps, c0 = swap ? ps : pc;
+    sn = (iq & 2) ? -s0 : s0;
+    cs = ((iq + 1) & 2) ? -c0 : c0;
+}
+
 __device__ __forceinline__ void bessel_large(float xh, float xl, float& j0, float& j1, float& y0, float& y1) {
     const float TWOPI_H = 6.28318548f, TWOPI_L = -1.74845553e-7f;  // 2 pi = H + L
     const float PI4_H = 0.785398185f, PI4_L = -2.18556949e-8f;     // pi / 4 = H + L
@@ -218,7 +241,7 @@ __device__ __forceinline__ void bessel_large(float xh, float xl, float& j0, floa
     const float ph = s + pl;
     pl -= ph - s;
     float sn, cs;
-    sincosf(ph, &sn, &cs);
+    sincos_reduced(ph, sn, cs);
     const float s0 = fmaf(cs, pl, sn), c0 = fmaf(-sn, pl, cs);  // sin, cos theta_0
     // theta_1 = theta_0 - pi/2 + (d1 - d0); |d1 - d0| < 0.17 for x >= 3, where the
     // Taylor series below are exact to ~1e-12

@@ -205,16 +205,86 @@ __global__ void __launch_bounds__(256) k_wave(WaveArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// K2, mixed precision.  Every term of G and dG in FP32; the FP64 operator
-// gets the real part (Rankine FP64 + wave FP32) and the LU copy gets both parts
-// in FP32.  The imaginary part of the operator and of S*B is not taken from
-// here: it is applied exactly, in FP64, by the plane-wave kernels below
-// (k_pw_*), because the radiation damping at low K is a small difference of
-// O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
-__global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
-    const int lane = threadIdx.x & 31;
-    __shared__ int s_admit;
-    uint32_t smid;
+// One receiver of the mixed assembly: the collocation point as float pairs.
+struct Recv32 {
+    float xh, yh, zh, xl, yl, zl;
+};
+__device__ __forceinline__ Recv32 load_recv32(const WaveArgs& a, int r) {
+    const int N = a.N;
+    return Recv32{a.xr32[r], a.xr32[N + r], a.xr32[2 * N + r], a.xr32[3 * N + r], a.xr32[4 * N + r],
+                  a.xr32[5 * N + r]};
+}
+
+// One Gauss point of a mirrored wave panel (coordinates as float pairs g*, g*l; normal n;
+// weights wc1 = w K/4pi, wc2 = w K^2/4pi) at receiver R: adds its FP32 terms of ws and wd
+// (FreeSurface_Wave_Kernel and CInf_SingleDoubleLayerQuad, Panel.cpp:601-636, 776-794).
+__device__ __forceinline__ void gauss_eval32(const Recv32& R, float gx, float gy, float gz, float gxl, float gyl,
+                                             float gzl, float nx, float ny, float nz, float wc1, float wc2, float Kh,
+                                             float Kl, float& wsr, float& wsi, float& wdr, float& wdi) {
+    const float twopi = 6.28318530717959f;
+    const float K = Kh;
+    // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
+    const float sx = R.xh - gx, sy = R.yh - gy;
+    const float bx = sx - R.xh, by = sy - R.yh;
+    const float lx = ((R.xh - (sx - bx)) - (gx + bx)) + (R.xl - gxl);
+    const float ly = ((R.yh - (sy - by)) - (gy + by)) + (R.yl - gyl);
+    // v = K (z_r - z_q) as a float pair (VV, vl), like h = (hh, hl)
+    const float sz = R.zh - gz;
+    const float bz = sz - R.zh;
+    const float ez = ((R.zh - (sz - bz)) - (gz + bz)) + (R.zl - gzl);
+    const float vh = sz * Kh;
+    const float vlo = fmaf(sz, Kh, -vh) + fmaf(sz, Kl, ez * Kh);
+    const float VV = vh + vlo;
+    const float vl = vlo - (VV - vh);
+    const float XX = (sx + lx) * K, YY = (sy + ly) * K;
+    float hh, hl;
+    df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
+    const float ev = expf(VV);
+    float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
+    if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
+    else bessel_j01_small(hh, j0v, j1v);
+    float Gr, Ghr, Gv;
+    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr, Gv);
+    // G at the unrounded (h, v): the first-order terms of the float pairs' low parts.
+    // The radiation damping is a small difference of terms that each carry this
+    // rounding, so without it B loses ~1e-6 at the highest frequencies.
+    Gr = fmaf(Ghr, hl, fmaf(Gv, vl, Gr));
+    const float proj = fmaf(XX, nx, YY * ny);
+    float dgr = 0.f, dgi = 0.f;
+    if (hh > 1.0e-6f) {
+        const float inv_h = __frcp_rn(hh);
+        dgr = Ghr * proj * inv_h;
+        dgi = twopi * ev * j1v * proj * inv_h;
+    }
+    const float Gi = -twopi * ev * j0v;
+    wsr = fmaf(wc1, Gr, wsr);
+    wsi = fmaf(wc1, Gi, wsi);
+    wdr = fmaf(wc2, fmaf(Gr, nz, dgr), wdr);
+    wdi = fmaf(wc2, fmaf(Gi, nz, dgi), wdi);
+}
+
+// Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
+// FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
+__device__ __forceinline__ void redf_store(const WaveArgs& a, size_t o, float rdh, float rdl, float rsh, float rsl,
+                                           float wdr, float wdi) {
+    const float Kh = a.kh, Kl = a.kl;
+    const float ph = Kh * rsh;
+    const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
+    const float sh = rdh + ph;
+    float bb = sh - rdh;
+    const float se = ((rdh - (sh - bb)) + (ph - bb)) + (rdl + pe);
+    const float th = sh + wdr;
+    bb = th - sh;
+    const float te = ((sh - (th - bb)) + (wdr - bb)) + se;
+    const float hi = th + te;
+    a.Dhi[o] = hi;
+    a.Dlo[o] = te - (hi - th);
+    a.D32r[o] = hi;
+    a.D32i[o] = wdi;
+}
+
+// Admission of a persistent assembly CTA (see WaveArgs): returns false if it should leave.
+__device__ __forceinline__ bool wave_admit(const WaveArgs& a, uint32_t& smid, int* s_admit) {
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     if (smid >= (uint32_t)WAVE_SM_SLOTS) smid = WAVE_SM_SLOTS - 1;  // only the admission policy shares a slot
     if (threadIdx.x == 0) {
@@ -228,10 +298,23 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
             atomicSub(a.sm_ctr + smid, 1);
             ok = 0;
         }
-        s_admit = ok;
+        *s_admit = ok;
     }
     __syncthreads();
-    if (!s_admit) return;
+    return *s_admit != 0;
+}
+
+// K2, mixed precision.  Every term of G and dG in FP32; the FP64 operator
+// gets the real part (Rankine FP64 + wave FP32) and the LU copy gets both parts
+// in FP32.  The imaginary part of the operator and of S*B is not taken from
+// here: it is applied exactly, in FP64, by the plane-wave kernels below
+// (k_pw_*), because the radiation damping at low K is a small difference of
+// O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
+__global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
+    const int lane = threadIdx.x & 31;
+    __shared__ int s_admit;
+    uint32_t smid;
+    if (!wave_admit(a, smid, &s_admit)) return;
     // work item = one receiver row x one of a.split source ranges, so the last items
     // are short and the tail of the launch leaves few SMs idle
     const int split = a.split > 0 ? a.split : WAVE_SPLIT;
@@ -244,12 +327,9 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         const int r = item / split, s_begin = (item % split) * chunk;
         const int s_end = min(a.N, s_begin + chunk);
         const int N = a.N, R = a.R;
-        const float xh = a.xr32[r], yh = a.xr32[N + r], zh = a.xr32[2 * N + r];
-        const float xl = a.xr32[3 * N + r], yl = a.xr32[4 * N + r], zl = a.xr32[5 * N + r];
-        const float K = a.kh;
+        const Recv32 Rv = load_recv32(a, r);
         const float Kh = a.kh, Kl = a.kl;
         const float c1 = a.c1f, c2 = a.c2f;
-        const float twopi = 6.28318530717959f;
         float acc_re[MAX_RHS], acc_im[MAX_RHS];
     #pragma unroll
         for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
@@ -269,50 +349,12 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (q < nq) {
-                    const float* g = a.gq32 + (size_t)q * N + s;
-                    // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
                     // source data is read by every row: read-only path
-                    const float gx = __ldg(g), gy = __ldg(g + fs);
-                    const float sx = xh - gx, sy = yh - gy;
-                    float bx = sx - xh, by = sy - yh;
-                    const float lx = ((xh - (sx - bx)) - (gx + bx)) + (xl - __ldg(g + 7 * fs));
-                    const float ly = ((yh - (sy - by)) - (gy + by)) + (yl - __ldg(g + 8 * fs));
-                    // v = K (z_r - z_q) as a float pair (VV, vl), like h = (hh, hl)
-                    const float gz = __ldg(g + 2 * fs);
-                    const float sz = zh - gz;
-                    const float bz = sz - zh;
-                    const float ez = ((zh - (sz - bz)) - (gz + bz)) + (zl - __ldg(g + 9 * fs));
-                    float w = __ldg(g + 3 * fs), nx = __ldg(g + 4 * fs), ny = __ldg(g + 5 * fs),
-                          nz = __ldg(g + 6 * fs);
-                    const float vh = sz * Kh;
-                    const float vlo = fmaf(sz, Kh, -vh) + fmaf(sz, Kl, ez * Kh);
-                    const float VV = vh + vlo;
-                    const float vl = vlo - (VV - vh);
-                    float XX = (sx + lx) * K, YY = (sy + ly) * K;
-                    float hh, hl;
-                    df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
-                    float ev = expf(VV);
-                    float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
-                    if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
-                    else bessel_j01_small(hh, j0v, j1v);
-                    float Gr, Ghr, Gv;
-                    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr, Gv);
-                    // G at the unrounded (h, v): the first-order terms of the float pairs' low
-                    // parts.  The radiation damping is a small difference of terms that each
-                    // carry this rounding, so without it B loses ~1e-6 at the highest frequencies.
-                    Gr = fmaf(Ghr, hl, fmaf(Gv, vl, Gr));
-                    float proj = fmaf(XX, nx, YY * ny);
-                    float dgr = 0.f, dgi = 0.f;
-                    if (hh > 1.0e-6f) {
-                        float inv_h = __frcp_rn(hh);
-                        dgr = Ghr * proj * inv_h;
-                        dgi = twopi * ev * j1v * proj * inv_h;
-                    }
-                    float Gi = -twopi * ev * j0v;
-                    wsr = fmaf(w * c1, Gr, wsr);
-                    wsi = fmaf(w * c1, Gi, wsi);
-                    wdr = fmaf(w * c2, fmaf(Gr, nz, dgr), wdr);
-                    wdi = fmaf(w * c2, fmaf(Gi, nz, dgi), wdi);
+                    const float* g = a.gq32 + (size_t)q * N + s;
+                    const float w = __ldg(g + 3 * fs);
+                    gauss_eval32(Rv, __ldg(g), __ldg(g + fs), __ldg(g + 2 * fs), __ldg(g + 7 * fs), __ldg(g + 8 * fs),
+                                 __ldg(g + 9 * fs), __ldg(g + 4 * fs), __ldg(g + 5 * fs), __ldg(g + 6 * fs), w * c1,
+                                 w * c2, Kh, Kl, wsr, wsi, wdr, wdi);
                 }
             }
             if (a.mode == 1) {
@@ -321,21 +363,7 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
                 a.wd_out[o] = (double)wdr; a.wd_out[o + 1] = (double)wdi;
                 continue;
             }
-            // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
-            // FMA-exact products and Knuth two-sums keep ~48 bits, as the refinement residual needs.
-            const float ph = Kh * rsh;
-            const float pe = fmaf(Kh, rsl, fmaf(Kl, rsh, fmaf(Kh, rsh, -ph)));
-            const float sh = rdh + ph;
-            float bb = sh - rdh;
-            const float se = ((rdh - (sh - bb)) + (ph - bb)) + (rdl + pe);
-            const float th = sh + wdr;
-            bb = th - sh;
-            const float te = ((sh - (th - bb)) + (wdr - bb)) + se;
-            const float hi = th + te;
-            a.Dhi[row + s] = hi;
-            a.Dlo[row + s] = te - (hi - th);
-            a.D32r[row + s] = hi;
-            a.D32i[row + s] = wdi;
+            redf_store(a, row + s, rdh, rdl, rsh, rsl, wdr, wdi);
             // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
             const float* b = a.Bm32 + (size_t)s * 2 * R;
     #pragma unroll
