@@ -114,6 +114,8 @@ def lib():
         "bem_mlp_grad": ([vp, c_int, _dp, _dp, _dp, _dp], c_int),
         "bem_mlp_train": ([vp, c_int, _dp, _dp, c_int, c_int, ctypes.c_double, ctypes.c_ulonglong, _dp], c_int),
         "bem_mlp_throughput": ([vp, c_int, _dp], c_int),
+        "bem_mlp_eval_tc": ([vp, c_int, _dp, _dp], c_int),
+        "bem_mlp_throughput_tc": ([vp, c_int, _dp], c_int),
         "bem_havelock_throughput": ([c_int, c_int, c_int, _dp], c_int),
         "bem_batch_solve": ([c_int, c_int, ctypes.POINTER(_Mesh), ctypes.POINTER(_Props), c_double, c_double, c_int,
                              _dp, c_int, _dp, c_int, c_double, c_int, ctypes.POINTER(_Result), _dp], c_int),
@@ -689,6 +691,18 @@ class HavelockSurrogate:
         y = np.zeros((x.shape[0], 6))
         self._chk(lib().bem_mlp_eval(self._h, x.shape[0], _p(x), _p(y)))
         return y
+
+    def eval_tc(self, x):
+        """Forward pass on the tensor cores (BF16 activations; bem_mlp_eval_tc)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)
+        y = np.zeros((x.shape[0], 6))
+        self._chk(lib().bem_mlp_eval_tc(self._h, x.shape[0], _p(x), _p(y)))
+        return y
+
+    def throughput_tc(self, n=1 << 20):
+        r = np.zeros(1)
+        self._chk(lib().bem_mlp_throughput_tc(self._h, int(n), _p(r)))
+        return float(r[0])
 
     def grad(self, x, y):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)

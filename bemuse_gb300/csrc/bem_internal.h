@@ -203,6 +203,16 @@ void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
 void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
 
+// Tensor-core inference of the Green-function surrogate network (k_mlp_tc.cu).
+// mlp_tc_build_image: the operand image (mlp_tc_image_bytes() bytes) and FP32 tail
+// (mlp_tc_param_floats() floats) from the FP32 master parameters of k_mlp.cu.
+// mlp_tc_forward: y (n x 6) = network(x (n x 2)), normalised values; nonzero if the
+// launch failed.
+int mlp_tc_image_bytes();
+int mlp_tc_param_floats();
+void mlp_tc_build_image(cudaStream_t st, const float* w, uint8_t* img, float* fw);
+int mlp_tc_forward(cudaStream_t st, int n, const float* x, float* y, const uint8_t* img, const float* fw, int* flags);
+
 int tc_gemm_supported(int device);
 // Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA), or < 0 on failure.
 double ffma_peak_tflops(int device);

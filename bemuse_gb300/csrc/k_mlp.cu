@@ -191,6 +191,14 @@ struct bem_mlp {
     float* A[NL + 1] = {};         // activations; A[0] = normalised input
     float *dA = nullptr, *dZ = nullptr, *T = nullptr;
     double* d_loss = nullptr;
+    // tensor-core inference (k_mlp_tc.cu): operand image of the BF16 weights, rebuilt
+    // when the weights change (version counts set_params / train calls)
+    uint8_t* tc_img = nullptr;
+    float* tc_f = nullptr;
+    int* tc_flags = nullptr;
+    float *tc_x = nullptr, *tc_y = nullptr;
+    int tc_cap = 0;
+    long version = 0, tc_version = -1;
     std::string err;
 };
 
@@ -273,11 +281,91 @@ void upload_inputs(bem_mlp* p, int B, const double* x, const double* y, std::vec
     }
 }
 
+// The tensor-core operand image of the current weights and n samples of I/O space.
+bem_status ensure_tc(bem_mlp* p, int n) {
+    if (!bem::tc_gemm_supported(p->device))
+        return mlp_fail(p, "tensor-core inference needs an sm_103 GPU", BEM_ERR_UNSUPPORTED);
+    if (!p->tc_img) {
+        MK(cudaMalloc(&p->tc_img, bem::mlp_tc_image_bytes()));
+        MK(cudaMalloc(&p->tc_f, sizeof(float) * bem::mlp_tc_param_floats()));
+        MK(cudaMalloc(&p->tc_flags, sizeof(int)));
+    }
+    if (n > p->tc_cap) {
+        cudaFree(p->tc_x);
+        cudaFree(p->tc_y);
+        p->tc_x = p->tc_y = nullptr;
+        p->tc_cap = 0;
+        MK(cudaMalloc(&p->tc_x, sizeof(float) * 2 * (size_t)n));
+        MK(cudaMalloc(&p->tc_y, sizeof(float) * 6 * (size_t)n));
+        p->tc_cap = n;
+    }
+    if (p->tc_version != p->version) {
+        bem::mlp_tc_build_image(p->st, p->w, p->tc_img, p->tc_f);
+        p->tc_version = p->version;
+    }
+    MK(cudaMemsetAsync(p->tc_flags, 0, sizeof(int), p->st));
+    return BEM_OK;
+}
+
+bem_status tc_flags_ok(bem_mlp* p) {
+    int hf = 0;
+    MK(cudaMemcpyAsync(&hf, p->tc_flags, sizeof(int), cudaMemcpyDeviceToHost, p->st));
+    MK(cudaStreamSynchronize(p->st));
+    if (hf & bem::FLAG_TIMEOUT) return mlp_fail(p, "a device-side wait of the tensor-core forward expired");
+    return BEM_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int bem_mlp_num_params(void) { return N_PARAMS; }
+
+bem_status bem_mlp_eval_tc(bem_mlp* p, int n, const double* x, double* y) {
+    if (!p || n < 0 || (n > 0 && (!x || !y))) return BEM_ERR_ARG;
+    MK(cudaSetDevice(p->device));
+    if (n == 0) return BEM_OK;
+    bem_status s = ensure_tc(p, n);
+    if (s != BEM_OK) return s;
+    std::vector<float> hx((size_t)n * 2), hy((size_t)n * 6);
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < 2; ++c) hx[2 * (size_t)i + c] = (float)((x[2 * (size_t)i + c] - p->in_shift[c]) / p->in_scale[c]);
+    MK(cudaMemcpyAsync(p->tc_x, hx.data(), hx.size() * 4, cudaMemcpyHostToDevice, p->st));
+    if (bem::mlp_tc_forward(p->st, n, p->tc_x, p->tc_y, p->tc_img, p->tc_f, p->tc_flags))
+        return mlp_fail(p, "tensor-core forward launch failed");
+    MK(cudaMemcpyAsync(hy.data(), p->tc_y, hy.size() * 4, cudaMemcpyDeviceToHost, p->st));
+    s = tc_flags_ok(p);
+    if (s != BEM_OK) return s;
+    for (size_t i = 0; i < (size_t)n; ++i)
+        for (int c = 0; c < 6; ++c) y[6 * i + c] = hy[6 * i + c] * p->out_scale[c] + p->out_shift[c];
+    return BEM_OK;
+}
+
+bem_status bem_mlp_throughput_tc(bem_mlp* p, int n, double* evals_per_s) {
+    if (!p || n <= 0 || !evals_per_s) return BEM_ERR_ARG;
+    MK(cudaSetDevice(p->device));
+    bem_status s = ensure_tc(p, n);
+    if (s != BEM_OK) return s;
+    MK(cudaMemsetAsync(p->tc_x, 0, sizeof(float) * 2 * (size_t)n, p->st));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    bem::mlp_tc_forward(p->st, n, p->tc_x, p->tc_y, p->tc_img, p->tc_f, p->tc_flags);  // warm-up
+    cudaEventRecord(e0, p->st);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) bem::mlp_tc_forward(p->st, n, p->tc_x, p->tc_y, p->tc_img, p->tc_f, p->tc_flags);
+    cudaEventRecord(e1, p->st);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ce != cudaSuccess) return mlp_fail(p, cudaGetErrorString(ce));
+    s = tc_flags_ok(p);
+    if (s != BEM_OK) return s;
+    *evals_per_s = (double)n * reps / (ms / 1000.0);
+    return BEM_OK;
+}
 
 bem_status bem_mlp_create(bem_mlp** out, int device, unsigned long long seed) {
     if (!out) return BEM_ERR_ARG;
@@ -328,6 +416,7 @@ void bem_mlp_destroy(bem_mlp* p) {
     for (int l = 0; l <= NL; ++l) cudaFree(p->A[l]);
     cudaFree(p->dA); cudaFree(p->dZ); cudaFree(p->T);
     cudaFree(p->w); cudaFree(p->wb); cudaFree(p->m); cudaFree(p->v); cudaFree(p->g); cudaFree(p->d_loss);
+    cudaFree(p->tc_img); cudaFree(p->tc_f); cudaFree(p->tc_flags); cudaFree(p->tc_x); cudaFree(p->tc_y);
     if (p->st) cudaStreamDestroy(p->st);
     delete p;
 }
@@ -366,6 +455,7 @@ bem_status bem_mlp_set_params(bem_mlp* p, const double* w) {
     MK(cudaMemcpyAsync(p->w, h.data(), 4 * N_PARAMS, cudaMemcpyHostToDevice, p->st));
     BEM_LAUNCH(k_to_bf16<<<(N_PARAMS + 255) / 256, 256, 0, p->st>>>(N_PARAMS, p->w, p->wb));
     MK(cudaStreamSynchronize(p->st));
+    ++p->version;
     p->adam_t = 0;
     MK(cudaMemsetAsync(p->m, 0, 4 * N_PARAMS, p->st));
     MK(cudaMemsetAsync(p->v, 0, 4 * N_PARAMS, p->st));
@@ -459,6 +549,7 @@ bem_status bem_mlp_train(bem_mlp* p, int n, const double* x, const double* y, in
     cudaError_t ce = cudaStreamSynchronize(p->st);
     cudaFree(dx);
     cudaFree(dy);
+    ++p->version;
     if (ce != cudaSuccess) return mlp_fail(p, std::string("training: ") + cudaGetErrorString(ce));
     return BEM_OK;
 }

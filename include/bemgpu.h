@@ -363,6 +363,14 @@ bem_status bem_mlp_eval(bem_mlp* m, int n, const double* x, double* y);
 bem_status bem_mlp_grad(bem_mlp* m, int n, const double* x, const double* y, double* grad, double* loss);
 bem_status bem_mlp_train(bem_mlp* m, int n, const double* x, const double* y, int epochs, int batch, double lr,
                          unsigned long long seed, double* loss_per_epoch);
+/* Forward pass on the tensor cores (tcgen05 kind::f16: BF16 weights and activations,
+ * FP32 accumulation in TMEM, SiLU as x/2 (1 + tanh(x/2)) with the hardware tanh):
+ * the inference form the assembly uses.  It differs from bem_mlp_eval (FP32
+ * activations) by the BF16 rounding of the activations (about 1e-3 relative).
+ * Needs an sm_103 GPU (BEM_ERR_UNSUPPORTED otherwise). */
+bem_status bem_mlp_eval_tc(bem_mlp* m, int n, const double* x, double* y);
+/* Throughput of the tensor-core forward pass (evaluations per second of device time). */
+bem_status bem_mlp_throughput_tc(bem_mlp* m, int n, double* mlp_evals_per_s);
 /* Forward-pass throughput (evaluations per second of device time) on n resident samples. */
 bem_status bem_mlp_throughput(bem_mlp* m, int n, double* mlp_evals_per_s);
 /* Throughput of the closed-form HavelockGF kernel (evaluations per second of device

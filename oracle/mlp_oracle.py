@@ -37,9 +37,11 @@ def silu_d(z):
     return s * (1.0 + z * (1.0 - s))
 
 
-def forward(params, x, quantize=True):
+def forward(params, x, quantize=True, act_bf16=False):
     """x: n x 2 normalised inputs; returns (y, pre-activations, activations).
-    quantize=False uses the weights as given (for finite-difference checks)."""
+    quantize=False uses the weights as given (for finite-difference checks);
+    act_bf16=True also rounds every hidden activation to BF16, as the tensor-core
+    inference (whose MMA operands are BF16) does."""
     a = np.asarray(x, dtype=np.float64)
     zs, acts = [], [a]
     layers = unpack(np.asarray(params, dtype=np.float64))
@@ -48,6 +50,8 @@ def forward(params, x, quantize=True):
         z = a @ Wq.T + b
         zs.append(z)
         a = silu(z) if l < len(layers) - 1 else z
+        if act_bf16 and l < len(layers) - 1:
+            a = bf16(a).astype(np.float64)
         acts.append(a)
     return a, zs, acts
 

@@ -66,6 +66,34 @@ def test_gpu_forward_backward_match_oracle():
 
 
 @pytest.mark.gpu
+def test_tensor_core_forward_matches_oracle():
+    """The tcgen05 forward (BF16 weights and activations, FP32 accumulation in TMEM)
+    against the oracle with BF16-rounded activations, on a sample count that is not a
+    multiple of the 128-sample tile.  Differences come from FP32 summation order, the
+    hardware tanh in SiLU and the BF16 roundings these shift; a wrong operand layout
+    would give O(1) errors."""
+    import bemuse_gb300 as bg
+    s = bg.HavelockSurrogate(seed=4)
+    p = _rand_params(6)
+    s.set_params(p)
+    s.set_normalization([0, 0], [1, 1], np.zeros(6), np.ones(6))
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=(1000, 2)) * 1.5
+    y_tc = s.eval_tc(x)
+    y_ref = mo.forward(p, x, act_bf16=True)[0]
+    err = np.max(np.abs(y_tc - y_ref)) / np.max(np.abs(y_ref))
+    err32 = np.max(np.abs(y_tc - s.eval(x))) / np.max(np.abs(y_ref))
+    print("tensor-core forward vs BF16-activation oracle %.3e, vs FP32-activation kernel %.3e" % (err, err32))
+    assert err < 1e-2 and err32 < 2e-2
+    # the weights change: the operand image follows
+    p2 = _rand_params(7)
+    s.set_params(p2)
+    err2 = np.max(np.abs(s.eval_tc(x[:130]) - mo.forward(p2, x[:130], act_bf16=True)[0])) / np.max(
+        np.abs(mo.forward(p2, x[:130], act_bf16=True)[0]))
+    assert err2 < 1e-2
+
+
+@pytest.mark.gpu
 def test_training_and_gain_report():
     """Trains on the plain integrator's samples and reports accuracy and throughput
     against the FP32 closed form; the closed form is expected to win (a negative
