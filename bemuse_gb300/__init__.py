@@ -133,6 +133,8 @@ def lib():
         "bem_aero_setup": ([vp, ctypes.POINTER(_Mesh)], c_int),
         "bem_aero_solve": ([vp, c_int, _dp, c_int, c_double, _dp, _dp], c_int),
         "bem_fp32_peak": ([c_int, _dp], c_int),
+        "bem_set_surrogate": ([vp, vp, c_int, c_double, c_double, _dp], c_int),
+        "bem_surrogate_stats": ([vp, _dp, c_int], c_int),
         "bem_tc_probe": ([c_int, c_int, c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp], c_int),
     }
     for name, (args, res) in sig.items():
@@ -569,6 +571,24 @@ class Hydrodynamic_Radiation_Solver:
         _check(lib().bem_stage_times(self._h, _p(t), int(reset)), self._h)
         return t
 
+    def set_surrogate(self, surrogate, mode="strict", judge_tol=1e-6, judge_fraction=0.01, domain=None):
+        """Far-field wave terms from a trained HavelockSurrogate (bem_set_surrogate): mode
+        "strict" solves again, with the closed form, every frequency whose judged error
+        exceeds judge_tol; "accept" keeps the network's values; None turns it off."""
+        m = {None: 0, "off": 0, "strict": 1, "accept": 2}[mode]
+        dom = None if domain is None else np.ascontiguousarray(domain, dtype=np.float64)
+        self._surrogate = surrogate if m else None  # keeps the network alive while it is used
+        _check(lib().bem_set_surrogate(self._h, surrogate._h if m else None, m, float(judge_tol),
+                                       float(judge_fraction), _p(dom) if dom is not None else None), self._h)
+
+    def surrogate_stats(self, reset=True):
+        """Totals of the surrogate form since the last reset (bem_surrogate_stats)."""
+        v = np.zeros(7)
+        _check(lib().bem_surrogate_stats(self._h, _p(v), int(reset)), self._h)
+        return {"gauss_points_network": int(v[0]), "gauss_points_closed_form": int(v[1]), "judged_pairs": int(v[2]),
+                "judged_error_max": float(v[3]), "frequencies_resolved": int(v[4]),
+                "frequencies_with_surrogate": int(v[5])}
+
     def set_tuning(self, key, value):
         _check(lib().bem_set_tuning(self._h, key.encode(), float(value)), self._h)
 
@@ -724,6 +744,58 @@ class HavelockSurrogate:
         r = np.zeros(1)
         self._chk(lib().bem_mlp_throughput(self._h, int(n), _p(r)))
         return float(r[0])
+
+    # The domain where the surrogate stands in for HavelockGF: far-field pairs with
+    # K R and K Z inside these ranges (the rest is out of domain and keeps the closed form).
+    KR_RANGE = (1.0e-3, 20.0)
+    KZ_RANGE = (-40.0, 0.0)
+
+    @staticmethod
+    def envelope(kr, kz):
+        """Per-sample scales of the six outputs (Re/Im of G, dG/dR, dG/dZ) that make the
+        targets O(1) over the domain: 2/(d + 0.05) + w for G and dG/dZ (= G in the
+        reference form), 2 KR/(d^2 (1 + d)) + w for dG/dR and w = 2 pi e^KZ / sqrt(1 + KR)
+        (the wave part's envelope) for the imaginary parts; d = sqrt(KR^2 + KZ^2).  The
+        fused assembly kernel computes the same expressions in FP32."""
+        kr = np.asarray(kr, dtype=np.float64)
+        kz = np.asarray(kz, dtype=np.float64)
+        d = np.sqrt(kr * kr + kz * kz)
+        w = 2.0 * np.pi * np.exp(kz) / np.sqrt(1.0 + kr)
+        eg = 2.0 / (d + 0.05) + w
+        er = 2.0 * kr / (d * d * (1.0 + d) + 1e-12) + w
+        return np.stack([eg, w, er, w, eg, w], axis=-1)
+
+    @staticmethod
+    def domain_set(n, seed=0, device=0):
+        """Samples of the surrogate's domain and their targets from the plain FP64
+        integrator: inputs (log10 KR, KZ) with KR log-uniform on KR_RANGE and KZ on
+        KZ_RANGE (half uniform, half concentrated near the free surface, where the wave
+        part is largest); returns inputs x (n x 2), the six outputs y (n x 6) and the
+        scaled targets t = y / envelope."""
+        rng = np.random.default_rng(seed)
+        lo, hi = np.log10(HavelockSurrogate.KR_RANGE[0]), np.log10(HavelockSurrogate.KR_RANGE[1])
+        lkr = rng.uniform(lo, hi, n)
+        u = rng.uniform(0.0, 1.0, n)
+        half = rng.uniform(0.0, 1.0, n) < 0.5
+        kz = HavelockSurrogate.KZ_RANGE[0] * np.where(half, u, u ** 3)
+        g = havelock_gf(10.0 ** lkr, np.zeros(n), kz, PLAIN_FP64, device)
+        y = np.stack([g[:, 0].real, g[:, 0].imag, g[:, 1].real, g[:, 1].imag, g[:, 3].real, g[:, 3].imag], axis=1)
+        return np.stack([lkr, kz], axis=1), y, y / HavelockSurrogate.envelope(10.0 ** lkr, kz)
+
+    def set_domain_normalization(self, t):
+        """Fixed input normalisation of the domain (log10 KR and KZ mapped to [-1, 1]) and
+        per-output standardisation of the scaled targets t."""
+        lo, hi = np.log10(self.KR_RANGE[0]), np.log10(self.KR_RANGE[1])
+        z0, z1 = self.KZ_RANGE
+        self.set_normalization([(lo + hi) / 2, (z0 + z1) / 2], [(hi - lo) / 2, (z1 - z0) / 2], t.mean(0),
+                               t.std(0) + 1e-12)
+
+    def predict(self, x, tensor_cores=True):
+        """The six outputs at raw inputs x = (log10 KR, KZ): the network's scaled output
+        times the envelope."""
+        x = np.asarray(x, dtype=np.float64).reshape(-1, 2)
+        t = self.eval_tc(x) if tensor_cores else self.eval(x)
+        return t * self.envelope(10.0 ** x[:, 0], x[:, 1])
 
     @staticmethod
     def training_set(n, seed=0, device=0, kr=(1e-3, 200.0), kz=(-100.0, 0.0)):

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct bem_mlp;
+
 namespace bem {
 
 // Count of kernel launches issued by this library (all contexts).
@@ -75,6 +77,30 @@ struct WaveArgs {
     int live;
 };
 void set_wave_f32_constants(WaveArgs& a);
+
+// The surrogate form of the mixed assembly (k_wave_surrogate): far-field pairs inside the
+// network's domain take G and dG/dh from the tensor-core network, the rest (pairs nearer
+// than `near` panel diameters, out-of-domain pairs and a seeded sample of far pairs, the
+// judge) from the FP32 closed form.  Re ws goes to ws32 ([N][ld]); the host adds -ws32 B
+// to the right-hand sides.  stats (zeroed by the caller): [0] Gauss points by the network,
+// [1] by the closed form, [2] judged pairs, [3] largest judged error |surrogate - closed
+// form| / envelope as float bits.
+struct SurArgs {
+    const uint8_t* img;       // operand image and FP32 tail of the network (mlp_tc_build_image)
+    const float* fw;
+    float in_shift[2], in_scale[2], out_shift[6], out_scale[6];
+    float kr_min, kr_max, kz_min;  // the domain in K R and K Z
+    float near2;              // (near-field distance in panel diameters)^2
+    const float* pdiam;       // panel diameters [N]
+    unsigned judge_mod;       // a far pair is judged if hash(row, column, seed) % judge_mod == 0
+    unsigned judge_seed;
+    float* ws32;
+    unsigned long long* stats;
+    int* gflags;
+};
+// Launches k_wave_surrogate on the persistent-assembly counters of a (a.mode 0 or 1); nonzero
+// if the launch failed.
+int launch_wave_surrogate(cudaStream_t st, const WaveArgs& a, const SurArgs& sa);
 
 cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
@@ -212,6 +238,17 @@ int mlp_tc_image_bytes();
 int mlp_tc_param_floats();
 void mlp_tc_build_image(cudaStream_t st, const float* w, uint8_t* img, float* fw);
 int mlp_tc_forward(cudaStream_t st, int n, const float* x, float* y, const uint8_t* img, const float* fw, int* flags);
+
+// The network of a bem_mlp as the assembly uses it: operand image, FP32 tail and the
+// input / output normalisation (built for the current weights; synchronises the network's
+// stream).  Returns nonzero (message in bem_mlp_last_error) if that fails.
+struct MlpTcRef {
+    const uint8_t* img;
+    const float* fw;
+    double in_shift[2], in_scale[2], out_shift[6], out_scale[6];
+    int device;
+};
+int mlp_tc_ref(struct ::bem_mlp* m, MlpTcRef* out);
 
 int tc_gemm_supported(int device);
 // Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA), or < 0 on failure.

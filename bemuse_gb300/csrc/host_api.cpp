@@ -53,6 +53,9 @@ struct FreqState {
     cudaEvent_t ev_free = nullptr;            // solves of this slot done: buffers reusable
     cudaEvent_t ev_t[4] = {};                 // timing: assembly start, static RHS done, wave kernel start/end
     cudaEvent_t ev_t5 = nullptr;              // timing: assembly end
+    float* Ws32 = nullptr;                    // surrogate form: Re ws per pair [N][Np]
+    unsigned long long* sur_stats = nullptr;  // surrogate form: the assembly's counts (SurArgs::stats)
+    bool sur_used = false;                    // this slot's frequency was assembled with the surrogate
 };
 
 // One captured tensor-core LU (per frequency slot) and what it was captured for.
@@ -103,6 +106,16 @@ struct bem_ctx {
     int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
     int refine_coarse_first = 1;  // 1: the first classic sweep's residual from the FP32 high words
     int refine_max = 60;          // preconditioner solves the refinement may use before it fails
+    // surrogate form of the mixed assembly (bem_set_surrogate): the network, the mode (0 off,
+    // 1 strict: a frequency whose judged error exceeds sur_tol is solved again with the closed
+    // form, 2 accept), the judged fraction of far pairs and the domain {KR min, KR max, KZ min,
+    // near-field distance in panel diameters}; totals since the last reset (bem_surrogate_stats)
+    bem_mlp* sur = nullptr;
+    int sur_mode = 0;
+    double sur_tol = 1e-6, sur_judge = 0.01;
+    double sur_dom[4] = {1.0e-3, 20.0, -40.0, 3.0};
+    double sur_totals[7] = {0, 0, 0, 0, 0, 0, 0};
+    float* d_pdiam = nullptr;     // panel diameters (largest vertex distance), for the near-field test
     // failure-detection tests only: the triangular-solve chain waits for a flag value that
     // nothing publishes (test_wait_skew > 0) and gives up after test_wait_ns
     int test_wait_skew = 0;
@@ -203,6 +216,9 @@ void reset_slot(FreqState& F) {
     F.Bm = F.Y = F.phiI = F.dphiI = F.mx = F.pwT = nullptr;
     F.pw_Mmax = F.pw_M = 0;
     F.pw_K = -1.0;
+    F.Ws32 = nullptr;
+    F.sur_stats = nullptr;
+    F.sur_used = false;
 }
 
 void free_all(bem_ctx* ctx) {
@@ -233,6 +249,7 @@ void free_all(bem_ctx* ctx) {
         g = LuGraph();
     }
     ctx->d_wctr = nullptr;
+    ctx->d_pdiam = nullptr;
     ctx->wpts_dirty = true;
     ctx->ready = false;
 }
@@ -1068,7 +1085,21 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
     DA(ctx->d_xr32, xr32.size());
     DA(ctx->d_gq32, gq32.size());
+    std::vector<float> pdiam(N);
+    for (int i = 0; i < N; ++i) {
+        const bem::PanelGeom& pg = mirror[i];
+        double dmax = 0.0;
+        for (int u = 0; u < pg.nv; ++u)
+            for (int v = u + 1; v < pg.nv; ++v) {
+                double d2 = 0.0;
+                for (int k = 0; k < 3; ++k) d2 += (pg.v[3 * u + k] - pg.v[3 * v + k]) * (pg.v[3 * u + k] - pg.v[3 * v + k]);
+                dmax = std::max(dmax, std::sqrt(d2));
+            }
+        pdiam[i] = (float)dmax;
+    }
+    DA(ctx->d_pdiam, N);
     cudaStream_t st = ctx->st;
+    CK(cudaMemcpyAsync(ctx->d_pdiam, pdiam.data(), pdiam.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_xr32, xr32.data(), xr32.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_gq32, gq32.data(), gq32.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
@@ -1185,8 +1216,42 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         a.per_sm = overlapped && ctx->asm_overlap ? ctx->asm_per_sm : 3;
         a.split = ctx->asm_split;
     }
+    F.sur_used = mixed && ctx->sur && ctx->sur_mode > 0 && K != 0.0;
+    bem::SurArgs sa = {};
+    if (F.sur_used) {
+        DA(F.Ws32, (size_t)N * Np);
+        DA(F.sur_stats, 4);
+        bem::MlpTcRef ref;
+        if (bem::mlp_tc_ref(ctx->sur, &ref) != 0)
+            return fail(ctx, BEM_ERR_CUDA, std::string("surrogate: ") + bem_mlp_last_error(ctx->sur));
+        if (ref.device != ctx->device) return fail(ctx, BEM_ERR_ARG, "surrogate: the network is on another device");
+        CK(cudaSetDevice(ctx->device));
+        sa.img = ref.img;
+        sa.fw = ref.fw;
+        for (int c = 0; c < 2; ++c) { sa.in_shift[c] = (float)ref.in_shift[c]; sa.in_scale[c] = (float)ref.in_scale[c]; }
+        for (int c = 0; c < 6; ++c) { sa.out_shift[c] = (float)ref.out_shift[c]; sa.out_scale[c] = (float)ref.out_scale[c]; }
+        sa.kr_min = (float)ctx->sur_dom[0];
+        sa.kr_max = (float)ctx->sur_dom[1];
+        sa.kz_min = (float)ctx->sur_dom[2];
+        sa.near2 = (float)(ctx->sur_dom[3] * ctx->sur_dom[3]);
+        sa.pdiam = ctx->d_pdiam;
+        sa.judge_mod = ctx->sur_judge > 0 ? (unsigned)std::max(1.0, std::round(1.0 / ctx->sur_judge)) : 0u;
+        uint64_t kb;
+        memcpy(&kb, &K, 8);
+        sa.judge_seed = (unsigned)(kb ^ (kb >> 32));
+        sa.ws32 = F.Ws32;
+        sa.stats = F.sur_stats;
+        sa.gflags = ctx->d_flags;
+        CK(cudaMemsetAsync(F.sur_stats, 0, sizeof(unsigned long long) * 4, st));
+    }
     CK(cudaEventRecord(F.ev_t[2], st));
-    bem::launch_wave(st, a, mixed);
+    if (F.sur_used) {
+        if (bem::launch_wave_surrogate(st, a, sa)) return fail(ctx, BEM_ERR_CUDA, "surrogate assembly launch failed");
+        // S B += -Re(ws) B (the closed-form path accumulates this inside k_wave_mixed)
+        bem::launch_matx_df(st, N, Np, F.Ws32, nullptr, R, F.Bm, R, 0, F.Xdf, F.mx, -1.0, 1.0, F.Y, F.Y, R);
+    } else {
+        bem::launch_wave(st, a, mixed);
+    }
     CK(cudaEventRecord(F.ev_t[3], st));
     if (mixed && K != 0.0) {
         // exact imaginary part of S applied to B:  Y += -i Im(ws) B
@@ -1264,6 +1329,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     };
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
+    std::vector<int> sur_redo;  // strict surrogate mode: frequencies whose judged error exceeded the tolerance
     if (n_freq > 0) {
         s = enqueue_assembly(0);
         if (s != BEM_OK) return s;
@@ -1350,6 +1416,20 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         CK(cudaEventRecord(ctx->ev[7], st));
         CK(cudaEventRecord(F.ev_free, st));
         CK(cudaStreamSynchronize(st));
+        if (F.sur_used) {
+            // the surrogate assembly's counts and judged error for this frequency
+            unsigned long long hs[4] = {0, 0, 0, 0};
+            CK(cudaMemcpy(hs, F.sur_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+            const uint32_t eb = (uint32_t)hs[3];
+            float err;
+            memcpy(&err, &eb, 4);
+            ctx->sur_totals[0] += (double)hs[0];
+            ctx->sur_totals[1] += (double)hs[1];
+            ctx->sur_totals[2] += (double)hs[2];
+            ctx->sur_totals[3] = std::max(ctx->sur_totals[3], (double)err);
+            ctx->sur_totals[5] += 1;
+            if (ctx->sur_mode == 1 && !((double)err <= ctx->sur_tol)) sur_redo.push_back(f);
+        }
         // split [n][R] rows into the radiation [f][n][6] and diffraction [f][n][NB] blocks
         auto split_ext = [&](const std::vector<double>& e, int n, double* rad, double* diff) {
             for (int w = 0; w < n; ++w) {
@@ -1426,6 +1506,84 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
                                 sizeof(double) * 2 * NB, NPA, cudaMemcpyDeviceToHost));
         }
     }
+    if (!sur_redo.empty()) {
+        // strict surrogate mode: the judge found the network's error above the tolerance at
+        // these frequencies, which are solved again with the closed form (the plain
+        // integrator of the fallback) and their results replaced
+        const int nr = (int)sur_redo.size();
+        const int NW = (int)(ctx->wave_pts.size() / 3), NK = ctx->n_kochin;
+        std::vector<double> om_r(nr);
+        for (int i = 0; i < nr; ++i) om_r[i] = omega[sur_redo[i]];
+        const bool last = sur_redo.back() == n_freq - 1;
+        struct Blk { double* dst; size_t per; std::vector<double> tmp; };
+        std::vector<Blk> blk;
+        bem_result sub = {};
+        auto add = [&](double* dst, size_t per) -> double* {
+            if (!dst) return nullptr;
+            blk.push_back(Blk{dst, per, std::vector<double>(per * nr)});
+            return blk.back().tmp.data();
+        };
+        blk.reserve(12);
+        if (out) {
+            sub.A = add(out->A, 36);
+            sub.B = add(out->B, 36);
+            sub.FK = add(out->FK, 12 * (size_t)NB);
+            sub.SC = add(out->SC, 12 * (size_t)NB);
+            sub.F = add(out->F, 12 * (size_t)NB);
+            sub.RAO = add(out->RAO, 12 * (size_t)NB);
+            sub.residual = add(out->residual, 1);
+            sub.fs_rad = add(out->fs_rad, 12 * (size_t)NW);
+            sub.fs_diff = add(out->fs_diff, 2 * (size_t)NB * NW);
+            sub.kochin_rad = add(out->kochin_rad, 12 * (size_t)NK);
+            sub.kochin_diff = add(out->kochin_diff, 2 * (size_t)NB * NK);
+            if (last) {
+                sub.phi_rad = out->phi_rad;
+                sub.phi_scat = out->phi_scat;
+            }
+        }
+        std::vector<int> it_r(nr);
+        if (out && out->refine_iters) sub.refine_iters = it_r.data();
+        const int mode = ctx->sur_mode;
+        ctx->sur_mode = 0;
+        const bem_status rs = bem_solve(ctx, nr, om_r.data(), precision, tol, out ? &sub : nullptr);
+        ctx->sur_mode = mode;
+        if (rs != BEM_OK) return rs;
+        for (Blk& b : blk)
+            for (int i = 0; i < nr; ++i)
+                std::copy(b.tmp.begin() + b.per * i, b.tmp.begin() + b.per * (i + 1), b.dst + b.per * sur_redo[i]);
+        if (out && out->refine_iters)
+            for (int i = 0; i < nr; ++i) out->refine_iters[sur_redo[i]] = it_r[i];
+        ctx->sur_totals[4] += nr;
+    }
+    return BEM_OK;
+}
+
+bem_status bem_set_surrogate(bem_ctx* ctx, bem_mlp* m, int mode, double judge_tol, double judge_fraction,
+                             const double* domain) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (mode < 0 || mode > 2) return fail(ctx, BEM_ERR_ARG, "surrogate mode must be 0 (off), 1 (strict) or 2 (accept)");
+    if (mode > 0 && !m) return fail(ctx, BEM_ERR_ARG, "surrogate: null network");
+    if (!(judge_fraction >= 0.0 && judge_fraction <= 1.0))
+        return fail(ctx, BEM_ERR_ARG, "surrogate: judge fraction must be in [0, 1]");
+    if (mode == 1 && !(judge_fraction > 0.0))
+        return fail(ctx, BEM_ERR_ARG, "surrogate: the strict mode needs a judged fraction > 0");
+    if (!(judge_tol >= 0.0)) return fail(ctx, BEM_ERR_ARG, "surrogate: judge tolerance must be >= 0");
+    if (domain && !(domain[0] > 0.0 && domain[1] >= domain[0] && domain[2] <= 0.0 && domain[3] >= 0.0))
+        return fail(ctx, BEM_ERR_ARG, "surrogate: domain must be {KR min > 0, KR max >= KR min, KZ min <= 0, near >= 0}");
+    if (mode > 0 && !bem::tc_gemm_supported(ctx->device))
+        return fail(ctx, BEM_ERR_UNSUPPORTED, "surrogate: the tensor-core network needs an sm_103 GPU");
+    ctx->sur = mode > 0 ? m : nullptr;
+    ctx->sur_mode = mode;
+    ctx->sur_tol = judge_tol;
+    ctx->sur_judge = judge_fraction;
+    if (domain) memcpy(ctx->sur_dom, domain, sizeof(ctx->sur_dom));
+    return BEM_OK;
+}
+
+bem_status bem_surrogate_stats(bem_ctx* ctx, double* out7, int reset) {
+    if (!ctx || !out7) return fail(ctx, BEM_ERR_ARG, "bem_surrogate_stats: bad arguments");
+    memcpy(out7, ctx->sur_totals, sizeof(ctx->sur_totals));
+    if (reset) memset(ctx->sur_totals, 0, sizeof(ctx->sur_totals));
     return BEM_OK;
 }
 

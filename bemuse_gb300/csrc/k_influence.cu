@@ -18,6 +18,7 @@
 #include "bem_internal.h"
 #include <algorithm>
 #include "green.cuh"
+#include "mlp_tc.cuh"
 
 namespace bem {
 
@@ -215,52 +216,84 @@ __device__ __forceinline__ Recv32 load_recv32(const WaveArgs& a, int r) {
                   a.xr32[5 * N + r]};
 }
 
-// One Gauss point of a mirrored wave panel (coordinates as float pairs g*, g*l; normal n;
-// weights wc1 = w K/4pi, wc2 = w K^2/4pi) at receiver R: adds its FP32 terms of ws and wd
-// (FreeSurface_Wave_Kernel and CInf_SingleDoubleLayerQuad, Panel.cpp:601-636, 776-794).
-__device__ __forceinline__ void gauss_eval32(const Recv32& R, float gx, float gy, float gz, float gxl, float gyl,
-                                             float gzl, float nx, float ny, float nz, float wc1, float wc2, float Kh,
-                                             float Kl, float& wsr, float& wsi, float& wdr, float& wdi) {
-    const float twopi = 6.28318530717959f;
+// Geometry of one (receiver, Gauss point) pair of the mixed assembly: coordinate
+// differences as float pairs, K (x, y) and the nondimensional h = (hh, hl), v = (VV, vl)
+// as float pairs.
+struct GaussGeo {
+    float sx, lx, sy, ly, sz, ez;  // dimensional differences receiver - Gauss point (hi, lo)
+    float XX, YY;                  // K dx, K dy
+    float hh, hl, VV, vl;
+};
+
+__device__ __forceinline__ GaussGeo gauss_geo32(const Recv32& R, float gx, float gy, float gz, float gxl, float gyl,
+                                                float gzl, float Kh, float Kl) {
+    GaussGeo o;
     const float K = Kh;
     // coordinate differences as float pairs (two-differences of the hi parts + lo parts)
-    const float sx = R.xh - gx, sy = R.yh - gy;
-    const float bx = sx - R.xh, by = sy - R.yh;
-    const float lx = ((R.xh - (sx - bx)) - (gx + bx)) + (R.xl - gxl);
-    const float ly = ((R.yh - (sy - by)) - (gy + by)) + (R.yl - gyl);
+    o.sx = R.xh - gx;
+    o.sy = R.yh - gy;
+    const float bx = o.sx - R.xh, by = o.sy - R.yh;
+    o.lx = ((R.xh - (o.sx - bx)) - (gx + bx)) + (R.xl - gxl);
+    o.ly = ((R.yh - (o.sy - by)) - (gy + by)) + (R.yl - gyl);
     // v = K (z_r - z_q) as a float pair (VV, vl), like h = (hh, hl)
-    const float sz = R.zh - gz;
-    const float bz = sz - R.zh;
-    const float ez = ((R.zh - (sz - bz)) - (gz + bz)) + (R.zl - gzl);
-    const float vh = sz * Kh;
-    const float vlo = fmaf(sz, Kh, -vh) + fmaf(sz, Kl, ez * Kh);
-    const float VV = vh + vlo;
-    const float vl = vlo - (VV - vh);
-    const float XX = (sx + lx) * K, YY = (sy + ly) * K;
-    float hh, hl;
-    df_hdist(sx, lx, sy, ly, Kh, Kl, hh, hl);
-    const float ev = expf(VV);
+    o.sz = R.zh - gz;
+    const float bz = o.sz - R.zh;
+    o.ez = ((R.zh - (o.sz - bz)) - (gz + bz)) + (R.zl - gzl);
+    const float vh = o.sz * Kh;
+    const float vlo = fmaf(o.sz, Kh, -vh) + fmaf(o.sz, Kl, o.ez * Kh);
+    o.VV = vh + vlo;
+    o.vl = vlo - (o.VV - vh);
+    o.XX = (o.sx + o.lx) * K;
+    o.YY = (o.sy + o.ly) * K;
+    df_hdist(o.sx, o.lx, o.sy, o.ly, Kh, Kl, o.hh, o.hl);
+    return o;
+}
+
+// HavelockGF at the pair by the FP32 closed form: Re/Im of G and of dG/dh.
+__device__ __forceinline__ void gauss_G32(const GaussGeo& o, float& Gr, float& Gi, float& Ghr, float& Ghi) {
+    const float twopi = 6.28318530717959f;
+    const float ev = expf(o.VV);
     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
-    if (hh > 3.0f) bessel_large(hh, hl, j0v, j1v, y0v, y1v);
-    else bessel_j01_small(hh, j0v, j1v);
-    float Gr, Ghr, Gv;
-    gf32_re(c_poly32, hh, VV, ev, y0v, y1v, Gr, Ghr, Gv);
+    if (o.hh > 3.0f) bessel_large(o.hh, o.hl, j0v, j1v, y0v, y1v);
+    else bessel_j01_small(o.hh, j0v, j1v);
+    float Gv;
+    gf32_re(c_poly32, o.hh, o.VV, ev, y0v, y1v, Gr, Ghr, Gv);
     // G at the unrounded (h, v): the first-order terms of the float pairs' low parts.
     // The radiation damping is a small difference of terms that each carry this
     // rounding, so without it B loses ~1e-6 at the highest frequencies.
-    Gr = fmaf(Ghr, hl, fmaf(Gv, vl, Gr));
-    const float proj = fmaf(XX, nx, YY * ny);
+    Gr = fmaf(Ghr, o.hl, fmaf(Gv, o.vl, Gr));
+    Ghi = twopi * ev * j1v;
+    Gi = -twopi * ev * j0v;
+}
+
+// The pair's terms of ws and wd from G and dG/dh at one Gauss point (normal n, weights
+// wc1 = w K/4pi, wc2 = w K^2/4pi): FreeSurface_Wave_Kernel and
+// CInf_SingleDoubleLayerQuad (Panel.cpp:601-636, 776-794).
+__device__ __forceinline__ void gauss_accum32(const GaussGeo& o, float Gr, float Gi, float Ghr, float Ghi, float nx,
+                                              float ny, float nz, float wc1, float wc2, float& wsr, float& wsi,
+                                              float& wdr, float& wdi) {
+    const float proj = fmaf(o.XX, nx, o.YY * ny);
     float dgr = 0.f, dgi = 0.f;
-    if (hh > 1.0e-6f) {
-        const float inv_h = __frcp_rn(hh);
+    if (o.hh > 1.0e-6f) {
+        const float inv_h = __frcp_rn(o.hh);
         dgr = Ghr * proj * inv_h;
-        dgi = twopi * ev * j1v * proj * inv_h;
+        dgi = Ghi * proj * inv_h;
     }
-    const float Gi = -twopi * ev * j0v;
     wsr = fmaf(wc1, Gr, wsr);
     wsi = fmaf(wc1, Gi, wsi);
     wdr = fmaf(wc2, fmaf(Gr, nz, dgr), wdr);
     wdi = fmaf(wc2, fmaf(Gi, nz, dgi), wdi);
+}
+
+// One Gauss point of a mirrored wave panel (coordinates as float pairs g*, g*l; normal n;
+// weights wc1 = w K/4pi, wc2 = w K^2/4pi) at receiver R: adds its FP32 terms of ws and wd.
+__device__ __forceinline__ void gauss_eval32(const Recv32& R, float gx, float gy, float gz, float gxl, float gyl,
+                                             float gzl, float nx, float ny, float nz, float wc1, float wc2, float Kh,
+                                             float Kl, float& wsr, float& wsi, float& wdr, float& wdi) {
+    const GaussGeo o = gauss_geo32(R, gx, gy, gz, gxl, gyl, gzl, Kh, Kl);
+    float Gr, Gi, Ghr, Ghi;
+    gauss_G32(o, Gr, Gi, Ghr, Ghi);
+    gauss_accum32(o, Gr, Gi, Ghr, Ghi, nx, ny, nz, wc1, wc2, wsr, wsi, wdr, wdi);
 }
 
 // Re D = RD + K RSR + wd_re in double-float arithmetic (RD, RSR stored as float pairs):
@@ -395,6 +428,197 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     if (threadIdx.x == 0) atomicSub(a.sm_ctr + smid, 1);
 }
 
+
+// ---------------------------------------------------------------------------
+// K2, surrogate form.  Work item = a receiver row x SUR_SB blocks of 32 source panels; a
+// warpgroup takes items from the counter and runs one 128-sample tile per block: thread
+// t = 4 p + q is Gauss point q of panel s0 + p.  Far pairs inside the network's domain
+// take G and dG/dh from the tensor-core network (mlp_tc.cuh), scaled back by the
+// envelope the network was trained on:
+//   G:      2 / (d + 0.05) + w,   dG/dh: 2 h / (d^2 (1 + d)) + w,   Im parts: w,
+//   w = 2 pi e^v / sqrt(1 + h), d = sqrt(h^2 + v^2);
+// near pairs (a Gauss point of the mirrored panel nearer than sqrt(near2) panel
+// diameters), out-of-domain pairs and the judged sample take the FP32 closed form
+// (gauss_G32).  A tile whose pairs all take the closed form skips the network.  The
+// imaginary parts of the operator and of S B still come from the plane waves (exact);
+// the network's imaginary parts only reach the FP32 copy that is factorised.
+constexpr int SUR_SB = 8;
+
+__device__ __forceinline__ bool wg_any(int g, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred pi, po;\n\t"
+        "setp.ne.u32 pi, %1, 0;\n\t"
+        "barrier.cta.red.or.pred po, %2, 128, pi;\n\t"
+        "selp.u32 %0, 1, 0, po;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + g)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ uint32_t pair_hash(uint32_t r, uint32_t s, uint32_t seed) {
+    uint32_t h = (r * 2654435761u) ^ (s * 2246822519u) ^ seed;
+    h ^= h >> 15;
+    h *= 0x2c1b3c6du;
+    h ^= h >> 12;
+    h *= 0x297a2d39u;
+    h ^= h >> 15;
+    return h;
+}
+
+__global__ void __launch_bounds__(mlptc::THREADS, 1) k_wave_surrogate(WaveArgs a, SurArgs sa) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_admit;
+    __shared__ int s_item[2];
+    uint32_t smid;
+    if (!wave_admit(a, smid, &s_admit)) return;
+    const mlptc::Smem m = mlptc::smem_layout(smem_raw);
+    const uint32_t tmem = mlptc::cta_setup(m, sa.img, sa.fw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = warp >> 2, t = threadIdx.x & 127;
+    const uint32_t acc = tmem + (uint32_t)g * 128;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t tile = m.s_tile0 + (uint32_t)g * mlptc::TILE_BYTES;
+    uint32_t phase = 0;
+    const int p = t >> 2, q = t & 3;
+    const int N = a.N;
+    const int nblk = (N + 31) / 32, ipr = (nblk + SUR_SB - 1) / SUR_SB;
+    const long long nitems = (long long)N * ipr;
+    const size_t fs = (size_t)4 * N;
+    const float Kh = a.kh, Kl = a.kl, c1 = a.c1f, c2 = a.c2f;
+    const float twopi = 6.28318530717959f;
+    unsigned long long n_mlp = 0, n_cf = 0, n_judge = 0;
+    float jerr = 0.f;
+    for (;;) {
+        if (t == 0) s_item[g] = atomicAdd(a.row_ctr, 1);
+        mlptc::wg_sync(g);
+        const int item = s_item[g];
+        mlptc::wg_sync(g);  // read by every thread before thread 0 draws the next item
+        if (item >= nitems) break;
+        const int r = item / ipr, b0 = (item % ipr) * SUR_SB;
+        const Recv32 Rv = load_recv32(a, r);
+        const size_t row = (size_t)r * a.ld;
+        for (int b = b0; b < min(b0 + SUR_SB, nblk); ++b) {
+            const int s = b * 32 + p;
+            const bool valid = s < N;
+            const int nq = (valid && a.live) ? __ldg(a.nq + s) : 0;
+            const bool active = q < nq;
+            GaussGeo o{};
+            float nx = 0.f, ny = 0.f, nz = 0.f, w = 0.f;
+            bool okq = true;
+            if (active) {
+                const float* gp = a.gq32 + (size_t)q * N + s;
+                w = __ldg(gp + 3 * fs);
+                nx = __ldg(gp + 4 * fs);
+                ny = __ldg(gp + 5 * fs);
+                nz = __ldg(gp + 6 * fs);
+                o = gauss_geo32(Rv, __ldg(gp), __ldg(gp + fs), __ldg(gp + 2 * fs), __ldg(gp + 7 * fs),
+                                __ldg(gp + 8 * fs), __ldg(gp + 9 * fs), Kh, Kl);
+                const float dx = o.sx + o.lx, dy = o.sy + o.ly, dz = o.sz + o.ez;
+                const float dia = __ldg(sa.pdiam + s);
+                okq = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= sa.near2 * dia * dia && o.hh >= sa.kr_min &&
+                      o.hh <= sa.kr_max && o.VV >= sa.kz_min;
+            }
+            // a pair is far when all its Gauss points are (lanes 4 p .. 4 p + 3 of one warp)
+            const unsigned bal = __ballot_sync(0xffffffffu, okq);
+            const bool far = valid && a.live && ((bal >> (lane & ~3)) & 0xFu) == 0xFu;
+            const bool judged =
+                far && sa.judge_mod != 0u && pair_hash((uint32_t)r, (uint32_t)s, sa.judge_seed) % sa.judge_mod == 0u;
+            const bool use_net = active && far && !judged;
+            float out[mlptc::NOUT];
+#pragma unroll
+            for (int j = 0; j < mlptc::NOUT; ++j) out[j] = 0.f;
+            if (wg_any(g, far)) {
+                const bool in = far && active;  // a triangle's fourth lane has no Gauss point
+                const float x0 = in ? (log10f(o.hh) - sa.in_shift[0]) / sa.in_scale[0] : 0.f;
+                const float x1 = in ? (o.VV - sa.in_shift[1]) / sa.in_scale[1] : 0.f;
+                mlptc::layer0(m, tile, t, x0, x1);
+                mlptc::layers(m, tile, acc, lane_base, g, t, phase, sa.gflags, out);
+            }
+            float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
+            if (active) {
+                float nGr = 0.f, nGi = 0.f, nGhr = 0.f, nGhi = 0.f, eg = 1.f, er = 1.f;
+                if (far) {
+                    const float d = sqrtf(fmaf(o.hh, o.hh, o.VV * o.VV));
+                    const float wv = twopi * expf(o.VV) * rsqrtf(1.0f + o.hh);
+                    eg = 2.0f / (d + 0.05f) + wv;
+                    er = 2.0f * o.hh / fmaf(d * d, 1.0f + d, 1e-12f) + wv;
+                    nGr = fmaf(out[0], sa.out_scale[0], sa.out_shift[0]) * eg;
+                    nGi = fmaf(out[1], sa.out_scale[1], sa.out_shift[1]) * wv;
+                    nGhr = fmaf(out[2], sa.out_scale[2], sa.out_shift[2]) * er;
+                    nGhi = fmaf(out[3], sa.out_scale[3], sa.out_shift[3]) * wv;
+                }
+                float Gr, Gi, Ghr, Ghi;
+                if (use_net) {
+                    Gr = nGr; Gi = nGi; Ghr = nGhr; Ghi = nGhi;
+                    ++n_mlp;
+                } else {
+                    gauss_G32(o, Gr, Gi, Ghr, Ghi);
+                    ++n_cf;
+                    if (judged) jerr = fmaxf(jerr, fmaxf(fabsf(nGr - Gr) / eg, fabsf(nGhr - Ghr) / er));
+                }
+                gauss_accum32(o, Gr, Gi, Ghr, Ghi, nx, ny, nz, w * c1, w * c2, wsr, wsi, wdr, wdi);
+            }
+            // sums over the pair's Gauss points (its four lanes)
+#pragma unroll
+            for (int off = 1; off <= 2; off <<= 1) {
+                wsr += __shfl_xor_sync(0xffffffffu, wsr, off);
+                wsi += __shfl_xor_sync(0xffffffffu, wsi, off);
+                wdr += __shfl_xor_sync(0xffffffffu, wdr, off);
+                wdi += __shfl_xor_sync(0xffffffffu, wdi, off);
+            }
+            if (q == 0 && valid) {
+                if (judged) ++n_judge;
+                if (a.mode == 1) {
+                    const size_t o2 = 2 * ((size_t)r * N + s);
+                    a.ws_out[o2] = (double)wsr; a.ws_out[o2 + 1] = (double)wsi;
+                    a.wd_out[o2] = (double)wdr; a.wd_out[o2 + 1] = (double)wdi;
+                } else {
+                    redf_store(a, row + s, __ldcs(a.RDhi + row + s), __ldcs(a.RDlo + row + s),
+                               __ldcs(a.RSRhi + row + s), __ldcs(a.RSRlo + row + s), wdr, wdi);
+                    sa.ws32[row + s] = wsr;
+                }
+            }
+        }
+    }
+    // counts and the largest judged error (non-negative floats order like their bits)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        n_mlp += __shfl_xor_sync(0xffffffffu, n_mlp, off);
+        n_cf += __shfl_xor_sync(0xffffffffu, n_cf, off);
+        n_judge += __shfl_xor_sync(0xffffffffu, n_judge, off);
+        jerr = fmaxf(jerr, __shfl_xor_sync(0xffffffffu, jerr, off));
+    }
+    if (lane == 0) {
+        atomicAdd(sa.stats, n_mlp);
+        atomicAdd(sa.stats + 1, n_cf);
+        atomicAdd(sa.stats + 2, n_judge);
+        atomicMax(sa.stats + 3, (unsigned long long)__float_as_uint(jerr));
+    }
+    mlptc::cta_teardown(tmem);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicSub(a.sm_ctr + smid, 1);
+}
+
+int launch_wave_surrogate(cudaStream_t st, const WaveArgs& a, const SurArgs& sa) {
+    WaveArgs b = a;
+    set_wave_f32_constants(b);
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_wave_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, mlptc::SMEM_BYTES) !=
+            cudaSuccess)
+            return 1;
+        attr = true;
+    }
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    b.per_sm = 1;  // one CTA fits per SM (shared memory)
+    cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (2 + WAVE_SM_SLOTS), st);
+    BEM_LAUNCH(k_wave_surrogate<<<nsm, mlptc::THREADS, mlptc::SMEM_BYTES, st>>>(b, sa));
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
+}
 
 // ---------------------------------------------------------------------------
 // Exact FP64 imaginary parts by plane waves.  With Bessel's integral

@@ -317,6 +317,24 @@ bem_status tc_flags_ok(bem_mlp* p) {
 
 }  // namespace
 
+int bem::mlp_tc_ref(bem_mlp* p, bem::MlpTcRef* out) {
+    if (!p || !out) return 1;
+    if (cudaSetDevice(p->device) != cudaSuccess) return 1;
+    if (ensure_tc(p, 1) != BEM_OK) return 1;
+    if (cudaStreamSynchronize(p->st) != cudaSuccess) {
+        p->err = "building the tensor-core operand image failed";
+        return 1;
+    }
+    out->img = p->tc_img;
+    out->fw = p->tc_f;
+    memcpy(out->in_shift, p->in_shift, sizeof(out->in_shift));
+    memcpy(out->in_scale, p->in_scale, sizeof(out->in_scale));
+    memcpy(out->out_shift, p->out_shift, sizeof(out->out_shift));
+    memcpy(out->out_scale, p->out_scale, sizeof(out->out_scale));
+    out->device = p->device;
+    return 0;
+}
+
 extern "C" {
 
 int bem_mlp_num_params(void) { return N_PARAMS; }

@@ -363,6 +363,33 @@ bem_status bem_mlp_eval(bem_mlp* m, int n, const double* x, double* y);
 bem_status bem_mlp_grad(bem_mlp* m, int n, const double* x, const double* y, double* grad, double* loss);
 bem_status bem_mlp_train(bem_mlp* m, int n, const double* x, const double* y, int epochs, int batch, double lr,
                          unsigned long long seed, double* loss_per_epoch);
+/* The surrogate form of the mixed assembly (no reference counterpart; the learned
+ * stand-in for HavelockGF, Kernels.cpp:342-412, in FreeSurface_Wave_Kernel,
+ * Panel.cpp:601-636).  With mode != 0 the mixed path's wave assembly takes G and
+ * dG/dh of far-field pairs inside the network's domain from network m (its
+ * tensor-core forward, fused into the assembly kernel), scaled back by the envelope
+ * the network is trained on (bemuse_gb300.HavelockSurrogate.envelope); near pairs
+ * (a mirrored Gauss point closer than domain[3] panel diameters), pairs outside
+ * KR in [domain[0], domain[1]] or KZ >= domain[2] and a seeded fraction
+ * judge_fraction of the far pairs (the judge) use the FP32 closed form.  The judged
+ * error is max |network - closed form| / envelope over the judged Gauss points.
+ *   mode 0  off (the closed form everywhere).
+ *   mode 1  strict: every frequency whose judged error exceeds judge_tol is solved
+ *           again with the closed form and its results replaced, so the results keep
+ *           the mixed path's accuracy whenever the network is not good enough.
+ *   mode 2  accept: the network's values are kept (the judged pairs use the closed form).
+ * The imaginary parts of the operator and of the right-hand sides keep their exact
+ * plane-wave form; the network's imaginary parts reach only the FP32 copy of D that
+ * is factorised.  domain may be NULL for {1e-3, 20, -40, 3}.  m must stay alive
+ * while the context uses it and be on the context's device.  BEM_MIXED only. */
+bem_status bem_set_surrogate(bem_ctx* ctx, bem_mlp* m, int mode, double judge_tol, double judge_fraction,
+                             const double* domain);
+/* Totals of the surrogate form since the last reset: [0] Gauss points evaluated by the
+ * network, [1] by the closed form, [2] judged pairs, [3] largest judged error,
+ * [4] frequencies solved again by the strict mode, [5] frequencies assembled with the
+ * surrogate, [6] reserved.  reset != 0 zeroes them after reading. */
+bem_status bem_surrogate_stats(bem_ctx* ctx, double* out7, int reset);
+
 /* Forward pass on the tensor cores (tcgen05 kind::f16: BF16 weights and activations,
  * FP32 accumulation in TMEM, SiLU as x/2 (1 + tanh(x/2)) with the hardware tanh):
  * the inference form the assembly uses.  It differs from bem_mlp_eval (FP32

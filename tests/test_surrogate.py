@@ -95,21 +95,25 @@ def test_tensor_core_forward_matches_oracle():
 
 @pytest.mark.gpu
 def test_training_and_gain_report():
-    """Trains on the plain integrator's samples and reports accuracy and throughput
-    against the FP32 closed form; the closed form is expected to win (a negative
-    result for the surrogate is the expected, reported outcome)."""
+    """Trains on samples of the plain FP64 integrator in the surrogate's domain (targets
+    divided by the per-sample envelope) and reports accuracy and throughput: the
+    tensor-core network against the FP32 closed form it would replace.  The closed form
+    is expected to be faster and the network's error far above the 1e-6 the solve
+    needs; a negative result, reported."""
     import bemuse_gb300 as bg
-    x, y = bg.HavelockSurrogate.training_set(1 << 16, seed=0)
-    xv, yv = bg.HavelockSurrogate.training_set(1 << 12, seed=1)
+    x, y, t = bg.HavelockSurrogate.domain_set(1 << 17, seed=0)
+    xv, yv, tv = bg.HavelockSurrogate.domain_set(1 << 13, seed=1)
     s = bg.HavelockSurrogate(seed=0)
-    s.set_normalization(x.mean(0), x.std(0), y.mean(0), y.std(0) + 1e-12)
-    losses = s.train(x, y, epochs=8, batch=2048, lr=2e-3)
-    print("losses", losses)
-    assert losses[-1] < 0.8 * losses[0]
-    pred = s.eval(xv)
-    rel = np.max(np.abs(pred - yv), axis=0) / np.max(np.abs(yv), axis=0)
-    print("max error / max |target| per output:", rel)
-    mlp = s.throughput(1 << 18)
+    s.set_domain_normalization(t)
+    losses = [s.train(x, t, epochs=1, batch=4096, lr=2e-3 * (0.93 ** e), seed=e)[0] for e in range(40)]
+    print("losses", losses[0], losses[-1])
+    assert losses[-1] < 0.2 * losses[0]
+    pred = s.predict(xv)
+    env = bg.HavelockSurrogate.envelope(10 ** xv[:, 0], xv[:, 1])
+    med = np.median(np.abs(pred - yv) / env, axis=0)
+    print("median error / envelope per output:", med)
+    assert np.all(med < 0.05)
+    mlp = s.throughput_tc(1 << 20)
     closed = bg.havelock_throughput(1 << 20, bg.MIXED)
-    print("evaluations/s: surrogate %.3e, FP32 closed form %.3e" % (mlp, closed))
+    print("evaluations/s: tensor-core network %.3e, FP32 closed form %.3e" % (mlp, closed))
     assert mlp > 0 and closed > 0
