@@ -8,12 +8,18 @@ right-hand sides).  Synthetic by construction (generated mesh, no dataset).
 
 One step = one frequency-solve in the mixed-precision mode: wave assembly
 (FP32 real parts, FP64-accurate imaginary parts), TF32 tensor-core LU, FP64
-iterative refinement to 1e-12 relative residual, hull integrals.  The plain
-FP64 GPU path is timed on `--plain-steps` of the same frequencies and the
-mixed results are compared with it (A, B normwise).
+iterative refinement to 1e-12 relative residual, hull integrals.
 
-  value  = freq-solves/s from device time (CUDA events on the library stream)
-  e2e    = freq-solves/s of wall time around bem_solve (host in, host out)
+  value         = freq-solves/s from device time (CUDA events on the library stream)
+  e2e           = freq-solves/s of wall time around bem_solve (host in, host out)
+  roofline      = the wave-assembly kernel on its FP32 bound (345 FP operations per
+                  Green-function evaluation against a measured FMA rate), with the HBM view
+  lu_roofline   = the tensor-core LU against a measured cuBLAS TF32 rate
+  cpu_baseline  = one unscaled frequency-solve of the same array by the oracle port on the
+                  host cores (setup excluded); the same solve pins accuracy_vs_oracle
+  plain_fp64    = the plain FP64 GPU path on --plain-steps of the timed frequencies, with
+                  cuSOLVER zgetrf at the same order beside its LU (plain_lu_vs_cusolver)
+  surrogate     = the learned form measured on the same frequencies (accept and strict)
 """
 import argparse
 import json
@@ -43,11 +49,13 @@ def parse():
     p.add_argument("--plain-steps", type=int, default=2)
     p.add_argument("--na", type=int, default=64, help="azimuthal panels per cylinder (64 -> 8192 panels)")
     p.add_argument("--batched", type=int, default=1, help="1: also run the 64-body batched form")
+    p.add_argument("--cpu-baseline", type=int, default=1,
+                   help="1: time one unscaled oracle frequency-solve on the host cores (also the accuracy pin)")
     p.add_argument("--autotune", type=int, default=1,
                    help="1: time a small grid of schedule settings on 8 sample frequencies before the "
                         "warm-up (outside the timed region) and keep the fastest")
-    p.add_argument("--surrogate-seconds", type=float, default=20.0,
-                   help="training budget of the Green-function surrogate report (0 skips it)")
+    p.add_argument("--surrogate-seconds", type=float, default=45.0,
+                   help="training budget of the Green-function surrogate legs (0 skips them)")
     return p.parse_args()
 
 
@@ -311,42 +319,75 @@ def batched_report(bg, n_workers=8):
             "note": "wall time of one bem_batch_solve call (setup of each body included)"}
 
 
-def surrogate_report(bg, budget_s, ms_per_solve, wave_kernel_ms, evals_per_solve):
-    """The MLP stand-in for HavelockGF (2 -> 128 x 4 -> 6, SiLU, BF16 weights / FP32
-    accumulation): trained on 2^22 samples of the plain FP64 integrator for a bounded
-    time, then measured against the FP32 closed form it would replace.  The
-    mixed+surrogate rate is composed from measured parts: the mixed frequency-solve
-    with its wave-kernel time replaced by the same number of surrogate evaluations."""
+def surrogate_report(bg, solver, timed, budget_s, results, oref, hi):
+    """The learned form of the metric, measured: the surrogate network (2 -> 128 x 4 -> 6,
+    SiLU, BF16 weights, FP32 accumulation) trained by the library's own kernels on 2^22
+    samples of the plain FP64 integrator in its domain for a bounded time, then fused into
+    the mixed assembly (tensor-core forward) and run on the same timed frequencies in the
+    two modes of bem_set_surrogate: "accept" keeps the network's far-field values, "strict"
+    solves a frequency again with the closed form when the judged error (1 % of the far
+    pairs, checked against the closed form) exceeds 1e-6.  Rates are device time of the
+    whole call, as for the headline."""
     t0 = time.perf_counter()
-    x, y = bg.HavelockSurrogate.training_set(1 << 22, seed=0)
-    xv, yv = bg.HavelockSurrogate.training_set(1 << 14, seed=1)
-    s = bg.HavelockSurrogate(seed=0)
-    s.set_normalization(x.mean(0), x.std(0), y.mean(0), y.std(0) + 1e-12)
-    lr, epochs, losses = 1e-3, 0, []
-    while time.perf_counter() - t0 < budget_s and epochs < 40:
-        losses += list(s.train(x, y, epochs=1, batch=8192, lr=lr, seed=epochs))
+    HS = bg.HavelockSurrogate
+    x, y, t = HS.domain_set(1 << 22, seed=0)
+    xv, yv, tv = HS.domain_set(1 << 16, seed=1)
+    sur = HS(seed=0)
+    sur.set_domain_normalization(t)
+    t1 = time.perf_counter()
+    epochs, losses = 0, []
+    while time.perf_counter() - t1 < budget_s and epochs < 200:
+        frac = (time.perf_counter() - t1) / budget_s
+        lr = 2e-3 * 0.5 * (1.0 + np.cos(np.pi * min(frac, 1.0))) + 1e-5
+        losses += list(sur.train(x, t, epochs=1, batch=4096, lr=lr, seed=epochs))
         epochs += 1
-        if epochs % 8 == 0:
-            lr *= 0.5
-    pred = s.eval(xv)
-    err = np.max(np.abs(pred - yv), axis=0) / np.max(np.abs(yv), axis=0)
-    far = xv[:, 0] > 0.0  # KR > 1
-    err_far = np.max(np.abs(pred[far] - yv[far]), axis=0) / np.max(np.abs(yv[far]), axis=0)
-    mlp_rate = s.throughput(1 << 20)
-    closed_rate = bg.havelock_throughput(1 << 22, bg.MIXED)
-    mlp_wave_ms = evals_per_solve / mlp_rate * 1000.0
-    ms_sur = ms_per_solve - wave_kernel_ms + mlp_wave_ms
-    return {"network": "2-128x4-6 SiLU, BF16 weights, FP32 accumulate", "train_samples": int(x.shape[0]),
-            "epochs": epochs, "train_s": time.perf_counter() - t0, "final_loss": float(losses[-1]) if losses else None,
-            "max_err_over_max_target": [float(v) for v in err],
-            "max_err_over_max_target_KR_gt_1": [float(v) for v in err_far],
-            "evals_per_s_surrogate": mlp_rate, "evals_per_s_fp32_closed_form": closed_rate,
-            "surrogate_slowdown": closed_rate / mlp_rate,
-            "mixed_plus_surrogate_freq_solves_per_s": 1000.0 / ms_sur,
-            "mixed_plus_surrogate_note": "composed: measured mixed frequency-solve minus its measured wave-kernel "
-                                         "time plus %.3g surrogate evaluations at the measured surrogate rate; the "
-                                         "headline value uses the closed form" % evals_per_solve,
-            "used_in_headline": False}
+    train_s = time.perf_counter() - t1
+    pred = sur.predict(xv)
+    env = HS.envelope(10.0 ** xv[:, 0], xv[:, 1])
+    rel_env = np.abs(pred - yv) / env
+    rep = {"network": "2-128x4-6 SiLU, BF16 weights and activations, FP32 accumulation (tcgen05 kind::f16, TMEM)",
+           "domain": {"KR": list(HS.KR_RANGE), "KZ": list(HS.KZ_RANGE), "near_field_panel_diameters": 3.0},
+           "train_samples": int(x.shape[0]), "epochs": epochs, "train_s": train_s,
+           "data_s": t1 - t0, "final_loss": float(losses[-1]) if losses else None,
+           "validation": {"median_err_over_envelope": [float(v) for v in np.median(rel_env, axis=0)],
+                          "max_err_over_envelope": [float(v) for v in rel_env.max(axis=0)],
+                          "max_err_over_max_target": [float(v) for v in
+                                                      np.max(np.abs(pred - yv), axis=0) / np.max(np.abs(yv), axis=0)]},
+           "evals_per_s_tensor_core_network": sur.throughput_tc(1 << 22),
+           "evals_per_s_fp32_closed_form": bg.havelock_throughput(1 << 22, bg.MIXED)}
+    rep["network_slowdown"] = rep["evals_per_s_fp32_closed_form"] / rep["evals_per_s_tensor_core_network"]
+    legs = {}
+    for mode in ("accept", "strict"):
+        solver.set_surrogate(sur, mode=mode, judge_tol=1e-6, judge_fraction=0.01)
+        solver.solve_omegas(timed[:2])  # warm-up
+        solver.surrogate_stats(reset=True)
+        solver.kernel_times(reset=True)
+        w0 = time.perf_counter()
+        r = solver.solve_omegas(timed)
+        wall = time.perf_counter() - w0
+        kt = solver.kernel_times(reset=True)
+        st = solver.surrogate_stats(reset=True)
+        n = len(timed)
+        keys = ("A", "B", "F")
+        legs[mode] = {"value": n / (kt[3] / 1000.0), "unit": "freq-solves/s", "ms_per_step": kt[3] / n,
+                      "e2e": n / wall,
+                      "accuracy_vs_oracle": {k: normwise(r[k][hi], oref[k][0]) for k in keys} if oref else None,
+                      "accuracy_vs_closed_form_mixed": {
+                          k: max(normwise(r[k][i], results[i][k][0]) for i in range(n)) for k in keys},
+                      "network_share_of_gauss_points": st["gauss_points_network"] / max(
+                          1, st["gauss_points_network"] + st["gauss_points_closed_form"]),
+                      "judged_pairs": st["judged_pairs"], "judged_error_max": st["judged_error_max"],
+                      "frequencies_resolved_with_closed_form": st["frequencies_resolved"],
+                      "refine_sweeps_max": int(np.max(r["iters"]))}
+    solver.set_surrogate(None, mode=None)
+    rep["mixed_plus_surrogate"] = legs
+    rep["omega_of_oracle_check"] = float(timed[hi])
+    rep["used_in_headline"] = False
+    rep["headline_note"] = ("measured, not composed; the headline is the closed-form mixed path, which meets "
+                            "the accuracy target and is faster: the network is slower than the closed form it "
+                            "replaces, and its BF16 error, once in the operator, moves A/B far beyond 1e-6 "
+                            "(accept), so strict mode falls back to the closed form")
+    return rep
 
 
 def normwise(a, b):
@@ -486,16 +527,18 @@ def main():
     # the measured CPU baseline: one unscaled frequency-solve by the oracle port at the highest
     # timed frequency, which also pins the GPU results at benchmark size
     hi = len(timed) - 1
-    oref, cpu = oracle_frequency_solve(args.na, timed[hi])
-    cpu.pop("seconds_per_solve", None)
-    acc = {"omega": float(timed[hi]), "metric": "max|x-ref|/max|ref| per 6x6 (or 6 x NB) block, FP64 oracle",
-           "mixed": {k: normwise(results[hi][k][0], oref[k][0]) for k in KEYS}}
-    if hi in plain_res:
-        acc["plain_fp64"] = {k: normwise(plain_res[hi][k][0], oref[k][0]) for k in KEYS}
+    oref, cpu, acc = None, None, None
+    if args.cpu_baseline:
+        oref, cpu = oracle_frequency_solve(args.na, timed[hi])
+        cpu.pop("seconds_per_solve", None)
+        acc = {"omega": float(timed[hi]), "metric": "max|x-ref|/max|ref| per 6x6 (or 6 x NB) block, FP64 oracle",
+               "mixed": {k: normwise(results[hi][k][0], oref[k][0]) for k in KEYS}}
+        if hi in plain_res:
+            acc["plain_fp64"] = {k: normwise(plain_res[hi][k][0], oref[k][0]) for k in KEYS}
     batched = batched_report(bg) if args.batched else None
     sur = None
     if args.surrogate_seconds > 0:
-        sur = surrogate_report(bg, args.surrogate_seconds, dev_ms_max / args.steps, wk_ms, evals)
+        sur = surrogate_report(bg, s, timed, args.surrogate_seconds, results, oref, hi)
     h2d = 8 + 6 * N * 8
     d2h = (36 + 12 * len(BETAS)) * 16 + int(np.mean(iters)) * (2 * 9 * 8) + 4
     line = {"metric": METRIC, "value": value, "unit": "freq-solves/s", "n_gpus": world, "steps": args.steps,
