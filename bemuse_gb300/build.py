@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(OUT_DIR, "libbemgpu.so")
 
-SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "host_batch.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "k_gmres.cu", "noalloc.cu", "k_mlp.cu", "k_mlp_tc.cu"]
+SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "host_batch.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "k_gmres.cu", "noalloc.cu", "k_mlp.cu", "k_mlp_tc.cu", "k_lu_piv.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -148,6 +148,11 @@ struct LUWork;  // opaque workspace (host_api.cpp)
 // diagonal-block inverses go to inv (re/im, [n/nb][2][nb][nb]: L^-1 then U^-1).
 int lu_factor_f64(cudaStream_t st, int n, CMat<double> A, double* invr, double* invi, double* wl, double* wu,
                   int* flags);
+// LU with partial pivoting (k_lu_piv.cu; Eigen's rule: the first row of largest |a_ij|), in
+// place, pivots in piv (n ints), FLAG_ZERO_PIVOT on a zero pivot; the solve exchanges X's rows
+// (n x R complex interleaved) and substitutes in place.  Nonzero if a launch failed.
+int lu_piv_factor_f64(cudaStream_t st, int n, CMat<double> A, int* piv, int* flags);
+int lu_piv_solve_f64(cudaStream_t st, int n, CMat<double> A, const int* piv, int R, double* X);
 // Lookahead schedule for the tensor-core LU: the panel of step k+1 (diagonal-block
 // inverse, W21, U12^T) runs on `panel` (a higher-priority stream) while the main
 // stream applies the rest of step k's trailing update on all but `reserve_sms` SMs.

@@ -1744,6 +1744,52 @@ bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, doubl
     }
     double t0 = 0, t1 = 0;
     s = factor_and_solve(ctx, ctx->fs[0], n, Np, nrhs, mixed, tol, ctx->refine_max, iters, resid, &t0, &t1);
+    if (s == BEM_ERR_NUMERIC) {
+        // The no-exchange LU met a multiplier |l_ik| > 1 or a zero pivot (or, mixed, its
+        // refinement did not converge): the matrix needs row exchanges.  Factor it again
+        // with partial pivoting in FP64, as Eigen::PartialPivLU does, and solve directly.
+        int* piv = nullptr;
+        DA(piv, Np);
+        CMat<double> M{ctx->d_D64r, ctx->d_D64i, Np};
+        double* X = ctx->fs[0].Y;
+        CK(cudaMemcpyAsync(ctx->d_D64r, re.data(), re.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->d_D64i, im.data(), im.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(X, 0, sizeof(double) * 2 * (size_t)Np * nrhs, st));
+        CK(cudaMemcpyAsync(X, B, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), st));
+        if (bem::lu_piv_factor_f64(st, Np, M, piv, ctx->d_flags) || bem::lu_piv_solve_f64(st, Np, M, piv, nrhs, X)) {
+            free_all(ctx);
+            return fail(ctx, BEM_ERR_CUDA, "bem_dense_solve: pivoted LU launch failed");
+        }
+        int hf = 0;
+        std::vector<double> X_h((size_t)2 * n * nrhs);
+        cudaError_t e = cudaMemcpyAsync(&hf, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(X_h.data(), X, X_h.size() * 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        free_all(ctx);
+        if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_dense_solve: ") + cudaGetErrorString(e));
+        if (hf & bem::FLAG_ZERO_PIVOT) return fail(ctx, BEM_ERR_NUMERIC, "bem_dense_solve: the matrix is singular");
+        if (resid) {
+            // max over right-hand sides of |b - A x|_inf / |b|_inf, as the refinement reports it
+            double worst = 0.0;
+            for (int r = 0; r < nrhs; ++r) {
+                double rn = 0.0, bn = 0.0;
+                for (int i = 0; i < n; ++i) {
+                    cplx acc(B[2 * ((size_t)i * nrhs + r)], B[2 * ((size_t)i * nrhs + r) + 1]);
+                    bn = std::max(bn, std::abs(acc));
+                    for (int j = 0; j < n; ++j)
+                        acc -= cplx(A[2 * ((size_t)i * n + j)], A[2 * ((size_t)i * n + j) + 1]) *
+                               cplx(X_h[2 * ((size_t)j * nrhs + r)], X_h[2 * ((size_t)j * nrhs + r) + 1]);
+                    rn = std::max(rn, std::abs(acc));
+                }
+                worst = std::max(worst, bn > 0 ? rn / bn : rn);
+            }
+            *resid = worst;
+        }
+        if (iters) *iters = 0;
+        std::copy(X_h.begin(), X_h.end(), B);
+        return BEM_OK;
+    }
     if (s != BEM_OK) { free_all(ctx); return s; }
     cudaError_t e = cudaMemcpyAsync(B, ctx->d_X, sizeof(double) * 2 * (size_t)n * nrhs, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -239,7 +239,12 @@ bem_status bem_havelock(int device, int n, const double* x, const double* y, con
 /* Solves A X = B for complex A (n x n) and B (n x nrhs), both row-major
  * interleaved, with the GPU LU of `precision` (refined to refine_tol in
  * BEM_MIXED).  X overwrites B.  Replaces Eigen::PartialPivLU<CMatrix>
- * compute/solve (Hydrodynamic_Solver.cpp:430, 438, 446).  The call uses the
+ * compute/solve (Hydrodynamic_Solver.cpp:430, 438, 446).  The fast path is the
+ * blocked LU without row exchanges; when it meets a multiplier |l_ik| > 1 or a zero
+ * pivot (or, in BEM_MIXED, its refinement does not converge), the matrix is factored
+ * again in FP64 with partial pivoting (Eigen's rule: the first row of largest
+ * |a_ij|) and solved directly; refine_iters is then 0 and residual is computed on
+ * the host.  BEM_ERR_NUMERIC only for a singular matrix.  The call uses the
  * context's solver buffers and discards any previous bem_setup. */
 bem_status bem_dense_solve(bem_ctx* ctx, int n, const double* A, int nrhs, double* B, int precision,
                            double refine_tol, int* refine_iters, double* residual);
