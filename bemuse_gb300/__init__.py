@@ -16,7 +16,7 @@ from . import build as _build
 
 __all__ = [
     "BEMError", "lib", "Parameter", "Mesh", "Half_Cylinder", "Barge", "unify",
-    "Hydrodynamic_Radiation_Solver", "Aerodynamic_Solver", "NACA_Wing", "havelock_gf", "dense_solve",
+    "Hydrodynamic_Radiation_Solver", "Aerodynamic_Solver", "NACA_Wing", "NACA_Wing_Wake", "havelock_gf", "dense_solve",
     "PLAIN_FP64", "MIXED", "read_mesh", "GDF_Geometry", "MAR_Geometry", "STL_Geometry", "PNL_Geometry",
     "write_wamit",
 ]
@@ -132,6 +132,9 @@ def lib():
         "bem_mesh_wing": ([c_double, c_double, c_double, c_int, c_int, c_int, _dp, _ip], c_int),
         "bem_aero_setup": ([vp, ctypes.POINTER(_Mesh)], c_int),
         "bem_aero_solve": ([vp, c_int, _dp, c_int, c_double, _dp, _dp], c_int),
+        "bem_aero_set_wake": ([vp, c_int, _dp, _ip, _ip], c_int),
+        "bem_aero_surface": ([vp, _dp, _dp, c_double, _dp, _dp], c_int),
+        "bem_mesh_wing_wake": ([c_double, c_double, c_int, c_int, c_double, _dp, _ip, _ip], c_int),
         "bem_fp32_peak": ([c_int, _dp], c_int),
         "bem_set_surrogate": ([vp, vp, c_int, c_double, c_double, _dp], c_int),
         "bem_surrogate_stats": ([vp, _dp, c_int], c_int),
@@ -233,6 +236,18 @@ def NACA_Wing(chord=1.0, span=8.0, thickness=0.12, n_chord=120, n_span=60, cosin
     elems = np.zeros((ne.value, 4), np.int32)
     _check(L.bem_mesh_wing(chord, span, thickness, n_chord, n_span, int(cosine), _p(nodes), _p(elems, _ip)))
     return Mesh(nodes, elems)
+
+
+def NACA_Wing_Wake(chord=1.0, span=8.0, n_chord=120, n_span=60, length=20.0):
+    """Flat trailing wake of NACA_Wing's wing: one strip per panel column from the
+    trailing edge (x = chord, z = 0) to length chords downstream (normal -z).
+    Returns (quads n_span x 4 x 3, te_upper, te_lower): the Kutta pair of strip j is
+    the upper trailing-edge panel j n_chord + n_chord - 1 and the lower one j n_chord."""
+    quads = np.zeros((n_span, 4, 3))
+    up = np.zeros(n_span, np.int32)
+    lo = np.zeros(n_span, np.int32)
+    _check(lib().bem_mesh_wing_wake(chord, span, n_chord, n_span, length, _p(quads), _p(up, _ip), _p(lo, _ip)))
+    return quads, up, lo
 
 
 def unify(meshes, origins):
@@ -651,8 +666,30 @@ class Aerodynamic_Solver:
         _check(lib().bem_aero_setup(self._h, ctypes.byref(ms)), self._h)
         self.N = mesh.n
 
+    def Set_Wake(self, quads, te_upper, te_lower):
+        """Flat constant-doublet wake strips carrying the Kutta jumps
+        X[te_upper] - X[te_lower] (no reference counterpart: the reference's steady
+        solve has no wake); takes effect at the next Setup."""
+        q = np.ascontiguousarray(quads, dtype=np.float64).reshape(-1, 4, 3)
+        up = np.ascontiguousarray(te_upper, dtype=np.int32).ravel()
+        lo = np.ascontiguousarray(te_lower, dtype=np.int32).ravel()
+        if not (q.shape[0] == up.size == lo.size):
+            raise BEMError(1, "wake: one Kutta pair per strip")
+        _check(lib().bem_aero_set_wake(self._h, q.shape[0], _p(q), _p(up, _ip), _p(lo, _ip)), self._h)
+
     def Set_External_BC(self, vels):
         self.vels = np.ascontiguousarray(vels, dtype=np.float64).reshape(-1, 3)
+
+    def Surface(self, U, s_ref, X=None):
+        """Surface pressure of the solution for the uniform onset flow U: cp per panel
+        (1 - |U_t + grad X|^2 / |U|^2, least-squares surface gradient) and the force
+        coefficients {CF (3), CL, CD} with CF = sum cp n A / s_ref."""
+        X = np.ascontiguousarray(self.X if X is None else X, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.float64).ravel()
+        cp = np.zeros(self.N)
+        co = np.zeros(5)
+        _check(lib().bem_aero_surface(self._h, _p(X), _p(U), float(s_ref), _p(cp), _p(co)), self._h)
+        return cp, {"CF": co[:3].copy(), "CL": float(co[3]), "CD": float(co[4])}
 
     def Solve_Steady(self):
         X = np.zeros(self.N)

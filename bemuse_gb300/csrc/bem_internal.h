@@ -106,6 +106,10 @@ cudaError_t upload_poly_constants(int device);
 void launch_rankine(cudaStream_t st, int N, int ld, const double* rec, const double* xr, const double* rn, int mode,
                     double* o0, double* o1, double* o2, double* o3);
 void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32);
+// Folds the dipole influence of W trailing-wake strips into H (N x N, leading dimension ld):
+// H[r][te_up[w]] += D_w(x_r), H[r][te_lo[w]] -= D_w(x_r) (Kutta condition).
+void launch_wake_fold(cudaStream_t st, int N, int ld, int W, const double* rec_w, const double* xr, const int* te_up,
+                      const int* te_lo, double* H);
 // Exterior outputs after a solve (X = [Phi_J | Phi_S], N x (6 + NB) complex):
 // free-surface elevation at NW points wp ([3][NW]) and Kochin functions at NK angles;
 // out: [NW or NK][6 + NB] complex interleaved.

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/bemgpu.h"
@@ -116,6 +117,17 @@ struct bem_ctx {
     double sur_dom[4] = {1.0e-3, 20.0, -40.0, 3.0};
     double sur_totals[7] = {0, 0, 0, 0, 0, 0, 0};
     float* d_pdiam = nullptr;     // panel diameters (largest vertex distance), for the near-field test
+    // steady solve: trailing wake (bem_aero_set_wake, applied by the next bem_aero_setup) and
+    // the panel data of bem_aero_surface (centroid, ex, ey, n, area per panel; edge
+    // neighbours facing the same side)
+    std::vector<double> wake_quads;
+    std::vector<int> wake_up, wake_lo;
+    std::vector<double> aero_geo;
+    std::vector<std::vector<int>> aero_nbr;
+    double* d_recw = nullptr;
+    int* d_aero_piv = nullptr;
+    bool aero_pivoted = false;    // the last bem_aero_solve fell back to the pivoted FP64 LU
+    int* d_wake_te = nullptr;
     // failure-detection tests only: the triangular-solve chain waits for a flag value that
     // nothing publishes (test_wait_skew > 0) and gives up after test_wait_ns
     int test_wait_skew = 0;
@@ -250,6 +262,9 @@ void free_all(bem_ctx* ctx) {
     }
     ctx->d_wctr = nullptr;
     ctx->d_pdiam = nullptr;
+    ctx->d_recw = nullptr;
+    ctx->d_wake_te = nullptr;
+    ctx->d_aero_piv = nullptr;
     ctx->wpts_dirty = true;
     ctx->ready = false;
 }
@@ -1845,6 +1860,56 @@ bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh) {
     CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
     bem::launch_rankine(st, N, Np, ctx->d_rec, ctx->d_xr, nullptr, 2, ctx->d_RS, ctx->d_RD, nullptr, nullptr);
     CK(cudaGetLastError());
+    const int W = (int)ctx->wake_up.size();
+    if (W > 0) {
+        // the trailing wake: strip w's dipole influence joins the columns of its Kutta pair
+        for (int w = 0; w < W; ++w)
+            if (ctx->wake_up[w] < 0 || ctx->wake_up[w] >= N || ctx->wake_lo[w] < 0 || ctx->wake_lo[w] >= N)
+                return fail(ctx, BEM_ERR_ARG, "wake: a Kutta panel index is outside the mesh");
+        std::vector<int> welems(4 * (size_t)W);
+        for (int i = 0; i < 4 * W; ++i) welems[i] = i;
+        bem::MeshView wv{4 * W, ctx->wake_quads.data(), W, welems.data(), 0, nullptr, nullptr};
+        std::vector<bem::PanelGeom> wb, wmir;
+        if (!bem::build_geometry(wv, wb, wmir, gerr)) return fail(ctx, BEM_ERR_ARG, "wake: " + gerr);
+        std::vector<double> recw((size_t)W * bem::RK_STRIDE, 0.0);
+        for (int w = 0; w < W; ++w) bem::rankine_record(wb[w], &recw[(size_t)w * bem::RK_STRIDE]);
+        std::vector<int> te(2 * (size_t)W);
+        std::copy(ctx->wake_up.begin(), ctx->wake_up.end(), te.begin());
+        std::copy(ctx->wake_lo.begin(), ctx->wake_lo.end(), te.begin() + W);
+        DA(ctx->d_recw, recw.size());
+        DA(ctx->d_wake_te, te.size());
+        CK(cudaMemcpyAsync(ctx->d_recw, recw.data(), recw.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->d_wake_te, te.data(), te.size() * 4, cudaMemcpyHostToDevice, st));
+        bem::launch_wake_fold(st, N, Np, W, ctx->d_recw, ctx->d_xr, ctx->d_wake_te, ctx->d_wake_te + W, ctx->d_RD);
+        CK(cudaGetLastError());
+    }
+    // panel data and edge neighbours for bem_aero_surface
+    ctx->aero_geo.assign(13 * (size_t)N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        double* g = &ctx->aero_geo[13 * (size_t)i];
+        for (int d = 0; d < 3; ++d) { g[d] = body[i].c[d]; g[3 + d] = body[i].e[d]; g[6 + d] = body[i].e[3 + d]; g[9 + d] = body[i].e[6 + d]; }
+        g[12] = body[i].area;
+    }
+    {
+        std::map<std::pair<int, int>, std::vector<int>> edges;
+        for (int e = 0; e < N; ++e) {
+            const int* el = mesh->elems + 4 * (size_t)e;
+            const int nv = el[3] < 0 ? 3 : 4;
+            for (int k = 0; k < nv; ++k) {
+                const int a = el[k], b = el[(k + 1) % nv];
+                edges[{std::min(a, b), std::max(a, b)}].push_back(e);
+            }
+        }
+        ctx->aero_nbr.assign(N, {});
+        for (auto& kv : edges)
+            for (int a : kv.second)
+                for (int b : kv.second) {
+                    if (a == b) continue;
+                    const double* na = &ctx->aero_geo[13 * (size_t)a + 9];
+                    const double* nb = &ctx->aero_geo[13 * (size_t)b + 9];
+                    if (na[0] * nb[0] + na[1] * nb[1] + na[2] * nb[2] > 0.0) ctx->aero_nbr[a].push_back(b);
+                }
+    }
     CK(cudaStreamSynchronize(st));
     ctx->aero = true;
     ctx->ready = true;
@@ -1887,11 +1952,110 @@ bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precis
     ctx->resid_mode = mixed ? 1 : 0;
     s = factor_and_solve(ctx, ctx->fs[0], N, Np, 1, mixed, tol, ctx->refine_max, &iters, &resid, &t0, &t1);
     ctx->resid_mode = 0;
-    if (s != BEM_OK) return s;
+    if (s == BEM_ERR_NUMERIC) {
+        // The no-exchange LU met a multiplier |l_ik| > 1 (the wake's Kutta columns can make
+        // H lose diagonal dominance) or the mixed refinement did not converge: factor H
+        // again with partial pivoting in FP64 (Eigen::PartialPivLU's rule, as the
+        // reference's solver does) and solve directly.
+        if (!ctx->d_aero_piv) DA(ctx->d_aero_piv, Np);
+        int* piv = ctx->d_aero_piv;
+        CK(cudaMemcpyAsync(ctx->d_D64r, ctx->d_RD, sizeof(double) * (size_t)N * Np, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemsetAsync(ctx->d_D64r + (size_t)N * Np, 0, sizeof(double) * (size_t)(Np - N) * Np, st));
+        CK(cudaMemsetAsync(ctx->d_D64i, 0, sizeof(double) * (size_t)Np * Np, st));
+        bem::launch_pad_identity(st, N, Np, ctx->d_D64r, ctx->d_D64i, nullptr, nullptr);
+        bem::launch_matx(st, N, Np, ctx->d_RS, nullptr, 1, 0, ctx->fs[0].Bm, 1, ctx->fs[0].mx, 1.0, 0.0, nullptr,
+                         ctx->fs[0].Y, 1);
+        CK(cudaMemsetAsync(ctx->d_X, 0, sizeof(double) * 2 * (size_t)Np, st));
+        CK(cudaMemcpyAsync(ctx->d_X, ctx->fs[0].Y, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), st));
+        CMat<double> M{ctx->d_D64r, ctx->d_D64i, Np};
+        const int bad = bem::lu_piv_factor_f64(st, Np, M, piv, ctx->d_flags) ||
+                        bem::lu_piv_solve_f64(st, Np, M, piv, 1, ctx->d_X);
+        int hf = 0;
+        cudaError_t e = bad ? cudaErrorLaunchFailure : cudaMemcpyAsync(&hf, ctx->d_flags, sizeof(int),
+                                                                       cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return fail(ctx, BEM_ERR_CUDA, std::string("bem_aero_solve: ") + cudaGetErrorString(e));
+        if (hf & bem::FLAG_ZERO_PIVOT) return fail(ctx, BEM_ERR_NUMERIC, "bem_aero_solve: H is singular");
+        ctx->aero_pivoted = true;
+    } else if (s != BEM_OK) {
+        return s;
+    } else {
+        ctx->aero_pivoted = false;
+    }
     std::vector<double> x(2 * (size_t)N);
     CK(cudaMemcpy(x.data(), ctx->d_X, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost));
     if (X) for (int i = 0; i < N; ++i) X[i] = x[2 * (size_t)i];
     if (BC) memcpy(BC, bc.data(), sizeof(double) * N);
+    return BEM_OK;
+}
+
+bem_status bem_aero_set_wake(bem_ctx* ctx, int n_wake, const double* quads, const int* te_upper,
+                             const int* te_lower) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (n_wake < 0 || (n_wake > 0 && (!quads || !te_upper || !te_lower)))
+        return fail(ctx, BEM_ERR_ARG, "bem_aero_set_wake: bad arguments");
+    ctx->wake_quads.assign(quads, quads + 12 * (size_t)n_wake);
+    ctx->wake_up.assign(te_upper, te_upper + n_wake);
+    ctx->wake_lo.assign(te_lower, te_lower + n_wake);
+    return BEM_OK;
+}
+
+bem_status bem_aero_surface(bem_ctx* ctx, const double* X, const double* vel, double s_ref, double* cp,
+                            double* coeffs) {
+    if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
+    if (!ctx->ready || !ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_aero_surface before bem_aero_setup");
+    if (!X || !vel || !(s_ref > 0)) return fail(ctx, BEM_ERR_ARG, "bem_aero_surface: bad arguments");
+    const int N = ctx->N;
+    const double U[3] = {vel[0], vel[1], vel[2]};
+    const double U2 = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
+    if (!(U2 > 0)) return fail(ctx, BEM_ERR_ARG, "bem_aero_surface: zero onset velocity");
+    double CF[3] = {0, 0, 0};
+    for (int i = 0; i < N; ++i) {
+        const double* g = &ctx->aero_geo[13 * (size_t)i];
+        const double *c = g, *ex = g + 3, *ey = g + 6, *n = g + 9;
+        // least-squares gradient of X in the tangent plane over the edge neighbours
+        double a11 = 0, a12 = 0, a22 = 0, b1 = 0, b2 = 0;
+        for (int j : ctx->aero_nbr[i]) {
+            const double* cj = &ctx->aero_geo[13 * (size_t)j];
+            const double d[3] = {cj[0] - c[0], cj[1] - c[1], cj[2] - c[2]};
+            const double t1 = d[0] * ex[0] + d[1] * ex[1] + d[2] * ex[2];
+            const double t2 = d[0] * ey[0] + d[1] * ey[1] + d[2] * ey[2];
+            const double dx = X[j] - X[i];
+            a11 += t1 * t1; a12 += t1 * t2; a22 += t2 * t2;
+            b1 += dx * t1; b2 += dx * t2;
+        }
+        const double det = a11 * a22 - a12 * a12;
+        double g1 = 0, g2 = 0;
+        if (std::fabs(det) > 1e-300) {
+            g1 = (a22 * b1 - a12 * b2) / det;
+            g2 = (a11 * b2 - a12 * b1) / det;
+        }
+        const double un = U[0] * n[0] + U[1] * n[1] + U[2] * n[2];
+        double V[3], v2 = 0;
+        for (int d = 0; d < 3; ++d) {
+            V[d] = U[d] - un * n[d] + g1 * ex[d] + g2 * ey[d];
+            v2 += V[d] * V[d];
+        }
+        const double cpi = 1.0 - v2 / U2;
+        if (cp) cp[i] = cpi;
+        for (int d = 0; d < 3; ++d) CF[d] += cpi * n[d] * g[12] / s_ref;
+    }
+    if (coeffs) {
+        const double hz = std::hypot(U[0], U[2]);
+        coeffs[0] = CF[0]; coeffs[1] = CF[1]; coeffs[2] = CF[2];
+        coeffs[3] = hz > 0 ? (-U[2] * CF[0] + U[0] * CF[2]) / hz : 0.0;                 // CL
+        coeffs[4] = (U[0] * CF[0] + U[1] * CF[1] + U[2] * CF[2]) / std::sqrt(U2);      // CD
+    }
+    return BEM_OK;
+}
+
+int bem_mesh_wing_wake(double chord, double span, int nc, int ns, double length, double* quads, int* te_upper,
+                       int* te_lower) {
+    if (nc < 4 || nc % 2 || ns < 1 || !(chord > 0) || !(span > 0) || !(length > 0) || !quads || !te_upper ||
+        !te_lower)
+        return BEM_ERR_ARG;
+    bem::wing_wake(chord, span, nc, ns, length, quads, te_upper, te_lower);
     return BEM_OK;
 }
 

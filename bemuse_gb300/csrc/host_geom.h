@@ -42,6 +42,7 @@ void barge_mesh(double L, double W, double D, int NX, int NY, int NZ, bool cosin
                 double* aux_nodes, int* aux_elems);
 void wing_sizes(int nc, int ns, int* nn, int* ne);
 void wing_mesh(double chord, double span, double t, int nc, int ns, bool cosine, double* nodes, int* elems);
+void wing_wake(double chord, double span, int nc, int ns, double length, double* quads, int* te_up, int* te_lo);
 void mass_and_stiffness(const std::vector<PanelGeom>& body, const std::vector<PanelGeom>* aux, double rho, double g,
                         double mass, const double* cog, const double* gyr, double* M, double* C, double* vc);
 

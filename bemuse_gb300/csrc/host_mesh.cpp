@@ -381,6 +381,22 @@ void wing_mesh(double chord, double span, double t, int nc, int ns, bool cosine,
         }
 }
 
+// Flat trailing wake of the rectangular wing of wing_mesh: one constant-doublet strip per
+// spanwise panel column, from the trailing edge (x = chord, z = 0) to length chords
+// downstream, vertices ordered so the strip's normal points down (-z).  The Kutta
+// pairing of strip j: upper trailing-edge panel j nc + nc - 1, lower j nc.
+void wing_wake(double chord, double span, int nc, int ns, double length, double* quads, int* te_up, int* te_lo) {
+    for (int j = 0; j < ns; ++j) {
+        const double y0 = -0.5 * span + span * j / ns, y1 = -0.5 * span + span * (j + 1) / ns;
+        const double x0 = chord, x1 = chord * (1.0 + length);
+        const double v[4][3] = {{x0, y0, 0.0}, {x1, y0, 0.0}, {x1, y1, 0.0}, {x0, y1, 0.0}};
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) quads[12 * (size_t)j + 3 * k + d] = v[k][d];
+        te_up[j] = j * nc + nc - 1;
+        te_lo[j] = j * nc;
+    }
+}
+
 // Calculate_Volume / Calculate_COB (Boundary_Base.cpp:177-224, with
 // Calculate_GridParams :125-150 for the zero clean-up), Calculate_Mass_Matrix
 // and Calculate_Hydrostatic_Stiffness_Matrix (Hydrodynamic_Solver.cpp:300-397).

@@ -98,6 +98,26 @@ __global__ void __launch_bounds__(256) k_rankine(int N, int ld, const double* __
     }
 }
 
+// Trailing wake of the steady solve: wake strip w (Rankine record rec_w + w RK_STRIDE) is a
+// constant-doublet panel of strength X[te_up[w]] - X[te_lo[w]] (the Kutta condition), so its
+// dipole influence at collocation point r joins H[r][te_up[w]] with + and H[r][te_lo[w]] with -.
+__global__ void k_wake_fold(int N, int ld, int W, const double* __restrict__ rec_w, const double* __restrict__ xr,
+                            const int* __restrict__ te_up, const int* __restrict__ te_lo, double* __restrict__ H) {
+    const int w = blockIdx.y;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N || w >= W) return;
+    double sw, dw;
+    source_kernel(rec_w + (size_t)w * RK_STRIDE, xr[r], xr[N + r], xr[2 * N + r], sw, dw);
+    atomicAdd(H + (size_t)r * ld + te_up[w], dw);
+    atomicAdd(H + (size_t)r * ld + te_lo[w], -dw);
+}
+
+void launch_wake_fold(cudaStream_t st, int N, int ld, int W, const double* rec_w, const double* xr, const int* te_up,
+                      const int* te_lo, double* H) {
+    if (W <= 0) return;
+    BEM_LAUNCH(k_wake_fold<<<dim3((N + 127) / 128, W), 128, 0, st>>>(N, ld, W, rec_w, xr, te_up, te_lo, H));
+}
+
 // ---------------------------------------------------------------------------
 // K2: wave term.  One warp per receiver row, lanes over source panels; the
 // eight warps of a CTA sweep the same source tiles so those come from L1.

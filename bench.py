@@ -20,6 +20,10 @@ iterative refinement to 1e-12 relative residual, hull integrals.
   plain_fp64    = the plain FP64 GPU path on --plain-steps of the timed frequencies, with
                   cuSOLVER zgetrf at the same order beside its LU (plain_lu_vs_cusolver)
   surrogate     = the learned form measured on the same frequencies (accept and strict)
+  steady        = the steady lifting-wing workload: NACA 0012 wing of 7,200 panels at 5 deg
+                  with a 60-strip trailing wake (Kutta condition), surface pressure and CL;
+                  GPU wall time of setup (Rankine matrices + wake fold) and solve, and the
+                  oracle's solve of the same case on the host cores beside it
 """
 import argparse
 import json
@@ -56,6 +60,7 @@ def parse():
                         "warm-up (outside the timed region) and keep the fastest")
     p.add_argument("--surrogate-seconds", type=float, default=45.0,
                    help="training budget of the Green-function surrogate legs (0 skips them)")
+    p.add_argument("--steady", type=int, default=1, help="1: also run the steady lifting-wing leg")
     return p.parse_args()
 
 
@@ -319,6 +324,55 @@ def batched_report(bg, n_workers=8):
             "note": "wall time of one bem_batch_solve call (setup of each body included)"}
 
 
+def steady_report(bg, with_oracle, reps=3):
+    """Steady lifting flow: NACA 0012 wing (chord 1, span 8, 120 x 60 = 7,200 panels) at
+    alpha = 5 deg, flat wake of 60 strips 20 chords long carrying the Kutta jumps; setup
+    (Rankine G and H on the GPU, wake dipoles folded into H), solve in both precisions,
+    surface pressure and CL on the host.  Wall times (the calls are synchronous), median of
+    reps after one warm-up."""
+    c, span, nc, ns = 1.0, 8.0, 120, 60
+    w = bg.NACA_Wing(c, span, 0.12, nc, ns)
+    wake = bg.NACA_Wing_Wake(c, span, nc, ns, 20.0)
+    a = np.radians(5.0)
+    U = np.array([np.cos(a), 0.0, np.sin(a)])
+    out = {"workload": "NACA 0012 wing 7200 panels, 60 wake strips x 20 chords, alpha 5 deg", "panels": w.n}
+    sol = {}
+    for name, prec in (("mixed", bg.MIXED), ("plain_fp64", bg.PLAIN_FP64)):
+        sv = bg.Aerodynamic_Solver(precision=prec)
+        sv.Set_Wake(*wake)
+        ts, tv, tp = [], [], []
+        for r in range(reps + 1):
+            t0 = time.perf_counter()
+            sv.Setup(w)
+            t1 = time.perf_counter()
+            sv.Set_External_BC([U])
+            X = sv.Solve_Steady()
+            t2 = time.perf_counter()
+            cp, co = sv.Surface(U, c * span)
+            t3 = time.perf_counter()
+            if r:
+                ts.append(t1 - t0); tv.append(t2 - t1); tp.append(t3 - t2)
+        sol[name] = X
+        out[name] = {"setup_ms": 1e3 * float(np.median(ts)), "solve_ms": 1e3 * float(np.median(tv)),
+                     "surface_ms": 1e3 * float(np.median(tp)), "CL": co["CL"], "CD": co["CD"],
+                     "cp_min": float(cp.min())}
+    out["lifting_line_CL"] = 2 * np.pi * a / (1 + 2 / (span / c))
+    if with_oracle:
+        from oracle.oracle import Oracle, Mesh as OMesh
+        from oracle import aero_post
+        orc = Oracle()
+        om = OMesh(w.nodes, w.elems)
+        t0 = time.perf_counter()
+        Xo, _ = orc.aero_wake(om, *wake, U)
+        t1 = time.perf_counter()
+        cpo, CF, CL, CD = aero_post.surface(orc.panels(om), w.elems, Xo, U, c * span)
+        out["oracle"] = {"solve_s": t1 - t0, "threads": orc.num_threads(), "CL": CL, "CD": CD,
+                         "note": "setup and solve of the oracle port (FP64, OpenMP) on the host cores"}
+        out["accuracy_vs_oracle"] = {k: normwise(sol[k], Xo) for k in sol}
+        out["accuracy_vs_oracle"]["CL_abs_err_mixed"] = abs(out["mixed"]["CL"] - CL)
+    return out
+
+
 def surrogate_report(bg, solver, timed, budget_s, results, oref, hi):
     """The learned form of the metric, measured: the surrogate network (2 -> 128 x 4 -> 6,
     SiLU, BF16 weights, FP32 accumulation) trained by the library's own kernels on 2^22
@@ -540,6 +594,7 @@ def main():
     sur = None
     if args.surrogate_seconds > 0:
         sur = surrogate_report(bg, s, timed, args.surrogate_seconds, results, oref, hi)
+    steady = steady_report(bg, args.cpu_baseline) if args.steady else None
     h2d = 8 + 6 * N * 8
     d2h = (36 + 12 * len(BETAS)) * 16 + int(np.mean(iters)) * (2 * 9 * 8) + 4
     line = {"metric": METRIC, "value": value, "unit": "freq-solves/s", "n_gpus": world, "steps": args.steps,
@@ -565,6 +620,7 @@ def main():
             "refine_sweeps": iters,
             "surrogate": sur,
             "batched": batched,
+            "steady": steady,
             "stage_ms": dict(zip(names, [float(x) for x in per])),
             "stage_ms_note": "per frequency; assembly of f+1 overlaps factor+solve of f, so stages sum to more than ms_per_step",
             "setup_s": setup_s,

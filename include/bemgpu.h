@@ -213,6 +213,29 @@ bem_status bem_aero_setup(bem_ctx* ctx, const bem_mesh* mesh);
 bem_status bem_aero_solve(bem_ctx* ctx, int n_vel, const double* vel, int precision, double refine_tol, double* X,
                           double* BC);
 
+/* ---- steady flow with a trailing wake (no reference counterpart) ------------
+ * The reference's constant-panel steady solve has no wake, no Kutta condition and no
+ * pressure (Aerodynamic_Solver.cpp:169-180); these define them for lifting bodies.
+ * bem_aero_set_wake: n_wake flat constant-doublet wake strips (quads: n_wake x 4 x 3
+ * vertices, normal from the vertex order as for body panels) whose strengths are the
+ * Kutta jumps X[te_upper[w]] - X[te_lower[w]]; the next bem_aero_setup adds each
+ * strip's dipole influence to H's column te_upper[w] and subtracts it from column
+ * te_lower[w] (on the GPU).  n_wake = 0 removes the wake.
+ * bem_mesh_wing_wake: the wake of bem_mesh_wing's wing: one strip per panel column from
+ * the trailing edge (x = chord, z = 0) to length chords downstream, normal -z, Kutta pair
+ * (upper trailing-edge panel j nc + nc - 1, lower j nc).
+ * bem_aero_surface: surface pressure of a solution X for a uniform onset flow vel (3):
+ * V = U - (U . n) n + grad X, the least-squares surface gradient over each panel's edge
+ * neighbours that face the same side (n_i . n_j > 0); cp = 1 - |V|^2 / |U|^2 (N values,
+ * may be NULL); coeffs (may be NULL) = {CFx, CFy, CFz, CL, CD} with CF = sum cp n A / s_ref
+ * (n into the body), CL along the unit normal to U in the x-z plane, CD along U.  Host only. */
+bem_status bem_aero_set_wake(bem_ctx* ctx, int n_wake, const double* quads, const int* te_upper,
+                             const int* te_lower);
+int bem_mesh_wing_wake(double chord, double span, int nc, int ns, double length, double* quads, int* te_upper,
+                       int* te_lower);
+bem_status bem_aero_surface(bem_ctx* ctx, const double* X, const double* vel, double s_ref, double* cp,
+                            double* coeffs);
+
 /* ---- influence matrices (Prepare_Linear_System / _Wave_Terms) -------------- */
 
 /* Copies the Rankine kernel values of the current setup to host, N x N

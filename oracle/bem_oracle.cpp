@@ -855,6 +855,52 @@ void orc_aero(int nn, const double* nodes, int ne, const int* elems, int ncomp, 
     for (int i = 0; i < N; ++i) X[i] = b[i].real();
 }
 
+// The steady solve with a trailing wake (the configuration the reference's
+// Aerodynamic_Solver lacks, defined here): wake strip w is a constant-doublet panel
+// (wake mesh element w, normal pointing down, i.e. away from the fluid above it) whose
+// strength is the Kutta jump X[te_up[w]] - X[te_lo[w]] (Morino), so its dipole influence
+// D_w(x_R) joins column te_up[w] of H with + and column te_lo[w] with -.  Otherwise as
+// orc_aero: H X = G (V . n).
+void orc_aero_wake(int nn, const double* nodes, int ne, const int* elems, int ncomp, const int* comp_first,
+                   const double* comp_origin, int nwn, const double* wnodes, int nw, const int* welems,
+                   const int* te_up, const int* te_lo, int nvel, const double* vel, double* X, double* BC) {
+    Mesh m = make_mesh(nn, nodes, ne, elems, ncomp, comp_first, comp_origin);
+    Mesh wm = make_mesh(nwn, wnodes, nw, welems, 0, nullptr, nullptr);
+    std::vector<Panel> body, mir, wake, wmir;
+    build_panels(m, body, mir);
+    build_panels(wm, wake, wmir);
+    std::vector<V3> x = collocation(body);
+    const int N = ne;
+    std::vector<double> G((size_t)N * N), H((size_t)N * N);
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int S = 0; S < N; ++S)
+        for (int R = 0; R < N; ++R) inf_source_kernel(body[S], x[R], G[(size_t)R * N + S], H[(size_t)R * N + S]);
+    #pragma omp parallel for schedule(static)
+    for (int R = 0; R < N; ++R)
+        for (int w = 0; w < nw; ++w) {
+            double sw, dw;
+            inf_source_kernel(wake[w], x[R], sw, dw);
+            H[(size_t)R * N + te_up[w]] += dw;
+            H[(size_t)R * N + te_lo[w]] -= dw;
+        }
+    for (int i = 0; i < N; ++i) {
+        const double* v = nvel == 1 ? vel : vel + 3 * (size_t)i;
+        BC[i] = v[0] * body[i].ez.x + v[1] * body[i].ez.y + v[2] * body[i].ez.z;
+    }
+    std::vector<cplx> A((size_t)N * N), b(N);
+    for (size_t k = 0; k < (size_t)N * N; ++k) A[k] = cplx(H[k], 0.0);
+    #pragma omp parallel for schedule(static)
+    for (int R = 0; R < N; ++R) {
+        double acc = 0;
+        for (int S = 0; S < N; ++S) acc += G[(size_t)R * N + S] * BC[S];
+        b[R] = cplx(acc, 0.0);
+    }
+    std::vector<int> piv(N);
+    lu_factor(N, A.data(), piv.data());
+    lu_solve(N, A.data(), piv.data(), 1, b.data());
+    for (int i = 0; i < N; ++i) X[i] = b[i].real();
+}
+
 // Complex LU + solve (interleaved re/im, row-major), exposed for baselines/tests.
 void orc_lu_solve(int n, double* a, int nr, double* b) {
     std::vector<int> piv(n);

@@ -94,6 +94,7 @@ class Oracle:
         L.orc_wave.argtypes = mesh_args + [_d, _dp, _dp]
         L.orc_wave_rows.argtypes = mesh_args + [_d, _i, _i, _dp, _dp]
         L.orc_lu_solve.argtypes = [_i, _dp, _i, _dp]
+        L.orc_aero_wake.argtypes = mesh_args + [_i, _dp, _i, _ip, _ip, _ip, _i, _dp, _dp, _dp]
         L.orc_aero.argtypes = mesh_args + [_i, _dp, _dp, _dp]
         L.orc_mass_hydrostatics.argtypes = mesh_args + mesh_args + [_d, _d, _d, _dp, _dp, _dp, _dp, _dp]
         L.orc_solve.argtypes = mesh_args + [_i, _dp, _i, _dp, _d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -267,6 +268,23 @@ class Oracle:
         X = np.zeros(mesh.n)
         BC = np.zeros(mesh.n)
         self.L.orc_aero(*mesh.args(), vel.shape[0], _p(vel), _p(X), _p(BC))
+        return X, BC
+
+    def aero_wake(self, mesh, wake_quads, te_up, te_lo, vel):
+        """The steady constant-panel solve with a trailing wake (orc_aero_wake): wake strip w
+        is the quad wake_quads[w] (4 x 3 vertices), its strength the Kutta jump
+        X[te_up[w]] - X[te_lo[w]].  Returns (X, BC)."""
+        q = np.ascontiguousarray(wake_quads, dtype=np.float64).reshape(-1, 4, 3)
+        nw = q.shape[0]
+        wn = np.ascontiguousarray(q.reshape(-1, 3))
+        we = np.ascontiguousarray(np.arange(4 * nw, dtype=np.int32).reshape(nw, 4))
+        up = np.ascontiguousarray(te_up, dtype=np.int32)
+        lo = np.ascontiguousarray(te_lo, dtype=np.int32)
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        X = np.zeros(mesh.n)
+        BC = np.zeros(mesh.n)
+        self.L.orc_aero_wake(*mesh.args(), wn.shape[0], _p(wn), nw, _p(we, _ip), _p(up, _ip), _p(lo, _ip),
+                             vel.shape[0], _p(vel), _p(X), _p(BC))
         return X, BC
 
     def set_threads(self, n):
