@@ -363,6 +363,7 @@ __device__ __forceinline__ bool wave_admit(const WaveArgs& a, uint32_t& smid, in
 // here: it is applied exactly, in FP64, by the plane-wave kernels below
 // (k_pw_*), because the radiation damping at low K is a small difference of
 // O(K) imaginary terms and amplifies FP32 rounding in them up to ~200x.
+template <int RM>
 __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     const int lane = threadIdx.x & 31;
     __shared__ int s_admit;
@@ -383,9 +384,9 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         const Recv32 Rv = load_recv32(a, r);
         const float Kh = a.kh, Kl = a.kl;
         const float c1 = a.c1f, c2 = a.c2f;
-        float acc_re[MAX_RHS], acc_im[MAX_RHS];
+        float acc_re[RM], acc_im[RM];
     #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
+        for (int j = 0; j < RM; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
         const size_t row = (size_t)r * a.ld;
         const bool live = a.live != 0;
         const size_t fs = (size_t)4 * N;
@@ -420,7 +421,7 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
             // the real part of S = Ssrc + Srefl - ws applied to B: -ws_re * B
             const float* b = a.Bm32 + (size_t)s * 2 * R;
     #pragma unroll
-            for (int j = 0; j < MAX_RHS; ++j) {
+            for (int j = 0; j < RM; ++j) {
                 if (j < R) {
                     acc_re[j] = fmaf(-wsr, __ldg(b + 2 * j), acc_re[j]);
                     acc_im[j] = fmaf(-wsr, __ldg(b + 2 * j + 1), acc_im[j]);
@@ -429,7 +430,7 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         }
         if (a.mode == 1) continue;
     #pragma unroll
-        for (int j = 0; j < MAX_RHS; ++j) {
+        for (int j = 0; j < RM; ++j) {
             if (j < R) {
                 float vr = acc_re[j], vi = acc_im[j];
     #pragma unroll
@@ -1174,7 +1175,12 @@ void launch_wave(cudaStream_t st, const WaveArgs& a, bool fp32) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaMemsetAsync(a.row_ctr, 0, sizeof(int) * (2 + WAVE_SM_SLOTS), st);
-        BEM_LAUNCH(k_wave_mixed<<<std::min(3 * nsm, (b.N + 7) / 8), 256, 0, st>>>(b));
+        // the S*B accumulators are sized for the right-hand sides at hand: with 16 of them the
+        // kernel spills at its 80-register bound (three CTAs per SM), with 8 or 10 it does not
+        const int grid = std::min(3 * nsm, (b.N + 7) / 8);
+        if (b.R <= 8) BEM_LAUNCH(k_wave_mixed<8><<<grid, 256, 0, st>>>(b));
+        else if (b.R <= 10) BEM_LAUNCH(k_wave_mixed<10><<<grid, 256, 0, st>>>(b));
+        else BEM_LAUNCH(k_wave_mixed<MAX_RHS><<<grid, 256, 0, st>>>(b));
     } else {
         BEM_LAUNCH(k_wave<double><<<(a.N + 7) / 8, 256, 0, st>>>(a));
     }
