@@ -551,8 +551,8 @@ def main():
             "peak_source": "measured: FP32 FMA loop timed with CUDA events (bem_fp32_peak); not in MEASURED_PEAKS.json",
             "ops_per_eval": 345, "evals_per_launch": evals, "avg_launch_ms": wk_ms, "launches": int(kt[1]),
             "green_evals_per_s": evals / (wk_ms / 1000.0),
-            "traffic": 32.0 * N * N * (483.9e6 / (32.0 * 4096 * 4096)),
-            "traffic_source": "ncu dram__bytes_read+write of one 4096-panel launch (270.9 MB + 213.0 MB), scaled by "
+            "traffic": 32.0 * N * N * (480.9e6 / (32.0 * 4096 * 4096)),
+            "traffic_source": "ncu dram__bytes_read+write of one 4096-panel launch (270.7 MB + 210.2 MB), scaled by "
                               "N^2 (the pair count)",
             "hbm": {"bytes_per_launch": 16.0 * N * N, "achieved_gbs": 16.0 * N * N / (wk_ms / 1000.0) / 1e9,
                     "peak_gbs": hbm_peak, "peak_source": "measured, MEASURED_PEAKS.json"}}
