@@ -143,7 +143,14 @@ struct bem_ctx {
     int resid_mode = 0;
     FreqState fs[2];
     cudaStream_t sa = nullptr;        // assembly stream of the pipelined mixed path (lowest priority)
+    // Device memory.  allocs: the blocks in use (each with its size in alloc_bytes).
+    // free_all returns them to pool, from which later allocations of this context are
+    // served (best fit, at most twice the request), so that setting up body after body
+    // does not call cudaMalloc / cudaFree (which synchronize the whole device) each time;
+    // the pool is released on bem_destroy and when a cudaMalloc fails.
     std::vector<void*> allocs;
+    std::map<void*, size_t> alloc_bytes;
+    std::multimap<size_t, void*> pool;
     // stage timing (ms) and launch counts
     cudaEvent_t ev[8] = {};
     cudaStream_t sp = nullptr;                   // panel stream of the lookahead LU (higher priority)
@@ -202,18 +209,47 @@ bem_status fail(bem_ctx* c, bem_status s, const std::string& msg) {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                       \
     } while (0)
 
+void release_pool(bem_ctx* ctx) {
+    for (auto& kv : ctx->pool) {
+        cudaFree(kv.second);
+        ctx->alloc_bytes.erase(kv.second);
+    }
+    ctx->pool.clear();
+}
+
 template <typename T> bem_status dalloc(bem_ctx* ctx, T** p, size_t count) {
     if (*p) return BEM_OK;
+    const size_t bytes = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~(size_t)255;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(ctx, BEM_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
-                                            " bytes failed: " + cudaGetErrorString(e));
+    auto it = ctx->pool.lower_bound(bytes);
+    if (it != ctx->pool.end() && it->first <= 2 * bytes + ((size_t)1 << 20)) {
+        q = it->second;
+        ctx->pool.erase(it);
+    } else {
+        cudaError_t e = cudaMalloc(&q, bytes);
+        if (e != cudaSuccess && !ctx->pool.empty()) {
+            cudaGetLastError();
+            release_pool(ctx);
+            e = cudaMalloc(&q, bytes);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, BEM_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) +
+                                                " bytes failed: " + cudaGetErrorString(e));
+        }
+        ctx->alloc_bytes[q] = bytes;
     }
     *p = static_cast<T*>(q);
     ctx->allocs.push_back(q);
     return BEM_OK;
+}
+
+// returns a block in use to the context's pool
+void pool_return(bem_ctx* ctx, void* q) {
+    auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), q);
+    if (it == ctx->allocs.end()) return;
+    ctx->allocs.erase(it);
+    ctx->pool.insert({ctx->alloc_bytes[q], q});
 }
 #define DA(ptr, count)                                         \
     do {                                                       \
@@ -234,7 +270,10 @@ void reset_slot(FreqState& F) {
 }
 
 void free_all(bem_ctx* ctx) {
-    for (void* p : ctx->allocs) cudaFree(p);
+    // the blocks go back to the pool, so this context's work on them must be finished
+    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr})
+        if (q) cudaStreamSynchronize(q);
+    for (void* p : ctx->allocs) ctx->pool.insert({ctx->alloc_bytes[p], p});
     ctx->allocs.clear();
     double** dp[] = {&ctx->d_rec, &ctx->d_xr, &ctx->d_gq, &ctx->d_rn, &ctx->d_cen, &ctx->d_nrm, &ctx->d_area,
                      &ctx->d_Nk, &ctx->d_betas, &ctx->d_RS, &ctx->d_RD, &ctx->d_RSR, &ctx->d_D64r, &ctx->d_D64i,
@@ -286,10 +325,11 @@ bem_status pw_prepare(bem_ctx* ctx, FreqState& F, double K, cudaStream_t st) {
     if (M > F.pw_Mmax) {
         if (F.pwE) {
             // grow: release the old factor buffers
+            // (after this slot's previous work, which used them, has finished)
+            CK(cudaStreamSynchronize(st));
+            if (ctx->sa) CK(cudaStreamSynchronize(ctx->sa));
             for (void** p : {(void**)&F.pwE, (void**)&F.pwV, (void**)&F.pwW, (void**)&F.pwT}) {
-                auto it = std::find(ctx->allocs.begin(), ctx->allocs.end(), *p);
-                if (it != ctx->allocs.end()) ctx->allocs.erase(it);
-                cudaFree(*p);
+                pool_return(ctx, *p);
                 *p = nullptr;
             }
         }
@@ -910,6 +950,7 @@ void bem_destroy(bem_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_all(ctx);
+    release_pool(ctx);
     if (ctx->sp) cudaStreamSynchronize(ctx->sp);
     if (ctx->sa) cudaStreamSynchronize(ctx->sa);
     if (ctx->su) cudaStreamSynchronize(ctx->su);
