@@ -1339,6 +1339,7 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     if (precision != BEM_PLAIN_FP64 && precision != BEM_MIXED) return fail(ctx, BEM_ERR_ARG, "unknown precision mode");
     for (int f = 0; f < n_freq; ++f)
         if (!std::isfinite(omega[f])) return fail(ctx, BEM_ERR_ARG, "non-finite frequency");
+    if (n_freq == 0) return BEM_OK;
     CK(cudaSetDevice(ctx->device));
     const bool mixed = precision == BEM_MIXED;
     if (!(tol > 0)) tol = 1e-12;

@@ -57,7 +57,15 @@ __device__ __forceinline__ void source_kernel(const double* __restrict__ p, doub
         if (k < n) {
             int k1 = (k + 1 < n) ? k + 1 : 0;
             double m = p[21 + k];
-            Phi += atan((m * e[k] - h[k]) / (PLz * r[k])) - atan((m * e[k1] - h[k1]) / (PLz * r[k1]));
+            // atan(A0 / (z r0)) - atan(A1 / (z r1)) as one atan2: both angles lie in
+            // (-pi/2, pi/2), so their difference is the angle of (z (A0 r1 - A1 r0),
+            // z^2 r0 r1 + A0 A1) (both multiplied by z^2 r0 r1 > 0).  Half the arctangents
+            // and none of the divisions; a vertical edge (infinite slope) keeps the two terms.
+            const double A0 = m * e[k] - h[k], A1 = m * e[k1] - h[k1];
+            if (isfinite(m))
+                Phi += atan2(PLz * (A0 * r[k1] - A1 * r[k]), Z2 * r[k] * r[k1] + A0 * A1);
+            else
+                Phi += atan(A0 / (PLz * r[k])) - atan(A1 / (PLz * r[k1]));
             double ddx = p[13 + k1] - p[13 + k], ddy = p[17 + k1] - p[17 + k];
             double d = p[25 + k];
             double B = (DX[k] * ddy - DY[k] * ddx) / d;
