@@ -145,14 +145,14 @@ __device__ __forceinline__ void gf64(const PolyCoef64& P, double hh, double vv, 
 }
 
 // ---- FP32 -----------------------------------------------------------------
-__device__ __forceinline__ float struve_h0_32(float x, float y0x) {
+// t3 = 3 / x (used for x > 3), computed once by the caller for all the x > 3 forms.
+__device__ __forceinline__ float struve_h0_32(float x, float y0x, float t3) {
     if (x <= 3.0f) {
         float yy = (x * (1.0f / 3.0f)) * (x * (1.0f / 3.0f));
         float s = fmaf(fmaf(fmaf(fmaf(fmaf(-0.000876918f, yy, 0.013828813f), yy, -0.126164557f), yy, 0.687514637f), yy, -1.909855001f), yy, 1.909859164f);
         return s * (x * (1.0f / 3.0f));
     }
-    float r = 3.0f / x;
-    float yy = r * r;
+    float yy = t3 * t3;
     float c1 = 2.0f * fmaf(fmaf(fmaf(0.32303607f, yy, 3.85542044f), yy, 4.77228920f), yy, 0.99999906f);
     float c2 = 3.14159265f * x * fmaf(fmaf(fmaf(0.52120508f, yy, 4.28957333f), yy, 4.88331068f), yy, 1.0f);
     return __fdividef(c1, c2) + y0x;
@@ -164,7 +164,7 @@ __device__ __forceinline__ float struve_h0_32(float x, float y0x) {
 // about yy = 1/2 with t = x^2 - 9/2 formed by one FMA; for x > 3,
 // 2/pi - c1/c2 = ((2/pi) c2 - c1) / c2 with the numerator's coefficients
 // subtracted exactly on the host, so only Y1 is added to a small, accurate term.
-__device__ __forceinline__ float h1_gap32(const PolyCoef32& P, float x, float y1x) {
+__device__ __forceinline__ float h1_gap32(const PolyCoef32& P, float x, float y1x, float t3) {
     if (x <= 3.0f) {
         const float t = fmaf(x, x, -4.5f);
         float r = P.h1s[6];
@@ -172,8 +172,7 @@ __device__ __forceinline__ float h1_gap32(const PolyCoef32& P, float x, float y1
         for (int k = 5; k >= 0; --k) r = fmaf(r, t, P.h1s[k]);
         return r;
     }
-    const float r = 3.0f / x;
-    const float yy = r * r;
+    const float yy = t3 * t3;
     const float num = fmaf(fmaf(fmaf(P.h1d[3], yy, P.h1d[2]), yy, P.h1d[1]), yy, P.h1d[0]);
     const float c2 = 3.14159265f * fmaf(fmaf(fmaf(0.10885141f, yy, 2.26216956f), yy, 3.81095112f), yy, 1.0f);
     return __fdividef(num, c2) - y1x;
@@ -219,10 +218,11 @@ __device__ __forceinline__ void sincos_reduced(float x, float& sn, float& cs) {
     cs = ((iq + 1) & 2) ? -c0 : c0;
 }
 
-__device__ __forceinline__ void bessel_large(float xh, float xl, float& j0, float& j1, float& y0, float& y1) {
+__device__ __forceinline__ void bessel_large(float xh, float xl, float t3, float& j0, float& j1, float& y0,
+                                             float& y1) {
     const float TWOPI_H = 6.28318548f, TWOPI_L = -1.74845553e-7f;  // 2 pi = H + L
     const float PI4_H = 0.785398185f, PI4_L = -2.18556949e-8f;     // pi / 4 = H + L
-    const float t = 3.0f * __frcp_rn(xh);
+    const float t = t3;
     const float f0 = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00014476f, -0.00072805f), 0.00137237f),
                                                 -0.00009512f), -0.00552740f), -0.00000077f), 0.79788456f);
     const float d0 = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.00013558f, -0.00029333f), -0.00054125f),
@@ -300,10 +300,11 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
     bool far = hh > 3.0f;
+    const float t3 = far ? 3.0f * __frcp_rn(hh) : 0.0f;
     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
-    if (far) bessel_large(hh, 0.0f, j0v, j1v, y0v, y1v);
+    if (far) bessel_large(hh, 0.0f, t3, j0v, j1v, y0v, y1v);
     else bessel_j01_small(hh, j0v, j1v);
-    float H0 = struve_h0_32(hh, y0v), H1g = h1_gap32(P, hh, y1v);
+    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(P, hh, y1v, t3);
     float E = 2.0f * PI * ev;
     G.re = fmaf(E, H0, L0);
     G.im = -E * j0v;
@@ -323,11 +324,11 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
 
 // ---- FP32 real parts + imaginary-part remainders ----------------------------
 // Real parts of G and dG/dh (as gf32 computes them).
-// y0v, y1v: Y0(hh), Y1(hh) (used when hh > 3).
+// y0v, y1v: Y0(hh), Y1(hh), t3 = 3 / hh (used when hh > 3).
 // Gv: dG/dv ~ Gr - 2/d (to about 1 %: the infinite-depth wave term satisfies dG/dv = G
 // up to the Rankine image's 2/d), used for the first-order correction of the rounding of v.
 __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float y0v, float y1v,
-                                        float& Gr, float& Ghr, float& Gv) {
+                                        float t3, float& Gr, float& Ghr, float& Gv) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
@@ -350,7 +351,7 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     RR = fmaf(beta * (1.0f - beta), D, RR);
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
-    float H0 = struve_h0_32(hh, y0v), H1g = h1_gap32(P, hh, y1v);
+    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(P, hh, y1v, t3);
     float E = 2.0f * PI * ev;
     Gr = fmaf(E, H0, L0);
     Gv = fmaf(-2.0f, inv_d, Gr);

@@ -251,6 +251,7 @@ struct GaussGeo {
     float sx, lx, sy, ly, sz, ez;  // dimensional differences receiver - Gauss point (hi, lo)
     float XX, YY;                  // K dx, K dy
     float hh, hl, VV, vl;
+    float inv_h;                   // 1 / hh: the x > 3 Bessel/Struve forms and dG/dx, dG/dy
 };
 
 __device__ __forceinline__ GaussGeo gauss_geo32(const Recv32& R, float gx, float gy, float gz, float gxl, float gyl,
@@ -274,6 +275,7 @@ __device__ __forceinline__ GaussGeo gauss_geo32(const Recv32& R, float gx, float
     o.XX = (o.sx + o.lx) * K;
     o.YY = (o.sy + o.ly) * K;
     df_hdist(o.sx, o.lx, o.sy, o.ly, Kh, Kl, o.hh, o.hl);
+    o.inv_h = __frcp_rn(o.hh);
     return o;
 }
 
@@ -282,10 +284,11 @@ __device__ __forceinline__ void gauss_G32(const GaussGeo& o, float& Gr, float& G
     const float twopi = 6.28318530717959f;
     const float ev = expf(o.VV);
     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
-    if (o.hh > 3.0f) bessel_large(o.hh, o.hl, j0v, j1v, y0v, y1v);
+    const float t3 = 3.0f * o.inv_h;
+    if (o.hh > 3.0f) bessel_large(o.hh, o.hl, t3, j0v, j1v, y0v, y1v);
     else bessel_j01_small(o.hh, j0v, j1v);
     float Gv;
-    gf32_re(c_poly32, o.hh, o.VV, ev, y0v, y1v, Gr, Ghr, Gv);
+    gf32_re(c_poly32, o.hh, o.VV, ev, y0v, y1v, t3, Gr, Ghr, Gv);
     // G at the unrounded (h, v): the first-order terms of the float pairs' low parts.
     // The radiation damping is a small difference of terms that each carry this
     // rounding, so without it B loses ~1e-6 at the highest frequencies.
@@ -303,9 +306,8 @@ __device__ __forceinline__ void gauss_accum32(const GaussGeo& o, float Gr, float
     const float proj = fmaf(o.XX, nx, o.YY * ny);
     float dgr = 0.f, dgi = 0.f;
     if (o.hh > 1.0e-6f) {
-        const float inv_h = __frcp_rn(o.hh);
-        dgr = Ghr * proj * inv_h;
-        dgi = Ghi * proj * inv_h;
+        dgr = Ghr * proj * o.inv_h;
+        dgi = Ghi * proj * o.inv_h;
     }
     wsr = fmaf(wc1, Gr, wsr);
     wsi = fmaf(wc1, Gi, wsi);
