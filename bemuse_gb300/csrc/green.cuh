@@ -267,8 +267,11 @@ __device__ __forceinline__ void df_hdist(float dxh, float dxl, float dyh, float 
     const float r2 = p + q;
     const float bb = r2 - p;
     const float r2l = ((p - (r2 - bb)) + (q - bb)) + (ep + eq);
-    const float rh = sqrtf(r2);
-    const float rl = r2 > 0.0f ? (fmaf(-rh, rh, r2) + r2l) * (0.5f * __frcp_rn(rh)) : 0.0f;
+    // sqrt(r2) to about an ulp from the reciprocal square root; rl, formed from the exact
+    // residual r2 - rh^2, makes (rh, rl) the square root to second order all the same
+    const float rs = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+    const float rh = r2 * rs;
+    const float rl = (fmaf(-rh, rh, r2) + r2l) * (0.5f * rs);
     const float h = kh * rh;
     const float h2 = fmaf(kh, rh, -h) + fmaf(kh, rl, kl * rh);
     hh = h + h2;
@@ -332,14 +335,16 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
-    float inv_d = __frcp_rn(dd);
+    // approximate reciprocals (about an ulp): they scale terms whose FP32 rounding is
+    // of the same size, while dd itself stays correctly rounded
+    float inv_d = __fdividef(1.0f, dd);
     float alpha = -vv * inv_d;
     float beta = hh * inv_d;
     float rho = __fdividef(dd, 1.0f + dd);
     float u = rho - 0.5f;
     float d2 = dd * dd;
     float d3 = d2 * dd;
-    float inv_1d3 = __frcp_rn(1.0f + d3);
+    float inv_1d3 = __fdividef(1.0f, 1.0f + d3);
     float dmv = dd - vv;
     float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
     PP = fmaf(PP, ev, d2 - vv);

@@ -275,7 +275,7 @@ __device__ __forceinline__ GaussGeo gauss_geo32(const Recv32& R, float gx, float
     o.XX = (o.sx + o.lx) * K;
     o.YY = (o.sy + o.ly) * K;
     df_hdist(o.sx, o.lx, o.sy, o.ly, Kh, Kl, o.hh, o.hl);
-    o.inv_h = __frcp_rn(o.hh);
+    o.inv_h = __fdividef(1.0f, o.hh);
     return o;
 }
 
