@@ -58,6 +58,7 @@ struct WaveArgs {
     // mixed mode only
     const float* xr32;    // collocation points, hi/lo split: [6][N] (xh, yh, zh, xl, yl, zl)
     const float* gq32;    // Gauss data [10][4][N]: xh, yh, zh, w, nx, ny, nz, xl, yl, zl
+    const float4* gq32v;  // the same as [4][3][N] float4: (xh, yh, zh, w), (nx, ny, nz, xl), (yl, zl, 0, 0)
     float* Dhi; float* Dlo;   // Re D as a float pair hi + lo (~48-bit) for the refinement residual [N][ld]
     const float* Bm32;        // B as floats [N][R] complex interleaved
     const float* RDhi; const float* RDlo;    // RD as float pairs [N][ld]

@@ -136,6 +136,7 @@ struct bem_ctx {
     double last_contraction = 0.0;  // residual ratio of the last two full-accuracy sweeps
     // mixed-precision wave assembly
     float *d_xr32 = nullptr, *d_gq32 = nullptr;
+    float4* d_gq32v = nullptr;
     double pw_D = 0.0;                // largest horizontal receiver-to-Gauss-point distance
     // operator used by the refinement residual: 0 = stored D64 (re, im); 1 = stored
     // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
@@ -293,6 +294,7 @@ void free_all(bem_ctx* ctx) {
     ctx->d_norms = nullptr;
     ctx->d_xr32 = nullptr;
     ctx->d_gq32 = nullptr;
+    ctx->d_gq32v = nullptr;
     ctx->d_wpts = ctx->d_ext = nullptr;
     ctx->wpts_cap = ctx->ext_cap = 0;
     for (LuGraph& g : ctx->lu_graph) {
@@ -1087,6 +1089,18 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
             for (int k = 3; k < 7; ++k) gq32[((size_t)k * 4 + q) * N + i] = (float)f[k];
         }
     }
+    // the same grouped for 16-byte loads: [q][group][panel] float4,
+    // groups (xh, yh, zh, w), (nx, ny, nz, xl), (yl, zl, 0, 0)
+    std::vector<float> gq32v((size_t)4 * 3 * N * 4, 0.0f);
+    {
+        const int grp[3][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {8, 9, -1, -1}};
+        for (int q = 0; q < 4; ++q)
+            for (int g = 0; g < 3; ++g)
+                for (int i = 0; i < N; ++i)
+                    for (int c = 0; c < 4; ++c)
+                        if (grp[g][c] >= 0)
+                            gq32v[(((size_t)q * 3 + g) * N + i) * 4 + c] = gq32[((size_t)grp[g][c] * 4 + q) * N + i];
+    }
     {
         // largest horizontal distance between a collocation point and a Gauss point (bounding boxes)
         double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
@@ -1141,6 +1155,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
     DA(ctx->d_xr32, xr32.size());
     DA(ctx->d_gq32, gq32.size());
+    DA(ctx->d_gq32v, gq32v.size() / 4);
     std::vector<float> pdiam(N);
     for (int i = 0; i < N; ++i) {
         const bem::PanelGeom& pg = mirror[i];
@@ -1158,6 +1173,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     CK(cudaMemcpyAsync(ctx->d_pdiam, pdiam.data(), pdiam.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_xr32, xr32.data(), xr32.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_gq32, gq32.data(), gq32.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_gq32v, gq32v.data(), gq32v.size() * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_rec, rec.data(), rec.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_gq, gq.data(), gq.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ctx->d_xr, xr.data(), xr.size() * 8, cudaMemcpyHostToDevice, st));
@@ -1262,6 +1278,7 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         a.RSRhi = ctx->d_RSRhi; a.RSRlo = ctx->d_RSRlo;
         a.xr32 = ctx->d_xr32;
         a.gq32 = ctx->d_gq32;
+        a.gq32v = ctx->d_gq32v;
         a.Dhi = F.Dhi;
         a.Dlo = F.Dlo;
         a.D64r = nullptr;
@@ -1679,6 +1696,7 @@ bem_status bem_wave_matrices(bem_ctx* ctx, double K, int precision, double* ws, 
     a.ws_out = buf; a.wd_out = buf + 2 * (size_t)N * N;
     a.xr32 = ctx->d_xr32;
     a.gq32 = ctx->d_gq32;
+    a.gq32v = ctx->d_gq32v;
     a.row_ctr = ctx->d_wctr;
     a.sm_ctr = ctx->d_wctr + 1;
     a.reserve = 0;

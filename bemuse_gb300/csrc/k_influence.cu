@@ -399,7 +399,6 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
         for (int j = 0; j < RM; ++j) { acc_re[j] = 0.f; acc_im[j] = 0.f; }
         const size_t row = (size_t)r * a.ld;
         const bool live = a.live != 0;
-        const size_t fs = (size_t)4 * N;
         for (int s = s_begin + lane; s < s_end; s += 32) {
             float wsr = 0.f, wsi = 0.f, wdr = 0.f, wdi = 0.f;
             // the pair's Rankine float pairs come from HBM: issued first, so that their latency
@@ -413,12 +412,11 @@ __global__ void __launch_bounds__(256, 3) k_wave_mixed(WaveArgs a) {
     #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (q < nq) {
-                    // source data is read by every row: read-only path
-                    const float* g = a.gq32 + (size_t)q * N + s;
-                    const float w = __ldg(g + 3 * fs);
-                    gauss_eval32(Rv, __ldg(g), __ldg(g + fs), __ldg(g + 2 * fs), __ldg(g + 7 * fs), __ldg(g + 8 * fs),
-                                 __ldg(g + 9 * fs), __ldg(g + 4 * fs), __ldg(g + 5 * fs), __ldg(g + 6 * fs), w * c1,
-                                 w * c2, Kh, Kl, wsr, wsi, wdr, wdi);
+                    // source data is read by every row: read-only path, three 16-byte loads
+                    const float4* gv = a.gq32v + (size_t)q * 3 * N + s;
+                    const float4 g0 = __ldg(gv), g1 = __ldg(gv + N), g2 = __ldg(gv + 2 * N);
+                    gauss_eval32(Rv, g0.x, g0.y, g0.z, g1.w, g2.x, g2.y, g1.x, g1.y, g1.z, g0.w * c1, g0.w * c2, Kh,
+                                 Kl, wsr, wsi, wdr, wdi);
                 }
             }
             if (a.mode == 1) {
