@@ -55,8 +55,15 @@ struct FreqState {
     cudaEvent_t ev_t[4] = {};                 // timing: assembly start, static RHS done, wave kernel start/end
     cudaEvent_t ev_t5 = nullptr;              // timing: assembly end
     float* Ws32 = nullptr;                    // surrogate form: Re ws per pair [N][Np]
-    unsigned long long* sur_stats = nullptr;  // surrogate form: the assembly's counts (SurArgs::stats)
+    unsigned long long* sur_stats = nullptr;  // surrogate form: the assembly's counts (SurArgs::stats), and
+                                              // in word 4 its device flags (an expired wait)
     bool sur_used = false;                    // this slot's frequency was assembled with the surrogate
+    // mixed path: this slot's FP32 block inverses and device flags, so that the LU of one
+    // frequency can run while the solves of the other slot's frequency read their own
+    float *inv32r = nullptr, *inv32i = nullptr;
+    int* flags = nullptr;
+    cudaEvent_t ev_lu0 = nullptr, ev_lu = nullptr;   // LU start / done (stream st)
+    cudaEvent_t ev_sv0 = nullptr, ev_sv1 = nullptr;  // solves start / done
 };
 
 // One captured tensor-core LU (per frequency slot) and what it was captured for.
@@ -93,7 +100,11 @@ struct bem_ctx {
     float* d_X32 = nullptr;
     double *d_part = nullptr, *d_post = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
-    float *d_inv32r = nullptr, *d_inv32i = nullptr, *d_wl32 = nullptr, *d_pairT = nullptr, *d_wut32 = nullptr;
+    float *d_wl32 = nullptr, *d_pairT = nullptr, *d_wut32 = nullptr;
+    // solve stream of the pipelined mixed path: the refinement and post-processing of
+    // frequency f run here while the LU of f + 1 runs on st (tuning key lu_overlap)
+    cudaStream_t ss = nullptr;
+    int lu_overlap = 1;
     int* d_flags = nullptr;
     int* d_ready = nullptr;           // block-ready flags of the cooperative triangular solves
     int solve_epoch = 0;
@@ -142,7 +153,7 @@ struct bem_ctx {
     // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
     // 3 = Re D as float pairs + plane-wave Im D (hydro, K != 0)
     int resid_mode = 0;
-    FreqState fs[2];
+    FreqState fs[3];                  // frequency slots (the split pipeline uses three)
     cudaStream_t sa = nullptr;        // assembly stream of the pipelined mixed path (lowest priority)
     // Device memory.  allocs: the blocks in use (each with its size in alloc_bytes).
     // free_all returns them to pool, from which later allocations of this context are
@@ -181,7 +192,7 @@ struct bem_ctx {
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
-    LuGraph lu_graph[2];                        // captured LU per frequency slot
+    LuGraph lu_graph[3];                        // captured LU per frequency slot
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
     // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
@@ -268,11 +279,13 @@ void reset_slot(FreqState& F) {
     F.Ws32 = nullptr;
     F.sur_stats = nullptr;
     F.sur_used = false;
+    F.inv32r = F.inv32i = nullptr;
+    F.flags = nullptr;
 }
 
 void free_all(bem_ctx* ctx) {
     // the blocks go back to the pool, so this context's work on them must be finished
-    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr})
+    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr, ctx->ss})
         if (q) cudaStreamSynchronize(q);
     for (void* p : ctx->allocs) ctx->pool.insert({ctx->alloc_bytes[p], p});
     ctx->allocs.clear();
@@ -282,7 +295,7 @@ void free_all(bem_ctx* ctx) {
                      &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64, &ctx->d_gmV, &ctx->d_gmZ, &ctx->d_gmW,
                      &ctx->d_gmPart, &ctx->d_gmH, &ctx->d_gmC};
     for (auto p : dp) *p = nullptr;
-    float** fp[] = {&ctx->d_X32, &ctx->d_inv32r, &ctx->d_inv32i, &ctx->d_wl32, &ctx->d_pairT, &ctx->d_wut32,
+    float** fp[] = {&ctx->d_X32, &ctx->d_wl32, &ctx->d_pairT, &ctx->d_wut32,
                     &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi, &ctx->d_RSRlo};
     for (auto p : fp) *p = nullptr;
     for (FreqState& F : ctx->fs) reset_slot(F);
@@ -387,8 +400,9 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     } else {
         DA(ctx->fs[0].D32r, (size_t)Np * Np);
         DA(ctx->fs[0].D32i, (size_t)Np * Np);
-        DA(ctx->d_inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
-        DA(ctx->d_inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
+        DA(ctx->fs[0].inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
+        DA(ctx->fs[0].inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
+        DA(ctx->fs[0].flags, 1);
         DA(ctx->d_wl32, (size_t)8 * Np * nb32);  // four [2][Np][128] buffers (lookahead; two steps per pass)
         DA(ctx->d_pairT, (size_t)2 * Np * nb32);  // transposed pair blocks of the pair fold (4 (Np/256) 128^2)
         DA(ctx->d_wut32, (size_t)8 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
@@ -428,9 +442,8 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
 bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double tol, int max_iter,
                         const std::function<void(const double*, const double*, double, double, double*)>& apply_op,
                         const std::function<bem_status(const double*, double*)>& precond, int& iters,
-                        double& resid) {
+                        double& resid, cudaStream_t st) {
     using C = std::complex<double>;
-    cudaStream_t st = ctx->st;
     const size_t vs = (size_t)2 * Np * R;
     const int M = GM_M;
     double* V = ctx->d_gmV;
@@ -493,7 +506,7 @@ bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(hh, h1, sizeof(double) * hblock, cudaMemcpyDeviceToHost, st));
             int it_flags = 0;
-            CK(cudaMemcpyAsync(&it_flags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(&it_flags, F.flags ? F.flags : ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             ++iters;
             if (it_flags & bem::FLAG_TIMEOUT)
@@ -603,15 +616,24 @@ bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double
 // Factor + solve.  D64 (planar, ld = Np) holds the operator; Y (N x R, interleaved)
 // the right-hand sides; the solution lands in d_X.  mixed: TF32 LU of the FP32
 // copy + FP64 refinement against D64; plain: FP64 LU of D64 (destroyed).
+// phase (mixed path only): 1 = factor only (on st; the slot's ev_lu marks the end),
+// 2 = solve only, on stream ss, after the slot's ev_lu; 3 = both on st.
 bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
                             double* resid_out, double* t_lu, double* t_solve,
-                            const std::function<bem_status()>& after_lu = nullptr) {
+                            const std::function<bem_status()>& after_lu = nullptr, int phase = 3,
+                            cudaStream_t ss = nullptr) {
     cudaStream_t st = ctx->st;
+    if (!mixed) phase = 3;
+    const bool do_factor = (phase & 1) != 0, do_solve = (phase & 2) != 0;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
-    CK(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), st));
+    int* const flags = mixed ? F.flags : ctx->d_flags;
     const size_t nr2 = (size_t)2 * Np * R;
-    CK(cudaEventRecord(ctx->ev[2], st));
+    if (do_factor) {
+        CK(cudaMemsetAsync(flags, 0, sizeof(int), st));
+        CK(cudaEventRecord(ctx->ev[2], st));
+        if (mixed) CK(cudaEventRecord(F.ev_lu0, st));
+    }
     int iters = 0;
     double resid = 0.0;
     if (!mixed) {
@@ -630,8 +652,12 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
     } else {
         CMat<float> A{F.D32r, F.D32i, Np};
         bool tc = bem::tc_gemm_supported(ctx->device) != 0;
-        int rc_lu;
-        if (tc) {
+        int rc_lu = 0;
+        if (!do_factor) {
+            // the LU ran earlier on st: the solves follow it on their own stream
+            st = ss;
+            CK(cudaStreamWaitEvent(st, F.ev_lu, 0));
+        } else if (tc) {
             const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->ev_rest, ctx->su, ctx->ev_ucol,
                                     ctx->lu_reserve_sms,
                                     ctx->lu_rest_tiles,
@@ -643,13 +669,13 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2,
                                     ctx->d_pairT};
             if (ls.timeline) {
-                rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i, ctx->d_wl32,
-                                                     ctx->d_wut32, ctx->d_flags);
+                rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, ctx->d_wl32,
+                                                     ctx->d_wut32, flags);
             } else {
                 // The ~320 launches and 128 cross-stream event edges of one factorization are
                 // captured once per slot into a CUDA graph and replayed, which removes the host
                 // enqueue work (tensor-map encodes) and most launch gaps of the panel chain.
-                LuGraph& g = ctx->lu_graph[&F == &ctx->fs[1] ? 1 : 0];
+                LuGraph& g = ctx->lu_graph[&F - ctx->fs];
                 if (!g.exec || g.A != A.re || g.Np != Np || g.reserve != ctx->lu_reserve_sms ||
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
                     g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
@@ -661,10 +687,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     cudaGraph_t graph = nullptr;
                     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
                     const bool paired = ctx->lu_pair_update && ls.panel_tail && ls.ucol_own;
-                    rc_lu = paired ? bem::lu_factor_f32_paired(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i,
-                                                               ctx->d_wl32, ctx->d_wut32, ctx->d_flags)
-                                   : bem::lu_factor_f32_lookahead(st, ls, Np, A, ctx->d_inv32r, ctx->d_inv32i,
-                                                                  ctx->d_wl32, ctx->d_wut32, ctx->d_flags);
+                    rc_lu = paired ? bem::lu_factor_f32_paired(st, ls, Np, A, F.inv32r, F.inv32i,
+                                                               ctx->d_wl32, ctx->d_wut32, flags)
+                                   : bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i,
+                                                                  ctx->d_wl32, ctx->d_wut32, flags);
                     const cudaError_t ec = cudaStreamEndCapture(st, &graph);
                     if (rc_lu == 0 && ec == cudaSuccess) {
                         const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
@@ -697,8 +723,13 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         }
         if (rc_lu != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update: TMA descriptor setup failed");
         CK(cudaGetLastError());
-        CK(cudaEventRecord(ctx->ev[3], st));
-        if (after_lu) {
+        if (do_factor) {
+            CK(cudaEventRecord(ctx->ev[3], st));
+            CK(cudaEventRecord(F.ev_lu, st));
+            if (!do_solve) return BEM_OK;  // its flags are read by the solve phase
+        }
+        CK(cudaEventRecord(F.ev_sv0, st));
+        if (after_lu && do_factor) {
             // work that should overlap the solves rather than the factorization
             const bem_status sa = after_lu();
             if (sa != BEM_OK) return sa;
@@ -732,8 +763,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         auto precond = [&](const double* v, double* z) -> bem_status {
             bem::launch_to_f32(st, nr2, v, ctx->d_X32);
             ctx->solve_epoch += 2;
-            if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
-                                  ctx->solve_epoch - 1, ctx->d_flags, ctx->test_wait_skew, ctx->test_wait_ns))
+            if (bem::lu_solve_f32(st, Np, A, F.inv32r, F.inv32i, R, ctx->d_X32, ctx->d_ready,
+                                  ctx->solve_epoch - 1, flags, ctx->test_wait_skew, ctx->test_wait_ns))
                 return fail(ctx, BEM_ERR_CUDA, "triangular-solve launch failed");
             bem::launch_f32_to_f64(st, nr2, ctx->d_X32, z);
             return BEM_OK;
@@ -742,7 +773,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         CK(cudaMemcpyAsync(ctx->d_Rr, F.Y, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice, st));
         bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
         auto gmres = [&]() -> bem_status {
-            const bem_status gs = refine_gmres(ctx, F, N, Np, R, tol, max_iter, apply_op, precond, iters, resid);
+            const bem_status gs = refine_gmres(ctx, F, N, Np, R, tol, max_iter, apply_op, precond, iters, resid, st);
             if (gs != BEM_OK) {
                 if (iters_out) *iters_out = iters;
                 if (resid_out) *resid_out = resid;
@@ -762,8 +793,8 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             for (;;) {
                 bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
                 ctx->solve_epoch += 2;
-                if (bem::lu_solve_f32(st, Np, A, ctx->d_inv32r, ctx->d_inv32i, R, ctx->d_X32, ctx->d_ready,
-                                      ctx->solve_epoch - 1, ctx->d_flags, ctx->test_wait_skew, ctx->test_wait_ns))
+                if (bem::lu_solve_f32(st, Np, A, F.inv32r, F.inv32i, R, ctx->d_X32, ctx->d_ready,
+                                      ctx->solve_epoch - 1, flags, ctx->test_wait_skew, ctx->test_wait_ns))
                     return fail(ctx, BEM_ERR_CUDA, "cooperative triangular-solve launch failed");
                 bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
                 CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
@@ -775,7 +806,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 CK(cudaMemcpyAsync(hn.data(), ctx->d_norms, sizeof(unsigned long long) * 2 * R,
                                    cudaMemcpyDeviceToHost, st));
                 int sweep_flags = 0;
-                CK(cudaMemcpyAsync(&sweep_flags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaMemcpyAsync(&sweep_flags, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
                 ++iters;
                 // an expired device wait leaves this sweep's solve unfinished: report it as the
@@ -814,9 +845,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             }
         }
         CK(cudaEventRecord(ctx->ev[4], st));
+        CK(cudaEventRecord(F.ev_sv1, st));
     }
     int hflags = 0;
-    CK(cudaMemcpyAsync(&hflags, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (mixed && ctx->lu_tl_armed && ctx->lu_tl.size() >= (size_t)6 * (Np / 128)) {
         ctx->lu_tl_armed = false;
@@ -831,10 +863,17 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
         cudaGetLastError();  // an unrecorded event only leaves a NaN
     }
     float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
-    *t_lu += ms;
-    cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
-    *t_solve += ms;
+    if (mixed) {
+        cudaEventElapsedTime(&ms, F.ev_lu0, F.ev_lu);
+        *t_lu += ms;
+        cudaEventElapsedTime(&ms, F.ev_sv0, F.ev_sv1);
+        *t_solve += ms;
+    } else {
+        cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+        *t_lu += ms;
+        cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+        *t_solve += ms;
+    }
     if (iters_out) *iters_out = iters;
     if (resid_out) *resid_out = resid;
     if (hflags & bem::FLAG_TIMEOUT)
@@ -936,7 +975,9 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaEventCreate(&ctx->ev_call));
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
     CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
+    CK(cudaStreamCreateWithPriority(&ctx->ss, cudaStreamNonBlocking, prio_hi));
     for (FreqState& F : ctx->fs) {
+        for (cudaEvent_t* e : {&F.ev_lu0, &F.ev_lu, &F.ev_sv0, &F.ev_sv1}) CK(cudaEventCreate(e));
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&F.ev_free, cudaEventDisableTiming));
         for (auto& ev : F.ev_t) CK(cudaEventCreate(&ev));
@@ -958,10 +999,13 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->su) cudaStreamSynchronize(ctx->su);
     if (ctx->sq) cudaStreamSynchronize(ctx->sq);
     if (ctx->sr) cudaStreamSynchronize(ctx->sr);
+    if (ctx->ss) cudaStreamSynchronize(ctx->ss);
     for (FreqState& F : ctx->fs) {
-        for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5})
+        for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5, F.ev_lu0,
+                              F.ev_lu, F.ev_sv0, F.ev_sv1})
             if (e) cudaEventDestroy(e);
     }
+    if (ctx->ss) cudaStreamDestroy(ctx->ss);
     if (ctx->sa) cudaStreamDestroy(ctx->sa);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -1236,6 +1280,9 @@ bem_status ensure_slot(bem_ctx* ctx, FreqState& F, bool mixed) {
         DA(F.Dlo, (size_t)N * Np);
         DA(F.Xdf, (size_t)N * R);
         DA(F.Bm32, (size_t)2 * N * R);
+        DA(F.inv32r, (size_t)(Np / 128) * 2 * 128 * 128);
+        DA(F.inv32i, (size_t)(Np / 128) * 2 * 128 * 128);
+        DA(F.flags, 1);
     }
     if (&F != &ctx->fs[0])  // radiation columns of B (set once by bem_setup)
         CK(cudaMemcpyAsync(F.Bm, ctx->fs[0].Bm, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice,
@@ -1293,7 +1340,7 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
     bem::SurArgs sa = {};
     if (F.sur_used) {
         DA(F.Ws32, (size_t)N * Np);
-        DA(F.sur_stats, 4);
+        DA(F.sur_stats, 5);
         bem::MlpTcRef ref;
         if (bem::mlp_tc_ref(ctx->sur, &ref) != 0)
             return fail(ctx, BEM_ERR_CUDA, std::string("surrogate: ") + bem_mlp_last_error(ctx->sur));
@@ -1314,8 +1361,8 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
         sa.judge_seed = (unsigned)(kb ^ (kb >> 32));
         sa.ws32 = F.Ws32;
         sa.stats = F.sur_stats;
-        sa.gflags = ctx->d_flags;
-        CK(cudaMemsetAsync(F.sur_stats, 0, sizeof(unsigned long long) * 4, st));
+        sa.gflags = reinterpret_cast<int*>(F.sur_stats + 4);
+        CK(cudaMemsetAsync(F.sur_stats, 0, sizeof(unsigned long long) * 5, st));
     }
     CK(cudaEventRecord(F.ev_t[2], st));
     if (F.sur_used) {
@@ -1373,10 +1420,12 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
     if (s != BEM_OK) return s;
     const bool pipe = mixed && n_freq > 1;
-    s = ensure_slot(ctx, ctx->fs[0], mixed);
-    if (s != BEM_OK) return s;
-    if (pipe) {
-        s = ensure_slot(ctx, ctx->fs[1], mixed);
+    // split: the LU of frequency f + 1 (stream st) runs beside the refinement of f (stream
+    // ss) while f + 2 is assembled (stream sa): three frequency slots
+    const bool split = pipe && ctx->asm_overlap && ctx->lu_overlap;
+    const int nslots = split ? 3 : pipe ? 2 : 1;
+    for (int k = 0; k < nslots; ++k) {
+        s = ensure_slot(ctx, ctx->fs[k], mixed);
         if (s != BEM_OK) return s;
     }
     if (mixed && !ctx->rs_df) {
@@ -1392,10 +1441,12 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         ctx->rs_df = true;
     }
     cudaStream_t sa = pipe ? ctx->sa : st;
+    cudaStream_t so = split ? ctx->ss : st;  // refinement and post-processing
     CK(cudaEventRecord(ctx->ev_call, st));
     ctx->lu_tl_armed = true;  // the timeline (if enabled) follows this call's first LU
     if (pipe) CK(cudaStreamWaitEvent(sa, ctx->ev_call, 0));  // assembly starts after the work queued so far
-    auto slot = [&](int f) -> FreqState& { return ctx->fs[pipe ? (f & 1) : 0]; };
+    if (split) CK(cudaStreamWaitEvent(so, ctx->ev_call, 0));
+    auto slot = [&](int f) -> FreqState& { return ctx->fs[f % nslots]; };
     auto enqueue_assembly = [&](int f) -> bem_status {
         FreqState& F = slot(f);
         if (pipe) CK(cudaStreamWaitEvent(sa, F.ev_free, 0));
@@ -1404,14 +1455,37 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     const int nout = 36 + 12 * NB;
     std::vector<double> post(2 * (size_t)nout);
     std::vector<int> sur_redo;  // strict surrogate mode: frequencies whose judged error exceeded the tolerance
+    auto sync_all = [&]() {
+        cudaStreamSynchronize(sa);
+        cudaStreamSynchronize(st);
+        if (split) cudaStreamSynchronize(so);
+    };
+    double t_lu_next = 0, t_unused = 0;
+    // factor of frequency g, queued on st after its assembly (split schedule)
+    auto enqueue_factor = [&](int g) -> bem_status {
+        FreqState& G = slot(g);
+        CK(cudaStreamWaitEvent(st, G.ev_asm, 0));
+        return factor_and_solve(ctx, G, N, Np, R, mixed, tol, ctx->refine_max, nullptr, nullptr, &t_lu_next,
+                                &t_unused, nullptr, 1);
+    };
     if (n_freq > 0) {
         s = enqueue_assembly(0);
         if (s != BEM_OK) return s;
+        if (split) {
+            s = enqueue_factor(0);
+            if (s == BEM_OK && n_freq > 1) s = enqueue_assembly(1);
+            if (s != BEM_OK) { sync_all(); return s; }
+        }
     }
     for (int f = 0; f < n_freq; ++f) {
         FreqState& F = slot(f);
         const double Om = omega[f];
-        if (pipe && ctx->asm_overlap && f + 1 < n_freq) {
+        if (split) {
+            if (f + 2 < n_freq) {
+                s = enqueue_assembly(f + 2);  // two ahead: overlaps the LU of f + 1 and the solves of f
+                if (s != BEM_OK) { sync_all(); return s; }
+            }
+        } else if (pipe && ctx->asm_overlap && f + 1 < n_freq) {
             s = enqueue_assembly(f + 1);  // overlaps this frequency's LU and solve
             if (s != BEM_OK) return s;
         } else if (!pipe && f > 0) {
@@ -1430,22 +1504,35 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
                 return enqueue_assembly(f + 1);
             };
         const double K = F.K;  // set by this frequency's assemble()
-        if (pipe) CK(cudaStreamWaitEvent(st, F.ev_asm, 0));
         int iters = 0;
         double resid = 0;
         double t_lu = 0, t_sv = 0;
-        ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
-        s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, ctx->refine_max, &iters, &resid, &t_lu, &t_sv, next_asm);
+        if (split) {
+            // the LU of f was queued one iteration earlier; queue the LU of f + 1 now, so that it
+            // runs while this thread drives the refinement of f
+            if (f + 1 < n_freq) {
+                s = enqueue_factor(f + 1);
+                if (s != BEM_OK) { sync_all(); return s; }
+            }
+            ctx->resid_mode = K != 0.0 ? 3 : 2;
+            s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, ctx->refine_max, &iters, &resid, &t_lu, &t_sv,
+                                 nullptr, 2, so);
+        } else {
+            if (pipe) CK(cudaStreamWaitEvent(st, F.ev_asm, 0));
+            ctx->resid_mode = mixed ? (K != 0.0 ? 3 : 2) : 0;
+            s = factor_and_solve(ctx, F, N, Np, R, mixed, tol, ctx->refine_max, &iters, &resid, &t_lu, &t_sv,
+                                 next_asm);
+        }
         ctx->resid_mode = 0;
         if (s != BEM_OK) {
-            if (pipe) cudaStreamSynchronize(sa);
+            if (pipe) sync_all();
             return s;
         }
-        CK(cudaEventRecord(ctx->ev[6], st));
+        CK(cudaEventRecord(ctx->ev[6], so));
         // hull panels only: Phi_J, Phi_S, Phi_I are cut to NPA rows (:452-457)
-        bem::launch_post(st, NPA, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
+        bem::launch_post(so, NPA, NB, R, ctx->d_X, ctx->d_Nk, ctx->d_area, F.phiI, F.dphiI, ctx->d_part, ctx->d_post);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(post.data(), ctx->d_post, post.size() * 8, cudaMemcpyDeviceToHost, so));
         // exterior outputs of this frequency (Hydrodynamic_Solver.cpp:489-505)
         const int NW = (int)(ctx->wave_pts.size() / 3), NK = ctx->n_kochin;
         const bool want_fs = out && (out->fs_rad || out->fs_diff) && NW > 0;
@@ -1469,31 +1556,35 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         if (want_fs) {
             if (ctx->wpts_dirty) {
                 CK(cudaMemcpyAsync(ctx->d_wpts, ctx->wave_pts.data(), ctx->wave_pts.size() * 8,
-                                   cudaMemcpyHostToDevice, st));
+                                   cudaMemcpyHostToDevice, so));
                 ctx->wpts_dirty = false;
             }
             bem::WaveArgs a = {};
             a.N = N; a.K = K; a.gq = ctx->d_gq; a.nq = ctx->d_nq;
-            bem::launch_fs_elevation(st, a, NPA, NW, ctx->d_wpts, ctx->d_rec, ctx->d_rn, Om, NB, ctx->d_Nk,
+            bem::launch_fs_elevation(so, a, NPA, NW, ctx->d_wpts, ctx->d_rec, ctx->d_rn, Om, NB, ctx->d_Nk,
                                      F.dphiI, ctx->d_X, ctx->d_ext);
             CK(cudaGetLastError());
             ext_fs.resize((size_t)2 * R * NW);
-            CK(cudaMemcpyAsync(ext_fs.data(), ctx->d_ext, ext_fs.size() * 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(ext_fs.data(), ctx->d_ext, ext_fs.size() * 8, cudaMemcpyDeviceToHost, so));
         }
         if (want_k) {
-            bem::launch_kochin(st, N, NPA, NK, NB, K, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_Nk, F.dphiI,
+            bem::launch_kochin(so, N, NPA, NK, NB, K, ctx->d_cen, ctx->d_nrm, ctx->d_area, ctx->d_Nk, F.dphiI,
                                ctx->d_X, ctx->d_ext);
             CK(cudaGetLastError());
             ext_k.resize((size_t)2 * R * NK);
-            CK(cudaMemcpyAsync(ext_k.data(), ctx->d_ext, ext_k.size() * 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(ext_k.data(), ctx->d_ext, ext_k.size() * 8, cudaMemcpyDeviceToHost, so));
         }
-        CK(cudaEventRecord(ctx->ev[7], st));
-        CK(cudaEventRecord(F.ev_free, st));
-        CK(cudaStreamSynchronize(st));
+        CK(cudaEventRecord(ctx->ev[7], so));
+        CK(cudaEventRecord(F.ev_free, so));
+        CK(cudaStreamSynchronize(so));
         if (F.sur_used) {
             // the surrogate assembly's counts and judged error for this frequency
-            unsigned long long hs[4] = {0, 0, 0, 0};
+            unsigned long long hs[5] = {0, 0, 0, 0, 0};
             CK(cudaMemcpy(hs, F.sur_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+            int sflags;
+            memcpy(&sflags, &hs[4], sizeof(int));
+            if (sflags & bem::FLAG_TIMEOUT)
+                return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the surrogate assembly expired");
             const uint32_t eb = (uint32_t)hs[3];
             float err;
             memcpy(&err, &eb, 4);
@@ -2193,6 +2284,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         ctx->lu_split_panel = (int)value;
         return BEM_OK;
     }
+    if (k == "lu_overlap") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_overlap must be 0 or 1");
+        ctx->lu_overlap = (int)value;
+        return BEM_OK;
+    }
     if (k == "asm_overlap") {
         if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "asm_overlap must be 0 or 1");
         ctx->asm_overlap = (int)value;
@@ -2223,18 +2319,17 @@ bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* m
     if (!ctx->ready || ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_autotune before bem_setup");
     if (n_freq < 2 || !omega) return fail(ctx, BEM_ERR_ARG, "bem_autotune needs at least 2 sample frequencies");
     struct Setting {
-        int asm_reserve, cluster, block, pair;
+        int asm_reserve, lu_overlap;
     };
-    // the default first; the others move one knob at a time
-    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_cluster_inverse, ctx->lu_block_inverse, ctx->lu_pair_update},
-                            {56, 8, 2, 1}, {64, 8, 2, 1}, {80, 8, 2, 1}, {88, 8, 2, 1}, {72, 4, 1, 1}, {72, 8, 2, 0}};
+    // the default first; then reserves with the LU beside the previous frequency's
+    // refinement, and two without that overlap
+    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 1}, {48, 1}, {56, 1}, {64, 1}, {80, 1},
+                            {72, 0}};
     const int ng = (int)(sizeof(grid) / sizeof(grid[0]));
     std::vector<double> best(ng, 1e300);
     auto apply = [&](const Setting& g) {
         ctx->asm_reserve = g.asm_reserve;
-        ctx->lu_cluster_inverse = g.cluster;
-        ctx->lu_block_inverse = g.block;
-        ctx->lu_pair_update = g.pair;
+        ctx->lu_overlap = g.lu_overlap;
     };
     bem_result none;
     memset(&none, 0, sizeof(none));
@@ -2265,9 +2360,8 @@ bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* m
         std::string r;
         for (int g = 0; g < ng; ++g) {
             char line[160];
-            snprintf(line, sizeof(line), "%sasm_reserve_sms=%d lu_cluster_inverse=%d lu_block_inverse=%d "
-                     "lu_pair_update=%d: %.3f ms/frequency\n", g == pick ? "* " : "  ", grid[g].asm_reserve,
-                     grid[g].cluster, grid[g].block, grid[g].pair, best[g]);
+            snprintf(line, sizeof(line), "%sasm_reserve_sms=%d lu_overlap=%d: %.3f ms/frequency\n",
+                     g == pick ? "* " : "  ", grid[g].asm_reserve, grid[g].lu_overlap, best[g]);
             r += line;
         }
         const size_t n = std::min(r.size(), (size_t)report_len - 1);

@@ -319,6 +319,10 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
+ *   "lu_overlap"      with asm_overlap = 1: 1 = the LU of frequency f + 1 runs beside the
+ *                     refinement of f (its own stream; each frequency slot keeps its own
+ *                     block inverses and flags; default), 0 = LU and refinement of one
+ *                     frequency after the other on one stream.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
  *                     LU when it overlaps it (default 72).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
@@ -335,9 +339,9 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Autotuner of the pipelined mixed solve: times bem_solve (BEM_MIXED, outputs skipped)
  * on the n_freq >= 2 sample frequencies for each of a small grid of the schedule knobs
- * above (the current setting, assembly reserves of 56-88 SMs, the 4-CTA blocked and
- * the 8-CTA pivot-warp block inverse, one or two elimination steps per pass), every
- * setting twice in alternation, and keeps the fastest on the context.  ms_per_freq
+ * above (the current setting; assembly reserves of 40, 48, 56, 64 and 80 SMs with
+ * lu_overlap = 1; a reserve of 72 with lu_overlap = 0), every setting twice in
+ * alternation, and keeps the fastest on the context.  ms_per_freq
  * (optional) receives its time per frequency; report (optional, report_len bytes) one
  * line per setting, the chosen one marked '*'.  Needs bem_setup.  The project's
  * replacement for hand-picked launch shapes: the best split of the GPU between the
