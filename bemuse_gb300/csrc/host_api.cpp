@@ -187,7 +187,7 @@ struct bem_ctx {
     int lu_pair_update = 1;                     // trailing updates of two steps per pass
     // pipelined mixed solves: 1 = the next frequency's assembly overlaps this LU and solve,
     // 0 = only the solve; SMs kept free of assembly CTAs, assembly CTAs allowed per SM
-    int asm_overlap = 1, asm_reserve = 72, asm_per_sm = 3;
+    int asm_overlap = 1, asm_reserve = 56, asm_per_sm = 3;
     int asm_split = bem::WAVE_SPLIT;            // work items per receiver row of the assembly kernel
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
@@ -2309,6 +2309,22 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         ctx->asm_per_sm = (int)value;
         return BEM_OK;
     }
+    if (k == "solve_priority") {
+        // priority of the refinement stream: 0 highest (default), 1 that of the LU stream
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "solve_priority must be 0 or 1");
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        const int want = value == 0 ? hi : std::max(hi, lo - 1);
+        int cur = 0;
+        CK(cudaStreamGetPriority(ctx->ss, &cur));
+        if (cur != want) {
+            CK(cudaStreamSynchronize(ctx->ss));
+            CK(cudaStreamDestroy(ctx->ss));
+            ctx->ss = nullptr;
+            CK(cudaStreamCreateWithPriority(&ctx->ss, cudaStreamNonBlocking, want));
+        }
+        return BEM_OK;
+    }
     return fail(ctx, BEM_ERR_ARG, "unknown tuning key: " + k);
 }
 
@@ -2323,7 +2339,7 @@ bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* m
     };
     // the default first; then reserves with the LU beside the previous frequency's
     // refinement, and two without that overlap
-    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 1}, {48, 1}, {56, 1}, {64, 1}, {80, 1},
+    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 1}, {48, 1}, {64, 1}, {72, 1}, {80, 1},
                             {72, 0}};
     const int ng = (int)(sizeof(grid) / sizeof(grid[0]));
     std::vector<double> best(ng, 1e300);

@@ -324,8 +324,10 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     block inverses and flags; default), 0 = LU and refinement of one
  *                     frequency after the other on one stream.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
- *                     LU when it overlaps it (default 72).
+ *                     LU and the refinement when it overlaps them (default 56).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
+ *   "solve_priority"  stream priority of the refinement beside the LU: 0 = highest
+ *                     (default), 1 = that of the LU's main stream.
  *   "asm_split"       work items per receiver row of the persistent assembly kernel
  *                     (1..64, default 4; finer items measured slower).
  *   "refine_max_solves" preconditioner solves the mixed path's refinement may use
@@ -339,7 +341,7 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 
 /* Autotuner of the pipelined mixed solve: times bem_solve (BEM_MIXED, outputs skipped)
  * on the n_freq >= 2 sample frequencies for each of a small grid of the schedule knobs
- * above (the current setting; assembly reserves of 40, 48, 56, 64 and 80 SMs with
+ * above (the current setting; assembly reserves of 40, 48, 64, 72 and 80 SMs with
  * lu_overlap = 1; a reserve of 72 with lu_overlap = 0), every setting twice in
  * alternation, and keeps the fastest on the context.  ms_per_freq
  * (optional) receives its time per frequency; report (optional, report_len bytes) one
