@@ -334,10 +334,13 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
                                         float t3, float& Gr, float& Ghr, float& Gv) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
-    float dd = sqrtf(fmaf(hh, hh, vv * vv));
-    // approximate reciprocals (about an ulp): they scale terms whose FP32 rounding is
-    // of the same size, while dd itself stays correctly rounded
-    float inv_d = __fdividef(1.0f, dd);
+    // d from the reciprocal square root and one Newton step (within about an ulp);
+    // 1/d is the reciprocal square root itself.  Approximate reciprocals (about an ulp)
+    // scale terms whose FP32 rounding is of the same size.
+    const float d2s = fmaf(hh, hh, vv * vv);
+    const float inv_d = rsqrtf(d2s);
+    float dd = d2s * inv_d;
+    dd = fmaf(fmaf(-dd, dd, d2s), 0.5f * inv_d, dd);
     float alpha = -vv * inv_d;
     float beta = hh * inv_d;
     float rho = __fdividef(dd, 1.0f + dd);
@@ -364,7 +367,9 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     PS -= 2.0f * beta;
     PS = fmaf(2.0f * dd, ev, PS);
     PS -= hh;
-    float QS = expf(-dd) * (1.0f - beta);
+    // e^-d with the fast exponential: its error is relative to |d| e^-d, small beside the
+    // other terms at every d
+    float QS = __expf(-dd) * (1.0f - beta);
     QS *= 1.0f + dd * inv_1d3;
     float a2 = horner32(P.dA, 10, u), b2 = horner32(P.dB, 10, u), c2 = horner32(P.dC, 6, u);
     float RS = beta * a2 - (1.0f - alpha) * b2;
