@@ -74,19 +74,23 @@ def test_non_finite_frequency_is_rejected(bg, orc, bad):
     assert normwise(got["A"][0], ref["A"][0]) < 1e-6
 
 
-def test_refinement_out_of_solves_is_numeric_failure(bg, orc):
+@pytest.mark.parametrize("omegas", [[0.8], [0.8, 1.0, 1.3, 1.7]])
+def test_refinement_out_of_solves_is_numeric_failure(bg, orc, omegas):
+    # with several frequencies the failure comes while the next frequency's LU and the
+    # one after's assembly are in flight on their own streams
     s = _solver(bg, bg.MIXED)
     s.Setup(cases.lib_cylinder(cases.CYL_SMALL))
     s.set_tuning("refine_max_solves", 0)
     with pytest.raises(bg.BEMError) as ex:
-        s.solve_omegas([0.8])
+        s.solve_omegas(omegas)
     assert _status(ex) == BEM_ERR_NUMERIC and "did not reach the tolerance" in str(ex.value)
     s.set_tuning("refine_max_solves", 60)
     m, _ = cases.oracle_cylinder(orc, cases.CYL_SMALL)
-    ref = orc.solve(m, [0.8], [0.0], M=s.M_ij, C=s.C_ij)
-    got = s.solve_omegas([0.8])
-    assert got["residual"][0] <= 1e-12
-    assert normwise(got["A"][0], ref["A"][0]) < 1e-6
+    ref = orc.solve(m, omegas, [0.0], M=s.M_ij, C=s.C_ij)
+    got = s.solve_omegas(omegas)
+    assert np.all(got["residual"] <= 1e-12)
+    for f in range(len(omegas)):
+        assert normwise(got["A"][f], ref["A"][f]) < 1e-6
     with pytest.raises(bg.BEMError):
         s.set_tuning("refine_max_solves", -1)
 
@@ -105,7 +109,7 @@ def test_expired_device_wait_is_reported_and_context_survives(bg, orc, gmres):
     s.set_tuning("test_wait_ms", 1.0)
     s.set_tuning("test_wait_skew", 1)
     with pytest.raises(bg.BEMError) as ex:
-        s.solve_omegas([0.8])
+        s.solve_omegas([0.8, 1.1, 1.5])
     assert _status(ex) == BEM_ERR_CUDA and "expired" in str(ex.value)
     s.set_tuning("test_wait_skew", 0)
     s.set_tuning("test_wait_ms", 2000.0)
