@@ -349,7 +349,7 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     float d3 = d2 * dd;
     float inv_1d3 = __fdividef(1.0f, 1.0f + d3);
     float dmv = dd - vv;
-    float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
+    float PP = __logf(0.5f * dmv) + EUL - 2.0f * d2;  // fast log: ~4e-7 absolute, scaled by e^v / (1 + d^3)
     PP = fmaf(PP, ev, d2 - vv);
     float A = horner32(P.A, 10, u), B = horner32(P.B, 10, u);
     float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
