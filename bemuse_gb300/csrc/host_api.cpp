@@ -2310,11 +2310,13 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "solve_priority") {
-        // priority of the refinement stream: 0 highest (default), 1 that of the LU stream
-        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "solve_priority must be 0 or 1");
+        // priority of the refinement stream: 0 highest (default), 1 that of the LU stream,
+        // 2 the lowest (that of the assembly)
+        if (!(value == 0 || value == 1 || value == 2))
+            return fail(ctx, BEM_ERR_ARG, "solve_priority must be 0, 1 or 2");
         int lo = 0, hi = 0;
         CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        const int want = value == 0 ? hi : std::max(hi, lo - 1);
+        const int want = value == 0 ? hi : value == 1 ? std::max(hi, lo - 1) : lo;
         int cur = 0;
         CK(cudaStreamGetPriority(ctx->ss, &cur));
         if (cur != want) {
