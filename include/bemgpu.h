@@ -327,7 +327,7 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     LU and the refinement when it overlaps them (default 56).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
  *   "solve_priority"  stream priority of the refinement beside the LU: 0 = highest
- *                     (default), 1 = that of the LU's main stream.
+ *                     (default), 1 = that of the LU's main stream, 2 = the lowest.
  *   "asm_split"       work items per receiver row of the persistent assembly kernel
  *                     (1..64, default 4; finer items measured slower).
  *   "refine_max_solves" preconditioner solves the mixed path's refinement may use
