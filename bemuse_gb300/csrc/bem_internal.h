@@ -179,6 +179,8 @@ struct LuStreams {
     cudaStream_t rest;      // paired schedule: trailing updates of two steps at a time
     cudaEvent_t ev_panel2, ev_cross2;
     float* pair_t;          // 4 (n / 256) 128 128 floats: transposed pair blocks of the pair fold
+    int pdl;                // 1: each block inverse is launched as a programmatic dependent of the
+                            // corner update before it (its CTAs start while the update finishes)
 };
 // wl2: two [2][n][128] buffers (4 n 128 floats); wut2: the same plus the transposed
 // diagonal-block inverses, [n/128][2][128][128] (4 n 128 + 256 n floats).  The

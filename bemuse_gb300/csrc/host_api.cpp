@@ -70,7 +70,8 @@ struct FreqState {
 struct LuGraph {
     cudaGraphExec_t exec = nullptr;
     const float* A = nullptr;
-    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1, blocked = -1, pair = -1;
+    int Np = 0, reserve = -1, rest = -1, cluster = -1, ucol = -1, ucol_ctas = -1, split = -1, blocked = -1, pair = -1,
+        pdl = -1;
     long long launches = 0;
 };
 
@@ -179,6 +180,7 @@ struct bem_ctx {
     std::vector<cudaEvent_t> lu_tl;             // LU timeline events (empty = off)
     int lu_reserve_sms = 32;                    // SMs the persistent trailing update leaves to the panel chain
     int lu_rest_tiles = 4;                      // tiles per short-lived trailing-update CTA
+    int lu_pdl = 1;                             // block inverses as programmatic dependents
     int lu_cluster_inverse = 8;                 // CTAs per block inverse (2, 4, 8: a cluster; 1: one CTA)
     int lu_ucol_stream = 1;                     // U D^-1 transforms on their own stream (0: panel stream)
     int lu_ucol_ctas = 0;                       // CTAs per U D^-1 transform (0: one per tile)
@@ -667,7 +669,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
                                     ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
                                     ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2,
-                                    ctx->d_pairT};
+                                    ctx->d_pairT, ctx->lu_pdl};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, flags);
@@ -680,7 +682,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
                     g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
                     g.split != ctx->lu_split_panel || g.blocked != ctx->lu_block_inverse ||
-                    g.pair != ctx->lu_pair_update) {
+                    g.pair != ctx->lu_pair_update || g.pdl != ctx->lu_pdl) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -710,6 +712,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.split = ctx->lu_split_panel;
                     g.blocked = ctx->lu_block_inverse;
                     g.pair = ctx->lu_pair_update;
+                    g.pdl = ctx->lu_pdl;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));
@@ -2219,6 +2222,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "lu_reserve_sms") {
         if (!(value >= 0 && value <= 144)) return fail(ctx, BEM_ERR_ARG, "lu_reserve_sms must be in [0, 144]");
         ctx->lu_reserve_sms = (int)value;
+        return BEM_OK;
+    }
+    if (k == "lu_pdl") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_pdl must be 0 or 1");
+        ctx->lu_pdl = (int)value;
         return BEM_OK;
     }
     if (k == "lu_rest_tiles") {

@@ -318,6 +318,9 @@ __device__ __forceinline__ bool ic_wait(uint32_t bar, unsigned long long deadlin
 template <int CL>
 __global__ void __launch_bounds__(IC_THREADS, 1)
     k_inv128c(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    // launched as a programmatic dependent of the update that produced this block: wait
+    // for its completion before reading A (returns at once for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 ic_smem[];
@@ -496,6 +499,9 @@ constexpr int IB_SMEM = 128 * 64 * 16      // panel rows R, [128][4][16] float4 
 template <int CL>
 __global__ void __launch_bounds__(IC_THREADS, 1)
     k_inv128b(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    // launched as a programmatic dependent of the update that produced this block: wait
+    // for its completion before reading A (returns at once for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 ib_smem[];
@@ -738,6 +744,9 @@ constexpr int IL_SMEM = 128 * 64 * 16       // panel rows R, [128][4][16] float4
 template <int CL>
 __global__ void __launch_bounds__(IL_THREADS, 1)
     k_inv128l(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
+    // launched as a programmatic dependent of the update that produced this block: wait
+    // for its completion before reading A (returns at once for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 il_smem[];
@@ -1026,20 +1035,25 @@ __global__ void __launch_bounds__(IL_THREADS, 1)
 
 // One cluster of cl CTAs (2, 4 or 8) inverting the diagonal block at k0.
 static void inv128_cluster(cudaStream_t st, int cl, int blocked, int k0, CMat<float> A, float* invr, float* invi,
-                           float* dT, int* flags) {
+                           float* dT, int* flags, int pdl = 0) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
     cfg.blockDim = dim3(IC_THREADS);
     cfg.dynamicSmemBytes = blocked == 2 ? IL_SMEM : blocked ? IB_SMEM : IC_SMEM;
     if (blocked == 2) cfg.blockDim = dim3(IL_THREADS);
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = cl;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    // programmatic dependent launch: the inverse's CTAs may be scheduled once the kernel
+    // before it on this stream has signalled (griddepcontrol.launch_dependents); they wait
+    // for that kernel's completion and memory (griddepcontrol.wait) before reading A
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = pdl ? 2 : 1;
     if (blocked == 2) {
         switch (cl) {
             case 2: BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_inv128l<2>, k0, A, invr, invi, dT, flags)); break;
@@ -1282,7 +1296,7 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
     auto inverse = [&](int k) {
         const int k0 = k * NB;
         if (ls.cluster_inverse >= 2)
-            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags);
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags, ls.pdl);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
         mark(k - 1, 2, sp);
@@ -1403,7 +1417,7 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
     auto inverse = [&](int k) {
         const int k0 = k * NB;
         if (ls.cluster_inverse >= 2)
-            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags);
+            inv128_cluster(sp, ls.cluster_inverse, ls.block_inverse, k0, A, invr, invi, dTb(k), flags, ls.pdl);
         else
             BEM_LAUNCH(k_inv128<<<1, IV_THREADS, 0, sp>>>(k0, A, invr, invi, dTb(k), flags));
     };

@@ -119,6 +119,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const __grid_constant__ CUtensorMap mapL2r, const __grid_constant__ CUtensorMap mapL2i,
                 const __grid_constant__ CUtensorMap mapU2r, const __grid_constant__ CUtensorMap mapU2i,
                 const TcTiles a, int* gflags) {
+    // a kernel launched after this one as its programmatic dependent (the block inverse after
+    // the corner update) may be scheduled now; it waits for this grid's completion itself
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;  // 1024-byte aligned (128-byte swizzle atoms)
