@@ -25,7 +25,7 @@ bool tc_trailing_update(cudaStream_t st, int n, int k0, int nb, CMat<float> A, c
 bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* wl, const float* wut, int lr0,
                     int ur0, int Mt, int Nt, int max_ctas, int* flags, int lshape);
 bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
-            int count);
+            int count, int pdl = 0);
 bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int max_ctas, int* flags);
 bool tc_pair_fold(cudaStream_t st, int n, CMat<float> A, const float* T, int which, int* flags);
 bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
@@ -319,8 +319,10 @@ template <int CL>
 __global__ void __launch_bounds__(IC_THREADS, 1)
     k_inv128c(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
     // launched as a programmatic dependent of the update that produced this block: wait
-    // for its completion before reading A (returns at once for an ordinary launch)
+    // for its completion before reading A (returns at once for an ordinary launch); the
+    // first W21 tile after it may be scheduled now and waits for this grid in turn
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 ic_smem[];
@@ -500,8 +502,10 @@ template <int CL>
 __global__ void __launch_bounds__(IC_THREADS, 1)
     k_inv128b(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
     // launched as a programmatic dependent of the update that produced this block: wait
-    // for its completion before reading A (returns at once for an ordinary launch)
+    // for its completion before reading A (returns at once for an ordinary launch); the
+    // first W21 tile after it may be scheduled now and waits for this grid in turn
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 ib_smem[];
@@ -745,8 +749,10 @@ template <int CL>
 __global__ void __launch_bounds__(IL_THREADS, 1)
     k_inv128l(int k0, CMat<float> A, float* invr, float* invi, float* dT, int* flags) {
     // launched as a programmatic dependent of the update that produced this block: wait
-    // for its completion before reading A (returns at once for an ordinary launch)
+    // for its completion before reading A (returns at once for an ordinary launch); the
+    // first W21 tile after it may be scheduled now and waits for this grid in turn
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     constexpr int RPC = 128 / CL, RPT = RPC / 16;
     static_assert(CL == 2 || CL == 4 || CL == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ __align__(16) float4 il_smem[];
@@ -1306,8 +1312,8 @@ int lu_factor_f32_lookahead(cudaStream_t st, const LuStreams& ls, int n, CMat<fl
         const int k0 = k * NB, rem = n - k0 - NB;
         // W21 = A21 D^-1 on the tensor cores, into wl and over A21 (for the solves), and
         // U12^T into wut, for row / column tiles t0 .. t0 + count - 1 (count < 0: to the end)
-        auto w21_tiles = [&](cudaStream_t s, int t0, int count) {
-            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count);
+        auto w21_tiles = [&](cudaStream_t s, int t0, int count, int pdl = 0) {
+            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count, pdl);
         };
         auto tr_tiles = [&](cudaStream_t s, int t0, int count) {
             const int c0 = t0 * NB, cols = std::min(rem - c0, count < 0 ? rem : count * NB);
@@ -1425,8 +1431,8 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
     // waited for it): first W21 tile on sp, first U^T tile on sq, the rest on sq
     auto panel = [&](int k, cudaEvent_t ready) -> bool {
         const int k0 = k * NB, rem = n - k0 - NB;
-        auto w21_tiles = [&](cudaStream_t s, int t0, int count) {
-            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count);
+        auto w21_tiles = [&](cudaStream_t s, int t0, int count, int pdl = 0) {
+            return tc_w21(s, n, k0, A, dTb(k), wlb(k), flags, t0, count, pdl);
         };
         auto tr_tiles = [&](cudaStream_t s, int t0, int count) {
             const int c0 = t0 * NB, cols = std::min(rem - c0, count < 0 ? rem : count * NB);
@@ -1438,7 +1444,7 @@ int lu_factor_f32_paired(cudaStream_t st, const LuStreams& ls, int n, CMat<float
         cudaStreamWaitEvent(sq, ready, 0);
         tr_tiles(sq, 0, 1);
         cudaEventRecord(ls.ev_t0, sq);
-        if (!w21_tiles(sp, 0, 1)) return false;
+        if (!w21_tiles(sp, 0, 1, ls.pdl)) return false;
         cudaStreamWaitEvent(sp, ls.ev_t0, 0);
         cudaEventRecord(ls.ev_head, sp);
         cudaStreamWaitEvent(sq, ls.ev_head, 0);

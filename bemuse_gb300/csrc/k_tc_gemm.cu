@@ -195,6 +195,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    // launched as a programmatic dependent (the first W21 tile after the block inverse): the
+    // set-up above overlaps the inverse; its results are read only after this wait (a no-op
+    // for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
@@ -423,7 +427,7 @@ bool tc_update_rect(cudaStream_t st, int n, int k0, CMat<float> A, const float* 
 // and over A21 in A.  Each tile reads its A21 rows before it overwrites them.
 // Row tiles t0 .. t0 + count - 1 of A21 (count < 0: all from t0).
 bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, float* w, int* flags, int t0,
-            int count) {
+            int count, int pdl) {
     const int rem = n - k0 - 128;
     if (rem <= 0) return true;
     if (n % 128 || k0 % 128 || A.ld % 4) return false;
@@ -437,6 +441,22 @@ bool tc_w21(cudaStream_t st, int n, int k0, CMat<float> A, const float* dT, floa
     const int mt = std::min(rem / 128 - t0, count < 0 ? rem / 128 : count);
     if (t0 < 0 || mt <= 0) return true;
     const TcTiles a{k0 + 128 + 128 * t0, 0, mt, 1, 0, 0, 128 * t0, 0, 1, k0 + 128 + 128 * t0, k0, 1, 0, 0};
+    if (pdl) {
+        // a programmatic dependent of the kernel before it on this stream (the block inverse)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(tc_grid(mt, 0));
+        cfg.blockDim = dim3(NTHREADS);
+        cfg.dynamicSmemBytes = SMEM_BYTES;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_tc_update, mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i, mLr, mLi, mUr,
+                                      mUi, a, flags));
+        return cudaPeekAtLastError() == cudaSuccess;
+    }
     BEM_LAUNCH(k_tc_update<<<tc_grid(mt, 0), NTHREADS, SMEM_BYTES, st>>>(mLr, mLi, mUr, mUi, mCr, mCi, mC2r, mC2i,
                                                                         mLr, mLi, mUr, mUi, a, flags));
     return true;
@@ -582,7 +602,7 @@ int tc_probe(int device, int mode, int n, float* C, const float* Wa, const float
             case 0: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, nullptr, nullptr, 0, 0); break;
             case 1: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
             case 2: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 2, 1, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
-            case 3: ok = tc_w21(st, n, 0, A, dT, dW, flags, 0, -1); break;
+            case 3: ok = tc_w21(st, n, 0, A, dT, dW, flags, 0, -1, 0); break;
             case 4: ok = tc_ucol(st, n, n - 128, A, dT, 0, flags); break;
             default: ok = tc_pair_fold(st, n, A, dT, mode - 4, flags); break;
         }
