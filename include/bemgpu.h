@@ -316,6 +316,9 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *   "lu_split_panel"  1: only the first tile of each panel's W21 and U transpose runs on
  *                     the inverse chain, the rest on a second panel stream (default);
  *                     0: the whole panel on the panel stream.
+ *   "lu_pdl"          1: each block inverse of the tensor-core LU, and the first W21 tile
+ *                     after it, start as programmatic dependents of the kernel before them
+ *                     (default); 0: ordinary launches.
  *   "asm_overlap"     pipelined mixed solves: 1 = the next frequency's wave assembly
  *                     runs beside this frequency's LU and solves (default), 0 = beside
  *                     the solves only.
