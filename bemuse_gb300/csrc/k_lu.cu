@@ -30,7 +30,7 @@ bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int
 bool tc_pair_fold(cudaStream_t st, int n, CMat<float> A, const float* T, int which, int* flags);
 bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
                     int max_ctas, int* flags, const float* wl_a, const float* wut_a, int lr_a, int ur_a,
-                    const float* wl_b, const float* wut_b, int lr_b, int ur_b, int pdl = 0);
+                    const float* wl_b, const float* wut_b, int lr_b, int ur_b);
 
 template <typename T> __device__ __forceinline__ bool finite_(T x) { return isfinite(x); }
 

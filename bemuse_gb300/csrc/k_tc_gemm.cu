@@ -488,7 +488,7 @@ bool tc_ucol(cudaStream_t st, int n, int c0, CMat<float> A, const float* dT, int
 // dropped (see k_tc_update).
 bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, int Mt, int Nt, int lw, int lskip,
                     int max_ctas, int* flags, const float* wl_a, const float* wut_a, int lr_a, int ur_a,
-                    const float* wl_b, const float* wut_b, int lr_b, int ur_b, int pdl) {
+                    const float* wl_b, const float* wut_b, int lr_b, int ur_b) {
     if (Mt <= 0 || Nt <= 0) return true;
     if (n % 128 || row0 % 128 || col0 % 128 || lr_a % 128 || ur_a % 128 || A.ld % 4) return false;
     if (row0 + 128 * Mt > n || col0 + 128 * Nt > n || lr_a < 0 || ur_a < 0) return false;
@@ -512,22 +512,6 @@ bool tc_update_pair(cudaStream_t st, int n, CMat<float> A, int row0, int col0, i
         mL2r = mLr; mL2i = mLi; mU2r = mUr; mU2i = mUi;
     }
     const TcTiles a{lr_a, ur_a, Mt, Nt, lw, lskip, row0, col0, 0, 0, 0, npair, lr_b, ur_b};
-    if (pdl) {
-        // a programmatic dependent of the kernel before it on this stream
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(tc_grid(ntiles, max_ctas));
-        cfg.blockDim = dim3(NTHREADS);
-        cfg.dynamicSmemBytes = SMEM_BYTES;
-        cfg.stream = st;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        BEM_LAUNCH(cudaLaunchKernelEx(&cfg, k_tc_update, mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mL2r, mL2i, mU2r,
-                                      mU2i, a, flags));
-        return cudaPeekAtLastError() == cudaSuccess;
-    }
     BEM_LAUNCH(k_tc_update<<<tc_grid(ntiles, max_ctas), NTHREADS, SMEM_BYTES, st>>>(
         mLr, mLi, mUr, mUi, mCr, mCi, mCr, mCi, mL2r, mL2i, mU2r, mU2i, a, flags));
     return true;
@@ -615,9 +599,9 @@ int tc_probe(int device, int mode, int n, float* C, const float* Wa, const float
         const int mt = n / 128 - 1;
         bool ok = false;
         switch (mode) {
-            case 0: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, nullptr, nullptr, 0, 0, 0); break;
-            case 1: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0, 0); break;
-            case 2: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 2, 1, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0, 0); break;
+            case 0: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, nullptr, nullptr, 0, 0); break;
+            case 1: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 0, 0, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
+            case 2: ok = tc_update_pair(st, n, A, 128, 128, mt, mt, 2, 1, 0, flags, dWa, dUa, 0, 0, dWb, dUb, 0, 0); break;
             case 3: ok = tc_w21(st, n, 0, A, dT, dW, flags, 0, -1, 0); break;
             case 4: ok = tc_ucol(st, n, n - 128, A, dT, 0, flags); break;
             default: ok = tc_pair_fold(st, n, A, dT, mode - 4, flags); break;
