@@ -660,6 +660,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             st = ss;
             CK(cudaStreamWaitEvent(st, F.ev_lu, 0));
         } else if (tc) {
+            // programmatic launches on the panel chain, but not beside the surrogate assembly:
+            // there the early-scheduled LU kernels take SMs from the (much longer) assembly,
+            // measured 85-92 -> 130-150 ms per frequency
+            const int pdl = ctx->lu_pdl && !(ctx->sur && ctx->sur_mode > 0);
             const bem::LuStreams ls{ctx->sp, ctx->ev_panel, ctx->ev_cross, ctx->ev_rest, ctx->su, ctx->ev_ucol,
                                     ctx->lu_reserve_sms,
                                     ctx->lu_rest_tiles,
@@ -669,7 +673,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
                                     ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
                                     ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2,
-                                    ctx->d_pairT, ctx->lu_pdl};
+                                    ctx->d_pairT, pdl};
             if (ls.timeline) {
                 rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, ctx->d_wl32,
                                                      ctx->d_wut32, flags);
@@ -682,7 +686,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.rest != ctx->lu_rest_tiles || g.cluster != ctx->lu_cluster_inverse ||
                     g.ucol != ctx->lu_ucol_stream || g.ucol_ctas != ctx->lu_ucol_ctas ||
                     g.split != ctx->lu_split_panel || g.blocked != ctx->lu_block_inverse ||
-                    g.pair != ctx->lu_pair_update || g.pdl != ctx->lu_pdl) {
+                    g.pair != ctx->lu_pair_update || g.pdl != pdl) {
                     if (g.exec) cudaGraphExecDestroy(g.exec);
                     g.exec = nullptr;
                     const unsigned long long l0 = bem::t_launches;
@@ -712,7 +716,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     g.split = ctx->lu_split_panel;
                     g.blocked = ctx->lu_block_inverse;
                     g.pair = ctx->lu_pair_update;
-                    g.pdl = ctx->lu_pdl;
+                    g.pdl = pdl;
                 }
                 if (g.exec) {
                     CK(cudaGraphLaunch(g.exec, st));

@@ -189,16 +189,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (a.npair == 2) { prefetch_map(&mapL2r); prefetch_map(&mapL2i); prefetch_map(&mapU2r); prefetch_map(&mapU2i); }
     }
     __syncwarp();
+    // launched as a programmatic dependent (the first W21 tile after the block inverse): the
+    // set-up above overlaps the inverse; the TMEM allocation and every read of its results
+    // come after this wait, so a waiting CTA holds no tensor memory (a no-op for an
+    // ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32((void*)tmem_slot)),
                      "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    // launched as a programmatic dependent (the first W21 tile after the block inverse): the
-    // set-up above overlaps the inverse; its results are read only after this wait (a no-op
-    // for an ordinary launch)
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
