@@ -209,6 +209,21 @@ def test_lu_beside_refinement_matches_serial_schedule(bg):
     assert np.array_equal(out[0]["iters"], out[1]["iters"])
 
 
+def test_programmatic_launches_keep_the_results(bg):
+    """The LU with its block inverses and first W21 tiles launched as programmatic
+    dependents (lu_pdl = 1) gives the results of ordinary launches."""
+    mesh = cases.lib_cylinder(cases.CYL_MED)
+    om = np.array([0.4, 1.2, 2.0])
+    out = {}
+    for pdl in (0, 1):
+        s = _solver(bg, mesh, precision=bg.MIXED)
+        s.set_tuning("lu_pdl", pdl)
+        out[pdl] = s.solve_omegas(om)
+        assert np.all(out[pdl]["residual"] <= 1e-12)
+    for k in ("A", "B", "F"):
+        assert max(normwise(out[1][k][f], out[0][k][f]) for f in range(om.size)) < 1e-11, k
+
+
 def test_autotune_picks_a_setting(bg):
     # the autotuner times seven schedule settings on the sample frequencies, marks the one
     # it keeps, and the solver then solves with it to the mixed-path tolerance
