@@ -62,6 +62,9 @@ struct FreqState {
     // frequency can run while the solves of the other slot's frequency read their own
     float *inv32r = nullptr, *inv32i = nullptr;
     int* flags = nullptr;
+    // the LU's panel workspaces (W21 and U12^T buffers, transposed pair blocks), per slot so
+    // that the LUs of two frequencies can run at once (lu_overlap = 2)
+    float *wl32 = nullptr, *wut32 = nullptr, *pairT = nullptr;
     cudaEvent_t ev_lu0 = nullptr, ev_lu = nullptr;   // LU start / done (stream st)
     cudaEvent_t ev_sv0 = nullptr, ev_sv1 = nullptr;  // solves start / done
 };
@@ -101,11 +104,11 @@ struct bem_ctx {
     float* d_X32 = nullptr;
     double *d_part = nullptr, *d_post = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
-    float *d_wl32 = nullptr, *d_pairT = nullptr, *d_wut32 = nullptr;
+    cudaStream_t st2 = nullptr;   // second LU stream: the LUs of two frequencies at once
     // solve stream of the pipelined mixed path: the refinement and post-processing of
     // frequency f run here while the LU of f + 1 runs on st (tuning key lu_overlap)
     cudaStream_t ss = nullptr;
-    int lu_overlap = 1;
+    int lu_overlap = 2;
     int* d_flags = nullptr;
     int* d_ready = nullptr;           // block-ready flags of the cooperative triangular solves
     int solve_epoch = 0;
@@ -154,7 +157,7 @@ struct bem_ctx {
     // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
     // 3 = Re D as float pairs + plane-wave Im D (hydro, K != 0)
     int resid_mode = 0;
-    FreqState fs[3];                  // frequency slots (the split pipeline uses three)
+    FreqState fs[4];                  // frequency slots (the split pipelines use three or four)
     cudaStream_t sa = nullptr;        // assembly stream of the pipelined mixed path (lowest priority)
     // Device memory.  allocs: the blocks in use (each with its size in alloc_bytes).
     // free_all returns them to pool, from which later allocations of this context are
@@ -194,7 +197,7 @@ struct bem_ctx {
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
-    LuGraph lu_graph[3];                        // captured LU per frequency slot
+    LuGraph lu_graph[4];                        // captured LU per frequency slot
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
     // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
@@ -283,11 +286,12 @@ void reset_slot(FreqState& F) {
     F.sur_used = false;
     F.inv32r = F.inv32i = nullptr;
     F.flags = nullptr;
+    F.wl32 = F.wut32 = F.pairT = nullptr;
 }
 
 void free_all(bem_ctx* ctx) {
     // the blocks go back to the pool, so this context's work on them must be finished
-    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr, ctx->ss})
+    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr, ctx->ss, ctx->st2})
         if (q) cudaStreamSynchronize(q);
     for (void* p : ctx->allocs) ctx->pool.insert({ctx->alloc_bytes[p], p});
     ctx->allocs.clear();
@@ -297,7 +301,7 @@ void free_all(bem_ctx* ctx) {
                      &ctx->d_inv64i, &ctx->d_wl64, &ctx->d_wu64, &ctx->d_gmV, &ctx->d_gmZ, &ctx->d_gmW,
                      &ctx->d_gmPart, &ctx->d_gmH, &ctx->d_gmC};
     for (auto p : dp) *p = nullptr;
-    float** fp[] = {&ctx->d_X32, &ctx->d_wl32, &ctx->d_pairT, &ctx->d_wut32,
+    float** fp[] = {&ctx->d_X32,
                     &ctx->d_RShi, &ctx->d_RSlo, &ctx->d_RDhi, &ctx->d_RDlo, &ctx->d_RSRhi, &ctx->d_RSRlo};
     for (auto p : fp) *p = nullptr;
     for (FreqState& F : ctx->fs) reset_slot(F);
@@ -405,9 +409,9 @@ bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
         DA(ctx->fs[0].inv32r, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->fs[0].inv32i, (size_t)(Np / nb32) * 2 * nb32 * nb32);
         DA(ctx->fs[0].flags, 1);
-        DA(ctx->d_wl32, (size_t)8 * Np * nb32);  // four [2][Np][128] buffers (lookahead; two steps per pass)
-        DA(ctx->d_pairT, (size_t)2 * Np * nb32);  // transposed pair blocks of the pair fold (4 (Np/256) 128^2)
-        DA(ctx->d_wut32, (size_t)8 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
+        DA(ctx->fs[0].wl32, (size_t)8 * Np * nb32);  // four [2][Np][128] buffers (lookahead; two steps per pass)
+        DA(ctx->fs[0].pairT, (size_t)2 * Np * nb32);  // transposed pair blocks of the pair fold (4 (Np/256) 128^2)
+        DA(ctx->fs[0].wut32, (size_t)8 * Np * nb32 + (size_t)2 * Np * 128);  // + transposed D^-1 blocks
         DA(ctx->d_X32, (size_t)4 * Np * R);
         DA(ctx->d_Rr, (size_t)2 * Np * R);
         const size_t vs = (size_t)2 * Np * bem::MAX_RHS;
@@ -623,8 +627,8 @@ bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double
 bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bool mixed, double tol, int max_iter, int* iters_out,
                             double* resid_out, double* t_lu, double* t_solve,
                             const std::function<bem_status()>& after_lu = nullptr, int phase = 3,
-                            cudaStream_t ss = nullptr) {
-    cudaStream_t st = ctx->st;
+                            cudaStream_t ss = nullptr, cudaStream_t lu_stream = nullptr) {
+    cudaStream_t st = lu_stream && phase == 1 ? lu_stream : ctx->st;
     if (!mixed) phase = 3;
     const bool do_factor = (phase & 1) != 0, do_solve = (phase & 2) != 0;
     bem_status s = ensure_lu_buffers(ctx, Np, R, mixed);
@@ -673,10 +677,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                                     ctx->lu_cluster_inverse, ctx->lu_ucol_stream, ctx->lu_ucol_ctas,
                                     ctx->lu_split_panel ? ctx->sq : nullptr, ctx->ev_head, ctx->ev_t0,
                                     ctx->lu_block_inverse, ctx->sr, ctx->ev_panel2, ctx->ev_cross2,
-                                    ctx->d_pairT, pdl};
+                                    F.pairT, pdl};
             if (ls.timeline) {
-                rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, ctx->d_wl32,
-                                                     ctx->d_wut32, flags);
+                rc_lu = bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, F.wl32, F.wut32,
+                                                     flags);
             } else {
                 // The ~320 launches and 128 cross-stream event edges of one factorization are
                 // captured once per slot into a CUDA graph and replayed, which removes the host
@@ -693,10 +697,10 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     cudaGraph_t graph = nullptr;
                     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
                     const bool paired = ctx->lu_pair_update && ls.panel_tail && ls.ucol_own;
-                    rc_lu = paired ? bem::lu_factor_f32_paired(st, ls, Np, A, F.inv32r, F.inv32i,
-                                                               ctx->d_wl32, ctx->d_wut32, flags)
-                                   : bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i,
-                                                                  ctx->d_wl32, ctx->d_wut32, flags);
+                    rc_lu = paired ? bem::lu_factor_f32_paired(st, ls, Np, A, F.inv32r, F.inv32i, F.wl32,
+                                                               F.wut32, flags)
+                                   : bem::lu_factor_f32_lookahead(st, ls, Np, A, F.inv32r, F.inv32i, F.wl32,
+                                                                  F.wut32, flags);
                     const cudaError_t ec = cudaStreamEndCapture(st, &graph);
                     if (rc_lu == 0 && ec == cudaSuccess) {
                         const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
@@ -983,6 +987,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaEventCreateWithFlags(&ctx->ev_lu_done, cudaEventDisableTiming));
     CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
     CK(cudaStreamCreateWithPriority(&ctx->ss, cudaStreamNonBlocking, prio_hi));
+    CK(cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t* e : {&F.ev_lu0, &F.ev_lu, &F.ev_sv0, &F.ev_sv1}) CK(cudaEventCreate(e));
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
@@ -1007,12 +1012,14 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sq) cudaStreamSynchronize(ctx->sq);
     if (ctx->sr) cudaStreamSynchronize(ctx->sr);
     if (ctx->ss) cudaStreamSynchronize(ctx->ss);
+    if (ctx->st2) cudaStreamSynchronize(ctx->st2);
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5, F.ev_lu0,
                               F.ev_lu, F.ev_sv0, F.ev_sv1})
             if (e) cudaEventDestroy(e);
     }
     if (ctx->ss) cudaStreamDestroy(ctx->ss);
+    if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->sa) cudaStreamDestroy(ctx->sa);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -1290,6 +1297,9 @@ bem_status ensure_slot(bem_ctx* ctx, FreqState& F, bool mixed) {
         DA(F.inv32r, (size_t)(Np / 128) * 2 * 128 * 128);
         DA(F.inv32i, (size_t)(Np / 128) * 2 * 128 * 128);
         DA(F.flags, 1);
+        DA(F.wl32, (size_t)8 * Np * 128);
+        DA(F.pairT, (size_t)2 * Np * 128);
+        DA(F.wut32, (size_t)8 * Np * 128 + (size_t)2 * Np * 128);
     }
     if (&F != &ctx->fs[0])  // radiation columns of B (set once by bem_setup)
         CK(cudaMemcpyAsync(F.Bm, ctx->fs[0].Bm, sizeof(double) * 2 * (size_t)N * R, cudaMemcpyDeviceToDevice,
@@ -1432,8 +1442,11 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     const bool pipe = mixed && n_freq > 1;
     // split: the LU of frequency f + 1 (stream st) runs beside the refinement of f (stream
     // ss) while f + 2 is assembled (stream sa): three frequency slots
+    // lu_overlap = 2: four slots, and the LUs of f + 1 and f + 2 may run at once on two streams
     const bool split = pipe && ctx->asm_overlap && ctx->lu_overlap;
-    const int nslots = split ? 3 : pipe ? 2 : 1;
+    const bool two_lu = split && ctx->lu_overlap == 2;
+    const int nslots = two_lu ? 4 : split ? 3 : pipe ? 2 : 1;
+    const int asm_ahead = two_lu ? 3 : 2, lu_ahead = two_lu ? 2 : 1;
     for (int k = 0; k < nslots; ++k) {
         s = ensure_slot(ctx, ctx->fs[k], mixed);
         if (s != BEM_OK) return s;
@@ -1469,21 +1482,24 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         cudaStreamSynchronize(sa);
         cudaStreamSynchronize(st);
         if (split) cudaStreamSynchronize(so);
+        if (two_lu) cudaStreamSynchronize(ctx->st2);
     };
     double t_lu_next = 0, t_unused = 0;
     // factor of frequency g, queued on st after its assembly (split schedule)
     auto enqueue_factor = [&](int g) -> bem_status {
         FreqState& G = slot(g);
-        CK(cudaStreamWaitEvent(st, G.ev_asm, 0));
+        cudaStream_t ls = two_lu && (g & 1) ? ctx->st2 : st;
+        CK(cudaStreamWaitEvent(ls, G.ev_asm, 0));
         return factor_and_solve(ctx, G, N, Np, R, mixed, tol, ctx->refine_max, nullptr, nullptr, &t_lu_next,
-                                &t_unused, nullptr, 1);
+                                &t_unused, nullptr, 1, nullptr, ls);
     };
     if (n_freq > 0) {
         s = enqueue_assembly(0);
         if (s != BEM_OK) return s;
         if (split) {
-            s = enqueue_factor(0);
-            if (s == BEM_OK && n_freq > 1) s = enqueue_assembly(1);
+            // fill the pipeline: assemblies of 1 .. asm_ahead - 1, LUs of 0 .. lu_ahead - 1
+            for (int g = 1; g < asm_ahead && g < n_freq && s == BEM_OK; ++g) s = enqueue_assembly(g);
+            for (int g = 0; g < lu_ahead && g < n_freq && s == BEM_OK; ++g) s = enqueue_factor(g);
             if (s != BEM_OK) { sync_all(); return s; }
         }
     }
@@ -1491,8 +1507,8 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         FreqState& F = slot(f);
         const double Om = omega[f];
         if (split) {
-            if (f + 2 < n_freq) {
-                s = enqueue_assembly(f + 2);  // two ahead: overlaps the LU of f + 1 and the solves of f
+            if (f + asm_ahead < n_freq) {
+                s = enqueue_assembly(f + asm_ahead);  // ahead: overlaps the LUs queued and the solves of f
                 if (s != BEM_OK) { sync_all(); return s; }
             }
         } else if (pipe && ctx->asm_overlap && f + 1 < n_freq) {
@@ -1518,10 +1534,10 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         double resid = 0;
         double t_lu = 0, t_sv = 0;
         if (split) {
-            // the LU of f was queued one iteration earlier; queue the LU of f + 1 now, so that it
-            // runs while this thread drives the refinement of f
-            if (f + 1 < n_freq) {
-                s = enqueue_factor(f + 1);
+            // the LU of f was queued lu_ahead iterations earlier; queue the LU of f + lu_ahead
+            // now, so that it runs while this thread drives the refinement of f
+            if (f + lu_ahead < n_freq) {
+                s = enqueue_factor(f + lu_ahead);
                 if (s != BEM_OK) { sync_all(); return s; }
             }
             ctx->resid_mode = K != 0.0 ? 3 : 2;
@@ -2300,7 +2316,7 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "lu_overlap") {
-        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "lu_overlap must be 0 or 1");
+        if (!(value == 0 || value == 1 || value == 2)) return fail(ctx, BEM_ERR_ARG, "lu_overlap must be 0, 1 or 2");
         ctx->lu_overlap = (int)value;
         return BEM_OK;
     }
@@ -2354,9 +2370,9 @@ bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* m
     struct Setting {
         int asm_reserve, lu_overlap;
     };
-    // the default first; then reserves with the LU beside the previous frequency's
-    // refinement, and two without that overlap
-    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 1}, {48, 1}, {64, 1}, {72, 1}, {80, 1},
+    // the default first; then reserves with two LUs in flight (lu_overlap 2), with one
+    // LU beside the previous frequency's refinement (1), and the two-slot schedule (0)
+    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 2}, {48, 2}, {64, 2}, {40, 1}, {56, 1},
                             {72, 0}};
     const int ng = (int)(sizeof(grid) / sizeof(grid[0]));
     std::vector<double> best(ng, 1e300);
