@@ -104,7 +104,7 @@ struct bem_ctx {
     float* d_X32 = nullptr;
     double *d_part = nullptr, *d_post = nullptr;
     double *d_inv64r = nullptr, *d_inv64i = nullptr, *d_wl64 = nullptr, *d_wu64 = nullptr;
-    cudaStream_t st2 = nullptr;   // second LU stream: the LUs of two frequencies at once
+    cudaStream_t st2 = nullptr, st3 = nullptr;  // more LU streams: the LUs of several frequencies at once
     // solve stream of the pipelined mixed path: the refinement and post-processing of
     // frequency f run here while the LU of f + 1 runs on st (tuning key lu_overlap)
     cudaStream_t ss = nullptr;
@@ -157,7 +157,7 @@ struct bem_ctx {
     // D64 real part only (aero); 2 = Re D as float pairs (hydro, K = 0);
     // 3 = Re D as float pairs + plane-wave Im D (hydro, K != 0)
     int resid_mode = 0;
-    FreqState fs[4];                  // frequency slots (the split pipelines use three or four)
+    FreqState fs[5];                  // frequency slots (the split pipelines use 3 to 5)
     cudaStream_t sa = nullptr;        // assembly stream of the pipelined mixed path (lowest priority)
     // Device memory.  allocs: the blocks in use (each with its size in alloc_bytes).
     // free_all returns them to pool, from which later allocations of this context are
@@ -197,7 +197,7 @@ struct bem_ctx {
     int* d_wctr = nullptr;                      // row counter + per-SM counters of the wave kernel
     std::vector<double> lu_tl_ms;               // timeline of a call's first LU, ms from its first event
     bool lu_tl_armed = false;                   // the next LU records the timeline
-    LuGraph lu_graph[4];                        // captured LU per frequency slot
+    LuGraph lu_graph[5];                        // captured LU per frequency slot
     double kernel_ms[4] = {0, 0, 0, 0};         // wave-assembly kernel: ms, launches, panels^2 per launch
     long long launches = 0;
     // exterior outputs (Hydrodynamic_Solver.cpp:489-505)
@@ -291,7 +291,7 @@ void reset_slot(FreqState& F) {
 
 void free_all(bem_ctx* ctx) {
     // the blocks go back to the pool, so this context's work on them must be finished
-    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr, ctx->ss, ctx->st2})
+    for (cudaStream_t q : {ctx->st, ctx->sp, ctx->sa, ctx->su, ctx->sq, ctx->sr, ctx->ss, ctx->st2, ctx->st3})
         if (q) cudaStreamSynchronize(q);
     for (void* p : ctx->allocs) ctx->pool.insert({ctx->alloc_bytes[p], p});
     ctx->allocs.clear();
@@ -988,6 +988,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->sa, cudaStreamNonBlocking, prio_lo));
     CK(cudaStreamCreateWithPriority(&ctx->ss, cudaStreamNonBlocking, prio_hi));
     CK(cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
+    CK(cudaStreamCreateWithPriority(&ctx->st3, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t* e : {&F.ev_lu0, &F.ev_lu, &F.ev_sv0, &F.ev_sv1}) CK(cudaEventCreate(e));
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
@@ -1013,6 +1014,7 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->sr) cudaStreamSynchronize(ctx->sr);
     if (ctx->ss) cudaStreamSynchronize(ctx->ss);
     if (ctx->st2) cudaStreamSynchronize(ctx->st2);
+    if (ctx->st3) cudaStreamSynchronize(ctx->st3);
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t e : {F.ev_asm, F.ev_free, F.ev_t[0], F.ev_t[1], F.ev_t[2], F.ev_t[3], F.ev_t5, F.ev_lu0,
                               F.ev_lu, F.ev_sv0, F.ev_sv1})
@@ -1020,6 +1022,7 @@ void bem_destroy(bem_ctx* ctx) {
     }
     if (ctx->ss) cudaStreamDestroy(ctx->ss);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
+    if (ctx->st3) cudaStreamDestroy(ctx->st3);
     if (ctx->sa) cudaStreamDestroy(ctx->sa);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -1442,11 +1445,13 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
     const bool pipe = mixed && n_freq > 1;
     // split: the LU of frequency f + 1 (stream st) runs beside the refinement of f (stream
     // ss) while f + 2 is assembled (stream sa): three frequency slots
-    // lu_overlap = 2: four slots, and the LUs of f + 1 and f + 2 may run at once on two streams
+    // lu_overlap = L >= 1: L + 2 slots, and the LUs of f + 1 .. f + L may run at once on L
+    // streams beside the refinement of f while f + L + 1 is assembled
     const bool split = pipe && ctx->asm_overlap && ctx->lu_overlap;
-    const bool two_lu = split && ctx->lu_overlap == 2;
-    const int nslots = two_lu ? 4 : split ? 3 : pipe ? 2 : 1;
-    const int asm_ahead = two_lu ? 3 : 2, lu_ahead = two_lu ? 2 : 1;
+    const int nlu = split ? ctx->lu_overlap : 1;
+    const int nslots = split ? nlu + 2 : pipe ? 2 : 1;
+    const int asm_ahead = nlu + 1, lu_ahead = nlu;
+    cudaStream_t lu_streams[3] = {st, ctx->st2, ctx->st3};
     for (int k = 0; k < nslots; ++k) {
         s = ensure_slot(ctx, ctx->fs[k], mixed);
         if (s != BEM_OK) return s;
@@ -1482,13 +1487,13 @@ bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precisio
         cudaStreamSynchronize(sa);
         cudaStreamSynchronize(st);
         if (split) cudaStreamSynchronize(so);
-        if (two_lu) cudaStreamSynchronize(ctx->st2);
+        for (int q = 1; q < nlu; ++q) cudaStreamSynchronize(lu_streams[q]);
     };
     double t_lu_next = 0, t_unused = 0;
     // factor of frequency g, queued on st after its assembly (split schedule)
     auto enqueue_factor = [&](int g) -> bem_status {
         FreqState& G = slot(g);
-        cudaStream_t ls = two_lu && (g & 1) ? ctx->st2 : st;
+        cudaStream_t ls = lu_streams[g % nlu];
         CK(cudaStreamWaitEvent(ls, G.ev_asm, 0));
         return factor_and_solve(ctx, G, N, Np, R, mixed, tol, ctx->refine_max, nullptr, nullptr, &t_lu_next,
                                 &t_unused, nullptr, 1, nullptr, ls);
@@ -2316,7 +2321,7 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
         return BEM_OK;
     }
     if (k == "lu_overlap") {
-        if (!(value == 0 || value == 1 || value == 2)) return fail(ctx, BEM_ERR_ARG, "lu_overlap must be 0, 1 or 2");
+        if (!(value >= 0 && value <= 3)) return fail(ctx, BEM_ERR_ARG, "lu_overlap must be 0, 1, 2 or 3");
         ctx->lu_overlap = (int)value;
         return BEM_OK;
     }
@@ -2370,10 +2375,10 @@ bem_status bem_autotune(bem_ctx* ctx, int n_freq, const double* omega, double* m
     struct Setting {
         int asm_reserve, lu_overlap;
     };
-    // the default first; then reserves with two LUs in flight (lu_overlap 2), with one
-    // LU beside the previous frequency's refinement (1), and the two-slot schedule (0)
-    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 2}, {48, 2}, {64, 2}, {40, 1}, {56, 1},
-                            {72, 0}};
+    // the default first; then reserves with two or three LUs in flight (lu_overlap 2, 3)
+    // and with one LU beside the previous frequency's refinement (1)
+    const Setting grid[] = {{ctx->asm_reserve, ctx->lu_overlap}, {40, 2}, {48, 2}, {64, 2}, {40, 3}, {48, 3},
+                            {56, 1}};
     const int ng = (int)(sizeof(grid) / sizeof(grid[0]));
     std::vector<double> best(ng, 1e300);
     auto apply = [&](const Setting& g) {

@@ -328,10 +328,10 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     the solves only.
  *   "lu_overlap"      with asm_overlap = 1: 1 = the LU of frequency f + 1 runs beside the
  *                     refinement of f (its own stream; each frequency slot keeps its own
- *                     block inverses, flags and LU workspaces; three slots), 2 = the LUs
- *                     of f + 1 and f + 2 may also run at once on two streams (four slots;
- *                     default), 0 = LU and refinement of one frequency after the other on
- *                     one stream.
+ *                     block inverses, flags and LU workspaces; three slots), 2 or 3 = the
+ *                     LUs of f + 1 .. f + 2 (3) may also run at once on as many streams
+ *                     (four or five slots; 2 is the default), 0 = LU and refinement of one
+ *                     frequency after the other on one stream.
  *   "asm_reserve_sms" SMs (lowest SM ids) the persistent assembly kernel leaves to the
  *                     LU and the refinement when it overlaps them (default 56).
  *   "asm_ctas_per_sm" assembly CTAs admitted per SM then (1..3, default 3).
@@ -351,7 +351,7 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value);
 /* Autotuner of the pipelined mixed solve: times bem_solve (BEM_MIXED, outputs skipped)
  * on the n_freq >= 2 sample frequencies for each of a small grid of the schedule knobs
  * above (the current setting; assembly reserves of 40, 48 and 64 SMs with
- * lu_overlap = 2, of 40 and 56 with lu_overlap = 1, of 72 with lu_overlap = 0), every
+ * lu_overlap = 2, of 40 and 48 with lu_overlap = 3, of 56 with lu_overlap = 1), every
  * setting twice in alternation, and keeps the fastest on the context.  ms_per_freq
  * (optional) receives its time per frequency; report (optional, report_len bytes) one
  * line per setting, the chosen one marked '*'.  Needs bem_setup.  The project's

@@ -194,18 +194,18 @@ def test_lu_schedule_variants_agree(bg):
 
 def test_lu_beside_refinement_matches_serial_schedule(bg):
     """The split pipelines (the LU of frequency f + 1 beside the refinement of f, f + 2
-    assembled meanwhile, three frequency slots; or four slots with the LUs of f + 1 and
-    f + 2 on two streams), cycled by seven frequencies, give the results of the schedule
+    assembled meanwhile, three frequency slots; or four or five slots with the LUs of
+    f + 1 .. f + 3 on as many streams), cycled by seven frequencies, give the results of the schedule
     that factors and refines one frequency after the other."""
     mesh = cases.lib_cylinder(cases.CYL_MED)
     om = np.array([0.3, 0.7, 1.1, 1.5, 1.9, 2.3, 0.5])
     out = {}
-    for lo in (0, 1, 2):
+    for lo in (0, 1, 2, 3):
         s = _solver(bg, mesh, precision=bg.MIXED)
         s.set_tuning("lu_overlap", lo)
         out[lo] = s.solve_omegas(om)
         assert np.all(out[lo]["residual"] <= 1e-12)
-    for lo in (1, 2):
+    for lo in (1, 2, 3):
         for k in ("A", "B", "F"):
             assert max(normwise(out[lo][k][f], out[0][k][f]) for f in range(om.size)) < 1e-11, (lo, k)
         assert np.array_equal(out[0]["iters"], out[lo]["iters"])
