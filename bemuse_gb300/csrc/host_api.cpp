@@ -1412,13 +1412,14 @@ bem_status assemble(bem_ctx* ctx, FreqState& F, double Om, bool mixed, cudaStrea
 
 }  // namespace
 
-// Mixed calls with several frequencies run as a three-stage pipeline over three
-// frequency slots (slot f % 3): the assembly of frequency f+2 (assembly stream,
-// lowest priority), the LU of f+1 (stream st, captured graph) and the refinement
-// and post-processing of f (stream ss), driven by this thread.  A slot is
-// reassembled only after its refinement has released it.  lu_overlap = 0 (or
-// asm_overlap = 0) gives the two-slot schedule: assembly of f+1 beside the LU and
-// refinement of f, one after the other on st.
+// Mixed calls with several frequencies run as a pipeline over lu_overlap + 2
+// frequency slots: at step f this thread queues the assembly of frequency
+// f + L + 1 (assembly stream, lowest priority) and the LU of f + L (a captured
+// graph on one of L LU streams, L = lu_overlap), then drives the refinement and
+// post-processing of f (stream ss), so up to L LUs run beside one assembly and one
+// refinement.  A slot is reassembled only after its refinement has released it.
+// lu_overlap = 0 (or asm_overlap = 0) gives the two-slot schedule: assembly of f+1
+// beside the LU and refinement of f, one after the other on st.
 bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double tol, bem_result* out) {
     if (!ctx) return fail(nullptr, BEM_ERR_ARG, "null context");
     if (!ctx->ready || ctx->aero) return fail(ctx, BEM_ERR_STATE, "bem_solve before bem_setup");

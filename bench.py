@@ -9,9 +9,9 @@ right-hand sides).  Synthetic by construction (generated mesh, no dataset).
 One step = one frequency-solve in the mixed-precision mode: wave assembly
 (FP32 real parts, FP64-accurate imaginary parts), TF32 tensor-core LU, FP64
 iterative refinement to 1e-12 relative residual, hull integrals.  The library runs
-the timed frequencies as a three-stage pipeline (assembly of f + 2, LU of f + 1 and
-refinement of f on three streams); the autotuner picks the SM split before the
-warm-up, outside the timed region.
+the timed frequencies as a pipeline (the assembly of f + 3, the LUs of f + 1 and
+f + 2 and the refinement of f on their own streams); the autotuner picks the SM
+split and the number of LUs in flight before the warm-up, outside the timed region.
 
   value         = freq-solves/s from device time (CUDA events on the library stream)
   e2e           = freq-solves/s of wall time around bem_solve (host in, host out)

@@ -190,9 +190,10 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
 /* Set_Real + Solve (Hydrodynamic_Solver.cpp:400-487) for n_freq angular
  * frequencies in one call.  refine_tol <= 0 selects the default 1e-12.  With
  * BEM_MIXED and n_freq >= 2 the frequencies run as a pipeline on the context's
- * streams (assembly of f + 2, LU of f + 1 and refinement of f side by side; the
- * tuning keys asm_overlap and lu_overlap select it); results are those of solving
- * the frequencies one at a time.  n_freq = 0 returns at once. */
+ * streams (the assembly of one frequency, the LUs of the next one or two and the
+ * refinement of the one before them side by side; the tuning keys asm_overlap and
+ * lu_overlap select it); results are those of solving the frequencies one at a
+ * time.  n_freq = 0 returns at once. */
 bem_status bem_solve(bem_ctx* ctx, int n_freq, const double* omega, int precision, double refine_tol,
                      bem_result* out);
 
