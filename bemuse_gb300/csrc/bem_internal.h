@@ -240,6 +240,21 @@ void launch_f32_to_f64(cudaStream_t st, size_t n, const float* src, double* dst)
 void launch_to_f32(cudaStream_t st, size_t n, const double* src, float* dst);
 void launch_add_f32(cudaStream_t st, size_t n, const float* src, double* dst);
 void launch_pad_rhs(cudaStream_t st, int N, int Np, int R, double* X);
+// Device-side state of one frequency's classic refinement when its sweeps repeat inside a
+// graph (conditional while node): sweeps done, outcome, the slot's device flags as the
+// last test saw them (the LU's and the solves'), last residual (max over the right-hand
+// sides of |r|_inf / |y|_inf), the previous sweep's and the previous full-accuracy
+// residual, and the last full-to-full contraction.  Zero it before the first sweep.
+enum { REFINE_RUNNING = 0, REFINE_CONVERGED = 1, REFINE_FAILED = 2, REFINE_STALLED = 3, REFINE_TIMEOUT = 4 };
+struct RefineState {
+    int iters, status, flags, pad;
+    double resid, prev, prev_full, contraction;
+};
+// One sweep's convergence test (k_gmres.cu): reads the norms of launch_norms and the
+// solve's flags, updates the state and sets h to 1 while the loop should go on.
+void launch_refine_step(cudaStream_t st, int R, const unsigned long long* nrm, const int* flags, double tol,
+                        int max_iter, int coarse_first, int gmres_switch, RefineState* state,
+                        cudaGraphConditionalHandle h);
 
 // Tensor-core inference of the Green-function surrogate network (k_mlp_tc.cu).
 // mlp_tc_build_image: the operand image (mlp_tc_image_bytes() bytes) and FP32 tail

@@ -67,6 +67,9 @@ struct FreqState {
     float *wl32 = nullptr, *wut32 = nullptr, *pairT = nullptr;
     cudaEvent_t ev_lu0 = nullptr, ev_lu = nullptr;   // LU start / done (stream st)
     cudaEvent_t ev_sv0 = nullptr, ev_sv1 = nullptr;  // solves start / done
+    // device-side refinement state of the frequency this slot holds (null: the context's
+    // first state); a solve captured into one graph gives each frequency its own
+    bem::RefineState* rstate = nullptr;
 };
 
 // One captured tensor-core LU (per frequency slot) and what it was captured for.
@@ -122,6 +125,15 @@ struct bem_ctx {
     int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
     int refine_coarse_first = 1;  // 1: the first classic sweep's residual from the FP32 high words
     int refine_max = 60;          // preconditioner solves the refinement may use before it fails
+    // classic refinement with its convergence test on the device, the sweeps repeating in a
+    // conditional while node of a graph (always inside a solve captured into a graph;
+    // refine_graph = 1 also for the stream-driven solves); the states (RSTATE_CAP, one per
+    // frequency of a captured solve), the stream the loop body is captured on, and the
+    // launches of one captured sweep
+    int refine_graph = 0;
+    bem::RefineState* d_rstate = nullptr;
+    cudaStream_t sbody = nullptr;
+    long long rg_body_launches = 0;
     // surrogate form of the mixed assembly (bem_set_surrogate): the network, the mode (0 off,
     // 1 strict: a frequency whose judged error exceeds sur_tol is solved again with the closed
     // form, 2 accept), the judged fraction of far pairs and the domain {KR min, KR max, KZ min,
@@ -395,6 +407,7 @@ bool inv6(const cplx* M, cplx* out) {
 }
 
 constexpr int GM_M = 16;  // restart length of the flexible GMRES refinement
+constexpr int RSTATE_CAP = 1024;  // device refinement states per context
 
 bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     const int nb64 = 64, nb32 = 128;
@@ -619,6 +632,27 @@ bem_status refine_gmres(bem_ctx* ctx, FreqState& F, int N, int Np, int R, double
     }
 }
 
+// Sets the priority attribute of every kernel node of g (not of nested graphs).
+cudaError_t set_kernel_priority(cudaGraph_t g, int prio) {
+    size_t n = 0;
+    cudaError_t e = cudaGraphGetNodes(g, nullptr, &n);
+    if (e != cudaSuccess || n == 0) return e;
+    std::vector<cudaGraphNode_t> nodes(n);
+    e = cudaGraphGetNodes(g, nodes.data(), &n);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttributeValue v = {};
+    v.priority = prio;
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(nd, &t);
+        if (e != cudaSuccess) return e;
+        if (t != cudaGraphNodeTypeKernel) continue;
+        e = cudaGraphKernelNodeSetAttribute(nd, cudaLaunchAttributePriority, &v);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Factor + solve.  D64 (planar, ld = Np) holds the operator; Y (N x R, interleaved)
 // the right-hand sides; the solution lands in d_X.  mixed: TF32 LU of the FP32
 // copy + FP64 refinement against D64; plain: FP64 LU of D64 (destroyed).
@@ -791,9 +825,144 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             }
             return gs;
         };
+        // Classic refinement with its convergence test on the device: the first sweep, then a
+        // conditional while node whose body is one sweep; k_refine_step, at the end of each,
+        // decides as the host loop below does and ends the loop.  Inside a caller's capture
+        // (a whole solve captured into one graph) the loop becomes part of that graph and its
+        // outcome stays in the slot's state for the caller to read; otherwise it is captured
+        // for this frequency alone (K, the plane-wave count and the slot's buffers are baked
+        // in), launched, and its outcome handled here.
+        auto refine_on_device = [&](bool outer) -> bem_status {
+            bem::RefineState* rs = F.rstate ? F.rstate : ctx->d_rstate;
+            const int ep = (ctx->solve_epoch += 2) - 1;
+            const size_t ready_bytes = sizeof(int) * ((size_t)Np / 8 + 32);
+            cudaGraphConditionalHandle h = 0;
+            auto sweep = [&](bool coarse_now) -> bem_status {
+                bem::launch_to_f32(st, nr2, ctx->d_Rr, ctx->d_X32);
+                // the epochs are fixed in the graph, so the chain's flags restart from zero
+                CK(cudaMemsetAsync(ctx->d_ready, 0, ready_bytes, st));
+                if (bem::lu_solve_f32(st, Np, A, F.inv32r, F.inv32i, R, ctx->d_X32, ctx->d_ready, ep, flags,
+                                      ctx->test_wait_skew, ctx->test_wait_ns))
+                    return fail(ctx, BEM_ERR_CUDA, "triangular-solve launch failed");
+                bem::launch_add_f32(st, nr2, ctx->d_X32, ctx->d_X);
+                CK(cudaMemsetAsync(ctx->d_norms, 0, sizeof(unsigned long long) * 2 * R, st));
+                coarse = coarse_now;
+                apply_op(ctx->d_X, F.Y, -1.0, 1.0, ctx->d_Rr);
+                coarse = false;
+                bem::launch_norms(st, N, R, ctx->d_Rr, F.Y, ctx->d_norms);
+                bem::launch_pad_rhs(st, N, Np, R, ctx->d_Rr);
+                bem::launch_refine_step(st, R, ctx->d_norms, flags, tol, max_iter, coarse_first ? 1 : 0,
+                                        ctx->refine_gmres == 2 ? 1 : 0, rs, h);
+                CK(cudaGetLastError());
+                return BEM_OK;
+            };
+            const cudaStream_t st0 = st;
+            if (!outer) CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            unsigned long long lb = 0;
+            cudaGraph_t loop_body = nullptr;
+            const bem_status cs = [&]() -> bem_status {
+                cudaStreamCaptureStatus q;
+                cudaGraph_t g = nullptr;
+                const cudaGraphNode_t* d = nullptr;
+                size_t nd = 0;
+                CK(cudaStreamGetCaptureInfo(st, &q, nullptr, &g, &d, nullptr, &nd));
+                CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+                CK(cudaMemsetAsync(rs, 0, sizeof(bem::RefineState), st));
+                bem_status s1 = sweep(coarse_first);
+                if (s1 != BEM_OK) return s1;
+                CK(cudaStreamGetCaptureInfo(st, &q, nullptr, &g, &d, nullptr, &nd));
+                std::vector<cudaGraphNode_t> deps(d, d + nd);
+                cudaGraphNodeParams p = {};
+                p.type = cudaGraphNodeTypeConditional;
+                p.conditional.handle = h;
+                p.conditional.type = cudaGraphCondTypeWhile;
+                p.conditional.size = 1;
+                cudaGraphNode_t node = nullptr;
+                CK(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &p));
+                CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+                loop_body = p.conditional.phGraph_out[0];
+                CK(cudaStreamBeginCaptureToGraph(ctx->sbody, loop_body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeRelaxed));
+                const unsigned long long b0 = bem::t_launches;
+                st = ctx->sbody;
+                s1 = sweep(false);
+                st = st0;
+                lb = bem::t_launches - b0;
+                cudaGraph_t body = nullptr;
+                const cudaError_t eb = cudaStreamEndCapture(ctx->sbody, &body);
+                if (s1 != BEM_OK) return s1;
+                CK(eb);
+                return BEM_OK;
+            }();
+            st = st0;
+            ctx->rg_body_launches = (long long)lb;
+            if (outer) return cs;
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+            if (cs != BEM_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                return cs;
+            }
+            CK(ee);
+            // every kernel of the loop, its body included, at the priority of the stream it
+            // is launched into (the refinement's high priority in the pipelined solves)
+            int prio = 0;
+            CK(cudaStreamGetPriority(st, &prio));
+            CK(set_kernel_priority(graph, prio));
+            if (loop_body) CK(set_kernel_priority(loop_body, prio));
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t ei = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+            cudaGraphDestroy(graph);
+            CK(ei);
+            bem::RefineState hs = {};
+            const cudaError_t el = cudaGraphLaunch(exec, st);
+            const cudaError_t em =
+                el == cudaSuccess ? cudaMemcpyAsync(&hs, rs, sizeof(hs), cudaMemcpyDeviceToHost, st) : el;
+            const cudaError_t es = cudaStreamSynchronize(st);
+            cudaGraphExecDestroy(exec);
+            CK(el);
+            CK(em);
+            CK(es);
+            // the capture counted the first sweep and one loop body; the body ran iters - 1 times
+            bem::g_launches += (unsigned long long)((long long)lb * (hs.iters - 2));
+            iters = hs.iters;
+            resid = hs.resid;
+            if (hs.contraction > 0.0) ctx->last_contraction = hs.contraction;
+            switch (hs.status) {
+                case bem::REFINE_CONVERGED:
+                    return BEM_OK;
+                case bem::REFINE_STALLED:
+                    return gmres();
+                case bem::REFINE_TIMEOUT:
+                    return fail(ctx, BEM_ERR_CUDA, "a device-side wait in the triangular solve expired");
+                case bem::REFINE_FAILED:
+                    if (iters_out) *iters_out = iters;
+                    if (resid_out) *resid_out = resid;
+                    return fail(ctx, BEM_ERR_NUMERIC, "iterative refinement did not reach the tolerance (residual " +
+                                                          std::to_string(resid) + " after " + std::to_string(iters) +
+                                                          " sweeps)");
+                default:
+                    return fail(ctx, BEM_ERR_CUDA, "the refinement graph ended without an outcome");
+            }
+        };
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(st, &cap));
+        const bool outer = cap != cudaStreamCaptureStatusNone;
+        if (outer && ctx->refine_gmres == 1)
+            return fail(ctx, BEM_ERR_STATE, "a solve captured into a graph needs the classic refinement");
         if (ctx->refine_gmres == 1) {
             const bem_status gs = gmres();
             if (gs != BEM_OK) return gs;
+        } else if (outer || ctx->refine_graph) {
+            const bem_status gs = refine_on_device(outer);
+            if (gs != BEM_OK) return gs;
+            if (outer) {
+                // the outcome and the flags are read after the caller's graph has run
+                CK(cudaEventRecord(ctx->ev[4], st));
+                CK(cudaEventRecord(F.ev_sv1, st));
+                return BEM_OK;
+            }
         } else {
             // classic refinement: x <- x + M^-1 (y - D x).  With refine_gmres = 2 a sweep
             // that reduces the residual by less than 20x (a nearly singular system, e.g. a
@@ -989,6 +1158,8 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->ss, cudaStreamNonBlocking, prio_hi));
     CK(cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     CK(cudaStreamCreateWithPriority(&ctx->st3, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
+    CK(cudaStreamCreateWithFlags(&ctx->sbody, cudaStreamNonBlocking));
+    CK(cudaMalloc(&ctx->d_rstate, sizeof(bem::RefineState) * RSTATE_CAP));
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t* e : {&F.ev_lu0, &F.ev_lu, &F.ev_sv0, &F.ev_sv1}) CK(cudaEventCreate(e));
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));
@@ -1043,6 +1214,8 @@ void bem_destroy(bem_ctx* ctx) {
     if (ctx->ev_cross2) cudaEventDestroy(ctx->ev_cross2);
     if (ctx->sr) cudaStreamDestroy(ctx->sr);
     if (ctx->h_gm) cudaFreeHost(ctx->h_gm);
+    if (ctx->d_rstate) cudaFree(ctx->d_rstate);
+    if (ctx->sbody) cudaStreamDestroy(ctx->sbody);
     if (ctx->sp) cudaStreamDestroy(ctx->sp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -2303,6 +2476,11 @@ bem_status bem_set_tuning(bem_ctx* ctx, const char* key, double value) {
     if (k == "test_wait_ms") {
         if (!(value >= 0.01 && value <= 2000)) return fail(ctx, BEM_ERR_ARG, "test_wait_ms must be in [0.01, 2000]");
         ctx->test_wait_ns = (unsigned long long)(value * 1e6);
+        return BEM_OK;
+    }
+    if (k == "refine_graph") {
+        if (!(value == 0 || value == 1)) return fail(ctx, BEM_ERR_ARG, "refine_graph must be 0 or 1");
+        ctx->refine_graph = (int)value;
         return BEM_OK;
     }
     if (k == "refine_gmres") {

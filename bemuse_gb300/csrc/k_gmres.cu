@@ -118,4 +118,53 @@ void launch_f32_to_f64(cudaStream_t st, size_t n, const float* src, double* dst)
     BEM_LAUNCH(k_f32_to_f64<<<1024, 256, 0, st>>>(n, src, dst));
 }
 
+// The convergence test of one classic refinement sweep, on the device: the decision the
+// host loop of factor_and_solve makes after reading the sweep's residual norms, so that
+// the sweeps can repeat inside a graph (a conditional while node on handle h) without a
+// round trip to the host.  One thread; the loop continues while it sets h to 1.
+__global__ void k_refine_step(int R, const unsigned long long* __restrict__ nrm, const int* __restrict__ flags,
+                              double tol, int max_iter, int coarse_first, int gmres_switch, RefineState* st,
+                              cudaGraphConditionalHandle h) {
+    RefineState v = *st;
+    v.iters += 1;
+    v.flags = *flags;
+    unsigned int go = 0;
+    if (v.flags & FLAG_TIMEOUT) {
+        v.status = REFINE_TIMEOUT;
+    } else {
+        double resid = 0.0;
+        for (int j = 0; j < R; ++j) {
+            const double rn = __longlong_as_double((long long)nrm[j]);
+            const double yn = __longlong_as_double((long long)nrm[R + j]);
+            const double rel = yn > 0 ? rn / yn : rn;
+            if (resid < rel) resid = rel;
+        }
+        v.resid = resid;
+        // the coarse first residual (high words of Re D only) never certifies convergence
+        const bool full = !(v.iters == 1 && coarse_first);
+        if (full) {
+            if (v.prev_full > 0.0) v.contraction = resid / v.prev_full;
+            v.prev_full = resid;
+        }
+        if (resid <= tol && full) {
+            v.status = REFINE_CONVERGED;
+        } else if (v.iters >= max_iter || !(resid < 1e300)) {
+            v.status = REFINE_FAILED;
+        } else if (gmres_switch && v.iters >= 2 && resid > 0.05 * v.prev) {
+            v.status = REFINE_STALLED;  // a sweep that gained less than 20x: flexible GMRES takes over
+        } else {
+            v.prev = resid;
+            go = 1;
+        }
+    }
+    *st = v;
+    cudaGraphSetConditional(h, go);
+}
+
+void launch_refine_step(cudaStream_t st, int R, const unsigned long long* nrm, const int* flags, double tol,
+                        int max_iter, int coarse_first, int gmres_switch, RefineState* state,
+                        cudaGraphConditionalHandle h) {
+    BEM_LAUNCH(k_refine_step<<<1, 1, 0, st>>>(R, nrm, flags, tol, max_iter, coarse_first, gmres_switch, state, h));
+}
+
 }  // namespace bem

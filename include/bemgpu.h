@@ -314,6 +314,12 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     Re D (about 1e-7 relative), the later ones in double-float; the sweep
  *                     count stays the same at such contraction, and convergence is only
  *                     accepted on a double-float residual.  0: every residual double-float.
+ *   "refine_graph"    1: the classic sweeps of each frequency repeat inside a CUDA graph
+ *                     (a conditional while node) and their convergence test runs on the
+ *                     device, with the same decisions as the host loop (the same sweeps,
+ *                     the switch to GMRES, the same failures); 0 (default): the host reads
+ *                     each sweep's residual norms.  A solve enqueued while its stream is
+ *                     being captured into a graph always tests on the device.
  *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation,
  *                     2 (default): the same with the next panel's pivot block inverted
  *                     by a dedicated warp beside each rank-8 update, 0: one pivot per

@@ -74,12 +74,15 @@ def test_non_finite_frequency_is_rejected(bg, orc, bad):
     assert normwise(got["A"][0], ref["A"][0]) < 1e-6
 
 
+@pytest.mark.parametrize("graph", [0, 1])
 @pytest.mark.parametrize("omegas", [[0.8], [0.8, 1.0, 1.3, 1.7]])
-def test_refinement_out_of_solves_is_numeric_failure(bg, orc, omegas):
+def test_refinement_out_of_solves_is_numeric_failure(bg, orc, omegas, graph):
     # with several frequencies the failure comes while the next frequency's LU and the
-    # one after's assembly are in flight on their own streams
+    # one after's assembly are in flight on their own streams; graph = 1: the convergence
+    # test runs on the device (refine_graph) and reports the same failure
     s = _solver(bg, bg.MIXED)
     s.Setup(cases.lib_cylinder(cases.CYL_SMALL))
+    s.set_tuning("refine_graph", graph)
     s.set_tuning("refine_max_solves", 0)
     with pytest.raises(bg.BEMError) as ex:
         s.solve_omegas(omegas)
@@ -95,8 +98,8 @@ def test_refinement_out_of_solves_is_numeric_failure(bg, orc, omegas):
         s.set_tuning("refine_max_solves", -1)
 
 
-@pytest.mark.parametrize("gmres", [0, 1])
-def test_expired_device_wait_is_reported_and_context_survives(bg, orc, gmres):
+@pytest.mark.parametrize("gmres,graph", [(0, 0), (1, 0), (0, 1)])
+def test_expired_device_wait_is_reported_and_context_survives(bg, orc, gmres, graph):
     # Every wait of the triangular-solve chain asks for a flag value nothing publishes;
     # each gives up 1 ms after its CTA starts, sets FLAG_TIMEOUT and the chain finishes
     # (all accesses stay in bounds, the results are garbage).  The host must report
@@ -106,6 +109,7 @@ def test_expired_device_wait_is_reported_and_context_survives(bg, orc, gmres):
     s.Setup(cases.lib_cylinder(cases.CYL_MED))
     assert s.N == 288
     s.set_tuning("refine_gmres", gmres)
+    s.set_tuning("refine_graph", graph)
     s.set_tuning("test_wait_ms", 1.0)
     s.set_tuning("test_wait_skew", 1)
     with pytest.raises(bg.BEMError) as ex:
@@ -124,7 +128,7 @@ def test_expired_device_wait_is_reported_and_context_survives(bg, orc, gmres):
 
 def test_bad_tuning_values_are_rejected(bg):
     s = _solver(bg, bg.MIXED)
-    for key, val in (("test_wait_skew", 2), ("test_wait_ms", 0.0), ("no_such_key", 1)):
+    for key, val in (("test_wait_skew", 2), ("test_wait_ms", 0.0), ("refine_graph", 2), ("no_such_key", 1)):
         with pytest.raises(bg.BEMError) as ex:
             s.set_tuning(key, val)
         assert _status(ex) == BEM_ERR_ARG

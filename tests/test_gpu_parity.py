@@ -143,6 +143,31 @@ def test_refinement_variants_agree_near_irregular_frequency(bg, orc):
     assert np.all(got[2]["iters"] <= got[0]["iters"] + 1)
 
 
+def test_device_side_refinement_matches_host_loop(bg, orc):
+    """The classic refinement with its convergence test on the device (refine_graph = 1: a
+    conditional while node of a CUDA graph repeats the sweeps, k_refine_step decides) makes
+    the decisions of the host loop: the same sweeps, the switch to GMRES near the irregular
+    frequency of the 144-panel cylinder (Omega ~ 1.54), the coarse first residual, the
+    same results; with one LU in flight and with two beside the refinement."""
+    m, aux = cases.oracle_cylinder(orc, cases.CYL_SMALL)
+    om = np.array([0.5, 1.0, 1.50, 1.54, 1.58, 2.2])
+    got = {}
+    for lo in (0, 2):
+        for g in (0, 1):
+            s = _solver(bg, cases.lib_cylinder(cases.CYL_SMALL), precision=bg.MIXED)
+            s.set_tuning("lu_overlap", lo)
+            s.set_tuning("refine_graph", g)
+            got[lo, g] = s.solve_omegas(om)
+            print("lu_overlap", lo, "refine_graph", g, "sweeps", got[lo, g]["iters"])
+            assert np.all(got[lo, g]["residual"] <= 1e-12)
+    ref = _oracle_solve(orc, m, aux, om, cases.BETAS, s)
+    _compare(got[2, 1], ref, 1e-6)
+    for lo in (0, 2):
+        assert np.array_equal(got[lo, 0]["iters"], got[lo, 1]["iters"]), lo
+        for k in ("A", "B", "F"):
+            assert max(normwise(got[lo, 1][k][f], got[lo, 0][k][f]) for f in range(om.size)) < 1e-11, (lo, k)
+
+
 def test_coarse_first_residual_keeps_the_sweeps(bg, orc):
     # The first sweep's residual from the FP32 high words of Re D (refine_coarse_first = 1,
     # the default, used after a solve that contracted by less than 3e-4 per sweep) against
