@@ -16,7 +16,8 @@ split and the number of LUs in flight before the warm-up, outside the timed regi
   value         = freq-solves/s from device time (CUDA events on the library stream)
   e2e           = freq-solves/s of wall time around bem_solve (host in, host out)
   roofline      = the wave-assembly kernel on its FP32 bound (345 FP operations per
-                  Green-function evaluation against a measured FMA rate), with the HBM view
+                  Green-function evaluation against a measured FMA rate), with the HBM view;
+                  roofline.alone: the same kernel on the whole GPU (one frequency alone)
   lu_roofline   = the tensor-core LU against a measured cuBLAS TF32 rate
   cpu_baseline  = one unscaled frequency-solve of the same array by the oracle port on the
                   host cores (setup excluded); the same solve pins accuracy_vs_oracle
@@ -500,10 +501,13 @@ def main():
     KEYS = ("A", "B", "F", "FK", "SC")
     results = [{k: res[k][i:i + 1] for k in KEYS} for i in range(len(timed))]
     iters = [int(x) for x in res["iters"]]
-    # LU alone (one frequency, nothing overlapping) for the tensor-core roofline
+    # LU and assembly alone (one frequency, nothing overlapping: the tensor-core roofline,
+    # and k_wave_mixed on the whole GPU beside the pipelined figure)
     s.stage_times(reset=True)
+    s.kernel_times(reset=True)
     s.solve_omegas([timed[-1]])
     lu_alone_ms = float(s.stage_times(reset=True)[2])
+    kt_alone = s.kernel_times(reset=True)
     # plain FP64 GPU path at frequencies spread over the timed ones (highest and lowest
     # first); the mixed results are compared with it
     pick = []
@@ -561,6 +565,12 @@ def main():
                     "peak_gbs": hbm_peak, "peak_source": "measured, MEASURED_PEAKS.json"}}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["hbm"]["frac"] = roof["hbm"]["achieved_gbs"] / hbm_peak
+    if kt_alone[1] > 0:
+        a_ms = float(kt_alone[0] / kt_alone[1])
+        a_tf = 345.0 * evals / (a_ms / 1000.0) / 1e12
+        roof["alone"] = {"avg_launch_ms": a_ms, "achieved": a_tf, "frac": a_tf / roof["peak"],
+                         "note": "one frequency solved alone after the timed steps: the assembly on the whole "
+                                 "GPU; the timed launches keep off the SMs reserved for the LUs and refinement"}
     if rank != 0:
         return
     honesty = {}
