@@ -16,8 +16,9 @@
 //       e^v is computed once; the reference recomputes the same value).
 // gf32: FP32.  The polynomials have coefficients up to 2e5 with alternating
 //       signs, which cancel badly in FP32 around rho ~ 0.5; gf32 evaluates
-//       each one re-expanded about rho = 1/2 (coefficients from host-side FP64
-//       expansion, held in constant memory), which is the same polynomial.
+//       each one re-expanded about rho = 1/2, which is the same polynomial; the
+//       coefficients are compile-time literals (BEM_P32_*), so they stay instruction
+//       operands rather than constant-memory loads.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -51,27 +52,36 @@ struct PolyCoef64 {
     double A[10], B[10], C[10], D[10], dA[10], dB[10], dC[10];
 };
 
-// Shifted-basis coefficients for FP32: p(rho) = sum_k s_k (rho - 1/2)^k.
-// h1s, h1d: the two forms of 2/pi - H1(x) that dG/dh needs (h1_gap32).
-struct PolyCoef32 {
-    float A[10], B[10], C[10], D[10], dA[10], dB[10], dC[10];
-    float h1s[7];  // x <= 3: 2/pi - (x/3)^2 P((x/3)^2) as a polynomial in t = x^2 - 9/2
-    float h1d[4];  // x > 3: (2/pi) c2 - c1 of Kernels.cpp:95-97 in (3/x)^2, leading terms cancelled
-};
+// Shifted-basis coefficients for FP32, ascending powers: p(rho) = sum_k s_k (rho - 1/2)^k,
+// s_j = sum_{i >= j} c_i C(i, j) 2^-(i-j) from BEM_POLY_TABLE's c_i, rounded to float.
+// BEM_P32_h1s, BEM_P32_h1d: the two forms of 2/pi - H1(x) that dG/dh needs (h1_gap32):
+//   h1s: x <= 3, 2/pi - yy P(yy) (yy = (x/3)^2, P the series of BEM_H1_SMALL) re-expanded
+//        about yy = 1/2 and rescaled to t = x^2 - 9/2 = 9 (yy - 1/2);
+//   h1d: x > 3, 2 (c2_i - c1_i) of BEM_H1_C1 / BEM_H1_C2, leading terms cancelled.
+// tests/test_poly32.py recomputes every value with rational arithmetic.
+#define BEM_P32_A 1.671640635e+00f, 1.321628094e+01f, 9.012850189e+01f, 2.129387512e+02f, -2.447474976e+02f, -1.760199951e+03f, -1.364880005e+03f, 2.295699951e+03f, 8.530000305e+01f, -4.838600098e+03f
+#define BEM_P32_B 3.298913956e+00f, -6.148437411e-02f, -3.370587540e+01f, 3.631500006e+00f, 3.526837463e+02f, 1.743025055e+02f, -2.153469971e+03f, -2.185919922e+03f, 5.490250000e+03f, 7.671220215e+03f
+#define BEM_P32_C 5.853843689e+00f, 8.096312523e+00f, -4.139637375e+01f, -1.528125000e+01f, 4.885824890e+02f, 3.835950012e+02f, -2.317770020e+03f, -3.272620117e+03f
+#define BEM_P32_D -6.455031395e+00f, -3.069187546e+01f, -2.602031326e+01f, 1.522068787e+02f, 3.372087402e+02f, 8.551174927e+02f, 4.813345215e+03f, 3.288969971e+03f, -2.368050000e+04f, -3.374460156e+04f
+#define BEM_P32_dA 8.678410530e+00f, 1.629613304e+01f, -6.745562744e+01f, -1.360637512e+02f, 6.027931519e+02f, 6.803062744e+02f, -4.320740234e+03f, -4.930879883e+03f, 1.011212500e+04f, 1.262225000e+04f
+#define BEM_P32_dB 8.081609726e+00f, 1.605587578e+01f, -6.992500305e+01f, -1.364287567e+02f, 6.629874878e+02f, 7.710250244e+02f, -5.211000000e+03f, -6.650500000e+03f, 1.344494043e+04f, 1.992327930e+04f
+#define BEM_P32_dC 1.052343750e+01f, 4.784062576e+01f, 1.346174927e+02f, 4.244499969e+01f, -8.073250122e+02f, -1.590270020e+03f
+#define BEM_P32_h1s -6.614897400e-02f, -1.072273552e-01f, 9.413545020e-03f, -3.010456858e-04f, 5.088115813e-06f, -5.358563371e-08f, 3.898513734e-10f
+#define BEM_P32_h1d -7.999999951e-08f, -2.222040147e-01f, -7.735215425e-01f, -3.313150704e-01f
+
+// Horner's rule on literal coefficients in ascending order: hornerc(u, c0, .., cn) =
+// c0 + u (c1 + u (... + u cn)), each step one FMA (the order of horner32).
+__device__ __forceinline__ float hornerc(float, float c0) { return c0; }
+template <typename... T>
+__device__ __forceinline__ float hornerc(float u, float c0, T... cs) {
+    return fmaf(hornerc(u, cs...), u, c0);
+}
 
 // The reference's StruveH1 constants (Kernels.cpp:76-116): small-argument series
 // coefficients and the large-argument rational c1 / c2.
 #define BEM_H1_SMALL 1.909859286, -1.145914713, 0.294656958, -0.042070508, 0.003785727, -0.000207183
 #define BEM_H1_C1 1.00000004, 3.92205313, 2.64893033, 0.27450895
 #define BEM_H1_C2 1.0, 3.81095112, 2.26216956, 0.10885141
-
-__device__ __forceinline__ float horner32(const float* s, int n, float u) {
-    float r = s[n - 1];
-#pragma unroll
-    for (int k = 8; k >= 0; --k)
-        if (k < n - 1) r = fmaf(r, u, s[k]);
-    return r;
-}
 
 // ---- FP64 -----------------------------------------------------------------
 __device__ __forceinline__ double struve_h0_64(double x, double y0x) {
@@ -164,16 +174,13 @@ __device__ __forceinline__ float struve_h0_32(float x, float y0x, float t3) {
 // about yy = 1/2 with t = x^2 - 9/2 formed by one FMA; for x > 3,
 // 2/pi - c1/c2 = ((2/pi) c2 - c1) / c2 with the numerator's coefficients
 // subtracted exactly on the host, so only Y1 is added to a small, accurate term.
-__device__ __forceinline__ float h1_gap32(const PolyCoef32& P, float x, float y1x, float t3) {
+__device__ __forceinline__ float h1_gap32(float x, float y1x, float t3) {
     if (x <= 3.0f) {
         const float t = fmaf(x, x, -4.5f);
-        float r = P.h1s[6];
-#pragma unroll
-        for (int k = 5; k >= 0; --k) r = fmaf(r, t, P.h1s[k]);
-        return r;
+        return hornerc(t, BEM_P32_h1s);
     }
     const float yy = t3 * t3;
-    const float num = fmaf(fmaf(fmaf(P.h1d[3], yy, P.h1d[2]), yy, P.h1d[1]), yy, P.h1d[0]);
+    const float num = hornerc(yy, BEM_P32_h1d);
     const float c2 = 3.14159265f * fmaf(fmaf(fmaf(0.10885141f, yy, 2.26216956f), yy, 3.81095112f), yy, 1.0f);
     return __fdividef(num, c2) - y1x;
 }
@@ -278,7 +285,7 @@ __device__ __forceinline__ void df_hdist(float dxh, float dxl, float dyh, float 
     hl = h2 - (hh - h);
 }
 
-__device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf& G, cf& Gh) {
+__device__ __forceinline__ void gf32(float hh, float vv, cf& G, cf& Gh) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
     float dd = sqrtf(fmaf(hh, hh, vv * vv));
@@ -294,8 +301,8 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float dmv = dd - vv;
     float PP = logf(0.5f * dmv) + EUL - 2.0f * d2;
     PP = fmaf(PP, ev, d2 - vv);
-    float A = horner32(P.A, 10, u), B = horner32(P.B, 10, u);
-    float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
+    float A = hornerc(u, BEM_P32_A), B = hornerc(u, BEM_P32_B);
+    float C = hornerc(u, BEM_P32_C), D = hornerc(u, BEM_P32_D);
     float omr = 1.0f - rho;
     float RR = (1.0f - beta) * A - beta * B;
     RR -= alpha * C / fmaf(6.0f * alpha * rho, omr, 1.0f);
@@ -307,7 +314,7 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     float j0v, j1v, y0v = 0.0f, y1v = 0.0f;
     if (far) bessel_large(hh, 0.0f, t3, j0v, j1v, y0v, y1v);
     else bessel_j01_small(hh, j0v, j1v);
-    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(P, hh, y1v, t3);
+    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(hh, y1v, t3);
     float E = 2.0f * PI * ev;
     G.re = fmaf(E, H0, L0);
     G.im = -E * j0v;
@@ -317,7 +324,7 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
     PS -= hh;
     float QS = expf(-dd) * (1.0f - beta);
     QS *= 1.0f + dd * inv_1d3;
-    float a2 = horner32(P.dA, 10, u), b2 = horner32(P.dB, 10, u), c2 = horner32(P.dC, 6, u);
+    float a2 = hornerc(u, BEM_P32_dA), b2 = hornerc(u, BEM_P32_dB), c2 = hornerc(u, BEM_P32_dC);
     float RS = beta * a2 - (1.0f - alpha) * b2;
     RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
     float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);
@@ -330,7 +337,7 @@ __device__ __forceinline__ void gf32(const PolyCoef32& P, float hh, float vv, cf
 // y0v, y1v: Y0(hh), Y1(hh), t3 = 3 / hh (used when hh > 3).
 // Gv: dG/dv ~ Gr - 2/d (to about 1 %: the infinite-depth wave term satisfies dG/dv = G
 // up to the Rankine image's 2/d), used for the first-order correction of the rounding of v.
-__device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv, float ev, float y0v, float y1v,
+__device__ __forceinline__ void gf32_re(float hh, float vv, float ev, float y0v, float y1v,
                                         float t3, float& Gr, float& Ghr, float& Gv) {
     const float PI = 3.14159265358979f;
     const float EUL = 0.5772156649f;
@@ -351,15 +358,15 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     float dmv = dd - vv;
     float PP = __logf(0.5f * dmv) + EUL - 2.0f * d2;  // fast log: ~4e-7 absolute, scaled by e^v / (1 + d^3)
     PP = fmaf(PP, ev, d2 - vv);
-    float A = horner32(P.A, 10, u), B = horner32(P.B, 10, u);
-    float C = horner32(P.C, 8, u), D = horner32(P.D, 10, u);
+    float A = hornerc(u, BEM_P32_A), B = hornerc(u, BEM_P32_B);
+    float C = hornerc(u, BEM_P32_C), D = hornerc(u, BEM_P32_D);
     float omr = 1.0f - rho;
     float RR = (1.0f - beta) * A - beta * B;
     RR -= __fdividef(alpha * C, fmaf(6.0f * alpha * rho, omr, 1.0f));
     RR = fmaf(beta * (1.0f - beta), D, RR);
     float r3 = rho * (omr * omr * omr);
     float L0 = 2.0f * PP * inv_1d3 + 2.0f * (r3 * RR);
-    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(P, hh, y1v, t3);
+    float H0 = struve_h0_32(hh, y0v, t3), H1g = h1_gap32(hh, y1v, t3);
     float E = 2.0f * PI * ev;
     Gr = fmaf(E, H0, L0);
     Gv = fmaf(-2.0f, inv_d, Gr);
@@ -371,7 +378,7 @@ __device__ __forceinline__ void gf32_re(const PolyCoef32& P, float hh, float vv,
     // other terms at every d
     float QS = __expf(-dd) * (1.0f - beta);
     QS *= 1.0f + dd * inv_1d3;
-    float a2 = horner32(P.dA, 10, u), b2 = horner32(P.dB, 10, u), c2 = horner32(P.dC, 6, u);
+    float a2 = hornerc(u, BEM_P32_dA), b2 = hornerc(u, BEM_P32_dB), c2 = hornerc(u, BEM_P32_dC);
     float RS = beta * a2 - (1.0f - alpha) * b2;
     RS = fmaf(beta * (1.0f - beta) * rho * (1.0f - 2.0f * rho), c2, RS);
     float Ls = 2.0f * PS * inv_1d3 - 4.0f * QS + 2.0f * (r3 * RS);

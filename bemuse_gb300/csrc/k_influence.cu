@@ -23,7 +23,6 @@
 namespace bem {
 
 __constant__ PolyCoef64 c_poly64;
-__constant__ PolyCoef32 c_poly32;
 
 static const double kFourPIinv = 0.25 / 3.14159265358979323846;
 
@@ -136,7 +135,7 @@ template <> struct WaveMath<double> {
 };
 template <> struct WaveMath<float> {
     typedef cf C;
-    static __device__ __forceinline__ void gf(float h, float v, cf& G, cf& Gh) { gf32(c_poly32, h, v, G, Gh); }
+    static __device__ __forceinline__ void gf(float h, float v, cf& G, cf& Gh) { gf32(h, v, G, Gh); }
 };
 
 // Influence (ws, wd) of mirrored wave panel s at receiver point (xr, yr, zr).
@@ -290,7 +289,7 @@ __device__ __forceinline__ void gauss_G32(const GaussGeo& o, float& Gr, float& G
     if (o.hh > 3.0f) bessel_large(o.hh, o.hl, t3, j0v, j1v, y0v, y1v);
     else bessel_j01_small(o.hh, j0v, j1v);
     float Gv;
-    gf32_re(c_poly32, o.hh, o.VV, ev, y0v, y1v, t3, Gr, Ghr, Gv);
+    gf32_re(o.hh, o.VV, ev, y0v, y1v, t3, Gr, Ghr, Gv);
     // G at the unrounded (h, v): the first-order terms of the float pairs' low parts.
     // The radiation damping is a small difference of terms that each carry this
     // rounding, so without it B loses ~1e-6 at the highest frequencies.
@@ -1111,53 +1110,21 @@ double ffma_peak_tflops(int device) {
 cudaError_t upload_poly_constants(int device) {
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
     if (g_poly_ready[device]) return cudaSuccess;
+    // the FP64 monomial coefficients of the reference (the FP32 path uses the shifted
+    // literals BEM_P32_* compiled into its kernels)
     PolyCoef64 p64;
-    PolyCoef32 p32;
     memset(&p64, 0, sizeof(p64));
-    memset(&p32, 0, sizeof(p32));
     double* dst64[7] = {p64.A, p64.B, p64.C, p64.D, p64.dA, p64.dB, p64.dC};
-    float* dst32[7] = {p32.A, p32.B, p32.C, p32.D, p32.dA, p32.dB, p32.dC};
     int k = 0;
-#define BEM_FILL(name, n, ...)                                            \
-    {                                                                      \
-        const double c[] = {__VA_ARGS__};                                  \
-        for (int i = 0; i < n; ++i) dst64[k][i] = c[i];                    \
-        /* re-expand about rho = 1/2: s_j = sum_i c_i C(i,j) 2^-(i-j) */   \
-        for (int j = 0; j < n; ++j) {                                      \
-            long double s = 0;                                             \
-            for (int i = j; i < n; ++i) {                                  \
-                long double bin = 1;                                       \
-                for (int t = 0; t < j; ++t) bin = bin * (i - t) / (t + 1); \
-                s += (long double)c[i] * bin * powl(0.5L, i - j);          \
-            }                                                              \
-            dst32[k][j] = (float)s;                                        \
-        }                                                                  \
-        ++k;                                                               \
+#define BEM_FILL(name, n, ...)                         \
+    {                                                   \
+        const double c[] = {__VA_ARGS__};               \
+        for (int i = 0; i < n; ++i) dst64[k][i] = c[i]; \
+        ++k;                                            \
     }
     BEM_POLY_TABLE(BEM_FILL)
 #undef BEM_FILL
-    {
-        // 2/pi - H1 (h1_gap32): x <= 3, q(yy) = 2/pi - yy P(yy) re-expanded about yy = 1/2 and
-        // rescaled to t = x^2 - 9/2 = 9 (yy - 1/2); x > 3, (2/pi) c2 - c1 coefficient by coefficient
-        const double hs[6] = {BEM_H1_SMALL}, c1[4] = {BEM_H1_C1}, c2[4] = {BEM_H1_C2};
-        long double q[7];
-        q[0] = 2.0L / 3.14159265358979323846L;
-        for (int i = 0; i < 6; ++i) q[i + 1] = -(long double)hs[i];
-        for (int j = 0; j < 7; ++j) {
-            long double a = 0;
-            for (int i = j; i < 7; ++i) {
-                long double bin = 1;
-                for (int t = 0; t < j; ++t) bin = bin * (i - t) / (t + 1);
-                a += q[i] * bin * powl(0.5L, i - j);
-            }
-            p32.h1s[j] = (float)(a / powl(9.0L, j));
-        }
-        for (int i = 0; i < 4; ++i)
-            p32.h1d[i] = (float)(2.0L * ((long double)c2[i] - (long double)c1[i]));
-    }
-    cudaError_t e = cudaMemcpyToSymbol(c_poly64, &p64, sizeof(p64));
-    if (e != cudaSuccess) return e;
-    e = cudaMemcpyToSymbol(c_poly32, &p32, sizeof(p32));
+    const cudaError_t e = cudaMemcpyToSymbol(c_poly64, &p64, sizeof(p64));
     if (e == cudaSuccess) g_poly_ready[device] = true;
     return e;
 }
