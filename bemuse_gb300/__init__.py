@@ -136,6 +136,7 @@ def lib():
         "bem_aero_surface": ([vp, _dp, _dp, c_double, _dp, _dp], c_int),
         "bem_mesh_wing_wake": ([c_double, c_double, c_int, c_int, c_double, _dp, _ip, _ip], c_int),
         "bem_fp32_peak": ([c_int, _dp], c_int),
+        "bem_cusolver_zgetrf_ms": ([c_int, c_int, _dp], c_int),
         "bem_set_surrogate": ([vp, vp, c_int, c_double, c_double, _dp], c_int),
         "bem_surrogate_stats": ([vp, _dp, c_int], c_int),
         "bem_tc_probe": ([c_int, c_int, c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp], c_int),
@@ -894,6 +895,14 @@ def fp32_peak(device=0):
     """Measured FP32 FMA throughput of the device in TFLOP/s (bem_fp32_peak)."""
     t = ctypes.c_double()
     _check(lib().bem_fp32_peak(int(device), ctypes.byref(t)))
+    return t.value
+
+
+def cusolver_zgetrf_ms(n, device=0):
+    """Device time in ms of cuSOLVER's complex LU with partial pivoting at order n
+    (bem_cusolver_zgetrf_ms): the library figure beside the plain FP64 path's LU."""
+    t = ctypes.c_double()
+    _check(lib().bem_cusolver_zgetrf_ms(int(device), int(n), ctypes.byref(t)))
     return t.value
 
 

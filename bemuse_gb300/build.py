@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(OUT_DIR, "libbemgpu.so")
 
-SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "host_batch.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "k_gmres.cu", "noalloc.cu", "k_mlp.cu", "k_mlp_tc.cu", "k_lu_piv.cu"]
+SOURCES = ["host_api.cpp", "host_mesh.cpp", "host_io.cpp", "host_batch.cpp", "k_influence.cu", "k_lu.cu", "k_tc_gemm.cu", "k_gmres.cu", "noalloc.cu", "k_mlp.cu", "k_mlp_tc.cu", "k_lu_piv.cu", "host_cusolver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -59,7 +59,7 @@ def build(verbose=False, force=False):
             if log:
                 sys.stderr.write(log)
     objs = [o for o, _ in results]
-    cmd = [nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-lpthread"]
+    cmd = [nvcc(), "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -240,31 +240,6 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line))
 
 
-def cusolver_zgetrf_ms(n, device):
-    """cuSOLVER's complex LU (zgetrf, partial pivoting) at order n through torch, timed
-    with CUDA events after a warm-up: the library figure beside the plain FP64 path's
-    own LU, so that the plain path is not a strawman denominator."""
-    import torch
-    torch.backends.cuda.preferred_linalg_library("cusolver")
-    dev = torch.device("cuda", device)
-    g = torch.Generator(device=dev).manual_seed(0)
-    A = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g) * (0.2 / n ** 0.5)
-    A.diagonal().add_(0.5)
-    torch.linalg.lu_factor(A)
-    torch.cuda.synchronize(dev)
-    best = float("inf")
-    for _ in range(2):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.linalg.lu_factor(A)
-        e1.record()
-        torch.cuda.synchronize(dev)
-        best = min(best, e0.elapsed_time(e1))
-    del A
-    torch.cuda.empty_cache()
-    return best
-
-
 def tf32_peak_tflops(device, n=8192):
     """cuBLAS TF32 GEMM throughput (torch.matmul on FP32 with TF32 allowed, n^3, best
     of 5 with CUDA events): the roofline denominator of the tensor-core LU."""
@@ -576,7 +551,7 @@ def main():
     honesty = {}
     try:
         honesty["tf32_peak_tflops"] = tf32_peak_tflops(local)
-        honesty["cusolver_zgetrf_ms"] = cusolver_zgetrf_ms(N, local)
+        honesty["cusolver_zgetrf_ms"] = bg.cusolver_zgetrf_ms(Np, local)
     except Exception as exc:  # torch or cuSOLVER unavailable: report why
         honesty["unavailable"] = str(exc)[:200]
     F_lu = 8.0 / 3.0 * float(Np) ** 3

@@ -559,6 +559,13 @@ bem_status bem_tc_probe(int device, int mode, int n, float* C, const float* Wa, 
  * assembly.  No reference counterpart. */
 bem_status bem_fp32_peak(int device, double* tflops);
 
+/* Device time (ms, CUDA events, best of two after a warm-up) of cuSOLVER's complex LU
+ * with partial pivoting (cusolverDnZgetrf) of a dense n x n complex matrix (seeded,
+ * entries of size 0.2 / sqrt(n) plus 0.5 on the diagonal): the library figure beside the
+ * plain FP64 path's own LU.  Measurement only; cuSOLVER is opened at run time and its
+ * absence returns BEM_ERR_UNSUPPORTED.  No reference counterpart. */
+bem_status bem_cusolver_zgetrf_ms(int device, int n, double* ms);
+
 /* Library version string. */
 const char* bem_version(void);
 

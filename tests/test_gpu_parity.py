@@ -391,3 +391,12 @@ def test_batch_solve_many_concurrent_contexts(bg):
         ref = s.solve_omegas(om)
         for k in ("A", "B", "F"):
             assert normwise(o[k], ref[k]) < 1e-9, k
+
+
+def test_cusolver_reference_lu_runs(bg):
+    """bem_cusolver_zgetrf_ms (measurement only: cuSOLVER's partial-pivot complex LU,
+    opened at run time) returns a positive device time, growing with the order."""
+    t1 = bg.cusolver_zgetrf_ms(512)
+    t2 = bg.cusolver_zgetrf_ms(2048)
+    print("cusolver zgetrf ms", t1, t2)
+    assert 0.0 < t1 < t2
