@@ -67,9 +67,6 @@ struct FreqState {
     float *wl32 = nullptr, *wut32 = nullptr, *pairT = nullptr;
     cudaEvent_t ev_lu0 = nullptr, ev_lu = nullptr;   // LU start / done (stream st)
     cudaEvent_t ev_sv0 = nullptr, ev_sv1 = nullptr;  // solves start / done
-    // device-side refinement state of the frequency this slot holds (null: the context's
-    // first state); a solve captured into one graph gives each frequency its own
-    bem::RefineState* rstate = nullptr;
 };
 
 // One captured tensor-core LU (per frequency slot) and what it was captured for.
@@ -125,15 +122,12 @@ struct bem_ctx {
     int refine_gmres = 2;  // 0 classic refinement, 1 flexible GMRES, 2 classic switching to GMRES
     int refine_coarse_first = 1;  // 1: the first classic sweep's residual from the FP32 high words
     int refine_max = 60;          // preconditioner solves the refinement may use before it fails
-    // classic refinement with its convergence test on the device, the sweeps repeating in a
-    // conditional while node of a graph (always inside a solve captured into a graph;
-    // refine_graph = 1 also for the stream-driven solves); the states (RSTATE_CAP, one per
-    // frequency of a captured solve), the stream the loop body is captured on, and the
-    // launches of one captured sweep
+    // refine_graph = 1: classic refinement with its convergence test on the device, the
+    // sweeps repeating in a conditional while node of a graph; its device state and the
+    // stream the loop body is captured on
     int refine_graph = 0;
     bem::RefineState* d_rstate = nullptr;
     cudaStream_t sbody = nullptr;
-    long long rg_body_launches = 0;
     // surrogate form of the mixed assembly (bem_set_surrogate): the network, the mode (0 off,
     // 1 strict: a frequency whose judged error exceeds sur_tol is solved again with the closed
     // form, 2 accept), the judged fraction of far pairs and the domain {KR min, KR max, KZ min,
@@ -407,7 +401,6 @@ bool inv6(const cplx* M, cplx* out) {
 }
 
 constexpr int GM_M = 16;  // restart length of the flexible GMRES refinement
-constexpr int RSTATE_CAP = 1024;  // device refinement states per context
 
 bem_status ensure_lu_buffers(bem_ctx* ctx, int Np, int R, bool mixed) {
     const int nb64 = 64, nb32 = 128;
@@ -825,15 +818,13 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
             }
             return gs;
         };
-        // Classic refinement with its convergence test on the device: the first sweep, then a
-        // conditional while node whose body is one sweep; k_refine_step, at the end of each,
-        // decides as the host loop below does and ends the loop.  Inside a caller's capture
-        // (a whole solve captured into one graph) the loop becomes part of that graph and its
-        // outcome stays in the slot's state for the caller to read; otherwise it is captured
-        // for this frequency alone (K, the plane-wave count and the slot's buffers are baked
-        // in), launched, and its outcome handled here.
-        auto refine_on_device = [&](bool outer) -> bem_status {
-            bem::RefineState* rs = F.rstate ? F.rstate : ctx->d_rstate;
+        // Classic refinement with its convergence test on the device (refine_graph): the first
+        // sweep, then a conditional while node whose body is one sweep; k_refine_step, at the
+        // end of each, decides as the host loop below does and ends the loop.  Captured for
+        // this frequency (K, the plane-wave count and the slot's buffers are baked in),
+        // launched, and its outcome read back and handled here.
+        auto refine_on_device = [&]() -> bem_status {
+            bem::RefineState* rs = ctx->d_rstate;
             const int ep = (ctx->solve_epoch += 2) - 1;
             const size_t ready_bytes = sizeof(int) * ((size_t)Np / 8 + 32);
             cudaGraphConditionalHandle h = 0;
@@ -857,7 +848,7 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 return BEM_OK;
             };
             const cudaStream_t st0 = st;
-            if (!outer) CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
             unsigned long long lb = 0;
             cudaGraph_t loop_body = nullptr;
             const bem_status cs = [&]() -> bem_status {
@@ -895,8 +886,6 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                 return BEM_OK;
             }();
             st = st0;
-            ctx->rg_body_launches = (long long)lb;
-            if (outer) return cs;
             cudaGraph_t graph = nullptr;
             const cudaError_t ee = cudaStreamEndCapture(st, &graph);
             if (cs != BEM_OK) {
@@ -946,23 +935,12 @@ bem_status factor_and_solve(bem_ctx* ctx, FreqState& F, int N, int Np, int R, bo
                     return fail(ctx, BEM_ERR_CUDA, "the refinement graph ended without an outcome");
             }
         };
-        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-        CK(cudaStreamIsCapturing(st, &cap));
-        const bool outer = cap != cudaStreamCaptureStatusNone;
-        if (outer && ctx->refine_gmres == 1)
-            return fail(ctx, BEM_ERR_STATE, "a solve captured into a graph needs the classic refinement");
         if (ctx->refine_gmres == 1) {
             const bem_status gs = gmres();
             if (gs != BEM_OK) return gs;
-        } else if (outer || ctx->refine_graph) {
-            const bem_status gs = refine_on_device(outer);
+        } else if (ctx->refine_graph) {
+            const bem_status gs = refine_on_device();
             if (gs != BEM_OK) return gs;
-            if (outer) {
-                // the outcome and the flags are read after the caller's graph has run
-                CK(cudaEventRecord(ctx->ev[4], st));
-                CK(cudaEventRecord(F.ev_sv1, st));
-                return BEM_OK;
-            }
         } else {
             // classic refinement: x <- x + M^-1 (y - D x).  With refine_gmres = 2 a sweep
             // that reduces the residual by less than 20x (a nearly singular system, e.g. a
@@ -1159,7 +1137,7 @@ bem_status bem_create(bem_ctx** out, int device) {
     CK(cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     CK(cudaStreamCreateWithPriority(&ctx->st3, cudaStreamNonBlocking, std::max(prio_hi, prio_lo - 1)));
     CK(cudaStreamCreateWithFlags(&ctx->sbody, cudaStreamNonBlocking));
-    CK(cudaMalloc(&ctx->d_rstate, sizeof(bem::RefineState) * RSTATE_CAP));
+    CK(cudaMalloc(&ctx->d_rstate, sizeof(bem::RefineState)));
     for (FreqState& F : ctx->fs) {
         for (cudaEvent_t* e : {&F.ev_lu0, &F.ev_lu, &F.ev_sv0, &F.ev_sv1}) CK(cudaEventCreate(e));
         CK(cudaEventCreateWithFlags(&F.ev_asm, cudaEventDisableTiming));

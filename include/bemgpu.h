@@ -318,8 +318,8 @@ bem_status bem_kernel_times(bem_ctx* ctx, double* out4, int reset);
  *                     (a conditional while node) and their convergence test runs on the
  *                     device, with the same decisions as the host loop (the same sweeps,
  *                     the switch to GMRES, the same failures); 0 (default): the host reads
- *                     each sweep's residual norms.  A solve enqueued while its stream is
- *                     being captured into a graph always tests on the device.
+ *                     each sweep's residual norms (faster inside the frequency pipeline,
+ *                     where the loop's kernels would lose the refinement's stream priority).
  *   "lu_block_inverse" 1: the cluster inverse eliminates 8 pivots per synchronisation,
  *                     2 (default): the same with the next panel's pivot block inverted
  *                     by a dedicated warp beside each rank-8 update, 0: one pivot per
