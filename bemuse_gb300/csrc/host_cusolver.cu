@@ -64,6 +64,8 @@ extern "C" bem_status bem_cusolver_zgetrf_ms(int device, int n, double* ms) {
         dlclose(lib);
         return cs_fail(BEM_ERR_UNSUPPORTED, "libcusolver lacks the zgetrf entry points");
     }
+    int prev_device = 0;
+    cudaGetDevice(&prev_device);
     bem_status st = BEM_OK;
     std::string why;
     cudaStream_t s = nullptr;
@@ -123,6 +125,7 @@ extern "C" bem_status bem_cusolver_zgetrf_ms(int device, int n, double* ms) {
     if (e1) cudaEventDestroy(e1);
     if (s) cudaStreamDestroy(s);
     dlclose(lib);
+    cudaSetDevice(prev_device);  // the caller's current device is left as it was
     if (st != BEM_OK) return cs_fail(st, why);
     *ms = (double)best;
     return BEM_OK;
