@@ -134,6 +134,9 @@ void launch_pad_identity(cudaStream_t st, int N, int ld, double* D64r, double* D
 void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas, double K, double Omega,
                      const double* cen, const double* nrm, const double* area, double* phiI, double* dphiI,
                      double* Bm);
+// Blocks of the hull integrations (launch_post); their partial sums need
+// 2 * post_blocks(N) * (36 + 12 NB) doubles.
+int post_blocks(int N);
 void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
                  const double* phiI, const double* dphiI, double* part, double* out);
 void launch_havelock(cudaStream_t st, int n, const double* x, const double* y, const double* v, double* out,

@@ -1363,7 +1363,7 @@ bem_status bem_setup(bem_ctx* ctx, const bem_mesh* mesh, const bem_body_props* p
     DA(ctx->d_Ys6, 2 * (size_t)N * R);
     DA(ctx->fs[0].phiI, 2 * (size_t)N * std::max(NB, 1));
     DA(ctx->fs[0].dphiI, 2 * (size_t)N * std::max(NB, 1));
-    DA(ctx->d_part, 2 * (size_t)((N + 255) / 256) * (36 + 12 * NB));
+    DA(ctx->d_part, 2 * (size_t)bem::post_blocks(N) * (36 + 12 * NB));
     DA(ctx->d_post, 2 * (size_t)(36 + 12 * NB));
     DA(ctx->d_xr32, xr32.size());
     DA(ctx->d_gq32, gq32.size());

@@ -857,17 +857,20 @@ __global__ void k_incident(int N, int NB, int R, const double* __restrict__ beta
 
 // ---------------------------------------------------------------------------
 // Hull integrations (Hydrodynamic_Solver.cpp:462-476).  X = solution (N x R,
-// interleaved complex; columns 0..5 = Phi_J).  Outputs per CTA partial sums of
+// interleaved complex; columns 0..5 = Phi_J).  Outputs per CTA (POST_PANELS panels, so
+// each thread's FP64 sum is a short dependent chain) partial sums of
 //   AM[i][j]  = sum_p Nk[p][i] A_p X[p][j]          (36 complex)
 //   F1[i][b]  = sum_p Nk[p][i] A_p PhiI[p][b]       (6 NB complex)
 //   F2[i][b]  = sum_p X[p][i] dPhiI[p][b] A_p       (6 NB complex)
+constexpr int POST_PANELS = 32;
+
 __global__ void __launch_bounds__(256) k_post_partial(int N, int NB, int R, const double* __restrict__ X,
                                                       const double* __restrict__ Nk, const double* __restrict__ area,
                                                       const double* __restrict__ phiI,
                                                       const double* __restrict__ dphiI, double* __restrict__ part) {
     const int nout = 36 + 12 * NB;
-    const int p0 = blockIdx.x * 256;
-    const int pend = min(N, p0 + 256);
+    const int p0 = blockIdx.x * POST_PANELS;
+    const int pend = min(N, p0 + POST_PANELS);
     for (int t = threadIdx.x; t < nout; t += blockDim.x) {
         double sr = 0, si = 0;
         if (t < 36) {
@@ -1215,9 +1218,11 @@ void launch_incident(cudaStream_t st, int N, int NB, int R, const double* betas,
     BEM_LAUNCH(k_incident<<<(N + 127) / 128, 128, 0, st>>>(N, NB, R, betas, K, Omega, cen, nrm, area, phiI, dphiI, Bm));
 }
 
+int post_blocks(int N) { return (N + POST_PANELS - 1) / POST_PANELS; }
+
 void launch_post(cudaStream_t st, int N, int NB, int R, const double* X, const double* Nk, const double* area,
                  const double* phiI, const double* dphiI, double* part, double* out) {
-    int nblk = (N + 255) / 256;
+    int nblk = post_blocks(N);
     int nout = 36 + 12 * NB;
     BEM_LAUNCH(k_post_partial<<<nblk, 256, 0, st>>>(N, NB, R, X, Nk, area, phiI, dphiI, part));
     BEM_LAUNCH(k_post_reduce<<<(nout + 127) / 128, 128, 0, st>>>(nblk, nout, part, out));
